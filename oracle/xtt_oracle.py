@@ -1,0 +1,923 @@
+"""CPU restatement of the xerus Tensor-Train sweep path, used ONLY as a checker.
+
+This module is test infrastructure. It is imported by ``tests/``, by
+``__graft_entry__.smoke()`` and by the ``cpu_baseline`` / ``--impl reference``
+legs of ``bench.py`` - never by the product package ``xerus_gb300``.
+
+It restates, in FP64 numpy/scipy on top of LAPACK, the reference's algorithms:
+
+* RNG streams: ``std::mt19937_64``, libstdc++'s ``normal_distribution`` (Marsaglia
+  polar method with one cached variate), ``uniform_int_distribution`` (Lemire's
+  nearly-divisionless reduction on a 128-bit product) and
+  ``uniform_real_distribution`` (``generate_canonical``), as used by
+  ``src/xerus/misc/random.cpp:29-30``, ``include/xerus/tensor.h:213-220`` and
+  ``src/xerus/measurments.cpp:222-248``.
+* ``TTNetwork::random`` (``include/xerus/ttNetwork.h:128-155``),
+  ``reduce_to_maximal_ranks`` (``src/xerus/ttNetwork.cpp:369-402``).
+* ``move_core`` / ``transfer_core`` (``src/xerus/ttNetwork.cpp:581-628``,
+  ``src/xerus/tensorNetwork.cpp:821-909``) with the QC/CQ rank rule of
+  ``src/xerus/blasLapackWrapper.cpp:243-371`` (first k with
+  ``|R[k,k]| < 16 eps R[0,0]``, compared against the SIGNED ``R[0,0]``).
+* ``round`` / ``round_edge`` (``src/xerus/ttNetwork.cpp:643-684``,
+  ``src/xerus/tensorNetwork.cpp:678-818``) and the SVD truncation rule of
+  ``calculate_svd`` (``src/xerus/tensor.cpp:1463-1474``).
+* The TT dot product / ``frob_norm`` (``src/xerus/ttNetwork.cpp:781-789``).
+* ``ALSVariant::solve`` with ``lapack_solver`` / ``ASD_solver`` for SPD operators,
+  1 and 2 sites (``src/xerus/algorithms/als.cpp:43-553``).
+* ``ADFVariant`` for ``SinglePointMeasurementSet`` (``src/xerus/algorithms/adf.cpp``).
+
+Parity of this restatement is pinned against golden vectors produced by the
+reference itself (compiled from its own sources against SciPy's OpenBLAS 0.3.34,
+see ``tests/golden/make_golden.py``).
+"""
+from __future__ import annotations
+
+import math
+from dataclasses import dataclass, field
+
+import numpy as np
+import scipy.linalg
+
+EPS = np.finfo(np.float64).eps
+EPSILON = 8 * EPS  # include/xerus/basic.h:50
+
+# --------------------------------------------------------------------------- RNG
+
+_MASK64 = (1 << 64) - 1
+
+
+class MT19937_64:
+    """std::mt19937_64 (the published 64-bit Mersenne Twister, MT19937-64)."""
+
+    N, M = 312, 156
+
+    def __init__(self, seed: int = 5489):
+        self.seed(seed)
+
+    def seed(self, seed: int) -> None:
+        mt = [0] * self.N
+        mt[0] = seed & _MASK64
+        for i in range(1, self.N):
+            mt[i] = (6364136223846793005 * (mt[i - 1] ^ (mt[i - 1] >> 62)) + i) & _MASK64
+        self._mt = np.array(mt, dtype=np.uint64)
+        self._idx = self.N
+        self._buf = None
+
+    def _twist(self) -> None:
+        mt = self._mt
+        N, M = self.N, self.M
+        upper = np.uint64(0xFFFFFFFF80000000)
+        lower = np.uint64(0x7FFFFFFF)
+        mag = np.uint64(0xB5026F5AA96619E9)
+        one = np.uint64(1)
+
+        def step(lo, hi, nxt):
+            y = (mt[lo:hi] & upper) | (mt[lo + 1:hi + 1] & lower)
+            return nxt ^ (y >> one) ^ np.where((y & one) != 0, mag, np.uint64(0))
+
+        mt[0:N - M] = step(0, N - M, mt[M:N])
+        mt[N - M:N - 1] = step(N - M, N - 1, mt[0:M - 1])
+        y = (mt[N - 1] & upper) | (mt[0] & lower)
+        mt[N - 1] = mt[M - 1] ^ (y >> one) ^ (mag if (int(y) & 1) else np.uint64(0))
+        # tempering of the whole block
+        z = mt.copy()
+        z ^= (z >> np.uint64(29)) & np.uint64(0x5555555555555555)
+        z ^= (z << np.uint64(17)) & np.uint64(0x71D67FFFEDA60000)
+        z ^= (z << np.uint64(37)) & np.uint64(0xFFF7EEE000000000)
+        z ^= z >> np.uint64(43)
+        self._buf = [int(v) for v in z]
+        self._idx = 0
+
+    def __call__(self) -> int:
+        if self._idx >= self.N:
+            self._twist()
+        v = self._buf[self._idx]
+        self._idx += 1
+        return v
+
+
+def canonical(eng: MT19937_64) -> float:
+    """std::generate_canonical<double, 53>(mt19937_64): one draw / 2^64."""
+    r = float(eng()) / 18446744073709551616.0
+    return r if r < 1.0 else math.nextafter(1.0, 0.0)
+
+
+class NormalDist:
+    """libstdc++ std::normal_distribution<double> (polar method, cached variate)."""
+
+    def __init__(self, mean: float = 0.0, stddev: float = 1.0):
+        self.mean, self.stddev = mean, stddev
+        self.reset()
+
+    def reset(self) -> None:
+        self._saved = None
+
+    def __call__(self, eng: MT19937_64) -> float:
+        if self._saved is not None:
+            ret, self._saved = self._saved, None
+        else:
+            while True:
+                x = 2.0 * canonical(eng) - 1.0
+                y = 2.0 * canonical(eng) - 1.0
+                r2 = x * x + y * y
+                if not (r2 > 1.0 or r2 == 0.0):
+                    break
+            mult = math.sqrt(-2.0 * math.log(r2) / r2)
+            self._saved = x * mult
+            ret = y * mult
+        return ret * self.stddev + self.mean
+
+    def draw(self, eng: MT19937_64, count: int) -> np.ndarray:
+        return np.array([self(eng) for _ in range(count)], dtype=np.float64)
+
+
+def uniform_int(eng: MT19937_64, a: int, b: int) -> int:
+    """libstdc++ std::uniform_int_distribution<size_t>(a, b) on a 64-bit engine."""
+    rng = b - a + 1  # the engine covers [0, 2^64), rng < 2^64 here
+    if rng == 0:
+        return a + eng()
+    prod = eng() * rng
+    low = prod & _MASK64
+    if low < rng:
+        threshold = ((1 << 64) - rng) % rng
+        while low < threshold:
+            prod = eng() * rng
+            low = prod & _MASK64
+    return a + (prod >> 64)
+
+
+def uniform_real(eng: MT19937_64, a: float = 0.0, b: float = 1.0) -> float:
+    """libstdc++ std::uniform_real_distribution<double>(a, b)."""
+    return canonical(eng) * (b - a) + a
+
+
+class RandomEngine:
+    """The reference's default random state: an engine plus the normal
+    distribution object whose cached variate carries over between calls."""
+
+    def __init__(self, seed: int = 0xBAADF00D):
+        self.eng = MT19937_64(seed)
+        self.normal = NormalDist()
+
+    def reseed(self, seed: int = 0xBAADF00D) -> None:
+        self.eng.seed(seed)
+        self.normal.reset()
+
+
+# --------------------------------------------------------------------------- TT container
+
+
+@dataclass
+class TT:
+    """A TT tensor: cores (r_{k-1}, n_k, r_k), row-major; canonical flag and core position."""
+
+    cores: list
+    canonicalized: bool = False
+    core_position: int = 0
+
+    @property
+    def d(self):
+        return len(self.cores)
+
+    @property
+    def dims(self):
+        return [c.shape[1] for c in self.cores]
+
+    @property
+    def ranks(self):
+        return [c.shape[2] for c in self.cores[:-1]]
+
+    def copy(self):
+        return TT([c.copy() for c in self.cores], self.canonicalized, self.core_position)
+
+
+@dataclass
+class TTOp:
+    """A TT operator: cores (R_{k-1}, n_k (row), n_k (col), R_k)."""
+
+    cores: list
+
+    @property
+    def d(self):
+        return len(self.cores)
+
+
+def tt_from_flat(dims, ranks, data) -> TT:
+    cores, off = [], 0
+    for k, n in enumerate(dims):
+        sz = ranks[k] * n * ranks[k + 1]
+        cores.append(np.asarray(data[off:off + sz], dtype=np.float64).reshape(ranks[k], n, ranks[k + 1]).copy())
+        off += sz
+    return TT(cores)
+
+
+def op_from_flat(dims, ranks, data) -> TTOp:
+    cores, off = [], 0
+    for k, n in enumerate(dims):
+        sz = ranks[k] * n * n * ranks[k + 1]
+        cores.append(np.asarray(data[off:off + sz], dtype=np.float64).reshape(ranks[k], n, n, ranks[k + 1]).copy())
+        off += sz
+    return TTOp(cores)
+
+
+def reduce_to_maximal_ranks(ranks, dims):
+    """src/xerus/ttNetwork.cpp:369-402 (TTTensor case)."""
+    ranks = list(ranks)
+    d = len(dims)
+    cur = 1
+    for i in range(d - 1):
+        cur *= dims[i]
+        if cur < ranks[i]:
+            ranks[i] = cur
+        else:
+            cur = ranks[i]
+    cur = 1
+    for i in range(1, d):
+        cur *= dims[d - i]
+        if cur < ranks[d - i - 1]:
+            ranks[d - i - 1] = cur
+        else:
+            cur = ranks[d - i - 1]
+    return ranks
+
+
+def tt_random(dims, ranks, rs: RandomEngine, dist: NormalDist | None = None) -> TT:
+    """TTNetwork::random (include/xerus/ttNetwork.h:128-155): fill each core in
+    order, row-major, one draw per entry, then move_core(0) with QC."""
+    dist = dist if dist is not None else rs.normal
+    if isinstance(ranks, int):
+        ranks = [ranks] * (len(dims) - 1)
+    r = [1] + reduce_to_maximal_ranks(ranks, dims) + [1]
+    cores = []
+    for k, n in enumerate(dims):
+        cores.append(dist.draw(rs.eng, r[k] * n * r[k + 1]).reshape(r[k], n, r[k + 1]))
+    x = TT(cores, canonicalized=True, core_position=0)
+    # TTNetwork(dims) starts canonical at 0, set_component on k > 0 clears it.
+    x.canonicalized = len(dims) == 1
+    move_core(x, 0, keep_rank=False)
+    return x
+
+
+def tt_full(x: TT) -> np.ndarray:
+    v = x.cores[0]
+    for c in x.cores[1:]:
+        v = np.tensordot(v, c, axes=([v.ndim - 1], [0]))
+    return v.reshape(x.dims)
+
+
+def tt_entries(x: TT, positions: np.ndarray) -> np.ndarray:
+    """Entries at multi-indices (N, d), by left-to-right slice products."""
+    positions = np.asarray(positions)
+    v = np.ones((positions.shape[0], 1))
+    for k, c in enumerate(x.cores):
+        v = np.einsum("sa,sab->sb", v, c[:, positions[:, k], :].transpose(1, 0, 2))
+    return v[:, 0]
+
+
+def tt_dot(x: TT, y: TT) -> float:
+    """Full contraction <x, y> by the left-to-right zipper."""
+    m = np.ones((1, 1))
+    for a, b in zip(x.cores, y.cores):
+        t = np.tensordot(m, a, axes=([0], [0]))  # (s, n, r)
+        m = np.tensordot(t, b, axes=([0, 1], [0, 1]))  # (r, r')
+    return float(m[0, 0])
+
+
+def frob_norm(x: TT) -> float:
+    """src/xerus/ttNetwork.cpp:781-789: the core's norm when canonical, else sqrt(<x,x>)."""
+    if x.canonicalized:
+        return float(np.linalg.norm(x.cores[x.core_position]))
+    return math.sqrt(tt_dot(x, x))
+
+
+def tt_add(x: TT, y: TT) -> TT:
+    """TTNetwork::operator+= block structure (src/xerus/ttNetwork.cpp:796-847)."""
+    d = x.d
+    cores = []
+    for k in range(d):
+        a, b = x.cores[k], y.cores[k]
+        r0 = 1 if k == 0 else a.shape[0] + b.shape[0]
+        r1 = 1 if k == d - 1 else a.shape[2] + b.shape[2]
+        c = np.zeros((r0, a.shape[1], r1))
+        c[:a.shape[0], :, :a.shape[2]] += a
+        lo = 0 if k == 0 else a.shape[0]
+        ro = 0 if k == d - 1 else a.shape[2]
+        c[lo:lo + b.shape[0], :, ro:ro + b.shape[2]] += b
+        cores.append(c)
+    out = TT(cores, canonicalized=False)
+    if x.canonicalized:
+        move_core(out, x.core_position, keep_rank=False)
+    return out
+
+
+def tt_scale(x: TT, f: float) -> TT:
+    y = x.copy()
+    y.cores[y.core_position if y.canonicalized else 0] *= f
+    return y
+
+
+# --------------------------------------------------------------------------- factorisations
+
+
+def qc(a: np.ndarray):
+    """Rank-revealing QR with column pivoting (dgeqp3 + dorgqr),
+    src/xerus/blasLapackWrapper.cpp:243-305. Returns (Q (m x rank), C (rank x n), rank)."""
+    m, n = a.shape
+    q, r, piv = scipy.linalg.qr(a, mode="economic", pivoting=True)
+    max_rank = min(m, n)
+    rank = 1
+    while rank <= max_rank:
+        if rank == max_rank or abs(r[rank, rank]) < 16 * EPS * r[0, 0]:
+            break
+        rank += 1
+    c = np.zeros((rank, n))
+    c[:, piv] = np.triu(r[:rank, :])
+    return q[:, :rank].copy(), c, rank
+
+
+def cq(a: np.ndarray):
+    """A = C Q with Q row-orthonormal: the transposed QC (blasLapackWrapper.cpp:317-371)."""
+    qt, ct, rank = qc(a.T)
+    return ct.T.copy(), qt.T.copy(), rank
+
+
+def qr(a: np.ndarray):
+    q, r = np.linalg.qr(a, mode="reduced")
+    return q, r
+
+
+def rq(a: np.ndarray):
+    m, n = a.shape
+    if m <= n:
+        r, q = scipy.linalg.rq(a, mode="economic")
+        return r, q
+    # more rows than columns: R is m x n, Q is n x n (blasLapackWrapper.cpp:455-498)
+    r, q = scipy.linalg.rq(a, mode="full")
+    return r[:, m - n:], q[m - n:, :] if q.shape[0] > n else q
+
+
+def svd_trunc(x: np.ndarray, max_rank: int, eps: float):
+    """calculate_svd (src/xerus/tensor.cpp:1424-1489): dgesdd, then the
+    rank = min(rank, maxRank) cap and the first j >= 1 with S[j] <= eps*S[0]."""
+    u, s, vt = np.linalg.svd(x, full_matrices=False)
+    rank = len(s)
+    if max_rank:
+        rank = min(rank, max_rank)
+    for j in range(1, rank):
+        if s[j] <= eps * s[0]:
+            rank = j
+            break
+    return u[:, :rank], s[:rank], vt[:rank, :]
+
+
+# --------------------------------------------------------------------------- core movement
+
+
+def transfer_core(x: TT, frm: int, to: int, allow_rank_reduction: bool) -> None:
+    """src/xerus/tensorNetwork.cpp:821-909 for neighbouring TT cores."""
+    f = x.cores[frm]
+    r0, n, r1 = f.shape
+    if to == frm + 1:
+        mat = f.reshape(r0 * n, r1)
+        if allow_rank_reduction:
+            q, rmat, rank = qc(mat)
+        else:
+            q, rmat = qr(mat)
+            rank = q.shape[1]
+        x.cores[frm] = q.reshape(r0, n, rank)
+        nxt = x.cores[to]
+        x.cores[to] = np.tensordot(rmat, nxt, axes=([1], [0]))
+    else:
+        mat = f.reshape(r0, n * r1)
+        if allow_rank_reduction:
+            cmat, q, rank = cq(mat)
+        else:
+            cmat, q = rq(mat)
+            rank = q.shape[0]
+        x.cores[frm] = q.reshape(rank, n, r1)
+        prv = x.cores[to]
+        x.cores[to] = np.tensordot(prv, cmat, axes=([2], [0]))
+
+
+def exceeds_maximal_ranks(x: TT) -> bool:
+    return x.ranks != reduce_to_maximal_ranks(x.ranks, x.dims)
+
+
+def move_core(x: TT, pos: int, keep_rank: bool = False) -> None:
+    """TTNetwork::move_core (src/xerus/ttNetwork.cpp:581-628)."""
+    d = x.d
+    if x.canonicalized:
+        for n in range(x.core_position, pos):
+            transfer_core(x, n, n + 1, not keep_rank)
+        for n in range(x.core_position, pos, -1):
+            transfer_core(x, n, n - 1, not keep_rank)
+    else:
+        for n in range(0, pos):
+            transfer_core(x, n, n + 1, not keep_rank)
+        for n in range(d - 1, pos, -1):
+            transfer_core(x, n, n - 1, not keep_rank)
+    while exceeds_maximal_ranks(x):
+        for n in range(pos, 0, -1):
+            transfer_core(x, n, n - 1, not keep_rank)
+        for n in range(0, d - 1):
+            transfer_core(x, n, n + 1, not keep_rank)
+        for n in range(d - 1, pos, -1):
+            transfer_core(x, n, n - 1, not keep_rank)
+    x.canonicalized = True
+    x.core_position = pos
+
+
+def round_edge(x: TT, frm: int, to: int, max_rank: int, eps: float, spectra=None) -> None:
+    """TensorNetwork::round_edge (src/xerus/tensorNetwork.cpp:678-818) for
+    from = core k+1 (bond on its left) and to = core k (bond on its right)."""
+    F, T = x.cores[frm], x.cores[to]
+    r, n, r1 = F.shape
+    r2, n2, _ = T.shape
+    if 5 * F.size * T.size >= 6 * r ** 4:
+        coreA, Fq, ka = cq(F.reshape(r, n * r1))            # F = coreA Fq
+        Tq, coreB, kb = qc(T.reshape(r2 * n2, r))           # T = Tq coreB
+        X = coreA.T @ coreB.T                               # (ka, kb)
+        U, S, Vt = svd_trunc(X, max_rank, eps)
+        coreB = S[:, None] * Vt
+        x.cores[frm] = (U.T @ Fq).reshape(len(S), n, r1)
+        x.cores[to] = (Tq @ coreB.T).reshape(r2, n2, len(S))
+    else:
+        X = F.reshape(r, n * r1).T @ T.reshape(r2 * n2, r).T    # (n r1, r2 n2)
+        U, S, Vt = svd_trunc(X, max_rank, eps)
+        s = len(S)
+        x.cores[frm] = U.reshape(n, r1, s).transpose(2, 0, 1).copy()
+        x.cores[to] = (Vt.T * S[None, :]).reshape(r2, n2, s)
+    if spectra is not None:
+        spectra.append(S.copy())
+
+
+def tt_round(x: TT, max_ranks, eps: float = EPSILON, spectra=None) -> None:
+    """TTNetwork::round(maxRanks, eps) (src/xerus/ttNetwork.cpp:643-665)."""
+    d = x.d
+    if isinstance(max_ranks, int):
+        max_ranks = [max_ranks] * (d - 1)
+    init_canon, init_pos = x.canonicalized, x.core_position
+    move_core(x, d - 1, keep_rank=False)
+    for i in range(d - 1):
+        round_edge(x, d - 1 - i, d - 2 - i, max_ranks[d - 2 - i], eps, spectra)
+    x.canonicalized, x.core_position = True, 0
+    if init_canon:
+        move_core(x, init_pos, keep_rank=False)
+
+
+def orthogonal_norm(x: TT) -> float:
+    """||x|| through a left-to-right QR sweep: accurate even when the entries
+    cancel (e.g. x = A y - b near a solution)."""
+    y = x.copy()
+    y.canonicalized = False
+    for k in range(y.d - 1):
+        transfer_core(y, k, k + 1, False)
+    return float(np.linalg.norm(y.cores[-1]))
+
+
+# --------------------------------------------------------------------------- operator application
+
+
+def op_apply(A: TTOp, x: TT) -> TT:
+    """The TT of A x, core by core with ranks R_k r_k."""
+    cores = []
+    for a, c in zip(A.cores, x.cores):
+        t = np.einsum("kijl,ajb->kailb", a, c)
+        K, ra, n, L, rb = t.shape
+        cores.append(t.reshape(K * ra, n, L * rb))
+    return TT(cores)
+
+
+def residual(A: TTOp, x: TT, b: TT) -> float:
+    """||A x - b|| / ||b|| in FP64 through orthogonalisation (no cancellation)."""
+    diff = tt_add(op_apply(A, x), tt_scale(b, -1.0))
+    return orthogonal_norm(diff) / orthogonal_norm(b)
+
+
+def laplace_operator(d: int, n: int, V=None, rank3: bool = False, shift: float = 0.0) -> TTOp:
+    """sum_i I x..x (L (+V_i)) x..x I, L = tridiag(-1, 2, -1); the same
+    construction as the golden driver (rank 2, or rank 3 with V in its own channel)."""
+    L = 2 * np.eye(n) - np.eye(n, k=1) - np.eye(n, k=-1)
+    I = np.eye(n)
+    R = 3 if rank3 else 2
+    cores = []
+    for k in range(d):
+        Vk = np.diag(V[k]) if V is not None else np.zeros((n, n))
+        l = L + (0 if rank3 else Vk) + shift * I / d
+        rl, rr = (1 if k == 0 else R), (1 if k == d - 1 else R)
+        c = np.zeros((rl, n, n, rr))
+        if d == 1:
+            c[0, :, :, 0] = L + Vk + shift * I
+        elif k == 0:
+            c[0, :, :, 0] = l + (Vk if rank3 else 0)
+            c[0, :, :, 1] = I
+            if rank3:
+                c[0, :, :, 2] = I
+        elif k == d - 1:
+            c[0, :, :, 0] = I
+            c[1, :, :, 0] = l
+            if rank3:
+                c[2, :, :, 0] = Vk
+        else:
+            c[0, :, :, 0] = I
+            c[1, :, :, 0] = l
+            c[1, :, :, 1] = I
+            if rank3:
+                c[2, :, :, 0] = Vk
+                c[2, :, :, 2] = I
+        cores.append(c)
+    return TTOp(cores)
+
+
+# --------------------------------------------------------------------------- ALS (SPD)
+
+FLAG_FINISHED_HALFSWEEP = 1
+FLAG_FINISHED_FULLSWEEP = 3
+
+
+def _push_left_op(L, xc, ac):
+    # L'(c1,c2,c3) = sum L(a1,a2,a3) x(a1,i,c1) A(a2,i,j,c2) x(a3,j,c3)   (als.cpp:184-200, 247)
+    return np.einsum("xky,xic,kijl,yjm->clm", L, xc, ac, xc, optimize=True)
+
+
+def _push_right_op(R, xc, ac):
+    # R'(a1,a2,a3) = sum x(a1,i,c1) A(a2,i,j,c2) x(a3,j,c3) R(c1,c2,c3)   (als.cpp:239)
+    return np.einsum("xic,kijl,yjm,clm->xky", xc, ac, xc, R, optimize=True)
+
+
+def _push_left_rhs(Lb, bc, xc):
+    # Lb'(c1,c2) = sum Lb(a1,a2) b(a1,i,c1) x(a2,i,c2)   (als.cpp:202-215, 250)
+    return np.einsum("st,sic,tid->cd", Lb, bc, xc, optimize=True)
+
+
+def _push_right_rhs(Rb, bc, xc):
+    # Rb'(a1,a2) = sum b(a1,i,c1) x(a2,i,c2) Rb(c1,c2)   (als.cpp:242)
+    return np.einsum("sic,tid,cd->st", bc, xc, Rb, optimize=True)
+
+
+def local_operator(L, Acores, R):
+    """Dense local operator of construct_local_operator (als.cpp:383-401):
+    rows (a, i_1..i_s, b), columns (a', j_1..j_s, b')."""
+    if len(Acores) == 1:
+        op = np.einsum("xka,kijl,ylb->xiyajb", L, Acores[0], R, optimize=True)
+    else:
+        op = np.einsum("xka,kijl,lmnp,ypb->ximyajnb", L, Acores[0], Acores[1], R, optimize=True)
+    half = op.ndim // 2
+    N = int(np.prod(op.shape[:half]))
+    return op.reshape(N, N), op.shape[half:]
+
+
+def local_rhs(Lb, bcores, Rb):
+    """construct_local_RHS (als.cpp:404-423): (a, i_1..i_s, b)."""
+    if len(bcores) == 1:
+        return np.einsum("sa,sit,tb->aib", Lb, bcores[0], Rb, optimize=True)
+    return np.einsum("sa,sit,tju,ub->aijb", Lb, bcores[0], bcores[1], Rb, optimize=True)
+
+
+def _is_symmetric(M):
+    # blasLapackWrapper.cpp:500-514
+    mx = max(0.0, float(M.max()))
+    return np.all(np.abs(M - M.T) < 4 * mx * EPS)
+
+
+def dense_solve(M, rhs):
+    """xerus::solve for a square dense system (blasLapackWrapper.cpp:542-651):
+    LU if not symmetric, Cholesky if the diagonal is one-signed, else LDL^T."""
+    if not _is_symmetric(M):
+        return scipy.linalg.solve(M, rhs)
+    diag = np.diag(M)
+    pos = diag[0] > 0
+    onesigned = np.all(diag[1:] >= EPS) if pos else np.all(diag[1:] <= -EPS)
+    if onesigned:
+        try:
+            c = scipy.linalg.cho_factor(M, lower=False, check_finite=False)
+            return scipy.linalg.cho_solve(c, rhs, check_finite=False)
+        except np.linalg.LinAlgError:
+            pass
+    return scipy.linalg.solve(M, rhs, assume_a="sym")
+
+
+@dataclass
+class ALSResult:
+    energy: float
+    residuals: list = field(default_factory=list)   # after every micro-step (accurate FP64)
+    flags: list = field(default_factory=list)
+    energies: list = field(default_factory=list)    # at the end of each half-sweep
+    half_sweeps: int = 0
+
+
+def als_spd(A: TTOp, x: TT, b: TT, sites: int = 1, num_half_sweeps: int = 0, conv_eps: float = 1e-6,
+            solver: str = "lapack", preserve_core_position: bool = True, track_residual: bool = False,
+            residual_target: float | None = None) -> ALSResult:
+    """ALSVariant::solve for an SPD operator (src/xerus/algorithms/als.cpp:483-553).
+
+    ``x`` is updated in place. ``solver`` is "lapack" (lapack_solver, als.cpp:43-71)
+    or "asd" (ASD_solver, als.cpp:73-92). With ``track_residual`` the accurate
+    relative residual is recorded where the reference records perfData.
+    ``residual_target`` stops at the end of the first half-sweep whose residual
+    is at or below it (a time-to-residual measurement, not a reference feature)."""
+    d = x.d
+    target_rank = list(x.ranks)
+    norm_b = frob_norm(b)
+    canon_end, core_end = x.canonicalized, x.core_position
+    # prepare_x_for_als (als.cpp:105-182)
+    first, prod = 0, 1
+    while first + 1 < d:
+        nd = x.dims[first]
+        newp = prod * nd
+        if x.ranks[first] < newp:
+            break
+        comp = x.cores[first].reshape(prod * nd, x.ranks[first])
+        x.cores[first + 1] = np.tensordot(comp, x.cores[first + 1], axes=([1], [0]))
+        ident = np.zeros((prod, nd, newp))
+        for i0 in range(prod):
+            for i1 in range(nd):
+                ident[i0, i1, i0 * nd + i1] = 1.0
+        x.cores[first] = ident
+        first += 1
+        prod = newp
+    last, prod = d, 1
+    while last > first + sites:
+        nd = x.dims[last - 1]
+        newp = prod * nd
+        if x.ranks[last - 2] < newp:
+            break
+        comp = x.cores[last - 1].reshape(x.ranks[last - 2], nd * prod)
+        x.cores[last - 2] = np.tensordot(x.cores[last - 2], comp, axes=([2], [0])).reshape(
+            x.cores[last - 2].shape[0], x.dims[last - 2], nd * prod)
+        ident = np.zeros((newp, nd, prod))
+        for i1 in range(nd):
+            for i2 in range(prod):
+                ident[i1 * prod + i2, i1, i2] = 1.0
+        x.cores[last - 1] = ident
+        last -= 1
+        prod = newp
+    if canon_end and core_end < first:
+        x.canonicalized, x.core_position = True, first
+    else:
+        if canon_end and core_end >= last:
+            x.canonicalized, x.core_position = True, last - 1
+        move_core(x, first, keep_rank=True)
+    # prepare_stacks (als.cpp:217-253)
+    Lop, Rop = [np.ones((1, 1, 1))], [np.ones((1, 1, 1))]
+    Lb, Rb = [np.ones((1, 1))], [np.ones((1, 1))]
+    for i in range(d - 1, first + sites - 1, -1):
+        Rop.append(_push_right_op(Rop[-1], x.cores[i], A.cores[i]))
+        Rb.append(_push_right_rhs(Rb[-1], b.cores[i], x.cores[i]))
+    for i in range(first):
+        Lop.append(_push_left_op(Lop[-1], x.cores[i], A.cores[i]))
+        Lb.append(_push_left_rhs(Lb[-1], b.cores[i], x.cores[i]))
+    cur = first
+    inc = True
+
+    def energy_f():
+        # |0.5 <x,Ax> - <x,b>| from the stacks (als.cpp:265-278)
+        xAx, bx = Lop[-1], Lb[-1]
+        for i in range(sites):
+            xAx = _push_left_op(xAx, x.cores[cur + i], A.cores[cur + i])
+            bx = _push_left_rhs(bx, b.cores[cur + i], x.cores[cur + i])
+        return abs(0.5 * float(np.sum(xAx * Rop[-1])) - float(np.sum(bx * Rb[-1])))
+
+    res = ALSResult(energy=0.0)
+
+    def record(flag):
+        if track_residual:
+            res.residuals.append(residual(A, x, b))
+            res.flags.append(flag)
+
+    energy, last_e, last_e2 = energy_f(), 1e101, 1e102
+    record(FLAG_FINISHED_FULLSWEEP)
+    half = 0
+    while True:
+        # local operator L . A_k [. A_k+1] . R and rhs (als.cpp:383-423)
+        M, shape_x = local_operator(Lop[-1], A.cores[cur:cur + sites], Rop[-1])
+        N = M.shape[0]
+        rhs = local_rhs(Lb[-1], b.cores[cur:cur + sites], Rb[-1]).reshape(N)
+        if solver == "asd":
+            xv = x.cores[cur].reshape(N)
+            grad = rhs - M @ xv
+            alpha = float(grad @ grad) / float(grad @ (M @ grad))
+            x.cores[cur] = (xv + alpha * grad).reshape(shape_x)
+        else:
+            xv = dense_solve(M, rhs).reshape(shape_x)
+            if sites == 1:
+                x.cores[cur] = xv
+            else:
+                a_, j1, j2, b_ = xv.shape
+                U, S, Vt = svd_trunc(xv.reshape(a_ * j1, j2 * b_), target_rank[cur], EPSILON)
+                s = len(S)
+                if inc:
+                    x.cores[cur] = U.reshape(a_, j1, s)
+                    x.cores[cur + 1] = (S[:, None] * Vt).reshape(s, j2, b_)
+                else:
+                    x.cores[cur] = (U * S[None, :]).reshape(a_, j1, s)
+                    x.cores[cur + 1] = Vt.reshape(s, j2, b_)
+                # set_component on a non-core position clears the canonical flag (ttNetwork.cpp:491)
+                if not (x.canonicalized and x.core_position == cur + 1):
+                    x.canonicalized = False
+        # check_for_end_of_sweep (als.cpp:426-475)
+        if (not inc and cur == first) or (inc and cur == last - sites):
+            half += 1
+            last_e2, last_e = last_e, energy
+            energy = energy_f()
+            res.energies.append(energy)
+            record(FLAG_FINISHED_HALFSWEEP if inc else FLAG_FINISHED_FULLSWEEP)
+            done_target = residual_target is not None and residual(A, x, b) <= residual_target
+            if (half == num_half_sweeps or abs(last_e - energy) < conv_eps or abs(last_e2 - energy) < conv_eps
+                    or last - first <= sites or done_target):
+                if canon_end and preserve_core_position:
+                    move_core(x, core_end, keep_rank=True)
+                res.energy, res.half_sweeps = energy, half
+                return res
+            inc = not inc
+        else:
+            record(0)
+        # move_to_next_index (als.cpp:340-380)
+        if inc:
+            if sites == 1:
+                move_core(x, cur + 1, keep_rank=True)
+            Rop.pop()
+            Rb.pop()
+            Lop.append(_push_left_op(Lop[-1], x.cores[cur], A.cores[cur]))
+            Lb.append(_push_left_rhs(Lb[-1], b.cores[cur], x.cores[cur]))
+            cur += 1
+        else:
+            if sites == 1:
+                move_core(x, cur - 1, keep_rank=True)
+            Lop.pop()
+            Lb.pop()
+            Rop.append(_push_right_op(Rop[-1], x.cores[cur], A.cores[cur]))
+            Rb.append(_push_right_rhs(Rb[-1], b.cores[cur], x.cores[cur]))
+            cur -= 1
+
+
+# --------------------------------------------------------------------------- measurement sets / ADF
+
+
+def random_positions(num: int, dims, rs: RandomEngine) -> np.ndarray:
+    """SinglePointMeasurementSet::create_random_positions (measurments.cpp:222-248):
+    per sample one uniform_int per mode, duplicates (by linear index) rejected,
+    then sorted lexicographically."""
+    seen = set()
+    out = []
+    while len(out) < num:
+        idx = [uniform_int(rs.eng, 0, n - 1) for n in dims]
+        lin = 0
+        for i, n in zip(idx, dims):
+            lin = lin * n + i
+        if lin not in seen:
+            seen.add(lin)
+            out.append(idx)
+    out.sort()
+    return np.array(out, dtype=np.int64).reshape(num, len(dims))
+
+
+def _num_unique(pos: np.ndarray) -> int:
+    if pos.shape[1] == 0:
+        return 1
+    return int(np.unique(pos, axis=0).shape[0])
+
+
+@dataclass
+class ADFResult:
+    residual_norm: float
+    residuals: list = field(default_factory=list)
+    iterations: int = 0
+
+
+class ADFSolver:
+    """ADFVariant::InternalSolver<SinglePointMeasurementSet> (src/xerus/algorithms/adf.cpp),
+    with the per-sample stacks held as dense (N, r) arrays instead of deduplicated slots
+    (deduplication shares identical values and so does not change them)."""
+
+    def __init__(self, x: TT, positions: np.ndarray, values: np.ndarray, max_iter: int, target: float, min_dec: float):
+        self.x = x
+        self.pos = np.asarray(positions, dtype=np.int64)
+        self.y = np.asarray(values, dtype=np.float64)
+        self.N, self.d = self.pos.shape
+        self.max_iter, self.target, self.min_dec = max_iter, target, min_dec
+        self.norm_y = math.sqrt(float(np.sum(self.y ** 2)))
+        # unique-entry counts per position decide which side evaluates (adf.cpp:295, 420)
+        self.fwd_updates = [_num_unique(self.pos[:, :k + 1]) for k in range(self.d)]
+        self.bwd_updates = [_num_unique(self.pos[:, k:]) for k in range(self.d)]
+        self.F = {}
+        self.B = {}
+        self.iteration = 0
+        self.residual_norm = np.finfo(np.float64).max
+        self.last_residual_norm = np.finfo(np.float64).max
+
+    def _slices(self, core, k):
+        return core[:, self.pos[:, k], :].transpose(1, 0, 2)   # (N, r0, r1)
+
+    def fstack(self, k):
+        return np.ones((self.N, 1)) if k < 0 else self.F[k]
+
+    def bstack(self, k):
+        return np.ones((self.N, 1)) if k >= self.d else self.B[k]
+
+    def update_forward(self, k, core):
+        return np.einsum("sa,sab->sb", self.fstack(k - 1), self._slices(core, k))
+
+    def update_backward(self, k, core):
+        return np.einsum("sab,sb->sa", self._slices(core, k), self.bstack(k + 1))
+
+    def calculate_residual(self, k):
+        if self.fwd_updates[k] < self.bwd_updates[k]:
+            self.F[k] = self.update_forward(k, self.x.cores[k])
+            cur = np.einsum("sa,sa->s", self.F[k], self.bstack(k + 1))
+        else:
+            self.B[k] = self.update_backward(k, self.x.cores[k])
+            cur = np.einsum("sa,sa->s", self.fstack(k - 1), self.B[k])
+        self.res = self.y - cur
+
+    def projected_gradient(self, k):
+        c = self.x.cores[k]
+        n = c.shape[1]
+        outer = self.res[:, None, None] * self.fstack(k - 1)[:, :, None] * self.bstack(k + 1)[:, None, :]
+        G = np.zeros((n, c.shape[0], c.shape[2]))
+        np.add.at(G, self.pos[:, k], outer)
+        return G.transpose(1, 0, 2).copy()   # (r0, n, r1)   (adf.cpp:395)
+
+    def slicewise_norm(self, k, G):
+        if self.fwd_updates[k] < self.bwd_updates[k]:
+            tmp = self.update_forward(k, G)
+            cur = np.einsum("sa,sa->s", tmp, self.bstack(k + 1))
+        else:
+            tmp = self.update_backward(k, G)
+            cur = np.einsum("sa,sa->s", self.fstack(k - 1), tmp)
+        return np.bincount(self.pos[:, k], weights=cur ** 2, minlength=G.shape[1])
+
+    def update_x(self, k, G, norms):
+        c = self.x.cores[k]
+        for j in range(c.shape[1]):
+            g = G[:, j, :]
+            pyr = float(np.sum(g * g))
+            c[:, j, :] = c[:, j, :] + (pyr / norms[j]) * g
+
+    def sweep_step(self, k, log=None):
+        if k > 0:
+            self.calculate_residual(k)
+        G = self.projected_gradient(k)
+        norms = self.slicewise_norm(k, G)
+        if log is not None:
+            log.append((G.copy(), norms.copy()))
+        self.update_x(k, G, norms)
+        if k + 1 < self.d:
+            move_core(self.x, k + 1, keep_rank=True)
+            self.F[k] = self.update_forward(k, self.x.cores[k])
+
+    def begin_iteration(self):
+        move_core(self.x, 0, keep_rank=True)
+        for k in range(self.d - 1, 0, -1):
+            self.B[k] = self.update_backward(k, self.x.cores[k])
+        self.calculate_residual(0)
+
+    def solve(self, first_sweep_log=None) -> ADFResult:
+        """solve() + solve_with_current_ranks() (adf.cpp:489-542, 566-604) without rank increase
+        (the case when x already has its maximal ranks)."""
+        move_core(self.x, 0, keep_rank=False)      # canonicalize_left
+        out = ADFResult(residual_norm=0.0)
+        dec = [0.0, 0.0, 0.0]
+        while self.max_iter == 0 or self.iteration < self.max_iter:
+            self.begin_iteration()
+            self.last_residual_norm = self.residual_norm
+            self.residual_norm = math.sqrt(float(np.sum(self.res ** 2))) / self.norm_y
+            out.residuals.append(self.residual_norm)
+            d4 = dec[2]
+            dec = [self.residual_norm / self.last_residual_norm, dec[0], dec[1]]
+            if self.residual_norm < self.target or dec[0] * dec[1] * dec[2] * d4 > self.min_dec ** 4:
+                break
+            for k in range(self.d):
+                self.sweep_step(k, first_sweep_log if self.iteration == 0 else None)
+            self.iteration += 1
+        out.residual_norm = self.residual_norm
+        out.iterations = self.iteration
+        return out
+
+
+def adf(x: TT, positions, values, max_iter: int = 0, target: float = 1e-8, min_dec: float = 0.999) -> ADFResult:
+    return ADFSolver(x, positions, values, max_iter, target, min_dec).solve()
+
+
+def adf_loss_gradient(x: TT, positions, values):
+    """Gradient of 0.5 * ||P_Omega(x) - y||^2 with respect to every core (no gauge
+    condition), by the same stacks: dL/dX_k[a,i,b] = -sum_{s: i_s=i} res_s F_{k-1}[s,a] B_{k+1}[s,b]."""
+    pos = np.asarray(positions, dtype=np.int64)
+    y = np.asarray(values, dtype=np.float64)
+    N, d = pos.shape
+    F = [np.ones((N, 1))]
+    for k in range(d):
+        F.append(np.einsum("sa,sab->sb", F[-1], x.cores[k][:, pos[:, k], :].transpose(1, 0, 2)))
+    Bk = [None] * (d + 1)
+    Bk[d] = np.ones((N, 1))
+    for k in range(d - 1, -1, -1):
+        Bk[k] = np.einsum("sab,sb->sa", x.cores[k][:, pos[:, k], :].transpose(1, 0, 2), Bk[k + 1])
+    res = y - F[d][:, 0]
+    grads = []
+    for k in range(d):
+        c = x.cores[k]
+        outer = -res[:, None, None] * F[k][:, :, None] * Bk[k + 1][:, None, :]
+        G = np.zeros((c.shape[1], c.shape[0], c.shape[2]))
+        np.add.at(G, pos[:, k], outer)
+        grads.append(G.transpose(1, 0, 2).copy())
+    return 0.5 * float(np.sum(res ** 2)), grads
