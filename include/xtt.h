@@ -1,0 +1,204 @@
+/*
+ * xtt.h - C ABI of the GB300-native Tensor-Train sweep engine (libxtt.so).
+ *
+ * The library keeps TT tensors and TT operators resident on one CUDA device and
+ * runs the xerus sweep path on it: TTNetwork::move_core / round / frob_norm, the
+ * TT dot product, ALSVariant::solve (ALS_SPD, DMRG_SPD, ASD_SPD) and ADFVariant
+ * for single-point measurement sets. Every entry point takes plain pointers and
+ * sizes, returns an xtt_status, and leaves a message for xtt_last_error() when it
+ * fails. A context owns one CUDA stream; calls on one context are serialised by
+ * the caller (one host thread per context), different contexts are independent.
+ *
+ * Layout: a TT tensor of order d has cores (r_{k-1}, n_k, r_k), a TT operator
+ * cores (R_{k-1}, n_k, n_k, R_k), all row-major FP64 (last index fastest) with
+ * boundary ranks r_0 = r_d = 1, exactly as xerus stores its component tensors
+ * (include/xerus/ttNetwork.h:145-150, include/xerus/tensor.h:536). Host buffers
+ * hold the cores concatenated in order.
+ *
+ * Each declaration names the reference interface it replaces (paths relative to
+ * the xerus 3.0.1 source tree).
+ */
+#ifndef XTT_H
+#define XTT_H
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef enum xtt_status {
+	XTT_OK = 0,
+	XTT_ERR_ARGUMENT = 1,        /* bad shape, index or option: xerus REQUIRE failure (misc/check.h:60-65) */
+	XTT_ERR_CUDA = 2,            /* a CUDA runtime call failed */
+	XTT_ERR_NOT_CONVERGED = 3,   /* a local solver or the SVD hit its iteration cap */
+	XTT_ERR_NUMERIC = 4,         /* NaN/Inf or a breakdown (non-SPD local operator) */
+	XTT_ERR_TIMEOUT = 5,         /* a bounded device-side wait gave up */
+	XTT_ERR_CAPACITY = 6,        /* a size exceeds a fixed limit of the library */
+	XTT_ERR_NO_MEMORY = 7
+} xtt_status;
+
+typedef enum xtt_precision {
+	XTT_PRECISION_FP64 = 0,      /* plain form: FP64 everywhere */
+	XTT_PRECISION_MIXED = 1      /* local solves in FP32 with FP64 iterative refinement */
+} xtt_precision;
+
+typedef struct xtt_context xtt_context;
+typedef struct xtt_tensor xtt_tensor;
+
+/* Message of the last failing call on this host thread ("" if none). */
+const char* xtt_last_error(void);
+const char* xtt_version(void);
+
+/* --------------------------------------------------------------- context */
+int xtt_context_create(int device, xtt_context** out);
+int xtt_context_destroy(xtt_context* ctx);
+/* Use an existing cudaStream_t (passed as void*); NULL restores the context's own stream. */
+int xtt_context_set_stream(xtt_context* ctx, void* stream);
+int xtt_context_synchronize(xtt_context* ctx);
+/* Number of kernels this context has launched so far (a counter, for measurements). */
+int xtt_context_kernel_launches(xtt_context* ctx, int64_t* count);
+
+/* ---------------------------------------------------------------- tensors */
+/* TTNetwork(dims) + set_component: a device TT with the given ranks (order+1
+ * entries, r_0 = r_d = 1), all cores zero, not canonical.
+ * Replaces TTTensor/TTOperator construction (include/xerus/ttNetwork.h:44-100). */
+int xtt_tensor_create(xtt_context* ctx, int is_operator, int64_t order, const int64_t* dims,
+                      const int64_t* ranks, xtt_tensor** out);
+int xtt_tensor_destroy(xtt_tensor* t);
+/* Deep copy (TTNetwork copy constructor). */
+int xtt_tensor_copy(const xtt_tensor* src, xtt_tensor** out);
+int xtt_tensor_order(const xtt_tensor* t, int64_t* order);
+int xtt_tensor_dims(const xtt_tensor* t, int64_t* dims);
+/* Current ranks, order+1 entries (TTNetwork::ranks, include/xerus/ttNetwork.h:394, plus the boundary 1s). */
+int xtt_tensor_ranks(const xtt_tensor* t, int64_t* ranks);
+/* Number of doubles of all cores at the current ranks. */
+int xtt_tensor_size(const xtt_tensor* t, int64_t* count);
+/* Host <-> device copies of all cores (count must equal xtt_tensor_size). */
+int xtt_tensor_set_cores(xtt_tensor* t, const double* host, int64_t count);
+int xtt_tensor_get_cores(const xtt_tensor* t, double* host, int64_t count);
+/* Replace the whole tensor with new ranks and cores (TTNetwork::set_component for every core). */
+int xtt_tensor_assign(xtt_tensor* t, const int64_t* ranks, const double* host, int64_t count);
+/* TTNetwork::canonicalized / corePosition (include/xerus/ttNetwork.h:66-72) and assume_core_position (:421). */
+int xtt_tensor_get_canonical(const xtt_tensor* t, int* canonicalized, int64_t* core_position);
+int xtt_tensor_set_canonical(xtt_tensor* t, int canonicalized, int64_t core_position);
+/* x *= f on the core (TTNetwork::operator*=, src/xerus/ttNetwork.cpp:859-868). */
+int xtt_tensor_scale(xtt_tensor* t, double f);
+
+/* ------------------------------------------------------------- random state */
+/* Reseeds the library's random engine (std::mt19937_64, the analogue of
+ * xerus::misc::randomEngine, src/xerus/misc/random.cpp:29) and resets its normal
+ * distribution (drops a cached polar variate). Thread-local, like the reference. */
+int xtt_random_seed(uint64_t seed);
+/* TTNetwork::random(dims, ranks, normal(mean, stddev)) (include/xerus/ttNetwork.h:128-155):
+ * ranks has order-1 inner entries, reduced to the maximal ranks; entries drawn
+ * core by core in row-major order on the host from the library engine, then
+ * move_core(0) with rank-revealing QR on the device. */
+int xtt_tensor_random(xtt_context* ctx, int64_t order, const int64_t* dims, const int64_t* inner_ranks,
+                      double mean, double stddev, xtt_tensor** out);
+/* SinglePointMeasurementSet::random(num, dims) positions
+ * (src/xerus/measurments.cpp:42-47, 222-248): out holds num*order indices, sorted. */
+int xtt_random_positions(int64_t num, int64_t order, const int64_t* dims, int64_t* out);
+/* Draws `count` values from N(mean, stddev) with the library engine (what a caller
+ * of std::normal_distribution on misc::randomEngine gets). */
+int xtt_random_normal(double mean, double stddev, int64_t count, double* out);
+
+/* ----------------------------------------------------------- core movement */
+/* TTNetwork::move_core(position, keepRank) (include/xerus/ttNetwork.h:413,
+ * src/xerus/ttNetwork.cpp:581-628): keep_rank != 0 uses plain QR/LQ, else
+ * rank-revealing pivoted QR with the cutoff |R_kk| < 16 eps R_00. */
+int xtt_move_core(xtt_tensor* x, int64_t position, int keep_rank);
+/* TTNetwork::round(maxRanks, eps) (include/xerus/ttNetwork.h:352-373,
+ * src/xerus/ttNetwork.cpp:643-665). max_ranks has order-1 entries (use
+ * INT64_MAX for "no cap"). If spectra is not NULL it receives the kept singular
+ * values of each bond in sweep order (right to left), at most spectra_capacity. */
+int xtt_round(xtt_tensor* x, const int64_t* max_ranks, double eps, double* spectra, int64_t spectra_capacity,
+              int64_t* spectra_count);
+
+/* ---------------------------------------------------------- contractions */
+/* Full contraction value_t(x(i&0) * y(i&0)) of two TT tensors of equal dims
+ * (src/xerus/indexedTensorReadOnly.cpp:58-61 via tensorNetwork.cpp:1253-1333). */
+int xtt_dot(const xtt_tensor* x, const xtt_tensor* y, double* out);
+/* TTNetwork::frob_norm (src/xerus/ttNetwork.cpp:781-789): the core norm when
+ * canonical, else sqrt(<x,x>). */
+int xtt_frob_norm(const xtt_tensor* x, double* out);
+/* ||A x - b|| / ||b|| in FP64, through an orthogonalising sweep of the TT A x - b
+ * (no cancellation). Replaces ALSVariant's residual_f (src/xerus/algorithms/als.cpp:258-261). */
+int xtt_residual(const xtt_tensor* A, const xtt_tensor* x, const xtt_tensor* b, double* out);
+/* Entries of x at `count` multi-indices (count*order int64, row-major):
+ * SinglePointMeasurementSet::measure(TensorNetwork) (src/xerus/measurments.cpp:125-153). */
+int xtt_entries(const xtt_tensor* x, const int64_t* positions, int64_t count, double* out);
+
+/* ------------------------------------------------------------------- ALS */
+typedef struct xtt_als_options {
+	int32_t sites;                   /* ALSVariant::sites: 1 = ALS, 2 = DMRG (als.h:112) */
+	int32_t local_solver;            /* 0 = exact local solve (lapack_solver, als.cpp:43), 1 = one steepest-descent step (ASD_solver, als.cpp:73) */
+	int32_t preserve_core_position;  /* ALSVariant::preserveCorePosition (als.h:117) */
+	int32_t precision;               /* xtt_precision */
+	int64_t num_half_sweeps;         /* 0 = until convergence (als.h:113) */
+	double convergence_epsilon;      /* |dE| threshold (als.h:114), default 1e-6 */
+	double local_tolerance;          /* relative residual of the local CG solve, default 1e-13 */
+	int64_t local_max_iterations;    /* CG iteration cap per local solve, 0 = 10*N */
+	double residual_target;          /* > 0: also stop after the first half-sweep whose FP64 residual <= target */
+	int32_t record_residuals;        /* 1: FP64 residual after every micro-step into the trace (costly) */
+	int32_t max_rank;                /* DMRG only: > 0 lets the 2-site split grow ranks up to this cap */
+	double svd_epsilon;              /* DMRG only, with max_rank > 0: relative singular value cutoff */
+	int32_t exact_environment;       /* DMRG only: 0 reproduces the reference's decreasing half-sweep, which
+	                                    contracts core k (not k+1) into the right environment
+	                                    (src/xerus/algorithms/als.cpp:371); 1 contracts core k+1 */
+} xtt_als_options;
+
+typedef struct xtt_als_report {
+	double energy;                   /* the value ALSVariant::operator() returns */
+	double residual;                 /* FP64 ||A x - b|| / ||b|| of the result */
+	int64_t half_sweeps;
+	int64_t micro_steps;
+	int64_t local_iterations;        /* total CG iterations (FP32 + FP64) */
+	int64_t refinements;             /* FP64 refinement passes (mixed precision) */
+	int64_t trace_count;             /* entries written to each trace */
+} xtt_als_report;
+
+int xtt_als_default_options(xtt_als_options* opt);
+/* ALSVariant::solve(A, x, b, numHalfSweeps, convergenceEpsilon, perfData)
+ * (src/xerus/algorithms/als.cpp:483-553, include/xerus/algorithms/als.h:152-207)
+ * for a symmetric positive definite operator. x is updated in place. The traces
+ * (optional, trace_capacity entries each) receive, per recorded point, the
+ * residual (if record_residuals) and the flags of PerformanceData (0, 1 = half
+ * sweep, 3 = full sweep; include/xerus/algorithms/als.h:109-110); energies gets
+ * the energy at the end of every half-sweep. */
+int xtt_als(const xtt_tensor* A, xtt_tensor* x, const xtt_tensor* b, const xtt_als_options* opt,
+            xtt_als_report* report, double* residual_trace, int64_t* flag_trace, double* energy_trace,
+            int64_t trace_capacity);
+
+/* Gradient of the ALS energy J(x) = <x, A x> - 2 <x, b> with respect to every
+ * core of x (no gauge condition), for symmetric A: dJ/dX_k = 2 (L_k A_k R_k x_k -
+ * Lb_k b_k Rb_k) with environments built from all other cores. grad receives the
+ * cores concatenated like xtt_tensor_get_cores. At a canonical x with core k it
+ * equals -2 times the ASD_solver step direction (src/xerus/algorithms/als.cpp:81). */
+int xtt_als_energy_gradient(const xtt_tensor* A, const xtt_tensor* x, const xtt_tensor* b, double* energy,
+                            double* grad, int64_t count);
+
+/* ------------------------------------------------------------------- ADF */
+typedef struct xtt_adf_options {
+	int64_t max_iterations;          /* ADFVariant::maxIterations (adf.h:233), 0 = unlimited */
+	double target_residual;          /* ADFVariant::targetResidualNorm (adf.h:234) */
+	double min_decrease;             /* ADFVariant::minimalResidualNormDecrease (adf.h:235) */
+} xtt_adf_options;
+
+/* ADFVariant(maxIter, target, minDecrease)(x, SinglePointMeasurementSet{positions, values})
+ * (include/xerus/algorithms/adf.h:248-252, src/xerus/algorithms/adf.cpp:489-604), x at its
+ * maximal ranks. positions: num*order int64 (row-major), need not be sorted. residual_trace
+ * receives the relative residual at the start of every iteration (PerformanceData). */
+int xtt_adf(xtt_tensor* x, const int64_t* positions, const double* values, int64_t num,
+            const xtt_adf_options* opt, double* final_residual, double* residual_trace,
+            int64_t trace_capacity, int64_t* trace_count);
+/* Loss 0.5 ||P_Omega(x) - y||^2 and its gradient with respect to every core of x
+ * (adjoint of the sampled-entry map; at the core position it is minus
+ * ADF's projected gradient, src/xerus/algorithms/adf.cpp:359-396). */
+int xtt_adf_gradient(const xtt_tensor* x, const int64_t* positions, const double* values, int64_t num,
+                     double* loss, double* grad, int64_t count);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* XTT_H */

@@ -1,0 +1,297 @@
+"""Parity of the CUDA path (through the C ABI) with the xerus reference's golden
+vectors and the CPU oracle, on the GPU. Tolerances: integer results (ranks,
+sample positions, random streams) bit-exact; FP64 quantities within 1e-10
+relative (REL_TOL) unless a test states otherwise."""
+import numpy as np
+import pytest
+
+from oracle import xtt_oracle as o
+from tests.helpers import REL_TOL, fnv1a, op_of, rel_err, tt_of
+
+pytestmark = pytest.mark.gpu
+
+xg = pytest.importorskip("xerus_gb300")
+
+
+@pytest.fixture(scope="module")
+def ctx():
+    from xerus_gb300 import build
+    build.build()
+    return xg.Context(0)
+
+
+def dev_tt(ctx, x):
+    return xg.TTTensor.from_cores(x.cores, ctx=ctx, canonicalized=x.canonicalized, core_position=x.core_position)
+
+
+def dev_op(ctx, A):
+    return xg.TTOperator.from_cores(A.cores, ctx=ctx)
+
+
+def host_tt(t):
+    return o.TT(t.get_cores(), t.canonicalized, t.corePosition)
+
+
+# ------------------------------------------------------------------ random state (host side of the library)
+
+def test_random_streams_match_reference(ctx, golden):
+    z = golden("rng")
+    xg.seed(0xBAADF00D)
+    import ctypes
+    out = np.zeros(257)
+    xg._lib.load().xtt_random_normal(0.0, 1.0, 257, out.ctypes.data_as(xg._lib.c_double_p))
+    assert np.array_equal(out, z["rng_normal"])
+
+
+def test_tt_random_and_positions(ctx, golden):
+    z = golden("tt_random")
+    xg.seed(0xBAADF00D)
+    x = xg.TTTensor.random([3, 4, 2, 5], [2, 7, 3], ctx=ctx)
+    assert [1] + x.ranks() + [1] == list(z["small_ranks_after"])
+    assert rel_err(o.tt_full(host_tt(x)).ravel(), z["small_full"]) < REL_TOL
+    xg.seed(0xBAADF00D)
+    y = xg.TTTensor.random([4] * 8, 8, ctx=ctx)
+    assert rel_err(y.entries(z["d8_probe_pos"]), z["d8_probe_val"]) < REL_TOL
+    assert abs(y.frob_norm() / z["d8_norm"][0] - 1) < REL_TOL
+    a = golden("adf")
+    xg.seed(0xBAADF00D)
+    xg.TTTensor.random([4, 5, 3, 5, 4, 3], 3, ctx=ctx)
+    m = xg.SinglePointMeasurementSet.random(2000, [4, 5, 3, 5, 4, 3])
+    assert np.array_equal(m.positions, a["small_positions"].astype(np.int64))
+
+
+# ------------------------------------------------------------------ dot, norm, move_core, round
+
+def test_dot_and_norm_cfg2(ctx, golden):
+    z = golden("dot")
+    xg.seed(0xBAADF00D)
+    x = xg.TTTensor.random([4] * 32, 64, 0.0, 0.125, ctx=ctx)
+    y = xg.TTTensor.random([4] * 32, 64, 0.0, 0.125, ctx=ctx)
+    assert [1] + x.ranks() + [1] == list(z["cfg2_ranks_x"])
+    assert abs(xg.dot(x, y) / z["cfg2_dot_xy"][0] - 1) < REL_TOL
+    assert abs(x.frob_norm() / z["cfg2_norm_x"][0] - 1) < REL_TOL
+    assert abs(y.frob_norm() / z["cfg2_norm_y"][0] - 1) < REL_TOL
+    assert rel_err(x.entries(z["cfg2_x_probe_pos"]), z["cfg2_x_probe_val"]) < REL_TOL
+    a, b = dev_tt(ctx, tt_of(z, "small_a", False)), dev_tt(ctx, tt_of(z, "small_b", False))
+    assert abs(xg.dot(a, b) / z["small_dot"][0] - 1) < REL_TOL
+    assert abs(a.frob_norm() / np.sqrt(o.tt_dot(tt_of(z, "small_a"), tt_of(z, "small_a"))) - 1) < REL_TOL
+
+
+def test_move_core_qr_and_rank_revealing(ctx, golden):
+    z = golden("movecore")
+    for p in (5, 2, 0, 3):
+        y = dev_tt(ctx, tt_of(z, "x"))
+        y.move_core(p, True)
+        assert y.canonicalized and y.corePosition == p
+        assert rel_err(y.entries(z[f"qr_to{p}_probe_pos"]), z[f"qr_to{p}_probe_val"]) < REL_TOL
+        assert abs(np.linalg.norm(y.get_component(p)) / z[f"qr_to{p}_corenorm"][0] - 1) < REL_TOL
+        cores = y.get_cores()
+        for k in range(p):  # left-orthogonal
+            m = cores[k].reshape(-1, cores[k].shape[2])
+            assert np.allclose(m.T @ m, np.eye(m.shape[1]), atol=1e-12)
+        for k in range(p + 1, len(cores)):  # right-orthogonal
+            m = cores[k].reshape(cores[k].shape[0], -1)
+            assert np.allclose(m @ m.T, np.eye(m.shape[0]), atol=1e-12)
+    # rank-deficient (x + 2x in doubled ranks): the QC rank rule; ranks where the
+    # reference's decision is clear (R_kk exactly at rounding level) must agree
+    # with the oracle run on the same input, entries always
+    zz = tt_of(z, "z", canonicalized=False)
+    for p in (5, 0):
+        y = dev_tt(ctx, zz)
+        y.move_core(p, False)
+        ref = zz.copy()
+        o.move_core(ref, p, keep_rank=False)
+        assert rel_err(y.entries(z[f"qc_to{p}_probe_pos"]), z[f"qc_to{p}_probe_val"]) < 1e-9
+        # every rank is at least the true rank (x's ranks) and at most the representation's
+        assert all(a >= b for a, b in zip(y.ranks(), tt_of(z, "x").ranks))
+        assert all(a <= b for a, b in zip(y.ranks(), zz.ranks))
+
+
+def test_round_cfg2(ctx, golden):
+    r = golden("round")
+    xg.seed(0xBAADF00D)
+    x = xg.TTTensor.random([4] * 32, 64, 0.0, 0.125, ctx=ctx)
+    y = x.copy()
+    spectra = y.round(32, spectra=True)
+    assert [1] + y.ranks() + [1] == list(r["cfg2_round_ranks"])
+    assert rel_err(spectra, r["cfg2_round_spectra"]) < REL_TOL
+    assert abs(y.frob_norm() / r["cfg2_round_norm"][0] - 1) < REL_TOL
+    assert abs(xg.dot(y, x) / r["cfg2_round_dot_x"][0] - 1) < REL_TOL
+    assert rel_err(y.entries(r["cfg2_round_probe_pos"]), r["cfg2_round_probe_val"]) < REL_TOL
+
+
+def test_round_eps_and_max_ranks(ctx, golden):
+    r = golden("round")
+    e = tt_of(r, "eps_in", canonicalized=False)
+    y = dev_tt(ctx, e)
+    sp = y.round(1e-6, spectra=True)
+    assert [1] + y.ranks() + [1] == list(r["eps_round_ranks"])
+    assert rel_err(sp, r["eps_round_spectra"]) < REL_TOL
+    assert rel_err(y.entries(r["eps_round_probe_pos"]), r["eps_round_probe_val"]) < REL_TOL
+    y = dev_tt(ctx, e)
+    y.round([2, 5, 2, 5], 0.0)
+    assert [1] + y.ranks() + [1] == list(r["maxr_round_ranks"])
+    assert rel_err(y.entries(r["maxr_round_probe_pos"]), r["maxr_round_probe_val"]) < REL_TOL
+
+
+# ------------------------------------------------------------------ ALS / DMRG
+
+@pytest.mark.parametrize("tag,x0,b,hs,variant", [
+    ("r8_hs20", "x0", "b", 20, "als"),
+    ("r8_hs3", "x0", "b", 3, "als"),
+    ("r8_asd_hs4", "x0", "b", 4, "asd"),
+    ("r32_hs2", "x0_r32", "b_r32", 2, "als"),
+])
+def test_als_spd_matches_reference(ctx, golden, tag, x0, b, hs, variant):
+    z = golden("als")
+    A, bb, x = dev_op(ctx, op_of(z, "A")), dev_tt(ctx, tt_of(z, b)), dev_tt(ctx, tt_of(z, x0))
+    v = (xg.ASD_SPD if variant == "asd" else xg.ALS_SPD).copy()
+    v.convergenceEpsilon = 0.0
+    perf = xg.PerformanceData()
+    energy = v(A, x, bb, hs, perf)
+    assert abs(energy / z[tag + "_energy"][0] - 1) < REL_TOL
+    assert [1] + x.ranks() + [1] == list(z[tag + "_ranks"])
+    assert rel_err(x.entries(z[tag + "_x_probe_pos"]), z[tag + "_x_probe_val"]) < 1e-9
+    pr = z[tag + "_perf_residual"]
+    mine = np.array(perf.residuals)
+    assert len(mine) == len(pr)
+    keep = pr > 1e-6
+    assert rel_err(mine[keep], pr[keep]) < 1e-9
+    dense = z[tag + "_dense_residual"][0]
+    assert abs(xg.residual(A, x, bb) - dense) <= 1e-9 * max(dense, 1e-3)
+
+
+def test_als_ragged_dims(ctx, golden):
+    z = golden("als")
+    A, b, x = dev_op(ctx, op_of(z, "A_rag")), dev_tt(ctx, tt_of(z, "b_rag")), dev_tt(ctx, tt_of(z, "x0_rag"))
+    v = xg.ALS_SPD.copy()
+    v.convergenceEpsilon = 0.0
+    energy = v(A, x, b, 6)
+    assert abs(energy / z["rag_hs6_energy"][0] - 1) < REL_TOL
+    assert rel_err(x.entries(z["rag_hs6_x_probe_pos"]), z["rag_hs6_x_probe_val"]) < 1e-9
+
+
+def test_als_mixed_precision_matches_fp64(ctx, golden):
+    z = golden("als")
+    A, b = dev_op(ctx, op_of(z, "A")), dev_tt(ctx, tt_of(z, "b_r32"))
+    v = xg.ALS_SPD.copy()
+    v.convergenceEpsilon = 0.0
+    v.precision = xg.MIXED
+    x = dev_tt(ctx, tt_of(z, "x0_r32"))
+    energy = v(A, x, b, 2)
+    assert abs(energy / z["r32_hs2_energy"][0] - 1) < REL_TOL
+    assert rel_err(x.entries(z["r32_hs2_x_probe_pos"]), z["r32_hs2_x_probe_val"]) < 1e-8
+    assert xg.residual(A, x, b) < 1e-10
+
+
+def test_dmrg_spd(ctx, golden):
+    z = golden("dmrg")
+    A, b, x = dev_op(ctx, op_of(z, "A")), dev_tt(ctx, tt_of(z, "b")), dev_tt(ctx, tt_of(z, "x0"))
+    v = xg.DMRG_SPD.copy()
+    v.convergenceEpsilon = 0.0
+    perf = xg.PerformanceData()
+    energy = v(A, x, b, 4, perf)
+    assert abs(energy / z["d8_r4_hs4_energy"][0] - 1) < REL_TOL
+    assert [1] + x.ranks() + [1] == list(z["d8_r4_hs4_ranks"])
+    assert rel_err(x.entries(z["d8_r4_hs4_x_probe_pos"]), z["d8_r4_hs4_x_probe_val"]) < 1e-9
+    assert rel_err(perf.residuals, z["d8_r4_hs4_perf_residual"]) < 1e-8
+
+
+def test_dmrg_spd_potential_d20(ctx, golden):
+    z = golden("dmrg")
+    A, b, x = dev_op(ctx, op_of(z, "A_pot")), dev_tt(ctx, tt_of(z, "b_pot")), dev_tt(ctx, tt_of(z, "x0_pot"))
+    v = xg.DMRG_SPD.copy()
+    v.convergenceEpsilon = 0.0
+    energy = v(A, x, b, 2)
+    assert abs(energy / z["pot_r8_hs2_energy"][0] - 1) < 1e-10
+    assert rel_err(x.entries(z["pot_r8_hs2_x_probe_pos"]), z["pot_r8_hs2_x_probe_val"]) < 1e-9
+
+
+# ------------------------------------------------------------------ ADF and adjoints
+
+def _adf_inputs(ctx, dims, rank, n):
+    xg.seed(0xBAADF00D)
+    target = xg.TTTensor.random(dims, rank, ctx=ctx)
+    m = xg.SinglePointMeasurementSet.random(n, dims)
+    m.measure(target)
+    noise = np.zeros(n)
+    import ctypes
+    xg._lib.load().xtt_random_normal(0.0, 1e-6, n, noise.ctypes.data_as(xg._lib.c_double_p))
+    m.measuredValues = m.measuredValues + noise
+    x = xg.TTTensor.random(dims, rank, ctx=ctx)
+    return target, m, x
+
+
+def test_adf_small(ctx, golden):
+    z = golden("adf")
+    _, m, x = _adf_inputs(ctx, [4, 5, 3, 5, 4, 3], 3, 2000)
+    assert np.array_equal(m.positions, z["small_positions"].astype(np.int64))
+    assert rel_err(m.measuredValues, z["small_values"]) < 1e-12
+    perf = xg.PerformanceData()
+    res = xg.ADFVariant(30, 0.0, 1.0)(x, m, perf)
+    pr = z["small_perf_residual"]
+    assert len(perf.residuals) == len(pr)
+    assert rel_err(perf.residuals[:10], pr[:10]) < 1e-10
+    assert rel_err(perf.residuals, pr) < 1e-7
+    assert abs(res / z["small_final_residual"][0] - 1) < 1e-6
+
+
+def test_adf_cfg5_positions_gradient_and_first_iterations(ctx, golden):
+    z = golden("adf_cfg5")
+    _, m, x = _adf_inputs(ctx, [8] * 10, 6, 200000)
+    assert fnv1a(m.positions) == int(z["cfg5_positions_fnv1a"][0])
+    assert abs(m.measuredValues.sum() / z["cfg5_values_sum"][0] - 1) < 1e-12
+    x0 = host_tt(x)
+    # adjoint: loss gradient vs the oracle's (all cores, no gauge)
+    loss, grads = xg.ADFVariant.gradient(x, m)
+    lo, go = o.adf_loss_gradient(x0, m.positions, m.measuredValues)
+    assert abs(loss / lo - 1) < 1e-10
+    for g, h in zip(grads, go):
+        assert rel_err(g, h) < 1e-10
+    perf = xg.PerformanceData()
+    xg.ADFVariant(5, 0.0, 1.0)(x, m, perf)
+    assert rel_err(perf.residuals, z["cfg5_perf_residual"][:5]) < 1e-9
+
+
+def test_adf_gradient_central_differences(ctx):
+    xg.seed(7)
+    dims = [3, 4, 3, 2]
+    x = xg.TTTensor.random(dims, 2, ctx=ctx)
+    target = xg.TTTensor.random(dims, 2, ctx=ctx)
+    m = xg.SinglePointMeasurementSet.random(40, dims)
+    m.measure(target)
+    loss, grads = xg.ADFVariant.gradient(x, m)
+    cores = x.get_cores()
+    h = 1e-4
+    for k in range(len(cores)):
+        fd = np.zeros_like(cores[k])
+        for idx in np.ndindex(cores[k].shape):
+            for sgn in (+1, -1):
+                c = [cc.copy() for cc in cores]
+                c[k][idx] += sgn * h
+                xt = o.TT(c)
+                r = o.tt_entries(xt, m.positions) - m.measuredValues
+                fd[idx] += sgn * 0.5 * float(r @ r) / (2 * h)
+        assert rel_err(grads[k], fd) < 1e-6
+
+
+def test_als_energy_gradient(ctx, golden):
+    z = golden("als")
+    Ah, bh, xh = op_of(z, "A"), tt_of(z, "b"), tt_of(z, "x0")
+    A, b, x = dev_op(ctx, Ah), dev_tt(ctx, bh), dev_tt(ctx, xh)
+    J, grads = xg.als_energy_gradient(A, x, b)
+    Ax = o.op_apply(Ah, xh)
+    assert abs(J / (o.tt_dot(xh, Ax) - 2 * o.tt_dot(xh, bh)) - 1) < 1e-10
+    # directional derivative along a random core perturbation
+    rng = np.random.default_rng(3)
+    k = 3
+    dx = rng.standard_normal(xh.cores[k].shape)
+    h = 1e-6
+    vals = []
+    for s in (+1, -1):
+        c = [cc.copy() for cc in xh.cores]
+        c[k] = c[k] + s * h * dx
+        xt = o.TT(c)
+        vals.append(o.tt_dot(xt, o.op_apply(Ah, xt)) - 2 * o.tt_dot(xt, bh))
+    fd = (vals[0] - vals[1]) / (2 * h)
+    assert abs(float(np.sum(grads[k] * dx)) / fd - 1) < 1e-6

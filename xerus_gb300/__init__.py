@@ -1,0 +1,459 @@
+"""xerus_gb300: the xerus Tensor-Train sweep path on a GB300, behind xerus's API.
+
+TT tensors and operators live on the GPU (one CUDA device per Context); every
+operation runs through the C ABI of libxtt.so (include/xtt.h). The names mirror
+xerus's Python bindings (src/xerus/python/*.cpp): TTTensor, TTOperator,
+frob_norm, TTTensor.random, move_core, round, ALS_SPD / DMRG_SPD / ASD_SPD
+(ALSVariant), ADF (ADFVariant) and SinglePointMeasurementSet.
+
+There is no CPU fallback: without the built library or a GPU, calls raise.
+"""
+import ctypes
+
+import numpy as np
+
+from . import _lib as L
+
+__all__ = ["Context", "TTTensor", "TTOperator", "frob_norm", "dot", "residual", "ALSVariant", "ALS_SPD", "DMRG_SPD",
+           "ASD_SPD", "ADFVariant", "ADF", "SinglePointMeasurementSet", "PerformanceData", "seed", "EPSILON",
+           "XttError", "FP64", "MIXED"]
+
+EPSILON = 8 * np.finfo(np.float64).eps  # include/xerus/basic.h:50
+FP64, MIXED = 0, 1
+XttError = L.XttError
+INT64_MAX = np.iinfo(np.int64).max
+
+
+def _i64(a):
+    a = np.ascontiguousarray(np.asarray(a, dtype=np.int64))
+    return a, a.ctypes.data_as(L.c_int64_p)
+
+
+def _f64(a):
+    a = np.ascontiguousarray(np.asarray(a, dtype=np.float64))
+    return a, a.ctypes.data_as(L.c_double_p)
+
+
+class Context:
+    """One CUDA device and stream (xtt_context)."""
+
+    _default = None
+
+    def __init__(self, device=0):
+        self.lib = L.load()
+        h = ctypes.c_void_p()
+        L.check(self.lib.xtt_context_create(int(device), ctypes.byref(h)))
+        self.handle = h
+
+    @classmethod
+    def default(cls):
+        if cls._default is None:
+            cls._default = Context(0)
+        return cls._default
+
+    def synchronize(self):
+        L.check(self.lib.xtt_context_synchronize(self.handle))
+
+    def kernel_launches(self):
+        v = ctypes.c_int64()
+        L.check(self.lib.xtt_context_kernel_launches(self.handle, ctypes.byref(v)))
+        return v.value
+
+    def set_stream(self, stream_ptr):
+        L.check(self.lib.xtt_context_set_stream(self.handle, ctypes.c_void_p(stream_ptr)))
+
+    def __del__(self):
+        if getattr(self, "handle", None):
+            self.lib.xtt_context_destroy(self.handle)
+            self.handle = None
+
+
+def seed(value=0xBAADF00D):
+    """Reseeds the library's engine (xerus::misc::randomEngine.seed) and resets its normal distribution."""
+    L.check(L.load().xtt_random_seed(int(value)))
+
+
+class _TT:
+    is_operator = False
+
+    def __init__(self, dims=None, ranks=None, ctx=None, _handle=None):
+        self.ctx = ctx or Context.default()
+        self.lib = self.ctx.lib
+        if _handle is not None:
+            self.handle = _handle
+            return
+        dims = list(dims)
+        if ranks is None:
+            ranks = [1] * (len(dims) + 1)
+        d, pd = _i64(dims)
+        r, pr = _i64(ranks)
+        h = ctypes.c_void_p()
+        L.check(self.lib.xtt_tensor_create(self.ctx.handle, int(self.is_operator), len(dims), pd, pr, ctypes.byref(h)))
+        self.handle = h
+
+    def __del__(self):
+        if getattr(self, "handle", None):
+            self.lib.xtt_tensor_destroy(self.handle)
+            self.handle = None
+
+    # -- shape
+    def degree(self):
+        v = ctypes.c_int64()
+        L.check(self.lib.xtt_tensor_order(self.handle, ctypes.byref(v)))
+        return v.value
+
+    @property
+    def dimensions(self):
+        d = self.degree()
+        out = np.zeros(d, dtype=np.int64)
+        L.check(self.lib.xtt_tensor_dims(self.handle, out.ctypes.data_as(L.c_int64_p)))
+        return [int(v) for v in out]
+
+    def all_ranks(self):
+        out = np.zeros(self.degree() + 1, dtype=np.int64)
+        L.check(self.lib.xtt_tensor_ranks(self.handle, out.ctypes.data_as(L.c_int64_p)))
+        return [int(v) for v in out]
+
+    def ranks(self):
+        return self.all_ranks()[1:-1]
+
+    def size(self):
+        v = ctypes.c_int64()
+        L.check(self.lib.xtt_tensor_size(self.handle, ctypes.byref(v)))
+        return v.value
+
+    @property
+    def canonicalized(self):
+        c, p = ctypes.c_int(), ctypes.c_int64()
+        L.check(self.lib.xtt_tensor_get_canonical(self.handle, ctypes.byref(c), ctypes.byref(p)))
+        return bool(c.value)
+
+    @property
+    def corePosition(self):
+        c, p = ctypes.c_int(), ctypes.c_int64()
+        L.check(self.lib.xtt_tensor_get_canonical(self.handle, ctypes.byref(c), ctypes.byref(p)))
+        return p.value
+
+    def assume_core_position(self, pos):
+        L.check(self.lib.xtt_tensor_set_canonical(self.handle, 1, int(pos)))
+
+    def set_canonical(self, canonicalized, pos=0):
+        L.check(self.lib.xtt_tensor_set_canonical(self.handle, int(bool(canonicalized)), int(pos)))
+
+    # -- data
+    def get_flat(self):
+        out = np.zeros(self.size())
+        L.check(self.lib.xtt_tensor_get_cores(self.handle, out.ctypes.data_as(L.c_double_p), out.size))
+        return out
+
+    def set_flat(self, data, ranks=None):
+        a, pa = _f64(data)
+        if ranks is None:
+            L.check(self.lib.xtt_tensor_set_cores(self.handle, pa, a.size))
+        else:
+            r, pr = _i64(ranks)
+            L.check(self.lib.xtt_tensor_assign(self.handle, pr, pa, a.size))
+
+    def _core_shape(self, k, r):
+        n = self.dimensions[k]
+        return (r[k], n, n, r[k + 1]) if self.is_operator else (r[k], n, r[k + 1])
+
+    def get_cores(self):
+        flat, r = self.get_flat(), self.all_ranks()
+        out, off = [], 0
+        for k in range(self.degree()):
+            shp = self._core_shape(k, r)
+            sz = int(np.prod(shp))
+            out.append(flat[off:off + sz].reshape(shp).copy())
+            off += sz
+        return out
+
+    def set_cores(self, cores):
+        r = [1] + [int(c.shape[-1]) for c in cores]
+        self.set_flat(np.concatenate([np.asarray(c, dtype=np.float64).ravel() for c in cores]), ranks=r)
+
+    def get_component(self, k):
+        return self.get_cores()[k]
+
+    def copy(self):
+        h = ctypes.c_void_p()
+        L.check(self.lib.xtt_tensor_copy(self.handle, ctypes.byref(h)))
+        return type(self)(ctx=self.ctx, _handle=h)
+
+    def __imul__(self, f):
+        L.check(self.lib.xtt_tensor_scale(self.handle, float(f)))
+        return self
+
+    def __itruediv__(self, f):
+        return self.__imul__(1.0 / f)
+
+    # -- TTNetwork operations
+    def move_core(self, position, keepRank=False):
+        L.check(self.lib.xtt_move_core(self.handle, int(position), int(bool(keepRank))))
+
+    def canonicalize_left(self):
+        self.move_core(0)
+
+    def canonicalize_right(self):
+        self.move_core(self.degree() - 1)
+
+    def round(self, arg, eps=None, spectra=False):
+        """round(maxRanks: list, eps=EPSILON) | round(maxRank: int) | round(eps: float)
+        (include/xerus/ttNetwork.h:352-373)."""
+        d = self.degree()
+        if isinstance(arg, (float, np.floating)):
+            mr, e = [INT64_MAX] * (d - 1), float(arg)
+        elif isinstance(arg, (int, np.integer)):
+            if int(arg) <= 0:
+                raise ValueError("MaxRank must be positive")
+            mr, e = [int(arg)] * (d - 1), EPSILON
+        else:
+            mr, e = [int(v) for v in arg], EPSILON if eps is None else float(eps)
+        m, pm = _i64(mr if d > 1 else [0])
+        cap = sum(self.all_ranks()) * 4 + 16
+        sp = np.zeros(cap)
+        cnt = ctypes.c_int64()
+        L.check(self.lib.xtt_round(self.handle, pm, e, sp.ctypes.data_as(L.c_double_p) if spectra else None, cap,
+                                   ctypes.byref(cnt)))
+        return sp[:cnt.value].copy() if spectra else None
+
+    def frob_norm(self):
+        v = ctypes.c_double()
+        L.check(self.lib.xtt_frob_norm(self.handle, ctypes.byref(v)))
+        return v.value
+
+
+class TTTensor(_TT):
+    """xerus::TTTensor on the device."""
+
+    @staticmethod
+    def random(dims, ranks, mean=0.0, stddev=1.0, ctx=None):
+        """TTNetwork::random(dims, ranks, dist=N(mean, stddev)) (include/xerus/ttNetwork.h:128-169)."""
+        ctx = ctx or Context.default()
+        dims = list(dims)
+        if isinstance(ranks, (int, np.integer)):
+            ranks = [int(ranks)] * (len(dims) - 1)
+        d, pd = _i64(dims)
+        r, pr = _i64(list(ranks) if ranks else [1])
+        h = ctypes.c_void_p()
+        L.check(ctx.lib.xtt_tensor_random(ctx.handle, len(dims), pd, pr, float(mean), float(stddev), ctypes.byref(h)))
+        return TTTensor(ctx=ctx, _handle=h)
+
+    @staticmethod
+    def from_cores(cores, ctx=None, canonicalized=False, core_position=0):
+        dims = [int(c.shape[1]) for c in cores]
+        t = TTTensor(dims, [1] + [int(c.shape[2]) for c in cores], ctx=ctx)
+        t.set_cores(cores)
+        t.set_canonical(canonicalized, core_position)
+        return t
+
+    def entries(self, positions):
+        pos, pp = _i64(positions)
+        out = np.zeros(pos.shape[0])
+        L.check(self.lib.xtt_entries(self.handle, pp, pos.shape[0], out.ctypes.data_as(L.c_double_p)))
+        return out
+
+
+class TTOperator(_TT):
+    """xerus::TTOperator on the device (cores (R_{k-1}, n, n, R_k))."""
+
+    is_operator = True
+
+    @staticmethod
+    def from_cores(cores, ctx=None):
+        dims = [int(c.shape[1]) for c in cores]
+        t = TTOperator(dims, [1] + [int(c.shape[3]) for c in cores], ctx=ctx)
+        t.set_cores(cores)
+        return t
+
+
+def frob_norm(x):
+    return x.frob_norm()
+
+
+def dot(x, y):
+    """value_t(x(i&0) * y(i&0))."""
+    v = ctypes.c_double()
+    L.check(x.lib.xtt_dot(x.handle, y.handle, ctypes.byref(v)))
+    return v.value
+
+
+def residual(A, x, b):
+    """||A x - b|| / ||b|| in FP64 (no cancellation)."""
+    v = ctypes.c_double()
+    L.check(x.lib.xtt_residual(A.handle, x.handle, b.handle, ctypes.byref(v)))
+    return v.value
+
+
+class PerformanceData:
+    """The parts of xerus::PerformanceData the sweep fills (include/xerus/performanceData.h)."""
+
+    def __init__(self, active=True):
+        self.active = active
+        self.residuals, self.flags, self.energies = [], [], []
+
+    def __bool__(self):
+        return self.active
+
+
+class ALSVariant:
+    """xerus::ALSVariant for SPD operators (include/xerus/algorithms/als.h:37-207)."""
+
+    FLAG_FINISHED_HALFSWEEP = 1
+    FLAG_FINISHED_FULLSWEEP = 3
+
+    def __init__(self, sites, numHalfSweeps, localSolver, assumeSPD, useResidual=False):
+        self.sites = sites
+        self.numHalfSweeps = numHalfSweeps
+        self.convergenceEpsilon = 1e-6
+        self.useResidualForEndCriterion = useResidual
+        self.preserveCorePosition = True
+        self.assumeSPD = assumeSPD
+        self.localSolver = localSolver  # "lapack" (exact) or "asd"
+        self.precision = FP64
+        self.local_tolerance = 1e-13
+        self.local_max_iterations = 0
+        self.residual_target = 0.0
+        self.max_rank = 0
+        self.svd_epsilon = 0.0
+        self.exact_environment = False
+        self.last_report = None
+
+    def copy(self):
+        v = ALSVariant(self.sites, self.numHalfSweeps, self.localSolver, self.assumeSPD, self.useResidualForEndCriterion)
+        v.__dict__.update({k: val for k, val in self.__dict__.items() if k != "last_report"})
+        return v
+
+    def options(self, num_half_sweeps, eps, record):
+        o = L.AlsOptions()
+        L.check(L.load().xtt_als_default_options(ctypes.byref(o)))
+        o.sites = self.sites
+        o.local_solver = 1 if self.localSolver == "asd" else 0
+        o.preserve_core_position = int(self.preserveCorePosition)
+        o.precision = int(self.precision)
+        o.num_half_sweeps = int(num_half_sweeps)
+        o.convergence_epsilon = float(eps)
+        o.local_tolerance = float(self.local_tolerance)
+        o.local_max_iterations = int(self.local_max_iterations)
+        o.residual_target = float(self.residual_target)
+        o.record_residuals = int(bool(record))
+        o.max_rank = int(self.max_rank)
+        o.svd_epsilon = float(self.svd_epsilon)
+        o.exact_environment = int(bool(self.exact_environment))
+        return o
+
+    def __call__(self, A, x, b, arg=None, perfData=None):
+        """ALS(A, x, b[, numHalfSweeps: int | convergenceEpsilon: float][, perfData]) -> energy."""
+        if not self.assumeSPD:
+            raise NotImplementedError("only the SPD variants (ALS_SPD, DMRG_SPD, ASD_SPD) run on the device")
+        if isinstance(arg, PerformanceData):
+            arg, perfData = None, arg
+        hs, eps = self.numHalfSweeps, self.convergenceEpsilon
+        if isinstance(arg, (int, np.integer)):
+            hs = int(arg)
+        elif isinstance(arg, (float, np.floating)):
+            eps = float(arg)
+        record = bool(perfData)
+        o = self.options(hs, eps, record)
+        rep = L.AlsReport()
+        cap = 4096
+        res, flags, en = np.zeros(cap), np.zeros(cap, dtype=np.int64), np.zeros(cap)
+        L.check(x.lib.xtt_als(A.handle, x.handle, b.handle, ctypes.byref(o), ctypes.byref(rep),
+                              res.ctypes.data_as(L.c_double_p), flags.ctypes.data_as(L.c_int64_p),
+                              en.ctypes.data_as(L.c_double_p), cap))
+        self.last_report = rep
+        if perfData is not None and record:
+            n = min(rep.micro_steps + 1, cap)
+            perfData.residuals = list(res[:n])
+            perfData.flags = list(flags[:n])
+            perfData.energies = list(en[:rep.half_sweeps])
+        return rep.energy
+
+
+ALS_SPD = ALSVariant(1, 0, "lapack", True)
+DMRG_SPD = ALSVariant(2, 0, "lapack", True)
+ASD_SPD = ALSVariant(1, 0, "asd", True)
+
+
+class SinglePointMeasurementSet:
+    """xerus::SinglePointMeasurementSet (include/xerus/measurments.h:43-91)."""
+
+    def __init__(self, positions=None, measuredValues=None):
+        self.positions = np.zeros((0, 0), dtype=np.int64) if positions is None else np.asarray(positions, dtype=np.int64)
+        self.measuredValues = np.zeros(0) if measuredValues is None else np.asarray(measuredValues, dtype=np.float64)
+
+    @staticmethod
+    def random(num, dims):
+        dims = [int(v) for v in dims]
+        out = np.zeros((int(num), len(dims)), dtype=np.int64)
+        d, pd = _i64(dims)
+        L.check(L.load().xtt_random_positions(int(num), len(dims), pd, out.ctypes.data_as(L.c_int64_p)))
+        return SinglePointMeasurementSet(out, np.zeros(int(num)))
+
+    def size(self):
+        return int(self.positions.shape[0])
+
+    def degree(self):
+        return int(self.positions.shape[1]) if self.positions.ndim == 2 else 0
+
+    def measure(self, tt):
+        self.measuredValues = tt.entries(self.positions)
+
+    def frob_norm(self):
+        return float(np.sqrt(np.sum(self.measuredValues ** 2)))
+
+
+class ADFVariant:
+    """xerus::ADFVariant (include/xerus/algorithms/adf.h:39-266) for single-point samples."""
+
+    def __init__(self, maxIterations, targetResidualNorm, minimalResidualNormDecrease):
+        self.maxIterations = maxIterations
+        self.targetResidualNorm = targetResidualNorm
+        self.minimalResidualNormDecrease = minimalResidualNormDecrease
+
+    def __call__(self, x, measurements, perfData=None):
+        pos, pp = _i64(measurements.positions)
+        val, pv = _f64(measurements.measuredValues)
+        o = L.AdfOptions(int(self.maxIterations), float(self.targetResidualNorm),
+                         float(self.minimalResidualNormDecrease))
+        cap = max(16, int(self.maxIterations) + 2 if self.maxIterations else 100000)
+        trace = np.zeros(cap)
+        fin, cnt = ctypes.c_double(), ctypes.c_int64()
+        L.check(x.lib.xtt_adf(x.handle, pp, pv, pos.shape[0], ctypes.byref(o), ctypes.byref(fin),
+                              trace.ctypes.data_as(L.c_double_p), cap, ctypes.byref(cnt)))
+        if perfData is not None:
+            perfData.residuals = list(trace[:min(cnt.value, cap)])
+        return fin.value
+
+    @staticmethod
+    def gradient(x, measurements):
+        """(0.5 ||P(x) - y||^2, [dL/dX_k]) for every core."""
+        pos, pp = _i64(measurements.positions)
+        val, pv = _f64(measurements.measuredValues)
+        g = np.zeros(x.size())
+        loss = ctypes.c_double()
+        L.check(x.lib.xtt_adf_gradient(x.handle, pp, pv, pos.shape[0], ctypes.byref(loss),
+                                       g.ctypes.data_as(L.c_double_p), g.size))
+        return loss.value, _split(g, x)
+
+
+def _split(flat, x):
+    r, dims, out, off = x.all_ranks(), x.dimensions, [], 0
+    for k in range(len(dims)):
+        shp = (r[k], dims[k], r[k + 1])
+        sz = int(np.prod(shp))
+        out.append(flat[off:off + sz].reshape(shp).copy())
+        off += sz
+    return out
+
+
+def als_energy_gradient(A, x, b):
+    """(J, [dJ/dX_k]) for J(x) = <x, A x> - 2 <x, b>."""
+    g = np.zeros(x.size())
+    e = ctypes.c_double()
+    L.check(x.lib.xtt_als_energy_gradient(A.handle, x.handle, b.handle, ctypes.byref(e),
+                                          g.ctypes.data_as(L.c_double_p), g.size))
+    return e.value, _split(g, x)
+
+
+ADF = ADFVariant(0, 1e-8, 0.999)

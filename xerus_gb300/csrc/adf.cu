@@ -1,0 +1,466 @@
+// ADF tensor completion for single-point measurement sets
+// (src/xerus/algorithms/adf.cpp, include/xerus/algorithms/adf.h) on the device.
+//
+// The reference keeps, per sample, a forward stack F_k (contraction of cores
+// 0..k at the sample's indices) and a backward stack B_k (cores k..d-1),
+// deduplicated over shared prefixes/suffixes (adf.cpp:102-191), and updates
+// them with one tiny GEMV per unique entry under OpenMP. Here every stack
+// level is one dense array of r x N doubles stored mode-major (entry a of
+// sample s at a*N + s) so that consecutive threads touch consecutive samples;
+// a level update is one pass over the samples (HBM-bound). Deduplication only
+// shares identical arithmetic, so dropping it changes no value.
+//
+// Per core position k the sweep needs (adf.cpp:524-539):
+//   res_s   = y_s - F_{k-1}[s]^T X_k[:, i_s, :] B_{k+1}[s]          (calculate_residual)
+//   G[:,i,:] = sum_{s: i_s = i} res_s F_{k-1}[s] (x) B_{k+1}[s]       (calculate_projected_gradient)
+//   nrm_i   = sum_{s: i_s = i} (F_{k-1}[s]^T G[:, i_s, :] B_{k+1}[s])^2 (calculate_slicewise_norm_A_projGrad)
+//   X_k[:, i, :] += (||G_i||^2 / nrm_i) G_i                           (update_x)
+// The gradient and slice norms are reduced deterministically: each warp
+// accumulates its contiguous chunk of samples in registers in a fixed order,
+// and the per-warp partials are summed in a fixed order by a second kernel.
+#include <algorithm>
+#include <cfloat>
+#include <cmath>
+
+#include "engine.cuh"
+
+namespace xtt {
+
+constexpr int kAdfThreads = 256;
+constexpr int kAdfWarpsPerBlock = kAdfThreads / 32;
+constexpr int kAdfMaxR = 8;        // fast path: ranks <= 8
+constexpr int kAdfMaxSlices = 16;  // fast path: mode sizes <= 16
+constexpr int kAdfPairsPerLane = 2;  // r0 * r1 <= 64
+
+struct AdfLevel {
+	const int* pos;     // indices of this mode, N ints
+	const double* F;    // F_{k-1}: r0 x N (nullptr: the constant 1)
+	const double* B;    // B_{k+1}: r1 x N (nullptr: the constant 1)
+	const double* X;    // core (r0, n, r1)
+	int r0, n, r1;
+	long long N;
+};
+
+// res_s (optional write), and per-warp partials of G (r0, n, r1) and of sum res^2.
+// mode 0: res_s = y_s - <F, X_i B>; mode 1: res_s given in `res` (read only).
+__global__ void __launch_bounds__(kAdfThreads) k_adf_res_grad(AdfLevel L, const double* y, double* res, int mode,
+                                                               double* gpart, double* rrpart, long long chunk) {
+	__shared__ double Xs[kAdfMaxR * kAdfMaxSlices * kAdfMaxR];
+	const int lane = threadIdx.x & 31;
+	const long long warp = (long long)blockIdx.x * kAdfWarpsPerBlock + (threadIdx.x >> 5);
+	const int r0 = L.r0, n = L.n, r1 = L.r1, P = r0 * r1;
+	for (int e = threadIdx.x; e < r0 * n * r1; e += blockDim.x) Xs[e] = L.X[e];
+	__syncthreads();
+	double acc[kAdfMaxSlices][kAdfPairsPerLane];
+#pragma unroll
+	for (int i = 0; i < kAdfMaxSlices; ++i)
+#pragma unroll
+		for (int t = 0; t < kAdfPairsPerLane; ++t) acc[i][t] = 0.0;
+	double rr = 0.0;
+	const long long s0 = warp * chunk, s1 = min(L.N, s0 + chunk);
+	for (long long base = s0; base < s1; base += 32) {
+		const long long s = base + lane;
+		const bool valid = s < s1;
+		double f[kAdfMaxR], b[kAdfMaxR];
+		int idx = 0;
+		double rs = 0.0;
+		if (valid) {
+			idx = L.pos[s];
+#pragma unroll
+			for (int a = 0; a < kAdfMaxR; ++a) f[a] = (a < r0) ? (L.F ? L.F[a * L.N + s] : 1.0) : 0.0;
+#pragma unroll
+			for (int c = 0; c < kAdfMaxR; ++c) b[c] = (c < r1) ? (L.B ? L.B[c * L.N + s] : 1.0) : 0.0;
+			if (mode == 0) {
+				double v = 0.0;
+				for (int a = 0; a < r0; ++a) {
+					double t = 0.0;
+					const double* xr = Xs + (a * n + idx) * r1;
+					for (int c = 0; c < r1; ++c) t += xr[c] * b[c];
+					v += f[a] * t;
+				}
+				rs = y[s] - v;
+				res[s] = rs;
+			} else {
+				rs = res[s];
+			}
+			rr += rs * rs;
+		}
+		// broadcast each of the 32 samples and accumulate its outer product
+		const int cnt = int((s1 - base) < 32 ? (s1 - base) : 32);
+		for (int j = 0; j < cnt; ++j) {
+			const int ij = __shfl_sync(0xffffffffu, idx, j);
+			const double rj = __shfl_sync(0xffffffffu, rs, j);
+			double fj[kAdfMaxR], bj[kAdfMaxR];
+#pragma unroll
+			for (int a = 0; a < kAdfMaxR; ++a) fj[a] = __shfl_sync(0xffffffffu, f[a], j);
+#pragma unroll
+			for (int c = 0; c < kAdfMaxR; ++c) bj[c] = __shfl_sync(0xffffffffu, b[c], j);
+#pragma unroll
+			for (int t = 0; t < kAdfPairsPerLane; ++t) {
+				const int p = lane + 32 * t;
+				if (p < P) {
+					const int a = p / r1, c = p - a * r1;
+					double fa = 0, bc = 0;
+#pragma unroll
+					for (int q = 0; q < kAdfMaxR; ++q) {
+						fa = (q == a) ? fj[q] : fa;
+						bc = (q == c) ? bj[q] : bc;
+					}
+					const double contrib = rj * fa * bc;
+#pragma unroll
+					for (int i = 0; i < kAdfMaxSlices; ++i) acc[i][t] += (i == ij) ? contrib : 0.0;
+				}
+			}
+		}
+	}
+	// per-warp partials: G stored (r0, n, r1)
+	double* gp = gpart + warp * (long long)r0 * n * r1;
+#pragma unroll
+	for (int t = 0; t < kAdfPairsPerLane; ++t) {
+		const int p = lane + 32 * t;
+		if (p < P) {
+			const int a = p / r1, c = p - a * r1;
+			for (int i = 0; i < n; ++i) gp[(a * n + i) * r1 + c] = acc[i][t];
+		}
+	}
+	rr = warp_sum(rr);
+	if (lane == 0 && rrpart) rrpart[warp] = rr;
+}
+
+// Generic (slow) path for shapes beyond the fast path: residual per sample,
+// then one thread per gradient entry summing over all samples in order.
+__global__ void k_adf_res_generic(AdfLevel L, const double* y, double* res) {
+	for (long long s = blockIdx.x * (long long)blockDim.x + threadIdx.x; s < L.N; s += (long long)gridDim.x * blockDim.x) {
+		const int idx = L.pos[s];
+		double v = 0.0;
+		for (int a = 0; a < L.r0; ++a) {
+			double t = 0.0;
+			for (int c = 0; c < L.r1; ++c) t += L.X[(a * L.n + idx) * L.r1 + c] * (L.B ? L.B[c * L.N + s] : 1.0);
+			v += (L.F ? L.F[a * L.N + s] : 1.0) * t;
+		}
+		res[s] = y[s] - v;
+	}
+}
+
+__global__ void k_adf_grad_generic(AdfLevel L, const double* res, double* G) {
+	const int total = L.r0 * L.n * L.r1;
+	for (int e = blockIdx.x * blockDim.x + threadIdx.x; e < total; e += gridDim.x * blockDim.x) {
+		const int c = e % L.r1, i = (e / L.r1) % L.n, a = e / (L.r1 * L.n);
+		double s = 0.0;
+		for (long long q = 0; q < L.N; ++q)
+			if (L.pos[q] == i) s += res[q] * (L.F ? L.F[a * L.N + q] : 1.0) * (L.B ? L.B[c * L.N + q] : 1.0);
+		G[e] = s;
+	}
+}
+
+// sum of `parts` partial arrays of length len, in order
+__global__ void k_sum_parts(const double* part, long long parts, int len, double* out, double scale) {
+	for (int e = blockIdx.x * blockDim.x + threadIdx.x; e < len; e += gridDim.x * blockDim.x) {
+		double s = 0.0;
+		for (long long p = 0; p < parts; ++p) s += part[p * len + e];
+		out[e] = scale * s;
+	}
+}
+
+// slice norms: nrm_i = sum_{s: i_s = i} (F[s]^T G[:, i_s, :] B[s])^2, per-warp partials (n values)
+__global__ void __launch_bounds__(kAdfThreads) k_adf_slicenorm(AdfLevel L, const double* G, double* npart,
+                                                                long long chunk) {
+	__shared__ double Gs[kAdfMaxR * kAdfMaxSlices * kAdfMaxR];
+	const int lane = threadIdx.x & 31;
+	const long long warp = (long long)blockIdx.x * kAdfWarpsPerBlock + (threadIdx.x >> 5);
+	const int r0 = L.r0, n = L.n, r1 = L.r1;
+	for (int e = threadIdx.x; e < r0 * n * r1; e += blockDim.x) Gs[e] = G[e];
+	__syncthreads();
+	double acc[kAdfMaxSlices];
+#pragma unroll
+	for (int i = 0; i < kAdfMaxSlices; ++i) acc[i] = 0.0;
+	const long long s0 = warp * chunk, s1 = min(L.N, s0 + chunk);
+	for (long long s = s0 + lane; s < s1; s += 32) {
+		const int idx = L.pos[s];
+		double v = 0.0;
+		for (int a = 0; a < r0; ++a) {
+			double t = 0.0;
+			const double* gr = Gs + (a * n + idx) * r1;
+			for (int c = 0; c < r1; ++c) t += gr[c] * (L.B ? L.B[c * L.N + s] : 1.0);
+			v += (L.F ? L.F[a * L.N + s] : 1.0) * t;
+		}
+		const double v2 = v * v;
+#pragma unroll
+		for (int i = 0; i < kAdfMaxSlices; ++i) acc[i] += (i == idx) ? v2 : 0.0;
+	}
+#pragma unroll
+	for (int i = 0; i < kAdfMaxSlices; ++i) acc[i] = warp_sum(acc[i]);
+	if (lane == 0)
+		for (int i = 0; i < n; ++i) npart[warp * n + i] = acc[i];
+}
+
+__global__ void k_adf_slicenorm_generic(AdfLevel L, const double* G, double* nrm) {
+	for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < L.n; i += gridDim.x * blockDim.x) {
+		double s = 0.0;
+		for (long long q = 0; q < L.N; ++q) {
+			if (L.pos[q] != i) continue;
+			double v = 0.0;
+			for (int a = 0; a < L.r0; ++a) {
+				double t = 0.0;
+				for (int c = 0; c < L.r1; ++c) t += G[(a * L.n + i) * L.r1 + c] * (L.B ? L.B[c * L.N + q] : 1.0);
+				v += (L.F ? L.F[a * L.N + q] : 1.0) * t;
+			}
+			s += v * v;
+		}
+		nrm[i] = s;
+	}
+}
+
+// X[:, j, :] += (||G_j||^2 / nrm_j) G_j   (update_x, adf.cpp:468-478); one block
+__global__ void k_adf_update(double* X, const double* G, const double* nrm, int r0, int n, int r1) {
+	__shared__ double sc[32];
+	for (int j = 0; j < n; ++j) {
+		double s = 0.0;
+		for (int e = threadIdx.x; e < r0 * r1; e += blockDim.x) {
+			const int a = e / r1, c = e % r1;
+			const double g = G[(a * n + j) * r1 + c];
+			s += g * g;
+		}
+		const double pyr = block_sum(s, sc);
+		const double step = pyr / nrm[j];
+		for (int e = threadIdx.x; e < r0 * r1; e += blockDim.x) {
+			const int a = e / r1, c = e % r1;
+			X[(a * n + j) * r1 + c] += step * G[(a * n + j) * r1 + c];
+		}
+		__syncthreads();
+	}
+}
+
+// F_k[b][s] = sum_a F_{k-1}[a][s] X[a, i_s, b]
+__global__ void k_adf_forward(const int* pos, const double* Fp, const double* X, double* Fo, int r0, int n, int r1,
+                              long long N) {
+	extern __shared__ double Xs[];
+	for (int e = threadIdx.x; e < r0 * n * r1; e += blockDim.x) Xs[e] = X[e];
+	__syncthreads();
+	for (long long s = blockIdx.x * (long long)blockDim.x + threadIdx.x; s < N; s += (long long)gridDim.x * blockDim.x) {
+		const int idx = pos[s];
+		for (int b = 0; b < r1; ++b) {
+			double v = 0.0;
+			for (int a = 0; a < r0; ++a) v += (Fp ? Fp[a * N + s] : 1.0) * Xs[(a * n + idx) * r1 + b];
+			Fo[b * N + s] = v;
+		}
+	}
+}
+
+// B_k[a][s] = sum_b X[a, i_s, b] B_{k+1}[b][s]
+__global__ void k_adf_backward(const int* pos, const double* Bn, const double* X, double* Bo, int r0, int n, int r1,
+                               long long N) {
+	extern __shared__ double Xs[];
+	for (int e = threadIdx.x; e < r0 * n * r1; e += blockDim.x) Xs[e] = X[e];
+	__syncthreads();
+	for (long long s = blockIdx.x * (long long)blockDim.x + threadIdx.x; s < N; s += (long long)gridDim.x * blockDim.x) {
+		const int idx = pos[s];
+		for (int a = 0; a < r0; ++a) {
+			double v = 0.0;
+			for (int b = 0; b < r1; ++b) v += Xs[(a * n + idx) * r1 + b] * (Bn ? Bn[b * N + s] : 1.0);
+			Bo[a * N + s] = v;
+		}
+	}
+}
+
+namespace {
+
+struct AdfData {
+	Context& c;
+	Tensor& x;
+	int d;
+	long long N;
+	int* pos = nullptr;  // d x N (mode-major)
+	double* y = nullptr;
+	double* res = nullptr;
+	std::vector<double*> F, B;  // F[k]: r_{k+1} x N ; B[k]: r_k x N
+	double *gpart = nullptr, *npart = nullptr, *rrpart = nullptr, *G = nullptr, *nrm = nullptr, *rr = nullptr;
+	long long warps = 0, chunk = 0;
+	bool fast = true;
+
+	AdfData(Context& cc, Tensor& xx, const int64_t* positions, const double* values, long long n)
+	    : c(cc), x(xx), d(xx.d), N(n) {
+		std::vector<int> hp(size_t(d) * N);
+		for (long long s = 0; s < N; ++s)
+			for (int k = 0; k < d; ++k) {
+				const int64_t v = positions[s * d + k];
+				XTT_REQUIRE(v >= 0 && v < x.dims[k], "measurement position out of range");
+				hp[size_t(k) * N + s] = int(v);
+			}
+		pos = c.scratch<int>(S_ADF_FIRST + 0, hp.size());
+		y = c.scratch<double>(S_ADF_FIRST + 1, N);
+		res = c.scratch<double>(S_ADF_FIRST + 2, N);
+		XTT_CUDA(cudaMemcpyAsync(pos, hp.data(), hp.size() * sizeof(int), cudaMemcpyHostToDevice, c.stream));
+		XTT_CUDA(cudaMemcpyAsync(y, values, N * sizeof(double), cudaMemcpyHostToDevice, c.stream));
+		int64_t maxr = 1, maxn = 1;
+		for (int k = 0; k <= d; ++k) maxr = std::max(maxr, x.ranks[k]);
+		for (int k = 0; k < d; ++k) maxn = std::max(maxn, x.dims[k]);
+		fast = maxr <= kAdfMaxR && maxn <= kAdfMaxSlices && maxr * maxr <= 32 * kAdfPairsPerLane;
+		F.assign(d, nullptr);
+		B.assign(d, nullptr);
+		size_t fo = 0, bo = 0;
+		for (int k = 0; k < d; ++k) {
+			fo += size_t(x.ranks[k + 1]) * N;
+			bo += size_t(x.ranks[k]) * N;
+		}
+		double* Fa = c.scratch<double>(S_ADF_FIRST + 8, fo);
+		double* Ba = c.scratch<double>(S_ADF_FIRST + 9, bo);
+		fo = bo = 0;
+		for (int k = 0; k < d; ++k) {
+			F[k] = Fa + fo;
+			B[k] = Ba + bo;
+			fo += size_t(x.ranks[k + 1]) * N;
+			bo += size_t(x.ranks[k]) * N;
+		}
+		warps = std::max<long long>(1, std::min<long long>((N + 127) / 128, (long long)c.num_sms * kAdfWarpsPerBlock * 2));
+		warps = (warps + kAdfWarpsPerBlock - 1) / kAdfWarpsPerBlock * kAdfWarpsPerBlock;
+		chunk = (N + warps - 1) / warps;
+		gpart = c.scratch<double>(S_ADF_FIRST + 3, size_t(warps) * maxr * maxn * maxr);
+		npart = c.scratch<double>(S_ADF_FIRST + 4, size_t(warps) * maxn);
+		rrpart = c.scratch<double>(S_ADF_FIRST + 5, size_t(warps));
+		G = c.scratch<double>(S_ADF_FIRST + 6, size_t(maxr) * maxn * maxr);
+		nrm = c.scratch<double>(S_ADF_FIRST + 7, size_t(maxn) + 8);
+		rr = nrm + maxn;
+	}
+	AdfLevel level(int k, const double* X) const {
+		AdfLevel L;
+		L.pos = pos + size_t(k) * N;
+		L.F = k > 0 ? F[k - 1] : nullptr;
+		L.B = k + 1 < d ? B[k + 1] : nullptr;
+		L.X = X;
+		L.r0 = int(x.ranks[k]);
+		L.n = int(x.dims[k]);
+		L.r1 = int(x.ranks[k + 1]);
+		L.N = N;
+		return L;
+	}
+	unsigned blocks() const { return unsigned(warps / kAdfWarpsPerBlock); }
+	// res (mode 0) or given res (mode 1), G into this->G, and sum res^2 into rr[0]
+	void res_grad(int k, int mode, const double* X, double* Gout, double gscale) {
+		const AdfLevel L = level(k, X);
+		const int len = L.r0 * L.n * L.r1;
+		if (fast) {
+			k_adf_res_grad<<<blocks(), kAdfThreads, 0, c.stream>>>(L, y, res, mode, gpart, rrpart, chunk);
+			k_sum_parts<<<std::max(1, (len + 127) / 128), 128, 0, c.stream>>>(gpart, warps, len, Gout, gscale);
+			k_sum_parts<<<1, 32, 0, c.stream>>>(rrpart, warps, 1, rr, 1.0);
+			c.count_launch(3);
+		} else {
+			if (mode == 0) k_adf_res_generic<<<std::max<long long>(1, std::min<long long>((N + 255) / 256, 4096)), 256, 0, c.stream>>>(L, y, res);
+			k_adf_grad_generic<<<std::max(1, (len + 127) / 128), 128, 0, c.stream>>>(L, res, Gout);
+			if (gscale != 1.0) scale(c, Gout, gscale, size_t(len));
+			dot_async(c, res, res, size_t(N), 20);
+			XTT_CUDA(cudaMemcpyAsync(rr, c.d_dbl + 20, sizeof(double), cudaMemcpyDeviceToDevice, c.stream));
+			c.count_launch(2);
+		}
+		XTT_CUDA(cudaGetLastError());
+	}
+	void slicenorm(int k) {
+		const AdfLevel L = level(k, x.core[k]);
+		if (fast) {
+			k_adf_slicenorm<<<blocks(), kAdfThreads, 0, c.stream>>>(L, G, npart, chunk);
+			k_sum_parts<<<1, 32, 0, c.stream>>>(npart, warps, L.n, nrm, 1.0);
+			c.count_launch(2);
+		} else {
+			k_adf_slicenorm_generic<<<1, 32, 0, c.stream>>>(L, G, nrm);
+			c.count_launch();
+		}
+		XTT_CUDA(cudaGetLastError());
+	}
+	void forward(int k) {
+		const int r0 = int(x.ranks[k]), n = int(x.dims[k]), r1 = int(x.ranks[k + 1]);
+		const unsigned bl = unsigned(std::max<long long>(1, std::min<long long>((N + 255) / 256, (long long)c.num_sms * 8)));
+		k_adf_forward<<<bl, 256, size_t(r0) * n * r1 * sizeof(double), c.stream>>>(pos + size_t(k) * N,
+		                                                                           k > 0 ? F[k - 1] : nullptr,
+		                                                                           x.core[k], F[k], r0, n, r1, N);
+		XTT_CUDA(cudaGetLastError());
+		c.count_launch();
+	}
+	void backward(int k) {
+		const int r0 = int(x.ranks[k]), n = int(x.dims[k]), r1 = int(x.ranks[k + 1]);
+		const unsigned bl = unsigned(std::max<long long>(1, std::min<long long>((N + 255) / 256, (long long)c.num_sms * 8)));
+		k_adf_backward<<<bl, 256, size_t(r0) * n * r1 * sizeof(double), c.stream>>>(pos + size_t(k) * N,
+		                                                                            k + 1 < d ? B[k + 1] : nullptr,
+		                                                                            x.core[k], B[k], r0, n, r1, N);
+		XTT_CUDA(cudaGetLastError());
+		c.count_launch();
+	}
+	double read_rr() {
+		XTT_CUDA(cudaMemcpyAsync(c.h_dbl + 30, rr, sizeof(double), cudaMemcpyDeviceToHost, c.stream));
+		c.sync();
+		return c.h_dbl[30];
+	}
+};
+
+}  // namespace
+
+AdfResult adf(Tensor& x, const int64_t* positions, const double* values, long long N, int64_t max_iter,
+              double target, double min_dec) {
+	// ADFVariant::InternalSolver::solve / solve_with_current_ranks (adf.cpp:489-604), x at its maximal ranks
+	Context& c = *x.ctx;
+	XTT_REQUIRE(!x.op, "ADF needs a TT tensor");
+	XTT_REQUIRE(N > 0, "need at very least one measurement");
+	double ny2 = 0;
+	for (long long s = 0; s < N; ++s) ny2 += values[s] * values[s];
+	const double norm_y = std::sqrt(ny2);
+	move_core(x, 0, false);  // canonicalize_left (adf.cpp:582)
+	AdfData D(c, x, positions, values, N);
+	AdfResult out;
+	double residual_norm = DBL_MAX, last_residual_norm = DBL_MAX;
+	double dec1 = 0, dec2 = 0, dec3 = 0;
+	const int d = x.d;
+	for (int64_t it = 0; max_iter == 0 || it < max_iter; ++it) {
+		move_core(x, 0, true);
+		for (int k = d - 1; k > 0; --k) D.backward(k);
+		D.res_grad(0, 0, x.core[0], D.G, 1.0);
+		last_residual_norm = residual_norm;
+		residual_norm = std::sqrt(D.read_rr()) / norm_y;
+		out.trace.push_back(residual_norm);
+		const double dec4 = dec3;
+		dec3 = dec2;
+		dec2 = dec1;
+		dec1 = residual_norm / last_residual_norm;
+		if (residual_norm < target || dec1 * dec2 * dec3 * dec4 > std::pow(min_dec, 4)) break;
+		for (int k = 0; k < d; ++k) {
+			if (k > 0) D.res_grad(k, 0, x.core[k], D.G, 1.0);
+			D.slicenorm(k);
+			k_adf_update<<<1, 128, 0, c.stream>>>(x.core[k], D.G, D.nrm, int(x.ranks[k]), int(x.dims[k]), int(x.ranks[k + 1]));
+			XTT_CUDA(cudaGetLastError());
+			c.count_launch();
+			if (k + 1 < d) {
+				move_core(x, k + 1, true);
+				D.forward(k);
+			}
+		}
+	}
+	out.residual = residual_norm;
+	return out;
+}
+
+double adf_gradient(const Tensor& xc, const int64_t* positions, const double* values, long long N,
+                    std::vector<double>& grad) {
+	// loss 0.5 ||P(x) - y||^2 and d loss / d X_k = -sum_s res_s F_{k-1}[s] (x) e_{i_s} (x) B_{k+1}[s]
+	Tensor& x = const_cast<Tensor&>(xc);
+	Context& c = *x.ctx;
+	XTT_REQUIRE(!x.op && N > 0, "ADF gradient needs a TT tensor and samples");
+	AdfData D(c, x, positions, values, N);
+	const int d = x.d;
+	for (int k = 0; k + 1 < d; ++k) D.forward(k);
+	for (int k = d - 1; k > 0; --k) D.backward(k);
+	grad.assign(x.total_size(), 0.0);
+	double* Gk = c.scratch<double>(S_ADF_FIRST + 10, x.total_size());
+	size_t off = 0;
+	// residual from the last level (mode 0 at k = d-1), then gradients with the fixed residual
+	std::vector<size_t> offs(d);
+	for (int k = 0; k < d; ++k) {
+		offs[k] = off;
+		off += x.core_size(k);
+	}
+	D.res_grad(d - 1, 0, x.core[d - 1], Gk + offs[d - 1], -1.0);
+	for (int k = 0; k + 1 < d; ++k) D.res_grad(k, 1, x.core[k], Gk + offs[k], -1.0);
+	const double loss = 0.5 * D.read_rr();
+	XTT_CUDA(cudaMemcpyAsync(grad.data(), Gk, sizeof(double) * grad.size(), cudaMemcpyDeviceToHost, c.stream));
+	c.sync();
+	return loss;
+}
+
+}  // namespace xtt

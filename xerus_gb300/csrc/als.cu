@@ -1,0 +1,956 @@
+// ALS / DMRG sweep engine for SPD operators (src/xerus/algorithms/als.cpp).
+//
+// The reference assembles the local operator densely and factors it with
+// LAPACK (lapack_solver, als.cpp:43-71: O((r n r)^3) per step). Here the local
+// operator is never formed: it is applied as a chain of strided GEMMs on the
+// resident environment stacks, inside one persistent cooperative kernel that
+// runs the whole conjugate-gradient solve (bounded grid barriers between the
+// stages, deterministic fixed-order reductions). The mixed form runs the CG
+// in FP32 on FP32 copies of the environments and corrects it against FP64
+// residuals (iterative refinement) in the same launch.
+#include <algorithm>
+#include <cmath>
+#include <cstring>
+
+#include "als.cuh"
+
+namespace xtt {
+
+// ------------------------------------------------------------ GEMM plans
+
+size_t matvec_tmp_elems(const LocalShape& s, int stage) {
+	const size_t ra = s.ra, rb = s.rb, n1 = s.n1, n2 = s.n2, K0 = s.K0, K1 = s.K1, K2 = s.K2;
+	if (s.sites == 1) {
+		if (stage == 0) return ra * K0 * n1 * rb;  // S1 (a, k, j, b')
+		if (stage == 1) return ra * n1 * K1 * rb;  // S2 (a, i, k', b')
+		return 1;
+	}
+	if (stage == 0) return ra * K0 * n1 * n2 * rb;  // S1 (a, k0, j1, j2, b')
+	if (stage == 1) return ra * n1 * K1 * n2 * rb;  // S2 (a, i1, k1, j2, b')
+	return ra * n1 * n2 * K2 * rb;                  // S3 (a, i1, i2, k2, b')
+}
+
+// y(a,i,b) = sum L(a,k,a') A(k,i,j,k') R(b,k',b') x(a',j,b')  (1 site), and the
+// analogous 2-site product; row index (a, i.., b), column index (a', j.., b').
+template <class T>
+MatvecPlan<T> make_matvec_plan(const LocalShape& s, const T* L, const T* A1, const T* A2, const T* R, T* t1, T* t2,
+                               T* t3) {
+	MatvecPlan<T> p;
+	p.n = s.dim();
+	const long long ra = s.ra, rb = s.rb, n1 = s.n1, n2 = s.n2, K0 = s.K0, K1 = s.K1, K2 = s.K2;
+	const long long nL = ra * K0 * ra, nA1 = K0 * n1 * n1 * K1, nA2 = K1 * n2 * n2 * K2;
+	const long long nR = rb * (s.sites == 2 ? K2 : K1) * rb, nx = p.n;
+	const long long n0 = (long long)matvec_tmp_elems(s, 0), nt1 = (long long)matvec_tmp_elems(s, 1),
+	                nt2 = (long long)matvec_tmp_elems(s, 2);
+	if (s.sites == 1) {
+		p.ns = 3;
+		Gemm<T>& g1 = p.g[0];  // S1((a,k),(j,b')) = L((a,k),a') x(a',(j,b'))
+		g1.M = int(ra * K0); g1.N = int(n1 * rb); g1.K = int(ra);
+		g1.A = L; g1.sAm = ra; g1.sAk = 1;
+		g1.sBk = n1 * rb; g1.sBn = 1;
+		g1.C = t1; g1.sCm = n1 * rb; g1.sCn = 1;
+		g1.lens(nL, nx, n0);
+		Gemm<T>& g2 = p.g[1];  // per a: S2(a,i,k',b') = sum_(k,j) S1(a,k,j,b') A(k,i,j,k')
+		g2.batch = int(ra); g2.M = int(rb); g2.N = int(n1 * K1); g2.Ni = int(K1); g2.K = int(K0 * n1); g2.Ki = int(n1);
+		g2.A = t1; g2.sAb = K0 * n1 * rb; g2.sAm = 1; g2.sAko = n1 * rb; g2.sAk = rb;
+		g2.B = A1; g2.sBko = n1 * n1 * K1; g2.sBk = K1; g2.sBno = n1 * K1; g2.sBn = 1;
+		g2.C = t2; g2.sCb = n1 * K1 * rb; g2.sCm = 1; g2.sCno = K1 * rb; g2.sCn = rb;
+		g2.lens(n0, nA1, nt1);
+		Gemm<T>& g3 = p.g[2];  // y((a,i),b) = sum_(k',b') S2((a,i),(k',b')) R(b,(k',b'))
+		g3.M = int(ra * n1); g3.N = int(rb); g3.K = int(K1 * rb);
+		g3.A = t2; g3.sAm = K1 * rb; g3.sAk = 1;
+		g3.B = R; g3.sBk = 1; g3.sBn = K1 * rb;
+		g3.sCm = rb; g3.sCn = 1;
+		g3.lens(nt1, nR, nx);
+	} else {
+		p.ns = 4;
+		Gemm<T>& g1 = p.g[0];  // S1((a,k0),(j1,j2,b'))
+		g1.M = int(ra * K0); g1.N = int(n1 * n2 * rb); g1.K = int(ra);
+		g1.A = L; g1.sAm = ra; g1.sAk = 1;
+		g1.sBk = n1 * n2 * rb; g1.sBn = 1;
+		g1.C = t1; g1.sCm = n1 * n2 * rb; g1.sCn = 1;
+		g1.lens(nL, nx, n0);
+		Gemm<T>& g2 = p.g[1];  // per a: S2(a,i1,k1,(j2,b')) = sum_(k0,j1) S1(a,k0,j1,(j2,b')) A1(k0,i1,j1,k1)
+		g2.batch = int(ra); g2.M = int(n2 * rb); g2.N = int(n1 * K1); g2.Ni = int(K1); g2.K = int(K0 * n1); g2.Ki = int(n1);
+		g2.A = t1; g2.sAb = K0 * n1 * n2 * rb; g2.sAm = 1; g2.sAko = n1 * n2 * rb; g2.sAk = n2 * rb;
+		g2.B = A1; g2.sBko = n1 * n1 * K1; g2.sBk = K1; g2.sBno = n1 * K1; g2.sBn = 1;
+		g2.C = t2; g2.sCb = n1 * K1 * n2 * rb; g2.sCm = 1; g2.sCno = K1 * n2 * rb; g2.sCn = n2 * rb;
+		g2.lens(n0, nA1, nt1);
+		Gemm<T>& g3 = p.g[2];  // per (a,i1): S3(a,i1,i2,k2,b') = sum_(k1,j2) S2(a,i1,k1,j2,b') A2(k1,i2,j2,k2)
+		g3.batch = int(ra * n1); g3.M = int(rb); g3.N = int(n2 * K2); g3.Ni = int(K2); g3.K = int(K1 * n2); g3.Ki = int(n2);
+		g3.A = t2; g3.sAb = K1 * n2 * rb; g3.sAm = 1; g3.sAko = n2 * rb; g3.sAk = rb;
+		g3.B = A2; g3.sBko = n2 * n2 * K2; g3.sBk = K2; g3.sBno = n2 * K2; g3.sBn = 1;
+		g3.C = t3; g3.sCb = n2 * K2 * rb; g3.sCm = 1; g3.sCno = K2 * rb; g3.sCn = rb;
+		g3.lens(nt1, nA2, nt2);
+		Gemm<T>& g4 = p.g[3];  // y((a,i1,i2),b) = sum_(k2,b') S3((a,i1,i2),(k2,b')) R(b,(k2,b'))
+		g4.M = int(ra * n1 * n2); g4.N = int(rb); g4.K = int(K2 * rb);
+		g4.A = t3; g4.sAm = K2 * rb; g4.sAk = 1;
+		g4.B = R; g4.sBk = 1; g4.sBn = K2 * rb;
+		g4.sCm = rb; g4.sCn = 1;
+		g4.lens(nt2, nR, nx);
+	}
+	return p;
+}
+
+template MatvecPlan<double> make_matvec_plan<double>(const LocalShape&, const double*, const double*, const double*,
+                                                     const double*, double*, double*, double*);
+template MatvecPlan<float> make_matvec_plan<float>(const LocalShape&, const float*, const float*, const float*,
+                                                   const float*, float*, float*, float*);
+
+void local_matvec(Context& c, const LocalShape& s, const double* L, const double* A1, const double* A2,
+                  const double* R, const double* x, double* y) {
+	double* t1 = c.scratch<double>(S_ALS_FIRST + 20, matvec_tmp_elems(s, 0));
+	double* t2 = c.scratch<double>(S_ALS_FIRST + 21, matvec_tmp_elems(s, 1));
+	double* t3 = c.scratch<double>(S_ALS_FIRST + 22, matvec_tmp_elems(s, 2));
+	MatvecPlan<double> p = make_matvec_plan<double>(s, L, A1, A2, R, t1, t2, t3);
+	p.g[0].B = x;
+	p.g[p.ns - 1].C = y;
+	for (int i = 0; i < p.ns; ++i) gemm(c, p.g[i]);
+}
+
+// ------------------------------------------------------------ persistent CG
+
+template <class T>
+struct CgParams {
+	MatvecPlan<T> plan;
+	T *x, *r, *p, *q;
+	const T* b;
+	long long n;
+	double* partial;  // 2 * gridDim
+	GridBarrier bar;
+	int max_iter;
+	double tol;
+	int zero_guess;
+};
+
+struct CgOut {
+	int iterations, refinements;
+	double rel_residual;
+};
+
+template <class T>
+__device__ bool matvec_dev(const MatvecPlan<T>& plan, const T* in, T* out, const T* dotv, GemmSmem<T>& sm,
+                           const GridBarrier& bar, T& blk_dot) {
+	for (int s = 0; s < plan.ns; ++s) {
+		Gemm<T> g = plan.g[s];
+		if (s == 0) g.B = in;
+		if (s == plan.ns - 1) {
+			g.C = out;
+			g.D = dotv;
+		}
+		const T part = gemm_tiles(g, blockIdx.x, gridDim.x, sm);
+		if (s == plan.ns - 1) blk_dot = part;
+		else if (!grid_sync(bar)) return false;
+	}
+	return true;
+}
+
+// Sum over the grid of one value per block (thread 0's `mine`), identical in every block.
+__device__ double grid_total(double mine, double* slot, const GridBarrier& bar, bool& ok) {
+	__shared__ double sc[32];
+	if (threadIdx.x == 0) slot[blockIdx.x] = mine;
+	ok = grid_sync(bar);
+	double t = 0;
+	for (int i = threadIdx.x; i < (int)gridDim.x; i += blockDim.x) t += slot[i];
+	return block_sum(t, sc);
+}
+
+template <class T>
+__device__ CgOut cg_body(const CgParams<T>& a, GemmSmem<T>& sm) {
+	__shared__ double sc[32];
+	CgOut out{0, 0, 0.0};
+	const long long gt = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+	const long long gs = (long long)gridDim.x * blockDim.x;
+	const int G = gridDim.x;
+	bool ok = true;
+	T dummy;
+	if (!a.zero_guess) {
+		if (!matvec_dev(a.plan, a.x, a.q, (const T*)nullptr, sm, a.bar, dummy)) return out;
+		if (!grid_sync(a.bar)) return out;
+		for (long long i = gt; i < a.n; i += gs) {
+			const T ri = a.b[i] - a.q[i];
+			a.r[i] = ri;
+			a.p[i] = ri;
+		}
+	} else {
+		for (long long i = gt; i < a.n; i += gs) {
+			a.x[i] = T(0);
+			a.r[i] = a.b[i];
+			a.p[i] = a.b[i];
+		}
+	}
+	double rl = 0, bl = 0;
+	for (long long i = gt; i < a.n; i += gs) {
+		rl += double(a.r[i]) * double(a.r[i]);
+		bl += double(a.b[i]) * double(a.b[i]);
+	}
+	rl = block_sum(rl, sc);
+	bl = block_sum(bl, sc);
+	if (threadIdx.x == 0) a.partial[G + blockIdx.x] = bl;
+	double rr = grid_total(rl, a.partial, a.bar, ok);
+	if (!ok) return out;
+	double bb = 0;
+	{
+		double t = 0;
+		for (int i = threadIdx.x; i < G; i += blockDim.x) t += a.partial[G + i];
+		bb = block_sum(t, sc);
+	}
+	if (bb == 0.0) {
+		for (long long i = gt; i < a.n; i += gs) a.x[i] = T(0);
+		return out;
+	}
+	const double tol2 = a.tol * a.tol * bb;
+	int it = 0;
+	while (rr > tol2 && it < a.max_iter) {
+		T blk = 0;
+		if (!matvec_dev(a.plan, a.p, a.q, a.p, sm, a.bar, blk)) return out;
+		const double pAp = grid_total(double(blk), a.partial, a.bar, ok);
+		if (!ok) return out;
+		if (!(pAp > 0.0) || !isfinite(pAp)) {
+			record_status(a.bar.status, DEV_BREAKDOWN);
+			break;
+		}
+		const double alpha = rr / pAp;
+		double l = 0;
+		for (long long i = gt; i < a.n; i += gs) {
+			a.x[i] += T(alpha) * a.p[i];
+			const T ri = a.r[i] - T(alpha) * a.q[i];
+			a.r[i] = ri;
+			l += double(ri) * double(ri);
+		}
+		l = block_sum(l, sc);
+		const double rrn = grid_total(l, a.partial + G, a.bar, ok);
+		if (!ok) return out;
+		const double beta = rrn / rr;
+		rr = rrn;
+		for (long long i = gt; i < a.n; i += gs) a.p[i] = a.r[i] + T(beta) * a.p[i];
+		if (!grid_sync(a.bar)) return out;
+		++it;
+	}
+	out.iterations = it;
+	out.rel_residual = sqrt(rr / bb);
+	return out;
+}
+
+template <class T>
+__global__ void __launch_bounds__(kGemmThreads) k_cg(CgParams<T> a, int* out_i, double* out_d) {
+	__shared__ GemmSmem<T> sm;
+	const CgOut o = cg_body(a, sm);
+	if (blockIdx.x == 0 && threadIdx.x == 0) {
+		out_i[0] = o.iterations;
+		out_i[1] = 0;
+		out_d[0] = o.rel_residual;
+	}
+}
+
+// Mixed precision: FP64 residual r = b - M x, FP32 CG for M d = r / ||r||, x += ||r|| d.
+struct MixedParams {
+	MatvecPlan<double> p64;
+	CgParams<float> inner;   // inner.b = rhs32, inner.x = d
+	double *x, *q64;
+	const double* b;
+	long long n;
+	double tol;
+	int max_refine;
+};
+
+__global__ void __launch_bounds__(kGemmThreads) k_cg_mixed(MixedParams a, int* out_i, double* out_d) {
+	__shared__ union U {
+		GemmSmem<double> d;
+		GemmSmem<float> f;
+		__device__ U() {}
+	} sm;
+	__shared__ double sc[32];
+	const long long gt = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+	const long long gs = (long long)gridDim.x * blockDim.x;
+	const GridBarrier& bar = a.inner.bar;
+	double* partial = a.inner.partial;
+	bool ok = true;
+	double bl = 0;
+	for (long long i = gt; i < a.n; i += gs) bl += a.b[i] * a.b[i];
+	const double bb = grid_total(block_sum(bl, sc), partial, bar, ok);
+	int iters = 0, refs = 0;
+	double rel = 0;
+	for (int ref = 0; ok && ref <= a.max_refine; ++ref) {
+		double dummy;
+		if (!matvec_dev(a.p64, a.x, a.q64, (const double*)nullptr, sm.d, bar, dummy)) break;
+		if (!grid_sync(bar)) break;
+		double l = 0;
+		for (long long i = gt; i < a.n; i += gs) {
+			const double ri = a.b[i] - a.q64[i];
+			a.q64[i] = ri;
+			l += ri * ri;
+		}
+		const double rr = grid_total(block_sum(l, sc), partial + gridDim.x, bar, ok);
+		if (!ok) break;
+		rel = bb > 0 ? sqrt(rr / bb) : 0.0;
+		if (rr <= a.tol * a.tol * bb || ref == a.max_refine) break;
+		const double nr = sqrt(rr);
+		for (long long i = gt; i < a.n; i += gs) const_cast<float*>(a.inner.b)[i] = float(a.q64[i] / nr);
+		if (!grid_sync(bar)) break;
+		const CgOut o = cg_body(a.inner, sm.f);
+		iters += o.iterations;
+		for (long long i = gt; i < a.n; i += gs) a.x[i] += nr * double(a.inner.x[i]);
+		if (!grid_sync(bar)) break;
+		++refs;
+	}
+	if (blockIdx.x == 0 && threadIdx.x == 0) {
+		out_i[0] = iters;
+		out_i[1] = refs;
+		out_d[0] = rel;
+	}
+}
+
+template <class F>
+static int coop_grid(F kernel, Context& c, long long work_blocks) {
+	static int occ_cache[4] = {0, 0, 0, 0};
+	int occ = 0;
+	XTT_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, kernel, kGemmThreads, 0));
+	(void)occ_cache;
+	const long long maxg = (long long)std::max(1, occ) * c.num_sms;
+	return int(std::max<long long>(1, std::min<long long>(maxg, work_blocks)));
+}
+
+__global__ void k_to_float(float* out, const double* in, size_t n) {
+	for (size_t i = blockIdx.x * size_t(blockDim.x) + threadIdx.x; i < n; i += size_t(gridDim.x) * blockDim.x)
+		out[i] = float(in[i]);
+}
+
+static void to_float(Context& c, float* out, const double* in, size_t n) {
+	if (!n) return;
+	k_to_float<<<unsigned(std::min<size_t>((n + 255) / 256, 2048)), 256, 0, c.stream>>>(out, in, n);
+	XTT_CUDA(cudaGetLastError());
+	c.count_launch();
+}
+
+CgResult local_solve(Context& c, const LocalShape& s, const double* L, const double* A1, const double* A2,
+                     const double* R, const double* b, double* x, double tol, int max_iter, int precision) {
+	const long long n = s.dim();
+	double* t1 = c.scratch<double>(S_ALS_FIRST + 20, matvec_tmp_elems(s, 0));
+	double* t2 = c.scratch<double>(S_ALS_FIRST + 21, matvec_tmp_elems(s, 1));
+	double* t3 = c.scratch<double>(S_ALS_FIRST + 22, matvec_tmp_elems(s, 2));
+	MatvecPlan<double> p64 = make_matvec_plan<double>(s, L, A1, A2, R, t1, t2, t3);
+	{
+		MatvecPlan<double> chk = p64;  // validate with the vectors the kernel substitutes
+		chk.g[0].B = b;
+		chk.g[chk.ns - 1].C = x;
+		for (int i = 0; i < chk.ns; ++i) check_gemm(chk.g[i]);
+	}
+	long long work = (n + kGemmThreads - 1) / kGemmThreads;
+	for (int i = 0; i < p64.ns; ++i) work = std::max(work, p64.g[i].tiles());
+	int* oi = c.d_ints + 8;
+	double* od = c.d_dbl + 8;
+	CgResult res;
+	if (precision == XTT_PRECISION_FP64) {
+		CgParams<double> a;
+		a.plan = p64;
+		a.x = x;
+		a.r = c.scratch<double>(S_ALS_FIRST + 23, n);
+		a.p = c.scratch<double>(S_ALS_FIRST + 24, n);
+		a.q = c.scratch<double>(S_ALS_FIRST + 25, n);
+		a.b = b;
+		a.n = n;
+		const int G = coop_grid(k_cg<double>, c, work);
+		a.partial = c.scratch<double>(S_ALS_FIRST + 26, 2 * size_t(G));
+		a.bar = GridBarrier{c.d_barrier, c.d_barrier + 1, c.d_status};
+		a.max_iter = max_iter;
+		a.tol = tol;
+		a.zero_guess = 0;
+		void* args[] = {&a, &oi, &od};
+		XTT_CUDA(cudaLaunchCooperativeKernel((void*)k_cg<double>, dim3(G), dim3(kGemmThreads), args, 0, c.stream));
+		c.count_launch();
+	} else {
+		// FP32 copies of the environments and operator cores
+		const size_t nL = size_t(s.ra) * s.K0 * s.ra, nA1 = size_t(s.K0) * s.n1 * s.n1 * s.K1;
+		const size_t nA2 = s.sites == 2 ? size_t(s.K1) * s.n2 * s.n2 * s.K2 : 0;
+		const size_t nR = size_t(s.rb) * (s.sites == 2 ? s.K2 : s.K1) * s.rb;
+		float* f = c.scratch<float>(S_ALS_FIRST + 27, nL + nA1 + nA2 + nR + 4);
+		to_float(c, f, L, nL);
+		to_float(c, f + nL, A1, nA1);
+		if (nA2) to_float(c, f + nL + nA1, A2, nA2);
+		to_float(c, f + nL + nA1 + nA2, R, nR);
+		float* u1 = c.scratch<float>(S_ALS_FIRST + 28, matvec_tmp_elems(s, 0));
+		float* u2 = c.scratch<float>(S_ALS_FIRST + 29, matvec_tmp_elems(s, 1));
+		float* u3 = c.scratch<float>(S_ALS_FIRST + 30, matvec_tmp_elems(s, 2));
+		MixedParams m;
+		m.p64 = p64;
+		m.inner.plan = make_matvec_plan<float>(s, f, f + nL, nA2 ? f + nL + nA1 : nullptr, f + nL + nA1 + nA2, u1, u2, u3);
+		{
+			MatvecPlan<float> chk = m.inner.plan;
+			chk.g[0].B = u1;  // any non-null vector of length n: lengths come from lens()
+			chk.g[chk.ns - 1].C = u1;
+			for (int i = 0; i < chk.ns; ++i) check_gemm(chk.g[i]);
+		}
+		float* v = c.scratch<float>(S_ALS_FIRST + 31, 5 * size_t(n));
+		m.inner.x = v;
+		m.inner.r = v + n;
+		m.inner.p = v + 2 * n;
+		m.inner.q = v + 3 * n;
+		m.inner.b = v + 4 * n;
+		m.inner.n = n;
+		const int G = coop_grid(k_cg_mixed, c, work);
+		m.inner.partial = c.scratch<double>(S_ALS_FIRST + 26, 2 * size_t(G));
+		m.inner.bar = GridBarrier{c.d_barrier, c.d_barrier + 1, c.d_status};
+		m.inner.max_iter = max_iter;
+		m.inner.tol = 1e-6;
+		m.inner.zero_guess = 1;
+		m.x = x;
+		m.q64 = c.scratch<double>(S_ALS_FIRST + 25, n);
+		m.b = b;
+		m.n = n;
+		m.tol = tol;
+		m.max_refine = 12;
+		void* args[] = {&m, &oi, &od};
+		XTT_CUDA(cudaLaunchCooperativeKernel((void*)k_cg_mixed, dim3(G), dim3(kGemmThreads), args, 0, c.stream));
+		c.count_launch();
+	}
+	return res;  // counters are read lazily by the driver (ctx d_ints[8..9], d_dbl[8])
+}
+
+// ------------------------------------------------------------ environment pushes
+
+// L'(c1,c2,c3) = sum L(a1,a2,a3) x(a1,i,c1) A(a2,i,j,c2) x(a3,j,c3)       (als.cpp:184-200, 247)
+static void push_left_op(Context& c, const double* L, const double* x, const double* A, double* out, long long r,
+                         long long K, long long n, long long r1, long long K1) {
+	double* s1 = c.scratch<double>(S_ALS_FIRST + 16, size_t(K * r * n * r1));
+	double* s2 = c.scratch<double>(S_ALS_FIRST + 17, size_t(r * r1 * n * K1));
+	Gemm<double> p1;  // S1((a2,a3),(i,c1)) = sum_a1 L(a1,(a2,a3)) x(a1,(i,c1))
+	p1.M = int(K * r); p1.N = int(n * r1); p1.K = int(r);
+	p1.A = L; p1.sAm = 1; p1.sAk = K * r;
+	p1.B = x; p1.sBk = n * r1; p1.sBn = 1;
+	p1.C = s1; p1.sCm = n * r1; p1.sCn = 1;
+	p1.lens(r * K * r, r * n * r1, K * r * n * r1);
+	gemm(c, p1);
+	Gemm<double> p2;  // per a3: S2(a3,c1,(j,c2)) = sum_(a2,i) S1(a2,a3,i,c1) A((a2,i),(j,c2))
+	p2.batch = int(r); p2.M = int(r1); p2.N = int(n * K1); p2.K = int(K * n); p2.Ki = int(n);
+	p2.A = s1; p2.sAb = n * r1; p2.sAm = 1; p2.sAko = r * n * r1; p2.sAk = r1;
+	p2.B = A; p2.sBko = n * n * K1; p2.sBk = n * K1; p2.sBn = 1;
+	p2.C = s2; p2.sCb = r1 * n * K1; p2.sCm = n * K1; p2.sCn = 1;
+	p2.lens(K * r * n * r1, K * n * n * K1, r * r1 * n * K1);
+	gemm(c, p2);
+	Gemm<double> p3;  // L'((c1,c2),c3) = sum_(a3,j) S2(a3,c1,j,c2) x((a3,j),c3)
+	p3.M = int(r1 * K1); p3.Mi = int(K1); p3.N = int(r1); p3.K = int(r * n); p3.Ki = int(n);
+	p3.A = s2; p3.sAmo = n * K1; p3.sAm = 1; p3.sAko = r1 * n * K1; p3.sAk = K1;
+	p3.B = x; p3.sBko = n * r1; p3.sBk = r1; p3.sBn = 1;
+	p3.C = out; p3.sCmo = K1 * r1; p3.sCm = r1; p3.sCn = 1;
+	p3.lens(r * r1 * n * K1, r * n * r1, r1 * K1 * r1);
+	gemm(c, p3);
+}
+
+// R'(a1,a2,a3) = sum x(a1,i,c1) A(a2,i,j,c2) x(a3,j,c3) R(c1,c2,c3)       (als.cpp:239)
+static void push_right_op(Context& c, const double* R, const double* x, const double* A, double* out, long long r,
+                          long long K, long long n, long long r1, long long K1) {
+	double* s1 = c.scratch<double>(S_ALS_FIRST + 16, size_t(r * n * r1 * K1));
+	double* s2 = c.scratch<double>(S_ALS_FIRST + 17, size_t(r * K * n * r1));
+	Gemm<double> q1;  // S1((a3,j),(c1,c2)) = sum_c3 x((a3,j),c3) R((c1,c2),c3)
+	q1.M = int(r * n); q1.N = int(r1 * K1); q1.K = int(r1);
+	q1.A = x; q1.sAm = r1; q1.sAk = 1;
+	q1.B = R; q1.sBk = 1; q1.sBn = r1;
+	q1.C = s1; q1.sCm = r1 * K1; q1.sCn = 1;
+	q1.lens(r * n * r1, r1 * K1 * r1, r * n * r1 * K1);
+	gemm(c, q1);
+	Gemm<double> q2;  // per a3: S2(a3,(a2,i),c1) = sum_(j,c2) A((a2,i),(j,c2)) S1(a3,j,c1,c2)
+	q2.batch = int(r); q2.M = int(K * n); q2.N = int(r1); q2.K = int(n * K1); q2.Ki = int(K1);
+	q2.A = A; q2.sAm = n * K1; q2.sAko = K1; q2.sAk = 1;
+	q2.B = s1; q2.sBb = n * r1 * K1; q2.sBko = r1 * K1; q2.sBk = 1; q2.sBn = K1;
+	q2.C = s2; q2.sCb = K * n * r1; q2.sCm = r1; q2.sCn = 1;
+	q2.lens(K * n * n * K1, r * n * r1 * K1, r * K * n * r1);
+	gemm(c, q2);
+	Gemm<double> q3;  // R'(a1,(a2,a3)) = sum_(i,c1) x(a1,(i,c1)) S2(a3,a2,(i,c1))
+	q3.M = int(r); q3.N = int(K * r); q3.Ni = int(r); q3.K = int(n * r1);
+	q3.A = x; q3.sAm = n * r1; q3.sAk = 1;
+	q3.B = s2; q3.sBk = 1; q3.sBno = n * r1; q3.sBn = K * n * r1;
+	q3.C = out; q3.sCm = K * r; q3.sCno = r; q3.sCn = 1;
+	q3.lens(r * n * r1, r * K * n * r1, r * K * r);
+	gemm(c, q3);
+}
+
+// Lb'(c1,c2) = sum Lb(a1,a2) b(a1,i,c1) x(a2,i,c2)   (als.cpp:202-215, 250)
+static void push_left_rhs(Context& c, const double* Lb, const double* bc, const double* x, double* out, long long s,
+                          long long r, long long n, long long s1, long long r1) {
+	double* t = c.scratch<double>(S_ALS_FIRST + 18, size_t(r * n * s1));
+	Gemm<double> u1;  // S1(a2,(i,c1)) = sum_a1 Lb(a1,a2) b(a1,(i,c1))
+	u1.M = int(r); u1.N = int(n * s1); u1.K = int(s);
+	u1.A = Lb; u1.sAm = 1; u1.sAk = r;
+	u1.B = bc; u1.sBk = n * s1; u1.sBn = 1;
+	u1.C = t; u1.sCm = n * s1; u1.sCn = 1;
+	u1.lens(s * r, s * n * s1, r * n * s1);
+	gemm(c, u1);
+	Gemm<double> u2;  // Lb'(c1,c2) = sum_(a2,i) S1((a2,i),c1) x((a2,i),c2)
+	u2.M = int(s1); u2.N = int(r1); u2.K = int(r * n);
+	u2.A = t; u2.sAm = 1; u2.sAk = s1;
+	u2.B = x; u2.sBk = r1; u2.sBn = 1;
+	u2.C = out; u2.sCm = r1; u2.sCn = 1;
+	u2.lens(r * n * s1, r * n * r1, s1 * r1);
+	gemm(c, u2);
+}
+
+// Rb'(a1,a2) = sum b(a1,i,c1) x(a2,i,c2) Rb(c1,c2)   (als.cpp:242)
+static void push_right_rhs(Context& c, const double* Rb, const double* bc, const double* x, double* out, long long s,
+                           long long r, long long n, long long s1, long long r1) {
+	double* t = c.scratch<double>(S_ALS_FIRST + 18, size_t(r * n * s1));
+	Gemm<double> v1;  // S1((a2,i),c1) = sum_c2 x((a2,i),c2) Rb(c1,c2)
+	v1.M = int(r * n); v1.N = int(s1); v1.K = int(r1);
+	v1.A = x; v1.sAm = r1; v1.sAk = 1;
+	v1.B = Rb; v1.sBk = 1; v1.sBn = r1;
+	v1.C = t; v1.sCm = s1; v1.sCn = 1;
+	v1.lens(r * n * r1, s1 * r1, r * n * s1);
+	gemm(c, v1);
+	Gemm<double> v2;  // Rb'(a1,a2) = sum_(i,c1) b(a1,(i,c1)) S1(a2,(i,c1))
+	v2.M = int(s); v2.N = int(r); v2.K = int(n * s1);
+	v2.A = bc; v2.sAm = n * s1; v2.sAk = 1;
+	v2.B = t; v2.sBk = 1; v2.sBn = n * s1;
+	v2.C = out; v2.sCm = r; v2.sCn = 1;
+	v2.lens(s * n * s1, r * n * s1, s * r);
+	gemm(c, v2);
+}
+
+// b_loc(a, i.., b) = sum Lb(s0,a) b_k(s0,i,s1) [b_k+1(s1,i2,s2)] Rb(s_last,b)   (als.cpp:404-423)
+static void local_rhs(Context& c, int sites, const double* Lb, const double* b1, const double* b2, const double* Rb,
+                      double* out, long long ra, long long rb, long long s0, long long s1, long long s2, long long n1,
+                      long long n2) {
+	double* t1 = c.scratch<double>(S_ALS_FIRST + 18, size_t(ra * n1 * s1));
+	Gemm<double> w1;
+	w1.M = int(ra); w1.N = int(n1 * s1); w1.K = int(s0);
+	w1.A = Lb; w1.sAm = 1; w1.sAk = ra;
+	w1.B = b1; w1.sBk = n1 * s1; w1.sBn = 1;
+	w1.C = t1; w1.sCm = n1 * s1; w1.sCn = 1;
+	w1.lens(s0 * ra, s0 * n1 * s1, ra * n1 * s1);
+	gemm(c, w1);
+	const double* last = t1;
+	long long rows = ra * n1, sl = s1;
+	if (sites == 2) {
+		double* t2 = c.scratch<double>(S_ALS_FIRST + 19, size_t(ra * n1 * n2 * s2));
+		Gemm<double> w2;
+		w2.M = int(ra * n1); w2.N = int(n2 * s2); w2.K = int(s1);
+		w2.A = t1; w2.sAm = s1; w2.sAk = 1;
+		w2.B = b2; w2.sBk = n2 * s2; w2.sBn = 1;
+		w2.C = t2; w2.sCm = n2 * s2; w2.sCn = 1;
+		w2.lens(ra * n1 * s1, s1 * n2 * s2, ra * n1 * n2 * s2);
+		gemm(c, w2);
+		last = t2;
+		rows = ra * n1 * n2;
+		sl = s2;
+	}
+	Gemm<double> w3;
+	w3.M = int(rows); w3.N = int(rb); w3.K = int(sl);
+	w3.A = last; w3.sAm = sl; w3.sAk = 1;
+	w3.B = Rb; w3.sBk = rb; w3.sBn = 1;
+	w3.C = out; w3.sCm = rb; w3.sCn = 1;
+	w3.lens(rows * sl, sl * rb, rows * rb);
+	gemm(c, w3);
+}
+
+// ------------------------------------------------------------ small kernels
+
+__global__ void k_identity_core(double* core, long long p0, long long n, long long p1, int right) {
+	const long long total = p0 * n * p1;
+	for (long long e = blockIdx.x * (long long)blockDim.x + threadIdx.x; e < total; e += (long long)gridDim.x * blockDim.x) {
+		const long long i2 = e % p1, i1 = (e / p1) % n, i0 = e / (p1 * n);
+		core[e] = right ? (i0 == i1 * p1 + i2 ? 1.0 : 0.0) : (i0 * n + i1 == i2 ? 1.0 : 0.0);
+	}
+}
+
+// v += (d_dbl[s0] / d_dbl[s1]) g     (ASD step, alpha = <g,g>/<g,Mg>)
+__global__ void k_asd_step(double* v, const double* g, long long n, const double* dd, int s0, int s1) {
+	const double alpha = dd[s0] / dd[s1];
+	for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x)
+		v[i] += alpha * g[i];
+}
+
+__global__ void k_sub(double* out, const double* a, const double* b, long long n) {
+	for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x)
+		out[i] = a[i] - b[i];
+}
+
+__global__ void k_energy(double* out, const double* dd, int sxq, int sxb) {
+	out[0] = fabs(0.5 * dd[sxq] - dd[sxb]);
+}
+
+static unsigned blocks_for(long long n) { return unsigned(std::max<long long>(1, std::min<long long>((n + 255) / 256, 2048))); }
+
+// ------------------------------------------------------------ the sweep
+
+namespace {
+
+struct Stacks {
+	std::vector<double*> Lop, Rop, Lb, Rb;
+};
+
+struct AlsState {
+	Context& c;
+	const Tensor& A;
+	Tensor& x;
+	const Tensor& b;
+	const AlsOptions& o;
+	int d, S;
+	Stacks st;
+	double *v, *bloc, *q, *grad;
+	AlsState(Context& cc, const Tensor& AA, Tensor& xx, const Tensor& bb, const AlsOptions& oo)
+	    : c(cc), A(AA), x(xx), b(bb), o(oo), d(xx.d), S(oo.sites) {}
+
+	LocalShape shape(int cur) const {
+		LocalShape s;
+		s.sites = S;
+		s.ra = int(x.ranks[cur]);
+		s.rb = int(x.ranks[cur + S]);
+		s.n1 = int(x.dims[cur]);
+		s.n2 = S == 2 ? int(x.dims[cur + 1]) : 1;
+		s.K0 = int(A.ranks[cur]);
+		s.K1 = int(A.ranks[cur + 1]);
+		s.K2 = S == 2 ? int(A.ranks[cur + 2]) : 1;
+		return s;
+	}
+	void push_left(int k) {
+		push_left_op(c, st.Lop[k], x.core[k], A.core[k], st.Lop[k + 1], x.ranks[k], A.ranks[k], x.dims[k],
+		             x.ranks[k + 1], A.ranks[k + 1]);
+		push_left_rhs(c, st.Lb[k], b.core[k], x.core[k], st.Lb[k + 1], b.ranks[k], x.ranks[k], x.dims[k], b.ranks[k + 1],
+		              x.ranks[k + 1]);
+	}
+	// right environment of bond `slot` from bond slot+1 and core kc
+	void push_right(int slot, int kc) {
+		XTT_REQUIRE(kc == slot || (x.ranks[kc + 1] == x.ranks[slot + 1] && A.ranks[kc + 1] == A.ranks[slot + 1] &&
+		                           b.ranks[kc + 1] == b.ranks[slot + 1] && x.ranks[kc] == x.ranks[slot] &&
+		                           A.ranks[kc] == A.ranks[slot] && b.ranks[kc] == b.ranks[slot] &&
+		                           x.dims[kc] == x.dims[slot]),
+		            "index dimensions do not coincide (the two-site decreasing sweep contracts core k into the right "
+		            "environment of bond k+2, which needs equal neighbouring ranks)");
+		push_right_op(c, st.Rop[slot + 1], x.core[kc], A.core[kc], st.Rop[slot], x.ranks[kc], A.ranks[kc], x.dims[kc],
+		              x.ranks[kc + 1], A.ranks[kc + 1]);
+		push_right_rhs(c, st.Rb[slot + 1], b.core[kc], x.core[kc], st.Rb[slot], b.ranks[kc], x.ranks[kc], x.dims[kc],
+		               b.ranks[kc + 1], x.ranks[kc + 1]);
+	}
+	// v <- current local block (core cur, or core cur * core cur+1)
+	void gather_block(int cur) {
+		const LocalShape s = shape(cur);
+		if (S == 1) {
+			copy_d2d(c, v, x.core[cur], size_t(s.dim()));
+		} else {
+			const long long ra = x.ranks[cur], m = x.ranks[cur + 1], n1 = x.dims[cur], n2 = x.dims[cur + 1],
+			                rb = x.ranks[cur + 2];
+			Gemm<double> g;
+			g.M = int(ra * n1); g.N = int(n2 * rb); g.K = int(m);
+			g.A = x.core[cur]; g.sAm = m; g.sAk = 1;
+			g.B = x.core[cur + 1]; g.sBk = n2 * rb; g.sBn = 1;
+			g.C = v; g.sCm = n2 * rb; g.sCn = 1;
+			g.lens(ra * n1 * m, m * n2 * rb, ra * n1 * n2 * rb);
+			gemm(c, g);
+		}
+	}
+	void rhs(int cur) {
+		const LocalShape s = shape(cur);
+		local_rhs(c, S, st.Lb[cur], b.core[cur], S == 2 ? b.core[cur + 1] : nullptr, st.Rb[cur + S], bloc, s.ra, s.rb,
+		          b.ranks[cur], b.ranks[cur + 1], S == 2 ? b.ranks[cur + 2] : 1, s.n1, s.n2);
+	}
+	const double* A2(int cur) const { return S == 2 ? A.core[cur + 1] : nullptr; }
+	// |0.5 <v, M v> - <v, b_loc>| with v, b_loc current  (als.cpp:265-278)
+	double energy(int cur) {
+		const LocalShape s = shape(cur);
+		local_matvec(c, s, st.Lop[cur], A.core[cur], A2(cur), st.Rop[cur + S], v, q);
+		dot_async(c, v, q, size_t(s.dim()), 4);
+		dot_async(c, v, bloc, size_t(s.dim()), 5);
+		k_energy<<<1, 1, 0, c.stream>>>(c.d_dbl + 6, c.d_dbl, 4, 5);
+		XTT_CUDA(cudaGetLastError());
+		c.count_launch();
+		XTT_CUDA(cudaMemcpyAsync(c.h_dbl + 6, c.d_dbl + 6, sizeof(double), cudaMemcpyDeviceToHost, c.stream));
+		c.sync();
+		return c.h_dbl[6];
+	}
+};
+
+}  // namespace
+
+AlsReport als(const Tensor& A, Tensor& x, const Tensor& b, const AlsOptions& o) {
+	// ALSVariant::solve, src/xerus/algorithms/als.cpp:483-553
+	Context& c = *x.ctx;
+	XTT_REQUIRE(A.op && !x.op && !b.op, "ALS needs a TT operator, a TT tensor x and a TT tensor b");
+	XTT_REQUIRE(x.d > 0 && x.dims == b.dims && A.dims == x.dims && A.d == x.d, "dimensions of A, x and b must match");
+	XTT_REQUIRE(o.sites == 1 || o.sites == 2, "sites must be 1 or 2");
+	XTT_REQUIRE(!(o.local_solver == 1 && o.sites != 1), "ASD only defined for single site alternation");
+	XTT_REQUIRE(o.sites <= x.d, "more sites than components");
+	const int d = x.d, S = o.sites;
+	AlsReport rep;
+	std::vector<int64_t> target(x.ranks.begin() + 1, x.ranks.end() - 1);
+	const bool canon_end = x.canonicalized;
+	const int64_t core_end = x.core_position;
+
+	// prepare_x_for_als (als.cpp:105-182)
+	int first = 0;
+	int64_t prod = 1;
+	while (first + 1 < d) {
+		const int64_t nd = x.dims[first], newp = prod * nd;
+		if (x.ranks[first + 1] < newp) break;
+		const int64_t rk = x.ranks[first + 1], n2 = x.dims[first + 1], r2 = x.ranks[first + 2];
+		double* T = c.scratch<double>(S_GEMM_A, size_t(newp * n2 * r2));
+		Gemm<double> g;  // core_{f+1} <- reshape(core_f, newp x rk) * core_{f+1}
+		g.M = int(newp); g.N = int(n2 * r2); g.K = int(rk);
+		g.A = x.core[first]; g.sAm = rk; g.sAk = 1;
+		g.B = x.core[first + 1]; g.sBk = n2 * r2; g.sBn = 1;
+		g.C = T; g.sCm = n2 * r2; g.sCn = 1;
+		g.lens((long long)x.core_size(first), (long long)x.core_size(first + 1), newp * n2 * r2);
+		gemm(c, g);
+		x.reshape_core(first + 1, newp, r2);
+		copy_d2d(c, x.core[first + 1], T, size_t(newp * n2 * r2));
+		x.reshape_core(first, prod, newp);
+		k_identity_core<<<blocks_for(prod * nd * newp), 256, 0, c.stream>>>(x.core[first], prod, nd, newp, 0);
+		c.count_launch();
+		++first;
+		prod = newp;
+	}
+	int last = d;
+	prod = 1;
+	while (last > first + S) {
+		const int64_t nd = x.dims[last - 1], newp = prod * nd;
+		if (x.ranks[last - 1] < newp) break;
+		const int64_t rk = x.ranks[last - 1], r0 = x.ranks[last - 2], n0 = x.dims[last - 2];
+		double* T = c.scratch<double>(S_GEMM_A, size_t(r0 * n0 * newp));
+		Gemm<double> g;  // core_{l-2} <- core_{l-2} * reshape(core_{l-1}, rk x newp)
+		g.M = int(r0 * n0); g.N = int(newp); g.K = int(rk);
+		g.A = x.core[last - 2]; g.sAm = rk; g.sAk = 1;
+		g.B = x.core[last - 1]; g.sBk = newp; g.sBn = 1;
+		g.C = T; g.sCm = newp; g.sCn = 1;
+		g.lens((long long)x.core_size(last - 2), (long long)x.core_size(last - 1), r0 * n0 * newp);
+		gemm(c, g);
+		x.reshape_core(last - 2, r0, newp);
+		copy_d2d(c, x.core[last - 2], T, size_t(r0 * n0 * newp));
+		x.reshape_core(last - 1, newp, prod);
+		k_identity_core<<<blocks_for(newp * nd * prod), 256, 0, c.stream>>>(x.core[last - 1], newp, nd, prod, 1);
+		c.count_launch();
+		--last;
+		prod = newp;
+	}
+	XTT_CUDA(cudaGetLastError());
+	if (canon_end && core_end < first) {
+		x.canonicalized = true;
+		x.core_position = first;
+	} else {
+		if (canon_end && core_end >= last) {
+			x.canonicalized = true;
+			x.core_position = last - 1;
+		}
+		move_core(x, first, true);
+	}
+
+	// rank bounds (ranks only change in DMRG with rank growth)
+	std::vector<int64_t> rmax(x.ranks);
+	if (S == 2 && o.max_rank > 0) {
+		std::vector<int64_t> nn(x.dims), inner(d - 1, o.max_rank);
+		auto red = reduce_to_maximal_ranks(inner, nn);
+		for (int k = 1; k < d; ++k) rmax[k] = std::max(x.ranks[k], red[k - 1]);
+	}
+	AlsState s(c, A, x, b, o);
+	// stacks: one buffer per family, a slot per bond 0..d
+	{
+		std::vector<size_t> oop(d + 2, 0), orh(d + 2, 0);
+		for (int k = 0; k <= d; ++k) {
+			oop[k + 1] = oop[k] + size_t(rmax[k] * A.ranks[k] * rmax[k]);
+			orh[k + 1] = orh[k] + size_t(b.ranks[k] * rmax[k]);
+		}
+		double* L = c.scratch<double>(S_ALS_FIRST + 0, oop[d + 1]);
+		double* R = c.scratch<double>(S_ALS_FIRST + 1, oop[d + 1]);
+		double* Lb = c.scratch<double>(S_ALS_FIRST + 2, orh[d + 1]);
+		double* Rb = c.scratch<double>(S_ALS_FIRST + 3, orh[d + 1]);
+		for (int k = 0; k <= d; ++k) {
+			s.st.Lop.push_back(L + oop[k]);
+			s.st.Rop.push_back(R + oop[k]);
+			s.st.Lb.push_back(Lb + orh[k]);
+			s.st.Rb.push_back(Rb + orh[k]);
+		}
+		fill(c, s.st.Lop[0], 1.0, 1);
+		fill(c, s.st.Rop[d], 1.0, 1);
+		fill(c, s.st.Lb[0], 1.0, 1);
+		fill(c, s.st.Rb[d], 1.0, 1);
+		long long maxdim = 1;
+		for (int k = 0; k + S <= d; ++k) {
+			long long dim = rmax[k] * rmax[k + S] * x.dims[k] * (S == 2 ? x.dims[k + 1] : 1);
+			maxdim = std::max(maxdim, dim);
+		}
+		s.v = c.scratch<double>(S_ALS_FIRST + 4, maxdim);
+		s.bloc = c.scratch<double>(S_ALS_FIRST + 5, maxdim);
+		s.q = c.scratch<double>(S_ALS_FIRST + 6, maxdim);
+		s.grad = c.scratch<double>(S_ALS_FIRST + 7, maxdim);
+	}
+	for (int i = d - 1; i > first + S - 1; --i) s.push_right(i, i);
+	for (int i = 0; i < first; ++i) s.push_left(i);
+
+	int cur = first;
+	bool inc = true;
+	const int max_it_opt = int(std::min<int64_t>(o.local_max_iterations, int64_t(1) << 30));
+	auto record = [&](int64_t flag) {
+		if (o.record_residuals) {
+			rep.residuals.push_back(residual(A, x, b));
+			rep.flags.push_back(flag);
+		}
+	};
+	s.gather_block(cur);
+	s.rhs(cur);
+	double energy = s.energy(cur), last_e = 1e101, last_e2 = 1e102;
+	record(3);
+	int half = 0;
+	while (true) {
+		const LocalShape sh = s.shape(cur);
+		const long long n = sh.dim();
+		s.rhs(cur);
+		s.gather_block(cur);
+		if (o.local_solver == 1) {
+			// ASD_solver (als.cpp:73-92): one exact line-search gradient step
+			local_matvec(c, sh, s.st.Lop[cur], A.core[cur], nullptr, s.st.Rop[cur + 1], s.v, s.q);
+			k_sub<<<blocks_for(n), 256, 0, c.stream>>>(s.grad, s.bloc, s.q, n);
+			c.count_launch();
+			local_matvec(c, sh, s.st.Lop[cur], A.core[cur], nullptr, s.st.Rop[cur + 1], s.grad, s.q);
+			dot_async(c, s.grad, s.grad, size_t(n), 10);
+			dot_async(c, s.grad, s.q, size_t(n), 11);
+			k_asd_step<<<blocks_for(n), 256, 0, c.stream>>>(s.v, s.grad, n, c.d_dbl, 10, 11);
+			c.count_launch();
+			XTT_CUDA(cudaGetLastError());
+		} else {
+			const int max_it = max_it_opt > 0 ? max_it_opt : int(std::min<long long>(10 * n + 100, 1 << 30));
+			local_solve(c, sh, s.st.Lop[cur], A.core[cur], s.A2(cur), s.st.Rop[cur + S], s.bloc, s.v, o.local_tolerance,
+			            max_it, o.precision);
+			XTT_CUDA(cudaMemcpyAsync(c.h_ints + 8, c.d_ints + 8, 2 * sizeof(int), cudaMemcpyDeviceToHost, c.stream));
+		}
+		if (S == 1) {
+			copy_d2d(c, x.core[cur], s.v, size_t(n));
+		} else {
+			// split by truncated SVD (als.cpp:51-70): increasing keeps U left, decreasing keeps Vt right
+			const long long ra = sh.ra, rb = sh.rb, n1 = sh.n1, n2 = sh.n2;
+			const bool grow = o.max_rank > 0;
+			const int mr = grow ? int(std::min<int64_t>(o.max_rank, rmax[cur + 1])) : int(target[cur]);
+			const double eps = grow ? o.svd_epsilon : 8 * 2.220446049250313e-16;
+			SvdArgs a;
+			const int m = int(ra * n1), nn = int(n2 * rb), q = std::min(m, nn);
+			double* U = c.scratch<double>(S_SVD_U, size_t(m) * q);
+			double* Sv = c.scratch<double>(S_SVD_S, size_t(q));
+			double* Vt = c.scratch<double>(S_SVD_VT, size_t(q) * nn);
+			const size_t wk = svd_work_doubles(m, nn);
+			a.X = s.v; a.ldx = nn; a.m = m; a.n = nn; a.max_rank = mr; a.eps = eps;
+			a.work = wk ? c.scratch<double>(S_SVD_WORK, wk) : nullptr;
+			a.U = U; a.S = Sv; a.Vt = Vt; a.rank_out = c.d_ints + 1; a.status = c.d_status;
+			launch_svd(a, c.stream);
+			c.count_launch();
+			const int rk = c.read_int(1);
+			XTT_REQUIRE(rk <= rmax[cur + 1], "DMRG split rank exceeds the stack capacity");
+			if (inc) {
+				x.reshape_core(cur, ra, rk);
+				copy_d2d(c, x.core[cur], U, size_t(m) * rk);
+				scale_rows(c, Vt, Sv, rk, nn);
+				x.reshape_core(cur + 1, rk, rb);
+				copy_d2d(c, x.core[cur + 1], Vt, size_t(rk) * nn);
+			} else {
+				scale_cols(c, U, Sv, m, rk);
+				x.reshape_core(cur, ra, rk);
+				copy_d2d(c, x.core[cur], U, size_t(m) * rk);
+				x.reshape_core(cur + 1, rk, rb);
+				copy_d2d(c, x.core[cur + 1], Vt, size_t(rk) * nn);
+			}
+			x.canonicalized = false;  // set_component on a second position (ttNetwork.cpp:491)
+		}
+		if (o.local_solver == 0) {
+			c.sync();
+			rep.local_iterations += c.h_ints[8];
+			rep.refinements += c.h_ints[9];
+		}
+		++rep.micro_steps;
+		// check_for_end_of_sweep (als.cpp:426-475)
+		if ((!inc && cur == first) || (inc && cur == last - S)) {
+			++half;
+			last_e2 = last_e;
+			last_e = energy;
+			s.gather_block(cur);
+			energy = s.energy(cur);
+			rep.energies.push_back(energy);
+			record(inc ? 1 : 3);
+			bool target_met = false;
+			if (o.residual_target > 0) {
+				rep.residual = o.record_residuals ? rep.residuals.back() : residual(A, x, b);
+				target_met = rep.residual <= o.residual_target;
+			}
+			if (half == o.num_half_sweeps || std::fabs(last_e - energy) < o.convergence_epsilon ||
+			    std::fabs(last_e2 - energy) < o.convergence_epsilon || last - first <= S || target_met) {
+				if (canon_end && o.preserve_core_position) move_core(x, core_end, true);
+				break;
+			}
+			inc = !inc;
+		} else {
+			record(0);
+		}
+		// move_to_next_index (als.cpp:340-380)
+		if (inc) {
+			if (S == 1) move_core(x, cur + 1, true);
+			s.push_left(cur);
+			++cur;
+		} else {
+			if (S == 1) move_core(x, cur - 1, true);
+			const int kc = (S == 2 && o.exact_environment) ? cur + 1 : cur;
+			s.push_right(cur + S - 1, kc);
+			--cur;
+		}
+	}
+	rep.energy = energy;
+	rep.half_sweeps = half;
+	if (o.record_residuals && !rep.residuals.empty()) rep.residual = rep.residuals.back();
+	c.sync();
+	return rep;
+}
+
+// ------------------------------------------------------------ ALS energy gradient
+
+double als_energy_gradient(const Tensor& A, const Tensor& x, const Tensor& b, std::vector<double>& grad) {
+	Context& c = *x.ctx;
+	XTT_REQUIRE(A.op && !x.op && !b.op && x.dims == b.dims && A.dims == x.dims, "dimensions of A, x and b must match");
+	const int d = x.d;
+	AlsOptions o;
+	AlsState s(c, A, const_cast<Tensor&>(x), b, o);
+	std::vector<size_t> oop(d + 2, 0), orh(d + 2, 0);
+	for (int k = 0; k <= d; ++k) {
+		oop[k + 1] = oop[k] + size_t(x.ranks[k] * A.ranks[k] * x.ranks[k]);
+		orh[k + 1] = orh[k] + size_t(b.ranks[k] * x.ranks[k]);
+	}
+	double* L = c.scratch<double>(S_ALS_FIRST + 0, oop[d + 1]);
+	double* R = c.scratch<double>(S_ALS_FIRST + 1, oop[d + 1]);
+	double* Lb = c.scratch<double>(S_ALS_FIRST + 2, orh[d + 1]);
+	double* Rb = c.scratch<double>(S_ALS_FIRST + 3, orh[d + 1]);
+	for (int k = 0; k <= d; ++k) {
+		s.st.Lop.push_back(L + oop[k]);
+		s.st.Rop.push_back(R + oop[k]);
+		s.st.Lb.push_back(Lb + orh[k]);
+		s.st.Rb.push_back(Rb + orh[k]);
+	}
+	fill(c, s.st.Lop[0], 1.0, 1);
+	fill(c, s.st.Rop[d], 1.0, 1);
+	fill(c, s.st.Lb[0], 1.0, 1);
+	fill(c, s.st.Rb[d], 1.0, 1);
+	for (int k = 0; k < d; ++k) s.push_left(k);
+	for (int k = d - 1; k >= 0; --k) s.push_right(k, k);
+	long long maxdim = 1;
+	for (int k = 0; k < d; ++k) maxdim = std::max<long long>(maxdim, x.core_size(k));
+	s.v = c.scratch<double>(S_ALS_FIRST + 4, maxdim);
+	s.bloc = c.scratch<double>(S_ALS_FIRST + 5, maxdim);
+	s.q = c.scratch<double>(S_ALS_FIRST + 6, maxdim);
+	grad.assign(x.total_size(), 0.0);
+	size_t off = 0;
+	double J = 0;
+	for (int k = 0; k < d; ++k) {
+		s.rhs(k);
+		const LocalShape sh = s.shape(k);
+		local_matvec(c, sh, s.st.Lop[k], A.core[k], nullptr, s.st.Rop[k + 1], x.core[k], s.q);
+		const long long n = sh.dim();
+		if (k == 0) {
+			dot_async(c, x.core[0], s.q, size_t(n), 12);
+			dot_async(c, x.core[0], s.bloc, size_t(n), 13);
+		}
+		// grad_k = 2 (M x_k - b_loc)
+		k_sub<<<blocks_for(n), 256, 0, c.stream>>>(s.v, s.q, s.bloc, n);
+		c.count_launch();
+		scale(c, s.v, 2.0, size_t(n));
+		XTT_CUDA(cudaMemcpyAsync(grad.data() + off, s.v, sizeof(double) * n, cudaMemcpyDeviceToHost, c.stream));
+		c.sync();
+		off += size_t(n);
+	}
+	XTT_CUDA(cudaMemcpyAsync(c.h_dbl + 12, c.d_dbl + 12, 2 * sizeof(double), cudaMemcpyDeviceToHost, c.stream));
+	c.sync();
+	J = c.h_dbl[12] - 2.0 * c.h_dbl[13];
+	return J;
+}
+
+}  // namespace xtt

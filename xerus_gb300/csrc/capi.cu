@@ -1,0 +1,473 @@
+// extern "C" entry points of libxtt.so (declared in include/xtt.h): argument
+// checks, exception-to-status translation, the host random state, and the
+// calls into the engine.
+#include <algorithm>
+#include <cstring>
+#include <new>
+#include <random>
+#include <set>
+#include <string>
+
+#include "als.cuh"
+
+namespace {
+
+thread_local std::string g_error;
+thread_local std::mt19937_64 g_engine;                   // analogue of xerus::misc::randomEngine
+thread_local std::normal_distribution<double> g_normal;  // analogue of xerus::misc::defaultNormalDistribution
+thread_local std::normal_distribution<double> g_custom;  // last non-default N(mean, stddev), reused while unchanged
+
+template <class F>
+int guard(F&& f) {
+	try {
+		f();
+		g_error.clear();
+		return XTT_OK;
+	} catch (const xtt::Error& e) {
+		g_error = e.what();
+		return e.code;
+	} catch (const std::bad_alloc&) {
+		g_error = "host allocation failed";
+		return XTT_ERR_NO_MEMORY;
+	} catch (const std::exception& e) {
+		g_error = e.what();
+		return XTT_ERR_ARGUMENT;
+	}
+}
+
+std::normal_distribution<double>& dist_for(double mean, double stddev) {
+	if (mean == 0.0 && stddev == 1.0) return g_normal;
+	if (g_custom.mean() != mean || g_custom.stddev() != stddev) g_custom = std::normal_distribution<double>(mean, stddev);
+	return g_custom;
+}
+
+}  // namespace
+
+struct xtt_context {
+	xtt::Context* c;
+};
+struct xtt_tensor {
+	xtt::Tensor* t;
+};
+
+#define ARG(cond, msg) XTT_REQUIRE(cond, msg)
+
+extern "C" {
+
+const char* xtt_last_error(void) { return g_error.c_str(); }
+const char* xtt_version(void) { return "xtt 0.1 (GB300 sm_103a; xerus 3.0.1 sweep path)"; }
+
+int xtt_context_create(int device, xtt_context** out) {
+	return guard([&] {
+		ARG(out, "out is NULL");
+		*out = nullptr;
+		auto* c = new xtt::Context(device);
+		*out = new xtt_context{c};
+	});
+}
+
+int xtt_context_destroy(xtt_context* ctx) {
+	return guard([&] {
+		if (!ctx) return;
+		delete ctx->c;
+		delete ctx;
+	});
+}
+
+int xtt_context_set_stream(xtt_context* ctx, void* stream) {
+	return guard([&] {
+		ARG(ctx, "ctx is NULL");
+		XTT_CUDA(cudaStreamSynchronize(ctx->c->stream));
+		ctx->c->stream = stream ? static_cast<cudaStream_t>(stream) : ctx->c->own;
+	});
+}
+
+int xtt_context_synchronize(xtt_context* ctx) {
+	return guard([&] {
+		ARG(ctx, "ctx is NULL");
+		ctx->c->sync();
+	});
+}
+
+int xtt_context_kernel_launches(xtt_context* ctx, int64_t* count) {
+	return guard([&] {
+		ARG(ctx && count, "NULL argument");
+		*count = ctx->c->launches;
+	});
+}
+
+int xtt_tensor_create(xtt_context* ctx, int is_operator, int64_t order, const int64_t* dims, const int64_t* ranks,
+                      xtt_tensor** out) {
+	return guard([&] {
+		ARG(ctx && dims && ranks && out, "NULL argument");
+		ARG(order > 0 && order < (1 << 20), "order must be positive");
+		*out = nullptr;
+		auto* t = new xtt::Tensor(ctx->c, is_operator != 0, int(order), dims, ranks);
+		*out = new xtt_tensor{t};
+	});
+}
+
+int xtt_tensor_destroy(xtt_tensor* t) {
+	return guard([&] {
+		if (!t) return;
+		delete t->t;
+		delete t;
+	});
+}
+
+int xtt_tensor_copy(const xtt_tensor* src, xtt_tensor** out) {
+	return guard([&] {
+		ARG(src && out, "NULL argument");
+		const xtt::Tensor& s = *src->t;
+		auto* t = new xtt::Tensor(s.ctx, s.op, s.d, s.dims.data(), s.ranks.data());
+		t->copy_from(s);
+		*out = new xtt_tensor{t};
+	});
+}
+
+int xtt_tensor_order(const xtt_tensor* t, int64_t* order) {
+	return guard([&] {
+		ARG(t && order, "NULL argument");
+		*order = t->t->d;
+	});
+}
+
+int xtt_tensor_dims(const xtt_tensor* t, int64_t* dims) {
+	return guard([&] {
+		ARG(t && dims, "NULL argument");
+		std::copy(t->t->dims.begin(), t->t->dims.end(), dims);
+	});
+}
+
+int xtt_tensor_ranks(const xtt_tensor* t, int64_t* ranks) {
+	return guard([&] {
+		ARG(t && ranks, "NULL argument");
+		std::copy(t->t->ranks.begin(), t->t->ranks.end(), ranks);
+	});
+}
+
+int xtt_tensor_size(const xtt_tensor* t, int64_t* count) {
+	return guard([&] {
+		ARG(t && count, "NULL argument");
+		*count = int64_t(t->t->total_size());
+	});
+}
+
+int xtt_tensor_set_cores(xtt_tensor* t, const double* host, int64_t count) {
+	return guard([&] {
+		ARG(t && host, "NULL argument");
+		xtt::Tensor& x = *t->t;
+		ARG(count == int64_t(x.total_size()), "count does not match the tensor size");
+		size_t off = 0;
+		for (int k = 0; k < x.d; ++k) {
+			XTT_CUDA(cudaMemcpyAsync(x.core[k], host + off, x.core_size(k) * sizeof(double), cudaMemcpyHostToDevice,
+			                         x.ctx->stream));
+			off += x.core_size(k);
+		}
+		x.ctx->sync();
+		x.canonicalized = false;
+	});
+}
+
+int xtt_tensor_get_cores(const xtt_tensor* t, double* host, int64_t count) {
+	return guard([&] {
+		ARG(t && host, "NULL argument");
+		const xtt::Tensor& x = *t->t;
+		ARG(count == int64_t(x.total_size()), "count does not match the tensor size");
+		size_t off = 0;
+		for (int k = 0; k < x.d; ++k) {
+			XTT_CUDA(cudaMemcpyAsync(host + off, x.core[k], x.core_size(k) * sizeof(double), cudaMemcpyDeviceToHost,
+			                         x.ctx->stream));
+			off += x.core_size(k);
+		}
+		x.ctx->sync();
+	});
+}
+
+int xtt_tensor_assign(xtt_tensor* t, const int64_t* ranks, const double* host, int64_t count) {
+	return guard([&] {
+		ARG(t && ranks && host, "NULL argument");
+		xtt::Tensor& x = *t->t;
+		ARG(ranks[0] == 1 && ranks[x.d] == 1, "boundary ranks must be 1");
+		size_t total = 0;
+		for (int k = 0; k < x.d; ++k) {
+			ARG(ranks[k + 1] > 0, "rank 0 is not valid");
+			total += size_t(ranks[k]) * x.n(k) * ranks[k + 1];
+		}
+		ARG(count == int64_t(total), "count does not match the ranks");
+		for (int k = 0; k < x.d; ++k) x.reshape_core(k, ranks[k], ranks[k + 1]);
+		size_t off = 0;
+		for (int k = 0; k < x.d; ++k) {
+			XTT_CUDA(cudaMemcpyAsync(x.core[k], host + off, x.core_size(k) * sizeof(double), cudaMemcpyHostToDevice,
+			                         x.ctx->stream));
+			off += x.core_size(k);
+		}
+		x.ctx->sync();
+		x.canonicalized = false;
+	});
+}
+
+int xtt_tensor_get_canonical(const xtt_tensor* t, int* canonicalized, int64_t* core_position) {
+	return guard([&] {
+		ARG(t && canonicalized && core_position, "NULL argument");
+		*canonicalized = t->t->canonicalized ? 1 : 0;
+		*core_position = t->t->core_position;
+	});
+}
+
+int xtt_tensor_set_canonical(xtt_tensor* t, int canonicalized, int64_t core_position) {
+	return guard([&] {
+		ARG(t, "NULL argument");
+		ARG(core_position >= 0 && core_position < t->t->d, "illegal core position");
+		t->t->canonicalized = canonicalized != 0;
+		t->t->core_position = core_position;
+	});
+}
+
+int xtt_tensor_scale(xtt_tensor* t, double f) {
+	return guard([&] {
+		ARG(t, "NULL argument");
+		xtt::Tensor& x = *t->t;
+		const int k = x.canonicalized ? int(x.core_position) : 0;
+		xtt::scale(*x.ctx, x.core[k], f, x.core_size(k));
+		x.ctx->sync();
+	});
+}
+
+int xtt_random_seed(uint64_t seed) {
+	return guard([&] {
+		g_engine.seed(seed);
+		g_normal.reset();
+		g_custom.reset();
+	});
+}
+
+int xtt_random_normal(double mean, double stddev, int64_t count, double* out) {
+	return guard([&] {
+		ARG(out || count == 0, "NULL argument");
+		auto& dist = dist_for(mean, stddev);
+		for (int64_t i = 0; i < count; ++i) out[i] = dist(g_engine);
+	});
+}
+
+int xtt_tensor_random(xtt_context* ctx, int64_t order, const int64_t* dims, const int64_t* inner_ranks, double mean,
+                      double stddev, xtt_tensor** out) {
+	return guard([&] {
+		ARG(ctx && dims && out && (order == 1 || inner_ranks), "NULL argument");
+		ARG(order > 0, "order must be positive");
+		*out = nullptr;
+		std::vector<int64_t> dv(dims, dims + order), inner(order > 1 ? inner_ranks : dims, order > 1 ? inner_ranks + order - 1 : dims);
+		for (auto v : dv) ARG(v > 0, "Trying to construct a TTTensor with dimension 0 is not possible.");
+		for (auto v : inner) ARG(v > 0, "Trying to construct random TTTensor with rank 0 is illegal.");
+		auto red = xtt::reduce_to_maximal_ranks(inner, dv);
+		std::vector<int64_t> r(order + 1, 1);
+		for (int64_t k = 1; k < order; ++k) r[k] = red[k - 1];
+		auto* t = new xtt::Tensor(ctx->c, false, int(order), dv.data(), r.data());
+		xtt_tensor* h = new xtt_tensor{t};
+		try {
+			auto& dist = dist_for(mean, stddev);
+			std::vector<double> host;
+			for (int k = 0; k < t->d; ++k) {
+				host.resize(t->core_size(k));
+				for (auto& v : host) v = dist(g_engine);
+				XTT_CUDA(cudaMemcpyAsync(t->core[k], host.data(), host.size() * sizeof(double), cudaMemcpyHostToDevice,
+				                         t->ctx->stream));
+				XTT_CUDA(cudaStreamSynchronize(t->ctx->stream));
+			}
+			t->canonicalized = (order == 1);
+			t->core_position = 0;
+			xtt::move_core(*t, 0, false);
+			t->ctx->sync();
+		} catch (...) {
+			delete t;
+			delete h;
+			throw;
+		}
+		*out = h;
+	});
+}
+
+int xtt_random_positions(int64_t num, int64_t order, const int64_t* dims, int64_t* out) {
+	return guard([&] {
+		ARG(dims && (out || num == 0) && order > 0, "NULL argument");
+		double total = 1;
+		for (int64_t k = 0; k < order; ++k) {
+			ARG(dims[k] > 0, "dimension 0 is not valid");
+			total *= double(dims[k]);
+		}
+		ARG(total >= double(num), "It's impossible to perform as many measurements as requested.");
+		// SinglePointMeasurementSet::create_random_positions (measurments.cpp:222-248)
+		std::vector<std::uniform_int_distribution<size_t>> idx;
+		for (int64_t k = 0; k < order; ++k) idx.emplace_back(0, size_t(dims[k] - 1));
+		std::set<size_t> seen;
+		std::vector<std::vector<size_t>> pos;
+		pos.reserve(size_t(num));
+		std::vector<size_t> m(order);
+		while (int64_t(pos.size()) < num) {
+			size_t lin = 0;
+			for (int64_t k = 0; k < order; ++k) {
+				m[k] = idx[k](g_engine);
+				lin = lin * size_t(dims[k]) + m[k];
+			}
+			if (seen.insert(lin).second) pos.push_back(m);
+		}
+		std::sort(pos.begin(), pos.end());
+		for (int64_t s = 0; s < num; ++s)
+			for (int64_t k = 0; k < order; ++k) out[s * order + k] = int64_t(pos[s][k]);
+	});
+}
+
+int xtt_move_core(xtt_tensor* x, int64_t position, int keep_rank) {
+	return guard([&] {
+		ARG(x, "NULL argument");
+		xtt::move_core(*x->t, position, keep_rank != 0);
+		x->t->ctx->sync();
+	});
+}
+
+int xtt_round(xtt_tensor* x, const int64_t* max_ranks, double eps, double* spectra, int64_t spectra_capacity,
+              int64_t* spectra_count) {
+	return guard([&] {
+		ARG(x && (max_ranks || x->t->d == 1), "NULL argument");
+		std::vector<int64_t> mr(max_ranks, max_ranks + (x->t->d - 1));
+		std::vector<double> sp;
+		xtt::round_tt(*x->t, mr, eps, spectra ? &sp : nullptr);
+		x->t->ctx->sync();
+		if (spectra) {
+			const int64_t n = std::min<int64_t>(spectra_capacity, int64_t(sp.size()));
+			std::copy(sp.begin(), sp.begin() + n, spectra);
+			if (spectra_count) *spectra_count = int64_t(sp.size());
+		}
+	});
+}
+
+int xtt_dot(const xtt_tensor* x, const xtt_tensor* y, double* out) {
+	return guard([&] {
+		ARG(x && y && out, "NULL argument");
+		ARG(x->t->ctx == y->t->ctx, "tensors belong to different contexts");
+		*out = xtt::dot(*x->t, *y->t);
+	});
+}
+
+int xtt_frob_norm(const xtt_tensor* x, double* out) {
+	return guard([&] {
+		ARG(x && out, "NULL argument");
+		*out = xtt::frob_norm(*x->t);
+	});
+}
+
+int xtt_residual(const xtt_tensor* A, const xtt_tensor* x, const xtt_tensor* b, double* out) {
+	return guard([&] {
+		ARG(A && x && b && out, "NULL argument");
+		*out = xtt::residual(*A->t, *x->t, *b->t);
+	});
+}
+
+int xtt_entries(const xtt_tensor* x, const int64_t* positions, int64_t count, double* out) {
+	return guard([&] {
+		ARG(x && (count == 0 || (positions && out)), "NULL argument");
+		xtt::entries(*x->t, positions, count, out);
+	});
+}
+
+int xtt_als_default_options(xtt_als_options* o) {
+	return guard([&] {
+		ARG(o, "NULL argument");
+		std::memset(o, 0, sizeof(*o));
+		o->sites = 1;
+		o->local_solver = 0;
+		o->preserve_core_position = 1;
+		o->precision = XTT_PRECISION_FP64;
+		o->num_half_sweeps = 0;
+		o->convergence_epsilon = 1e-6;
+		o->local_tolerance = 1e-13;
+		o->local_max_iterations = 0;
+		o->residual_target = 0;
+		o->record_residuals = 0;
+		o->max_rank = 0;
+		o->svd_epsilon = 0;
+		o->exact_environment = 0;
+	});
+}
+
+int xtt_als(const xtt_tensor* A, xtt_tensor* x, const xtt_tensor* b, const xtt_als_options* opt,
+            xtt_als_report* report, double* residual_trace, int64_t* flag_trace, double* energy_trace,
+            int64_t trace_capacity) {
+	return guard([&] {
+		ARG(A && x && b && opt, "NULL argument");
+		ARG(opt->local_tolerance > 0 && opt->local_tolerance < 1, "local_tolerance must be in (0, 1)");
+		ARG(opt->precision == XTT_PRECISION_FP64 || opt->precision == XTT_PRECISION_MIXED, "unknown precision");
+		xtt::AlsOptions o;
+		o.sites = opt->sites;
+		o.local_solver = opt->local_solver;
+		o.preserve_core_position = opt->preserve_core_position != 0;
+		o.precision = opt->precision;
+		o.num_half_sweeps = opt->num_half_sweeps;
+		o.convergence_epsilon = opt->convergence_epsilon;
+		o.local_tolerance = opt->local_tolerance;
+		o.local_max_iterations = opt->local_max_iterations;
+		o.residual_target = opt->residual_target;
+		o.record_residuals = opt->record_residuals != 0;
+		o.max_rank = opt->max_rank;
+		o.svd_epsilon = opt->svd_epsilon;
+		o.exact_environment = opt->exact_environment != 0;
+		xtt::AlsReport r = xtt::als(*A->t, *x->t, *b->t, o);
+		if (report) {
+			report->energy = r.energy;
+			report->residual = r.residual;
+			report->half_sweeps = r.half_sweeps;
+			report->micro_steps = r.micro_steps;
+			report->local_iterations = r.local_iterations;
+			report->refinements = r.refinements;
+			report->trace_count = int64_t(std::max(r.residuals.size(), r.energies.size()));
+		}
+		if (residual_trace)
+			for (size_t i = 0; i < r.residuals.size() && int64_t(i) < trace_capacity; ++i) residual_trace[i] = r.residuals[i];
+		if (flag_trace)
+			for (size_t i = 0; i < r.flags.size() && int64_t(i) < trace_capacity; ++i) flag_trace[i] = r.flags[i];
+		if (energy_trace)
+			for (size_t i = 0; i < r.energies.size() && int64_t(i) < trace_capacity; ++i) energy_trace[i] = r.energies[i];
+	});
+}
+
+int xtt_als_energy_gradient(const xtt_tensor* A, const xtt_tensor* x, const xtt_tensor* b, double* energy,
+                            double* grad, int64_t count) {
+	return guard([&] {
+		ARG(A && x && b && energy, "NULL argument");
+		std::vector<double> g;
+		*energy = xtt::als_energy_gradient(*A->t, *x->t, *b->t, g);
+		if (grad) {
+			ARG(count == int64_t(g.size()), "count does not match the tensor size");
+			std::copy(g.begin(), g.end(), grad);
+		}
+	});
+}
+
+int xtt_adf(xtt_tensor* x, const int64_t* positions, const double* values, int64_t num, const xtt_adf_options* opt,
+            double* final_residual, double* residual_trace, int64_t trace_capacity, int64_t* trace_count) {
+	return guard([&] {
+		ARG(x && positions && values && opt, "NULL argument");
+		xtt::AdfResult r = xtt::adf(*x->t, positions, values, num, opt->max_iterations, opt->target_residual,
+		                            opt->min_decrease);
+		x->t->ctx->sync();
+		if (final_residual) *final_residual = r.residual;
+		if (residual_trace)
+			for (size_t i = 0; i < r.trace.size() && int64_t(i) < trace_capacity; ++i) residual_trace[i] = r.trace[i];
+		if (trace_count) *trace_count = int64_t(r.trace.size());
+	});
+}
+
+int xtt_adf_gradient(const xtt_tensor* x, const int64_t* positions, const double* values, int64_t num, double* loss,
+                     double* grad, int64_t count) {
+	return guard([&] {
+		ARG(x && positions && values && loss, "NULL argument");
+		std::vector<double> g;
+		*loss = xtt::adf_gradient(*x->t, positions, values, num, g);
+		if (grad) {
+			ARG(count == int64_t(g.size()), "count does not match the tensor size");
+			std::copy(g.begin(), g.end(), grad);
+		}
+	});
+}
+
+}  // extern "C"

@@ -1,0 +1,128 @@
+// Host-side engine of the TT sweep library: contexts (one CUDA stream, a
+// device status word, scratch buffers), device-resident TT tensors and the
+// operations of the xerus sweep path built from the kernels.
+//
+// Shapes are authoritative on the host. Kernels get explicit shapes; the only
+// host<->device synchronisations inside an operation are the reads of a rank
+// that a rank-revealing factorisation decided on the device (QC/CQ in
+// move_core(keepRank=false), SVD truncation in round and DMRG).
+#pragma once
+
+#include <cstdint>
+#include <vector>
+
+#include "common.cuh"
+#include "gemm.cuh"
+#include "linalg.cuh"
+
+namespace xtt {
+
+struct Context {
+	int device = 0;
+	cudaStream_t own = nullptr;
+	cudaStream_t stream = nullptr;
+	int num_sms = 0;
+	int* d_status = nullptr;       // DeviceStatus word
+	unsigned* d_barrier = nullptr; // grid barrier count/phase
+	int* d_ints = nullptr;         // small device results (ranks), 64 ints
+	int* h_ints = nullptr;         // pinned mirror
+	double* d_dbl = nullptr;       // small device results (norms, dots), 64 doubles
+	double* h_dbl = nullptr;       // pinned mirror
+	long long launches = 0;
+	struct Slot {
+		void* p = nullptr;
+		size_t bytes = 0;
+	};
+	std::vector<Slot> slots;
+
+	explicit Context(int dev);
+	~Context();
+	// Scratch buffer `id` with at least `count` elements of T (contents undefined).
+	template <class T>
+	T* scratch(int id, size_t count) {
+		return static_cast<T*>(scratch_bytes(id, count * sizeof(T)));
+	}
+	void* scratch_bytes(int id, size_t bytes);
+	void sync();                      // stream sync + device status check
+	void check_status();              // reads d_status (after a sync) and throws on failure
+	int read_int(int idx);            // sync + d_ints[idx]
+	void count_launch(int n = 1) { launches += n; }
+};
+
+// Scratch slot ids (one per purpose, so nested operations never share a buffer).
+enum ScratchId : int {
+	S_QR_Q = 0, S_QR_C, S_QR_WORK, S_GEMM_A, S_GEMM_B, S_SVD_U, S_SVD_S, S_SVD_VT, S_SVD_WORK,
+	S_ROUND_X, S_ROUND_QA, S_ROUND_QB, S_ROUND_CA, S_ROUND_CB, S_ZIP_M, S_ZIP_T, S_ZIP_M2,
+	S_RES_CORE0, S_RES_CORE1, S_RES_R, S_RED, S_ENT_META, S_ENT_CORES, S_ENT_OUT,
+	S_ALS_FIRST = 32,
+	S_ADF_FIRST = 96,
+	S_MAX = 160
+};
+
+struct Tensor {
+	Context* ctx = nullptr;
+	bool op = false;
+	int d = 0;
+	std::vector<int64_t> dims;
+	std::vector<int64_t> ranks;     // d+1, ranks[0] = ranks[d] = 1
+	std::vector<double*> core;      // device pointers
+	std::vector<size_t> cap;        // capacity (doubles) of each core buffer
+	bool canonicalized = false;
+	int64_t core_position = 0;
+
+	Tensor(Context* c, bool is_op, int order, const int64_t* dims_, const int64_t* ranks_);
+	~Tensor();
+	Tensor(const Tensor&) = delete;
+	Tensor& operator=(const Tensor&) = delete;
+
+	int64_t n(int k) const { return op ? dims[k] * dims[k] : dims[k]; }
+	size_t core_size(int k) const { return size_t(ranks[k]) * size_t(n(k)) * size_t(ranks[k + 1]); }
+	size_t total_size() const;
+	// Resize core k for new ranks (content undefined when the buffer grows).
+	void reshape_core(int k, int64_t r0, int64_t r1);
+	void copy_from(const Tensor& o);  // same order/dims; takes ranks, cores and canonical state
+};
+
+// Host-side validation of a GEMM descriptor against its operand lengths (throws).
+template <class T>
+void check_gemm(const Gemm<T>& g);
+
+// Stream-ordered helpers.
+void gemm(Context& c, const Gemm<double>& g);
+void gemm_f(Context& c, const Gemm<float>& g);
+void copy_d2d(Context& c, double* dst, const double* src, size_t count);
+void fill(Context& c, double* dst, double v, size_t count);
+void scale(Context& c, double* x, double f, size_t count);
+void scale_rows(Context& c, double* X, const double* S, int rows, int cols);  // X (rows x cols) *= S[row]
+void scale_cols(Context& c, double* X, const double* S, int rows, int cols);  // X (rows x cols) *= S[col]
+// Sum of squares of x into ctx.d_dbl[slot] (deterministic two-level reduction).
+void sumsq_async(Context& c, const double* x, size_t count, int slot);
+// sum_i a[i] * b[i] into ctx.d_dbl[slot] (deterministic two-level reduction).
+void dot_async(Context& c, const double* a, const double* b, size_t count, int slot);
+
+// TT operations (xerus semantics).
+void transfer_core(Tensor& x, int from, int to, bool allow_rank_reduction);
+void move_core(Tensor& x, int64_t pos, bool keep_rank);
+void round_tt(Tensor& x, const std::vector<int64_t>& max_ranks, double eps, std::vector<double>* spectra);
+double dot(const Tensor& x, const Tensor& y);
+double frob_norm(const Tensor& x);
+double orthogonal_norm(Tensor& x);  // destroys x's gauge (QR sweep), returns ||x||
+double residual(const Tensor& A, const Tensor& x, const Tensor& b);
+void entries(const Tensor& x, const int64_t* positions, int64_t count, double* out);
+bool exceeds_maximal_ranks(const Tensor& x);
+std::vector<int64_t> reduce_to_maximal_ranks(std::vector<int64_t> ranks, const std::vector<int64_t>& dims);
+
+// y <- A x as a TT (cores R_k r_k), allocating y's cores.
+void op_apply_tt(const Tensor& A, const Tensor& x, Tensor& y);
+
+// ADF for single-point samples (positions: N x d, row-major).
+struct AdfResult {
+	double residual = 0;
+	std::vector<double> trace;
+};
+AdfResult adf(Tensor& x, const int64_t* positions, const double* values, long long N, int64_t max_iter, double target,
+              double min_dec);
+double adf_gradient(const Tensor& x, const int64_t* positions, const double* values, long long N,
+                    std::vector<double>& grad);
+
+}  // namespace xtt

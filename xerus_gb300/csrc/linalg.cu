@@ -1,0 +1,383 @@
+// FP64 Householder QR (optionally column-pivoted, rank-revealing) and one-sided
+// Jacobi SVD, one CTA per factorisation.
+//
+// QR follows LAPACK's conventions so that rank decisions and signs agree with
+// the reference's dgeqp3/dgeqrf path (src/xerus/blasLapackWrapper.cpp:243-438):
+// reflector H = I - tau v v^T with v_j = 1, beta = -sign(alpha) ||(alpha, x)||,
+// pivot = first column of largest remaining norm, rank = first k with
+// |R[k,k]| < 16 eps R[0,0] (R[0,0] signed, as in the reference), Q formed in
+// place by backward accumulation (dorg2r's scheme).
+//
+// The SVD orthogonalises the columns of the taller orientation by plane
+// rotations (Hestenes' one-sided Jacobi, cyclic round-robin ordering so a warp
+// owns one disjoint column pair per step), then sorts the singular values in
+// descending order and applies the truncation rule of calculate_svd
+// (src/xerus/tensor.cpp:1463-1474).
+#include <cfloat>
+
+#include "linalg.cuh"
+
+namespace xtt {
+
+constexpr int kQrThreads = 512;
+constexpr int kSvdThreads = 512;
+constexpr size_t kDynSmemMax = 200 * 1024;
+
+__host__ __device__ static size_t qr_aux_doubles(int mw, int nw) { return size_t(mw < nw ? mw : nw) + size_t(nw) + size_t(nw + 1) / 2 + 2; }
+
+size_t qr_work_doubles(int m, int n) {
+	const size_t need = (qr_aux_doubles(m, n) + size_t(m) * n) * sizeof(double);
+	return need <= kDynSmemMax ? 0 : size_t(m) * n;
+}
+
+__global__ void __launch_bounds__(kQrThreads) k_qr(QrArgs a, int use_smem) {
+	extern __shared__ double dyn[];
+	__shared__ double red[16][33];
+	__shared__ double wsh[32];
+	__shared__ double sred[32];
+	__shared__ double s_scal, s_beta;
+	__shared__ int s_idx[32];
+	__shared__ int s_rank;
+	const int tid = threadIdx.x, tx = tid & 31, ty = tid >> 5;
+	const int mw = a.transpose ? a.n : a.m;
+	const int nw = a.transpose ? a.m : a.n;
+	const int kq = min(mw, nw);
+	double* tau = dyn;
+	double* cn2 = dyn + kq;
+	int* perm = reinterpret_cast<int*>(dyn + kq + nw);
+	double* W = use_smem ? dyn + qr_aux_doubles(mw, nw) : a.work;
+	auto w = [&](int i, int j) -> double& { return W[(long long)i * nw + j]; };
+
+	for (long long e = tid; e < (long long)mw * nw; e += blockDim.x) {
+		const int i = int(e / nw), j = int(e % nw);
+		W[e] = a.transpose ? a.A[(long long)j * a.lda + i] : a.A[(long long)i * a.lda + j];
+	}
+	for (int j = tid; j < nw; j += blockDim.x) perm[j] = j;
+	__syncthreads();
+	if (a.pivot) {
+		for (int cb = 0; cb < nw; cb += 32) {
+			const int c = cb + tx;
+			double part = 0;
+			if (c < nw)
+				for (int i = ty; i < mw; i += 16) part += w(i, c) * w(i, c);
+			red[ty][tx] = part;
+			__syncthreads();
+			if (ty == 0 && c < nw) {
+				double s = 0;
+				for (int t = 0; t < 16; ++t) s += red[t][tx];
+				cn2[c] = s;
+			}
+			__syncthreads();
+		}
+	}
+
+	for (int j = 0; j < kq; ++j) {
+		if (a.pivot) {
+			// first column of maximal remaining norm (idamax semantics)
+			double best = -1.0;
+			int bi = nw;
+			for (int c = j + tid; c < nw; c += blockDim.x)
+				if (cn2[c] > best) { best = cn2[c]; bi = c; }
+#pragma unroll
+			for (int o = 16; o > 0; o >>= 1) {
+				const double ob = __shfl_xor_sync(0xffffffffu, best, o);
+				const int oi = __shfl_xor_sync(0xffffffffu, bi, o);
+				if (ob > best || (ob == best && oi < bi)) { best = ob; bi = oi; }
+			}
+			if (tx == 0) { sred[ty] = best; s_idx[ty] = bi; }
+			__syncthreads();
+			if (tid == 0) {
+				double b = -1.0;
+				int ix = nw;
+				for (int t = 0; t < (int)(blockDim.x >> 5); ++t)
+					if (sred[t] > b || (sred[t] == b && s_idx[t] < ix)) { b = sred[t]; ix = s_idx[t]; }
+				s_idx[0] = ix;
+			}
+			__syncthreads();
+			const int p = s_idx[0];
+			if (p != j && p < nw) {
+				for (int i = tid; i < mw; i += blockDim.x) {
+					const double t = w(i, j);
+					w(i, j) = w(i, p);
+					w(i, p) = t;
+				}
+				if (tid == 0) {
+					const double t = cn2[j]; cn2[j] = cn2[p]; cn2[p] = t;
+					const int q = perm[j]; perm[j] = perm[p]; perm[p] = q;
+				}
+			}
+			__syncthreads();
+		}
+		// Householder reflector of column j (dlarfg)
+		double part = 0;
+		for (int i = j + 1 + tid; i < mw; i += blockDim.x) part += w(i, j) * w(i, j);
+		const double xnorm2 = block_sum(part, sred);
+		if (tid == 0) {
+			const double alpha = w(j, j);
+			if (xnorm2 == 0.0) {
+				tau[j] = 0.0;
+				s_scal = 1.0;
+				s_beta = alpha;
+			} else {
+				const double beta = -copysign(sqrt(alpha * alpha + xnorm2), alpha);
+				tau[j] = (beta - alpha) / beta;
+				s_scal = 1.0 / (alpha - beta);
+				s_beta = beta;
+			}
+		}
+		__syncthreads();
+		const double scal = s_scal;
+		for (int i = j + 1 + tid; i < mw; i += blockDim.x) w(i, j) *= scal;
+		if (tid == 0) w(j, j) = s_beta;
+		__syncthreads();
+		const double tj = tau[j];
+		if (tj != 0.0 || a.pivot) {
+			for (int cb = j + 1; cb < nw; cb += 32) {
+				const int c = cb + tx;
+				double pt = 0;
+				if (c < nw && tj != 0.0) {
+					if (ty == 0) pt = w(j, c);
+					for (int i = j + 1 + ty; i < mw; i += 16) pt += w(i, j) * w(i, c);
+				}
+				red[ty][tx] = pt;
+				__syncthreads();
+				if (ty == 0) {
+					double s = 0;
+					for (int t = 0; t < 16; ++t) s += red[t][tx];
+					wsh[tx] = tj * s;
+				}
+				__syncthreads();
+				double nrm = 0;
+				if (c < nw) {
+					const double wc = wsh[tx];
+					if (ty == 0) w(j, c) -= wc;
+					for (int i = j + 1 + ty; i < mw; i += 16) {
+						const double v = w(i, c) - wc * w(i, j);
+						w(i, c) = v;
+						nrm += v * v;
+					}
+				}
+				if (a.pivot) {
+					red[ty][tx] = nrm;
+					__syncthreads();
+					if (ty == 0 && c < nw) {
+						double s = 0;
+						for (int t = 0; t < 16; ++t) s += red[t][tx];
+						cn2[c] = s;
+					}
+				}
+				__syncthreads();
+			}
+		}
+	}
+	__syncthreads();
+	if (tid == 0) {
+		int rank = kq;
+		if (a.pivot) {
+			const double r00 = w(0, 0);
+			for (int k = 1; k < kq; ++k)
+				if (fabs(w(k, k)) < 16.0 * DBL_EPSILON * r00) { rank = k; break; }
+		}
+		s_rank = rank;
+		if (a.rank_out) *a.rank_out = rank;
+	}
+	__syncthreads();
+	const int rank = s_rank;
+	// C (upper triangle of the first `rank` rows, columns un-permuted)
+	for (long long e = tid; e < (long long)rank * nw; e += blockDim.x) {
+		const int r = int(e / nw), j = int(e % nw);
+		const double v = (r <= j) ? w(r, j) : 0.0;
+		if (!a.transpose) a.C[(long long)r * nw + perm[j]] = v;
+		else a.C[(long long)perm[j] * rank + r] = v;
+	}
+	__syncthreads();
+	// Q = H_0 ... H_{rank-1} [I; 0], in place in the first `rank` columns
+	for (int j = rank - 1; j >= 0; --j) {
+		const double tj = tau[j];
+		if (j < rank - 1 && tj != 0.0) {
+			for (int cb = j + 1; cb < rank; cb += 32) {
+				const int c = cb + tx;
+				double pt = 0;
+				if (c < rank)
+					for (int i = j + 1 + ty; i < mw; i += 16) pt += w(i, j) * w(i, c);
+				red[ty][tx] = pt;  // row j of column c is zero here
+				__syncthreads();
+				if (ty == 0) {
+					double s = 0;
+					for (int t = 0; t < 16; ++t) s += red[t][tx];
+					wsh[tx] = tj * s;
+				}
+				__syncthreads();
+				if (c < rank) {
+					const double wc = wsh[tx];
+					if (ty == 0) w(j, c) = -wc;
+					for (int i = j + 1 + ty; i < mw; i += 16) w(i, c) -= wc * w(i, j);
+				}
+				__syncthreads();
+			}
+		}
+		for (int i = tid; i < mw; i += blockDim.x) {
+			if (i > j) w(i, j) *= -tj;
+			else if (i == j) w(i, j) = 1.0 - tj;
+			else w(i, j) = 0.0;
+		}
+		__syncthreads();
+	}
+	for (long long e = tid; e < (long long)mw * rank; e += blockDim.x) {
+		const int i = int(e / rank), c = int(e % rank);
+		const double v = w(i, c);
+		if (!a.transpose) a.Q[(long long)i * rank + c] = v;
+		else a.Q[(long long)c * mw + i] = v;
+	}
+}
+
+void launch_qr(const QrArgs& a, cudaStream_t s) {
+	const int mw = a.transpose ? a.n : a.m, nw = a.transpose ? a.m : a.n;
+	const size_t aux = qr_aux_doubles(mw, nw) * sizeof(double);
+	const size_t full = aux + size_t(mw) * nw * sizeof(double);
+	const int use_smem = full <= kDynSmemMax ? 1 : 0;
+	XTT_REQUIRE(use_smem || a.work, "QR workspace missing");
+	XTT_REQUIRE(aux <= kDynSmemMax, "QR: too many columns");
+	static bool attr = false;
+	if (!attr) {
+		XTT_CUDA(cudaFuncSetAttribute(k_qr, cudaFuncAttributeMaxDynamicSharedMemorySize, int(kDynSmemMax)));
+		attr = true;
+	}
+	k_qr<<<1, kQrThreads, use_smem ? full : aux, s>>>(a, use_smem);
+	XTT_CUDA(cudaGetLastError());
+}
+
+// ------------------------------------------------------------------- SVD
+
+__host__ __device__ static size_t svd_aux_doubles(int q) { return 2 * size_t(q) + 2; }
+
+size_t svd_work_doubles(int m, int n) {
+	const int p = std::max(m, n), q = std::min(m, n);
+	const size_t need = (svd_aux_doubles(q) + size_t(p) * q + size_t(q) * q) * sizeof(double);
+	return need <= kDynSmemMax ? 0 : size_t(p) * q + size_t(q) * q;
+}
+
+__global__ void __launch_bounds__(kSvdThreads) k_svd(SvdArgs a, int use_smem) {
+	extern __shared__ double dyn[];
+	__shared__ int s_rot, s_rank;
+	const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5, nwarps = blockDim.x >> 5;
+	const bool tall = a.m >= a.n;
+	const int p = tall ? a.m : a.n, q = tall ? a.n : a.m;
+	const int qe = q + (q & 1);
+	double* sig = dyn;
+	int* order = reinterpret_cast<int*>(dyn + q);
+	double* B = use_smem ? dyn + svd_aux_doubles(q) : a.work;  // column-major p x q
+	double* V = B + (long long)p * q;                            // column-major q x q
+	for (long long e = tid; e < (long long)p * q; e += blockDim.x) {
+		const int c = int(e / p), i = int(e % p);
+		B[e] = tall ? a.X[(long long)i * a.ldx + c] : a.X[(long long)c * a.ldx + i];
+	}
+	for (long long e = tid; e < (long long)q * q; e += blockDim.x) V[e] = (e / q == e % q) ? 1.0 : 0.0;
+	__syncthreads();
+	const double tol = DBL_EPSILON * sqrt(double(p));
+	int sweep = 0;
+	bool converged = (q < 2);
+	for (; sweep < a.max_sweeps && !converged; ++sweep) {
+		if (tid == 0) s_rot = 0;
+		__syncthreads();
+		for (int step = 0; step < qe - 1; ++step) {
+			for (int pr = warp; pr < qe / 2; pr += nwarps) {
+				const int k1 = pr, k2 = qe - 1 - pr;
+				const int i = (k1 == 0) ? 0 : ((k1 - 1 + step) % (qe - 1)) + 1;
+				const int j = (k2 == 0) ? 0 : ((k2 - 1 + step) % (qe - 1)) + 1;
+				if (i >= q || j >= q) continue;
+				double* bi = B + (long long)i * p;
+				double* bj = B + (long long)j * p;
+				double al = 0, be = 0, ga = 0;
+				for (int r = lane; r < p; r += 32) {
+					const double x = bi[r], y = bj[r];
+					al += x * x;
+					be += y * y;
+					ga += x * y;
+				}
+				al = warp_sum(al);
+				be = warp_sum(be);
+				ga = warp_sum(ga);
+				if (ga != 0.0 && fabs(ga) > tol * sqrt(al * be)) {
+					const double zeta = (be - al) / (2.0 * ga);
+					const double t = copysign(1.0, zeta) / (fabs(zeta) + sqrt(1.0 + zeta * zeta));
+					const double c = 1.0 / sqrt(1.0 + t * t), s = c * t;
+					for (int r = lane; r < p; r += 32) {
+						const double x = bi[r], y = bj[r];
+						bi[r] = c * x - s * y;
+						bj[r] = s * x + c * y;
+					}
+					double* vi = V + (long long)i * q;
+					double* vj = V + (long long)j * q;
+					for (int r = lane; r < q; r += 32) {
+						const double x = vi[r], y = vj[r];
+						vi[r] = c * x - s * y;
+						vj[r] = s * x + c * y;
+					}
+					if (lane == 0) s_rot = 1;
+				}
+			}
+			__syncthreads();
+		}
+		converged = (s_rot == 0);
+		__syncthreads();
+	}
+	if (!converged) record_status(a.status, DEV_NOT_CONVERGED);
+	for (int c = warp; c < q; c += nwarps) {
+		double s = 0;
+		for (int r = lane; r < p; r += 32) s += B[(long long)c * p + r] * B[(long long)c * p + r];
+		s = warp_sum(s);
+		if (lane == 0) sig[c] = sqrt(s);
+	}
+	__syncthreads();
+	for (int c = tid; c < q; c += blockDim.x) {
+		int pos = 0;
+		for (int o = 0; o < q; ++o) pos += (sig[o] > sig[c]) || (sig[o] == sig[c] && o < c);
+		order[pos] = c;
+	}
+	__syncthreads();
+	if (tid == 0) {
+		int rank = q;
+		if (a.max_rank > 0 && a.max_rank < rank) rank = a.max_rank;
+		const double s0 = sig[order[0]];
+		for (int j = 1; j < rank; ++j)
+			if (sig[order[j]] <= a.eps * s0) { rank = j; break; }
+		s_rank = rank;
+		if (a.rank_out) *a.rank_out = rank;
+	}
+	__syncthreads();
+	const int rank = s_rank;
+	for (int k = tid; k < rank; k += blockDim.x) a.S[k] = sig[order[k]];
+	// tall: X = Bn Sigma V^T (Bn: normalised B columns); wide: X^T = Bn Sigma V^T
+	for (long long e = tid; e < (long long)a.m * rank; e += blockDim.x) {
+		const int i = int(e / rank), k = int(e % rank), c = order[k];
+		double v;
+		if (tall) v = sig[c] > 0 ? B[(long long)c * p + i] / sig[c] : 0.0;
+		else v = V[(long long)c * q + i];
+		a.U[(long long)i * rank + k] = v;
+	}
+	for (long long e = tid; e < (long long)rank * a.n; e += blockDim.x) {
+		const int k = int(e / a.n), j = int(e % a.n), c = order[k];
+		double v;
+		if (tall) v = V[(long long)c * q + j];
+		else v = sig[c] > 0 ? B[(long long)c * p + j] / sig[c] : 0.0;
+		a.Vt[(long long)k * a.n + j] = v;
+	}
+}
+
+void launch_svd(const SvdArgs& a, cudaStream_t s) {
+	const int p = std::max(a.m, a.n), q = std::min(a.m, a.n);
+	const size_t aux = svd_aux_doubles(q) * sizeof(double);
+	const size_t full = aux + (size_t(p) * q + size_t(q) * q) * sizeof(double);
+	const int use_smem = full <= kDynSmemMax ? 1 : 0;
+	XTT_REQUIRE(use_smem || a.work, "SVD workspace missing");
+	static bool attr = false;
+	if (!attr) {
+		XTT_CUDA(cudaFuncSetAttribute(k_svd, cudaFuncAttributeMaxDynamicSharedMemorySize, int(kDynSmemMax)));
+		attr = true;
+	}
+	k_svd<<<1, kSvdThreads, use_smem ? full : aux, s>>>(a, use_smem);
+	XTT_CUDA(cudaGetLastError());
+}
+
+}  // namespace xtt

@@ -1,0 +1,47 @@
+// Dense FP64 factorisations of TT cores on the device: Householder QR (plain
+// or with column pivoting and the reference's rank rule) and a one-sided Jacobi
+// SVD with the reference's truncation rule. One CTA per factorisation; the
+// matrix is staged in shared memory when it fits, else in a global workspace.
+#pragma once
+
+#include "common.cuh"
+
+namespace xtt {
+
+struct QrArgs {
+	const double* A = nullptr;  // input, row-major with leading dimension lda
+	long long lda = 0;
+	int m = 0, n = 0;           // A is m x n
+	int transpose = 0;          // factor A^T instead of A (for LQ / CQ)
+	int pivot = 0;              // column pivoting + rank rule (QC / CQ)
+	double* work = nullptr;     // global workspace (mw*nw doubles) when shared memory is too small
+	// Outputs, written after the rank is known:
+	//  transpose == 0: A = Q C, Q (m x rank) row-major ld rank, C (rank x n) row-major ld n
+	//  transpose == 1: A = C Q, C (m x rank) row-major ld rank, Q (rank x n) row-major ld n
+	double* Q = nullptr;
+	double* C = nullptr;
+	int* rank_out = nullptr;    // device int
+};
+
+struct SvdArgs {
+	const double* X = nullptr;  // m x n row-major, leading dimension ldx
+	long long ldx = 0;
+	int m = 0, n = 0;
+	int max_rank = 0;           // 0 = no cap
+	double eps = 0.0;           // drop from the first j >= 1 with S[j] <= eps * S[0]
+	double* work = nullptr;     // global workspace when shared memory is too small
+	double* U = nullptr;        // m x rank, ld rank
+	double* S = nullptr;        // rank
+	double* Vt = nullptr;       // rank x n, ld n
+	int* rank_out = nullptr;
+	int* status = nullptr;
+	int max_sweeps = 60;
+};
+
+// Launchers (stream-ordered, asynchronous).
+void launch_qr(const QrArgs& a, cudaStream_t s);
+size_t qr_work_doubles(int m, int n);        // global workspace needed (0 if shared memory suffices)
+void launch_svd(const SvdArgs& a, cudaStream_t s);
+size_t svd_work_doubles(int m, int n);
+
+}  // namespace xtt

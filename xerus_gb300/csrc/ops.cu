@@ -1,0 +1,719 @@
+// TT operations of the xerus sweep path on device-resident tensors:
+// move_core / transfer_core, round / round_edge, the dot-product zipper,
+// frob_norm, sampled entries, operator application and the FP64 residual.
+#include <algorithm>
+#include <cmath>
+#include <cstring>
+
+#include "engine.cuh"
+
+namespace xtt {
+
+// ------------------------------------------------------------ context
+
+Context::Context(int dev) : device(dev) {
+	XTT_CUDA(cudaSetDevice(dev));
+	XTT_CUDA(cudaStreamCreateWithFlags(&own, cudaStreamNonBlocking));
+	stream = own;
+	XTT_CUDA(cudaDeviceGetAttribute(&num_sms, cudaDevAttrMultiProcessorCount, dev));
+	XTT_CUDA(cudaMalloc(&d_status, sizeof(int)));
+	XTT_CUDA(cudaMalloc(&d_barrier, 2 * sizeof(unsigned)));
+	XTT_CUDA(cudaMalloc(&d_ints, 64 * sizeof(int)));
+	XTT_CUDA(cudaMalloc(&d_dbl, 64 * sizeof(double)));
+	XTT_CUDA(cudaMallocHost(&h_ints, 64 * sizeof(int)));
+	XTT_CUDA(cudaMallocHost(&h_dbl, 64 * sizeof(double)));
+	XTT_CUDA(cudaMemset(d_status, 0, sizeof(int)));
+	XTT_CUDA(cudaMemset(d_barrier, 0, 2 * sizeof(unsigned)));
+	slots.resize(S_MAX);
+}
+
+Context::~Context() {
+	cudaSetDevice(device);
+	cudaStreamSynchronize(stream);
+	for (auto& s : slots)
+		if (s.p) cudaFree(s.p);
+	cudaFree(d_status);
+	cudaFree(d_barrier);
+	cudaFree(d_ints);
+	cudaFree(d_dbl);
+	cudaFreeHost(h_ints);
+	cudaFreeHost(h_dbl);
+	cudaStreamDestroy(own);
+}
+
+void* Context::scratch_bytes(int id, size_t bytes) {
+	XTT_REQUIRE(id >= 0 && id < S_MAX, "scratch id");
+	Slot& s = slots[id];
+	if (s.bytes < bytes) {
+		const size_t nb = std::max(bytes, s.bytes * 3 / 2) + 256;
+		if (s.p) {
+			XTT_CUDA(cudaStreamSynchronize(stream));
+			XTT_CUDA(cudaFree(s.p));
+			s.p = nullptr;
+		}
+		cudaError_t e = cudaMalloc(&s.p, nb);
+		if (e != cudaSuccess) throw Error(XTT_ERR_NO_MEMORY, "device allocation of scratch failed");
+		s.bytes = nb;
+	}
+	return s.p;
+}
+
+void Context::check_status() {
+	int st = 0;
+	XTT_CUDA(cudaMemcpy(&st, d_status, sizeof(int), cudaMemcpyDeviceToHost));
+	if (st != DEV_OK) {
+		XTT_CUDA(cudaMemset(d_status, 0, sizeof(int)));
+		XTT_CUDA(cudaMemset(d_barrier, 0, 2 * sizeof(unsigned)));
+		switch (st) {
+			case DEV_TIMEOUT: throw Error(XTT_ERR_TIMEOUT, "a device-side wait timed out");
+			case DEV_NOT_CONVERGED: throw Error(XTT_ERR_NOT_CONVERGED, "iteration cap reached on the device");
+			case DEV_BREAKDOWN: throw Error(XTT_ERR_NUMERIC, "numerical breakdown (non-SPD operator or NaN)");
+			default: throw Error(XTT_ERR_CAPACITY, "device kernel rejected a size");
+		}
+	}
+}
+
+void Context::sync() {
+	XTT_CUDA(cudaStreamSynchronize(stream));
+	check_status();
+}
+
+int Context::read_int(int idx) {
+	XTT_CUDA(cudaMemcpyAsync(h_ints + idx, d_ints + idx, sizeof(int), cudaMemcpyDeviceToHost, stream));
+	sync();
+	return h_ints[idx];
+}
+
+// ------------------------------------------------------------ tensors
+
+Tensor::Tensor(Context* c, bool is_op, int order, const int64_t* dims_, const int64_t* ranks_)
+    : ctx(c), op(is_op), d(order), dims(dims_, dims_ + order), ranks(ranks_, ranks_ + order + 1) {
+	XTT_REQUIRE(order >= 1, "order must be positive");
+	XTT_REQUIRE(ranks[0] == 1 && ranks[order] == 1, "boundary ranks must be 1");
+	for (int k = 0; k < order; ++k) XTT_REQUIRE(dims[k] > 0, "dimension 0 is not valid");
+	for (int k = 0; k <= order; ++k) XTT_REQUIRE(ranks[k] > 0, "rank 0 is not valid");
+	core.assign(d, nullptr);
+	cap.assign(d, 0);
+	for (int k = 0; k < d; ++k) {
+		const size_t sz = core_size(k);
+		if (cudaMalloc(&core[k], std::max<size_t>(sz, 1) * sizeof(double)) != cudaSuccess)
+			throw Error(XTT_ERR_NO_MEMORY, "device allocation of a TT core failed");
+		cap[k] = std::max<size_t>(sz, 1);
+		XTT_CUDA(cudaMemsetAsync(core[k], 0, sz * sizeof(double), ctx->stream));
+	}
+}
+
+Tensor::~Tensor() {
+	if (ctx) cudaStreamSynchronize(ctx->stream);
+	for (double* p : core)
+		if (p) cudaFree(p);
+}
+
+size_t Tensor::total_size() const {
+	size_t s = 0;
+	for (int k = 0; k < d; ++k) s += core_size(k);
+	return s;
+}
+
+void Tensor::reshape_core(int k, int64_t r0, int64_t r1) {
+	const size_t sz = size_t(r0) * size_t(n(k)) * size_t(r1);
+	if (sz > cap[k]) {
+		XTT_CUDA(cudaStreamSynchronize(ctx->stream));
+		XTT_CUDA(cudaFree(core[k]));
+		core[k] = nullptr;
+		const size_t nc = std::max(sz, cap[k] * 3 / 2);
+		if (cudaMalloc(&core[k], nc * sizeof(double)) != cudaSuccess)
+			throw Error(XTT_ERR_NO_MEMORY, "device allocation of a TT core failed");
+		cap[k] = nc;
+	}
+	ranks[k] = r0;
+	ranks[k + 1] = r1;
+}
+
+void Tensor::copy_from(const Tensor& o) {
+	XTT_REQUIRE(o.d == d && o.dims == dims && o.op == op, "copy between different shapes");
+	for (int k = 0; k < d; ++k) {
+		const size_t sz = o.core_size(k);
+		if (sz > cap[k]) {
+			XTT_CUDA(cudaStreamSynchronize(ctx->stream));
+			XTT_CUDA(cudaFree(core[k]));
+			XTT_CUDA(cudaMalloc(&core[k], sz * sizeof(double)));
+			cap[k] = sz;
+		}
+	}
+	ranks = o.ranks;
+	for (int k = 0; k < d; ++k) copy_d2d(*ctx, core[k], o.core[k], core_size(k));
+	canonicalized = o.canonicalized;
+	core_position = o.core_position;
+}
+
+// ------------------------------------------------------------ kernels
+
+template <class T>
+__global__ void __launch_bounds__(kGemmThreads) k_gemm(Gemm<T> g) {
+	__shared__ GemmSmem<T> sm;
+	gemm_tile(g, blockIdx.x, sm);
+}
+
+template <class T>
+void check_gemm(const Gemm<T>& g) {
+	XTT_REQUIRE(g.lenA >= 0 && g.lenB >= 0 && g.lenC >= 0, "internal: GEMM launched without operand lengths");
+	XTT_REQUIRE(g.strides_nonnegative(), "internal: negative GEMM stride");
+	XTT_REQUIRE(g.K <= 0 || (g.A && g.B), "internal: GEMM operand missing");
+	XTT_REQUIRE(g.max_off_A() < g.lenA || g.K <= 0, "internal: GEMM operand A out of bounds");
+	XTT_REQUIRE(g.max_off_B() < g.lenB || g.K <= 0, "internal: GEMM operand B out of bounds");
+	XTT_REQUIRE(g.C && g.max_off_C() < g.lenC, "internal: GEMM output out of bounds");
+	XTT_REQUIRE(!g.D || g.max_off_C() < g.lenC, "internal: GEMM epilogue operand out of bounds");
+}
+template void check_gemm<double>(const Gemm<double>&);
+template void check_gemm<float>(const Gemm<float>&);
+
+void gemm(Context& c, const Gemm<double>& g) {
+	if (g.M <= 0 || g.N <= 0 || g.batch <= 0) return;
+	check_gemm(g);
+	const long long t = g.tiles();
+	XTT_REQUIRE(t < (1ll << 31), "GEMM too large");
+	k_gemm<double><<<unsigned(t), kGemmThreads, 0, c.stream>>>(g);
+	XTT_CUDA(cudaGetLastError());
+	c.count_launch();
+}
+
+void gemm_f(Context& c, const Gemm<float>& g) {
+	if (g.M <= 0 || g.N <= 0 || g.batch <= 0) return;
+	check_gemm(g);
+	k_gemm<float><<<unsigned(g.tiles()), kGemmThreads, 0, c.stream>>>(g);
+	XTT_CUDA(cudaGetLastError());
+	c.count_launch();
+}
+
+__global__ void k_fill(double* x, double v, size_t n) {
+	for (size_t i = blockIdx.x * size_t(blockDim.x) + threadIdx.x; i < n; i += size_t(gridDim.x) * blockDim.x) x[i] = v;
+}
+__global__ void k_scale(double* x, double f, size_t n) {
+	for (size_t i = blockIdx.x * size_t(blockDim.x) + threadIdx.x; i < n; i += size_t(gridDim.x) * blockDim.x) x[i] *= f;
+}
+
+static unsigned grid_for(size_t n, int threads = 256) {
+	return unsigned(std::max<size_t>(1, std::min<size_t>((n + threads - 1) / threads, 4096)));
+}
+
+void copy_d2d(Context& c, double* dst, const double* src, size_t count) {
+	if (count == 0 || dst == src) return;
+	XTT_CUDA(cudaMemcpyAsync(dst, src, count * sizeof(double), cudaMemcpyDeviceToDevice, c.stream));
+}
+
+void fill(Context& c, double* dst, double v, size_t count) {
+	if (!count) return;
+	k_fill<<<grid_for(count), 256, 0, c.stream>>>(dst, v, count);
+	XTT_CUDA(cudaGetLastError());
+	c.count_launch();
+}
+
+void scale(Context& c, double* x, double f, size_t count) {
+	if (!count) return;
+	k_scale<<<grid_for(count), 256, 0, c.stream>>>(x, f, count);
+	XTT_CUDA(cudaGetLastError());
+	c.count_launch();
+}
+
+constexpr int kRedBlocks = 64;
+
+__global__ void k_dot_partial(const double* a, const double* b, size_t n, double* partial) {
+	__shared__ double sc[32];
+	double s = 0;
+	for (size_t i = blockIdx.x * size_t(blockDim.x) + threadIdx.x; i < n; i += size_t(gridDim.x) * blockDim.x)
+		s += a[i] * b[i];
+	s = block_sum(s, sc);
+	if (threadIdx.x == 0) partial[blockIdx.x] = s;
+}
+__global__ void k_sum_partials(const double* partial, int np, double* out) {
+	__shared__ double sc[32];
+	double s = 0;
+	for (int i = threadIdx.x; i < np; i += blockDim.x) s += partial[i];
+	s = block_sum(s, sc);
+	if (threadIdx.x == 0) *out = s;
+}
+
+void dot_async(Context& c, const double* a, const double* b, size_t count, int slot) {
+	double* part = c.scratch<double>(S_RED, kRedBlocks);
+	k_dot_partial<<<kRedBlocks, 256, 0, c.stream>>>(a, b, count, part);
+	k_sum_partials<<<1, 64, 0, c.stream>>>(part, kRedBlocks, c.d_dbl + slot);
+	XTT_CUDA(cudaGetLastError());
+	c.count_launch(2);
+}
+
+void sumsq_async(Context& c, const double* x, size_t count, int slot) { dot_async(c, x, x, count, slot); }
+
+static double read_dbl(Context& c, int slot) {
+	XTT_CUDA(cudaMemcpyAsync(c.h_dbl + slot, c.d_dbl + slot, sizeof(double), cudaMemcpyDeviceToHost, c.stream));
+	c.sync();
+	return c.h_dbl[slot];
+}
+
+// out(c, a, b) = in(a, b, c) for in of shape (A, B, C)
+__global__ void k_cab(double* out, const double* in, int A, int B, int C) {
+	const size_t n = size_t(A) * B * C;
+	for (size_t e = blockIdx.x * size_t(blockDim.x) + threadIdx.x; e < n; e += size_t(gridDim.x) * blockDim.x) {
+		const int c = int(e / (size_t(A) * B));
+		const size_t r = e % (size_t(A) * B);
+		const int a = int(r / B), b = int(r % B);
+		out[e] = in[(size_t(a) * B + b) * C + c];
+	}
+}
+
+// out (M x s) = in^T (in: s x M) scaled by S per column
+__global__ void k_transpose_scale(double* out, const double* in, const double* S, int s, int M) {
+	const size_t n = size_t(s) * M;
+	for (size_t e = blockIdx.x * size_t(blockDim.x) + threadIdx.x; e < n; e += size_t(gridDim.x) * blockDim.x) {
+		const int j = int(e / s), c = int(e % s);
+		out[e] = in[size_t(c) * M + j] * S[c];
+	}
+}
+
+// rows of X (s x M) scaled by S
+__global__ void k_scale_rows(double* X, const double* S, int s, int M) {
+	const size_t n = size_t(s) * M;
+	for (size_t e = blockIdx.x * size_t(blockDim.x) + threadIdx.x; e < n; e += size_t(gridDim.x) * blockDim.x)
+		X[e] *= S[e / M];
+}
+
+__global__ void k_scale_cols(double* X, const double* S, int m, int k) {
+	const size_t n = size_t(m) * k;
+	for (size_t e = blockIdx.x * size_t(blockDim.x) + threadIdx.x; e < n; e += size_t(gridDim.x) * blockDim.x)
+		X[e] *= S[e % k];
+}
+
+void scale_rows(Context& c, double* X, const double* S, int rows, int cols) {
+	if (size_t(rows) * cols == 0) return;
+	k_scale_rows<<<grid_for(size_t(rows) * cols), 256, 0, c.stream>>>(X, S, rows, cols);
+	XTT_CUDA(cudaGetLastError());
+	c.count_launch();
+}
+
+void scale_cols(Context& c, double* X, const double* S, int rows, int cols) {
+	if (size_t(rows) * cols == 0) return;
+	k_scale_cols<<<grid_for(size_t(rows) * cols), 256, 0, c.stream>>>(X, S, rows, cols);
+	XTT_CUDA(cudaGetLastError());
+	c.count_launch();
+}
+
+// ------------------------------------------------------------ move_core
+
+std::vector<int64_t> reduce_to_maximal_ranks(std::vector<int64_t> r, const std::vector<int64_t>& n) {
+	// src/xerus/ttNetwork.cpp:369-402 with n = the product of the component's external dimensions
+	const size_t d = n.size();
+	int64_t cur = 1;
+	for (size_t i = 0; i + 1 < d; ++i) {
+		cur *= n[i];
+		if (cur < r[i]) r[i] = cur;
+		else cur = r[i];
+	}
+	cur = 1;
+	for (size_t i = 1; i < d; ++i) {
+		cur *= n[d - i];
+		if (cur < r[d - i - 1]) r[d - i - 1] = cur;
+		else cur = r[d - i - 1];
+	}
+	return r;
+}
+
+bool exceeds_maximal_ranks(const Tensor& x) {
+	std::vector<int64_t> inner(x.ranks.begin() + 1, x.ranks.end() - 1), nn(x.d);
+	for (int k = 0; k < x.d; ++k) nn[k] = x.n(k);
+	return reduce_to_maximal_ranks(inner, nn) != inner;
+}
+
+void transfer_core(Tensor& x, int from, int to, bool rr) {
+	Context& c = *x.ctx;
+	const int64_t r0 = x.ranks[from], nf = x.n(from), r1 = x.ranks[from + 1];
+	QrArgs a;
+	if (to == from + 1) {
+		const int m = int(r0 * nf), n = int(r1), kq = std::min(m, n);
+		double* Q = c.scratch<double>(S_QR_Q, size_t(m) * kq);
+		double* C = c.scratch<double>(S_QR_C, size_t(kq) * n);
+		const size_t wk = qr_work_doubles(m, n);
+		a.A = x.core[from]; a.lda = n; a.m = m; a.n = n; a.transpose = 0; a.pivot = rr ? 1 : 0;
+		a.work = wk ? c.scratch<double>(S_QR_WORK, wk) : nullptr;
+		a.Q = Q; a.C = C; a.rank_out = c.d_ints;
+		launch_qr(a, c.stream);
+		c.count_launch();
+		const int rank = rr ? c.read_int(0) : kq;
+		const int64_t nt = x.n(to), r2 = x.ranks[to + 1];
+		// new right neighbour: C (rank x r1) * core_to (r1 x nt*r2)
+		double* T = c.scratch<double>(S_GEMM_A, size_t(rank) * nt * r2);
+		Gemm<double> g;
+		g.M = rank; g.N = int(nt * r2); g.K = int(r1);
+		g.A = C; g.sAm = r1; g.sAk = 1;
+		g.B = x.core[to]; g.sBk = nt * r2; g.sBn = 1;
+		g.C = T; g.sCm = nt * r2; g.sCn = 1;
+		g.lens((long long)kq * n, (long long)x.core_size(to), (long long)rank * nt * r2);
+		gemm(c, g);
+		x.reshape_core(from, r0, rank);
+		copy_d2d(c, x.core[from], Q, size_t(m) * rank);
+		x.reshape_core(to, rank, r2);
+		copy_d2d(c, x.core[to], T, size_t(rank) * nt * r2);
+	} else {
+		XTT_REQUIRE(to + 1 == from, "transfer_core between non-neighbours");
+		const int m = int(r0), n = int(nf * r1), kq = std::min(m, n);
+		double* Q = c.scratch<double>(S_QR_Q, size_t(kq) * n);
+		double* C = c.scratch<double>(S_QR_C, size_t(m) * kq);
+		const size_t wk = qr_work_doubles(n, m);
+		a.A = x.core[from]; a.lda = n; a.m = m; a.n = n; a.transpose = 1; a.pivot = rr ? 1 : 0;
+		a.work = wk ? c.scratch<double>(S_QR_WORK, wk) : nullptr;
+		a.Q = Q; a.C = C; a.rank_out = c.d_ints;
+		launch_qr(a, c.stream);
+		c.count_launch();
+		const int rank = rr ? c.read_int(0) : kq;
+		const int64_t rt = x.ranks[to], nt = x.n(to);
+		// new left neighbour: core_to (rt*nt x r0) * C (r0 x rank)
+		double* T = c.scratch<double>(S_GEMM_A, size_t(rt) * nt * rank);
+		Gemm<double> g;
+		g.M = int(rt * nt); g.N = rank; g.K = int(r0);
+		g.A = x.core[to]; g.sAm = r0; g.sAk = 1;
+		g.B = C; g.sBk = rank; g.sBn = 1;
+		g.C = T; g.sCm = rank; g.sCn = 1;
+		g.lens((long long)x.core_size(to), (long long)m * kq, (long long)rt * nt * rank);
+		gemm(c, g);
+		x.reshape_core(from, rank, r1);
+		copy_d2d(c, x.core[from], Q, size_t(rank) * n);
+		x.reshape_core(to, rt, rank);
+		copy_d2d(c, x.core[to], T, size_t(rt) * nt * rank);
+	}
+}
+
+void move_core(Tensor& x, int64_t pos, bool keep_rank) {
+	// TTNetwork::move_core, src/xerus/ttNetwork.cpp:581-628
+	XTT_REQUIRE(pos >= 0 && pos < x.d, "illegal core position");
+	const int d = x.d;
+	if (x.canonicalized) {
+		for (int64_t n = x.core_position; n < pos; ++n) transfer_core(x, int(n), int(n + 1), !keep_rank);
+		for (int64_t n = x.core_position; n > pos; --n) transfer_core(x, int(n), int(n - 1), !keep_rank);
+	} else {
+		for (int64_t n = 0; n < pos; ++n) transfer_core(x, int(n), int(n + 1), !keep_rank);
+		for (int64_t n = d - 1; n > pos; --n) transfer_core(x, int(n), int(n - 1), !keep_rank);
+	}
+	while (exceeds_maximal_ranks(x)) {
+		for (int64_t n = pos; n > 0; --n) transfer_core(x, int(n), int(n - 1), !keep_rank);
+		for (int n = 0; n + 1 < d; ++n) transfer_core(x, n, n + 1, !keep_rank);
+		for (int64_t n = d - 1; n > pos; --n) transfer_core(x, int(n), int(n - 1), !keep_rank);
+	}
+	x.canonicalized = true;
+	x.core_position = pos;
+}
+
+// ------------------------------------------------------------ round
+
+static int svd_into(Context& c, const double* X, int m, int n, int max_rank, double eps, double*& U, double*& S,
+                    double*& Vt) {
+	const int q = std::min(m, n);
+	U = c.scratch<double>(S_SVD_U, size_t(m) * q);
+	S = c.scratch<double>(S_SVD_S, size_t(q));
+	Vt = c.scratch<double>(S_SVD_VT, size_t(q) * n);
+	SvdArgs a;
+	a.X = X; a.ldx = n; a.m = m; a.n = n; a.max_rank = max_rank; a.eps = eps;
+	const size_t wk = svd_work_doubles(m, n);
+	a.work = wk ? c.scratch<double>(S_SVD_WORK, wk) : nullptr;
+	a.U = U; a.S = S; a.Vt = Vt; a.rank_out = c.d_ints + 1; a.status = c.d_status;
+	launch_svd(a, c.stream);
+	c.count_launch();
+	return c.read_int(1);
+}
+
+static void round_edge(Tensor& x, int from, int to, int64_t max_rank, double eps, std::vector<double>* spectra) {
+	// TensorNetwork::round_edge (src/xerus/tensorNetwork.cpp:678-818) for from = core k+1, to = core k.
+	Context& c = *x.ctx;
+	const int64_t r = x.ranks[from], nF = x.n(from), rF = x.ranks[from + 1];
+	const int64_t rT = x.ranks[to], nT = x.n(to);
+	const double sizeF = double(r * nF * rF), sizeT = double(rT * nT * r);
+	const int mr = max_rank >= (int64_t(1) << 31) - 1 ? 0 : int(max_rank);
+	double *U, *S, *Vt;
+	int s;
+	if (5.0 * sizeF * sizeT >= 6.0 * std::pow(double(r), 4)) {
+		// F = C_A Q_F (CQ), T = Q_T C_B (QC), X = C_A^T C_B^T
+		QrArgs a;
+		const int mF = int(r), nFc = int(nF * rF);
+		double* CA = c.scratch<double>(S_ROUND_CA, size_t(mF) * std::min(mF, nFc));
+		double* QF = c.scratch<double>(S_ROUND_QA, size_t(std::min(mF, nFc)) * nFc);
+		size_t wk = qr_work_doubles(nFc, mF);
+		a.A = x.core[from]; a.lda = nFc; a.m = mF; a.n = nFc; a.transpose = 1; a.pivot = 1;
+		a.work = wk ? c.scratch<double>(S_QR_WORK, wk) : nullptr;
+		a.Q = QF; a.C = CA; a.rank_out = c.d_ints + 2;
+		launch_qr(a, c.stream);
+		c.count_launch();
+		const int mT = int(rT * nT), nTc = int(r);
+		double* QT = c.scratch<double>(S_ROUND_QB, size_t(mT) * std::min(mT, nTc));
+		double* CB = c.scratch<double>(S_ROUND_CB, size_t(std::min(mT, nTc)) * nTc);
+		wk = qr_work_doubles(mT, nTc);
+		QrArgs b;
+		b.A = x.core[to]; b.lda = nTc; b.m = mT; b.n = nTc; b.transpose = 0; b.pivot = 1;
+		b.work = wk ? c.scratch<double>(S_ROUND_X, wk) : nullptr;  // not S_QR_WORK: may run concurrently in the future
+		b.Q = QT; b.C = CB; b.rank_out = c.d_ints + 3;
+		launch_qr(b, c.stream);
+		c.count_launch();
+		const int ka = c.read_int(2), kb = c.read_int(3);
+		double* X = c.scratch<double>(S_GEMM_B, size_t(ka) * kb);
+		Gemm<double> g;
+		g.M = ka; g.N = kb; g.K = int(r);
+		g.A = CA; g.sAm = 1; g.sAk = ka;
+		g.B = CB; g.sBk = 1; g.sBn = r;
+		g.C = X; g.sCm = kb; g.sCn = 1;
+		g.lens((long long)mF * std::min(mF, nFc), (long long)std::min(mT, nTc) * nTc, (long long)ka * kb);
+		gemm(c, g);
+		s = svd_into(c, X, ka, kb, mr, eps, U, S, Vt);
+		// coreB = S Vt ; F' = U^T Q_F ; T' = Q_T coreB^T
+		scale_rows(c, Vt, S, s, kb);
+		double* Fn = c.scratch<double>(S_RES_CORE0, size_t(s) * nFc);
+		Gemm<double> gf;
+		gf.M = s; gf.N = nFc; gf.K = ka;
+		gf.A = U; gf.sAm = 1; gf.sAk = s;
+		gf.B = QF; gf.sBk = nFc; gf.sBn = 1;
+		gf.C = Fn; gf.sCm = nFc; gf.sCn = 1;
+		gf.lens((long long)ka * std::min(ka, kb), (long long)std::min(mF, nFc) * nFc, (long long)s * nFc);
+		gemm(c, gf);
+		double* Tn = c.scratch<double>(S_RES_CORE1, size_t(mT) * s);
+		Gemm<double> gt;
+		gt.M = mT; gt.N = s; gt.K = kb;
+		gt.A = QT; gt.sAm = kb; gt.sAk = 1;
+		gt.B = Vt; gt.sBk = 1; gt.sBn = kb;
+		gt.C = Tn; gt.sCm = s; gt.sCn = 1;
+		gt.lens((long long)mT * std::min(mT, nTc), (long long)std::min(ka, kb) * kb, (long long)mT * s);
+		gemm(c, gt);
+		x.reshape_core(from, s, rF);
+		copy_d2d(c, x.core[from], Fn, size_t(s) * nFc);
+		x.reshape_core(to, rT, s);
+		copy_d2d(c, x.core[to], Tn, size_t(mT) * s);
+	} else {
+		// X = F^T T^T : (nF rF) x (rT nT)
+		const int mX = int(nF * rF), nX = int(rT * nT);
+		double* X = c.scratch<double>(S_GEMM_B, size_t(mX) * nX);
+		Gemm<double> g;
+		g.M = mX; g.N = nX; g.K = int(r);
+		g.A = x.core[from]; g.sAm = 1; g.sAk = nF * rF;
+		g.B = x.core[to]; g.sBk = 1; g.sBn = r;
+		g.C = X; g.sCm = nX; g.sCn = 1;
+		g.lens((long long)x.core_size(from), (long long)x.core_size(to), (long long)mX * nX);
+		gemm(c, g);
+		s = svd_into(c, X, mX, nX, mr, eps, U, S, Vt);
+		x.reshape_core(from, s, rF);
+		k_cab<<<grid_for(size_t(mX) * s), 256, 0, c.stream>>>(x.core[from], U, int(nF), int(rF), s);
+		x.reshape_core(to, rT, s);
+		k_transpose_scale<<<grid_for(size_t(nX) * s), 256, 0, c.stream>>>(x.core[to], Vt, S, s, nX);
+		c.count_launch(2);
+	}
+	XTT_CUDA(cudaGetLastError());
+	if (spectra) {
+		std::vector<double> h(s);
+		XTT_CUDA(cudaMemcpyAsync(h.data(), S, sizeof(double) * s, cudaMemcpyDeviceToHost, c.stream));
+		c.sync();
+		spectra->insert(spectra->end(), h.begin(), h.end());
+	}
+}
+
+void round_tt(Tensor& x, const std::vector<int64_t>& max_ranks, double eps, std::vector<double>* spectra) {
+	// TTNetwork::round(maxRanks, eps), src/xerus/ttNetwork.cpp:643-665
+	XTT_REQUIRE(eps < 1.0 && eps >= 0.0, "_eps must be in [0, 1)");
+	XTT_REQUIRE(int(max_ranks.size()) + 1 == x.d, "there must be exactly order-1 maxRanks");
+	for (auto m : max_ranks) XTT_REQUIRE(m > 0, "rounding to rank 0 is not possible");
+	const bool init_canon = x.canonicalized;
+	const int64_t init_pos = x.core_position;
+	const int d = x.d;
+	move_core(x, d - 1, false);
+	for (int i = 0; i + 1 < d; ++i) round_edge(x, d - 1 - i, d - 2 - i, max_ranks[d - 2 - i], eps, spectra);
+	x.canonicalized = true;
+	x.core_position = 0;
+	if (init_canon) move_core(x, init_pos, false);
+}
+
+// ------------------------------------------------------------ contractions
+
+// Zipper M_k = sum over cores 0..k-1 of x (x) y; returns <x, y>.
+double dot(const Tensor& x, const Tensor& y) {
+	XTT_REQUIRE(x.d == y.d && x.dims == y.dims && x.op == y.op, "dot of tensors with different dimensions");
+	Context& c = *x.ctx;
+	int64_t maxr = 1;
+	for (int k = 0; k <= x.d; ++k) maxr = std::max({maxr, x.ranks[k], y.ranks[k]});
+	int64_t maxn = 1;
+	for (int k = 0; k < x.d; ++k) maxn = std::max(maxn, x.n(k));
+	double* M = c.scratch<double>(S_ZIP_M, size_t(maxr) * maxr);
+	double* M2 = c.scratch<double>(S_ZIP_M2, size_t(maxr) * maxr);
+	double* T = c.scratch<double>(S_ZIP_T, size_t(maxr) * maxn * maxr);
+	fill(c, M, 1.0, 1);
+	for (int k = 0; k < x.d; ++k) {
+		const int64_t rx = x.ranks[k], rx1 = x.ranks[k + 1], ry = y.ranks[k], ry1 = y.ranks[k + 1], n = x.n(k);
+		Gemm<double> g;  // T[b][(i, a')] = sum_a M[a][b] x[a][(i, a')]
+		g.M = int(ry); g.N = int(n * rx1); g.K = int(rx);
+		g.A = M; g.sAm = 1; g.sAk = ry;
+		g.B = x.core[k]; g.sBk = n * rx1; g.sBn = 1;
+		g.C = T; g.sCm = n * rx1; g.sCn = 1;
+		g.lens(maxr * maxr, (long long)x.core_size(k), maxr * maxn * maxr);
+		gemm(c, g);
+		Gemm<double> h;  // M'[a'][b'] = sum_{(b,i)} T[(b,i)][a'] y[(b,i)][b']
+		h.M = int(rx1); h.N = int(ry1); h.K = int(ry * n);
+		h.A = T; h.sAm = 1; h.sAk = rx1;
+		h.B = y.core[k]; h.sBk = ry1; h.sBn = 1;
+		h.C = M2; h.sCm = ry1; h.sCn = 1;
+		h.lens(maxr * maxn * maxr, (long long)y.core_size(k), maxr * maxr);
+		gemm(c, h);
+		std::swap(M, M2);
+	}
+	XTT_CUDA(cudaMemcpyAsync(c.h_dbl, M, sizeof(double), cudaMemcpyDeviceToHost, c.stream));
+	c.sync();
+	return c.h_dbl[0];
+}
+
+double frob_norm(const Tensor& x) {
+	// TTNetwork::frob_norm, src/xerus/ttNetwork.cpp:781-789
+	if (x.canonicalized) {
+		Context& c = *x.ctx;
+		const int k = int(x.core_position);
+		sumsq_async(c, x.core[k], x.core_size(k), 0);
+		return std::sqrt(read_dbl(c, 0));
+	}
+	return std::sqrt(dot(x, x));
+}
+
+double orthogonal_norm(Tensor& x) {
+	for (int k = 0; k + 1 < x.d; ++k) transfer_core(x, k, k + 1, false);
+	x.canonicalized = true;
+	x.core_position = x.d - 1;
+	Context& c = *x.ctx;
+	sumsq_async(c, x.core[x.d - 1], x.core_size(x.d - 1), 0);
+	return std::sqrt(read_dbl(c, 0));
+}
+
+// y[(K,a), i, (L,b)] = sum_j A[K,i,j,L] x[a,j,b]
+__global__ void k_op_apply(double* y, const double* A, const double* x, int K, int L, int n, int ra, int rb) {
+	const size_t total = size_t(K) * ra * n * L * rb;
+	for (size_t e = blockIdx.x * size_t(blockDim.x) + threadIdx.x; e < total; e += size_t(gridDim.x) * blockDim.x) {
+		size_t t = e;
+		const int b = int(t % rb); t /= rb;
+		const int l = int(t % L); t /= L;
+		const int i = int(t % n); t /= n;
+		const int a = int(t % ra); t /= ra;
+		const int k = int(t);
+		double s = 0;
+		for (int j = 0; j < n; ++j)
+			s += A[((size_t(k) * n + i) * n + j) * L + l] * x[(size_t(a) * n + j) * rb + b];
+		y[e] = s;
+	}
+}
+
+void op_apply_tt(const Tensor& A, const Tensor& x, Tensor& y) {
+	XTT_REQUIRE(A.op && !x.op && A.d == x.d && A.dims == x.dims, "operator and tensor dimensions differ");
+	Context& c = *x.ctx;
+	for (int k = 0; k < x.d; ++k) {
+		const int K = int(A.ranks[k]), L = int(A.ranks[k + 1]), ra = int(x.ranks[k]), rb = int(x.ranks[k + 1]);
+		const int n = int(x.dims[k]);
+		y.reshape_core(k, int64_t(K) * ra, int64_t(L) * rb);
+		k_op_apply<<<grid_for(y.core_size(k)), 256, 0, c.stream>>>(y.core[k], A.core[k], x.core[k], K, L, n, ra, rb);
+		c.count_launch();
+	}
+	XTT_CUDA(cudaGetLastError());
+	y.canonicalized = false;
+}
+
+// Block core of p - q (TT sum of p and -q, src/xerus/ttNetwork.cpp:796-856):
+// out (P0+Q0 or 1, n, P1+Q1 or 1) with p in the leading block, -q (first core) / q in the trailing one.
+__global__ void k_block_core(double* out, const double* p, const double* q, int P0, int P1, int Q0, int Q1, int n,
+                             int first, int last) {
+	const int O0 = first ? 1 : P0 + Q0, O1 = last ? 1 : P1 + Q1;
+	const size_t total = size_t(O0) * n * O1;
+	for (size_t e = blockIdx.x * size_t(blockDim.x) + threadIdx.x; e < total; e += size_t(gridDim.x) * blockDim.x) {
+		const int o1 = int(e % O1);
+		const int i = int((e / O1) % n);
+		const int o0 = int(e / (size_t(O1) * n));
+		double v = 0;
+		// p block at (0.., 0..)
+		if (o0 < P0 && o1 < P1) v += p[(size_t(o0) * n + i) * P1 + o1];
+		const int q0 = first ? o0 : o0 - P0, q1 = last ? o1 : o1 - P1;
+		if (q0 >= 0 && q0 < Q0 && q1 >= 0 && q1 < Q1) v += (first ? -1.0 : 1.0) * q[(size_t(q0) * n + i) * Q1 + q1];
+		out[e] = v;
+	}
+}
+
+double residual(const Tensor& A, const Tensor& x, const Tensor& b) {
+	XTT_REQUIRE(x.dims == b.dims, "x and b dimensions differ");
+	Context& c = *x.ctx;
+	const int d = x.d;
+	std::vector<int64_t> r(d + 1, 1);
+	Tensor ax(&c, false, d, x.dims.data(), r.data());
+	op_apply_tt(A, x, ax);
+	Tensor y(&c, false, d, x.dims.data(), r.data());
+	if (d == 1) {
+		y.reshape_core(0, 1, 1);
+		k_block_core<<<grid_for(x.dims[0]), 256, 0, c.stream>>>(y.core[0], ax.core[0], b.core[0], 1, 1, 1, 1,
+		                                                        int(x.dims[0]), 1, 1);
+		c.count_launch();
+	} else {
+		for (int k = 0; k < d; ++k) {
+			const int P0 = int(ax.ranks[k]), P1 = int(ax.ranks[k + 1]), Q0 = int(b.ranks[k]), Q1 = int(b.ranks[k + 1]);
+			const int first = k == 0, last = k == d - 1;
+			y.reshape_core(k, first ? 1 : P0 + Q0, last ? 1 : P1 + Q1);
+			k_block_core<<<grid_for(y.core_size(k)), 256, 0, c.stream>>>(y.core[k], ax.core[k], b.core[k], P0, P1, Q0,
+			                                                              Q1, int(x.dims[k]), first, last);
+			c.count_launch();
+		}
+	}
+	XTT_CUDA(cudaGetLastError());
+	const double ny = orthogonal_norm(y);
+	const double nb = frob_norm(b);
+	return ny / nb;
+}
+
+// One block per sample: v <- v * x_k[:, i_k, :]
+__global__ void k_entries(const double* const* cores, const int64_t* ranks, const int64_t* dims, int d,
+                          const int64_t* pos, int64_t count, double* out, int maxr) {
+	extern __shared__ double buf[];
+	double* v = buf;
+	double* w = buf + maxr;
+	for (int64_t s = blockIdx.x; s < count; s += gridDim.x) {
+		if (threadIdx.x == 0) v[0] = 1.0;
+		__syncthreads();
+		for (int k = 0; k < d; ++k) {
+			const int r0 = int(ranks[k]), r1 = int(ranks[k + 1]), n = int(dims[k]);
+			const int64_t i = pos[s * d + k];
+			const double* c = cores[k];
+			for (int b = threadIdx.x; b < r1; b += blockDim.x) {
+				double acc = 0;
+				for (int a = 0; a < r0; ++a) acc += v[a] * c[(size_t(a) * n + i) * r1 + b];
+				w[b] = acc;
+			}
+			__syncthreads();
+			for (int b = threadIdx.x; b < r1; b += blockDim.x) v[b] = w[b];
+			__syncthreads();
+		}
+		if (threadIdx.x == 0) out[s] = v[0];
+		__syncthreads();
+	}
+}
+
+void entries(const Tensor& x, const int64_t* positions, int64_t count, double* out) {
+	XTT_REQUIRE(!x.op, "entries of a TT operator are not supported");
+	Context& c = *x.ctx;
+	if (count == 0) return;
+	for (int64_t s = 0; s < count; ++s)
+		for (int k = 0; k < x.d; ++k)
+			XTT_REQUIRE(positions[s * x.d + k] >= 0 && positions[s * x.d + k] < x.dims[k], "position out of range");
+	int64_t maxr = 1;
+	for (auto r : x.ranks) maxr = std::max(maxr, r);
+	const size_t meta = size_t(x.d) * 3 + 1;
+	int64_t* dmeta = c.scratch<int64_t>(S_ENT_META, meta + size_t(count) * x.d);
+	std::vector<int64_t> hm(meta + size_t(count) * x.d);
+	for (int k = 0; k < x.d; ++k) { hm[k] = x.dims[k]; }
+	for (int k = 0; k <= x.d; ++k) hm[x.d + k] = x.ranks[k];
+	std::memcpy(hm.data() + meta, positions, sizeof(int64_t) * count * x.d);
+	double** dcores = c.scratch<double*>(S_ENT_CORES, x.d);
+	std::vector<double*> hc(x.core.begin(), x.core.end());
+	double* dout = c.scratch<double>(S_ENT_OUT, count);
+	XTT_CUDA(cudaMemcpyAsync(dmeta, hm.data(), hm.size() * sizeof(int64_t), cudaMemcpyHostToDevice, c.stream));
+	XTT_CUDA(cudaMemcpyAsync(dcores, hc.data(), hc.size() * sizeof(double*), cudaMemcpyHostToDevice, c.stream));
+	const unsigned blocks = unsigned(std::min<int64_t>(count, 8192));
+	k_entries<<<blocks, 128, 2 * maxr * sizeof(double), c.stream>>>(dcores, dmeta + x.d, dmeta, x.d, dmeta + meta,
+	                                                                 count, dout, int(maxr));
+	XTT_CUDA(cudaGetLastError());
+	c.count_launch();
+	XTT_CUDA(cudaMemcpyAsync(out, dout, sizeof(double) * count, cudaMemcpyDeviceToHost, c.stream));
+	c.sync();
+}
+
+}  // namespace xtt
