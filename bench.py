@@ -1,0 +1,339 @@
+"""Headline benchmark: ALS_SPD time to relative residual 1e-8 on one GB300.
+
+Workload (the reference's CPU-runnable ALS configuration, at the smallest rank
+that reaches 1e-8): d=8, n=4 Laplacian-sum TT operator (rank 2), random rank-4
+right-hand side, random normalised rank-32 start, seeded 0xBAADF00D; one step =
+one full ALS_SPD solve from the start until the FP64 residual ||Ax-b||/||b|| at
+the end of a half-sweep is <= 1e-8 (cap 20 half-sweeps).
+
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl gb300|reference]
+
+The gb300 arm times both the mixed form (FP32 CG with FP64 refinement; the
+line's `value`) and the plain FP64 form. `e2e` repeats the mixed solve through
+the C ABI from pinned host buffers with the uploads and the download inside the
+timed region. The reference arm times the CPU restatement of the reference's
+algorithm (dense LAPACK local solves) on this host's cores.
+"""
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+WORKLOAD = dict(workload="ALS_SPD d=8 n=4 Laplacian, rhs rank 4, x rank 32, to rel. residual 1e-8", d=8, n=4,
+                rhs_rank=4, x_rank=32, target=1e-8, max_half_sweeps=20, seed="0xBAADF00D")
+METRIC = "ALS/DMRG time to rel. residual 1e-8"
+SEED = 0xBAADF00D
+
+
+def parse():
+    p = argparse.ArgumentParser()
+    p.add_argument("--gpus", type=int, default=1)
+    p.add_argument("--steps", type=int, default=10)
+    p.add_argument("--warmup", type=int, default=3)
+    p.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
+    p.add_argument("--no-cpu-baseline", action="store_true")
+    return p.parse_args()
+
+
+def dist_env():
+    return int(os.environ.get("RANK", 0)), int(os.environ.get("LOCAL_RANK", 0)), int(os.environ.get("WORLD_SIZE", 1))
+
+
+class ClockSampler:
+    """nvidia-smi clock / throttle samples while the timed region runs."""
+
+    def __init__(self, gpu=0):
+        self.gpu, self.samples, self.proc = gpu, [], None
+
+    def start(self):
+        q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,clocks_event_reasons.hw_slowdown,"
+             "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
+             "clocks_event_reasons.sw_power_cap")
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.gpu), f"--query-gpu={q}", "--format=csv,noheader,nounits",
+                                          "-lms", "200"], stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.thread = threading.Thread(target=self._read, daemon=True)
+            self.thread.start()
+        except OSError:
+            self.proc = None
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.samples.append([v.strip() for v in line.split(",")])
+
+    def stop(self):
+        if not self.proc:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        time.sleep(0.3)
+        self.proc.terminate()
+        self.proc.wait(timeout=5)
+        sm = [float(s[1]) for s in self.samples if len(s) > 8 and s[1].replace(".", "").isdigit()]
+        mx = [float(s[2]) for s in self.samples if len(s) > 8 and s[2].replace(".", "").isdigit()]
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        reasons = sorted({names[i] for s in self.samples if len(s) > 8 for i in range(4) if s[5 + i] == "Active"})
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": max(mx) if mx else None,
+                "reasons": reasons, "samples": len(self.samples)}
+
+
+def make_inputs(xg, ctx):
+    """Operator, rhs and start on the device, drawn with the library's engine."""
+    xg.seed(SEED)
+    A = xg.TTOperator.from_cores(xg.laplacian_cores(WORKLOAD["d"], WORKLOAD["n"]), ctx=ctx)
+    b = xg.TTTensor.random([WORKLOAD["n"]] * WORKLOAD["d"], WORKLOAD["rhs_rank"], ctx=ctx)
+    x0 = xg.TTTensor.random([WORKLOAD["n"]] * WORKLOAD["d"], WORKLOAD["x_rank"], ctx=ctx)
+    x0 /= x0.frob_norm()
+    return A, b, x0
+
+
+def als_variant(xg, precision):
+    v = xg.ALS_SPD.copy()
+    v.convergenceEpsilon = 0.0
+    v.residual_target = WORKLOAD["target"]
+    v.precision = precision
+    return v
+
+
+def matvec_cost(ranks, opranks, dims, w):
+    """Per 1-site local matvec at each position k: flops 2 n r r' (r R + n R R' + R' r')
+    and minimal operand bytes w (r^2 R + r n r' + R n^2 R' + r'^2 R')."""
+    out = {}
+    for k in range(len(dims)):
+        r, rp, R, Rp, n = ranks[k], ranks[k + 1], opranks[k], opranks[k + 1], dims[k]
+        out[k] = (2 * n * r * rp * (r * R + n * R * Rp + Rp * rp), w * (r * r * R + r * n * rp + R * n * n * Rp + rp * rp * Rp))
+    return out
+
+
+def read_profile_traffic(name):
+    """dram bytes per launch of a kernel class from its committed ncu summary (None if absent)."""
+    path = os.path.join(ROOT, "profiles", f"{name}.md")
+    if not os.path.exists(path):
+        return None
+    for line in open(path):
+        if line.strip().startswith("traffic_bytes_per_launch:"):
+            try:
+                return float(line.split(":", 1)[1].strip().split()[0])
+            except ValueError:
+                return None
+    return None
+
+
+def run_gpu(args):
+    import torch
+    import xerus_gb300 as xg
+    from xerus_gb300 import build
+    rank, local_rank, world = dist_env()
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl", device_id=torch.device("cuda", local_rank))
+    torch.cuda.set_device(local_rank)
+    build.build()
+    ctx = xg.Context(local_rank)
+    stream = torch.cuda.current_stream()
+    ctx.set_stream(stream.cuda_stream)
+    A, b, x0 = make_inputs(xg, ctx)
+    flush = torch.empty(256 * 1024 * 1024, dtype=torch.uint8, device="cuda")  # > 129 MB L2
+
+    def barrier():
+        if world > 1:
+            torch.distributed.barrier()
+        torch.cuda.synchronize()
+
+    def solve(precision):
+        x = x0.copy()
+        v = als_variant(xg, precision)
+        v(A, x, b, WORKLOAD["max_half_sweeps"])
+        return x, v.last_report
+
+    def timed(precision, steps, warmup, profile=False):
+        for _ in range(warmup):
+            solve(precision)
+        if profile:
+            ctx.profile(True)
+        times, reports = [], []
+        launches0 = ctx.kernel_launches()
+        for _ in range(steps):
+            flush.zero_()
+            barrier()
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            e0.record(stream)
+            x, rep = solve(precision)
+            e1.record(stream)
+            barrier()
+            times.append(e0.elapsed_time(e1) / 1e3)
+            reports.append(rep)
+        launches = ctx.kernel_launches() - launches0
+        prof = {}
+        if profile:
+            for name in ("cg_fp64", "cg_mixed", "gemm", "qr", "svd"):
+                prof[name] = ctx.profile_get(name)
+            ctx.profile(False)
+        return times, reports, launches, prof, x
+
+    clocks = ClockSampler(local_rank)
+    clocks.start()
+    t_mix, rep_mix, launches_mix, _, x_mix = timed(xg.MIXED, args.steps, args.warmup)
+    t_64, rep_64, launches_64, _, x_64 = timed(xg.FP64, args.steps, args.warmup)
+    clk = clocks.stop()
+    # per-kernel-class event timing in separate (untimed) passes: events add host work
+    nprof = max(1, min(3, args.steps))
+    _, _, _, prof_mix, _ = timed(xg.MIXED, nprof, 0, profile=True)
+    _, _, _, prof_64, _ = timed(xg.FP64, nprof, 0, profile=True)
+    prof_steps = nprof
+    res_mix = xg.residual(A, x_mix, b)
+    res_64 = xg.residual(A, x_64, b)
+
+    # end to end through the C ABI: host buffers in, result out, every step
+    import ctypes
+    hA = [np.ascontiguousarray(c) for c in A.get_cores()]
+    hb, hx0 = b.get_flat(), x0.get_flat()
+    pin = lambda a: torch.from_numpy(a).pin_memory().numpy()
+    hA_flat, hb, hx0 = pin(np.concatenate([c.ravel() for c in hA])), pin(hb), pin(hx0)
+    A_ranks, b_ranks, x_ranks = A.all_ranks(), b.all_ranks(), x0.all_ranks()
+    Ad = xg.TTOperator([WORKLOAD["n"]] * WORKLOAD["d"], A_ranks, ctx=ctx)
+    bd = xg.TTTensor([WORKLOAD["n"]] * WORKLOAD["d"], b_ranks, ctx=ctx)
+    xd = xg.TTTensor([WORKLOAD["n"]] * WORKLOAD["d"], x_ranks, ctx=ctx)
+    hout = pin(np.zeros(x0.size()))
+    e2e_times = []
+    v = als_variant(xg, xg.MIXED)
+    for i in range(args.warmup + args.steps):
+        flush.zero_()
+        barrier()
+        t0 = time.perf_counter()
+        Ad.set_flat(hA_flat)
+        bd.set_flat(hb)
+        bd.assume_core_position(0)
+        xd.set_flat(hx0, ranks=x_ranks)
+        xd.assume_core_position(0)
+        v(Ad, xd, bd, WORKLOAD["max_half_sweeps"])
+        out = xd.get_flat()
+        resid = v.last_report.residual
+        torch.cuda.synchronize()
+        if i >= args.warmup:
+            e2e_times.append(time.perf_counter() - t0)
+    h2d = 8 * (hA_flat.size + hb.size + hx0.size)
+    d2h = 8 * (out.size + 1)
+
+    # roofline of the dominant kernel class (the persistent CG) over the timed mixed solves
+    ranks, opr, dims = x0.all_ranks(), A.all_ranks(), x0.dimensions
+    iters = sum(r.local_iterations for r in rep_mix) / len(rep_mix)
+    refs = sum(r.refinements for r in rep_mix) / len(rep_mix)
+    steps_per = rep_mix[0].micro_steps
+    cost32, cost64 = matvec_cost(ranks, opr, dims, 4), matvec_cost(ranks, opr, dims, 8)
+    # sweep visits the optimised positions (rank < full) evenly; use their mean per-matvec cost
+    opt = [k for k in range(1, len(dims) - 1)]
+    f_avg = sum(cost32[k][0] for k in opt) / len(opt)
+    b32 = sum(cost32[k][1] for k in opt) / len(opt)
+    b64 = sum(cost64[k][1] for k in opt) / len(opt)
+    # per solve: FP32 matvecs = CG iterations; FP64 matvecs = one per refinement pass + 1 per step
+    cg_launches, cg_ms = prof_mix.get("cg_mixed", (0, 0.0))
+    per_launch_ms = cg_ms / max(cg_launches, 1)
+    mv32 = iters / max(steps_per, 1)
+    mv64 = (refs + steps_per) / max(steps_per, 1)
+    alg_bytes = mv32 * b32 + mv64 * b64
+    alg_flops = (mv32 + mv64) * f_avg
+    peaks = json.load(open(os.path.join(ROOT, "MEASURED_PEAKS.json"))) if os.path.exists(
+        os.path.join(ROOT, "MEASURED_PEAKS.json")) else {"hbm_gbs": 6800.0}
+    achieved = alg_bytes / (per_launch_ms / 1e3) / 1e9 if per_launch_ms > 0 else 0.0
+    traffic = read_profile_traffic("cg_mixed_als_d8_r32")
+    top = max(prof_mix.items(), key=lambda kv: kv[1][1])[0] if prof_mix else None
+
+    value = statistics.mean(t_mix)
+    vmax = value
+    if world > 1:
+        t = torch.tensor([value], device="cuda")
+        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+        vmax = float(t.item())
+    if rank != 0:
+        return None
+    line = {
+        "metric": METRIC, "value": vmax, "unit": "s", "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
+        "ms_per_step": 1e3 * vmax, "higher_is_better": False, "scaling": "weak", "vs_baseline": None,
+        "dtype": "f64+f32 (mixed: FP32 CG, FP64 refinement and residual)", "data": "synthetic, seeded 0xBAADF00D",
+        "config": dict(WORKLOAD, precision="mixed", parallelism="replicas" if world > 1 else "single GPU",
+                       l2="flushed (256 MB write) between timed steps"),
+        "fp64": {"ms_per_step": 1e3 * statistics.mean(t_64), "half_sweeps": rep_64[0].half_sweeps,
+                 "residual": res_64, "cg_iterations": rep_64[0].local_iterations, "gpu_launches": launches_64 // args.steps,
+                 "cg_kernel_ms": prof_64.get("cg_fp64", (0, 0.0))[1] / prof_steps},
+        "mixed": {"ms_per_step": 1e3 * value, "half_sweeps": rep_mix[0].half_sweeps, "residual": res_mix,
+                  "cg_iterations": rep_mix[0].local_iterations, "refinements": rep_mix[0].refinements},
+        "mixed_speedup_vs_fp64": statistics.mean(t_64) / value,
+        "e2e": {"value": statistics.mean(e2e_times), "unit": "s", "h2d_bytes_per_step": int(h2d),
+                "d2h_bytes_per_step": int(d2h), "residual": resid},
+        "gpu_launches": launches_mix // args.steps,
+        "roofline": {"kernel": "k_cg_mixed (persistent CG)", "bound": "hbm", "achieved": achieved,
+                     "peak": peaks.get("hbm_gbs", 6800.0), "unit": "GB/s",
+                     "frac": achieved / peaks.get("hbm_gbs", 6800.0), "traffic": traffic,
+                     "peak_source": "of measured" if "hbm_gbs" in peaks else "of fallback",
+                     "algorithmic_bytes_per_launch": alg_bytes, "algorithmic_flops_per_launch": alg_flops,
+                     "avg_launch_ms": per_launch_ms, "launches": cg_launches,
+                     "tflops_achieved": alg_flops / (per_launch_ms / 1e3) / 1e12 if per_launch_ms > 0 else 0.0,
+                     "top_kernel_class_by_time": top,
+                     "kernel_ms_per_step": {k: v[1] / prof_steps for k, v in prof_mix.items()}},
+        "clocks": clk,
+    }
+    if not args.no_cpu_baseline:
+        line["cpu_baseline"] = cpu_baseline(A, b, x0, samples=1)
+    return line
+
+
+def cpu_baseline(A, b, x0, samples=1):
+    """The CPU restatement of the reference's ALS (dense LAPACK local solves) on this
+    host, on the same inputs, timed for `samples` full solves."""
+    from oracle import xtt_oracle as o
+    Ah = o.TTOp(A.get_cores())
+    bh = o.TT(b.get_cores(), True, 0)
+    ts = []
+    for _ in range(samples):
+        x = o.TT(x0.get_cores(), True, 0)
+        t0 = time.perf_counter()
+        o.als_spd(Ah, x, bh, 1, WORKLOAD["max_half_sweeps"], 0.0, residual_target=WORKLOAD["target"])
+        ts.append(time.perf_counter() - t0)
+    return {"value": statistics.mean(ts), "unit": "s", "cores": os.cpu_count(), "kind": "port",
+            "sample": f"{samples} full solve(s) of the same workload (numpy/LAPACK dense local solves, all BLAS threads)"}
+
+
+def run_reference(args):
+    rank, _, world = dist_env()
+    if rank != 0:
+        return None
+    from oracle import xtt_oracle as o
+    d, n = WORKLOAD["d"], WORKLOAD["n"]
+    rs = o.RandomEngine(SEED)
+    Ah = o.laplace_operator(d, n)
+    bh = o.tt_random([n] * d, WORKLOAD["rhs_rank"], rs)
+    x0 = o.tt_random([n] * d, WORKLOAD["x_rank"], rs)
+    x0 = o.tt_scale(x0, 1.0 / o.frob_norm(x0))
+    ts = []
+    for i in range(args.warmup + args.steps):
+        x = x0.copy()
+        t0 = time.perf_counter()
+        o.als_spd(Ah, x, bh, 1, WORKLOAD["max_half_sweeps"], 0.0, residual_target=WORKLOAD["target"])
+        if i >= args.warmup:
+            ts.append(time.perf_counter() - t0)
+    v = statistics.mean(ts)
+    return {"metric": METRIC, "value": v, "unit": "s", "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
+            "ms_per_step": 1e3 * v, "higher_is_better": False, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+            "data": "synthetic, seeded 0xBAADF00D", "config": WORKLOAD, "impl": "reference",
+            "cpu_baseline": {"value": v, "unit": "s", "cores": os.cpu_count(), "kind": "port",
+                             "sample": "each step one full solve (dense LAPACK local solves, all BLAS threads)"},
+            "e2e": {"value": v, "unit": "s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+
+
+def main():
+    args = parse()
+    line = run_reference(args) if args.impl == "reference" else run_gpu(args)
+    if line is not None:
+        print(json.dumps(line))
+
+
+if __name__ == "__main__":
+    main()

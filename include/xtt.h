@@ -58,6 +58,13 @@ int xtt_context_set_stream(xtt_context* ctx, void* stream);
 int xtt_context_synchronize(xtt_context* ctx);
 /* Number of kernels this context has launched so far (a counter, for measurements). */
 int xtt_context_kernel_launches(xtt_context* ctx, int64_t* count);
+/* Per-kernel-class timing with CUDA events on the context's stream (the analogue
+ * of xerus's XERUS_PA_START/END accumulators, include/xerus/misc/performanceAnalysis.h:30-39).
+ * enable = 1 starts (and clears) it, 0 stops it. Classes: "cg_fp64", "cg_mixed",
+ * "gemm", "qr", "svd", "adf_res_grad", "adf_slicenorm", "adf_stack". */
+int xtt_context_profile(xtt_context* ctx, int enable);
+/* Launch count and total milliseconds of one class since profiling started (0 if none). */
+int xtt_context_profile_get(xtt_context* ctx, const char* name, int64_t* launches, double* milliseconds);
 
 /* ---------------------------------------------------------------- tensors */
 /* TTNetwork(dims) + set_component: a device TT with the given ranks (order+1

@@ -356,9 +356,12 @@ def rq(a: np.ndarray):
     return r[:, m - n:], q[m - n:, :] if q.shape[0] > n else q
 
 
-def svd_trunc(x: np.ndarray, max_rank: int, eps: float):
+def svd_trunc(x: np.ndarray, max_rank: int, eps: float, canonical_signs: bool = False):
     """calculate_svd (src/xerus/tensor.cpp:1424-1489): dgesdd, then the
-    rank = min(rank, maxRank) cap and the first j >= 1 with S[j] <= eps*S[0]."""
+    rank = min(rank, maxRank) cap and the first j >= 1 with S[j] <= eps*S[0].
+    canonical_signs: flip each singular pair so that the largest-magnitude entry
+    (first on ties) of the left vector is positive (the device's sign gauge)
+    instead of keeping LAPACK's."""
     u, s, vt = np.linalg.svd(x, full_matrices=False)
     rank = len(s)
     if max_rank:
@@ -367,7 +370,12 @@ def svd_trunc(x: np.ndarray, max_rank: int, eps: float):
         if s[j] <= eps * s[0]:
             rank = j
             break
-    return u[:, :rank], s[:rank], vt[:rank, :]
+    u, s, vt = u[:, :rank], s[:rank], vt[:rank, :]
+    if canonical_signs:
+        idx = np.argmax(np.abs(u), axis=0)
+        f = np.where(u[idx, np.arange(rank)] < 0, -1.0, 1.0)
+        u, vt = u * f[None, :], vt * f[:, None]
+    return u, s, vt
 
 
 # --------------------------------------------------------------------------- core movement
@@ -608,12 +616,18 @@ class ALSResult:
 
 def als_spd(A: TTOp, x: TT, b: TT, sites: int = 1, num_half_sweeps: int = 0, conv_eps: float = 1e-6,
             solver: str = "lapack", preserve_core_position: bool = True, track_residual: bool = False,
-            residual_target: float | None = None) -> ALSResult:
+            residual_target: float | None = None, canonical_signs: bool = False,
+            exact_environment: bool = False) -> ALSResult:
     """ALSVariant::solve for an SPD operator (src/xerus/algorithms/als.cpp:483-553).
 
     ``x`` is updated in place. ``solver`` is "lapack" (lapack_solver, als.cpp:43-71)
     or "asd" (ASD_solver, als.cpp:73-92). With ``track_residual`` the accurate
     relative residual is recorded where the reference records perfData.
+    Two sites: the decreasing half-sweep contracts core ``cur`` into the right
+    environment (als.cpp:371) as the reference does, which makes later half-
+    sweeps depend on the sign gauge of the split's singular vectors;
+    ``canonical_signs`` selects the device's gauge instead of LAPACK's, and
+    ``exact_environment`` contracts core ``cur + 1`` (gauge-invariant).
     ``residual_target`` stops at the end of the first half-sweep whose residual
     is at or below it (a time-to-residual measurement, not a reference feature)."""
     d = x.d
@@ -704,7 +718,7 @@ def als_spd(A: TTOp, x: TT, b: TT, sites: int = 1, num_half_sweeps: int = 0, con
                 x.cores[cur] = xv
             else:
                 a_, j1, j2, b_ = xv.shape
-                U, S, Vt = svd_trunc(xv.reshape(a_ * j1, j2 * b_), target_rank[cur], EPSILON)
+                U, S, Vt = svd_trunc(xv.reshape(a_ * j1, j2 * b_), target_rank[cur], EPSILON, canonical_signs)
                 s = len(S)
                 if inc:
                     x.cores[cur] = U.reshape(a_, j1, s)
@@ -746,8 +760,9 @@ def als_spd(A: TTOp, x: TT, b: TT, sites: int = 1, num_half_sweeps: int = 0, con
                 move_core(x, cur - 1, keep_rank=True)
             Lop.pop()
             Lb.pop()
-            Rop.append(_push_right_op(Rop[-1], x.cores[cur], A.cores[cur]))
-            Rb.append(_push_right_rhs(Rb[-1], b.cores[cur], x.cores[cur]))
+            kc = cur + 1 if (sites == 2 and exact_environment) else cur
+            Rop.append(_push_right_op(Rop[-1], x.cores[kc], A.cores[kc]))
+            Rb.append(_push_right_rhs(Rb[-1], b.cores[kc], x.cores[kc]))
             cur -= 1
 
 

@@ -35,12 +35,19 @@ def host_tt(t):
 # ------------------------------------------------------------------ random state (host side of the library)
 
 def test_random_streams_match_reference(ctx, golden):
+    """The engine and integer draws are bit-exact; the polar method's std::log
+    comes from the platform's libm and compiler (FMA contraction), which may round
+    the last bits differently on aarch64 than on the x86-64 host that wrote the
+    fixtures: allow 16 ulp."""
     z = golden("rng")
     xg.seed(0xBAADF00D)
-    import ctypes
     out = np.zeros(257)
     xg._lib.load().xtt_random_normal(0.0, 1.0, 257, out.ctypes.data_as(xg._lib.c_double_p))
-    assert np.array_equal(out, z["rng_normal"])
+    np.testing.assert_array_max_ulp(out, z["rng_normal"], maxulp=16)
+    xg.seed(0xBAADF00D)
+    m = xg.SinglePointMeasurementSet.random(64, [2, 3, 4, 5, 7, 8, 10, 1000])
+    rs = o.RandomEngine()
+    assert np.array_equal(m.positions, o.random_positions(64, [2, 3, 4, 5, 7, 8, 10, 1000], rs))
 
 
 def test_tt_random_and_positions(ctx, golden):
@@ -157,8 +164,14 @@ def test_als_spd_matches_reference(ctx, golden, tag, x0, b, hs, variant):
     assert len(mine) == len(pr)
     keep = pr > 1e-6
     assert rel_err(mine[keep], pr[keep]) < 1e-9
+    # the FP64 residual of this iterate, against the oracle on the same cores; and
+    # against the reference's (dense) residual of its own iterate, which differs
+    # from ours by the CG-vs-Cholesky rounding (~1e-13 in the cores)
+    r_dev = xg.residual(A, x, bb)
+    r_ora = o.residual(op_of(z, "A"), host_tt(x), tt_of(z, b))
+    assert abs(r_dev - r_ora) <= 1e-9 * r_ora + 1e-12
     dense = z[tag + "_dense_residual"][0]
-    assert abs(xg.residual(A, x, bb) - dense) <= 1e-9 * max(dense, 1e-3)
+    assert abs(r_dev - dense) <= 1e-9 * dense + 1e-11
 
 
 def test_als_ragged_dims(ctx, golden):
@@ -185,26 +198,59 @@ def test_als_mixed_precision_matches_fp64(ctx, golden):
 
 
 def test_dmrg_spd(ctx, golden):
+    """The reference's decreasing half-sweep contracts core k (not k+1) into the
+    right environment (als.cpp:371), so after the first half-sweep its result
+    depends on the sign gauge of LAPACK's singular vectors. Pinned here: the
+    first half-sweep against the reference; every half-sweep against the oracle
+    in the device's sign gauge; the corrected environment (gauge-invariant)
+    against the oracle."""
     z = golden("dmrg")
-    A, b, x = dev_op(ctx, op_of(z, "A")), dev_tt(ctx, tt_of(z, "b")), dev_tt(ctx, tt_of(z, "x0"))
+    Ah, bh, xh = op_of(z, "A"), tt_of(z, "b"), tt_of(z, "x0")
+    A, b, x = dev_op(ctx, Ah), dev_tt(ctx, bh), dev_tt(ctx, xh)
     v = xg.DMRG_SPD.copy()
     v.convergenceEpsilon = 0.0
     perf = xg.PerformanceData()
     energy = v(A, x, b, 4, perf)
-    assert abs(energy / z["d8_r4_hs4_energy"][0] - 1) < REL_TOL
     assert [1] + x.ranks() + [1] == list(z["d8_r4_hs4_ranks"])
-    assert rel_err(x.entries(z["d8_r4_hs4_x_probe_pos"]), z["d8_r4_hs4_x_probe_val"]) < 1e-9
-    assert rel_err(perf.residuals, z["d8_r4_hs4_perf_residual"]) < 1e-8
+    assert rel_err(perf.residuals[:6], z["d8_r4_hs4_perf_residual"][:6]) < 1e-10
+    ref = xh.copy()
+    r = o.als_spd(Ah, ref, bh, 2, 4, 0.0, track_residual=True, canonical_signs=True)
+    assert abs(energy / r.energy - 1) < 1e-9
+    assert rel_err(perf.residuals, r.residuals) < 1e-8
+    assert rel_err(x.entries(z["d8_r4_hs4_x_probe_pos"]), o.tt_entries(ref, z["d8_r4_hs4_x_probe_pos"])) < 1e-8
+    v.exact_environment = True
+    x = dev_tt(ctx, xh)
+    energy = v(A, x, b, 4)
+    ref = xh.copy()
+    r = o.als_spd(Ah, ref, bh, 2, 4, 0.0, exact_environment=True)
+    assert abs(energy / r.energy - 1) < 1e-10
+    assert rel_err(x.entries(z["d8_r4_hs4_x_probe_pos"]), o.tt_entries(ref, z["d8_r4_hs4_x_probe_pos"])) < 1e-9
 
 
 def test_dmrg_spd_potential_d20(ctx, golden):
+    """Laplacian + potential, rank-3 operator, d=20, n=8, rank 8. The first
+    half-sweep against the oracle (pinned to the reference); the corrected
+    environment for two half-sweeps. The reference-environment second half-sweep
+    is not pinned: its local systems reach condition numbers ~1e7 and a 1e-15
+    change of one core moves its energy by ~1e-9, so it is not reproducible
+    across solvers or BLAS builds to 1e-10."""
     z = golden("dmrg")
-    A, b, x = dev_op(ctx, op_of(z, "A_pot")), dev_tt(ctx, tt_of(z, "b_pot")), dev_tt(ctx, tt_of(z, "x0_pot"))
+    Ah, bh, xh = op_of(z, "A_pot"), tt_of(z, "b_pot"), tt_of(z, "x0_pot")
+    A, b, x = dev_op(ctx, Ah), dev_tt(ctx, bh), dev_tt(ctx, xh)
     v = xg.DMRG_SPD.copy()
     v.convergenceEpsilon = 0.0
+    energy = v(A, x, b, 1)
+    ref = xh.copy()
+    r = o.als_spd(Ah, ref, bh, 2, 1, 0.0)
+    assert abs(energy / r.energy - 1) < 1e-10
+    assert rel_err(x.entries(z["pot_r8_hs2_x_probe_pos"]), o.tt_entries(ref, z["pot_r8_hs2_x_probe_pos"])) < 1e-9
+    v.exact_environment = True
+    x = dev_tt(ctx, xh)
     energy = v(A, x, b, 2)
-    assert abs(energy / z["pot_r8_hs2_energy"][0] - 1) < 1e-10
-    assert rel_err(x.entries(z["pot_r8_hs2_x_probe_pos"]), z["pot_r8_hs2_x_probe_val"]) < 1e-9
+    ref = xh.copy()
+    r = o.als_spd(Ah, ref, bh, 2, 2, 0.0, exact_environment=True)
+    assert abs(energy / r.energy - 1) < 1e-10
+    assert rel_err(x.entries(z["pot_r8_hs2_x_probe_pos"]), o.tt_entries(ref, z["pot_r8_hs2_x_probe_pos"])) < 1e-9
 
 
 # ------------------------------------------------------------------ ADF and adjoints

@@ -9,6 +9,7 @@ frob_norm, TTTensor.random, move_core, round, ALS_SPD / DMRG_SPD / ASD_SPD
 There is no CPU fallback: without the built library or a GPU, calls raise.
 """
 import ctypes
+import sys
 
 import numpy as np
 
@@ -59,13 +60,23 @@ class Context:
         L.check(self.lib.xtt_context_kernel_launches(self.handle, ctypes.byref(v)))
         return v.value
 
+    def profile(self, enable=True):
+        """Starts (clears) or stops per-kernel-class CUDA-event timing."""
+        L.check(self.lib.xtt_context_profile(self.handle, int(bool(enable))))
+
+    def profile_get(self, name):
+        """(launches, milliseconds) of a kernel class since profiling started."""
+        n, ms = ctypes.c_int64(), ctypes.c_double()
+        L.check(self.lib.xtt_context_profile_get(self.handle, name.encode(), ctypes.byref(n), ctypes.byref(ms)))
+        return n.value, ms.value
+
     def set_stream(self, stream_ptr):
         L.check(self.lib.xtt_context_set_stream(self.handle, ctypes.c_void_p(stream_ptr)))
 
     def __del__(self):
-        if getattr(self, "handle", None):
+        if getattr(self, "handle", None) and not sys.is_finalizing():
             self.lib.xtt_context_destroy(self.handle)
-            self.handle = None
+        self.handle = None
 
 
 def seed(value=0xBAADF00D):
@@ -92,9 +103,9 @@ class _TT:
         self.handle = h
 
     def __del__(self):
-        if getattr(self, "handle", None):
+        if getattr(self, "handle", None) and not sys.is_finalizing():
             self.lib.xtt_tensor_destroy(self.handle)
-            self.handle = None
+        self.handle = None
 
     # -- shape
     def degree(self):
@@ -457,3 +468,39 @@ def als_energy_gradient(A, x, b):
 
 
 ADF = ADFVariant(0, 1e-8, 0.999)
+
+
+def laplacian_cores(d, n, potentials=None, rank3=False, shift=0.0):
+    """Cores of sum_i I x..x (L + V_i) x..x I with L = tridiag(-1, 2, -1) (n x n):
+    rank 2 ([[L+V_0, I]], [[I, 0], [L+V_k, I]], [[I], [L+V]]) or, with rank3, the
+    potential in its own channel ([[L+V_0, I, I]], [[I,0,0],[L,I,0],[V_k,0,I]], [[I],[L],[V]])."""
+    L = 2 * np.eye(n) - np.eye(n, k=1) - np.eye(n, k=-1)
+    I = np.eye(n)
+    R = 3 if rank3 else 2
+    cores = []
+    for k in range(d):
+        V = np.diag(potentials[k]) if potentials is not None else np.zeros((n, n))
+        lk = L + (0 if rank3 else V) + shift * I / d
+        rl, rr = (1 if k == 0 else R), (1 if k == d - 1 else R)
+        c = np.zeros((rl, n, n, rr))
+        if d == 1:
+            c[0, :, :, 0] = L + V + shift * I
+        elif k == 0:
+            c[0, :, :, 0] = lk + (V if rank3 else 0)
+            c[0, :, :, 1] = I
+            if rank3:
+                c[0, :, :, 2] = I
+        elif k == d - 1:
+            c[0, :, :, 0] = I
+            c[1, :, :, 0] = lk
+            if rank3:
+                c[2, :, :, 0] = V
+        else:
+            c[0, :, :, 0] = I
+            c[1, :, :, 0] = lk
+            c[1, :, :, 1] = I
+            if rank3:
+                c[2, :, :, 0] = V
+                c[2, :, :, 2] = I
+        cores.append(c)
+    return cores

@@ -340,6 +340,7 @@ struct AdfData {
 		const AdfLevel L = level(k, X);
 		const int len = L.r0 * L.n * L.r1;
 		if (fast) {
+			ProfScope ps(c, "adf_res_grad");
 			k_adf_res_grad<<<blocks(), kAdfThreads, 0, c.stream>>>(L, y, res, mode, gpart, rrpart, chunk);
 			k_sum_parts<<<std::max(1, (len + 127) / 128), 128, 0, c.stream>>>(gpart, warps, len, Gout, gscale);
 			k_sum_parts<<<1, 32, 0, c.stream>>>(rrpart, warps, 1, rr, 1.0);
@@ -357,6 +358,7 @@ struct AdfData {
 	void slicenorm(int k) {
 		const AdfLevel L = level(k, x.core[k]);
 		if (fast) {
+			ProfScope ps(c, "adf_slicenorm");
 			k_adf_slicenorm<<<blocks(), kAdfThreads, 0, c.stream>>>(L, G, npart, chunk);
 			k_sum_parts<<<1, 32, 0, c.stream>>>(npart, warps, L.n, nrm, 1.0);
 			c.count_launch(2);
@@ -369,6 +371,7 @@ struct AdfData {
 	void forward(int k) {
 		const int r0 = int(x.ranks[k]), n = int(x.dims[k]), r1 = int(x.ranks[k + 1]);
 		const unsigned bl = unsigned(std::max<long long>(1, std::min<long long>((N + 255) / 256, (long long)c.num_sms * 8)));
+		ProfScope ps(c, "adf_stack");
 		k_adf_forward<<<bl, 256, size_t(r0) * n * r1 * sizeof(double), c.stream>>>(pos + size_t(k) * N,
 		                                                                           k > 0 ? F[k - 1] : nullptr,
 		                                                                           x.core[k], F[k], r0, n, r1, N);
@@ -378,6 +381,7 @@ struct AdfData {
 	void backward(int k) {
 		const int r0 = int(x.ranks[k]), n = int(x.dims[k]), r1 = int(x.ranks[k + 1]);
 		const unsigned bl = unsigned(std::max<long long>(1, std::min<long long>((N + 255) / 256, (long long)c.num_sms * 8)));
+		ProfScope ps(c, "adf_stack");
 		k_adf_backward<<<bl, 256, size_t(r0) * n * r1 * sizeof(double), c.stream>>>(pos + size_t(k) * N,
 		                                                                            k + 1 < d ? B[k + 1] : nullptr,
 		                                                                            x.core[k], B[k], r0, n, r1, N);

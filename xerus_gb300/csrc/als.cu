@@ -357,6 +357,7 @@ CgResult local_solve(Context& c, const LocalShape& s, const double* L, const dou
 		a.tol = tol;
 		a.zero_guess = 0;
 		void* args[] = {&a, &oi, &od};
+		ProfScope ps(c, "cg_fp64");
 		XTT_CUDA(cudaLaunchCooperativeKernel((void*)k_cg<double>, dim3(G), dim3(kGemmThreads), args, 0, c.stream));
 		c.count_launch();
 	} else {
@@ -401,6 +402,7 @@ CgResult local_solve(Context& c, const LocalShape& s, const double* L, const dou
 		m.tol = tol;
 		m.max_refine = 12;
 		void* args[] = {&m, &oi, &od};
+		ProfScope ps(c, "cg_mixed");
 		XTT_CUDA(cudaLaunchCooperativeKernel((void*)k_cg_mixed, dim3(G), dim3(kGemmThreads), args, 0, c.stream));
 		c.count_launch();
 	}
@@ -826,7 +828,10 @@ AlsReport als(const Tensor& A, Tensor& x, const Tensor& b, const AlsOptions& o) 
 			a.X = s.v; a.ldx = nn; a.m = m; a.n = nn; a.max_rank = mr; a.eps = eps;
 			a.work = wk ? c.scratch<double>(S_SVD_WORK, wk) : nullptr;
 			a.U = U; a.S = Sv; a.Vt = Vt; a.rank_out = c.d_ints + 1; a.status = c.d_status;
-			launch_svd(a, c.stream);
+			{
+				ProfScope ps(c, "svd");
+				launch_svd(a, c.stream);
+			}
 			c.count_launch();
 			const int rk = c.read_int(1);
 			XTT_REQUIRE(rk <= rmax[cur + 1], "DMRG split rank exceeds the stack capacity");

@@ -66,10 +66,18 @@ int xtt_context_create(int device, xtt_context** out) {
 	});
 }
 
+// A context is freed only after its last tensor: tensor destructors use its
+// stream, and callers (garbage-collected bindings in particular) may destroy
+// them in any order.
+static void release_context(xtt::Context* c) {
+	if (c->closing && c->tensors == 0) delete c;
+}
+
 int xtt_context_destroy(xtt_context* ctx) {
 	return guard([&] {
 		if (!ctx) return;
-		delete ctx->c;
+		ctx->c->closing = true;
+		release_context(ctx->c);
 		delete ctx;
 	});
 }
@@ -96,6 +104,31 @@ int xtt_context_kernel_launches(xtt_context* ctx, int64_t* count) {
 	});
 }
 
+int xtt_context_profile(xtt_context* ctx, int enable) {
+	return guard([&] {
+		ARG(ctx, "ctx is NULL");
+		xtt::Context& c = *ctx->c;
+		c.resolve_profile();
+		if (enable) c.profile.clear();
+		c.profiling = enable != 0;
+	});
+}
+
+int xtt_context_profile_get(xtt_context* ctx, const char* name, int64_t* launches, double* milliseconds) {
+	return guard([&] {
+		ARG(ctx && name && launches && milliseconds, "NULL argument");
+		xtt::Context& c = *ctx->c;
+		c.resolve_profile();
+		*launches = 0;
+		*milliseconds = 0;
+		for (auto& e : c.profile)
+			if (e.first == name) {
+				*launches = e.second.launches;
+				*milliseconds = e.second.ms;
+			}
+	});
+}
+
 int xtt_tensor_create(xtt_context* ctx, int is_operator, int64_t order, const int64_t* dims, const int64_t* ranks,
                       xtt_tensor** out) {
 	return guard([&] {
@@ -103,6 +136,7 @@ int xtt_tensor_create(xtt_context* ctx, int is_operator, int64_t order, const in
 		ARG(order > 0 && order < (1 << 20), "order must be positive");
 		*out = nullptr;
 		auto* t = new xtt::Tensor(ctx->c, is_operator != 0, int(order), dims, ranks);
+		ctx->c->tensors++;
 		*out = new xtt_tensor{t};
 	});
 }
@@ -110,8 +144,11 @@ int xtt_tensor_create(xtt_context* ctx, int is_operator, int64_t order, const in
 int xtt_tensor_destroy(xtt_tensor* t) {
 	return guard([&] {
 		if (!t) return;
+		xtt::Context* c = t->t->ctx;
 		delete t->t;
 		delete t;
+		c->tensors--;
+		release_context(c);
 	});
 }
 
@@ -120,8 +157,9 @@ int xtt_tensor_copy(const xtt_tensor* src, xtt_tensor** out) {
 		ARG(src && out, "NULL argument");
 		const xtt::Tensor& s = *src->t;
 		auto* t = new xtt::Tensor(s.ctx, s.op, s.d, s.dims.data(), s.ranks.data());
-		t->copy_from(s);
+		s.ctx->tensors++;
 		*out = new xtt_tensor{t};
+		t->copy_from(s);
 	});
 }
 
@@ -263,6 +301,7 @@ int xtt_tensor_random(xtt_context* ctx, int64_t order, const int64_t* dims, cons
 		std::vector<int64_t> r(order + 1, 1);
 		for (int64_t k = 1; k < order; ++k) r[k] = red[k - 1];
 		auto* t = new xtt::Tensor(ctx->c, false, int(order), dv.data(), r.data());
+		ctx->c->tensors++;
 		xtt_tensor* h = new xtt_tensor{t};
 		try {
 			auto& dist = dist_for(mean, stddev);
@@ -281,6 +320,7 @@ int xtt_tensor_random(xtt_context* ctx, int64_t order, const int64_t* dims, cons
 		} catch (...) {
 			delete t;
 			delete h;
+			ctx->c->tensors--;
 			throw;
 		}
 		*out = h;

@@ -9,6 +9,8 @@
 #pragma once
 
 #include <cstdint>
+#include <string>
+#include <utility>
 #include <vector>
 
 #include "common.cuh"
@@ -29,6 +31,8 @@ struct Context {
 	double* d_dbl = nullptr;       // small device results (norms, dots), 64 doubles
 	double* h_dbl = nullptr;       // pinned mirror
 	long long launches = 0;
+	int tensors = 0;        // live tensors created on this context
+	bool closing = false;   // destroy requested; freed when the last tensor goes
 	struct Slot {
 		void* p = nullptr;
 		size_t bytes = 0;
@@ -47,6 +51,30 @@ struct Context {
 	void check_status();              // reads d_status (after a sync) and throws on failure
 	int read_int(int idx);            // sync + d_ints[idx]
 	void count_launch(int n = 1) { launches += n; }
+
+	// Optional per-kernel-class timing: CUDA events recorded on the context's
+	// stream around each launch of a class, resolved when read.
+	bool profiling = false;
+	struct Timed {
+		std::string name;
+		cudaEvent_t start, stop;
+	};
+	std::vector<Timed> pending;
+	struct ProfileEntry {
+		long long launches = 0;
+		double ms = 0;
+	};
+	std::vector<std::pair<std::string, ProfileEntry>> profile;
+	void resolve_profile();
+};
+
+// RAII scope recording a launch class's start and stop events when profiling.
+struct ProfScope {
+	Context& c;
+	const char* name;
+	cudaEvent_t a = nullptr, b = nullptr;
+	ProfScope(Context& cc, const char* n);
+	~ProfScope();
 };
 
 // Scratch slot ids (one per purpose, so nested operations never share a buffer).

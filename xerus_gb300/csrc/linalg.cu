@@ -347,6 +347,27 @@ __global__ void __launch_bounds__(kSvdThreads) k_svd(SvdArgs a, int use_smem) {
 	}
 	__syncthreads();
 	const int rank = s_rank;
+	// Canonical sign gauge: the entry of largest magnitude (first on ties) of
+	// each kept left singular vector is made positive, the right vector follows.
+	__shared__ double s_sign[1024];
+	for (int k = warp; k < rank && k < 1024; k += nwarps) {
+		const int c = order[k];
+		double best = -1.0, val = 0.0;
+		int bi = 1 << 30;
+		for (int i = lane; i < a.m; i += 32) {
+			const double u = tall ? B[(long long)c * p + i] : V[(long long)c * q + i];
+			if (fabs(u) > best) { best = fabs(u); val = u; bi = i; }
+		}
+#pragma unroll
+		for (int o = 16; o > 0; o >>= 1) {
+			const double ob = __shfl_xor_sync(0xffffffffu, best, o);
+			const double ov = __shfl_xor_sync(0xffffffffu, val, o);
+			const int oi = __shfl_xor_sync(0xffffffffu, bi, o);
+			if (ob > best || (ob == best && oi < bi)) { best = ob; val = ov; bi = oi; }
+		}
+		if (lane == 0) s_sign[k] = val < 0.0 ? -1.0 : 1.0;
+	}
+	__syncthreads();
 	for (int k = tid; k < rank; k += blockDim.x) a.S[k] = sig[order[k]];
 	// tall: X = Bn Sigma V^T (Bn: normalised B columns); wide: X^T = Bn Sigma V^T
 	for (long long e = tid; e < (long long)a.m * rank; e += blockDim.x) {
@@ -354,14 +375,14 @@ __global__ void __launch_bounds__(kSvdThreads) k_svd(SvdArgs a, int use_smem) {
 		double v;
 		if (tall) v = sig[c] > 0 ? B[(long long)c * p + i] / sig[c] : 0.0;
 		else v = V[(long long)c * q + i];
-		a.U[(long long)i * rank + k] = v;
+		a.U[(long long)i * rank + k] = s_sign[k] * v;
 	}
 	for (long long e = tid; e < (long long)rank * a.n; e += blockDim.x) {
 		const int k = int(e / a.n), j = int(e % a.n), c = order[k];
 		double v;
 		if (tall) v = V[(long long)c * q + j];
 		else v = sig[c] > 0 ? B[(long long)c * p + j] / sig[c] : 0.0;
-		a.Vt[(long long)k * a.n + j] = v;
+		a.Vt[(long long)k * a.n + j] = s_sign[k] * v;
 	}
 }
 
@@ -371,6 +392,7 @@ void launch_svd(const SvdArgs& a, cudaStream_t s) {
 	const size_t full = aux + (size_t(p) * q + size_t(q) * q) * sizeof(double);
 	const int use_smem = full <= kDynSmemMax ? 1 : 0;
 	XTT_REQUIRE(use_smem || a.work, "SVD workspace missing");
+	XTT_REQUIRE(std::min(a.m, a.n) <= 1024 || (a.max_rank > 0 && a.max_rank <= 1024), "SVD: more than 1024 kept singular values");
 	static bool attr = false;
 	if (!attr) {
 		XTT_CUDA(cudaFuncSetAttribute(k_svd, cudaFuncAttributeMaxDynamicSharedMemorySize, int(kDynSmemMax)));

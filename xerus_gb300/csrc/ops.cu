@@ -78,6 +78,37 @@ void Context::sync() {
 	check_status();
 }
 
+ProfScope::ProfScope(Context& cc, const char* n) : c(cc), name(n) {
+	if (!c.profiling) return;
+	XTT_CUDA(cudaEventCreate(&a));
+	XTT_CUDA(cudaEventCreate(&b));
+	XTT_CUDA(cudaEventRecord(a, c.stream));
+}
+
+ProfScope::~ProfScope() {
+	if (!a) return;
+	cudaEventRecord(b, c.stream);
+	c.pending.push_back(Context::Timed{name, a, b});
+}
+
+void Context::resolve_profile() {
+	for (auto& t : pending) {
+		float ms = 0;
+		XTT_CUDA(cudaEventSynchronize(t.stop));
+		XTT_CUDA(cudaEventElapsedTime(&ms, t.start, t.stop));
+		cudaEventDestroy(t.start);
+		cudaEventDestroy(t.stop);
+		auto it = std::find_if(profile.begin(), profile.end(), [&](const auto& e) { return e.first == t.name; });
+		if (it == profile.end()) {
+			profile.emplace_back(t.name, ProfileEntry{});
+			it = profile.end() - 1;
+		}
+		it->second.launches += 1;
+		it->second.ms += ms;
+	}
+	pending.clear();
+}
+
 int Context::read_int(int idx) {
 	XTT_CUDA(cudaMemcpyAsync(h_ints + idx, d_ints + idx, sizeof(int), cudaMemcpyDeviceToHost, stream));
 	sync();
@@ -173,6 +204,7 @@ void gemm(Context& c, const Gemm<double>& g) {
 	check_gemm(g);
 	const long long t = g.tiles();
 	XTT_REQUIRE(t < (1ll << 31), "GEMM too large");
+	ProfScope ps(c, "gemm");
 	k_gemm<double><<<unsigned(t), kGemmThreads, 0, c.stream>>>(g);
 	XTT_CUDA(cudaGetLastError());
 	c.count_launch();
@@ -335,7 +367,10 @@ void transfer_core(Tensor& x, int from, int to, bool rr) {
 		a.A = x.core[from]; a.lda = n; a.m = m; a.n = n; a.transpose = 0; a.pivot = rr ? 1 : 0;
 		a.work = wk ? c.scratch<double>(S_QR_WORK, wk) : nullptr;
 		a.Q = Q; a.C = C; a.rank_out = c.d_ints;
-		launch_qr(a, c.stream);
+		{
+			ProfScope ps(c, "qr");
+			launch_qr(a, c.stream);
+		}
 		c.count_launch();
 		const int rank = rr ? c.read_int(0) : kq;
 		const int64_t nt = x.n(to), r2 = x.ranks[to + 1];
@@ -361,7 +396,10 @@ void transfer_core(Tensor& x, int from, int to, bool rr) {
 		a.A = x.core[from]; a.lda = n; a.m = m; a.n = n; a.transpose = 1; a.pivot = rr ? 1 : 0;
 		a.work = wk ? c.scratch<double>(S_QR_WORK, wk) : nullptr;
 		a.Q = Q; a.C = C; a.rank_out = c.d_ints;
-		launch_qr(a, c.stream);
+		{
+			ProfScope ps(c, "qr");
+			launch_qr(a, c.stream);
+		}
 		c.count_launch();
 		const int rank = rr ? c.read_int(0) : kq;
 		const int64_t rt = x.ranks[to], nt = x.n(to);
@@ -414,7 +452,10 @@ static int svd_into(Context& c, const double* X, int m, int n, int max_rank, dou
 	const size_t wk = svd_work_doubles(m, n);
 	a.work = wk ? c.scratch<double>(S_SVD_WORK, wk) : nullptr;
 	a.U = U; a.S = S; a.Vt = Vt; a.rank_out = c.d_ints + 1; a.status = c.d_status;
-	launch_svd(a, c.stream);
+	{
+		ProfScope ps(c, "svd");
+		launch_svd(a, c.stream);
+	}
 	c.count_launch();
 	return c.read_int(1);
 }
@@ -438,7 +479,10 @@ static void round_edge(Tensor& x, int from, int to, int64_t max_rank, double eps
 		a.A = x.core[from]; a.lda = nFc; a.m = mF; a.n = nFc; a.transpose = 1; a.pivot = 1;
 		a.work = wk ? c.scratch<double>(S_QR_WORK, wk) : nullptr;
 		a.Q = QF; a.C = CA; a.rank_out = c.d_ints + 2;
-		launch_qr(a, c.stream);
+		{
+			ProfScope ps(c, "qr");
+			launch_qr(a, c.stream);
+		}
 		c.count_launch();
 		const int mT = int(rT * nT), nTc = int(r);
 		double* QT = c.scratch<double>(S_ROUND_QB, size_t(mT) * std::min(mT, nTc));
@@ -448,7 +492,10 @@ static void round_edge(Tensor& x, int from, int to, int64_t max_rank, double eps
 		b.A = x.core[to]; b.lda = nTc; b.m = mT; b.n = nTc; b.transpose = 0; b.pivot = 1;
 		b.work = wk ? c.scratch<double>(S_ROUND_X, wk) : nullptr;  // not S_QR_WORK: may run concurrently in the future
 		b.Q = QT; b.C = CB; b.rank_out = c.d_ints + 3;
-		launch_qr(b, c.stream);
+		{
+			ProfScope ps(c, "qr");
+			launch_qr(b, c.stream);
+		}
 		c.count_launch();
 		const int ka = c.read_int(2), kb = c.read_int(3);
 		double* X = c.scratch<double>(S_GEMM_B, size_t(ka) * kb);
