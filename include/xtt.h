@@ -136,6 +136,24 @@ int xtt_residual(const xtt_tensor* A, const xtt_tensor* x, const xtt_tensor* b, 
  * SinglePointMeasurementSet::measure(TensorNetwork) (src/xerus/measurments.cpp:125-153). */
 int xtt_entries(const xtt_tensor* x, const int64_t* positions, int64_t count, double* out);
 
+/* The TT dot product of xtt_dot on caller-owned device memory, for callers
+ * that cannot allocate device memory (for example when a framework's caching
+ * allocator already owns the device memory, or on paths where cudaMalloc /
+ * cudaFree and cudaFree's implicit synchronisation are not acceptable). It
+ * allocates nothing: its intermediates live in a fixed 2.25 MiB __device__
+ * array inside libxtt.so, one per device, kept until the library is unloaded.
+ * No counterpart in the reference.
+ * x_cores / y_cores: the cores concatenated (as xtt_tensor_get_cores lays them
+ * out) in device memory of the current device; x_ranks / y_ranks: order+1 host
+ * entries; result: one double of device memory, written asynchronously on
+ * `stream` (a cudaStream_t, NULL = legacy default stream). Limits: every rank
+ * <= 128 and every mode size <= 16, else XTT_ERR_CAPACITY before any launch.
+ * The first call on a device looks up the array's device address; make it
+ * before any stream capture on that device. All calls share the array:
+ * calls whose kernels may overlap on the GPU race and must be serialised. */
+int xtt_dot_noalloc(int64_t order, const int64_t* dims, const int64_t* x_ranks, const double* x_cores,
+                    const int64_t* y_ranks, const double* y_cores, double* result, void* stream);
+
 /* ------------------------------------------------------------------- ALS */
 typedef struct xtt_als_options {
 	int32_t sites;                   /* ALSVariant::sites: 1 = ALS, 2 = DMRG (als.h:112) */

@@ -86,6 +86,7 @@ _SIGNATURES = {
     "xtt_round": (ctypes.c_int, [VP, c_int64_p, ctypes.c_double, c_double_p, ctypes.c_int64, c_int64_p]),
     "xtt_dot": (ctypes.c_int, [VP, VP, c_double_p]),
     "xtt_frob_norm": (ctypes.c_int, [VP, c_double_p]),
+    "xtt_dot_noalloc": (ctypes.c_int, [ctypes.c_int64, c_int64_p, c_int64_p, VP, c_int64_p, VP, VP, VP]),
     "xtt_residual": (ctypes.c_int, [VP, VP, VP, c_double_p]),
     "xtt_entries": (ctypes.c_int, [VP, c_int64_p, ctypes.c_int64, c_double_p]),
     "xtt_als_default_options": (ctypes.c_int, [ctypes.POINTER(AlsOptions)]),

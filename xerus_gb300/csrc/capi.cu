@@ -43,6 +43,11 @@ std::normal_distribution<double>& dist_for(double mean, double stddev) {
 
 }  // namespace
 
+namespace xtt {
+// Lets entry points outside this file leave a message for xtt_last_error().
+void set_last_error(const std::string& msg) { g_error = msg; }
+}  // namespace xtt
+
 struct xtt_context {
 	xtt::Context* c;
 };
