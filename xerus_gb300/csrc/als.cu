@@ -12,6 +12,8 @@
 #include <cmath>
 #include <cstring>
 
+#include <cooperative_groups.h>
+
 #include "als.cuh"
 
 namespace xtt {
@@ -109,6 +111,64 @@ void local_matvec(Context& c, const LocalShape& s, const double* L, const double
 }
 
 // ------------------------------------------------------------ persistent CG
+//
+// One launch runs a whole local solve. The CG body is written against a
+// "group" of CTAs that provides its rank/size, a barrier and a sum over the
+// group: GridGroup is a cooperative launch over many SMs with a bounded
+// software barrier (large local systems), ClusterGroup is one thread-block
+// cluster of up to 16 CTAs with the hardware cluster barrier and sums through
+// distributed shared memory (local systems up to kClusterMaxN unknowns, where
+// the software grid barrier dominated the iteration time).
+
+constexpr long long kClusterMaxN = 65536;
+constexpr int kCgClusterMax = 16;
+
+struct GridGroup {
+	static constexpr bool kCluster = false;
+	GridBarrier bar;
+	double* partial;  // 2 * gridDim doubles
+	int turn = 0;
+	__device__ int rank() const { return blockIdx.x; }
+	__device__ int size() const { return gridDim.x; }
+	__device__ bool sync() { return grid_sync(bar); }
+	// sum over the group of one value per CTA (thread 0's), identical in every CTA
+	__device__ double total(double mine, bool& ok) {
+		__shared__ double sc[32];
+		double* slot = partial + (turn ^= 1) * gridDim.x;
+		if (threadIdx.x == 0) slot[blockIdx.x] = mine;
+		ok = grid_sync(bar);
+		double t = 0;
+		for (int i = threadIdx.x; i < (int)gridDim.x; i += blockDim.x) t += slot[i];
+		return block_sum(t, sc);
+	}
+	__device__ void record(int code) { record_status(bar.status, code); }
+};
+
+struct ClusterGroup {
+	static constexpr bool kCluster = true;
+	int* status;
+	int turn = 0;
+	__device__ int rank() const { return int(cooperative_groups::this_cluster().block_rank()); }
+	__device__ int size() const { return int(cooperative_groups::this_cluster().num_blocks()); }
+	__device__ bool sync() {
+		cooperative_groups::this_cluster().sync();
+		return true;
+	}
+	// two alternating slots: a slot is rewritten only after the barrier that follows its reads
+	__device__ double total(double mine, bool& ok) {
+		namespace cg = cooperative_groups;
+		__shared__ double slot[2];
+		const int t = (turn ^= 1);
+		if (threadIdx.x == 0) slot[t] = mine;
+		cg::cluster_group cl = cg::this_cluster();
+		cl.sync();
+		double s = 0;
+		for (int p = 0; p < (int)cl.num_blocks(); ++p) s += cl.map_shared_rank(slot, p)[t];
+		ok = true;
+		return s;
+	}
+	__device__ void record(int code) { record_status(status, code); }
+};
 
 template <class T>
 struct CgParams {
@@ -116,8 +176,6 @@ struct CgParams {
 	T *x, *r, *p, *q;
 	const T* b;
 	long long n;
-	double* partial;  // 2 * gridDim
-	GridBarrier bar;
 	int max_iter;
 	double tol;
 	int zero_guess;
@@ -128,9 +186,9 @@ struct CgOut {
 	double rel_residual;
 };
 
-template <class T>
-__device__ bool matvec_dev(const MatvecPlan<T>& plan, const T* in, T* out, const T* dotv, GemmSmem<T>& sm,
-                           const GridBarrier& bar, T& blk_dot) {
+template <class T, class Grp>
+__device__ bool matvec_dev(const MatvecPlan<T>& plan, const T* in, T* out, const T* dotv, GemmSmem<T>& sm, Grp& grp,
+                           T& blk_dot) {
 	for (int s = 0; s < plan.ns; ++s) {
 		Gemm<T> g = plan.g[s];
 		if (s == 0) g.B = in;
@@ -138,35 +196,24 @@ __device__ bool matvec_dev(const MatvecPlan<T>& plan, const T* in, T* out, const
 			g.C = out;
 			g.D = dotv;
 		}
-		const T part = gemm_tiles(g, blockIdx.x, gridDim.x, sm);
+		const T part = gemm_tiles(g, grp.rank(), grp.size(), sm);
 		if (s == plan.ns - 1) blk_dot = part;
-		else if (!grid_sync(bar)) return false;
+		else if (!grp.sync()) return false;
 	}
 	return true;
 }
 
-// Sum over the grid of one value per block (thread 0's `mine`), identical in every block.
-__device__ double grid_total(double mine, double* slot, const GridBarrier& bar, bool& ok) {
-	__shared__ double sc[32];
-	if (threadIdx.x == 0) slot[blockIdx.x] = mine;
-	ok = grid_sync(bar);
-	double t = 0;
-	for (int i = threadIdx.x; i < (int)gridDim.x; i += blockDim.x) t += slot[i];
-	return block_sum(t, sc);
-}
-
-template <class T>
-__device__ CgOut cg_body(const CgParams<T>& a, GemmSmem<T>& sm) {
+template <class T, class Grp>
+__device__ CgOut cg_body(const CgParams<T>& a, GemmSmem<T>& sm, Grp& grp) {
 	__shared__ double sc[32];
 	CgOut out{0, 0, 0.0};
-	const long long gt = blockIdx.x * (long long)blockDim.x + threadIdx.x;
-	const long long gs = (long long)gridDim.x * blockDim.x;
-	const int G = gridDim.x;
+	const long long gt = grp.rank() * (long long)blockDim.x + threadIdx.x;
+	const long long gs = (long long)grp.size() * blockDim.x;
 	bool ok = true;
 	T dummy;
 	if (!a.zero_guess) {
-		if (!matvec_dev(a.plan, a.x, a.q, (const T*)nullptr, sm, a.bar, dummy)) return out;
-		if (!grid_sync(a.bar)) return out;
+		if (!matvec_dev(a.plan, a.x, a.q, (const T*)nullptr, sm, grp, dummy)) return out;
+		if (!grp.sync()) return out;
 		for (long long i = gt; i < a.n; i += gs) {
 			const T ri = a.b[i] - a.q[i];
 			a.r[i] = ri;
@@ -186,15 +233,10 @@ __device__ CgOut cg_body(const CgParams<T>& a, GemmSmem<T>& sm) {
 	}
 	rl = block_sum(rl, sc);
 	bl = block_sum(bl, sc);
-	if (threadIdx.x == 0) a.partial[G + blockIdx.x] = bl;
-	double rr = grid_total(rl, a.partial, a.bar, ok);
+	double rr = grp.total(rl, ok);
 	if (!ok) return out;
-	double bb = 0;
-	{
-		double t = 0;
-		for (int i = threadIdx.x; i < G; i += blockDim.x) t += a.partial[G + i];
-		bb = block_sum(t, sc);
-	}
+	const double bb = grp.total(bl, ok);
+	if (!ok) return out;
 	if (bb == 0.0) {
 		for (long long i = gt; i < a.n; i += gs) a.x[i] = T(0);
 		return out;
@@ -203,11 +245,11 @@ __device__ CgOut cg_body(const CgParams<T>& a, GemmSmem<T>& sm) {
 	int it = 0;
 	while (rr > tol2 && it < a.max_iter) {
 		T blk = 0;
-		if (!matvec_dev(a.plan, a.p, a.q, a.p, sm, a.bar, blk)) return out;
-		const double pAp = grid_total(double(blk), a.partial, a.bar, ok);
+		if (!matvec_dev(a.plan, a.p, a.q, a.p, sm, grp, blk)) return out;
+		const double pAp = grp.total(double(blk), ok);
 		if (!ok) return out;
 		if (!(pAp > 0.0) || !isfinite(pAp)) {
-			record_status(a.bar.status, DEV_BREAKDOWN);
+			grp.record(DEV_BREAKDOWN);
 			break;
 		}
 		const double alpha = rr / pAp;
@@ -219,12 +261,12 @@ __device__ CgOut cg_body(const CgParams<T>& a, GemmSmem<T>& sm) {
 			l += double(ri) * double(ri);
 		}
 		l = block_sum(l, sc);
-		const double rrn = grid_total(l, a.partial + G, a.bar, ok);
+		const double rrn = grp.total(l, ok);
 		if (!ok) return out;
 		const double beta = rrn / rr;
 		rr = rrn;
 		for (long long i = gt; i < a.n; i += gs) a.p[i] = a.r[i] + T(beta) * a.p[i];
-		if (!grid_sync(a.bar)) return out;
+		if (!grp.sync()) return out;
 		++it;
 	}
 	out.iterations = it;
@@ -232,15 +274,16 @@ __device__ CgOut cg_body(const CgParams<T>& a, GemmSmem<T>& sm) {
 	return out;
 }
 
-template <class T>
-__global__ void __launch_bounds__(kGemmThreads) k_cg(CgParams<T> a, int* out_i, double* out_d) {
+template <class T, class Grp>
+__global__ void __launch_bounds__(kGemmThreads) k_cg(CgParams<T> a, Grp grp, int* out_i, double* out_d) {
 	__shared__ GemmSmem<T> sm;
-	const CgOut o = cg_body(a, sm);
-	if (blockIdx.x == 0 && threadIdx.x == 0) {
+	const CgOut o = cg_body(a, sm, grp);
+	if (grp.rank() == 0 && threadIdx.x == 0) {
 		out_i[0] = o.iterations;
 		out_i[1] = 0;
 		out_d[0] = o.rel_residual;
 	}
+	if (Grp::kCluster) grp.sync();
 }
 
 // Mixed precision: FP64 residual r = b - M x, FP32 CG for M d = r / ||r||, x += ||r|| d.
@@ -254,61 +297,87 @@ struct MixedParams {
 	int max_refine;
 };
 
-__global__ void __launch_bounds__(kGemmThreads) k_cg_mixed(MixedParams a, int* out_i, double* out_d) {
+template <class Grp>
+__global__ void __launch_bounds__(kGemmThreads) k_cg_mixed(MixedParams a, Grp grp, int* out_i, double* out_d) {
 	__shared__ union U {
 		GemmSmem<double> d;
 		GemmSmem<float> f;
 		__device__ U() {}
 	} sm;
 	__shared__ double sc[32];
-	const long long gt = blockIdx.x * (long long)blockDim.x + threadIdx.x;
-	const long long gs = (long long)gridDim.x * blockDim.x;
-	const GridBarrier& bar = a.inner.bar;
-	double* partial = a.inner.partial;
+	const long long gt = grp.rank() * (long long)blockDim.x + threadIdx.x;
+	const long long gs = (long long)grp.size() * blockDim.x;
 	bool ok = true;
 	double bl = 0;
 	for (long long i = gt; i < a.n; i += gs) bl += a.b[i] * a.b[i];
-	const double bb = grid_total(block_sum(bl, sc), partial, bar, ok);
+	const double bb = grp.total(block_sum(bl, sc), ok);
 	int iters = 0, refs = 0;
 	double rel = 0;
 	for (int ref = 0; ok && ref <= a.max_refine; ++ref) {
 		double dummy;
-		if (!matvec_dev(a.p64, a.x, a.q64, (const double*)nullptr, sm.d, bar, dummy)) break;
-		if (!grid_sync(bar)) break;
+		if (!matvec_dev(a.p64, a.x, a.q64, (const double*)nullptr, sm.d, grp, dummy)) break;
+		if (!grp.sync()) break;
 		double l = 0;
 		for (long long i = gt; i < a.n; i += gs) {
 			const double ri = a.b[i] - a.q64[i];
 			a.q64[i] = ri;
 			l += ri * ri;
 		}
-		const double rr = grid_total(block_sum(l, sc), partial + gridDim.x, bar, ok);
+		const double rr = grp.total(block_sum(l, sc), ok);
 		if (!ok) break;
 		rel = bb > 0 ? sqrt(rr / bb) : 0.0;
 		if (rr <= a.tol * a.tol * bb || ref == a.max_refine) break;
 		const double nr = sqrt(rr);
 		for (long long i = gt; i < a.n; i += gs) const_cast<float*>(a.inner.b)[i] = float(a.q64[i] / nr);
-		if (!grid_sync(bar)) break;
-		const CgOut o = cg_body(a.inner, sm.f);
+		if (!grp.sync()) break;
+		const CgOut o = cg_body(a.inner, sm.f, grp);
 		iters += o.iterations;
 		for (long long i = gt; i < a.n; i += gs) a.x[i] += nr * double(a.inner.x[i]);
-		if (!grid_sync(bar)) break;
+		if (!grp.sync()) break;
 		++refs;
 	}
-	if (blockIdx.x == 0 && threadIdx.x == 0) {
+	if (grp.rank() == 0 && threadIdx.x == 0) {
 		out_i[0] = iters;
 		out_i[1] = refs;
 		out_d[0] = rel;
 	}
+	if (Grp::kCluster) grp.sync();
 }
 
 template <class F>
 static int coop_grid(F kernel, Context& c, long long work_blocks) {
-	static int occ_cache[4] = {0, 0, 0, 0};
 	int occ = 0;
 	XTT_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, kernel, kGemmThreads, 0));
-	(void)occ_cache;
 	const long long maxg = (long long)std::max(1, occ) * c.num_sms;
 	return int(std::max<long long>(1, std::min<long long>(maxg, work_blocks)));
+}
+
+// Launches `kernel` as one cluster of P CTAs if the device can schedule it; returns false otherwise.
+template <class K, class... Args>
+static bool launch_cluster(K kernel, int P, cudaStream_t s, Args... args) {
+	static bool attr = false;
+	if (!attr) {
+		XTT_CUDA(cudaFuncSetAttribute(kernel, cudaFuncAttributeNonPortableClusterSizeAllowed, 1));
+		attr = true;
+	}
+	cudaLaunchConfig_t cfg = {};
+	cfg.gridDim = dim3(P);
+	cfg.blockDim = dim3(kGemmThreads);
+	cfg.stream = s;
+	cudaLaunchAttribute at[1];
+	at[0].id = cudaLaunchAttributeClusterDimension;
+	at[0].val.clusterDim.x = P;
+	at[0].val.clusterDim.y = 1;
+	at[0].val.clusterDim.z = 1;
+	cfg.attrs = at;
+	cfg.numAttrs = 1;
+	int clusters = 0;
+	if (cudaOccupancyMaxActiveClusters(&clusters, kernel, &cfg) != cudaSuccess || clusters < 1) {
+		cudaGetLastError();
+		return false;
+	}
+	XTT_CUDA(cudaLaunchKernelEx(&cfg, kernel, args...));
+	return true;
 }
 
 __global__ void k_to_float(float* out, const double* in, size_t n) {
@@ -338,9 +407,12 @@ CgResult local_solve(Context& c, const LocalShape& s, const double* L, const dou
 	}
 	long long work = (n + kGemmThreads - 1) / kGemmThreads;
 	for (int i = 0; i < p64.ns; ++i) work = std::max(work, p64.g[i].tiles());
+	const bool use_cluster = n <= kClusterMaxN;
+	const int P = int(std::max<long long>(2, std::min<long long>(kCgClusterMax, work)));
 	int* oi = c.d_ints + 8;
 	double* od = c.d_dbl + 8;
 	CgResult res;
+	ClusterGroup cgrp{c.d_status, 0};
 	if (precision == XTT_PRECISION_FP64) {
 		CgParams<double> a;
 		a.plan = p64;
@@ -350,15 +422,16 @@ CgResult local_solve(Context& c, const LocalShape& s, const double* L, const dou
 		a.q = c.scratch<double>(S_ALS_FIRST + 25, n);
 		a.b = b;
 		a.n = n;
-		const int G = coop_grid(k_cg<double>, c, work);
-		a.partial = c.scratch<double>(S_ALS_FIRST + 26, 2 * size_t(G));
-		a.bar = GridBarrier{c.d_barrier, c.d_barrier + 1, c.d_status};
 		a.max_iter = max_iter;
 		a.tol = tol;
 		a.zero_guess = 0;
-		void* args[] = {&a, &oi, &od};
 		ProfScope ps(c, "cg_fp64");
-		XTT_CUDA(cudaLaunchCooperativeKernel((void*)k_cg<double>, dim3(G), dim3(kGemmThreads), args, 0, c.stream));
+		if (!(use_cluster && launch_cluster(k_cg<double, ClusterGroup>, P, c.stream, a, cgrp, oi, od))) {
+			const int G = coop_grid(k_cg<double, GridGroup>, c, work);
+			GridGroup g{GridBarrier{c.d_barrier, c.d_barrier + 1, c.d_status}, c.scratch<double>(S_ALS_FIRST + 26, 2 * size_t(G)), 0};
+			void* args[] = {&a, &g, &oi, &od};
+			XTT_CUDA(cudaLaunchCooperativeKernel((void*)k_cg<double, GridGroup>, dim3(G), dim3(kGemmThreads), args, 0, c.stream));
+		}
 		c.count_launch();
 	} else {
 		// FP32 copies of the environments and operator cores
@@ -389,9 +462,6 @@ CgResult local_solve(Context& c, const LocalShape& s, const double* L, const dou
 		m.inner.q = v + 3 * n;
 		m.inner.b = v + 4 * n;
 		m.inner.n = n;
-		const int G = coop_grid(k_cg_mixed, c, work);
-		m.inner.partial = c.scratch<double>(S_ALS_FIRST + 26, 2 * size_t(G));
-		m.inner.bar = GridBarrier{c.d_barrier, c.d_barrier + 1, c.d_status};
 		m.inner.max_iter = max_iter;
 		m.inner.tol = 1e-6;
 		m.inner.zero_guess = 1;
@@ -401,9 +471,13 @@ CgResult local_solve(Context& c, const LocalShape& s, const double* L, const dou
 		m.n = n;
 		m.tol = tol;
 		m.max_refine = 12;
-		void* args[] = {&m, &oi, &od};
 		ProfScope ps(c, "cg_mixed");
-		XTT_CUDA(cudaLaunchCooperativeKernel((void*)k_cg_mixed, dim3(G), dim3(kGemmThreads), args, 0, c.stream));
+		if (!(use_cluster && launch_cluster(k_cg_mixed<ClusterGroup>, P, c.stream, m, cgrp, oi, od))) {
+			const int G = coop_grid(k_cg_mixed<GridGroup>, c, work);
+			GridGroup g{GridBarrier{c.d_barrier, c.d_barrier + 1, c.d_status}, c.scratch<double>(S_ALS_FIRST + 26, 2 * size_t(G)), 0};
+			void* args[] = {&m, &g, &oi, &od};
+			XTT_CUDA(cudaLaunchCooperativeKernel((void*)k_cg_mixed<GridGroup>, dim3(G), dim3(kGemmThreads), args, 0, c.stream));
+		}
 		c.count_launch();
 	}
 	return res;  // counters are read lazily by the driver (ctx d_ints[8..9], d_dbl[8])

@@ -15,6 +15,8 @@
 // (src/xerus/tensor.cpp:1463-1474).
 #include <cfloat>
 
+#include <cooperative_groups.h>
+
 #include "linalg.cuh"
 
 namespace xtt {
@@ -191,6 +193,7 @@ __global__ void __launch_bounds__(kQrThreads) k_qr(QrArgs a, int use_smem) {
 		else a.C[(long long)perm[j] * rank + r] = v;
 	}
 	__syncthreads();
+	if (!a.want_q) return;
 	// Q = H_0 ... H_{rank-1} [I; 0], in place in the first `rank` columns
 	for (int j = rank - 1; j >= 0; --j) {
 		const double tj = tau[j];
@@ -231,8 +234,338 @@ __global__ void __launch_bounds__(kQrThreads) k_qr(QrArgs a, int use_smem) {
 	}
 }
 
+// ----------------------------------------------------------- cluster QR
+//
+// The same factorisation with the rows of the working matrix split across the
+// CTAs of one thread-block cluster (up to 16 SMs), each holding its row block
+// in shared memory. Per column j: every CTA contributes partial sums over its
+// rows (column norm below the diagonal, then w = v^T A[:, j+1:]) to a buffer
+// in its own shared memory, one hardware cluster barrier later every CTA sums
+// all CTAs' partials through distributed shared memory in rank order, so all
+// CTAs hold bit-identical reflectors and update only their own rows. Partial
+// buffers alternate with the column's parity, which is what lets two barriers
+// per column (three with pivoting) suffice. GB300's FP64 rate per SM (~8
+// GFLOP/s) is what this buys back: the trailing updates run on 16 SMs.
+
+constexpr int kQcThreads = 256;
+
+struct QcLayout {
+	int mb, nw, kq;
+	__host__ __device__ size_t wl() const { return 0; }
+	__host__ __device__ size_t vec() const { return size_t(mb) * nw; }
+	__host__ __device__ size_t nrm() const { return vec() + 2 * size_t(nw); }
+	__host__ __device__ size_t cn2() const { return nrm() + 2 * size_t(nw); }
+	__host__ __device__ size_t tau() const { return cn2() + nw; }
+	__host__ __device__ size_t scl() const { return tau() + kq; }
+	__host__ __device__ size_t dg() const { return scl() + 8; }
+	__host__ __device__ size_t perm() const { return dg() + mb; }
+	__host__ __device__ size_t total() const { return perm() + size_t(nw + 1) / 2 + 1; }
+};
+
+__global__ void __launch_bounds__(kQcThreads) k_qr_cluster(QrArgs a, QcLayout lay) {
+	namespace cg = cooperative_groups;
+	cg::cluster_group cl = cg::this_cluster();
+	const int P = int(cl.num_blocks()), me = int(cl.block_rank());
+	const int tid = threadIdx.x, tx = tid & 31, ty = tid >> 5, NY = kQcThreads / 32;
+	const int mw = a.transpose ? a.n : a.m, nw = lay.nw, kq = lay.kq, mb = lay.mb;
+	const int r0 = me * mb, r1 = min(mw, r0 + mb), nl = max(0, r1 - r0);
+	extern __shared__ double sm[];
+	double* Wl = sm + lay.wl();
+	double* vec = sm + lay.vec();
+	double* nrm = sm + lay.nrm();
+	double* cn2 = sm + lay.cn2();
+	double* tau = sm + lay.tau();
+	double* scl = sm + lay.scl();
+	double* dg = sm + lay.dg();
+	int* perm = reinterpret_cast<int*>(sm + lay.perm());
+	__shared__ double red[kQcThreads / 32][33];
+	__shared__ double s_w[32];
+	__shared__ double s_coef[3];
+	__shared__ int s_idx[kQcThreads / 32];
+	__shared__ double s_best[kQcThreads / 32];
+	auto w = [&](int il, int j) -> double& { return Wl[(long long)il * nw + j]; };
+
+	for (long long e = tid; e < (long long)nl * nw; e += blockDim.x) {
+		const int il = int(e / nw), j = int(e % nw), gi = r0 + il;
+		w(il, j) = a.transpose ? a.A[(long long)j * a.lda + gi] : a.A[(long long)gi * a.lda + j];
+	}
+	for (int j = tid; j < nw; j += blockDim.x) perm[j] = j;
+	__syncthreads();
+	// column c partial sums over local rows il >= lo of f(il, c) into dst[c] (c in [c0, nw))
+	auto colsum = [&](int c0, int lo, double* dst, auto f) {
+		for (int cb = c0; cb < nw; cb += 32) {
+			const int c = cb + tx;
+			double pt = 0;
+			if (c < nw)
+				for (int il = lo + ty; il < nl; il += NY) pt += f(il, c);
+			red[ty][tx] = pt;
+			__syncthreads();
+			if (ty == 0 && c < nw) {
+				double s = 0;
+				for (int t = 0; t < NY; ++t) s += red[t][tx];
+				dst[c] = s;
+			}
+			__syncthreads();
+		}
+	};
+	auto lo_of = [&](int g) { return min(max(g - r0, 0), nl); };  // first local row with global index >= g
+	if (a.pivot) {
+		colsum(0, 0, nrm, [&](int il, int c) { return w(il, c) * w(il, c); });
+		cl.sync();
+		for (int c = tid; c < nw; c += blockDim.x) {
+			double s = 0;
+			for (int p = 0; p < P; ++p) s += cl.map_shared_rank(nrm, p)[c];
+			cn2[c] = s;
+		}
+		__syncthreads();
+	}
+	for (int j = 0; j < kq; ++j) {
+		const int par = j & 1;
+		double* vecp = vec + par * nw;
+		double* nrmp = nrm + (1 - par) * nw;  // the initial norms used buffer 0
+		double* sclp = scl + par * 4;
+		if (a.pivot) {
+			double best = -1.0;
+			int bi = nw;
+			for (int c = j + tid; c < nw; c += blockDim.x)
+				if (cn2[c] > best) { best = cn2[c]; bi = c; }
+#pragma unroll
+			for (int o = 16; o > 0; o >>= 1) {
+				const double ob = __shfl_xor_sync(0xffffffffu, best, o);
+				const int oi = __shfl_xor_sync(0xffffffffu, bi, o);
+				if (ob > best || (ob == best && oi < bi)) { best = ob; bi = oi; }
+			}
+			if (tx == 0) { s_best[ty] = best; s_idx[ty] = bi; }
+			__syncthreads();
+			if (tid == 0) {
+				double b = -1.0;
+				int ix = nw;
+				for (int t = 0; t < NY; ++t)
+					if (s_best[t] > b || (s_best[t] == b && s_idx[t] < ix)) { b = s_best[t]; ix = s_idx[t]; }
+				s_idx[0] = ix;
+			}
+			__syncthreads();
+			const int p = s_idx[0];
+			if (p != j && p < nw) {
+				for (int il = tid; il < nl; il += blockDim.x) {
+					const double t = w(il, j);
+					w(il, j) = w(il, p);
+					w(il, p) = t;
+				}
+				if (tid == 0) {
+					const double t = cn2[j]; cn2[j] = cn2[p]; cn2[p] = t;
+					const int q = perm[j]; perm[j] = perm[p]; perm[p] = q;
+				}
+			}
+			__syncthreads();
+		}
+		// reflector of column j: partial norm below the diagonal and alpha from the owner of row j
+		{
+			double part = 0;
+			for (int il = lo_of(j + 1) + tid; il < nl; il += blockDim.x) part += w(il, j) * w(il, j);
+			__shared__ double sc[32];
+			part = block_sum(part, sc);
+			if (tid == 0) {
+				sclp[0] = part;
+				sclp[1] = (j >= r0 && j < r1) ? w(j - r0, j) : 0.0;
+			}
+		}
+		cl.sync();
+		if (tid == 0) {
+			double xn2 = 0, alpha = 0;
+			for (int p = 0; p < P; ++p) {
+				const double* rs = cl.map_shared_rank(sclp, p);
+				xn2 += rs[0];
+				alpha += rs[1];
+			}
+			double t = 0, scal = 1.0, beta = alpha;
+			if (xn2 != 0.0) {
+				beta = -copysign(sqrt(alpha * alpha + xn2), alpha);
+				t = (beta - alpha) / beta;
+				scal = 1.0 / (alpha - beta);
+			}
+			tau[j] = t;
+			s_coef[0] = t;
+			s_coef[1] = scal;
+			s_coef[2] = beta;
+		}
+		__syncthreads();
+		const double tj = s_coef[0], scal = s_coef[1];
+		for (int il = lo_of(j + 1) + tid; il < nl; il += blockDim.x) w(il, j) *= scal;
+		if (tid == 0 && j >= r0 && j < r1) w(j - r0, j) = s_coef[2];
+		__syncthreads();
+		// w = v^T A[:, j+1:] over local rows >= j (v_j = 1)
+		const int lo = lo_of(j);
+		colsum(j + 1, lo, vecp, [&](int il, int c) { return (r0 + il == j ? 1.0 : w(il, j)) * w(il, c); });
+		cl.sync();
+		for (int cb = j + 1; cb < nw; cb += 32) {
+			const int c = cb + tx;
+			if (ty == 0) {
+				double s = 0;
+				if (c < nw)
+					for (int p = 0; p < P; ++p) s += cl.map_shared_rank(vecp, p)[c];
+				s_w[tx] = tj * s;
+			}
+			__syncthreads();
+			double nr = 0;
+			if (c < nw) {
+				const double wc = s_w[tx];
+				for (int il = lo + ty; il < nl; il += NY) {
+					const double v = (r0 + il == j) ? 1.0 : w(il, j);
+					const double u = w(il, c) - wc * v;
+					w(il, c) = u;
+					if (r0 + il > j) nr += u * u;
+				}
+			}
+			if (a.pivot) {
+				red[ty][tx] = nr;
+				__syncthreads();
+				if (ty == 0 && c < nw) {
+					double s = 0;
+					for (int t = 0; t < NY; ++t) s += red[t][tx];
+					nrmp[c] = s;
+				}
+			}
+			__syncthreads();
+		}
+		if (a.pivot) {
+			cl.sync();
+			for (int c = j + 1 + tid; c < nw; c += blockDim.x) {
+				double s = 0;
+				for (int p = 0; p < P; ++p) s += cl.map_shared_rank(nrmp, p)[c];
+				cn2[c] = s;
+			}
+			__syncthreads();
+		}
+	}
+	// rank rule: every CTA reads the diagonal through DSMEM and decides identically
+	for (int il = tid; il < nl; il += blockDim.x) dg[il] = (r0 + il < kq) ? w(il, r0 + il) : 0.0;
+	cl.sync();
+	__shared__ int s_rank;
+	if (tid == 0) {
+		int rank = kq;
+		if (a.pivot) {
+			const double r00 = cl.map_shared_rank(dg, 0)[0];
+			for (int k = 1; k < kq; ++k) {
+				const int p = k / mb;
+				if (fabs(cl.map_shared_rank(dg, p)[k - p * mb]) < 16.0 * DBL_EPSILON * r00) { rank = k; break; }
+			}
+		}
+		s_rank = rank;
+		if (me == 0 && a.rank_out) *a.rank_out = rank;
+	}
+	__syncthreads();
+	const int rank = s_rank;
+	for (long long e = tid; e < (long long)nl * nw; e += blockDim.x) {
+		const int il = int(e / nw), jj = int(e % nw), r = r0 + il;
+		if (r >= rank) continue;
+		const double v = (r <= jj) ? w(il, jj) : 0.0;
+		if (!a.transpose) a.C[(long long)r * nw + perm[jj]] = v;
+		else a.C[(long long)perm[jj] * rank + r] = v;
+	}
+	if (!a.want_q) {
+		cl.sync();  // keep every CTA's shared memory alive until all remote reads are done
+		return;
+	}
+	__syncthreads();
+	for (int j = rank - 1; j >= 0; --j) {
+		const int par = j & 1;
+		double* vecp = vec + par * nw;
+		const double tj = tau[j];
+		const int lo = lo_of(j + 1);
+		if (j < rank - 1) {
+			// w_c = sum_{rows > j} v_i Q[i][c] for c in (j, rank); row j of those columns is zero
+			for (int cb = j + 1; cb < rank; cb += 32) {
+				const int c = cb + tx;
+				double pt = 0;
+				if (c < rank)
+					for (int il = lo + ty; il < nl; il += NY) pt += w(il, j) * w(il, c);
+				red[ty][tx] = pt;
+				__syncthreads();
+				if (ty == 0 && c < rank) {
+					double s = 0;
+					for (int t = 0; t < NY; ++t) s += red[t][tx];
+					vecp[c] = s;
+				}
+				__syncthreads();
+			}
+			cl.sync();
+			for (int cb = j + 1; cb < rank; cb += 32) {
+				const int c = cb + tx;
+				if (ty == 0) {
+					double s = 0;
+					if (c < rank)
+						for (int p = 0; p < P; ++p) s += cl.map_shared_rank(vecp, p)[c];
+					s_w[tx] = tj * s;
+				}
+				__syncthreads();
+				if (c < rank) {
+					const double wc = s_w[tx];
+					if (ty == 0 && j >= r0 && j < r1) w(j - r0, c) = -wc;
+					for (int il = lo + ty; il < nl; il += NY) w(il, c) -= wc * w(il, j);
+				}
+				__syncthreads();
+			}
+		}
+		for (int il = tid; il < nl; il += blockDim.x) {
+			const int gi = r0 + il;
+			if (gi > j) w(il, j) *= -tj;
+			else if (gi == j) w(il, j) = 1.0 - tj;
+			else w(il, j) = 0.0;
+		}
+		__syncthreads();
+	}
+	for (long long e = tid; e < (long long)nl * rank; e += blockDim.x) {
+		const int il = int(e / rank), c = int(e % rank), gi = r0 + il;
+		const double v = w(il, c);
+		if (!a.transpose) a.Q[(long long)gi * rank + c] = v;
+		else a.Q[(long long)c * mw + gi] = v;
+	}
+	cl.sync();  // no CTA leaves while others may still read its shared memory
+}
+
+// Cluster geometry for an mw x nw factorisation: 0 CTAs if the one-CTA kernel is used.
+static int qr_cluster_size(int mw, int nw, QcLayout& lay) {
+	if (mw < 96 || nw < 8) return 0;
+	int P = std::min(16, (mw + 15) / 16);
+	lay.mb = (mw + P - 1) / P;
+	P = (mw + lay.mb - 1) / lay.mb;
+	lay.nw = nw;
+	lay.kq = std::min(mw, nw);
+	if (lay.total() * sizeof(double) > kDynSmemMax) return 0;
+	return P;
+}
+
 void launch_qr(const QrArgs& a, cudaStream_t s) {
 	const int mw = a.transpose ? a.n : a.m, nw = a.transpose ? a.m : a.n;
+	QcLayout lay;
+	const int P = qr_cluster_size(mw, nw, lay);
+	if (P > 1) {
+		static bool attr = false;
+		if (!attr) {
+			XTT_CUDA(cudaFuncSetAttribute(k_qr_cluster, cudaFuncAttributeMaxDynamicSharedMemorySize, int(kDynSmemMax)));
+			XTT_CUDA(cudaFuncSetAttribute(k_qr_cluster, cudaFuncAttributeNonPortableClusterSizeAllowed, 1));
+			attr = true;
+		}
+		cudaLaunchConfig_t cfg = {};
+		cfg.gridDim = dim3(P);
+		cfg.blockDim = dim3(kQcThreads);
+		cfg.dynamicSmemBytes = lay.total() * sizeof(double);
+		cfg.stream = s;
+		cudaLaunchAttribute at[1];
+		at[0].id = cudaLaunchAttributeClusterDimension;
+		at[0].val.clusterDim.x = P;
+		at[0].val.clusterDim.y = 1;
+		at[0].val.clusterDim.z = 1;
+		cfg.attrs = at;
+		cfg.numAttrs = 1;
+		int clusters = 0;
+		if (cudaOccupancyMaxActiveClusters(&clusters, k_qr_cluster, &cfg) == cudaSuccess && clusters > 0) {
+			XTT_CUDA(cudaLaunchKernelEx(&cfg, k_qr_cluster, a, lay));
+			return;
+		}
+		cudaGetLastError();  // not schedulable as a cluster here: one CTA below
+	}
 	const size_t aux = qr_aux_doubles(mw, nw) * sizeof(double);
 	const size_t full = aux + size_t(mw) * nw * sizeof(double);
 	const int use_smem = full <= kDynSmemMax ? 1 : 0;

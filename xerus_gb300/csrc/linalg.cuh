@@ -21,6 +21,7 @@ struct QrArgs {
 	double* Q = nullptr;
 	double* C = nullptr;
 	int* rank_out = nullptr;    // device int
+	int want_q = 1;             // 0: only C (the triangular factor) is written, Q is not formed
 };
 
 struct SvdArgs {

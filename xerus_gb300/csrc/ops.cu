@@ -679,32 +679,65 @@ __global__ void k_block_core(double* out, const double* p, const double* q, int 
 }
 
 double residual(const Tensor& A, const Tensor& x, const Tensor& b) {
-	XTT_REQUIRE(x.dims == b.dims, "x and b dimensions differ");
+	// ||A x - b|| / ||b|| (src/xerus/algorithms/als.cpp:258-261) without cancellation: the block
+	// cores of y = A x - b (TT sum, src/xerus/ttNetwork.cpp:796-856) are formed one at a time and
+	// orthogonalised left to right; only the triangular factor R is carried, so neither the
+	// residual TT nor any orthogonal factor is ever stored.
+	XTT_REQUIRE(x.dims == b.dims && A.dims == x.dims && A.op && !x.op && !b.op, "x and b dimensions differ");
 	Context& c = *x.ctx;
 	const int d = x.d;
-	std::vector<int64_t> r(d + 1, 1);
-	Tensor ax(&c, false, d, x.dims.data(), r.data());
-	op_apply_tt(A, x, ax);
-	Tensor y(&c, false, d, x.dims.data(), r.data());
-	if (d == 1) {
-		y.reshape_core(0, 1, 1);
-		k_block_core<<<grid_for(x.dims[0]), 256, 0, c.stream>>>(y.core[0], ax.core[0], b.core[0], 1, 1, 1, 1,
-		                                                        int(x.dims[0]), 1, 1);
-		c.count_launch();
-	} else {
-		for (int k = 0; k < d; ++k) {
-			const int P0 = int(ax.ranks[k]), P1 = int(ax.ranks[k + 1]), Q0 = int(b.ranks[k]), Q1 = int(b.ranks[k + 1]);
-			const int first = k == 0, last = k == d - 1;
-			y.reshape_core(k, first ? 1 : P0 + Q0, last ? 1 : P1 + Q1);
-			k_block_core<<<grid_for(y.core_size(k)), 256, 0, c.stream>>>(y.core[k], ax.core[k], b.core[k], P0, P1, Q0,
-			                                                              Q1, int(x.dims[k]), first, last);
-			c.count_launch();
-		}
-	}
-	XTT_CUDA(cudaGetLastError());
-	const double ny = orthogonal_norm(y);
 	const double nb = frob_norm(b);
-	return ny / nb;
+	size_t cap_core = 1, cap_r = 1;
+	for (int k = 0; k < d; ++k) {
+		const size_t p0 = size_t(A.ranks[k] * x.ranks[k] + b.ranks[k]), p1 = size_t(A.ranks[k + 1] * x.ranks[k + 1] + b.ranks[k + 1]);
+		cap_core = std::max(cap_core, p0 * size_t(x.dims[k]) * p1);
+		cap_r = std::max({cap_r, p0 * p1, p0 * p0, p1 * p1});
+	}
+	double* ax = c.scratch<double>(S_RES_CORE0, cap_core);
+	double* Y = c.scratch<double>(S_RES_CORE1, cap_core);
+	double* Z = c.scratch<double>(S_RES_R, cap_core + cap_r);
+	double* R = Z + cap_core;
+	fill(c, R, 1.0, 1);
+	int64_t rr = 1;
+	for (int k = 0; k < d; ++k) {
+		const int K = int(A.ranks[k]), L = int(A.ranks[k + 1]), ra = int(x.ranks[k]), rb = int(x.ranks[k + 1]);
+		const int n = int(x.dims[k]);
+		const int P0 = K * ra, P1 = L * rb, Q0 = int(b.ranks[k]), Q1 = int(b.ranks[k + 1]);
+		const int first = k == 0, last = k == d - 1;
+		const int O0 = first ? 1 : P0 + Q0, O1 = last ? 1 : P1 + Q1;
+		const size_t nax = size_t(P0) * n * P1, ny = size_t(O0) * n * O1;
+		k_op_apply<<<grid_for(nax), 256, 0, c.stream>>>(ax, A.core[k], x.core[k], K, L, n, ra, rb);
+		k_block_core<<<grid_for(ny), 256, 0, c.stream>>>(Y, ax, b.core[k], P0, P1, Q0, Q1, n, first, last);
+		c.count_launch(2);
+		XTT_CUDA(cudaGetLastError());
+		Gemm<double> g;  // Z = R (rr x O0) * Y (O0 x n O1)
+		g.M = int(rr); g.N = int(n * O1); g.K = O0;
+		g.A = R; g.sAm = O0; g.sAk = 1;
+		g.B = Y; g.sBk = n * O1; g.sBn = 1;
+		g.C = Z; g.sCm = n * O1; g.sCn = 1;
+		g.lens((long long)cap_r, (long long)ny, (long long)cap_core);
+		gemm(c, g);
+		const size_t nz = size_t(rr) * n * O1;
+		if (last) {
+			sumsq_async(c, Z, nz, 0);
+			return std::sqrt(read_dbl(c, 0)) / nb;
+		}
+		// R <- triangular factor of Z viewed as (rr n) x O1 (Householder, R only)
+		const int m = int(rr * n), kq = std::min(m, O1);
+		QrArgs a;
+		const size_t wk = qr_work_doubles(m, O1);
+		a.A = Z; a.lda = O1; a.m = m; a.n = O1; a.transpose = 0; a.pivot = 0; a.want_q = 0;
+		a.work = wk ? c.scratch<double>(S_QR_WORK, wk) : nullptr;
+		a.Q = nullptr; a.C = R; a.rank_out = nullptr;
+		XTT_REQUIRE(size_t(kq) * O1 <= cap_r, "internal: residual carry too small");
+		{
+			ProfScope ps(c, "qr");
+			launch_qr(a, c.stream);
+		}
+		c.count_launch();
+		rr = kq;
+	}
+	return 0.0;
 }
 
 // One block per sample: v <- v * x_k[:, i_k, :]
