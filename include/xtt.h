@@ -66,6 +66,15 @@ int xtt_context_profile(xtt_context* ctx, int enable);
 /* Launch count and total milliseconds of one class since profiling started (0 if none). */
 int xtt_context_profile_get(xtt_context* ctx, const char* name, int64_t* launches, double* milliseconds);
 
+/* Which kernel family runs the local conjugate-gradient solves of xtt_als (no
+ * reference counterpart; the reference factors the local system densely,
+ * src/xerus/algorithms/als.cpp:43-71). AUTO: one thread-block cluster with all
+ * operands in shared memory when the local system fits (up to 16 CTAs), else
+ * the grid-wide cooperative kernel. GRID: always the grid-wide kernel. Results
+ * agree to the CG tolerance; the choice only changes speed. */
+typedef enum xtt_cg_path { XTT_CG_PATH_AUTO = 0, XTT_CG_PATH_GRID = 1 } xtt_cg_path;
+int xtt_context_set_cg_path(xtt_context* ctx, int path);
+
 /* ---------------------------------------------------------------- tensors */
 /* TTNetwork(dims) + set_component: a device TT with the given ranks (order+1
  * entries, r_0 = r_d = 1), all cores zero, not canonical.

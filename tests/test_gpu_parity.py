@@ -184,6 +184,28 @@ def test_als_ragged_dims(ctx, golden):
     assert rel_err(x.entries(z["rag_hs6_x_probe_pos"]), z["rag_hs6_x_probe_val"]) < 1e-9
 
 
+@pytest.mark.parametrize("precision", ["fp64", "mixed"])
+def test_cg_paths_agree(ctx, golden, precision):
+    """The cluster-resident local CG (default where the local system fits) and the
+    grid-wide kernel give the reference's energy on the rank-32 workload."""
+    z = golden("als")
+    out = {}
+    try:
+        for path in ("grid", "auto"):
+            ctx.set_cg_path(path)
+            A, b, x = dev_op(ctx, op_of(z, "A")), dev_tt(ctx, tt_of(z, "b_r32")), dev_tt(ctx, tt_of(z, "x0_r32"))
+            v = xg.ALS_SPD.copy()
+            v.convergenceEpsilon = 0.0
+            if precision == "mixed":
+                v.precision = xg.MIXED
+            out[path] = (v(A, x, b, 2), xg.residual(A, x, b))
+            assert abs(out[path][0] / z["r32_hs2_energy"][0] - 1) < REL_TOL
+    finally:
+        ctx.set_cg_path("auto")
+    # both iterates sit at the local-solve noise floor (1e-13 per local CG), far below 1e-8
+    assert max(out["grid"][1], out["auto"][1]) < 1e-10
+
+
 def test_als_mixed_precision_matches_fp64(ctx, golden):
     z = golden("als")
     A, b = dev_op(ctx, op_of(z, "A")), dev_tt(ctx, tt_of(z, "b_r32"))
@@ -341,3 +363,45 @@ def test_als_energy_gradient(ctx, golden):
         vals.append(o.tt_dot(xt, o.op_apply(Ah, xt)) - 2 * o.tt_dot(xt, bh))
     fd = (vals[0] - vals[1]) / (2 * h)
     assert abs(float(np.sum(grads[k] * dx)) / fd - 1) < 1e-6
+
+
+def test_torch_autograd_adjoints(ctx):
+    """The torch.autograd.Function wrappers return the device gradients; checked
+    by a directional central difference in FP64 (h = 1e-4, as for ADF's check)."""
+    torch = pytest.importorskip("torch")
+    from xerus_gb300.autograd import adf_loss, als_energy
+    xg.seed(5)
+    dims = [3, 4, 3, 2, 3]
+    x = xg.TTTensor.random(dims, 2, ctx=ctx)
+    target = xg.TTTensor.random(dims, 2, ctx=ctx)
+    m = xg.SinglePointMeasurementSet.random(60, dims)
+    m.measure(target)
+    cores = [torch.tensor(c, requires_grad=True) for c in x.get_cores()]
+    pos, val = torch.tensor(m.positions), torch.tensor(m.measuredValues)
+    loss = adf_loss(pos, val, cores)
+    loss.backward()
+    g = [c.grad.clone() for c in cores]
+    rng = np.random.default_rng(0)
+    dirs = [torch.tensor(rng.standard_normal(c.shape)) for c in cores]
+    h = 1e-4
+    with torch.no_grad():
+        lp = adf_loss(pos, val, [c + h * d for c, d in zip(cores, dirs)])
+        lm = adf_loss(pos, val, [c - h * d for c, d in zip(cores, dirs)])
+    fd = float((lp - lm) / (2 * h))
+    an = float(sum((gi * di).sum() for gi, di in zip(g, dirs)))
+    assert abs(an / fd - 1) < 1e-6
+    d3 = [3] * 5
+    A = xg.TTOperator.from_cores(xg.laplacian_cores(len(d3), 3, shift=0.3), ctx=ctx)
+    b = xg.TTTensor.random(d3, 2, ctx=ctx)
+    x3 = xg.TTTensor.random(d3, 2, ctx=ctx)
+    cores = [torch.tensor(c, requires_grad=True) for c in x3.get_cores()]
+    J = als_energy(A, b, cores)
+    J.backward()
+    g = [c.grad.clone() for c in cores]
+    dirs = [torch.tensor(rng.standard_normal(c.shape)) for c in cores]
+    with torch.no_grad():
+        Jp = als_energy(A, b, [c + h * d for c, d in zip(cores, dirs)])
+        Jm = als_energy(A, b, [c - h * d for c, d in zip(cores, dirs)])
+    fd = float((Jp - Jm) / (2 * h))
+    an = float(sum((gi * di).sum() for gi, di in zip(g, dirs)))
+    assert abs(an / fd - 1) < 1e-6

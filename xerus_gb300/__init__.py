@@ -64,6 +64,10 @@ class Context:
         """Starts (clears) or stops per-kernel-class CUDA-event timing."""
         L.check(self.lib.xtt_context_profile(self.handle, int(bool(enable))))
 
+    def set_cg_path(self, path):
+        """'auto' (cluster-resident CG where the local system fits) or 'grid'."""
+        L.check(self.lib.xtt_context_set_cg_path(self.handle, {"auto": 0, "grid": 1}[path]))
+
     def profile_get(self, name):
         """(launches, milliseconds) of a kernel class since profiling started."""
         n, ms = ctypes.c_int64(), ctypes.c_double()

@@ -64,6 +64,7 @@ _SIGNATURES = {
     "xtt_context_kernel_launches": (ctypes.c_int, [VP, c_int64_p]),
     "xtt_context_profile": (ctypes.c_int, [VP, ctypes.c_int]),
     "xtt_context_profile_get": (ctypes.c_int, [VP, ctypes.c_char_p, c_int64_p, c_double_p]),
+    "xtt_context_set_cg_path": (ctypes.c_int, [VP, ctypes.c_int]),
     "xtt_tensor_create": (ctypes.c_int, [VP, ctypes.c_int, ctypes.c_int64, c_int64_p, c_int64_p, ctypes.POINTER(VP)]),
     "xtt_tensor_destroy": (ctypes.c_int, [VP]),
     "xtt_tensor_copy": (ctypes.c_int, [VP, ctypes.POINTER(VP)]),

@@ -278,9 +278,8 @@ template <class T, class Grp>
 __global__ void __launch_bounds__(kGemmThreads) k_cg(CgParams<T> a, Grp grp, int* out_i, double* out_d) {
 	__shared__ GemmSmem<T> sm;
 	const CgOut o = cg_body(a, sm, grp);
-	if (grp.rank() == 0 && threadIdx.x == 0) {
-		out_i[0] = o.iterations;
-		out_i[1] = 0;
+	if (grp.rank() == 0 && threadIdx.x == 0) {  // counters accumulate over a sweep
+		out_i[0] += o.iterations;
 		out_d[0] = o.rel_residual;
 	}
 	if (Grp::kCluster) grp.sync();
@@ -337,8 +336,8 @@ __global__ void __launch_bounds__(kGemmThreads) k_cg_mixed(MixedParams a, Grp gr
 		++refs;
 	}
 	if (grp.rank() == 0 && threadIdx.x == 0) {
-		out_i[0] = iters;
-		out_i[1] = refs;
+		out_i[0] += iters;
+		out_i[1] += refs;
 		out_d[0] = rel;
 	}
 	if (Grp::kCluster) grp.sync();
@@ -405,13 +404,15 @@ CgResult local_solve(Context& c, const LocalShape& s, const double* L, const dou
 		chk.g[chk.ns - 1].C = x;
 		for (int i = 0; i < chk.ns; ++i) check_gemm(chk.g[i]);
 	}
+	CgResult res;
+	if (c.cg_path != XTT_CG_PATH_GRID && cluster_local_solve(c, s, L, A1, A2, R, b, x, tol, max_iter, precision))
+		return res;  // counters are read lazily by the driver (ctx d_ints[8..9], d_dbl[8])
 	long long work = (n + kGemmThreads - 1) / kGemmThreads;
 	for (int i = 0; i < p64.ns; ++i) work = std::max(work, p64.g[i].tiles());
-	const bool use_cluster = n <= kClusterMaxN;
+	const bool use_cluster = n <= kClusterMaxN && c.cg_path != XTT_CG_PATH_GRID;
 	const int P = int(std::max<long long>(2, std::min<long long>(kCgClusterMax, work)));
 	int* oi = c.d_ints + 8;
 	double* od = c.d_dbl + 8;
-	CgResult res;
 	ClusterGroup cgrp{c.d_status, 0};
 	if (precision == XTT_PRECISION_FP64) {
 		CgParams<double> a;
@@ -863,6 +864,7 @@ AlsReport als(const Tensor& A, Tensor& x, const Tensor& b, const AlsOptions& o) 
 	double energy = s.energy(cur), last_e = 1e101, last_e2 = 1e102;
 	record(3);
 	int half = 0;
+	XTT_CUDA(cudaMemsetAsync(c.d_ints + 8, 0, 2 * sizeof(int), c.stream));  // CG counters of this solve
 	while (true) {
 		const LocalShape sh = s.shape(cur);
 		const long long n = sh.dim();
@@ -883,7 +885,6 @@ AlsReport als(const Tensor& A, Tensor& x, const Tensor& b, const AlsOptions& o) 
 			const int max_it = max_it_opt > 0 ? max_it_opt : int(std::min<long long>(10 * n + 100, 1 << 30));
 			local_solve(c, sh, s.st.Lop[cur], A.core[cur], s.A2(cur), s.st.Rop[cur + S], s.bloc, s.v, o.local_tolerance,
 			            max_it, o.precision);
-			XTT_CUDA(cudaMemcpyAsync(c.h_ints + 8, c.d_ints + 8, 2 * sizeof(int), cudaMemcpyDeviceToHost, c.stream));
 		}
 		if (S == 1) {
 			copy_d2d(c, x.core[cur], s.v, size_t(n));
@@ -924,11 +925,6 @@ AlsReport als(const Tensor& A, Tensor& x, const Tensor& b, const AlsOptions& o) 
 			}
 			x.canonicalized = false;  // set_component on a second position (ttNetwork.cpp:491)
 		}
-		if (o.local_solver == 0) {
-			c.sync();
-			rep.local_iterations += c.h_ints[8];
-			rep.refinements += c.h_ints[9];
-		}
 		++rep.micro_steps;
 		// check_for_end_of_sweep (als.cpp:426-475)
 		if ((!inc && cur == first) || (inc && cur == last - S)) {
@@ -968,7 +964,10 @@ AlsReport als(const Tensor& A, Tensor& x, const Tensor& b, const AlsOptions& o) 
 	rep.energy = energy;
 	rep.half_sweeps = half;
 	if (o.record_residuals && !rep.residuals.empty()) rep.residual = rep.residuals.back();
+	XTT_CUDA(cudaMemcpyAsync(c.h_ints + 8, c.d_ints + 8, 2 * sizeof(int), cudaMemcpyDeviceToHost, c.stream));
 	c.sync();
+	rep.local_iterations = c.h_ints[8];
+	rep.refinements = c.h_ints[9];
 	return rep;
 }
 

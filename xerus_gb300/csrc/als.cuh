@@ -43,6 +43,12 @@ struct CgResult {
 CgResult local_solve(Context& c, const LocalShape& s, const double* L, const double* A1, const double* A2,
                      const double* R, const double* b, double* x, double tol, int max_iter, int precision);
 
+// The same solve in one thread-block cluster with every operand in shared
+// memory (cg_cluster.cu); false when the system does not fit, in which case
+// nothing was launched.
+bool cluster_local_solve(Context& c, const LocalShape& s, const double* L, const double* A1, const double* A2,
+                         const double* R, const double* b, double* x, double tol, int max_iter, int precision);
+
 // y = M x once (FP64), host-launched chain.
 void local_matvec(Context& c, const LocalShape& s, const double* L, const double* A1, const double* A2,
                   const double* R, const double* x, double* y);

@@ -119,6 +119,14 @@ int xtt_context_profile(xtt_context* ctx, int enable) {
 	});
 }
 
+int xtt_context_set_cg_path(xtt_context* ctx, int path) {
+	return guard([&] {
+		ARG(ctx, "ctx is NULL");
+		ARG(path == XTT_CG_PATH_AUTO || path == XTT_CG_PATH_GRID, "unknown CG path");
+		ctx->c->cg_path = path;
+	});
+}
+
 int xtt_context_profile_get(xtt_context* ctx, const char* name, int64_t* launches, double* milliseconds) {
 	return guard([&] {
 		ARG(ctx && name && launches && milliseconds, "NULL argument");

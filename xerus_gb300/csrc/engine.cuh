@@ -31,6 +31,7 @@ struct Context {
 	double* d_dbl = nullptr;       // small device results (norms, dots), 64 doubles
 	double* h_dbl = nullptr;       // pinned mirror
 	long long launches = 0;
+	int cg_path = XTT_CG_PATH_AUTO;  // xtt_cg_path: which local CG kernel family runs
 	int tensors = 0;        // live tensors created on this context
 	bool closing = false;   // destroy requested; freed when the last tensor goes
 	struct Slot {

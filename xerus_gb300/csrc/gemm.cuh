@@ -155,6 +155,89 @@ __device__ T gemm_tile(const Gemm<T>& g, long long tile, GemmSmem<T>& sm) {
 	return T(0);
 }
 
+// Square TS x TS output tile (TS = 16 or 32) over the K range [kb, ke): the
+// 256 threads form a 16 x 16 grid, each accumulating (TS/16)^2 outputs into
+// acc (row-major 2x2 or 1x1). No epilogue; used by the split-K launcher,
+// whose CTAs of one cluster cover disjoint K ranges of the same tile.
+template <class T, int TS>
+struct TileSmem {
+	T As[32][TS + 1];  // [k][m]
+	T Bs[32][TS + 1];  // [k][n]
+};
+
+template <class T, int TS>
+__device__ void gemm_tile_acc(const Gemm<T>& g, long long tile, int kb, int ke, TileSmem<T, TS>& sm,
+                              T (&acc)[TS / 16][TS / 16]) {
+	constexpr int R = TS / 16;
+	const int tid = threadIdx.x;
+	const long long tn = (g.N + TS - 1) / TS, tm = (g.M + TS - 1) / TS;
+	const long long b = tile / (tm * tn);
+	const long long rem = tile - b * tm * tn;
+	const int m0 = int(rem / tn) * TS, n0 = int(rem % tn) * TS;
+	const T* A = g.A + b * g.sAb;
+	const T* B = g.B + b * g.sBb;
+	const int tx = tid & 15, ty = tid >> 4;
+#pragma unroll
+	for (int i = 0; i < R; ++i)
+#pragma unroll
+		for (int j = 0; j < R; ++j) acc[i][j] = T(0);
+	const bool a_k_fast = (g.sAk == 1);
+	const bool b_n_fast = (g.sBn == 1) || (g.sBk != 1);
+	for (int k0 = kb; k0 < ke; k0 += 32) {
+#pragma unroll
+		for (int t = 0; t < TS / 8; ++t) {
+			const int e = tid + t * kGemmThreads;  // e < 32 * TS
+			{
+				// A slab TS (m) x 32 (k): consecutive threads along k when A is k-contiguous
+				const int mm = a_k_fast ? (e >> 5) : (e % TS), kk = a_k_fast ? (e & 31) : (e / TS);
+				const int gm = m0 + mm, gk = k0 + kk;
+				sm.As[kk][mm] = (gm < g.M && gk < ke) ? A[g.offA(gm, gk)] : T(0);
+			}
+			{
+				const int nn = b_n_fast ? (e % TS) : (e >> 5), kk = b_n_fast ? (e / TS) : (e & 31);
+				const int gn = n0 + nn, gk = k0 + kk;
+				sm.Bs[kk][nn] = (gn < g.N && gk < ke) ? B[g.offB(gk, gn)] : T(0);
+			}
+		}
+		__syncthreads();
+		const int kmax = min(32, ke - k0);
+		for (int kk = 0; kk < kmax; ++kk) {
+			T av[R], bv[R];
+#pragma unroll
+			for (int i = 0; i < R; ++i) av[i] = sm.As[kk][ty + 16 * i];
+#pragma unroll
+			for (int j = 0; j < R; ++j) bv[j] = sm.Bs[kk][tx + 16 * j];
+#pragma unroll
+			for (int i = 0; i < R; ++i)
+#pragma unroll
+				for (int j = 0; j < R; ++j) acc[i][j] = fma(av[i], bv[j], acc[i][j]);
+		}
+		__syncthreads();
+	}
+}
+
+// Writes the accumulators of gemm_tile_acc through the alpha/beta epilogue.
+template <class T, int TS>
+__device__ void gemm_tile_store(const Gemm<T>& g, long long tile, const T (&acc)[TS / 16][TS / 16]) {
+	constexpr int R = TS / 16;
+	const int tid = threadIdx.x, tx = tid & 15, ty = tid >> 4;
+	const long long tn = (g.N + TS - 1) / TS, tm = (g.M + TS - 1) / TS;
+	const long long b = tile / (tm * tn);
+	const long long rem = tile - b * tm * tn;
+	const int m0 = int(rem / tn) * TS, n0 = int(rem % tn) * TS;
+	T* C = g.C + b * g.sCb;
+#pragma unroll
+	for (int i = 0; i < R; ++i)
+#pragma unroll
+		for (int j = 0; j < R; ++j) {
+			const int gm = m0 + ty + 16 * i, gn = n0 + tx + 16 * j;
+			if (gm < g.M && gn < g.N) {
+				const long long o = g.offC(gm, gn);
+				C[o] = (g.beta == T(0)) ? g.alpha * acc[i][j] : g.alpha * acc[i][j] + g.beta * C[o];
+			}
+		}
+}
+
 // Processes tiles start, start+stride, ... of g (a persistent block loop);
 // returns the epilogue partial sum of this block (thread 0).
 template <class T>

@@ -262,6 +262,23 @@ struct QcLayout {
 	__host__ __device__ size_t total() const { return perm() + size_t(nw + 1) / 2 + 1; }
 };
 
+// Sum over the cluster's CTAs, in rank order, of local[idx] in each CTA's shared
+// memory. All remote loads are issued before the first add (one round trip
+// instead of P); ranks >= P read rank 0 and contribute an exact zero.
+__device__ __forceinline__ double cluster_sum_at(cooperative_groups::cluster_group& cl, double* local, int idx,
+                                                 int P) {
+	double v[16];
+#pragma unroll
+	for (int p = 0; p < 16; ++p) {
+		const double t = cl.map_shared_rank(local, p < P ? p : 0)[idx];
+		v[p] = p < P ? t : 0.0;
+	}
+	double s = 0;
+#pragma unroll
+	for (int p = 0; p < 16; ++p) s += v[p];
+	return s;
+}
+
 __global__ void __launch_bounds__(kQcThreads) k_qr_cluster(QrArgs a, QcLayout lay) {
 	namespace cg = cooperative_groups;
 	cg::cluster_group cl = cg::this_cluster();
@@ -312,11 +329,7 @@ __global__ void __launch_bounds__(kQcThreads) k_qr_cluster(QrArgs a, QcLayout la
 	if (a.pivot) {
 		colsum(0, 0, nrm, [&](int il, int c) { return w(il, c) * w(il, c); });
 		cl.sync();
-		for (int c = tid; c < nw; c += blockDim.x) {
-			double s = 0;
-			for (int p = 0; p < P; ++p) s += cl.map_shared_rank(nrm, p)[c];
-			cn2[c] = s;
-		}
+		for (int c = tid; c < nw; c += blockDim.x) cn2[c] = cluster_sum_at(cl, nrm, c, P);
 		__syncthreads();
 	}
 	for (int j = 0; j < kq; ++j) {
@@ -371,13 +384,10 @@ __global__ void __launch_bounds__(kQcThreads) k_qr_cluster(QrArgs a, QcLayout la
 			}
 		}
 		cl.sync();
+		if (tid < 2) s_coef[tid] = cluster_sum_at(cl, sclp, tid, P);
+		__syncthreads();
 		if (tid == 0) {
-			double xn2 = 0, alpha = 0;
-			for (int p = 0; p < P; ++p) {
-				const double* rs = cl.map_shared_rank(sclp, p);
-				xn2 += rs[0];
-				alpha += rs[1];
-			}
+			const double xn2 = s_coef[0], alpha = s_coef[1];
 			double t = 0, scal = 1.0, beta = alpha;
 			if (xn2 != 0.0) {
 				beta = -copysign(sqrt(alpha * alpha + xn2), alpha);
@@ -400,12 +410,7 @@ __global__ void __launch_bounds__(kQcThreads) k_qr_cluster(QrArgs a, QcLayout la
 		cl.sync();
 		for (int cb = j + 1; cb < nw; cb += 32) {
 			const int c = cb + tx;
-			if (ty == 0) {
-				double s = 0;
-				if (c < nw)
-					for (int p = 0; p < P; ++p) s += cl.map_shared_rank(vecp, p)[c];
-				s_w[tx] = tj * s;
-			}
+			if (ty == 0) s_w[tx] = c < nw ? tj * cluster_sum_at(cl, vecp, c, P) : 0.0;
 			__syncthreads();
 			double nr = 0;
 			if (c < nw) {
@@ -430,11 +435,7 @@ __global__ void __launch_bounds__(kQcThreads) k_qr_cluster(QrArgs a, QcLayout la
 		}
 		if (a.pivot) {
 			cl.sync();
-			for (int c = j + 1 + tid; c < nw; c += blockDim.x) {
-				double s = 0;
-				for (int p = 0; p < P; ++p) s += cl.map_shared_rank(nrmp, p)[c];
-				cn2[c] = s;
-			}
+			for (int c = j + 1 + tid; c < nw; c += blockDim.x) cn2[c] = cluster_sum_at(cl, nrmp, c, P);
 			__syncthreads();
 		}
 	}
@@ -442,14 +443,17 @@ __global__ void __launch_bounds__(kQcThreads) k_qr_cluster(QrArgs a, QcLayout la
 	for (int il = tid; il < nl; il += blockDim.x) dg[il] = (r0 + il < kq) ? w(il, r0 + il) : 0.0;
 	cl.sync();
 	__shared__ int s_rank;
+	// the whole diagonal, gathered in parallel into this CTA's (now unused) column-norm buffer
+	double* diag = nrm;
+	if (a.pivot)
+		for (int k = tid; k < kq; k += blockDim.x) diag[k] = cl.map_shared_rank(dg, k / mb)[k - (k / mb) * mb];
+	__syncthreads();
 	if (tid == 0) {
 		int rank = kq;
 		if (a.pivot) {
-			const double r00 = cl.map_shared_rank(dg, 0)[0];
-			for (int k = 1; k < kq; ++k) {
-				const int p = k / mb;
-				if (fabs(cl.map_shared_rank(dg, p)[k - p * mb]) < 16.0 * DBL_EPSILON * r00) { rank = k; break; }
-			}
+			const double r00 = diag[0];
+			for (int k = 1; k < kq; ++k)
+				if (fabs(diag[k]) < 16.0 * DBL_EPSILON * r00) { rank = k; break; }
 		}
 		s_rank = rank;
 		if (me == 0 && a.rank_out) *a.rank_out = rank;
@@ -492,12 +496,7 @@ __global__ void __launch_bounds__(kQcThreads) k_qr_cluster(QrArgs a, QcLayout la
 			cl.sync();
 			for (int cb = j + 1; cb < rank; cb += 32) {
 				const int c = cb + tx;
-				if (ty == 0) {
-					double s = 0;
-					if (c < rank)
-						for (int p = 0; p < P; ++p) s += cl.map_shared_rank(vecp, p)[c];
-					s_w[tx] = tj * s;
-				}
+				if (ty == 0) s_w[tx] = c < rank ? tj * cluster_sum_at(cl, vecp, c, P) : 0.0;
 				__syncthreads();
 				if (c < rank) {
 					const double wc = s_w[tx];

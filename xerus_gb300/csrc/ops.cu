@@ -5,6 +5,8 @@
 #include <cmath>
 #include <cstring>
 
+#include <cooperative_groups.h>
+
 #include "engine.cuh"
 
 namespace xtt {
@@ -199,14 +201,94 @@ void check_gemm(const Gemm<T>& g) {
 template void check_gemm<double>(const Gemm<double>&);
 template void check_gemm<float>(const Gemm<float>&);
 
+// Split-K tile GEMM: the S CTAs of one cluster (S = cluster size) compute the
+// same TS x TS output tile over disjoint K ranges; their partial sums meet in
+// the rank-0 CTA through distributed shared memory, added in rank order
+// (deterministic), and rank 0 runs the epilogue. S = 1 is a plain tile GEMM.
+template <class T, int TS>
+__global__ void __launch_bounds__(kGemmThreads) k_gemm_sk(Gemm<T> g, int S, int kchunk) {
+	constexpr int R = TS / 16;
+	__shared__ TileSmem<T, TS> sm;
+	__shared__ T part[R * R][kGemmThreads];
+	const long long tile = blockIdx.x / S;
+	const int ks = blockIdx.x % S;
+	const int kb = ks * kchunk, ke = min(g.K, kb + kchunk);
+	T acc[R][R];
+	gemm_tile_acc<T, TS>(g, tile, kb, ke, sm, acc);
+	if (S == 1) {
+		gemm_tile_store<T, TS>(g, tile, acc);
+		return;
+	}
+	namespace cgn = cooperative_groups;
+	cgn::cluster_group cl = cgn::this_cluster();
+#pragma unroll
+	for (int i = 0; i < R; ++i)
+#pragma unroll
+		for (int j = 0; j < R; ++j) part[i * R + j][threadIdx.x] = acc[i][j];
+	cl.sync();
+	if (cl.block_rank() == 0) {
+#pragma unroll
+		for (int i = 0; i < R; ++i)
+#pragma unroll
+			for (int j = 0; j < R; ++j) {
+				T v[8];
+#pragma unroll
+				for (int p = 0; p < 8; ++p) {
+					const T t = cl.map_shared_rank(&part[i * R + j][threadIdx.x], p < S ? p : 0)[0];
+					v[p] = p < S ? t : T(0);
+				}
+				T s = T(0);
+#pragma unroll
+				for (int p = 0; p < 8; ++p) s += v[p];
+				acc[i][j] = s;
+			}
+		gemm_tile_store<T, TS>(g, tile, acc);
+	}
+	cl.sync();  // the partials stay readable until rank 0 has summed them
+}
+
+// Launch shape: 32 x 32 tiles when they already cover the SMs, else 16 x 16
+// tiles and up to 8-way split K so that FP64 work spreads over the GPU (GB300
+// retires about two FP64 FMAs per SM and clock, so one tile on one SM is slow).
+template <class T>
+static void launch_gemm_sk(Context& c, const Gemm<T>& g) {
+	const long long t32 = g.tiles();
+	XTT_REQUIRE(t32 < (1ll << 26), "GEMM too large");
+	const long long target = 2ll * c.num_sms;
+	if (t32 >= target || g.K <= 16) {
+		k_gemm_sk<T, 32><<<unsigned(t32), kGemmThreads, 0, c.stream>>>(g, 1, std::max(g.K, 1));
+		XTT_CUDA(cudaGetLastError());
+		return;
+	}
+	const long long t16 = (long long)g.batch * ((g.M + 15) / 16) * ((g.N + 15) / 16);
+	int S = int(std::min<long long>(8, std::max<long long>(1, (target + t16 - 1) / t16)));
+	S = std::min(S, std::max(1, g.K / 16));  // at least 16 K per CTA
+	const int kchunk = (g.K + S - 1) / S;
+	S = (g.K + kchunk - 1) / kchunk;
+	if (S == 1) {
+		k_gemm_sk<T, 16><<<unsigned(t16), kGemmThreads, 0, c.stream>>>(g, 1, g.K);
+		XTT_CUDA(cudaGetLastError());
+		return;
+	}
+	cudaLaunchConfig_t cfg = {};
+	cfg.gridDim = dim3(unsigned(t16 * S));
+	cfg.blockDim = dim3(kGemmThreads);
+	cfg.stream = c.stream;
+	cudaLaunchAttribute at[1];
+	at[0].id = cudaLaunchAttributeClusterDimension;
+	at[0].val.clusterDim.x = S;
+	at[0].val.clusterDim.y = 1;
+	at[0].val.clusterDim.z = 1;
+	cfg.attrs = at;
+	cfg.numAttrs = 1;
+	XTT_CUDA(cudaLaunchKernelEx(&cfg, k_gemm_sk<T, 16>, g, S, kchunk));
+}
+
 void gemm(Context& c, const Gemm<double>& g) {
 	if (g.M <= 0 || g.N <= 0 || g.batch <= 0) return;
 	check_gemm(g);
-	const long long t = g.tiles();
-	XTT_REQUIRE(t < (1ll << 31), "GEMM too large");
 	ProfScope ps(c, "gemm");
-	k_gemm<double><<<unsigned(t), kGemmThreads, 0, c.stream>>>(g);
-	XTT_CUDA(cudaGetLastError());
+	launch_gemm_sk(c, g);
 	c.count_launch();
 }
 
