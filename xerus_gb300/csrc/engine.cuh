@@ -23,6 +23,8 @@ struct Context {
 	int device = 0;
 	cudaStream_t own = nullptr;
 	cudaStream_t stream = nullptr;
+	cudaStream_t aux = nullptr;              // second stream for work that runs beside `stream`
+	cudaEvent_t ev_fork = nullptr, ev_join = nullptr;
 	int num_sms = 0;
 	int* d_status = nullptr;       // DeviceStatus word
 	unsigned* d_barrier = nullptr; // grid barrier count/phase
@@ -49,6 +51,9 @@ struct Context {
 	}
 	void* scratch_bytes(int id, size_t bytes);
 	void sync();                      // stream sync + device status check
+	// aux waits for everything issued so far on stream / stream waits for aux
+	void fork();
+	void join();
 	void check_status();              // reads d_status (after a sync) and throws on failure
 	int read_int(int idx);            // sync + d_ints[idx]
 	void count_launch(int n = 1) { launches += n; }
@@ -78,11 +83,20 @@ struct ProfScope {
 	~ProfScope();
 };
 
+// Issues the launches of its scope on the context's aux stream.
+struct OnAux {
+	Context& c;
+	cudaStream_t saved;
+	explicit OnAux(Context& cc) : c(cc), saved(cc.stream) { c.stream = c.aux; }
+	~OnAux() { c.stream = saved; }
+};
+
 // Scratch slot ids (one per purpose, so nested operations never share a buffer).
 enum ScratchId : int {
 	S_QR_Q = 0, S_QR_C, S_QR_WORK, S_GEMM_A, S_GEMM_B, S_SVD_U, S_SVD_S, S_SVD_VT, S_SVD_WORK,
 	S_ROUND_X, S_ROUND_QA, S_ROUND_QB, S_ROUND_CA, S_ROUND_CB, S_ZIP_M, S_ZIP_T, S_ZIP_M2,
 	S_RES_CORE0, S_RES_CORE1, S_RES_R, S_RED, S_ENT_META, S_ENT_CORES, S_ENT_OUT,
+	S_RES_CORE0B, S_RES_CORE1B, S_RES_RB, S_QR_WORKB,
 	S_ALS_FIRST = 32,
 	S_ADF_FIRST = 96,
 	S_MAX = 160

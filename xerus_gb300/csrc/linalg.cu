@@ -523,9 +523,276 @@ __global__ void __launch_bounds__(kQcThreads) k_qr_cluster(QrArgs a, QcLayout la
 	cl.sync();  // no CTA leaves while others may still read its shared memory
 }
 
+// ----------------------------------------------------------- cluster QR, no pivoting
+//
+// The unpivoted factorisation (the residual's R-only sweeps and move_core with
+// keepRank) with the same row-block distribution, arranged around GB300's FP64
+// pipe, which takes ~64 cycles per warp instruction: no FP64 reduction runs as
+// a long dependent chain. Per column j, two cluster barriers: (1) the partial
+// norms of column j below the diagonal (computed during the previous column's
+// update) and the diagonal entry meet in a 16-lane shuffle tree; (2) the
+// partials w_c = v^T A[:, c] of each CTA's rows meet in per-column 8+8 trees.
+// Inside a CTA each thread owns one column of one row group; row groups are
+// combined in fixed order. Every CTA computes bit-identical reflectors.
+
+constexpr int kQ2Threads = 256;
+
+struct Qc2Layout {
+	int mb, nw, kq, ldw;
+	__host__ __device__ size_t vecw() const { return size_t(mb) * ldw; }
+	__host__ __device__ size_t slot() const { return vecw() + 2 * size_t(nw); }
+	__host__ __device__ size_t tau() const { return slot() + 4; }
+	__host__ __device__ size_t sw() const { return tau() + kq; }
+	__host__ __device__ size_t part() const { return sw() + nw; }
+	__host__ __device__ size_t partn() const { return part() + 8 * 256; }
+	__host__ __device__ size_t coef() const { return partn() + 8; }
+	__host__ __device__ size_t total() const { return coef() + 4; }
+};
+
+// Column-chunk geometry of the thread-per-(column, row group) mapping.
+struct ColMap {
+	int Cc, ncw, G;
+	__device__ ColMap(int C, int cb) {
+		Cc = min(256, C - cb);
+		ncw = (Cc + 31) >> 5;
+		G = ncw > 0 ? max(1, 8 / ncw) : 1;
+	}
+};
+
+__global__ void __launch_bounds__(kQ2Threads) k_qr_cl2(QrArgs a, Qc2Layout lay) {
+	namespace cg = cooperative_groups;
+	cg::cluster_group cl = cg::this_cluster();
+	const int P = int(cl.num_blocks()), me = int(cl.block_rank());
+	const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+	const int mw = a.transpose ? a.n : a.m, nw = lay.nw, kq = lay.kq, mb = lay.mb, ldw = lay.ldw;
+	const int r0 = me * mb, r1 = min(mw, r0 + mb), nl = max(0, r1 - r0);
+	extern __shared__ double sm[];
+	double* W = sm;
+	double* vecw = sm + lay.vecw();
+	double* slot = sm + lay.slot();
+	double* tau = sm + lay.tau();
+	double* sw = sm + lay.sw();
+	double* part = sm + lay.part();
+	double* partn = sm + lay.partn();
+	double* coef = sm + lay.coef();
+	auto w = [&](int il, int c) -> double& { return W[(long long)il * ldw + c]; };
+	auto lo_of = [&](int g) { return min(max(g - r0, 0), nl); };
+
+	for (long long e = tid; e < (long long)nl * nw; e += kQ2Threads) {
+		const int il = int(e / nw), c = int(e % nw), gi = r0 + il;
+		w(il, c) = a.transpose ? a.A[(long long)c * a.lda + gi] : a.A[(long long)gi * a.lda + c];
+	}
+	__syncthreads();
+	if (warp == 0) {
+		double s = 0;
+		for (int il = lo_of(1) + lane; il < nl; il += 32) s = fma(w(il, 0), w(il, 0), s);
+#pragma unroll
+		for (int o = 16; o > 0; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
+		if (lane == 0) coef[3] = s;
+	}
+	__syncthreads();
+	for (int j = 0; j < kq; ++j) {
+		const int par = j & 1;
+		double* vp = vecw + par * nw;
+		double* sl = slot + par * 2;
+		if (tid == 0) {
+			sl[0] = coef[3];
+			sl[1] = (j >= r0 && j < r1) ? w(j - r0, j) : 0.0;
+		}
+		cl.sync();
+		if (warp == 0) {
+			const int src = lane & 15, which = lane >> 4;
+			const double t = cl.map_shared_rank(sl, src < P ? src : 0)[which];
+			double v = src < P ? t : 0.0;
+#pragma unroll
+			for (int o = 8; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+			const double alpha = __shfl_sync(0xffffffffu, v, 16);
+			if (lane == 0) {
+				const double xn2 = v;
+				double tt = 0, scal = 1.0, beta = alpha;
+				if (xn2 != 0.0) {
+					beta = -copysign(sqrt(alpha * alpha + xn2), alpha);
+					tt = (beta - alpha) / beta;
+					scal = 1.0 / (alpha - beta);
+				}
+				tau[j] = tt;
+				coef[0] = scal;
+				coef[1] = beta;
+				coef[2] = tt;
+			}
+		}
+		__syncthreads();
+		const double scal = coef[0], tj = coef[2];
+		for (int il = lo_of(j + 1) + tid; il < nl; il += kQ2Threads) w(il, j) *= scal;
+		if (tid == 0 && j >= r0 && j < r1) w(j - r0, j) = coef[1];
+		__syncthreads();
+		const int c0 = j + 1, C = nw - c0, lo = lo_of(j), nrows = nl - lo;
+		// partial w_c over this CTA's rows >= j
+		for (int cb = 0; cb < C; cb += 256) {
+			const ColMap cm(C, cb);
+			const int g = warp / cm.ncw, ci = (warp % cm.ncw) * 32 + lane, chunk = (nrows + cm.G - 1) / cm.G;
+			if (g < cm.G && ci < cm.Cc) {
+				const int c = c0 + cb + ci, ia = lo + g * chunk, ib = min(nl, ia + chunk);
+				double acc = 0;
+				for (int il = ia; il < ib; ++il) acc = fma((r0 + il == j) ? 1.0 : w(il, j), w(il, c), acc);
+				part[g * 256 + ci] = acc;
+			}
+			__syncthreads();
+			if (tid < cm.Cc) {
+				double s = 0;
+				for (int gg = 0; gg < cm.G; ++gg) s += part[gg * 256 + tid];
+				vp[c0 + cb + tid] = s;
+			}
+			__syncthreads();
+		}
+		cl.sync();
+		// totals over the cluster: two threads per column, 8 ranks each, then one shuffle
+		for (int cb = 0; cb < C; cb += 128) {
+			const int Cc = min(128, C - cb), ci = tid >> 1, h = tid & 1;
+			double s = 0;
+			if (ci < Cc) {
+				const int c = c0 + cb + ci;
+				double v[8];
+#pragma unroll
+				for (int q = 0; q < 8; ++q) {
+					const int p = 8 * h + q;
+					const double t = cl.map_shared_rank(vp, p < P ? p : 0)[c];
+					v[q] = p < P ? t : 0.0;
+				}
+				s = ((v[0] + v[1]) + (v[2] + v[3])) + ((v[4] + v[5]) + (v[6] + v[7]));
+			}
+			s += __shfl_xor_sync(0xffffffffu, s, 1);
+			if (ci < Cc && h == 0) sw[c0 + cb + ci] = tj * s;
+		}
+		__syncthreads();
+		// update, and the partial norm of column j+1 below its diagonal
+		int G0 = 1;
+		for (int cb = 0; cb < C; cb += 256) {
+			const ColMap cm(C, cb);
+			if (cb == 0) G0 = cm.G;
+			const int g = warp / cm.ncw, ci = (warp % cm.ncw) * 32 + lane, chunk = (nrows + cm.G - 1) / cm.G;
+			if (g < cm.G && ci < cm.Cc) {
+				const int c = c0 + cb + ci, ia = lo + g * chunk, ib = min(nl, ia + chunk);
+				const double wc = sw[c];
+				double ns = 0;
+				for (int il = ia; il < ib; ++il) {
+					const double u = fma(-wc, (r0 + il == j) ? 1.0 : w(il, j), w(il, c));
+					w(il, c) = u;
+					if (r0 + il > j + 1) ns = fma(u, u, ns);
+				}
+				if (c == j + 1) partn[g] = ns;
+			}
+		}
+		__syncthreads();
+		if (tid == 0) {
+			double s = 0;
+			if (C > 0)
+				for (int gg = 0; gg < G0; ++gg) s += partn[gg];
+			coef[3] = s;
+		}
+		__syncthreads();
+	}
+	const int rank = kq;
+	if (me == 0 && tid == 0 && a.rank_out) *a.rank_out = rank;
+	for (long long e = tid; e < (long long)nl * nw; e += kQ2Threads) {
+		const int il = int(e / nw), c = int(e % nw), r = r0 + il;
+		if (r >= rank) continue;
+		const double v = (r <= c) ? w(il, c) : 0.0;
+		if (!a.transpose) a.C[(long long)r * nw + c] = v;
+		else a.C[(long long)c * rank + r] = v;
+	}
+	if (!a.want_q) {
+		cl.sync();  // every CTA's shared memory stays alive until all remote reads are done
+		return;
+	}
+	__syncthreads();
+	// Q in place, backward accumulation of the reflectors (dorg2r)
+	for (int j = rank - 1; j >= 0; --j) {
+		const int par = j & 1;
+		double* vp = vecw + par * nw;
+		const double tj = tau[j];
+		const int c0 = j + 1, C = rank - c0, lo = lo_of(j + 1), nrows = nl - lo;
+		if (C > 0) {
+			for (int cb = 0; cb < C; cb += 256) {
+				const ColMap cm(C, cb);
+				const int g = warp / cm.ncw, ci = (warp % cm.ncw) * 32 + lane, chunk = (nrows + cm.G - 1) / cm.G;
+				if (g < cm.G && ci < cm.Cc) {
+					const int c = c0 + cb + ci, ia = lo + g * chunk, ib = min(nl, ia + chunk);
+					double acc = 0;
+					for (int il = ia; il < ib; ++il) acc = fma(w(il, j), w(il, c), acc);
+					part[g * 256 + ci] = acc;
+				}
+				__syncthreads();
+				if (tid < cm.Cc) {
+					double s = 0;
+					for (int gg = 0; gg < cm.G; ++gg) s += part[gg * 256 + tid];
+					vp[c0 + cb + tid] = s;
+				}
+				__syncthreads();
+			}
+			cl.sync();
+			for (int cb = 0; cb < C; cb += 128) {
+				const int Cc = min(128, C - cb), ci = tid >> 1, h = tid & 1;
+				double s = 0;
+				if (ci < Cc) {
+					const int c = c0 + cb + ci;
+					double v[8];
+#pragma unroll
+					for (int q = 0; q < 8; ++q) {
+						const int p = 8 * h + q;
+						const double t = cl.map_shared_rank(vp, p < P ? p : 0)[c];
+						v[q] = p < P ? t : 0.0;
+					}
+					s = ((v[0] + v[1]) + (v[2] + v[3])) + ((v[4] + v[5]) + (v[6] + v[7]));
+				}
+				s += __shfl_xor_sync(0xffffffffu, s, 1);
+				if (ci < Cc && h == 0) sw[c0 + cb + ci] = tj * s;
+			}
+			__syncthreads();
+			for (int cb = 0; cb < C; cb += 256) {
+				const ColMap cm(C, cb);
+				const int g = warp / cm.ncw, ci = (warp % cm.ncw) * 32 + lane, chunk = (nrows + cm.G - 1) / cm.G;
+				if (g < cm.G && ci < cm.Cc) {
+					const int c = c0 + cb + ci, ia = lo + g * chunk, ib = min(nl, ia + chunk);
+					const double wc = sw[c];
+					for (int il = ia; il < ib; ++il) w(il, c) = fma(-wc, w(il, j), w(il, c));
+					if (g == 0 && j >= r0 && j < r1) w(j - r0, c) = -wc;
+				}
+			}
+			__syncthreads();
+		}
+		for (int il = tid; il < nl; il += kQ2Threads) {
+			const int gi = r0 + il;
+			if (gi > j) w(il, j) *= -tj;
+			else if (gi == j) w(il, j) = 1.0 - tj;
+			else w(il, j) = 0.0;
+		}
+		__syncthreads();
+	}
+	for (long long e = tid; e < (long long)nl * rank; e += kQ2Threads) {
+		const int il = int(e / rank), c = int(e % rank), gi = r0 + il;
+		const double v = w(il, c);
+		if (!a.transpose) a.Q[(long long)gi * rank + c] = v;
+		else a.Q[(long long)c * mw + gi] = v;
+	}
+	cl.sync();
+}
+
+static int qr_cl2_size(int mw, int nw, Qc2Layout& lay) {
+	if (mw < 48 || nw < 8) return 0;
+	int P = std::min(16, (mw + 15) / 16);
+	lay.mb = (mw + P - 1) / P;
+	P = (mw + lay.mb - 1) / lay.mb;
+	lay.nw = nw;
+	lay.kq = std::min(mw, nw);
+	lay.ldw = nw | 1;
+	if (lay.total() * sizeof(double) > kDynSmemMax) return 0;
+	return P;
+}
+
 // Cluster geometry for an mw x nw factorisation: 0 CTAs if the one-CTA kernel is used.
 static int qr_cluster_size(int mw, int nw, QcLayout& lay) {
-	if (mw < 96 || nw < 8) return 0;
+	if (mw < 48 || nw < 8) return 0;
 	int P = std::min(16, (mw + 15) / 16);
 	lay.mb = (mw + P - 1) / P;
 	P = (mw + lay.mb - 1) / lay.mb;
@@ -537,6 +804,36 @@ static int qr_cluster_size(int mw, int nw, QcLayout& lay) {
 
 void launch_qr(const QrArgs& a, cudaStream_t s) {
 	const int mw = a.transpose ? a.n : a.m, nw = a.transpose ? a.m : a.n;
+	if (!a.pivot) {
+		Qc2Layout l2;
+		const int P2 = qr_cl2_size(mw, nw, l2);
+		if (P2 > 1) {
+			static bool attr2 = false;
+			if (!attr2) {
+				XTT_CUDA(cudaFuncSetAttribute(k_qr_cl2, cudaFuncAttributeMaxDynamicSharedMemorySize, int(kDynSmemMax)));
+				XTT_CUDA(cudaFuncSetAttribute(k_qr_cl2, cudaFuncAttributeNonPortableClusterSizeAllowed, 1));
+				attr2 = true;
+			}
+			cudaLaunchConfig_t cfg = {};
+			cfg.gridDim = dim3(P2);
+			cfg.blockDim = dim3(kQ2Threads);
+			cfg.dynamicSmemBytes = l2.total() * sizeof(double);
+			cfg.stream = s;
+			cudaLaunchAttribute at[1];
+			at[0].id = cudaLaunchAttributeClusterDimension;
+			at[0].val.clusterDim.x = P2;
+			at[0].val.clusterDim.y = 1;
+			at[0].val.clusterDim.z = 1;
+			cfg.attrs = at;
+			cfg.numAttrs = 1;
+			int clusters = 0;
+			if (cudaOccupancyMaxActiveClusters(&clusters, k_qr_cl2, &cfg) == cudaSuccess && clusters > 0) {
+				XTT_CUDA(cudaLaunchKernelEx(&cfg, k_qr_cl2, a, l2));
+				return;
+			}
+			cudaGetLastError();
+		}
+	}
 	QcLayout lay;
 	const int P = qr_cluster_size(mw, nw, lay);
 	if (P > 1) {

@@ -17,6 +17,9 @@ Context::Context(int dev) : device(dev) {
 	XTT_CUDA(cudaSetDevice(dev));
 	XTT_CUDA(cudaStreamCreateWithFlags(&own, cudaStreamNonBlocking));
 	stream = own;
+	XTT_CUDA(cudaStreamCreateWithFlags(&aux, cudaStreamNonBlocking));
+	XTT_CUDA(cudaEventCreateWithFlags(&ev_fork, cudaEventDisableTiming));
+	XTT_CUDA(cudaEventCreateWithFlags(&ev_join, cudaEventDisableTiming));
 	XTT_CUDA(cudaDeviceGetAttribute(&num_sms, cudaDevAttrMultiProcessorCount, dev));
 	XTT_CUDA(cudaMalloc(&d_status, sizeof(int)));
 	XTT_CUDA(cudaMalloc(&d_barrier, 2 * sizeof(unsigned)));
@@ -32,6 +35,7 @@ Context::Context(int dev) : device(dev) {
 Context::~Context() {
 	cudaSetDevice(device);
 	cudaStreamSynchronize(stream);
+	cudaStreamSynchronize(aux);
 	for (auto& s : slots)
 		if (s.p) cudaFree(s.p);
 	cudaFree(d_status);
@@ -40,7 +44,20 @@ Context::~Context() {
 	cudaFree(d_dbl);
 	cudaFreeHost(h_ints);
 	cudaFreeHost(h_dbl);
+	cudaEventDestroy(ev_fork);
+	cudaEventDestroy(ev_join);
+	cudaStreamDestroy(aux);
 	cudaStreamDestroy(own);
+}
+
+void Context::fork() {
+	XTT_CUDA(cudaEventRecord(ev_fork, stream));
+	XTT_CUDA(cudaStreamWaitEvent(aux, ev_fork, 0));
+}
+
+void Context::join() {
+	XTT_CUDA(cudaEventRecord(ev_join, aux));
+	XTT_CUDA(cudaStreamWaitEvent(stream, ev_join, 0));
 }
 
 void* Context::scratch_bytes(int id, size_t bytes) {
@@ -49,7 +66,9 @@ void* Context::scratch_bytes(int id, size_t bytes) {
 	if (s.bytes < bytes) {
 		const size_t nb = std::max(bytes, s.bytes * 3 / 2) + 256;
 		if (s.p) {
-			XTT_CUDA(cudaStreamSynchronize(stream));
+			XTT_CUDA(cudaStreamSynchronize(own));  // either stream may still use the old buffer
+			XTT_CUDA(cudaStreamSynchronize(aux));
+			if (stream != own) XTT_CUDA(cudaStreamSynchronize(stream));
 			XTT_CUDA(cudaFree(s.p));
 			s.p = nullptr;
 		}
@@ -761,10 +780,12 @@ __global__ void k_block_core(double* out, const double* p, const double* q, int 
 }
 
 double residual(const Tensor& A, const Tensor& x, const Tensor& b) {
-	// ||A x - b|| / ||b|| (src/xerus/algorithms/als.cpp:258-261) without cancellation: the block
-	// cores of y = A x - b (TT sum, src/xerus/ttNetwork.cpp:796-856) are formed one at a time and
-	// orthogonalised left to right; only the triangular factor R is carried, so neither the
-	// residual TT nor any orthogonal factor is ever stored.
+	// ||A x - b|| / ||b|| (src/xerus/algorithms/als.cpp:258-261) without cancellation. The block
+	// cores Y_k of y = A x - b (TT sum, src/xerus/ttNetwork.cpp:796-856) are formed one at a time
+	// and orthogonalised from both ends at once: cores 0..mid-1 left to right on the context's
+	// stream (Householder QR, only the triangular factor R is carried), cores d-1..mid+1 right to
+	// left on the aux stream (LQ, only the factor L is carried). The two halves meet at core mid:
+	// ||y|| = ||R Y_mid L||. Neither the residual TT nor any orthogonal factor is stored.
 	XTT_REQUIRE(x.dims == b.dims && A.dims == x.dims && A.op && !x.op && !b.op, "x and b dimensions differ");
 	Context& c = *x.ctx;
 	const int d = x.d;
@@ -775,51 +796,107 @@ double residual(const Tensor& A, const Tensor& x, const Tensor& b) {
 		cap_core = std::max(cap_core, p0 * size_t(x.dims[k]) * p1);
 		cap_r = std::max({cap_r, p0 * p1, p0 * p0, p1 * p1});
 	}
-	double* ax = c.scratch<double>(S_RES_CORE0, cap_core);
-	double* Y = c.scratch<double>(S_RES_CORE1, cap_core);
-	double* Z = c.scratch<double>(S_RES_R, cap_core + cap_r);
-	double* R = Z + cap_core;
-	fill(c, R, 1.0, 1);
-	int64_t rr = 1;
-	for (int k = 0; k < d; ++k) {
+	struct Bufs {
+		double *ax, *Y, *Z, *R;
+	};
+	auto bufs = [&](int i0, int i1, int i2) {
+		Bufs f;
+		f.ax = c.scratch<double>(i0, cap_core);
+		f.Y = c.scratch<double>(i1, cap_core);
+		f.Z = c.scratch<double>(i2, 2 * cap_core + cap_r);
+		f.R = f.Z + 2 * cap_core;
+		return f;
+	};
+	const Bufs lb = bufs(S_RES_CORE0, S_RES_CORE1, S_RES_R), rb_ = bufs(S_RES_CORE0B, S_RES_CORE1B, S_RES_RB);
+	struct Dims {
+		int n, O0, O1;
+	};
+	// block core k of A x - b into f.Y on the current stream
+	auto block = [&](int k, const Bufs& f) {
 		const int K = int(A.ranks[k]), L = int(A.ranks[k + 1]), ra = int(x.ranks[k]), rb = int(x.ranks[k + 1]);
 		const int n = int(x.dims[k]);
 		const int P0 = K * ra, P1 = L * rb, Q0 = int(b.ranks[k]), Q1 = int(b.ranks[k + 1]);
 		const int first = k == 0, last = k == d - 1;
 		const int O0 = first ? 1 : P0 + Q0, O1 = last ? 1 : P1 + Q1;
 		const size_t nax = size_t(P0) * n * P1, ny = size_t(O0) * n * O1;
-		k_op_apply<<<grid_for(nax), 256, 0, c.stream>>>(ax, A.core[k], x.core[k], K, L, n, ra, rb);
-		k_block_core<<<grid_for(ny), 256, 0, c.stream>>>(Y, ax, b.core[k], P0, P1, Q0, Q1, n, first, last);
+		k_op_apply<<<grid_for(nax), 256, 0, c.stream>>>(f.ax, A.core[k], x.core[k], K, L, n, ra, rb);
+		k_block_core<<<grid_for(ny), 256, 0, c.stream>>>(f.Y, f.ax, b.core[k], P0, P1, Q0, Q1, n, first, last);
 		c.count_launch(2);
 		XTT_CUDA(cudaGetLastError());
-		Gemm<double> g;  // Z = R (rr x O0) * Y (O0 x n O1)
-		g.M = int(rr); g.N = int(n * O1); g.K = O0;
-		g.A = R; g.sAm = O0; g.sAk = 1;
-		g.B = Y; g.sBk = n * O1; g.sBn = 1;
-		g.C = Z; g.sCm = n * O1; g.sCn = 1;
-		g.lens((long long)cap_r, (long long)ny, (long long)cap_core);
-		gemm(c, g);
-		const size_t nz = size_t(rr) * n * O1;
-		if (last) {
-			sumsq_async(c, Z, nz, 0);
-			return std::sqrt(read_dbl(c, 0)) / nb;
-		}
-		// R <- triangular factor of Z viewed as (rr n) x O1 (Householder, R only)
-		const int m = int(rr * n), kq = std::min(m, O1);
+		return Dims{n, O0, O1};
+	};
+	auto qr_r_only = [&](double* Zp, int m, int ncol, int transpose, double* out) {
 		QrArgs a;
-		const size_t wk = qr_work_doubles(m, O1);
-		a.A = Z; a.lda = O1; a.m = m; a.n = O1; a.transpose = 0; a.pivot = 0; a.want_q = 0;
-		a.work = wk ? c.scratch<double>(S_QR_WORK, wk) : nullptr;
-		a.Q = nullptr; a.C = R; a.rank_out = nullptr;
-		XTT_REQUIRE(size_t(kq) * O1 <= cap_r, "internal: residual carry too small");
-		{
-			ProfScope ps(c, "qr");
-			launch_qr(a, c.stream);
-		}
+		const int mw = transpose ? ncol : m, nw = transpose ? m : ncol;
+		const size_t wk = qr_work_doubles(mw, nw);
+		a.A = Zp; a.lda = ncol; a.m = m; a.n = ncol; a.transpose = transpose; a.pivot = 0; a.want_q = 0;
+		a.work = wk ? c.scratch<double>(c.stream == c.aux ? S_QR_WORKB : S_QR_WORK, wk) : nullptr;
+		a.Q = nullptr; a.C = out; a.rank_out = nullptr;
+		ProfScope ps(c, "qr");
+		launch_qr(a, c.stream);
 		c.count_launch();
+	};
+	const int mid = d / 2;
+	// right half on the aux stream: carry L (O1_k x rl), starting from [1]
+	int64_t rl = 1;
+	double* Lc = rb_.R;
+	c.fork();
+	{
+		OnAux on(c);
+		fill(c, Lc, 1.0, 1);
+		for (int k = d - 1; k > mid; --k) {
+			const Dims dm = block(k, rb_);
+			Gemm<double> g;  // Z = Y_k ((O0 n) x O1) * L (O1 x rl)
+			g.M = dm.O0 * dm.n; g.N = int(rl); g.K = dm.O1;
+			g.A = rb_.Y; g.sAm = dm.O1; g.sAk = 1;
+			g.B = Lc; g.sBk = rl; g.sBn = 1;
+			g.C = rb_.Z; g.sCm = rl; g.sCn = 1;
+			g.lens((long long)cap_core, (long long)cap_r, (long long)2 * cap_core);
+			gemm(c, g);
+			// L <- left factor of Z viewed as O0 x (n rl)  (LQ, L only)
+			const int ncol = int(dm.n * rl), kq = std::min(dm.O0, ncol);
+			XTT_REQUIRE(size_t(dm.O0) * kq <= cap_r, "internal: residual carry too small");
+			qr_r_only(rb_.Z, dm.O0, ncol, 1, Lc);
+			rl = kq;
+		}
+	}
+	c.join();
+	// left half on the context's stream: carry R (rr x O0_k), starting from [1]
+	int64_t rr = 1;
+	fill(c, lb.R, 1.0, 1);
+	for (int k = 0; k < mid; ++k) {
+		const Dims dm = block(k, lb);
+		Gemm<double> g;  // Z = R (rr x O0) * Y (O0 x n O1)
+		g.M = int(rr); g.N = dm.n * dm.O1; g.K = dm.O0;
+		g.A = lb.R; g.sAm = dm.O0; g.sAk = 1;
+		g.B = lb.Y; g.sBk = dm.n * dm.O1; g.sBn = 1;
+		g.C = lb.Z; g.sCm = dm.n * dm.O1; g.sCn = 1;
+		g.lens((long long)cap_r, (long long)cap_core, (long long)2 * cap_core);
+		gemm(c, g);
+		const int m = int(rr * dm.n), kq = std::min(m, dm.O1);
+		XTT_REQUIRE(size_t(kq) * dm.O1 <= cap_r, "internal: residual carry too small");
+		qr_r_only(lb.Z, m, dm.O1, 0, lb.R);
 		rr = kq;
 	}
-	return 0.0;
+	// meet at core mid: W = (R Y_mid) L, ||y|| = ||W||
+	const Dims dm = block(mid, lb);
+	Gemm<double> g1;  // Z = R (rr x O0) * Y (O0 x n O1)
+	g1.M = int(rr); g1.N = dm.n * dm.O1; g1.K = dm.O0;
+	g1.A = lb.R; g1.sAm = dm.O0; g1.sAk = 1;
+	g1.B = lb.Y; g1.sBk = dm.n * dm.O1; g1.sBn = 1;
+	g1.C = lb.Z; g1.sCm = dm.n * dm.O1; g1.sCn = 1;
+	g1.lens((long long)cap_r, (long long)cap_core, (long long)2 * cap_core);
+	gemm(c, g1);
+	Gemm<double> g2;  // W = Z ((rr n) x O1) * L (O1 x rl)
+	g2.M = int(rr * dm.n); g2.N = int(rl); g2.K = dm.O1;
+	g2.A = lb.Z; g2.sAm = dm.O1; g2.sAk = 1;
+	g2.B = Lc; g2.sBk = rl; g2.sBn = 1;
+	g2.C = lb.ax; g2.sCm = rl; g2.sCn = 1;
+	g2.lens((long long)2 * cap_core, (long long)cap_r, (long long)cap_core);
+	XTT_REQUIRE(size_t(rr) * dm.n * rl <= cap_core, "internal: residual meeting block too small");
+	gemm(c, g2);
+	sumsq_async(c, lb.ax, size_t(rr) * dm.n * rl, 0);
+	return std::sqrt(read_dbl(c, 0)) / nb;
 }
 
 // One block per sample: v <- v * x_k[:, i_k, :]
