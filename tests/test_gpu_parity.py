@@ -166,12 +166,13 @@ def test_als_spd_matches_reference(ctx, golden, tag, x0, b, hs, variant):
     assert rel_err(mine[keep], pr[keep]) < 1e-9
     # the FP64 residual of this iterate, against the oracle on the same cores; and
     # against the reference's (dense) residual of its own iterate, which differs
-    # from ours by the CG-vs-Cholesky rounding (~1e-13 in the cores)
+    # from ours by the CG-vs-Cholesky rounding (~1e-13 in the cores): at rank 32
+    # both iterates sit at the ~1e-11 noise floor of 1e-13 local solves
     r_dev = xg.residual(A, x, bb)
     r_ora = o.residual(op_of(z, "A"), host_tt(x), tt_of(z, b))
     assert abs(r_dev - r_ora) <= 1e-9 * r_ora + 1e-12
     dense = z[tag + "_dense_residual"][0]
-    assert abs(r_dev - dense) <= 1e-9 * dense + 1e-11
+    assert abs(r_dev - dense) <= 1e-9 * dense + 5e-11
 
 
 def test_als_ragged_dims(ctx, golden):
