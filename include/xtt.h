@@ -204,6 +204,31 @@ int xtt_als(const xtt_tensor* A, xtt_tensor* x, const xtt_tensor* b, const xtt_a
             xtt_als_report* report, double* residual_trace, int64_t* flag_trace, double* energy_trace,
             int64_t trace_capacity);
 
+/* Batched ALS_SPD over `count` independent instances (no reference counterpart
+ * as one call: each instance is what ALSVariant::solve does for one problem,
+ * src/xerus/algorithms/als.cpp:483-553, with sites = 1 and the exact local
+ * solver). Instances may differ in order (<= 16), mode sizes and ranks (x ranks
+ * <= 64, maximal-reduced); all tensors live on ctx. One persistent launch: each
+ * CTA sweeps one instance at a time, instances taken longest-first. The launch
+ * (descriptor upload, counter reset, kernel, result download) is captured as a
+ * CUDA graph and replayed by later calls with the same batch signature. With
+ * autotune = 1 the first call of a signature times the launch shapes
+ * (threads x CTAs per SM) on the batch itself, restoring x between trials, and
+ * caches the fastest. num_half_sweeps (or, when 0, the energy criterion) is
+ * capped at 1024 half-sweeps per instance. x[i] is updated in place (and left canonical at its
+ * start position if preserve_core_position, else where the sweep ended);
+ * energies[i] receives what ALSVariant::operator() returns for instance i. */
+typedef struct xtt_batch_report {
+	double milliseconds;   /* device time of the batched launch */
+	int32_t threads;       /* launch shape used */
+	int32_t ctas_per_sm;
+	int32_t ctas;
+	int32_t reserved;
+} xtt_batch_report;
+int xtt_als_batch(xtt_context* ctx, int64_t count, const xtt_tensor* const* A, xtt_tensor* const* x,
+                  const xtt_tensor* const* b, const xtt_als_options* opt, int autotune, double* energies,
+                  int64_t* local_iterations, xtt_batch_report* report);
+
 /* Gradient of the ALS energy J(x) = <x, A x> - 2 <x, b> with respect to every
  * core of x (no gauge condition), for symmetric A: dJ/dX_k = 2 (L_k A_k R_k x_k -
  * Lb_k b_k Rb_k) with environments built from all other cores. grad receives the

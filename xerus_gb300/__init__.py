@@ -17,7 +17,7 @@ from . import _lib as L
 
 __all__ = ["Context", "TTTensor", "TTOperator", "frob_norm", "dot", "residual", "ALSVariant", "ALS_SPD", "DMRG_SPD",
            "ASD_SPD", "ADFVariant", "ADF", "SinglePointMeasurementSet", "PerformanceData", "seed", "EPSILON",
-           "XttError", "FP64", "MIXED"]
+           "XttError", "FP64", "MIXED", "als_batch"]
 
 EPSILON = 8 * np.finfo(np.float64).eps  # include/xerus/basic.h:50
 FP64, MIXED = 0, 1
@@ -383,6 +383,29 @@ class ALSVariant:
             perfData.flags = list(flags[:n])
             perfData.energies = list(en[:rep.half_sweeps])
         return rep.energy
+
+
+def als_batch(As, xs, bs, variant=None, numHalfSweeps=8, autotune=False):
+    """Batched ALS_SPD: solves every (A_i, x_i, b_i) with one-site ALS in one
+    persistent launch (x_i updated in place). Returns (energies, local CG
+    iterations, {"milliseconds", "threads", "ctas_per_sm", "ctas"})."""
+    v = (variant or ALS_SPD).copy()
+    n = len(xs)
+    if not (len(As) == n == len(bs)) or n == 0:
+        raise ValueError("A, x and b lists must be non-empty and of equal length")
+    ctx = xs[0].ctx
+    o = v.options(numHalfSweeps, v.convergenceEpsilon, False)
+    arr = ctypes.c_void_p * n
+    pa = arr(*[t.handle for t in As])
+    px = arr(*[t.handle for t in xs])
+    pb = arr(*[t.handle for t in bs])
+    en = np.zeros(n)
+    it = np.zeros(n, dtype=np.int64)
+    rep = L.BatchReport()
+    L.check(ctx.lib.xtt_als_batch(ctx.handle, n, pa, px, pb, ctypes.byref(o), int(bool(autotune)),
+                                  en.ctypes.data_as(L.c_double_p), it.ctypes.data_as(L.c_int64_p), ctypes.byref(rep)))
+    return en, it, {"milliseconds": rep.milliseconds, "threads": rep.threads, "ctas_per_sm": rep.ctas_per_sm,
+                    "ctas": rep.ctas}
 
 
 ALS_SPD = ALSVariant(1, 0, "lapack", True)

@@ -45,6 +45,16 @@ class AlsReport(ctypes.Structure):
     ]
 
 
+class BatchReport(ctypes.Structure):
+    _fields_ = [
+        ("milliseconds", ctypes.c_double),
+        ("threads", ctypes.c_int32),
+        ("ctas_per_sm", ctypes.c_int32),
+        ("ctas", ctypes.c_int32),
+        ("reserved", ctypes.c_int32),
+    ]
+
+
 class AdfOptions(ctypes.Structure):
     _fields_ = [
         ("max_iterations", ctypes.c_int64),
@@ -65,6 +75,9 @@ _SIGNATURES = {
     "xtt_context_profile": (ctypes.c_int, [VP, ctypes.c_int]),
     "xtt_context_profile_get": (ctypes.c_int, [VP, ctypes.c_char_p, c_int64_p, c_double_p]),
     "xtt_context_set_cg_path": (ctypes.c_int, [VP, ctypes.c_int]),
+    "xtt_als_batch": (ctypes.c_int, [VP, ctypes.c_int64, ctypes.POINTER(VP), ctypes.POINTER(VP), ctypes.POINTER(VP),
+                                     ctypes.POINTER(AlsOptions), ctypes.c_int, c_double_p, c_int64_p,
+                                     ctypes.POINTER(BatchReport)]),
     "xtt_tensor_create": (ctypes.c_int, [VP, ctypes.c_int, ctypes.c_int64, c_int64_p, c_int64_p, ctypes.POINTER(VP)]),
     "xtt_tensor_destroy": (ctypes.c_int, [VP]),
     "xtt_tensor_copy": (ctypes.c_int, [VP, ctypes.POINTER(VP)]),

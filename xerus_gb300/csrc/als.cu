@@ -20,85 +20,6 @@ namespace xtt {
 
 // ------------------------------------------------------------ GEMM plans
 
-size_t matvec_tmp_elems(const LocalShape& s, int stage) {
-	const size_t ra = s.ra, rb = s.rb, n1 = s.n1, n2 = s.n2, K0 = s.K0, K1 = s.K1, K2 = s.K2;
-	if (s.sites == 1) {
-		if (stage == 0) return ra * K0 * n1 * rb;  // S1 (a, k, j, b')
-		if (stage == 1) return ra * n1 * K1 * rb;  // S2 (a, i, k', b')
-		return 1;
-	}
-	if (stage == 0) return ra * K0 * n1 * n2 * rb;  // S1 (a, k0, j1, j2, b')
-	if (stage == 1) return ra * n1 * K1 * n2 * rb;  // S2 (a, i1, k1, j2, b')
-	return ra * n1 * n2 * K2 * rb;                  // S3 (a, i1, i2, k2, b')
-}
-
-// y(a,i,b) = sum L(a,k,a') A(k,i,j,k') R(b,k',b') x(a',j,b')  (1 site), and the
-// analogous 2-site product; row index (a, i.., b), column index (a', j.., b').
-template <class T>
-MatvecPlan<T> make_matvec_plan(const LocalShape& s, const T* L, const T* A1, const T* A2, const T* R, T* t1, T* t2,
-                               T* t3) {
-	MatvecPlan<T> p;
-	p.n = s.dim();
-	const long long ra = s.ra, rb = s.rb, n1 = s.n1, n2 = s.n2, K0 = s.K0, K1 = s.K1, K2 = s.K2;
-	const long long nL = ra * K0 * ra, nA1 = K0 * n1 * n1 * K1, nA2 = K1 * n2 * n2 * K2;
-	const long long nR = rb * (s.sites == 2 ? K2 : K1) * rb, nx = p.n;
-	const long long n0 = (long long)matvec_tmp_elems(s, 0), nt1 = (long long)matvec_tmp_elems(s, 1),
-	                nt2 = (long long)matvec_tmp_elems(s, 2);
-	if (s.sites == 1) {
-		p.ns = 3;
-		Gemm<T>& g1 = p.g[0];  // S1((a,k),(j,b')) = L((a,k),a') x(a',(j,b'))
-		g1.M = int(ra * K0); g1.N = int(n1 * rb); g1.K = int(ra);
-		g1.A = L; g1.sAm = ra; g1.sAk = 1;
-		g1.sBk = n1 * rb; g1.sBn = 1;
-		g1.C = t1; g1.sCm = n1 * rb; g1.sCn = 1;
-		g1.lens(nL, nx, n0);
-		Gemm<T>& g2 = p.g[1];  // per a: S2(a,i,k',b') = sum_(k,j) S1(a,k,j,b') A(k,i,j,k')
-		g2.batch = int(ra); g2.M = int(rb); g2.N = int(n1 * K1); g2.Ni = int(K1); g2.K = int(K0 * n1); g2.Ki = int(n1);
-		g2.A = t1; g2.sAb = K0 * n1 * rb; g2.sAm = 1; g2.sAko = n1 * rb; g2.sAk = rb;
-		g2.B = A1; g2.sBko = n1 * n1 * K1; g2.sBk = K1; g2.sBno = n1 * K1; g2.sBn = 1;
-		g2.C = t2; g2.sCb = n1 * K1 * rb; g2.sCm = 1; g2.sCno = K1 * rb; g2.sCn = rb;
-		g2.lens(n0, nA1, nt1);
-		Gemm<T>& g3 = p.g[2];  // y((a,i),b) = sum_(k',b') S2((a,i),(k',b')) R(b,(k',b'))
-		g3.M = int(ra * n1); g3.N = int(rb); g3.K = int(K1 * rb);
-		g3.A = t2; g3.sAm = K1 * rb; g3.sAk = 1;
-		g3.B = R; g3.sBk = 1; g3.sBn = K1 * rb;
-		g3.sCm = rb; g3.sCn = 1;
-		g3.lens(nt1, nR, nx);
-	} else {
-		p.ns = 4;
-		Gemm<T>& g1 = p.g[0];  // S1((a,k0),(j1,j2,b'))
-		g1.M = int(ra * K0); g1.N = int(n1 * n2 * rb); g1.K = int(ra);
-		g1.A = L; g1.sAm = ra; g1.sAk = 1;
-		g1.sBk = n1 * n2 * rb; g1.sBn = 1;
-		g1.C = t1; g1.sCm = n1 * n2 * rb; g1.sCn = 1;
-		g1.lens(nL, nx, n0);
-		Gemm<T>& g2 = p.g[1];  // per a: S2(a,i1,k1,(j2,b')) = sum_(k0,j1) S1(a,k0,j1,(j2,b')) A1(k0,i1,j1,k1)
-		g2.batch = int(ra); g2.M = int(n2 * rb); g2.N = int(n1 * K1); g2.Ni = int(K1); g2.K = int(K0 * n1); g2.Ki = int(n1);
-		g2.A = t1; g2.sAb = K0 * n1 * n2 * rb; g2.sAm = 1; g2.sAko = n1 * n2 * rb; g2.sAk = n2 * rb;
-		g2.B = A1; g2.sBko = n1 * n1 * K1; g2.sBk = K1; g2.sBno = n1 * K1; g2.sBn = 1;
-		g2.C = t2; g2.sCb = n1 * K1 * n2 * rb; g2.sCm = 1; g2.sCno = K1 * n2 * rb; g2.sCn = n2 * rb;
-		g2.lens(n0, nA1, nt1);
-		Gemm<T>& g3 = p.g[2];  // per (a,i1): S3(a,i1,i2,k2,b') = sum_(k1,j2) S2(a,i1,k1,j2,b') A2(k1,i2,j2,k2)
-		g3.batch = int(ra * n1); g3.M = int(rb); g3.N = int(n2 * K2); g3.Ni = int(K2); g3.K = int(K1 * n2); g3.Ki = int(n2);
-		g3.A = t2; g3.sAb = K1 * n2 * rb; g3.sAm = 1; g3.sAko = n2 * rb; g3.sAk = rb;
-		g3.B = A2; g3.sBko = n2 * n2 * K2; g3.sBk = K2; g3.sBno = n2 * K2; g3.sBn = 1;
-		g3.C = t3; g3.sCb = n2 * K2 * rb; g3.sCm = 1; g3.sCno = K2 * rb; g3.sCn = rb;
-		g3.lens(nt1, nA2, nt2);
-		Gemm<T>& g4 = p.g[3];  // y((a,i1,i2),b) = sum_(k2,b') S3((a,i1,i2),(k2,b')) R(b,(k2,b'))
-		g4.M = int(ra * n1 * n2); g4.N = int(rb); g4.K = int(K2 * rb);
-		g4.A = t3; g4.sAm = K2 * rb; g4.sAk = 1;
-		g4.B = R; g4.sBk = 1; g4.sBn = K2 * rb;
-		g4.sCm = rb; g4.sCn = 1;
-		g4.lens(nt2, nR, nx);
-	}
-	return p;
-}
-
-template MatvecPlan<double> make_matvec_plan<double>(const LocalShape&, const double*, const double*, const double*,
-                                                     const double*, double*, double*, double*);
-template MatvecPlan<float> make_matvec_plan<float>(const LocalShape&, const float*, const float*, const float*,
-                                                   const float*, float*, float*, float*);
-
 void local_matvec(Context& c, const LocalShape& s, const double* L, const double* A1, const double* A2,
                   const double* R, const double* x, double* y) {
 	double* t1 = c.scratch<double>(S_ALS_FIRST + 20, matvec_tmp_elems(s, 0));
@@ -486,100 +407,34 @@ CgResult local_solve(Context& c, const LocalShape& s, const double* L, const dou
 
 // ------------------------------------------------------------ environment pushes
 
-// L'(c1,c2,c3) = sum L(a1,a2,a3) x(a1,i,c1) A(a2,i,j,c2) x(a3,j,c3)       (als.cpp:184-200, 247)
+static void run_plan(Context& c, const GemmChain& p) {
+	for (int i = 0; i < p.ns; ++i) gemm(c, p.g[i]);
+}
+
 static void push_left_op(Context& c, const double* L, const double* x, const double* A, double* out, long long r,
                          long long K, long long n, long long r1, long long K1) {
 	double* s1 = c.scratch<double>(S_ALS_FIRST + 16, size_t(K * r * n * r1));
 	double* s2 = c.scratch<double>(S_ALS_FIRST + 17, size_t(r * r1 * n * K1));
-	Gemm<double> p1;  // S1((a2,a3),(i,c1)) = sum_a1 L(a1,(a2,a3)) x(a1,(i,c1))
-	p1.M = int(K * r); p1.N = int(n * r1); p1.K = int(r);
-	p1.A = L; p1.sAm = 1; p1.sAk = K * r;
-	p1.B = x; p1.sBk = n * r1; p1.sBn = 1;
-	p1.C = s1; p1.sCm = n * r1; p1.sCn = 1;
-	p1.lens(r * K * r, r * n * r1, K * r * n * r1);
-	gemm(c, p1);
-	Gemm<double> p2;  // per a3: S2(a3,c1,(j,c2)) = sum_(a2,i) S1(a2,a3,i,c1) A((a2,i),(j,c2))
-	p2.batch = int(r); p2.M = int(r1); p2.N = int(n * K1); p2.K = int(K * n); p2.Ki = int(n);
-	p2.A = s1; p2.sAb = n * r1; p2.sAm = 1; p2.sAko = r * n * r1; p2.sAk = r1;
-	p2.B = A; p2.sBko = n * n * K1; p2.sBk = n * K1; p2.sBn = 1;
-	p2.C = s2; p2.sCb = r1 * n * K1; p2.sCm = n * K1; p2.sCn = 1;
-	p2.lens(K * r * n * r1, K * n * n * K1, r * r1 * n * K1);
-	gemm(c, p2);
-	Gemm<double> p3;  // L'((c1,c2),c3) = sum_(a3,j) S2(a3,c1,j,c2) x((a3,j),c3)
-	p3.M = int(r1 * K1); p3.Mi = int(K1); p3.N = int(r1); p3.K = int(r * n); p3.Ki = int(n);
-	p3.A = s2; p3.sAmo = n * K1; p3.sAm = 1; p3.sAko = r1 * n * K1; p3.sAk = K1;
-	p3.B = x; p3.sBko = n * r1; p3.sBk = r1; p3.sBn = 1;
-	p3.C = out; p3.sCmo = K1 * r1; p3.sCm = r1; p3.sCn = 1;
-	p3.lens(r * r1 * n * K1, r * n * r1, r1 * K1 * r1);
-	gemm(c, p3);
+	run_plan(c, plan_push_left_op(L, x, A, out, s1, s2, r, K, n, r1, K1));
 }
 
-// R'(a1,a2,a3) = sum x(a1,i,c1) A(a2,i,j,c2) x(a3,j,c3) R(c1,c2,c3)       (als.cpp:239)
 static void push_right_op(Context& c, const double* R, const double* x, const double* A, double* out, long long r,
                           long long K, long long n, long long r1, long long K1) {
 	double* s1 = c.scratch<double>(S_ALS_FIRST + 16, size_t(r * n * r1 * K1));
 	double* s2 = c.scratch<double>(S_ALS_FIRST + 17, size_t(r * K * n * r1));
-	Gemm<double> q1;  // S1((a3,j),(c1,c2)) = sum_c3 x((a3,j),c3) R((c1,c2),c3)
-	q1.M = int(r * n); q1.N = int(r1 * K1); q1.K = int(r1);
-	q1.A = x; q1.sAm = r1; q1.sAk = 1;
-	q1.B = R; q1.sBk = 1; q1.sBn = r1;
-	q1.C = s1; q1.sCm = r1 * K1; q1.sCn = 1;
-	q1.lens(r * n * r1, r1 * K1 * r1, r * n * r1 * K1);
-	gemm(c, q1);
-	Gemm<double> q2;  // per a3: S2(a3,(a2,i),c1) = sum_(j,c2) A((a2,i),(j,c2)) S1(a3,j,c1,c2)
-	q2.batch = int(r); q2.M = int(K * n); q2.N = int(r1); q2.K = int(n * K1); q2.Ki = int(K1);
-	q2.A = A; q2.sAm = n * K1; q2.sAko = K1; q2.sAk = 1;
-	q2.B = s1; q2.sBb = n * r1 * K1; q2.sBko = r1 * K1; q2.sBk = 1; q2.sBn = K1;
-	q2.C = s2; q2.sCb = K * n * r1; q2.sCm = r1; q2.sCn = 1;
-	q2.lens(K * n * n * K1, r * n * r1 * K1, r * K * n * r1);
-	gemm(c, q2);
-	Gemm<double> q3;  // R'(a1,(a2,a3)) = sum_(i,c1) x(a1,(i,c1)) S2(a3,a2,(i,c1))
-	q3.M = int(r); q3.N = int(K * r); q3.Ni = int(r); q3.K = int(n * r1);
-	q3.A = x; q3.sAm = n * r1; q3.sAk = 1;
-	q3.B = s2; q3.sBk = 1; q3.sBno = n * r1; q3.sBn = K * n * r1;
-	q3.C = out; q3.sCm = K * r; q3.sCno = r; q3.sCn = 1;
-	q3.lens(r * n * r1, r * K * n * r1, r * K * r);
-	gemm(c, q3);
+	run_plan(c, plan_push_right_op(R, x, A, out, s1, s2, r, K, n, r1, K1));
 }
 
-// Lb'(c1,c2) = sum Lb(a1,a2) b(a1,i,c1) x(a2,i,c2)   (als.cpp:202-215, 250)
 static void push_left_rhs(Context& c, const double* Lb, const double* bc, const double* x, double* out, long long s,
                           long long r, long long n, long long s1, long long r1) {
 	double* t = c.scratch<double>(S_ALS_FIRST + 18, size_t(r * n * s1));
-	Gemm<double> u1;  // S1(a2,(i,c1)) = sum_a1 Lb(a1,a2) b(a1,(i,c1))
-	u1.M = int(r); u1.N = int(n * s1); u1.K = int(s);
-	u1.A = Lb; u1.sAm = 1; u1.sAk = r;
-	u1.B = bc; u1.sBk = n * s1; u1.sBn = 1;
-	u1.C = t; u1.sCm = n * s1; u1.sCn = 1;
-	u1.lens(s * r, s * n * s1, r * n * s1);
-	gemm(c, u1);
-	Gemm<double> u2;  // Lb'(c1,c2) = sum_(a2,i) S1((a2,i),c1) x((a2,i),c2)
-	u2.M = int(s1); u2.N = int(r1); u2.K = int(r * n);
-	u2.A = t; u2.sAm = 1; u2.sAk = s1;
-	u2.B = x; u2.sBk = r1; u2.sBn = 1;
-	u2.C = out; u2.sCm = r1; u2.sCn = 1;
-	u2.lens(r * n * s1, r * n * r1, s1 * r1);
-	gemm(c, u2);
+	run_plan(c, plan_push_left_rhs(Lb, bc, x, out, t, s, r, n, s1, r1));
 }
 
-// Rb'(a1,a2) = sum b(a1,i,c1) x(a2,i,c2) Rb(c1,c2)   (als.cpp:242)
 static void push_right_rhs(Context& c, const double* Rb, const double* bc, const double* x, double* out, long long s,
                            long long r, long long n, long long s1, long long r1) {
 	double* t = c.scratch<double>(S_ALS_FIRST + 18, size_t(r * n * s1));
-	Gemm<double> v1;  // S1((a2,i),c1) = sum_c2 x((a2,i),c2) Rb(c1,c2)
-	v1.M = int(r * n); v1.N = int(s1); v1.K = int(r1);
-	v1.A = x; v1.sAm = r1; v1.sAk = 1;
-	v1.B = Rb; v1.sBk = 1; v1.sBn = r1;
-	v1.C = t; v1.sCm = s1; v1.sCn = 1;
-	v1.lens(r * n * r1, s1 * r1, r * n * s1);
-	gemm(c, v1);
-	Gemm<double> v2;  // Rb'(a1,a2) = sum_(i,c1) b(a1,(i,c1)) S1(a2,(i,c1))
-	v2.M = int(s); v2.N = int(r); v2.K = int(n * s1);
-	v2.A = bc; v2.sAm = n * s1; v2.sAk = 1;
-	v2.B = t; v2.sBk = 1; v2.sBn = n * s1;
-	v2.C = out; v2.sCm = r; v2.sCn = 1;
-	v2.lens(s * n * s1, r * n * s1, s * r);
-	gemm(c, v2);
+	run_plan(c, plan_push_right_rhs(Rb, bc, x, out, t, s, r, n, s1, r1));
 }
 
 // b_loc(a, i.., b) = sum Lb(s0,a) b_k(s0,i,s1) [b_k+1(s1,i2,s2)] Rb(s_last,b)   (als.cpp:404-423)

@@ -8,6 +8,8 @@
 #include <set>
 #include <string>
 
+#include <vector>
+
 #include "als.cuh"
 
 namespace {
@@ -443,6 +445,55 @@ int xtt_als_default_options(xtt_als_options* o) {
 	});
 }
 
+static xtt::AlsOptions to_options(const xtt_als_options* opt) {
+	xtt::AlsOptions o;
+	o.sites = opt->sites;
+	o.local_solver = opt->local_solver;
+	o.preserve_core_position = opt->preserve_core_position != 0;
+	o.precision = opt->precision;
+	o.num_half_sweeps = opt->num_half_sweeps;
+	o.convergence_epsilon = opt->convergence_epsilon;
+	o.local_tolerance = opt->local_tolerance;
+	o.local_max_iterations = opt->local_max_iterations;
+	o.residual_target = opt->residual_target;
+	o.record_residuals = opt->record_residuals != 0;
+	o.max_rank = opt->max_rank;
+	o.svd_epsilon = opt->svd_epsilon;
+	o.exact_environment = opt->exact_environment != 0;
+	return o;
+}
+
+int xtt_als_batch(xtt_context* ctx, int64_t count, const xtt_tensor* const* A, xtt_tensor* const* x,
+                  const xtt_tensor* const* b, const xtt_als_options* opt, int autotune, double* energies,
+                  int64_t* local_iterations, xtt_batch_report* report) {
+	return guard([&] {
+		ARG(ctx && A && x && b && opt, "NULL argument");
+		ARG(count > 0 && count <= (int64_t(1) << 24), "count must be in 1..2^24");
+		ARG(opt->local_tolerance > 0 && opt->local_tolerance < 1, "local_tolerance must be in (0, 1)");
+		ARG(opt->precision == XTT_PRECISION_FP64 || opt->precision == XTT_PRECISION_MIXED, "unknown precision");
+		ARG(opt->record_residuals == 0 && opt->residual_target == 0, "batch: no residual traces or targets");
+		std::vector<const xtt::Tensor*> av(count), bv(count);
+		std::vector<xtt::Tensor*> xv(count);
+		for (int64_t i = 0; i < count; ++i) {
+			ARG(A[i] && x[i] && b[i], "NULL tensor in the batch");
+			av[i] = A[i]->t;
+			xv[i] = x[i]->t;
+			bv[i] = b[i]->t;
+		}
+		xtt::BatchResult r = xtt::als_batch(*ctx->c, av, xv, bv, to_options(opt), autotune != 0);
+		for (int64_t i = 0; i < count; ++i) {
+			if (energies) energies[i] = r.energy[i];
+			if (local_iterations) local_iterations[i] = r.iterations[i];
+		}
+		if (report) {
+			report->milliseconds = r.ms;
+			report->threads = r.threads;
+			report->ctas_per_sm = r.ctas_per_sm;
+			report->ctas = r.ctas;
+		}
+	});
+}
+
 int xtt_als(const xtt_tensor* A, xtt_tensor* x, const xtt_tensor* b, const xtt_als_options* opt,
             xtt_als_report* report, double* residual_trace, int64_t* flag_trace, double* energy_trace,
             int64_t trace_capacity) {
@@ -450,21 +501,7 @@ int xtt_als(const xtt_tensor* A, xtt_tensor* x, const xtt_tensor* b, const xtt_a
 		ARG(A && x && b && opt, "NULL argument");
 		ARG(opt->local_tolerance > 0 && opt->local_tolerance < 1, "local_tolerance must be in (0, 1)");
 		ARG(opt->precision == XTT_PRECISION_FP64 || opt->precision == XTT_PRECISION_MIXED, "unknown precision");
-		xtt::AlsOptions o;
-		o.sites = opt->sites;
-		o.local_solver = opt->local_solver;
-		o.preserve_core_position = opt->preserve_core_position != 0;
-		o.precision = opt->precision;
-		o.num_half_sweeps = opt->num_half_sweeps;
-		o.convergence_epsilon = opt->convergence_epsilon;
-		o.local_tolerance = opt->local_tolerance;
-		o.local_max_iterations = opt->local_max_iterations;
-		o.residual_target = opt->residual_target;
-		o.record_residuals = opt->record_residuals != 0;
-		o.max_rank = opt->max_rank;
-		o.svd_epsilon = opt->svd_epsilon;
-		o.exact_environment = opt->exact_environment != 0;
-		xtt::AlsReport r = xtt::als(*A->t, *x->t, *b->t, o);
+		xtt::AlsReport r = xtt::als(*A->t, *x->t, *b->t, to_options(opt));
 		if (report) {
 			report->energy = r.energy;
 			report->residual = r.residual;

@@ -34,6 +34,13 @@ struct Context {
 	double* h_dbl = nullptr;       // pinned mirror
 	long long launches = 0;
 	int cg_path = XTT_CG_PATH_AUTO;  // xtt_cg_path: which local CG kernel family runs
+	// batched ALS: the CUDA graph of the last batch launch (replayed while its
+	// signature holds), its pinned descriptor staging, and autotuned launch shapes
+	unsigned long long batch_key = 0;
+	cudaGraphExec_t batch_exec = nullptr;
+	void* batch_host = nullptr;
+	size_t batch_host_bytes = 0;
+	std::vector<std::pair<unsigned long long, std::pair<int, int>>> batch_tuned;
 	int tensors = 0;        // live tensors created on this context
 	bool closing = false;   // destroy requested; freed when the last tensor goes
 	struct Slot {
@@ -96,7 +103,7 @@ enum ScratchId : int {
 	S_QR_Q = 0, S_QR_C, S_QR_WORK, S_GEMM_A, S_GEMM_B, S_SVD_U, S_SVD_S, S_SVD_VT, S_SVD_WORK,
 	S_ROUND_X, S_ROUND_QA, S_ROUND_QB, S_ROUND_CA, S_ROUND_CB, S_ZIP_M, S_ZIP_T, S_ZIP_M2,
 	S_RES_CORE0, S_RES_CORE1, S_RES_R, S_RED, S_ENT_META, S_ENT_CORES, S_ENT_OUT,
-	S_RES_CORE0B, S_RES_CORE1B, S_RES_RB, S_QR_WORKB,
+	S_RES_CORE0B, S_RES_CORE1B, S_RES_RB, S_QR_WORKB, S_BATCH_META, S_BATCH_WORK, S_BATCH_BACKUP,
 	S_ALS_FIRST = 32,
 	S_ADF_FIRST = 96,
 	S_MAX = 160

@@ -32,14 +32,14 @@ struct Gemm {
 	// Element counts of the A, B and C buffers (host-side bounds check before any launch).
 	long long lenA = -1, lenB = -1, lenC = -1;
 
-	Gemm& lens(long long a, long long b, long long c) {
+	__host__ __device__ Gemm& lens(long long a, long long b, long long c) {
 		lenA = a;
 		lenB = b;
 		lenC = c;
 		return *this;
 	}
 	// Upper bounds of the largest element offset each operand can touch (strides are >= 0).
-	static long long span(int ext, int inner, long long s_in, long long s_out) {
+	__host__ __device__ static long long span(int ext, int inner, long long s_in, long long s_out) {
 		if (ext <= 0) return 0;
 		if (!inner) return (long long)(ext - 1) * s_in;
 		const long long mo = (ext - 1) / inner, mi = (ext < inner ? ext : inner) - 1;

@@ -44,6 +44,8 @@ Context::~Context() {
 	cudaFree(d_dbl);
 	cudaFreeHost(h_ints);
 	cudaFreeHost(h_dbl);
+	if (batch_exec) cudaGraphExecDestroy(batch_exec);
+	if (batch_host) cudaFreeHost(batch_host);
 	cudaEventDestroy(ev_fork);
 	cudaEventDestroy(ev_join);
 	cudaStreamDestroy(aux);
