@@ -41,6 +41,9 @@ def parse():
     p.add_argument("--warmup", type=int, default=3)
     p.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     p.add_argument("--no-cpu-baseline", action="store_true")
+    p.add_argument("--workloads", default="all", choices=["all", "headline"],
+                   help="all: also time TT round/dot (d=32 r=64), ADF (d=10, 200k samples) and the 4096-instance batch")
+    p.add_argument("--batch-count", type=int, default=4096)
     return p.parse_args()
 
 
@@ -126,6 +129,130 @@ def read_profile_traffic(name):
     return None
 
 
+def _events(torch, stream):
+    return torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+
+
+def bench_round_dot(xg, ctx, torch, stream, steps, cpu):
+    """TT rounding and dot product: d=32, n=4, rank 64, cores N(0, 1/8); move_core(d-1)
+    (pivoted QC sweep), round to rank 32, dot with an independent second tensor (FP64)."""
+    d, n = 32, 4
+    xg.seed(SEED)
+    x0 = xg.TTTensor.random([n] * d, 64, 0.0, 1.0 / 8, ctx=ctx)
+    y = xg.TTTensor.random([n] * d, 64, 0.0, 1.0 / 8, ctx=ctx)
+    t = {"move_core": [], "round": [], "dot": []}
+    for i in range(steps + 1):
+        x = x0.copy()
+        torch.cuda.synchronize()
+        for name, fn in (("move_core", lambda: x.move_core(d - 1)), ("round", lambda: x.round(32)),
+                         ("dot", lambda: xg.dot(x0, y))):
+            e0, e1 = _events(torch, stream)
+            e0.record(stream)
+            fn()
+            e1.record(stream)
+            torch.cuda.synchronize()
+            if i > 0:
+                t[name].append(e0.elapsed_time(e1))
+    out = {"workload": "TT move_core + round(32) + dot, d=32 n=4 rank 64, FP64", "ranks_after_round": x.ranks()[:4],
+           "ms": {k: statistics.mean(v) for k, v in t.items()}}
+    if cpu:
+        from oracle import xtt_oracle as o
+        xh = o.TT(x0.get_cores(), x0.canonicalized, x0.corePosition)
+        yh = o.TT(y.get_cores(), y.canonicalized, y.corePosition)
+        c = {}
+        t0 = time.perf_counter()
+        o.move_core(xh, d - 1)
+        c["move_core"] = 1e3 * (time.perf_counter() - t0)
+        t0 = time.perf_counter()
+        o.tt_round(xh, [32] * (d - 1))
+        c["round"] = 1e3 * (time.perf_counter() - t0)
+        t0 = time.perf_counter()
+        o.tt_dot(o.TT(x0.get_cores(), x0.canonicalized, x0.corePosition), yh)
+        c["dot"] = 1e3 * (time.perf_counter() - t0)
+        out["cpu_ms"] = c
+        out["cpu_kind"] = "port (numpy/LAPACK, all BLAS threads)"
+    return out
+
+
+def bench_adf(xg, ctx, torch, stream, iters, peak, cpu):
+    """ADF completion: d=10, n=8, rank-6 target, 200000 samples (+N(0,1e-6) noise),
+    rank-6 model, `iters` iterations of ADFVariant(iters, 0, 1)."""
+    d, n, r, N = 10, 8, 6, 200000
+    xg.seed(SEED)
+    target = xg.TTTensor.random([n] * d, r, ctx=ctx)
+    m = xg.SinglePointMeasurementSet.random(N, [n] * d)
+    m.measure(target)
+    noise = np.zeros(N)
+    xg._lib.load().xtt_random_normal(0.0, 1e-6, N, noise.ctypes.data_as(xg._lib.c_double_p))
+    m.measuredValues = m.measuredValues + noise
+    x0 = xg.TTTensor.random([n] * d, r, ctx=ctx)
+    xg.ADFVariant(2, 0.0, 1.0)(x0.copy(), m)  # warm-up
+    x = x0.copy()
+    torch.cuda.synchronize()
+    e0, e1 = _events(torch, stream)
+    e0.record(stream)
+    res = xg.ADFVariant(iters, 0.0, 1.0)(x, m)
+    e1.record(stream)
+    torch.cuda.synchronize()
+    ms = e0.elapsed_time(e1) / iters
+    # per iteration: stack updates, residuals, gradient scatter and slice norms over all positions,
+    # N d w (5 r + 4) bytes (w = 8)
+    alg = N * d * 8 * (5 * r + 4)
+    out = {"workload": "ADF d=10 n=8 rank 6, 200000 samples, FP64", "iterations": iters, "ms_per_iteration": ms,
+           "samples_per_s": N / (ms / 1e3), "final_residual": res,
+           "roofline": {"bound": "hbm", "achieved": alg / (ms / 1e3) / 1e9, "peak": peak, "unit": "GB/s",
+                        "frac": alg / (ms / 1e3) / 1e9 / peak, "algorithmic_bytes_per_iteration": alg}}
+    if cpu:
+        from oracle import xtt_oracle as o
+        xh = o.TT(x0.get_cores(), x0.canonicalized, x0.corePosition)
+        t0 = time.perf_counter()
+        o.adf(xh, m.positions, m.measuredValues, 1, 0.0, 1.0)
+        out["cpu_ms_per_iteration"] = 1e3 * (time.perf_counter() - t0)
+        out["cpu_sample"] = "1 iteration of the same problem (numpy port, all BLAS threads)"
+    return out
+
+
+def bench_batch(xg, ctx, count, steps):
+    """Config-4 batch: `count` independent SPD problems, d ~ U{4..16}, n ~ U{2..8},
+    Laplacian sum + shift U[0.1, 1], rhs rank ~ U{2..8}, start rank ~ U{4..32}
+    (maximal-reduced), 4 ALS sweeps each, in one persistent launch (CUDA graph)."""
+    rng = np.random.default_rng(SEED)
+    xg.seed(SEED)
+    As, xs, bs = [], [], []
+    for i in range(count):
+        d, n = int(rng.integers(4, 17)), int(rng.integers(2, 9))
+        shift = float(rng.uniform(0.1, 1.0))
+        As.append(xg.TTOperator.from_cores(xg.laplacian_cores(d, n, shift=shift), ctx=ctx))
+        bs.append(xg.TTTensor.random([n] * d, int(rng.integers(2, 9)), ctx=ctx))
+        x = xg.TTTensor.random([n] * d, int(rng.integers(4, 33)), ctx=ctx)
+        x /= x.frob_norm()
+        xs.append(x)
+    saved = [(x.get_flat(), x.all_ranks()) for x in xs]
+
+    def restore():
+        for x, (f, r) in zip(xs, saved):
+            x.set_flat(f, ranks=r)
+            x.assume_core_position(0)
+
+    out = {"workload": f"{count} independent ALS_SPD problems (config 4), 4 sweeps each", "count": count}
+    for name, prec in (("fp64", xg.FP64), ("mixed", xg.MIXED)):
+        v = xg.ALS_SPD.copy()
+        v.convergenceEpsilon = 0.0
+        v.precision = prec
+        restore()
+        _, _, rep = xg.als_batch(As, xs, bs, variant=v, numHalfSweeps=8, autotune=True)
+        ms, its = [], None
+        for _ in range(steps):
+            restore()
+            en, its, rep = xg.als_batch(As, xs, bs, variant=v, numHalfSweeps=8)
+            ms.append(rep["milliseconds"])
+        t = statistics.mean(ms)
+        out[name] = {"ms": t, "instances_per_s": count / (t / 1e3), "launch": {k: rep[k] for k in ("threads", "ctas_per_sm", "ctas")},
+                     "cg_iterations": int(its.sum()), "energy_sum": float(en.sum())}
+    out["mixed_speedup_vs_fp64"] = out["fp64"]["ms"] / out["mixed"]["ms"]
+    return out
+
+
 def run_gpu(args):
     import torch
     import xerus_gb300 as xg
@@ -153,6 +280,8 @@ def run_gpu(args):
         v(A, x, b, WORKLOAD["max_half_sweeps"])
         return x, v.last_report
 
+    work = {}
+
     def timed(precision, steps, warmup, profile=False):
         for _ in range(warmup):
             solve(precision)
@@ -175,6 +304,7 @@ def run_gpu(args):
         if profile:
             for name in ("cg_fp64", "cg_mixed", "gemm", "qr", "svd"):
                 prof[name] = ctx.profile_get(name)
+                work[name] = ctx.profile_work(name)
             ctx.profile(False)
         return times, reports, launches, prof, x
 
@@ -186,6 +316,7 @@ def run_gpu(args):
     # per-kernel-class event timing in separate (untimed) passes: events add host work
     nprof = max(1, min(3, args.steps))
     _, _, _, prof_mix, _ = timed(xg.MIXED, nprof, 0, profile=True)
+    prof_work = dict(work)
     _, _, _, prof_64, _ = timed(xg.FP64, nprof, 0, profile=True)
     prof_steps = nprof
     res_mix = xg.residual(A, x_mix, b)
@@ -280,8 +411,43 @@ def run_gpu(args):
                      "kernel_ms_per_step": {k: v[1] / prof_steps for k, v in prof_mix.items()}},
         "clocks": clk,
     }
+    # per-class kernel time and declared algorithmic work (profiled mixed passes)
+    classes = {}
+    for name in ("cg_mixed", "qr", "gemm"):
+        nl, ms = prof_mix.get(name, (0, 0.0))
+        by, fl = prof_work.get(name, (0.0, 0.0))
+        if nl:
+            classes[name] = {"ms_per_step": ms / prof_steps, "launches_per_step": nl / prof_steps,
+                             "bytes_per_step": by / prof_steps, "flops_per_step": fl / prof_steps,
+                             "GB_per_s": by / (ms / 1e3) / 1e9 if ms > 0 and by else None,
+                             "GFLOP_per_s": fl / (ms / 1e3) / 1e9 if ms > 0 and fl else None}
+    line["kernel_classes"] = classes
+    if top in ("qr", "gemm") and classes.get(top, {}).get("GB_per_s"):
+        c_ = classes[top]
+        ach = c_["GB_per_s"]
+        line["roofline"] = {"kernel": {"qr": "k_qr_cl2 / k_qr (FP64 Householder)", "gemm": "k_gemm_sk (FP64)"}[top],
+                            "bound": "hbm", "achieved": ach, "peak": peaks.get("hbm_gbs", 6800.0), "unit": "GB/s",
+                            "frac": ach / peaks.get("hbm_gbs", 6800.0), "traffic": read_profile_traffic("qr_cl2_als_d8_r32"),
+                            "peak_source": "of measured" if "hbm_gbs" in peaks else "of fallback",
+                            "algorithmic_bytes_per_launch": c_["bytes_per_step"] / c_["launches_per_step"],
+                            "algorithmic_flops_per_launch": c_["flops_per_step"] / c_["launches_per_step"],
+                            "avg_launch_ms": c_["ms_per_step"] / c_["launches_per_step"],
+                            "launches": int(c_["launches_per_step"] * prof_steps),
+                            "top_kernel_class_by_time": top,
+                            "note": "latency-bound: per-column FP64 dependency chains and cluster barriers, "
+                                    "L2-resident operands",
+                            "kernel_ms_per_step": {k: v[1] / prof_steps for k, v in prof_mix.items()},
+                            "cg_mixed": line["roofline"]}
     if not args.no_cpu_baseline:
         line["cpu_baseline"] = cpu_baseline(A, b, x0, samples=1)
+    if args.workloads == "all":
+        peak = peaks.get("hbm_gbs", 6800.0)
+        cpu = not args.no_cpu_baseline
+        wl = {}
+        wl["round_dot_d32_r64"] = bench_round_dot(xg, ctx, torch, stream, 3, cpu)
+        wl["adf_d10_n8_r6_200k"] = bench_adf(xg, ctx, torch, stream, 50, peak, cpu)
+        wl["batch_als_cfg4"] = bench_batch(xg, ctx, args.batch_count, 2)
+        line["workloads"] = wl
     return line
 
 

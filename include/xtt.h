@@ -65,6 +65,10 @@ int xtt_context_kernel_launches(xtt_context* ctx, int64_t* count);
 int xtt_context_profile(xtt_context* ctx, int enable);
 /* Launch count and total milliseconds of one class since profiling started (0 if none). */
 int xtt_context_profile_get(xtt_context* ctx, const char* name, int64_t* launches, double* milliseconds);
+/* Algorithmic work the launches of one class declared since profiling started:
+ * minimal operand bytes and arithmetic (0 for classes whose work depends on
+ * device-side iteration counts, e.g. the CG solves). */
+int xtt_context_profile_work(xtt_context* ctx, const char* name, double* bytes, double* flops);
 
 /* Which kernel family runs the local conjugate-gradient solves of xtt_als (no
  * reference counterpart; the reference factors the local system densely,

@@ -64,6 +64,12 @@ class Context:
         """Starts (clears) or stops per-kernel-class CUDA-event timing."""
         L.check(self.lib.xtt_context_profile(self.handle, int(bool(enable))))
 
+    def profile_work(self, name):
+        """(bytes, flops) of algorithmic work declared by the launches of a class."""
+        by, fl = ctypes.c_double(), ctypes.c_double()
+        L.check(self.lib.xtt_context_profile_work(self.handle, name.encode(), ctypes.byref(by), ctypes.byref(fl)))
+        return by.value, fl.value
+
     def set_cg_path(self, path):
         """'auto' (cluster-resident CG where the local system fits) or 'grid'."""
         L.check(self.lib.xtt_context_set_cg_path(self.handle, {"auto": 0, "grid": 1}[path]))

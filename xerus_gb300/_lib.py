@@ -75,6 +75,7 @@ _SIGNATURES = {
     "xtt_context_profile": (ctypes.c_int, [VP, ctypes.c_int]),
     "xtt_context_profile_get": (ctypes.c_int, [VP, ctypes.c_char_p, c_int64_p, c_double_p]),
     "xtt_context_set_cg_path": (ctypes.c_int, [VP, ctypes.c_int]),
+    "xtt_context_profile_work": (ctypes.c_int, [VP, ctypes.c_char_p, c_double_p, c_double_p]),
     "xtt_als_batch": (ctypes.c_int, [VP, ctypes.c_int64, ctypes.POINTER(VP), ctypes.POINTER(VP), ctypes.POINTER(VP),
                                      ctypes.POINTER(AlsOptions), ctypes.c_int, c_double_p, c_int64_p,
                                      ctypes.POINTER(BatchReport)]),

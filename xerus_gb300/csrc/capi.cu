@@ -121,6 +121,21 @@ int xtt_context_profile(xtt_context* ctx, int enable) {
 	});
 }
 
+int xtt_context_profile_work(xtt_context* ctx, const char* name, double* bytes, double* flops) {
+	return guard([&] {
+		ARG(ctx && name && bytes && flops, "NULL argument");
+		xtt::Context& c = *ctx->c;
+		c.resolve_profile();
+		*bytes = 0;
+		*flops = 0;
+		for (auto& e : c.profile)
+			if (e.first == name) {
+				*bytes = e.second.bytes;
+				*flops = e.second.flops;
+			}
+	});
+}
+
 int xtt_context_set_cg_path(xtt_context* ctx, int path) {
 	return guard([&] {
 		ARG(ctx, "ctx is NULL");

@@ -71,22 +71,27 @@ struct Context {
 	struct Timed {
 		std::string name;
 		cudaEvent_t start, stop;
+		double bytes, flops;
 	};
 	std::vector<Timed> pending;
 	struct ProfileEntry {
 		long long launches = 0;
 		double ms = 0;
+		double bytes = 0, flops = 0;  // algorithmic work the launch sites declared
 	};
 	std::vector<std::pair<std::string, ProfileEntry>> profile;
 	void resolve_profile();
 };
 
 // RAII scope recording a launch class's start and stop events when profiling.
+// `bytes` / `flops`: the algorithmic work of the scope (minimal operand traffic,
+// arithmetic), accumulated per class for roofline figures.
 struct ProfScope {
 	Context& c;
 	const char* name;
+	double bytes, flops;
 	cudaEvent_t a = nullptr, b = nullptr;
-	ProfScope(Context& cc, const char* n);
+	ProfScope(Context& cc, const char* n, double bytes = 0, double flops = 0);
 	~ProfScope();
 };
 

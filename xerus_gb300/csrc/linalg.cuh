@@ -39,6 +39,19 @@ struct SvdArgs {
 	int max_sweeps = 60;
 };
 
+// Algorithmic work of one factorisation: operand bytes read and written once
+// (A, the triangular factor, Q if formed) and Householder flops (2 m n^2 - 2/3 n^3
+// for the factor, the same again to form Q).
+inline double qr_work_bytes(const QrArgs& a) {
+	const double mw = a.transpose ? a.n : a.m, nw = a.transpose ? a.m : a.n, kq = mw < nw ? mw : nw;
+	return 8.0 * (mw * nw + kq * nw + (a.want_q ? mw * kq : 0.0));
+}
+inline double qr_work_flops(const QrArgs& a) {
+	const double mw = a.transpose ? a.n : a.m, nw = a.transpose ? a.m : a.n, kq = mw < nw ? mw : nw;
+	const double f = 2.0 * mw * nw * kq - 2.0 / 3.0 * kq * kq * kq;
+	return a.want_q ? 2.0 * f : f;
+}
+
 // Launchers (stream-ordered, asynchronous).
 void launch_qr(const QrArgs& a, cudaStream_t s);
 size_t qr_work_doubles(int m, int n);        // global workspace needed (0 if shared memory suffices)

@@ -101,7 +101,7 @@ void Context::sync() {
 	check_status();
 }
 
-ProfScope::ProfScope(Context& cc, const char* n) : c(cc), name(n) {
+ProfScope::ProfScope(Context& cc, const char* n, double by, double fl) : c(cc), name(n), bytes(by), flops(fl) {
 	if (!c.profiling) return;
 	XTT_CUDA(cudaEventCreate(&a));
 	XTT_CUDA(cudaEventCreate(&b));
@@ -111,7 +111,7 @@ ProfScope::ProfScope(Context& cc, const char* n) : c(cc), name(n) {
 ProfScope::~ProfScope() {
 	if (!a) return;
 	cudaEventRecord(b, c.stream);
-	c.pending.push_back(Context::Timed{name, a, b});
+	c.pending.push_back(Context::Timed{name, a, b, bytes, flops});
 }
 
 void Context::resolve_profile() {
@@ -128,6 +128,8 @@ void Context::resolve_profile() {
 		}
 		it->second.launches += 1;
 		it->second.ms += ms;
+		it->second.bytes += t.bytes;
+		it->second.flops += t.flops;
 	}
 	pending.clear();
 }
@@ -308,7 +310,8 @@ static void launch_gemm_sk(Context& c, const Gemm<T>& g) {
 void gemm(Context& c, const Gemm<double>& g) {
 	if (g.M <= 0 || g.N <= 0 || g.batch <= 0) return;
 	check_gemm(g);
-	ProfScope ps(c, "gemm");
+	const double mn = double(g.batch) * g.M * g.N, mk = double(g.M) * g.K, kn = double(g.K) * g.N;
+	ProfScope ps(c, "gemm", 8.0 * (double(g.batch) * (mk + kn) + mn), 2.0 * mn * g.K);
 	launch_gemm_sk(c, g);
 	c.count_launch();
 }
@@ -471,7 +474,7 @@ void transfer_core(Tensor& x, int from, int to, bool rr) {
 		a.work = wk ? c.scratch<double>(S_QR_WORK, wk) : nullptr;
 		a.Q = Q; a.C = C; a.rank_out = c.d_ints;
 		{
-			ProfScope ps(c, "qr");
+			ProfScope ps(c, "qr", qr_work_bytes(a), qr_work_flops(a));
 			launch_qr(a, c.stream);
 		}
 		c.count_launch();
@@ -500,7 +503,7 @@ void transfer_core(Tensor& x, int from, int to, bool rr) {
 		a.work = wk ? c.scratch<double>(S_QR_WORK, wk) : nullptr;
 		a.Q = Q; a.C = C; a.rank_out = c.d_ints;
 		{
-			ProfScope ps(c, "qr");
+			ProfScope ps(c, "qr", qr_work_bytes(a), qr_work_flops(a));
 			launch_qr(a, c.stream);
 		}
 		c.count_launch();
@@ -583,7 +586,7 @@ static void round_edge(Tensor& x, int from, int to, int64_t max_rank, double eps
 		a.work = wk ? c.scratch<double>(S_QR_WORK, wk) : nullptr;
 		a.Q = QF; a.C = CA; a.rank_out = c.d_ints + 2;
 		{
-			ProfScope ps(c, "qr");
+			ProfScope ps(c, "qr", qr_work_bytes(a), qr_work_flops(a));
 			launch_qr(a, c.stream);
 		}
 		c.count_launch();
@@ -596,7 +599,7 @@ static void round_edge(Tensor& x, int from, int to, int64_t max_rank, double eps
 		b.work = wk ? c.scratch<double>(S_ROUND_X, wk) : nullptr;  // not S_QR_WORK: may run concurrently in the future
 		b.Q = QT; b.C = CB; b.rank_out = c.d_ints + 3;
 		{
-			ProfScope ps(c, "qr");
+			ProfScope ps(c, "qr", qr_work_bytes(a), qr_work_flops(a));
 			launch_qr(b, c.stream);
 		}
 		c.count_launch();
@@ -834,7 +837,7 @@ double residual(const Tensor& A, const Tensor& x, const Tensor& b) {
 		a.A = Zp; a.lda = ncol; a.m = m; a.n = ncol; a.transpose = transpose; a.pivot = 0; a.want_q = 0;
 		a.work = wk ? c.scratch<double>(c.stream == c.aux ? S_QR_WORKB : S_QR_WORK, wk) : nullptr;
 		a.Q = nullptr; a.C = out; a.rank_out = nullptr;
-		ProfScope ps(c, "qr");
+		ProfScope ps(c, "qr", qr_work_bytes(a), qr_work_flops(a));
 		launch_qr(a, c.stream);
 		c.count_launch();
 	};
