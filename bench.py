@@ -374,7 +374,7 @@ def run_gpu(args):
     peaks = json.load(open(os.path.join(ROOT, "MEASURED_PEAKS.json"))) if os.path.exists(
         os.path.join(ROOT, "MEASURED_PEAKS.json")) else {"hbm_gbs": 6800.0}
     achieved = alg_bytes / (per_launch_ms / 1e3) / 1e9 if per_launch_ms > 0 else 0.0
-    traffic = read_profile_traffic("cg_mixed_als_d8_r32")
+    traffic = read_profile_traffic("cg_cluster_mixed_als_d8_r32")
     top = max(prof_mix.items(), key=lambda kv: kv[1][1])[0] if prof_mix else None
 
     value = statistics.mean(t_mix)
