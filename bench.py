@@ -44,6 +44,8 @@ def parse():
     p.add_argument("--workloads", default="all", choices=["all", "headline"],
                    help="all: also time TT round/dot (d=32 r=64), ADF (d=10, 200k samples) and the 4096-instance batch")
     p.add_argument("--batch-count", type=int, default=4096)
+    p.add_argument("--only", choices=["round", "adf", "batch", "dmrg"],
+                   help="run one secondary workload alone and print its JSON (for profiling)")
     return p.parse_args()
 
 
@@ -494,8 +496,66 @@ def run_reference(args):
             "e2e": {"value": v, "unit": "s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
 
 
+def bench_dmrg(xg, ctx, torch, stream, half_sweeps):
+    """Configuration 3 at the reference's fixed-rank behaviour: two-site DMRG_SPD on
+    the d=20, n=8 Laplacian sum plus a diagonal potential U[0,1] per mode (operator
+    rank 3), random rank-16 start; `half_sweeps` half-sweeps, FP64 and mixed."""
+    d, n = 20, 8
+    rng = np.random.default_rng(SEED)
+    V = [rng.uniform(0.0, 1.0, n) for _ in range(d)]
+    xg.seed(SEED)
+    A = xg.TTOperator.from_cores(xg.laplacian_cores(d, n, potentials=V, rank3=True), ctx=ctx)
+    b = xg.TTTensor.random([n] * d, 4, ctx=ctx)
+    x0 = xg.TTTensor.random([n] * d, 16, ctx=ctx)
+    x0 /= x0.frob_norm()
+    out = {"workload": f"DMRG_SPD d=20 n=8, operator rank 3, rank 16 (fixed), {half_sweeps} half-sweeps, "
+                       "exact right environments (the reference's own decreasing sweep stops at the rank-8 ends)",
+           "local_unknowns": 16 * n * n * 16}
+    for name, prec in (("fp64", xg.FP64), ("mixed", xg.MIXED)):
+        v = xg.DMRG_SPD.copy()
+        v.convergenceEpsilon = 0.0
+        v.precision = prec
+        v.exact_environment = True
+        v(A, x0.copy(), b, 1)  # warm-up
+        x = x0.copy()
+        torch.cuda.synchronize()
+        e0, e1 = _events(torch, stream)
+        e0.record(stream)
+        en = v(A, x, b, half_sweeps)
+        e1.record(stream)
+        torch.cuda.synchronize()
+        ms = e0.elapsed_time(e1)
+        out[name] = {"ms": ms, "ms_per_half_sweep": ms / half_sweeps, "energy": en,
+                     "cg_iterations": v.last_report.local_iterations, "residual": xg.residual(A, x, b)}
+    out["mixed_speedup_vs_fp64"] = out["fp64"]["ms"] / out["mixed"]["ms"]
+    return out
+
+
+def run_only(args):
+    import torch
+    import xerus_gb300 as xg
+    from xerus_gb300 import build
+    build.build()
+    ctx = xg.Context(0)
+    stream = torch.cuda.current_stream()
+    ctx.set_stream(stream.cuda_stream)
+    peaks = json.load(open(os.path.join(ROOT, "MEASURED_PEAKS.json"))) if os.path.exists(
+        os.path.join(ROOT, "MEASURED_PEAKS.json")) else {"hbm_gbs": 6800.0}
+    cpu = not args.no_cpu_baseline
+    if args.only == "round":
+        return bench_round_dot(xg, ctx, torch, stream, args.steps, cpu)
+    if args.only == "adf":
+        return bench_adf(xg, ctx, torch, stream, 50, peaks.get("hbm_gbs", 6800.0), cpu)
+    if args.only == "batch":
+        return bench_batch(xg, ctx, args.batch_count, args.steps)
+    return bench_dmrg(xg, ctx, torch, stream, 2)
+
+
 def main():
     args = parse()
+    if args.only:
+        print(json.dumps(run_only(args)))
+        return
     line = run_reference(args) if args.impl == "reference" else run_gpu(args)
     if line is not None:
         print(json.dumps(line))

@@ -26,7 +26,7 @@
 
 namespace xtt {
 
-constexpr int kAdfThreads = 256;
+constexpr int kAdfThreads = 64;  // two warps: the per-warp accumulators stay under 48 KB of static smem
 constexpr int kAdfWarpsPerBlock = kAdfThreads / 32;
 constexpr int kAdfMaxR = 8;        // fast path: ranks <= 8
 constexpr int kAdfMaxSlices = 16;  // fast path: mode sizes <= 16
@@ -43,33 +43,44 @@ struct AdfLevel {
 
 // res_s (optional write), and per-warp partials of G (r0, n, r1) and of sum res^2.
 // mode 0: res_s = y_s - <F, X_i B>; mode 1: res_s given in `res` (read only).
+// Each warp walks its chunk of samples 32 at a time: lane s stages its sample's
+// F, B, index and residual in the warp's shared memory, then every lane (one or
+// two (a, c) pairs) adds res_j F_j[a] B_j[c] into slice i_j of the warp's
+// gradient accumulator, sample by sample in order (deterministic). One FP64
+// multiply-add per pair and sample: GB300's FP64 pipe is the bound.
 __global__ void __launch_bounds__(kAdfThreads) k_adf_res_grad(AdfLevel L, const double* y, double* res, int mode,
                                                                double* gpart, double* rrpart, long long chunk) {
 	__shared__ double Xs[kAdfMaxR * kAdfMaxSlices * kAdfMaxR];
-	const int lane = threadIdx.x & 31;
-	const long long warp = (long long)blockIdx.x * kAdfWarpsPerBlock + (threadIdx.x >> 5);
+	__shared__ double Gw[kAdfWarpsPerBlock][kAdfMaxSlices * kAdfMaxR * kAdfMaxR];
+	__shared__ double Fw[kAdfWarpsPerBlock][32 * kAdfMaxR];
+	__shared__ double Bw[kAdfWarpsPerBlock][32 * kAdfMaxR];
+	__shared__ double Rw[kAdfWarpsPerBlock][32];
+	__shared__ int Iw[kAdfWarpsPerBlock][32];
+	const int lane = threadIdx.x & 31, wib = threadIdx.x >> 5;
+	const long long warp = (long long)blockIdx.x * kAdfWarpsPerBlock + wib;
 	const int r0 = L.r0, n = L.n, r1 = L.r1, P = r0 * r1;
 	for (int e = threadIdx.x; e < r0 * n * r1; e += blockDim.x) Xs[e] = L.X[e];
+	double* G = Gw[wib];
+	for (int e = lane; e < n * P; e += 32) G[e] = 0.0;
 	__syncthreads();
-	double acc[kAdfMaxSlices][kAdfPairsPerLane];
+	int pa[kAdfPairsPerLane], pc[kAdfPairsPerLane];
 #pragma unroll
-	for (int i = 0; i < kAdfMaxSlices; ++i)
-#pragma unroll
-		for (int t = 0; t < kAdfPairsPerLane; ++t) acc[i][t] = 0.0;
+	for (int t = 0; t < kAdfPairsPerLane; ++t) {
+		const int p = lane + 32 * t;
+		pa[t] = p < P ? p / r1 : 0;
+		pc[t] = p < P ? p - pa[t] * r1 : 0;
+	}
 	double rr = 0.0;
 	const long long s0 = warp * chunk, s1 = min(L.N, s0 + chunk);
 	for (long long base = s0; base < s1; base += 32) {
 		const long long s = base + lane;
-		const bool valid = s < s1;
-		double f[kAdfMaxR], b[kAdfMaxR];
-		int idx = 0;
-		double rs = 0.0;
-		if (valid) {
-			idx = L.pos[s];
-#pragma unroll
-			for (int a = 0; a < kAdfMaxR; ++a) f[a] = (a < r0) ? (L.F ? L.F[a * L.N + s] : 1.0) : 0.0;
-#pragma unroll
-			for (int c = 0; c < kAdfMaxR; ++c) b[c] = (c < r1) ? (L.B ? L.B[c * L.N + s] : 1.0) : 0.0;
+		if (s < s1) {
+			const int idx = L.pos[s];
+			double* f = Fw[wib] + lane * kAdfMaxR;
+			double* b = Bw[wib] + lane * kAdfMaxR;
+			for (int a = 0; a < r0; ++a) f[a] = L.F ? L.F[a * L.N + s] : 1.0;
+			for (int c = 0; c < r1; ++c) b[c] = L.B ? L.B[c * L.N + s] : 1.0;
+			double rs;
 			if (mode == 0) {
 				double v = 0.0;
 				for (int a = 0; a < r0; ++a) {
@@ -84,44 +95,30 @@ __global__ void __launch_bounds__(kAdfThreads) k_adf_res_grad(AdfLevel L, const 
 				rs = res[s];
 			}
 			rr += rs * rs;
+			Rw[wib][lane] = rs;
+			Iw[wib][lane] = idx;
 		}
-		// broadcast each of the 32 samples and accumulate its outer product
+		__syncwarp();
 		const int cnt = int((s1 - base) < 32 ? (s1 - base) : 32);
 		for (int j = 0; j < cnt; ++j) {
-			const int ij = __shfl_sync(0xffffffffu, idx, j);
-			const double rj = __shfl_sync(0xffffffffu, rs, j);
-			double fj[kAdfMaxR], bj[kAdfMaxR];
-#pragma unroll
-			for (int a = 0; a < kAdfMaxR; ++a) fj[a] = __shfl_sync(0xffffffffu, f[a], j);
-#pragma unroll
-			for (int c = 0; c < kAdfMaxR; ++c) bj[c] = __shfl_sync(0xffffffffu, b[c], j);
+			const int ij = Iw[wib][j];
+			const double rj = Rw[wib][j];
+			const double* fj = Fw[wib] + j * kAdfMaxR;
+			const double* bj = Bw[wib] + j * kAdfMaxR;
+			double* gi = G + ij * P;
 #pragma unroll
 			for (int t = 0; t < kAdfPairsPerLane; ++t) {
 				const int p = lane + 32 * t;
-				if (p < P) {
-					const int a = p / r1, c = p - a * r1;
-					double fa = 0, bc = 0;
-#pragma unroll
-					for (int q = 0; q < kAdfMaxR; ++q) {
-						fa = (q == a) ? fj[q] : fa;
-						bc = (q == c) ? bj[q] : bc;
-					}
-					const double contrib = rj * fa * bc;
-#pragma unroll
-					for (int i = 0; i < kAdfMaxSlices; ++i) acc[i][t] += (i == ij) ? contrib : 0.0;
-				}
+				if (p < P) gi[p] += (rj * fj[pa[t]]) * bj[pc[t]];
 			}
 		}
+		__syncwarp();
 	}
 	// per-warp partials: G stored (r0, n, r1)
 	double* gp = gpart + warp * (long long)r0 * n * r1;
-#pragma unroll
-	for (int t = 0; t < kAdfPairsPerLane; ++t) {
-		const int p = lane + 32 * t;
-		if (p < P) {
-			const int a = p / r1, c = p - a * r1;
-			for (int i = 0; i < n; ++i) gp[(a * n + i) * r1 + c] = acc[i][t];
-		}
+	for (int e = lane; e < n * P; e += 32) {
+		const int i = e / P, p = e - i * P, a = p / r1, c = p - a * r1;
+		gp[(a * n + i) * r1 + c] = G[e];
 	}
 	rr = warp_sum(rr);
 	if (lane == 0 && rrpart) rrpart[warp] = rr;
@@ -153,27 +150,35 @@ __global__ void k_adf_grad_generic(AdfLevel L, const double* res, double* G) {
 	}
 }
 
-// sum of `parts` partial arrays of length len, in order
+// out[e] = scale * sum over `parts` partial arrays of length len: one block per
+// element, threads take the partials in a fixed stride, then a fixed-order
+// block reduction (deterministic).
 __global__ void k_sum_parts(const double* part, long long parts, int len, double* out, double scale) {
-	for (int e = blockIdx.x * blockDim.x + threadIdx.x; e < len; e += gridDim.x * blockDim.x) {
+	__shared__ double sc[32];
+	for (int e = blockIdx.x; e < len; e += gridDim.x) {
 		double s = 0.0;
-		for (long long p = 0; p < parts; ++p) s += part[p * len + e];
-		out[e] = scale * s;
+		for (long long p = threadIdx.x; p < parts; p += blockDim.x) s += part[p * len + e];
+		s = block_sum(s, sc);
+		if (threadIdx.x == 0) out[e] = scale * s;
 	}
+}
+
+static void sum_parts(Context& c, const double* part, long long parts, int len, double* out, double scale) {
+	k_sum_parts<<<unsigned(std::min(len, 4096)), 128, 0, c.stream>>>(part, parts, len, out, scale);
+	c.count_launch();
 }
 
 // slice norms: nrm_i = sum_{s: i_s = i} (F[s]^T G[:, i_s, :] B[s])^2, per-warp partials (n values)
 __global__ void __launch_bounds__(kAdfThreads) k_adf_slicenorm(AdfLevel L, const double* G, double* npart,
                                                                 long long chunk) {
 	__shared__ double Gs[kAdfMaxR * kAdfMaxSlices * kAdfMaxR];
-	const int lane = threadIdx.x & 31;
-	const long long warp = (long long)blockIdx.x * kAdfWarpsPerBlock + (threadIdx.x >> 5);
+	__shared__ double Aw[kAdfWarpsPerBlock][kAdfMaxSlices][33];  // lane-private accumulators per slice
+	const int lane = threadIdx.x & 31, wib = threadIdx.x >> 5;
+	const long long warp = (long long)blockIdx.x * kAdfWarpsPerBlock + wib;
 	const int r0 = L.r0, n = L.n, r1 = L.r1;
 	for (int e = threadIdx.x; e < r0 * n * r1; e += blockDim.x) Gs[e] = G[e];
+	for (int i = 0; i < kAdfMaxSlices; ++i) Aw[wib][i][lane] = 0.0;
 	__syncthreads();
-	double acc[kAdfMaxSlices];
-#pragma unroll
-	for (int i = 0; i < kAdfMaxSlices; ++i) acc[i] = 0.0;
 	const long long s0 = warp * chunk, s1 = min(L.N, s0 + chunk);
 	for (long long s = s0 + lane; s < s1; s += 32) {
 		const int idx = L.pos[s];
@@ -184,14 +189,13 @@ __global__ void __launch_bounds__(kAdfThreads) k_adf_slicenorm(AdfLevel L, const
 			for (int c = 0; c < r1; ++c) t += gr[c] * (L.B ? L.B[c * L.N + s] : 1.0);
 			v += (L.F ? L.F[a * L.N + s] : 1.0) * t;
 		}
-		const double v2 = v * v;
-#pragma unroll
-		for (int i = 0; i < kAdfMaxSlices; ++i) acc[i] += (i == idx) ? v2 : 0.0;
+		Aw[wib][idx][lane] += v * v;
 	}
-#pragma unroll
-	for (int i = 0; i < kAdfMaxSlices; ++i) acc[i] = warp_sum(acc[i]);
-	if (lane == 0)
-		for (int i = 0; i < n; ++i) npart[warp * n + i] = acc[i];
+	__syncwarp();
+	for (int i = 0; i < n; ++i) {
+		const double t = warp_sum(Aw[wib][i][lane]);
+		if (lane == 0) npart[warp * n + i] = t;
+	}
 }
 
 __global__ void k_adf_slicenorm_generic(AdfLevel L, const double* G, double* nrm) {
@@ -312,7 +316,7 @@ struct AdfData {
 			fo += size_t(x.ranks[k + 1]) * N;
 			bo += size_t(x.ranks[k]) * N;
 		}
-		warps = std::max<long long>(1, std::min<long long>((N + 127) / 128, (long long)c.num_sms * kAdfWarpsPerBlock * 2));
+		warps = std::max<long long>(1, std::min<long long>((N + 255) / 256, (long long)c.num_sms * 16));
 		warps = (warps + kAdfWarpsPerBlock - 1) / kAdfWarpsPerBlock * kAdfWarpsPerBlock;
 		chunk = (N + warps - 1) / warps;
 		gpart = c.scratch<double>(S_ADF_FIRST + 3, size_t(warps) * maxr * maxn * maxr);
@@ -342,9 +346,9 @@ struct AdfData {
 		if (fast) {
 			ProfScope ps(c, "adf_res_grad");
 			k_adf_res_grad<<<blocks(), kAdfThreads, 0, c.stream>>>(L, y, res, mode, gpart, rrpart, chunk);
-			k_sum_parts<<<std::max(1, (len + 127) / 128), 128, 0, c.stream>>>(gpart, warps, len, Gout, gscale);
-			k_sum_parts<<<1, 32, 0, c.stream>>>(rrpart, warps, 1, rr, 1.0);
-			c.count_launch(3);
+			sum_parts(c, gpart, warps, len, Gout, gscale);
+			sum_parts(c, rrpart, warps, 1, rr, 1.0);
+			c.count_launch();
 		} else {
 			if (mode == 0) k_adf_res_generic<<<std::max<long long>(1, std::min<long long>((N + 255) / 256, 4096)), 256, 0, c.stream>>>(L, y, res);
 			k_adf_grad_generic<<<std::max(1, (len + 127) / 128), 128, 0, c.stream>>>(L, res, Gout);
@@ -360,8 +364,8 @@ struct AdfData {
 		if (fast) {
 			ProfScope ps(c, "adf_slicenorm");
 			k_adf_slicenorm<<<blocks(), kAdfThreads, 0, c.stream>>>(L, G, npart, chunk);
-			k_sum_parts<<<1, 32, 0, c.stream>>>(npart, warps, L.n, nrm, 1.0);
-			c.count_launch(2);
+			sum_parts(c, npart, warps, L.n, nrm, 1.0);
+			c.count_launch();
 		} else {
 			k_adf_slicenorm_generic<<<1, 32, 0, c.stream>>>(L, G, nrm);
 			c.count_launch();

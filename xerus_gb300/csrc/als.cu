@@ -164,13 +164,14 @@ __device__ CgOut cg_body(const CgParams<T>& a, GemmSmem<T>& sm, Grp& grp) {
 	}
 	const double tol2 = a.tol * a.tol * bb;
 	int it = 0;
+	CgFloor floor_check;
 	while (rr > tol2 && it < a.max_iter) {
 		T blk = 0;
 		if (!matvec_dev(a.plan, a.p, a.q, a.p, sm, grp, blk)) return out;
 		const double pAp = grp.total(double(blk), ok);
 		if (!ok) return out;
 		if (!(pAp > 0.0) || !isfinite(pAp)) {
-			grp.record(DEV_BREAKDOWN);
+			if (cg_breakdown_is_error(rr, bb)) grp.record(DEV_BREAKDOWN);
 			break;
 		}
 		const double alpha = rr / pAp;
@@ -189,6 +190,7 @@ __device__ CgOut cg_body(const CgParams<T>& a, GemmSmem<T>& sm, Grp& grp) {
 		for (long long i = gt; i < a.n; i += gs) a.p[i] = a.r[i] + T(beta) * a.p[i];
 		if (!grp.sync()) return out;
 		++it;
+		if (floor_check.stalled(rr, it)) break;  // identical in every CTA
 	}
 	out.iterations = it;
 	out.rel_residual = sqrt(rr / bb);

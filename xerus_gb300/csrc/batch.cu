@@ -25,12 +25,13 @@
 #include <vector>
 
 #include "als.cuh"
+#include "blk_qr.cuh"
 #include "local_op.cuh"
 
 namespace xtt {
 
 constexpr int kBMaxD = 16;
-constexpr int kBMaxR = 64;
+constexpr int kBMaxR = kBlkQrMaxCols;
 constexpr int kBMaxHalfSweeps = 1024;  // bound of a launch that stops on the energy criterion
 
 struct BInst {
@@ -64,12 +65,9 @@ struct BArgs {
 };
 
 struct BShared {
+	BlkQrSmem qr;
 	double red[32];
 	float redf[32];
-	double coef[4];
-	double tau[kBMaxR];
-	double sw[kBMaxR];
-	double part[16 * kBMaxR];
 	long long opoff[kBMaxD + 2], rhoff[kBMaxD + 2];
 	int ibuf;
 };
@@ -113,115 +111,6 @@ __device__ void blk_copy(D* dst, const S* src, long long n) {
 	__syncthreads();
 }
 
-// Householder QR (unpivoted, LAPACK dgeqrf/dorg2r conventions) of the m x n
-// matrix A (transpose: of A^T) by one CTA, in the workspace W (mw x nw).
-// Writes C (kq x nw; transposed: nw x kq) and, if want_q, Q (mw x kq;
-// transposed: kq x mw). nw <= kBMaxR.
-__device__ void blk_qr(const double* A, long long lda, int m, int n, int transpose, double* W, double* C, double* Q,
-                       bool want_q, BShared& sh) {
-	const int tid = threadIdx.x, nt = blockDim.x, warp = tid >> 5, lane = tid & 31, nwarps = nt >> 5;
-	const int mw = transpose ? n : m, nw = transpose ? m : n, kq = min(mw, nw);
-	auto w = [&](int i, int j) -> double& { return W[(long long)i * nw + j]; };
-	for (long long e = tid; e < (long long)mw * nw; e += nt) {
-		const int i = int(e / nw), j = int(e % nw);
-		W[e] = transpose ? A[(long long)j * lda + i] : A[(long long)i * lda + j];
-	}
-	__syncthreads();
-	for (int j = 0; j < kq; ++j) {
-		double part = 0;
-		for (int i = j + 1 + tid; i < mw; i += nt) part = fma(w(i, j), w(i, j), part);
-		const double xn2 = block_sum(part, sh.red);
-		if (tid == 0) {
-			const double alpha = w(j, j);
-			double t = 0, scal = 1.0, beta = alpha;
-			if (xn2 != 0.0) {
-				beta = -copysign(sqrt(alpha * alpha + xn2), alpha);
-				t = (beta - alpha) / beta;
-				scal = 1.0 / (alpha - beta);
-			}
-			sh.tau[j] = t;
-			sh.coef[0] = scal;
-			sh.coef[1] = beta;
-		}
-		__syncthreads();
-		const double scal = sh.coef[0], tj = sh.tau[j];
-		for (int i = j + 1 + tid; i < mw; i += nt) w(i, j) *= scal;
-		if (tid == 0) w(j, j) = sh.coef[1];
-		__syncthreads();
-		const int c0 = j + 1, Cn = nw - c0;
-		if (Cn > 0) {
-			const int ncw = (Cn + 31) >> 5, G = max(1, nwarps / ncw);
-			const int g = warp / ncw, ci = (warp % ncw) * 32 + lane, rows = mw - j, chunk = (rows + G - 1) / G;
-			const int ia = j + g * chunk, ib = min(mw, ia + chunk);
-			if (g < G && ci < Cn) {
-				const int c = c0 + ci;
-				double acc = 0;
-				for (int i = ia; i < ib; ++i) acc = fma(i == j ? 1.0 : w(i, j), w(i, c), acc);
-				sh.part[g * kBMaxR + ci] = acc;
-			}
-			__syncthreads();
-			if (tid < Cn) {
-				double s = 0;
-				for (int gg = 0; gg < G; ++gg) s += sh.part[gg * kBMaxR + tid];
-				sh.sw[c0 + tid] = tj * s;
-			}
-			__syncthreads();
-			if (g < G && ci < Cn) {
-				const int c = c0 + ci;
-				const double wc = sh.sw[c];
-				for (int i = ia; i < ib; ++i) w(i, c) = fma(-wc, i == j ? 1.0 : w(i, j), w(i, c));
-			}
-			__syncthreads();
-		}
-	}
-	for (long long e = tid; e < (long long)kq * nw; e += nt) {
-		const int r = int(e / nw), c = int(e % nw);
-		const double v = (r <= c) ? w(r, c) : 0.0;
-		if (!transpose) C[(long long)r * nw + c] = v;
-		else C[(long long)c * kq + r] = v;
-	}
-	__syncthreads();
-	if (!want_q) return;
-	for (int j = kq - 1; j >= 0; --j) {
-		const double tj = sh.tau[j];
-		const int c0 = j + 1, Cn = kq - c0;
-		if (Cn > 0) {
-			const int ncw = (Cn + 31) >> 5, G = max(1, nwarps / ncw);
-			const int g = warp / ncw, ci = (warp % ncw) * 32 + lane, rows = mw - j - 1, chunk = (rows + G - 1) / G;
-			const int ia = j + 1 + g * chunk, ib = min(mw, ia + chunk);
-			if (g < G && ci < Cn) {
-				const int c = c0 + ci;
-				double acc = 0;
-				for (int i = ia; i < ib; ++i) acc = fma(w(i, j), w(i, c), acc);
-				sh.part[g * kBMaxR + ci] = acc;
-			}
-			__syncthreads();
-			if (tid < Cn) {
-				double s = 0;
-				for (int gg = 0; gg < G; ++gg) s += sh.part[gg * kBMaxR + tid];
-				sh.sw[c0 + tid] = tj * s;
-			}
-			__syncthreads();
-			if (g < G && ci < Cn) {
-				const int c = c0 + ci;
-				const double wc = sh.sw[c];
-				for (int i = ia; i < ib; ++i) w(i, c) = fma(-wc, w(i, j), w(i, c));
-				if (g == 0) w(j, c) = -wc;
-			}
-			__syncthreads();
-		}
-		for (int i = tid; i < mw; i += nt) w(i, j) = i > j ? -tj * w(i, j) : (i == j ? 1.0 - tj : 0.0);
-		__syncthreads();
-	}
-	for (long long e = tid; e < (long long)mw * kq; e += nt) {
-		const int i = int(e / kq), c = int(e % kq);
-		const double v = w(i, c);
-		if (!transpose) Q[(long long)i * kq + c] = v;
-		else Q[(long long)c * mw + i] = v;
-	}
-	__syncthreads();
-}
-
 // ------------------------------------------------------------ one instance
 
 struct BInstance {
@@ -253,7 +142,7 @@ struct BInstance {
 	__device__ void move_right(int k) {
 		const int m = I.rx[k] * I.n[k], nc = I.rx[k + 1];
 		double *Q = ws + a.lay.qq, *C = ws + a.lay.qc, *T = ws + a.lay.tg;
-		blk_qr(I.x[k], nc, m, nc, 0, ws + a.lay.qw, C, Q, true, sh);
+		blk_qr(I.x[k], nc, m, nc, 0, ws + a.lay.qw, C, Q, true, sh.qr);
 		Gemm<double> g;  // T = C (nc x nc) * core_{k+1} (nc x n r2)
 		const int n2r2 = I.n[k + 1] * I.rx[k + 2];
 		g.M = nc; g.N = n2r2; g.K = nc;
@@ -268,7 +157,7 @@ struct BInstance {
 	__device__ void move_left(int k) {
 		const int m = I.rx[k], nc = I.n[k] * I.rx[k + 1];
 		double *Q = ws + a.lay.qq, *C = ws + a.lay.qc, *T = ws + a.lay.tg;
-		blk_qr(I.x[k], nc, m, nc, 1, ws + a.lay.qw, C, Q, true, sh);
+		blk_qr(I.x[k], nc, m, nc, 1, ws + a.lay.qw, C, Q, true, sh.qr);
 		Gemm<double> g;  // T = core_{k-1} (r n x m) * C (m x m)
 		const int rn = I.rx[k - 1] * I.n[k - 1];
 		g.M = rn; g.N = m; g.K = m;
@@ -344,11 +233,12 @@ struct BInstance {
 		const int maxit = a.max_iter > 0 ? a.max_iter : int(min(10 * n + 100, (long long)1 << 30));
 		const double tol2 = a.tol * a.tol * bb;
 		int it = 0;
+		CgFloor floor_check;
 		while (bb > 0 && rr > tol2 && it < maxit) {
 			cc_matvec(s, s.rb, mp, q);
 			const double pAp = dot(p, q, n);
 			if (!(pAp > 0.0) || !isfinite(pAp)) {
-				if (threadIdx.x == 0) record_status(a.status, DEV_BREAKDOWN);
+				if (threadIdx.x == 0 && cg_breakdown_is_error(rr, bb)) record_status(a.status, DEV_BREAKDOWN);
 				break;
 			}
 			const double alpha = rr / pAp;
@@ -365,6 +255,7 @@ struct BInstance {
 			for (long long e = threadIdx.x; e < n; e += blockDim.x) p[e] = fma(beta, p[e], r[e]);
 			__syncthreads();
 			++it;
+			if (floor_check.stalled(rr, it)) break;
 		}
 		if (bb == 0) blk_copy(x, b, n);  // b_loc = 0: x = 0
 		iters += it;

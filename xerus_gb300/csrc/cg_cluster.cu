@@ -14,7 +14,8 @@
 // (remote stores do not stall the issuing warp), and one hardware cluster
 // barrier later each CTA holds the whole vector. Dot products are pushed the
 // same way (one partial per CTA) and summed in rank order, so every CTA takes
-// bit-identical, uniform decisions. Three cluster barriers per CG iteration.
+// bit-identical, uniform decisions. Three cluster barriers per CG iteration
+// (the push of p, p^T M p, r^T r).
 //
 // Precision. FP64 form: everything in double. Mixed form: the CG runs in FP32
 // on FP32 copies of L, A and R converted on load; each correction is checked
@@ -52,8 +53,8 @@ static CcLayout cc_layout(const CcShape& s, bool mixed) {
 	const size_t w = mixed ? sizeof(float) : sizeof(double);
 	CcLayout l;
 	size_t o = 0;
-	l.red = o;  // 4 arrays of 16 doubles
-	o = align16(o + 4 * kCcMaxCluster * sizeof(double));
+	l.red = o;  // reduction slots: 6 arrays of 16 doubles
+	o = align16(o + 6 * kCcMaxCluster * sizeof(double));
 	l.pf = o;  // the gathered vector: FP32 p or, in the mixed form, the FP64 iterate
 	o = align16(o + s.n_pf() * (mixed ? sizeof(double) : w));
 	l.L = o;
@@ -100,31 +101,52 @@ struct CcArgs {
 template <class T>
 __device__ void cc_push(T* pf, const T* v, int M1, int bwl, int b0, int ldp, int P) {
 	cgx::cluster_group cl = cgx::this_cluster();
+	T* dst[kCcMaxCluster];
+#pragma unroll
+	for (int q = 0; q < kCcMaxCluster; ++q) dst[q] = cl.map_shared_rank(pf, q < P ? q : 0);
 	const int n = M1 * bwl;
-	for (int q = 0; q < P; ++q) {
-		T* dst = cl.map_shared_rank(pf, q);
-		for (int e = threadIdx.x; e < n; e += kCcThreads) {
-			const int rho = e / bwl, bl = e - rho * bwl;
-			dst[(size_t)rho * ldp + b0 + bl] = v[e];
-		}
+	for (int e = threadIdx.x; e < n; e += blockDim.x) {
+		const int rho = e / bwl, bl = e - rho * bwl;
+		const size_t off = (size_t)rho * ldp + b0 + bl;
+		const T val = v[e];
+#pragma unroll
+		for (int q = 0; q < kCcMaxCluster; ++q)
+			if (q < P) dst[q][off] = val;
 	}
 }
 
-// Sum over the cluster of one value per CTA (`mine`, equal in all threads):
-// partials are pushed into slot[rank] of every CTA, then summed in rank order
-// by thread 0 and broadcast. Consecutive calls must use different slot arrays.
-template <class T>
-__device__ T cc_total(T mine, T* slots, T* bcast, int me, int P) {
+// Sums over the cluster of N values per CTA (`mine`, equal in all threads):
+// partials are pushed into slots[N rank + i] of every CTA, then summed in rank
+// order by thread 0 and broadcast, so every CTA gets bit-identical totals. A
+// slot array may be reused by the next call only after another cluster barrier.
+template <class T, int N>
+__device__ void cc_total(const T (&mine)[N], T* slots, T* bcast, int me, int P, T (&tot)[N]) {
 	cgx::cluster_group cl = cgx::this_cluster();
-	if ((int)threadIdx.x < P) cl.map_shared_rank(slots, (int)threadIdx.x)[me] = mine;
+	if ((int)threadIdx.x < P) {
+		T* d = cl.map_shared_rank(slots, (int)threadIdx.x);
+#pragma unroll
+		for (int i = 0; i < N; ++i) d[N * me + i] = mine[i];
+	}
 	cl.sync();
 	if (threadIdx.x == 0) {
-		T s = T(0);
-		for (int p = 0; p < P; ++p) s += slots[p];
-		*bcast = s;
+#pragma unroll
+		for (int i = 0; i < N; ++i) {
+			T s = T(0);
+			for (int p = 0; p < P; ++p) s += slots[N * p + i];
+			bcast[i] = s;
+		}
 	}
 	__syncthreads();
-	return *bcast;
+#pragma unroll
+	for (int i = 0; i < N; ++i) tot[i] = bcast[i];
+}
+
+template <class T>
+__device__ T cc_total(T mine, T* slots, T* bcast, int me, int P) {
+	const T m1[1] = {mine};
+	T t1[1];
+	cc_total<T, 1>(m1, slots, bcast, me, P, t1);
+	return t1[0];
 }
 
 template <class T>
@@ -147,6 +169,8 @@ __host__ __device__ void cc_load_operands(const CcArgs& a, int b0, int bwl, T* L
 // CG on this CTA's slices (x, r, p, q, b of length M1 * bwl) for M v = b:
 // from x (zero_guess: x = 0), to ||r|| <= tol ||b|| or max_iter iterations.
 // Returns the iteration count; rel receives ||r|| / ||b|| of the recursion.
+// p^T M p is formed directly each iteration (not by a recurrence), which keeps
+// the breakdown test meaningful down to the 1e-13 tolerances of the FP64 form.
 template <class T>
 __device__ int cc_cg(const CcShape& s, int me, int P, int b0, int bwl, const Mv<T>& m, T* pf, T* x, T* r, T* p, T* q,
                      const T* b, bool zero_guess, double tol, int max_iter, T* slots, T* bcast, int* status,
@@ -154,7 +178,7 @@ __device__ int cc_cg(const CcShape& s, int me, int P, int b0, int bwl, const Mv<
 	const int tid = threadIdx.x, n = s.M1() * bwl, M1 = s.M1(), ldp = s.ldp();
 	__shared__ T sc[32];
 	if (zero_guess) {
-		for (int e = tid; e < n; e += kCcThreads) {
+		for (int e = tid; e < n; e += blockDim.x) {
 			x[e] = T(0);
 			r[e] = b[e];
 			p[e] = b[e];
@@ -164,7 +188,7 @@ __device__ int cc_cg(const CcShape& s, int me, int P, int b0, int bwl, const Mv<
 		cc_push(pf, x, M1, bwl, b0, ldp, P);
 		cgx::this_cluster().sync();
 		cc_matvec(s, bwl, m, q);
-		for (int e = tid; e < n; e += kCcThreads) {
+		for (int e = tid; e < n; e += blockDim.x) {
 			const T v = b[e] - q[e];
 			r[e] = v;
 			p[e] = v;
@@ -172,47 +196,58 @@ __device__ int cc_cg(const CcShape& s, int me, int P, int b0, int bwl, const Mv<
 		__syncthreads();
 	}
 	T rl = 0, bl = 0;
-	for (int e = tid; e < n; e += kCcThreads) {
+	for (int e = tid; e < n; e += blockDim.x) {
 		rl = fma(r[e], r[e], rl);
 		bl = fma(b[e], b[e], bl);
 	}
 	rl = block_sum(rl, sc);
 	bl = block_sum(bl, sc);
-	const T bb = cc_total(bl, slots + 0 * kCcMaxCluster, bcast, me, P);
-	T rr = cc_total(rl, slots + 1 * kCcMaxCluster, bcast, me, P);
+	T tot[2];
+	{
+		const T mine[2] = {bl, rl};
+		cc_total<T, 2>(mine, slots, bcast, me, P, tot);
+	}
+	const T bb = tot[0];
+	T rr = tot[1];
 	if (bb == T(0)) {
-		for (int e = tid; e < n; e += kCcThreads) x[e] = T(0);
+		for (int e = tid; e < n; e += blockDim.x) x[e] = T(0);
 		__syncthreads();
 		rel = 0;
 		return 0;
 	}
 	const T tol2 = T(tol * tol) * bb;
+	T* s_pap = slots + 2 * kCcMaxCluster;
+	T* s_rr = slots + 3 * kCcMaxCluster;
 	int it = 0;
+	CgFloor floor_check;
 	while (rr > tol2 && it < max_iter) {
 		cc_push(pf, p, M1, bwl, b0, ldp, P);
 		cgx::this_cluster().sync();
 		cc_matvec(s, bwl, m, q);
 		T l = 0;
-		for (int e = tid; e < n; e += kCcThreads) l = fma(p[e], q[e], l);
-		const T pAp = cc_total(block_sum(l, sc), slots + 2 * kCcMaxCluster, bcast, me, P);
+		for (int e = tid; e < n; e += blockDim.x) l = fma(p[e], q[e], l);
+		const T pAp = cc_total(block_sum(l, sc), s_pap, bcast, me, P);
 		if (!(pAp > T(0)) || !isfinite(double(pAp))) {
-			if (tid == 0 && me == 0) record_status(status, DEV_BREAKDOWN);
+			// an FP32 correction solve just stops: the FP64 refinement around it decides
+			if (sizeof(T) == 8 && tid == 0 && me == 0 && cg_breakdown_is_error(double(rr), double(bb)))
+				record_status(status, DEV_BREAKDOWN);
 			break;
 		}
 		const T alpha = rr / pAp;
 		l = 0;
-		for (int e = tid; e < n; e += kCcThreads) {
+		for (int e = tid; e < n; e += blockDim.x) {
 			x[e] = fma(alpha, p[e], x[e]);
 			const T v = fma(-alpha, q[e], r[e]);
 			r[e] = v;
 			l = fma(v, v, l);
 		}
-		const T rrn = cc_total(block_sum(l, sc), slots + 1 * kCcMaxCluster, bcast, me, P);
+		const T rrn = cc_total(block_sum(l, sc), s_rr, bcast, me, P);
 		const T beta = rrn / rr;
 		rr = rrn;
-		for (int e = tid; e < n; e += kCcThreads) p[e] = fma(beta, p[e], r[e]);
+		for (int e = tid; e < n; e += blockDim.x) p[e] = fma(beta, p[e], r[e]);
 		__syncthreads();
 		++it;
+		if (floor_check.stalled(double(rr), it)) break;  // identical in every CTA
 	}
 	rel = sqrt(double(rr) / double(bb));
 	return it;
@@ -252,7 +287,7 @@ __global__ void __launch_bounds__(kCcThreads) k_cg_cluster_f64(CcArgs a) {
 	const int M1 = s.M1(), n = M1 * bwl, tid = threadIdx.x;
 	CcView<double> v(smem, s, a.lay);
 	double* slots = reinterpret_cast<double*>(smem + a.lay.red);
-	__shared__ double bcast;
+	__shared__ double bcast[4];
 	cc_load_operands(a, b0, bwl, v.L, v.A1, v.A2, v.R);
 	for (int e = tid; e < n; e += kCcThreads) {
 		const int rho = e / bwl, bl = e - rho * bwl;
@@ -261,8 +296,8 @@ __global__ void __launch_bounds__(kCcThreads) k_cg_cluster_f64(CcArgs a) {
 	}
 	__syncthreads();
 	double rel = 0;
-	const int it = cc_cg<double>(s, me, P, b0, bwl, v.mv(s), v.pf, v.x, v.r, v.p, v.q, v.b, false, a.tol, a.max_iter,
-	                             slots, &bcast, a.status, rel);
+	const int it = cc_cg<double>(s, me, P, b0, bwl, v.mv(s), v.pf, v.x, v.r, v.p, v.q, v.b, false, a.tol,
+	                             a.max_iter, slots, bcast, a.status, rel);
 	for (int e = tid; e < n; e += kCcThreads) {
 		const int rho = e / bwl, bl = e - rho * bwl;
 		a.x[(size_t)rho * s.rb + b0 + bl] = v.x[e];
@@ -286,8 +321,8 @@ __global__ void __launch_bounds__(kCcThreads) k_cg_cluster_mixed(CcArgs a) {
 	double* r64 = reinterpret_cast<double*>(smem + a.lay.r64);
 	double* dslots = reinterpret_cast<double*>(smem + a.lay.red);
 	float* fslots = reinterpret_cast<float*>(dslots + 2 * kCcMaxCluster);
-	__shared__ double dbc;
-	__shared__ float fbc;
+	__shared__ double dbc[4];
+	__shared__ float fbc[4];
 	__shared__ double dsc[32];
 	cc_load_operands(a, b0, bwl, v.L, v.A1, v.A2, v.R);
 	// FP64 operands straight from global memory (read-only during the launch)
@@ -300,7 +335,7 @@ __global__ void __launch_bounds__(kCcThreads) k_cg_cluster_mixed(CcArgs a) {
 		const double bv = a.b[(size_t)rho * s.rb + b0 + b];
 		bl = fma(bv, bv, bl);
 	}
-	const double bb = cc_total(block_sum(bl, dsc), dslots, &dbc, me, P);
+	const double bb = cc_total(block_sum(bl, dsc), dslots, dbc, me, P);
 	int iters = 0, refs = 0;
 	double rel = 0;
 	for (int ref = 0; ref <= a.max_refine; ++ref) {
@@ -318,7 +353,7 @@ __global__ void __launch_bounds__(kCcThreads) k_cg_cluster_mixed(CcArgs a) {
 			r64[e] = rv;
 			l = fma(rv, rv, l);
 		}
-		const double rr = cc_total(block_sum(l, dsc), dslots + kCcMaxCluster, &dbc, me, P);
+		const double rr = cc_total(block_sum(l, dsc), dslots + kCcMaxCluster, dbc, me, P);
 		rel = bb > 0 ? sqrt(rr / bb) : 0.0;
 		if (rr <= a.tol * a.tol * bb || ref == a.max_refine) break;
 		const double nr = sqrt(rr);
@@ -326,7 +361,7 @@ __global__ void __launch_bounds__(kCcThreads) k_cg_cluster_mixed(CcArgs a) {
 		__syncthreads();  // the FP32 CG below overwrites the region that held the FP64 iterate
 		double irel = 0;
 		iters += cc_cg<float>(s, me, P, b0, bwl, v.mv(s), v.pf, v.x, v.r, v.p, v.q, v.b, true, a.inner_tol,
-		                      a.max_iter, fslots, &fbc, a.status, irel);
+		                      a.max_iter, fslots, fbc, a.status, irel);
 		for (int e = tid; e < n; e += kCcThreads) {
 			const int rho = e / bwl, b = e - rho * bwl;
 			double* xp = a.x + (size_t)rho * s.rb + b0 + b;

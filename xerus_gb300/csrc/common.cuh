@@ -41,6 +41,27 @@ enum DeviceStatus : int {
 	DEV_CAPACITY = 4,       // a launch got a size beyond what it was built for
 };
 
+// Conjugate gradients on an SPD system whose tolerance lies below its rounding
+// floor stagnate, and p^T M p can then round to <= 0. Both are the floor, not
+// an indefinite operator, once the relative residual is small: a breakdown is
+// an error only while ||r|| > 1e-6 ||b||.
+__host__ __device__ __forceinline__ bool cg_breakdown_is_error(double rr, double bb) { return rr > 1e-12 * bb; }
+
+// Stagnation test: every 256 iterations the smallest ||r||^2 of the window must
+// improve on the best of the earlier windows by 1%, else the solve stops at its
+// floor (slow but genuine convergence, condition numbers up to ~1e8, passes).
+struct CgFloor {
+	double best = 1e300, window = 1e300;
+	__host__ __device__ bool stalled(double rr, int it) {
+		if (rr < window) window = rr;
+		if (it % 256 != 0) return false;
+		const bool stop = !(window < 0.99 * best);
+		best = window < best ? window : best;
+		window = 1e300;
+		return stop;
+	}
+};
+
 __device__ __forceinline__ void record_status(int* status, int code) {
 	if (status) atomicCAS(status, DEV_OK, code);
 }

@@ -17,6 +17,7 @@
 
 #include <cooperative_groups.h>
 
+#include "blk_qr.cuh"
 #include "linalg.cuh"
 
 namespace xtt {
@@ -790,6 +791,20 @@ static int qr_cl2_size(int mw, int nw, Qc2Layout& lay) {
 	return P;
 }
 
+// Small unpivoted factorisations (the rank-6 cores of ADF's move_core, short
+// residual factors): one CTA of 128 threads running the block Householder QR,
+// the working copy in dynamic shared memory.
+constexpr int kQrSmallThreads = 128;
+constexpr int kQrSmallMaxRows = 512;
+
+__global__ void __launch_bounds__(kQrSmallThreads) k_qr_small(QrArgs a) {
+	extern __shared__ double w_small[];
+	__shared__ BlkQrSmem sh;
+	const int mw = a.transpose ? a.n : a.m, nw = a.transpose ? a.m : a.n;
+	blk_qr(a.A, a.lda, a.m, a.n, a.transpose, w_small, a.C, a.Q, a.want_q != 0, sh);
+	if (threadIdx.x == 0 && a.rank_out) *a.rank_out = mw < nw ? mw : nw;
+}
+
 // Cluster geometry for an mw x nw factorisation: 0 CTAs if the one-CTA kernel is used.
 static int qr_cluster_size(int mw, int nw, QcLayout& lay) {
 	if (mw < 48 || nw < 8) return 0;
@@ -804,6 +819,19 @@ static int qr_cluster_size(int mw, int nw, QcLayout& lay) {
 
 void launch_qr(const QrArgs& a, cudaStream_t s) {
 	const int mw = a.transpose ? a.n : a.m, nw = a.transpose ? a.m : a.n;
+	if (!a.pivot && (mw < 48 || nw < 8) && nw <= kBlkQrMaxCols && mw <= kQrSmallMaxRows) {
+		const size_t bytes = size_t(mw) * nw * sizeof(double);
+		static bool attr_s = false;
+		if (!attr_s) {
+			XTT_CUDA(cudaFuncSetAttribute(k_qr_small, cudaFuncAttributeMaxDynamicSharedMemorySize, int(kDynSmemMax)));
+			attr_s = true;
+		}
+		if (bytes <= kDynSmemMax) {
+			k_qr_small<<<1, kQrSmallThreads, bytes, s>>>(a);
+			XTT_CUDA(cudaGetLastError());
+			return;
+		}
+	}
 	if (!a.pivot) {
 		Qc2Layout l2;
 		const int P2 = qr_cl2_size(mw, nw, l2);

@@ -66,14 +66,29 @@ template <class T>
 __host__ __device__ void cc_matvec(const CcShape& s, int bwl, const Mv<T>& m, T* out) {
 	const int tid = CC_TID;
 	const int KL = s.KL(), M1 = s.M1(), c1 = bwl * KL, ld3 = s.ld3(), c3 = s.nI() * bwl;
-	// t1[rho][(bl, k)] = sum_b' pf[rho][b'] R[(bl, k)][b']
-	for (int e = tid; e < M1 * c1; e += CC_STRIDE) {
-		const int rho = e / c1, c = e - rho * c1;
+	// t1[rho][(bl, k)] = sum_b' pf[rho][b'] R[(bl, k)][b']: each thread one row and up to
+	// four columns (four independent accumulators; one read of the row per b')
+	const int ng = (c1 + 3) >> 2;
+	for (int e = tid; e < M1 * ng; e += CC_STRIDE) {
+		const int rho = e / ng, c0 = (e - rho * ng) * 4, cw = c1 - c0;
 		const T* xp = m.pf + (size_t)rho * m.ldp;
-		const T* rp = m.R + (size_t)c * m.ldr;
-		T acc = T(0);
-		for (int q = 0; q < s.rb; ++q) acc = fma(xp[q], rp[q], acc);
-		m.t1[e] = acc;
+		const T* r0 = m.R + (size_t)c0 * m.ldr;
+		const T* r1 = r0 + (cw > 1 ? m.ldr : 0);  // rows past the last column repeat row c0
+		const T* r2 = r0 + (cw > 2 ? 2 * m.ldr : 0);
+		const T* r3 = r0 + (cw > 3 ? 3 * m.ldr : 0);
+		T a0 = T(0), a1 = T(0), a2 = T(0), a3 = T(0);
+		for (int q = 0; q < s.rb; ++q) {
+			const T xv = xp[q];
+			a0 = fma(xv, r0[q], a0);
+			a1 = fma(xv, r1[q], a1);
+			a2 = fma(xv, r2[q], a2);
+			a3 = fma(xv, r3[q], a3);
+		}
+		T* o = m.t1 + (size_t)rho * c1 + c0;
+		o[0] = a0;
+		if (cw > 1) o[1] = a1;
+		if (cw > 2) o[2] = a2;
+		if (cw > 3) o[3] = a3;
 	}
 	CC_SYNC();
 	if (!s.two) {
