@@ -100,6 +100,7 @@ struct CgParams {
 	int max_iter;
 	double tol;
 	int zero_guess;
+	const int* gate = nullptr;  // run only if *gate != 0 (FP64 polish after a mixed solve)
 };
 
 struct CgOut {
@@ -171,7 +172,8 @@ __device__ CgOut cg_body(const CgParams<T>& a, GemmSmem<T>& sm, Grp& grp) {
 		const double pAp = grp.total(double(blk), ok);
 		if (!ok) return out;
 		if (!(pAp > 0.0) || !isfinite(pAp)) {
-			if (cg_breakdown_is_error(rr, bb)) grp.record(DEV_BREAKDOWN);
+			// an FP32 correction solve just stops: the FP64 refinement around it decides
+			if (sizeof(T) == 8 && cg_breakdown_is_error(rr, bb)) grp.record(DEV_BREAKDOWN);
 			break;
 		}
 		const double alpha = rr / pAp;
@@ -199,6 +201,7 @@ __device__ CgOut cg_body(const CgParams<T>& a, GemmSmem<T>& sm, Grp& grp) {
 
 template <class T, class Grp>
 __global__ void __launch_bounds__(kGemmThreads) k_cg(CgParams<T> a, Grp grp, int* out_i, double* out_d) {
+	if (a.gate && __ldcg(a.gate) == 0) return;  // uniform: every block reads the same flag
 	__shared__ GemmSmem<T> sm;
 	const CgOut o = cg_body(a, sm, grp);
 	if (grp.rank() == 0 && threadIdx.x == 0) {  // counters accumulate over a sweep
@@ -217,6 +220,7 @@ struct MixedParams {
 	long long n;
 	double tol;
 	int max_refine;
+	int* flag;               // 1 when the FP64 target was not reached, else 0
 };
 
 template <class Grp>
@@ -234,7 +238,8 @@ __global__ void __launch_bounds__(kGemmThreads) k_cg_mixed(MixedParams a, Grp gr
 	for (long long i = gt; i < a.n; i += gs) bl += a.b[i] * a.b[i];
 	const double bb = grp.total(block_sum(bl, sc), ok);
 	int iters = 0, refs = 0;
-	double rel = 0;
+	double rel = 0, rr_prev = 0, nr_prev = 0;
+	bool reached = false;
 	for (int ref = 0; ok && ref <= a.max_refine; ++ref) {
 		double dummy;
 		if (!matvec_dev(a.p64, a.x, a.q64, (const double*)nullptr, sm.d, grp, dummy)) break;
@@ -247,9 +252,21 @@ __global__ void __launch_bounds__(kGemmThreads) k_cg_mixed(MixedParams a, Grp gr
 		}
 		const double rr = grp.total(block_sum(l, sc), ok);
 		if (!ok) break;
+		if (ref > 0 && !(rr < rr_prev)) {
+			// the FP32 correction did not help: take it back, the FP64 polish finishes
+			for (long long i = gt; i < a.n; i += gs) a.x[i] -= nr_prev * double(a.inner.x[i]);
+			rel = bb > 0 ? sqrt(rr_prev / bb) : 0.0;
+			break;
+		}
 		rel = bb > 0 ? sqrt(rr / bb) : 0.0;
-		if (rr <= a.tol * a.tol * bb || ref == a.max_refine) break;
+		if (rr <= a.tol * a.tol * bb) {
+			reached = true;
+			break;
+		}
+		if (ref == a.max_refine) break;
 		const double nr = sqrt(rr);
+		rr_prev = rr;
+		nr_prev = nr;
 		for (long long i = gt; i < a.n; i += gs) const_cast<float*>(a.inner.b)[i] = float(a.q64[i] / nr);
 		if (!grp.sync()) break;
 		const CgOut o = cg_body(a.inner, sm.f, grp);
@@ -262,6 +279,7 @@ __global__ void __launch_bounds__(kGemmThreads) k_cg_mixed(MixedParams a, Grp gr
 		out_i[0] += iters;
 		out_i[1] += refs;
 		out_d[0] = rel;
+		if (a.flag) *a.flag = (reached || bb == 0.0) ? 0 : 1;
 	}
 	if (Grp::kCluster) grp.sync();
 }
@@ -327,17 +345,20 @@ CgResult local_solve(Context& c, const LocalShape& s, const double* L, const dou
 		chk.g[chk.ns - 1].C = x;
 		for (int i = 0; i < chk.ns; ++i) check_gemm(chk.g[i]);
 	}
-	CgResult res;
-	if (c.cg_path != XTT_CG_PATH_GRID && cluster_local_solve(c, s, L, A1, A2, R, b, x, tol, max_iter, precision))
-		return res;  // counters are read lazily by the driver (ctx d_ints[8..9], d_dbl[8])
+	CgResult res;  // counters are read lazily by the driver (ctx d_ints[8..9], d_dbl[8])
 	long long work = (n + kGemmThreads - 1) / kGemmThreads;
 	for (int i = 0; i < p64.ns; ++i) work = std::max(work, p64.g[i].tiles());
 	const bool use_cluster = n <= kClusterMaxN && c.cg_path != XTT_CG_PATH_GRID;
 	const int P = int(std::max<long long>(2, std::min<long long>(kCgClusterMax, work)));
 	int* oi = c.d_ints + 8;
 	double* od = c.d_dbl + 8;
+	int* flag = c.d_ints + 10;  // mixed solve: 1 when its FP64 target was not reached
 	ClusterGroup cgrp{c.d_status, 0};
-	if (precision == XTT_PRECISION_FP64) {
+	// FP64 CG from the current x; with `gate`, only when *gate != 0 (checked on the device)
+	auto fp64_solve = [&](const int* gate) {
+		if (c.cg_path != XTT_CG_PATH_GRID &&
+		    cluster_local_solve(c, s, L, A1, A2, R, b, x, tol, max_iter, XTT_PRECISION_FP64, nullptr, gate))
+			return;
 		CgParams<double> a;
 		a.plan = p64;
 		a.x = x;
@@ -349,6 +370,7 @@ CgResult local_solve(Context& c, const LocalShape& s, const double* L, const dou
 		a.max_iter = max_iter;
 		a.tol = tol;
 		a.zero_guess = 0;
+		a.gate = gate;
 		ProfScope ps(c, "cg_fp64");
 		if (!(use_cluster && launch_cluster(k_cg<double, ClusterGroup>, P, c.stream, a, cgrp, oi, od))) {
 			const int G = coop_grid(k_cg<double, GridGroup>, c, work);
@@ -357,7 +379,17 @@ CgResult local_solve(Context& c, const LocalShape& s, const double* L, const dou
 			XTT_CUDA(cudaLaunchCooperativeKernel((void*)k_cg<double, GridGroup>, dim3(G), dim3(kGemmThreads), args, 0, c.stream));
 		}
 		c.count_launch();
-	} else {
+	};
+	if (precision == XTT_PRECISION_FP64) {
+		fp64_solve(nullptr);
+		return res;
+	}
+	if (c.cg_path != XTT_CG_PATH_GRID &&
+	    cluster_local_solve(c, s, L, A1, A2, R, b, x, tol, max_iter, precision, flag, nullptr)) {
+		fp64_solve(flag);  // FP64 polish, a no-op unless the mixed solve fell short
+		return res;
+	}
+	{
 		// FP32 copies of the environments and operator cores
 		const size_t nL = size_t(s.ra) * s.K0 * s.ra, nA1 = size_t(s.K0) * s.n1 * s.n1 * s.K1;
 		const size_t nA2 = s.sites == 2 ? size_t(s.K1) * s.n2 * s.n2 * s.K2 : 0;
@@ -395,16 +427,20 @@ CgResult local_solve(Context& c, const LocalShape& s, const double* L, const dou
 		m.n = n;
 		m.tol = tol;
 		m.max_refine = 12;
-		ProfScope ps(c, "cg_mixed");
-		if (!(use_cluster && launch_cluster(k_cg_mixed<ClusterGroup>, P, c.stream, m, cgrp, oi, od))) {
-			const int G = coop_grid(k_cg_mixed<GridGroup>, c, work);
-			GridGroup g{GridBarrier{c.d_barrier, c.d_barrier + 1, c.d_status}, c.scratch<double>(S_ALS_FIRST + 26, 2 * size_t(G)), 0};
-			void* args[] = {&m, &g, &oi, &od};
-			XTT_CUDA(cudaLaunchCooperativeKernel((void*)k_cg_mixed<GridGroup>, dim3(G), dim3(kGemmThreads), args, 0, c.stream));
+		m.flag = flag;
+		{
+			ProfScope ps(c, "cg_mixed");
+			if (!(use_cluster && launch_cluster(k_cg_mixed<ClusterGroup>, P, c.stream, m, cgrp, oi, od))) {
+				const int G = coop_grid(k_cg_mixed<GridGroup>, c, work);
+				GridGroup g{GridBarrier{c.d_barrier, c.d_barrier + 1, c.d_status}, c.scratch<double>(S_ALS_FIRST + 26, 2 * size_t(G)), 0};
+				void* args[] = {&m, &g, &oi, &od};
+				XTT_CUDA(cudaLaunchCooperativeKernel((void*)k_cg_mixed<GridGroup>, dim3(G), dim3(kGemmThreads), args, 0, c.stream));
+			}
+			c.count_launch();
 		}
-		c.count_launch();
+		fp64_solve(flag);  // FP64 polish, a no-op unless the mixed solve fell short
 	}
-	return res;  // counters are read lazily by the driver (ctx d_ints[8..9], d_dbl[8])
+	return res;
 }
 
 // ------------------------------------------------------------ environment pushes

@@ -243,8 +243,11 @@ CgResult local_solve(Context& c, const LocalShape& s, const double* L, const dou
 // The same solve in one thread-block cluster with every operand in shared
 // memory (cg_cluster.cu); false when the system does not fit, in which case
 // nothing was launched.
+// Mixed form: *flag (device) becomes 1 when the FP64 target was not reached. FP64
+// form with gate != nullptr: the launch does nothing unless *gate != 0.
 bool cluster_local_solve(Context& c, const LocalShape& s, const double* L, const double* A1, const double* A2,
-                         const double* R, const double* b, double* x, double tol, int max_iter, int precision);
+                         const double* R, const double* b, double* x, double tol, int max_iter, int precision,
+                         int* flag = nullptr, const int* gate = nullptr);
 
 // y = M x once (FP64), host-launched chain.
 void local_matvec(Context& c, const LocalShape& s, const double* L, const double* A1, const double* A2,

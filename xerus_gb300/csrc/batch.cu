@@ -275,6 +275,8 @@ struct BInstance {
 		const Mv<float> m32 = mv<float>(s, pf, Lf, Af, Rf, f + a.lay.ft1, f + a.lay.ft3);
 		const double bb = dot(b, b, n);
 		const int maxit = a.max_iter > 0 ? a.max_iter : int(min(10 * n + 100, (long long)1 << 30));
+		bool reached = bb == 0;
+		double rr_prev = 0, nr_prev = 0;
 		for (int ref = 0; ref <= a.max_refine && bb > 0; ++ref) {
 			cc_matvec(s, s.rb, m64, q);
 			double l = 0;
@@ -284,8 +286,20 @@ struct BInstance {
 				l = fma(v, v, l);
 			}
 			const double rr64 = block_sum(l, sh.red);
-			if (rr64 <= a.tol * a.tol * bb || ref == a.max_refine) break;
+			if (ref > 0 && !(rr64 < rr_prev)) {
+				// the FP32 correction did not help: take it back, FP64 CG finishes below
+				for (long long e = threadIdx.x; e < n; e += blockDim.x) x[e] = fma(-nr_prev, double(xf[e]), x[e]);
+				__syncthreads();
+				break;
+			}
+			if (rr64 <= a.tol * a.tol * bb) {
+				reached = true;
+				break;
+			}
+			if (ref == a.max_refine) break;
 			const double nr = sqrt(rr64);
+			rr_prev = rr64;
+			nr_prev = nr;
 			float bl = 0;
 			for (long long e = threadIdx.x; e < n; e += blockDim.x) {
 				const float v = float(q[e] / nr);
@@ -324,6 +338,7 @@ struct BInstance {
 			__syncthreads();
 			iters += it;
 		}
+		if (!reached) cg64(k);  // from the best mixed iterate
 		if (bb == 0) blk_copy(x, b, n);
 	}
 

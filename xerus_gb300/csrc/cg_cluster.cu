@@ -94,6 +94,8 @@ struct CcArgs {
 	int* status = nullptr;
 	int* out_i = nullptr;
 	double* out_d = nullptr;
+	int* flag = nullptr;        // mixed form: 1 when the FP64 target was not reached, else 0
+	const int* gate = nullptr;  // FP64 form: run only if *gate != 0 (polish after a mixed solve)
 };
 
 // Every CTA writes its slice v[(rho, bl)] into column b0 + bl of the gathered
@@ -280,6 +282,7 @@ struct CcView {
 
 // FP64 form.
 __global__ void __launch_bounds__(kCcThreads) k_cg_cluster_f64(CcArgs a) {
+	if (a.gate && __ldcg(a.gate) == 0) return;  // uniform: every CTA reads the same flag
 	extern __shared__ __align__(16) unsigned char smem[];
 	cgx::cluster_group cl = cgx::this_cluster();
 	const CcShape& s = a.s;
@@ -337,7 +340,8 @@ __global__ void __launch_bounds__(kCcThreads) k_cg_cluster_mixed(CcArgs a) {
 	}
 	const double bb = cc_total(block_sum(bl, dsc), dslots, dbc, me, P);
 	int iters = 0, refs = 0;
-	double rel = 0;
+	double rel = 0, rr_prev = 0, nr_prev = 0;
+	bool reached = false;
 	for (int ref = 0; ref <= a.max_refine; ++ref) {
 		// r64 = b - M x (FP64), x gathered from global memory (L1 bypassed: other CTAs wrote it)
 		for (int e = tid; e < M1 * s.rb; e += kCcThreads) {
@@ -354,9 +358,26 @@ __global__ void __launch_bounds__(kCcThreads) k_cg_cluster_mixed(CcArgs a) {
 			l = fma(rv, rv, l);
 		}
 		const double rr = cc_total(block_sum(l, dsc), dslots + kCcMaxCluster, dbc, me, P);
+		if (ref > 0 && !(rr < rr_prev)) {
+			// the FP32 correction did not help (FP32 CG past its precision on this system):
+			// take it back and leave the rest to the FP64 polish
+			for (int e = tid; e < n; e += kCcThreads) {
+				const int rho = e / bwl, b = e - rho * bwl;
+				double* xp = a.x + (size_t)rho * s.rb + b0 + b;
+				*xp = fma(-nr_prev, double(v.x[e]), *xp);
+			}
+			rel = bb > 0 ? sqrt(rr_prev / bb) : 0.0;
+			break;
+		}
 		rel = bb > 0 ? sqrt(rr / bb) : 0.0;
-		if (rr <= a.tol * a.tol * bb || ref == a.max_refine) break;
+		if (rr <= a.tol * a.tol * bb) {
+			reached = true;
+			break;
+		}
+		if (ref == a.max_refine) break;
 		const double nr = sqrt(rr);
+		rr_prev = rr;
+		nr_prev = nr;
 		for (int e = tid; e < n; e += kCcThreads) v.b[e] = float(r64[e] / nr);
 		__syncthreads();  // the FP32 CG below overwrites the region that held the FP64 iterate
 		double irel = 0;
@@ -374,6 +395,7 @@ __global__ void __launch_bounds__(kCcThreads) k_cg_cluster_mixed(CcArgs a) {
 		a.out_i[0] += iters;
 		a.out_i[1] += refs;
 		a.out_d[0] = rel;
+		if (a.flag) *a.flag = (reached || bb == 0.0) ? 0 : 1;
 	}
 	cl.sync();
 }
@@ -439,7 +461,8 @@ static bool cc_launch(K kernel, const CcArgs& a, cudaStream_t st) {
 }
 
 bool cluster_local_solve(Context& c, const LocalShape& ls, const double* L, const double* A1, const double* A2,
-                         const double* R, const double* b, double* x, double tol, int max_iter, int precision) {
+                         const double* R, const double* b, double* x, double tol, int max_iter, int precision,
+                         int* flag, const int* gate) {
 	const bool mixed = precision != XTT_PRECISION_FP64;
 	CcArgs a;
 	if (!cc_plan(ls, mixed, a)) return false;
@@ -456,6 +479,8 @@ bool cluster_local_solve(Context& c, const LocalShape& ls, const double* L, cons
 	a.status = c.d_status;
 	a.out_i = c.d_ints + 8;
 	a.out_d = c.d_dbl + 8;
+	a.flag = flag;
+	a.gate = gate;
 	bool launched;
 	{
 		ProfScope ps(c, mixed ? "cg_mixed" : "cg_fp64");

@@ -1043,6 +1043,243 @@ __global__ void __launch_bounds__(kSvdThreads) k_svd(SvdArgs a, int use_smem) {
 	}
 }
 
+// ----------------------------------------------------------- cluster SVD
+//
+// The one-sided Jacobi SVD above with the pairs of each round-robin step spread
+// over the CTAs of one cluster (up to 16), so the FP64 work of a step runs on
+// up to 16 SMs: each CTA holds the columns of its pairs (the B part, p entries,
+// followed by the V part, q entries) in a double buffer in shared memory,
+// rotates its pairs (one warp per pair), and after one cluster barrier pulls
+// the columns its pairs need in the next step from wherever they were. The
+// sweep's convergence flag, the singular values, the rank and the order are
+// exchanged through distributed shared memory, so every CTA takes identical
+// decisions; each CTA writes its own columns of U, S and V^T.
+
+constexpr int kSvcThreads = 256;
+
+struct SvcLayout {
+	int p, q, qe, P, ppc, cpc;
+	__host__ __device__ size_t colw() const { return size_t(p) + q; }
+	__host__ __device__ size_t buf(int b) const { return size_t(b) * cpc * colw(); }
+	__host__ __device__ size_t sig() const { return 2 * size_t(cpc) * colw(); }
+	__host__ __device__ size_t flg() const { return sig() + qe; }
+	__host__ __device__ size_t ord() const { return flg() + 16; }  // ints, stored from here
+	__host__ __device__ size_t total() const { return ord() + size_t(qe) + 8; }
+};
+
+// column at tournament position k in step t, and the position of column c in step t
+__device__ __forceinline__ int svc_col(int k, int t, int qe) { return k == 0 ? 0 : ((k - 1 + t) % (qe - 1)) + 1; }
+__device__ __forceinline__ int svc_pos(int c, int t, int qe) {
+	if (c == 0) return 0;
+	int v = (c - 1 - t) % (qe - 1);
+	if (v < 0) v += qe - 1;
+	return v + 1;
+}
+
+__global__ void __launch_bounds__(kSvcThreads) k_svd_cluster(SvdArgs a, SvcLayout lay) {
+	namespace cg = cooperative_groups;
+	cg::cluster_group cl = cg::this_cluster();
+	extern __shared__ double sm[];
+	const int me = int(cl.block_rank()), tid = threadIdx.x, lane = tid & 31, warp = tid >> 5, nwarps = blockDim.x >> 5;
+	const int p = lay.p, q = lay.q, qe = lay.qe, P = lay.P, ppc = lay.ppc, cpc = lay.cpc;
+	const size_t cw = lay.colw();
+	const bool tall = a.m >= a.n;
+	double* sig = sm + lay.sig();
+	double* flg = sm + lay.flg();
+	int* order = reinterpret_cast<int*>(sm + lay.ord());
+	__shared__ int s_rank, s_stop;
+	__shared__ const double* s_src[64];
+	// slot s of this CTA at step t: its tournament position
+	auto slot_pos = [&](int s) {
+		const int pr = me * ppc + (s >> 1);
+		return (s & 1) ? qe - 1 - pr : pr;
+	};
+	// initial columns (step 0)
+	{
+		double* b0 = sm + lay.buf(0);
+		for (long long e = tid; e < (long long)cpc * cw; e += blockDim.x) {
+			const int s = int(e / cw), off = int(e % cw);
+			const int pr = me * ppc + (s >> 1);
+			double v = 0.0;
+			if (pr < qe / 2) {
+				const int c = svc_col(slot_pos(s), 0, qe);
+				if (c < q) {
+					if (off < p) v = tall ? a.X[(long long)off * a.ldx + c] : a.X[(long long)c * a.ldx + off];
+					else v = (off - p == c) ? 1.0 : 0.0;
+				}
+			}
+			b0[e] = v;
+		}
+	}
+	__syncthreads();
+	const double tol = DBL_EPSILON * sqrt(double(p));
+	int cur = 0, t = 0, sweep = 0;
+	bool converged = (q < 2);
+	bool rot = false;
+	long long steps_left = (long long)a.max_sweeps * (qe - 1);
+	while (!converged && steps_left > 0) {
+		double* bc = sm + lay.buf(cur);
+		for (int lp = warp; lp < ppc; lp += nwarps) {
+			const int pr = me * ppc + lp;
+			if (pr >= qe / 2) continue;
+			const int i = svc_col(pr, t, qe), j = svc_col(qe - 1 - pr, t, qe);
+			if (i >= q || j >= q) continue;
+			double* bi = bc + (size_t)(2 * lp) * cw;
+			double* bj = bc + (size_t)(2 * lp + 1) * cw;
+			double al = 0, be = 0, ga = 0;
+			for (int r = lane; r < p; r += 32) {
+				const double x = bi[r], y = bj[r];
+				al = fma(x, x, al);
+				be = fma(y, y, be);
+				ga = fma(x, y, ga);
+			}
+			al = warp_sum(al);
+			be = warp_sum(be);
+			ga = warp_sum(ga);
+			if (ga != 0.0 && fabs(ga) > tol * sqrt(al * be)) {
+				const double zeta = (be - al) / (2.0 * ga);
+				const double tt = copysign(1.0, zeta) / (fabs(zeta) + sqrt(1.0 + zeta * zeta));
+				const double c = 1.0 / sqrt(1.0 + tt * tt), sn = c * tt;
+				for (int r = lane; r < p + q; r += 32) {
+					const double x = bi[r], y = bj[r];
+					bi[r] = c * x - sn * y;
+					bj[r] = sn * x + c * y;
+				}
+				rot = true;
+			}
+		}
+		const bool last_step = (t == qe - 2);
+		if (last_step) {
+			__shared__ int s_rot;
+			if (tid == 0) s_rot = 0;
+			__syncthreads();
+			if (rot) s_rot = 1;
+			__syncthreads();
+			if (tid < P) cl.map_shared_rank(flg, tid)[me] = double(s_rot);
+		}
+		cl.sync();
+		--steps_left;
+		if (last_step) {
+			++sweep;
+			if (tid == 0) {
+				int any = 0;
+				for (int c = 0; c < P; ++c) any |= flg[c] != 0.0;
+				s_stop = any ? 0 : 1;
+			}
+			__syncthreads();
+			converged = s_stop != 0;
+			rot = false;
+			if (converged) break;  // uniform: every CTA read the same flags
+		}
+		// pull the columns of the next step
+		const int tn = (t + 1) % (qe - 1);
+		if (tid < cpc) {
+			const int pr = me * ppc + (tid >> 1);
+			const double* src = nullptr;
+			if (pr < qe / 2) {
+				const int c = svc_col(slot_pos(tid), tn, qe);
+				const int k = svc_pos(c, t, qe);
+				const int opr = k < qe / 2 ? k : qe - 1 - k;
+				const int oc = opr / ppc, os = 2 * (opr % ppc) + (k < qe / 2 ? 0 : 1);
+				src = cl.map_shared_rank(sm + lay.buf(cur), oc) + (size_t)os * cw;
+			}
+			s_src[tid] = src;
+		}
+		__syncthreads();
+		double* bn = sm + lay.buf(cur ^ 1);
+		for (long long e = tid; e < (long long)cpc * cw; e += blockDim.x) {
+			const int s = int(e / cw), off = int(e % cw);
+			const double* src = s_src[s];
+			bn[e] = src ? src[off] : 0.0;
+		}
+		__syncthreads();
+		cur ^= 1;
+		t = tn;
+	}
+	if (!converged && me == 0 && tid == 0) record_status(a.status, DEV_NOT_CONVERGED);
+	// singular values of this CTA's columns, pushed to every CTA
+	double* bc = sm + lay.buf(cur);
+	for (int s = warp; s < cpc; s += nwarps) {
+		const int pr = me * ppc + (s >> 1);
+		if (pr >= qe / 2) continue;
+		const int c = svc_col(slot_pos(s), t, qe);
+		if (c >= q) continue;
+		double v = 0;
+		for (int r = lane; r < p; r += 32) v = fma(bc[(size_t)s * cw + r], bc[(size_t)s * cw + r], v);
+		v = warp_sum(v);
+		if (lane < P) cl.map_shared_rank(sig, lane)[c] = sqrt(v);
+	}
+	cl.sync();
+	for (int c = tid; c < q; c += blockDim.x) {
+		int pos = 0;
+		for (int o = 0; o < q; ++o) pos += (sig[o] > sig[c]) || (sig[o] == sig[c] && o < c);
+		order[pos] = c;
+	}
+	__syncthreads();
+	if (tid == 0) {
+		int rank = q;
+		if (a.max_rank > 0 && a.max_rank < rank) rank = a.max_rank;
+		const double s0 = sig[order[0]];
+		for (int j = 1; j < rank; ++j)
+			if (sig[order[j]] <= a.eps * s0) { rank = j; break; }
+		s_rank = rank;
+		if (me == 0 && a.rank_out) *a.rank_out = rank;
+	}
+	__syncthreads();
+	const int rank = s_rank;
+	if (me == 0)
+		for (int k = tid; k < rank; k += blockDim.x) a.S[k] = sig[order[k]];
+	// this CTA's kept columns: sign gauge (largest |entry| of the left vector positive), U, V^T
+	for (int s = warp; s < cpc; s += nwarps) {
+		const int pr = me * ppc + (s >> 1);
+		if (pr >= qe / 2) continue;
+		const int c = svc_col(slot_pos(s), t, qe);
+		if (c >= q) continue;
+		int k = 0;
+		for (int o = 0; o < q; ++o) k += (sig[o] > sig[c]) || (sig[o] == sig[c] && o < c);
+		if (k >= rank) continue;
+		const double* col = bc + (size_t)s * cw;  // B part [0, p), V part [p, p + q)
+		const double sc = sig[c];
+		double best = -1.0, val = 0.0;
+		int bi = 1 << 30;
+		for (int i = lane; i < a.m; i += 32) {
+			const double u = tall ? col[i] : col[p + i];
+			if (fabs(u) > best) { best = fabs(u); val = u; bi = i; }
+		}
+#pragma unroll
+		for (int o = 16; o > 0; o >>= 1) {
+			const double ob = __shfl_xor_sync(0xffffffffu, best, o);
+			const double ov = __shfl_xor_sync(0xffffffffu, val, o);
+			const int oi = __shfl_xor_sync(0xffffffffu, bi, o);
+			if (ob > best || (ob == best && oi < bi)) { best = ob; val = ov; bi = oi; }
+		}
+		const double sg = val < 0.0 ? -1.0 : 1.0;
+		for (int i = lane; i < a.m; i += 32) {
+			const double u = tall ? (sc > 0 ? col[i] / sc : 0.0) : col[p + i];
+			a.U[(long long)i * rank + k] = sg * u;
+		}
+		for (int j = lane; j < a.n; j += 32) {
+			const double v = tall ? col[p + j] : (sc > 0 ? col[j] / sc : 0.0);
+			a.Vt[(long long)k * a.n + j] = sg * v;
+		}
+	}
+	cl.sync();  // no CTA leaves while another may still read its shared memory
+}
+
+static int svd_cluster_size(int m, int n, SvcLayout& lay) {
+	lay.p = std::max(m, n);
+	lay.q = std::min(m, n);
+	if (lay.q < 16 || lay.q > 512) return 0;
+	lay.qe = lay.q + (lay.q & 1);
+	const int pairs = lay.qe / 2;
+	int P = std::min(16, pairs);
+	lay.ppc = (pairs + P - 1) / P;
+	lay.P = (pairs + lay.ppc - 1) / lay.ppc;
+	lay.cpc = 2 * lay.ppc;
+	if (lay.cpc > 64 || lay.total() * sizeof(double) > kDynSmemMax) return 0;
+	return lay.P;
+}
+
 void launch_svd(const SvdArgs& a, cudaStream_t s) {
 	const int p = std::max(a.m, a.n), q = std::min(a.m, a.n);
 	const size_t aux = svd_aux_doubles(q) * sizeof(double);
@@ -1050,6 +1287,34 @@ void launch_svd(const SvdArgs& a, cudaStream_t s) {
 	const int use_smem = full <= kDynSmemMax ? 1 : 0;
 	XTT_REQUIRE(use_smem || a.work, "SVD workspace missing");
 	XTT_REQUIRE(std::min(a.m, a.n) <= 1024 || (a.max_rank > 0 && a.max_rank <= 1024), "SVD: more than 1024 kept singular values");
+	SvcLayout lay;
+	const int P = svd_cluster_size(a.m, a.n, lay);
+	if (P > 1) {
+		static bool attr_c = false;
+		if (!attr_c) {
+			XTT_CUDA(cudaFuncSetAttribute(k_svd_cluster, cudaFuncAttributeMaxDynamicSharedMemorySize, int(kDynSmemMax)));
+			XTT_CUDA(cudaFuncSetAttribute(k_svd_cluster, cudaFuncAttributeNonPortableClusterSizeAllowed, 1));
+			attr_c = true;
+		}
+		cudaLaunchConfig_t cfg = {};
+		cfg.gridDim = dim3(P);
+		cfg.blockDim = dim3(kSvcThreads);
+		cfg.dynamicSmemBytes = lay.total() * sizeof(double);
+		cfg.stream = s;
+		cudaLaunchAttribute at[1];
+		at[0].id = cudaLaunchAttributeClusterDimension;
+		at[0].val.clusterDim.x = P;
+		at[0].val.clusterDim.y = 1;
+		at[0].val.clusterDim.z = 1;
+		cfg.attrs = at;
+		cfg.numAttrs = 1;
+		int clusters = 0;
+		if (cudaOccupancyMaxActiveClusters(&clusters, k_svd_cluster, &cfg) == cudaSuccess && clusters > 0) {
+			XTT_CUDA(cudaLaunchKernelEx(&cfg, k_svd_cluster, a, lay));
+			return;
+		}
+		cudaGetLastError();
+	}
 	static bool attr = false;
 	if (!attr) {
 		XTT_CUDA(cudaFuncSetAttribute(k_svd, cudaFuncAttributeMaxDynamicSharedMemorySize, int(kDynSmemMax)));
