@@ -450,16 +450,18 @@ class SinglePointMeasurementSet:
 class ADFVariant:
     """xerus::ADFVariant (include/xerus/algorithms/adf.h:39-266) for single-point samples."""
 
-    def __init__(self, maxIterations, targetResidualNorm, minimalResidualNormDecrease):
+    def __init__(self, maxIterations, targetResidualNorm, minimalResidualNormDecrease, precision=None):
         self.maxIterations = maxIterations
         self.targetResidualNorm = targetResidualNorm
         self.minimalResidualNormDecrease = minimalResidualNormDecrease
+        # FP64, or MIXED: FP32 stacks and per-sample arithmetic, FP64 cores, QR and final check
+        self.precision = FP64 if precision is None else precision
 
     def __call__(self, x, measurements, perfData=None):
         pos, pp = _i64(measurements.positions)
         val, pv = _f64(measurements.measuredValues)
         o = L.AdfOptions(int(self.maxIterations), float(self.targetResidualNorm),
-                         float(self.minimalResidualNormDecrease))
+                         float(self.minimalResidualNormDecrease), int(self.precision), 0)
         cap = max(16, int(self.maxIterations) + 2 if self.maxIterations else 100000)
         trace = np.zeros(cap)
         fin, cnt = ctypes.c_double(), ctypes.c_int64()

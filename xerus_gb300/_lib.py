@@ -60,6 +60,8 @@ class AdfOptions(ctypes.Structure):
         ("max_iterations", ctypes.c_int64),
         ("target_residual", ctypes.c_double),
         ("min_decrease", ctypes.c_double),
+        ("precision", ctypes.c_int32),
+        ("reserved", ctypes.c_int32),
     ]
 
 

@@ -32,14 +32,18 @@ constexpr int kAdfMaxR = 8;        // fast path: ranks <= 8
 constexpr int kAdfMaxSlices = 16;  // fast path: mode sizes <= 16
 constexpr int kAdfPairsPerLane = 2;  // r0 * r1 <= 64
 
-struct AdfLevel {
+// One core position of the sweep. S is the type of the stacks and of the
+// per-sample arithmetic (double; float in the FP32 form); the core is FP64.
+template <class S>
+struct AdfLevelT {
 	const int* pos;     // indices of this mode, N ints
-	const double* F;    // F_{k-1}: r0 x N (nullptr: the constant 1)
-	const double* B;    // B_{k+1}: r1 x N (nullptr: the constant 1)
+	const S* F;         // F_{k-1}: r0 x N (nullptr: the constant 1)
+	const S* B;         // B_{k+1}: r1 x N (nullptr: the constant 1)
 	const double* X;    // core (r0, n, r1)
 	int r0, n, r1;
 	long long N;
 };
+using AdfLevel = AdfLevelT<double>;
 
 // res_s (optional write), and per-warp partials of G (r0, n, r1) and of sum res^2.
 // mode 0: res_s = y_s - <F, X_i B>; mode 1: res_s given in `res` (read only).
@@ -48,20 +52,21 @@ struct AdfLevel {
 // two (a, c) pairs) adds res_j F_j[a] B_j[c] into slice i_j of the warp's
 // gradient accumulator, sample by sample in order (deterministic). One FP64
 // multiply-add per pair and sample: GB300's FP64 pipe is the bound.
-__global__ void __launch_bounds__(kAdfThreads) k_adf_res_grad(AdfLevel L, const double* y, double* res, int mode,
+template <class S>
+__global__ void __launch_bounds__(kAdfThreads) k_adf_res_grad(AdfLevelT<S> L, const S* y, S* res, int mode,
                                                                double* gpart, double* rrpart, long long chunk) {
-	__shared__ double Xs[kAdfMaxR * kAdfMaxSlices * kAdfMaxR];
-	__shared__ double Gw[kAdfWarpsPerBlock][kAdfMaxSlices * kAdfMaxR * kAdfMaxR];
-	__shared__ double Fw[kAdfWarpsPerBlock][32 * kAdfMaxR];
-	__shared__ double Bw[kAdfWarpsPerBlock][32 * kAdfMaxR];
-	__shared__ double Rw[kAdfWarpsPerBlock][32];
+	__shared__ S Xs[kAdfMaxR * kAdfMaxSlices * kAdfMaxR];
+	__shared__ S Gw[kAdfWarpsPerBlock][kAdfMaxSlices * kAdfMaxR * kAdfMaxR];
+	__shared__ S Fw[kAdfWarpsPerBlock][32 * kAdfMaxR];
+	__shared__ S Bw[kAdfWarpsPerBlock][32 * kAdfMaxR];
+	__shared__ S Rw[kAdfWarpsPerBlock][32];
 	__shared__ int Iw[kAdfWarpsPerBlock][32];
 	const int lane = threadIdx.x & 31, wib = threadIdx.x >> 5;
 	const long long warp = (long long)blockIdx.x * kAdfWarpsPerBlock + wib;
 	const int r0 = L.r0, n = L.n, r1 = L.r1, P = r0 * r1;
-	for (int e = threadIdx.x; e < r0 * n * r1; e += blockDim.x) Xs[e] = L.X[e];
-	double* G = Gw[wib];
-	for (int e = lane; e < n * P; e += 32) G[e] = 0.0;
+	for (int e = threadIdx.x; e < r0 * n * r1; e += blockDim.x) Xs[e] = S(L.X[e]);
+	S* G = Gw[wib];
+	for (int e = lane; e < n * P; e += 32) G[e] = S(0);
 	__syncthreads();
 	int pa[kAdfPairsPerLane], pc[kAdfPairsPerLane];
 #pragma unroll
@@ -76,16 +81,16 @@ __global__ void __launch_bounds__(kAdfThreads) k_adf_res_grad(AdfLevel L, const 
 		const long long s = base + lane;
 		if (s < s1) {
 			const int idx = L.pos[s];
-			double* f = Fw[wib] + lane * kAdfMaxR;
-			double* b = Bw[wib] + lane * kAdfMaxR;
-			for (int a = 0; a < r0; ++a) f[a] = L.F ? L.F[a * L.N + s] : 1.0;
-			for (int c = 0; c < r1; ++c) b[c] = L.B ? L.B[c * L.N + s] : 1.0;
-			double rs;
+			S* f = Fw[wib] + lane * kAdfMaxR;
+			S* b = Bw[wib] + lane * kAdfMaxR;
+			for (int a = 0; a < r0; ++a) f[a] = L.F ? L.F[a * L.N + s] : S(1);
+			for (int c = 0; c < r1; ++c) b[c] = L.B ? L.B[c * L.N + s] : S(1);
+			S rs;
 			if (mode == 0) {
-				double v = 0.0;
+				S v = S(0);
 				for (int a = 0; a < r0; ++a) {
-					double t = 0.0;
-					const double* xr = Xs + (a * n + idx) * r1;
+					S t = S(0);
+					const S* xr = Xs + (a * n + idx) * r1;
 					for (int c = 0; c < r1; ++c) t += xr[c] * b[c];
 					v += f[a] * t;
 				}
@@ -94,7 +99,7 @@ __global__ void __launch_bounds__(kAdfThreads) k_adf_res_grad(AdfLevel L, const 
 			} else {
 				rs = res[s];
 			}
-			rr += rs * rs;
+			rr += double(rs) * double(rs);
 			Rw[wib][lane] = rs;
 			Iw[wib][lane] = idx;
 		}
@@ -102,10 +107,10 @@ __global__ void __launch_bounds__(kAdfThreads) k_adf_res_grad(AdfLevel L, const 
 		const int cnt = int((s1 - base) < 32 ? (s1 - base) : 32);
 		for (int j = 0; j < cnt; ++j) {
 			const int ij = Iw[wib][j];
-			const double rj = Rw[wib][j];
-			const double* fj = Fw[wib] + j * kAdfMaxR;
-			const double* bj = Bw[wib] + j * kAdfMaxR;
-			double* gi = G + ij * P;
+			const S rj = Rw[wib][j];
+			const S* fj = Fw[wib] + j * kAdfMaxR;
+			const S* bj = Bw[wib] + j * kAdfMaxR;
+			S* gi = G + ij * P;
 #pragma unroll
 			for (int t = 0; t < kAdfPairsPerLane; ++t) {
 				const int p = lane + 32 * t;
@@ -118,7 +123,7 @@ __global__ void __launch_bounds__(kAdfThreads) k_adf_res_grad(AdfLevel L, const 
 	double* gp = gpart + warp * (long long)r0 * n * r1;
 	for (int e = lane; e < n * P; e += 32) {
 		const int i = e / P, p = e - i * P, a = p / r1, c = p - a * r1;
-		gp[(a * n + i) * r1 + c] = G[e];
+		gp[(a * n + i) * r1 + c] = double(G[e]);
 	}
 	rr = warp_sum(rr);
 	if (lane == 0 && rrpart) rrpart[warp] = rr;
@@ -169,31 +174,32 @@ static void sum_parts(Context& c, const double* part, long long parts, int len, 
 }
 
 // slice norms: nrm_i = sum_{s: i_s = i} (F[s]^T G[:, i_s, :] B[s])^2, per-warp partials (n values)
-__global__ void __launch_bounds__(kAdfThreads) k_adf_slicenorm(AdfLevel L, const double* G, double* npart,
+template <class S>
+__global__ void __launch_bounds__(kAdfThreads) k_adf_slicenorm(AdfLevelT<S> L, const double* G, double* npart,
                                                                 long long chunk) {
-	__shared__ double Gs[kAdfMaxR * kAdfMaxSlices * kAdfMaxR];
-	__shared__ double Aw[kAdfWarpsPerBlock][kAdfMaxSlices][33];  // lane-private accumulators per slice
+	__shared__ S Gs[kAdfMaxR * kAdfMaxSlices * kAdfMaxR];
+	__shared__ S Aw[kAdfWarpsPerBlock][kAdfMaxSlices][33];  // lane-private accumulators per slice
 	const int lane = threadIdx.x & 31, wib = threadIdx.x >> 5;
 	const long long warp = (long long)blockIdx.x * kAdfWarpsPerBlock + wib;
 	const int r0 = L.r0, n = L.n, r1 = L.r1;
-	for (int e = threadIdx.x; e < r0 * n * r1; e += blockDim.x) Gs[e] = G[e];
-	for (int i = 0; i < kAdfMaxSlices; ++i) Aw[wib][i][lane] = 0.0;
+	for (int e = threadIdx.x; e < r0 * n * r1; e += blockDim.x) Gs[e] = S(G[e]);
+	for (int i = 0; i < kAdfMaxSlices; ++i) Aw[wib][i][lane] = S(0);
 	__syncthreads();
 	const long long s0 = warp * chunk, s1 = min(L.N, s0 + chunk);
 	for (long long s = s0 + lane; s < s1; s += 32) {
 		const int idx = L.pos[s];
-		double v = 0.0;
+		S v = S(0);
 		for (int a = 0; a < r0; ++a) {
-			double t = 0.0;
-			const double* gr = Gs + (a * n + idx) * r1;
-			for (int c = 0; c < r1; ++c) t += gr[c] * (L.B ? L.B[c * L.N + s] : 1.0);
-			v += (L.F ? L.F[a * L.N + s] : 1.0) * t;
+			S t = S(0);
+			const S* gr = Gs + (a * n + idx) * r1;
+			for (int c = 0; c < r1; ++c) t += gr[c] * (L.B ? L.B[c * L.N + s] : S(1));
+			v += (L.F ? L.F[a * L.N + s] : S(1)) * t;
 		}
 		Aw[wib][idx][lane] += v * v;
 	}
 	__syncwarp();
 	for (int i = 0; i < n; ++i) {
-		const double t = warp_sum(Aw[wib][i][lane]);
+		const double t = warp_sum(double(Aw[wib][i][lane]));
 		if (lane == 0) npart[warp * n + i] = t;
 	}
 }
@@ -236,35 +242,44 @@ __global__ void k_adf_update(double* X, const double* G, const double* nrm, int 
 }
 
 // F_k[b][s] = sum_a F_{k-1}[a][s] X[a, i_s, b]
-__global__ void k_adf_forward(const int* pos, const double* Fp, const double* X, double* Fo, int r0, int n, int r1,
+template <class S>
+__global__ void k_adf_forward(const int* pos, const S* Fp, const double* X, S* Fo, int r0, int n, int r1,
                               long long N) {
-	extern __shared__ double Xs[];
-	for (int e = threadIdx.x; e < r0 * n * r1; e += blockDim.x) Xs[e] = X[e];
+	extern __shared__ __align__(16) unsigned char xs_raw[];
+	S* Xs = reinterpret_cast<S*>(xs_raw);
+	for (int e = threadIdx.x; e < r0 * n * r1; e += blockDim.x) Xs[e] = S(X[e]);
 	__syncthreads();
 	for (long long s = blockIdx.x * (long long)blockDim.x + threadIdx.x; s < N; s += (long long)gridDim.x * blockDim.x) {
 		const int idx = pos[s];
 		for (int b = 0; b < r1; ++b) {
-			double v = 0.0;
-			for (int a = 0; a < r0; ++a) v += (Fp ? Fp[a * N + s] : 1.0) * Xs[(a * n + idx) * r1 + b];
+			S v = S(0);
+			for (int a = 0; a < r0; ++a) v += (Fp ? Fp[a * N + s] : S(1)) * Xs[(a * n + idx) * r1 + b];
 			Fo[b * N + s] = v;
 		}
 	}
 }
 
 // B_k[a][s] = sum_b X[a, i_s, b] B_{k+1}[b][s]
-__global__ void k_adf_backward(const int* pos, const double* Bn, const double* X, double* Bo, int r0, int n, int r1,
+template <class S>
+__global__ void k_adf_backward(const int* pos, const S* Bn, const double* X, S* Bo, int r0, int n, int r1,
                                long long N) {
-	extern __shared__ double Xs[];
-	for (int e = threadIdx.x; e < r0 * n * r1; e += blockDim.x) Xs[e] = X[e];
+	extern __shared__ __align__(16) unsigned char xs_raw[];
+	S* Xs = reinterpret_cast<S*>(xs_raw);
+	for (int e = threadIdx.x; e < r0 * n * r1; e += blockDim.x) Xs[e] = S(X[e]);
 	__syncthreads();
 	for (long long s = blockIdx.x * (long long)blockDim.x + threadIdx.x; s < N; s += (long long)gridDim.x * blockDim.x) {
 		const int idx = pos[s];
 		for (int a = 0; a < r0; ++a) {
-			double v = 0.0;
-			for (int b = 0; b < r1; ++b) v += Xs[(a * n + idx) * r1 + b] * (Bn ? Bn[b * N + s] : 1.0);
+			S v = S(0);
+			for (int b = 0; b < r1; ++b) v += Xs[(a * n + idx) * r1 + b] * (Bn ? Bn[b * N + s] : S(1));
 			Bo[a * N + s] = v;
 		}
 	}
+}
+
+__global__ void k_to_f32(float* out, const double* in, long long n) {
+	for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x)
+		out[i] = float(in[i]);
 }
 
 namespace {
@@ -278,11 +293,15 @@ struct AdfData {
 	double* y = nullptr;
 	double* res = nullptr;
 	std::vector<double*> F, B;  // F[k]: r_{k+1} x N ; B[k]: r_k x N
+	// FP32 form: stacks, samples and residuals in single precision
+	bool f32 = false;
+	float *y32 = nullptr, *res32 = nullptr;
+	std::vector<float*> F32, B32;
 	double *gpart = nullptr, *npart = nullptr, *rrpart = nullptr, *G = nullptr, *nrm = nullptr, *rr = nullptr;
 	long long warps = 0, chunk = 0;
 	bool fast = true;
 
-	AdfData(Context& cc, Tensor& xx, const int64_t* positions, const double* values, long long n)
+	AdfData(Context& cc, Tensor& xx, const int64_t* positions, const double* values, long long n, bool want_f32 = false)
 	    : c(cc), x(xx), d(xx.d), N(n) {
 		std::vector<int> hp(size_t(d) * N);
 		for (long long s = 0; s < N; ++s)
@@ -300,21 +319,41 @@ struct AdfData {
 		for (int k = 0; k <= d; ++k) maxr = std::max(maxr, x.ranks[k]);
 		for (int k = 0; k < d; ++k) maxn = std::max(maxn, x.dims[k]);
 		fast = maxr <= kAdfMaxR && maxn <= kAdfMaxSlices && maxr * maxr <= 32 * kAdfPairsPerLane;
-		F.assign(d, nullptr);
-		B.assign(d, nullptr);
+		f32 = want_f32 && fast;
 		size_t fo = 0, bo = 0;
 		for (int k = 0; k < d; ++k) {
 			fo += size_t(x.ranks[k + 1]) * N;
 			bo += size_t(x.ranks[k]) * N;
 		}
-		double* Fa = c.scratch<double>(S_ADF_FIRST + 8, fo);
-		double* Ba = c.scratch<double>(S_ADF_FIRST + 9, bo);
-		fo = bo = 0;
-		for (int k = 0; k < d; ++k) {
-			F[k] = Fa + fo;
-			B[k] = Ba + bo;
-			fo += size_t(x.ranks[k + 1]) * N;
-			bo += size_t(x.ranks[k]) * N;
+		if (f32) {
+			y32 = c.scratch<float>(S_ADF_FIRST + 11, size_t(N));
+			res32 = c.scratch<float>(S_ADF_FIRST + 12, size_t(N));
+			k_to_f32<<<unsigned(std::min<long long>((N + 255) / 256, 4096)), 256, 0, c.stream>>>(y32, y, N);
+			XTT_CUDA(cudaGetLastError());
+			c.count_launch();
+			float* Fa = c.scratch<float>(S_ADF_FIRST + 8, fo);
+			float* Ba = c.scratch<float>(S_ADF_FIRST + 9, bo);
+			F32.assign(d, nullptr);
+			B32.assign(d, nullptr);
+			fo = bo = 0;
+			for (int k = 0; k < d; ++k) {
+				F32[k] = Fa + fo;
+				B32[k] = Ba + bo;
+				fo += size_t(x.ranks[k + 1]) * N;
+				bo += size_t(x.ranks[k]) * N;
+			}
+		} else {
+			double* Fa = c.scratch<double>(S_ADF_FIRST + 8, fo);
+			double* Ba = c.scratch<double>(S_ADF_FIRST + 9, bo);
+			F.assign(d, nullptr);
+			B.assign(d, nullptr);
+			fo = bo = 0;
+			for (int k = 0; k < d; ++k) {
+				F[k] = Fa + fo;
+				B[k] = Ba + bo;
+				fo += size_t(x.ranks[k + 1]) * N;
+				bo += size_t(x.ranks[k]) * N;
+			}
 		}
 		warps = std::max<long long>(1, std::min<long long>((N + 255) / 256, (long long)c.num_sms * 16));
 		warps = (warps + kAdfWarpsPerBlock - 1) / kAdfWarpsPerBlock * kAdfWarpsPerBlock;
@@ -326,11 +365,12 @@ struct AdfData {
 		nrm = c.scratch<double>(S_ADF_FIRST + 7, size_t(maxn) + 8);
 		rr = nrm + maxn;
 	}
-	AdfLevel level(int k, const double* X) const {
-		AdfLevel L;
+	template <class S>
+	AdfLevelT<S> level(int k, const double* X, const std::vector<S*>& Fs, const std::vector<S*>& Bs) const {
+		AdfLevelT<S> L;
 		L.pos = pos + size_t(k) * N;
-		L.F = k > 0 ? F[k - 1] : nullptr;
-		L.B = k + 1 < d ? B[k + 1] : nullptr;
+		L.F = k > 0 ? Fs[k - 1] : nullptr;
+		L.B = k + 1 < d ? Bs[k + 1] : nullptr;
 		L.X = X;
 		L.r0 = int(x.ranks[k]);
 		L.n = int(x.dims[k]);
@@ -338,18 +378,24 @@ struct AdfData {
 		L.N = N;
 		return L;
 	}
+	AdfLevel level(int k, const double* X) const { return level<double>(k, X, F, B); }
 	unsigned blocks() const { return unsigned(warps / kAdfWarpsPerBlock); }
-	// res (mode 0) or given res (mode 1), G into this->G, and sum res^2 into rr[0]
+	// res (mode 0) or given res (mode 1), G into Gout, and sum res^2 into rr[0]
 	void res_grad(int k, int mode, const double* X, double* Gout, double gscale) {
-		const AdfLevel L = level(k, X);
-		const int len = L.r0 * L.n * L.r1;
+		const int len = int(x.ranks[k] * x.dims[k] * x.ranks[k + 1]);
 		if (fast) {
 			ProfScope ps(c, "adf_res_grad");
-			k_adf_res_grad<<<blocks(), kAdfThreads, 0, c.stream>>>(L, y, res, mode, gpart, rrpart, chunk);
+			if (f32)
+				k_adf_res_grad<float><<<blocks(), kAdfThreads, 0, c.stream>>>(level<float>(k, X, F32, B32), y32, res32,
+				                                                              mode, gpart, rrpart, chunk);
+			else
+				k_adf_res_grad<double><<<blocks(), kAdfThreads, 0, c.stream>>>(level(k, X), y, res, mode, gpart, rrpart,
+				                                                               chunk);
+			c.count_launch();
 			sum_parts(c, gpart, warps, len, Gout, gscale);
 			sum_parts(c, rrpart, warps, 1, rr, 1.0);
-			c.count_launch();
 		} else {
+			const AdfLevel L = level(k, X);
 			if (mode == 0) k_adf_res_generic<<<std::max<long long>(1, std::min<long long>((N + 255) / 256, 4096)), 256, 0, c.stream>>>(L, y, res);
 			k_adf_grad_generic<<<std::max(1, (len + 127) / 128), 128, 0, c.stream>>>(L, res, Gout);
 			if (gscale != 1.0) scale(c, Gout, gscale, size_t(len));
@@ -360,14 +406,17 @@ struct AdfData {
 		XTT_CUDA(cudaGetLastError());
 	}
 	void slicenorm(int k) {
-		const AdfLevel L = level(k, x.core[k]);
 		if (fast) {
 			ProfScope ps(c, "adf_slicenorm");
-			k_adf_slicenorm<<<blocks(), kAdfThreads, 0, c.stream>>>(L, G, npart, chunk);
-			sum_parts(c, npart, warps, L.n, nrm, 1.0);
+			if (f32)
+				k_adf_slicenorm<float><<<blocks(), kAdfThreads, 0, c.stream>>>(level<float>(k, x.core[k], F32, B32), G,
+				                                                               npart, chunk);
+			else
+				k_adf_slicenorm<double><<<blocks(), kAdfThreads, 0, c.stream>>>(level(k, x.core[k]), G, npart, chunk);
 			c.count_launch();
+			sum_parts(c, npart, warps, int(x.dims[k]), nrm, 1.0);
 		} else {
-			k_adf_slicenorm_generic<<<1, 32, 0, c.stream>>>(L, G, nrm);
+			k_adf_slicenorm_generic<<<1, 32, 0, c.stream>>>(level(k, x.core[k]), G, nrm);
 			c.count_launch();
 		}
 		XTT_CUDA(cudaGetLastError());
@@ -376,9 +425,12 @@ struct AdfData {
 		const int r0 = int(x.ranks[k]), n = int(x.dims[k]), r1 = int(x.ranks[k + 1]);
 		const unsigned bl = unsigned(std::max<long long>(1, std::min<long long>((N + 255) / 256, (long long)c.num_sms * 8)));
 		ProfScope ps(c, "adf_stack");
-		k_adf_forward<<<bl, 256, size_t(r0) * n * r1 * sizeof(double), c.stream>>>(pos + size_t(k) * N,
-		                                                                           k > 0 ? F[k - 1] : nullptr,
-		                                                                           x.core[k], F[k], r0, n, r1, N);
+		if (f32)
+			k_adf_forward<float><<<bl, 256, size_t(r0) * n * r1 * sizeof(float), c.stream>>>(
+			    pos + size_t(k) * N, k > 0 ? F32[k - 1] : nullptr, x.core[k], F32[k], r0, n, r1, N);
+		else
+			k_adf_forward<double><<<bl, 256, size_t(r0) * n * r1 * sizeof(double), c.stream>>>(
+			    pos + size_t(k) * N, k > 0 ? F[k - 1] : nullptr, x.core[k], F[k], r0, n, r1, N);
 		XTT_CUDA(cudaGetLastError());
 		c.count_launch();
 	}
@@ -386,9 +438,12 @@ struct AdfData {
 		const int r0 = int(x.ranks[k]), n = int(x.dims[k]), r1 = int(x.ranks[k + 1]);
 		const unsigned bl = unsigned(std::max<long long>(1, std::min<long long>((N + 255) / 256, (long long)c.num_sms * 8)));
 		ProfScope ps(c, "adf_stack");
-		k_adf_backward<<<bl, 256, size_t(r0) * n * r1 * sizeof(double), c.stream>>>(pos + size_t(k) * N,
-		                                                                            k + 1 < d ? B[k + 1] : nullptr,
-		                                                                            x.core[k], B[k], r0, n, r1, N);
+		if (f32)
+			k_adf_backward<float><<<bl, 256, size_t(r0) * n * r1 * sizeof(float), c.stream>>>(
+			    pos + size_t(k) * N, k + 1 < d ? B32[k + 1] : nullptr, x.core[k], B32[k], r0, n, r1, N);
+		else
+			k_adf_backward<double><<<bl, 256, size_t(r0) * n * r1 * sizeof(double), c.stream>>>(
+			    pos + size_t(k) * N, k + 1 < d ? B[k + 1] : nullptr, x.core[k], B[k], r0, n, r1, N);
 		XTT_CUDA(cudaGetLastError());
 		c.count_launch();
 	}
@@ -402,7 +457,7 @@ struct AdfData {
 }  // namespace
 
 AdfResult adf(Tensor& x, const int64_t* positions, const double* values, long long N, int64_t max_iter,
-              double target, double min_dec) {
+              double target, double min_dec, int precision) {
 	// ADFVariant::InternalSolver::solve / solve_with_current_ranks (adf.cpp:489-604), x at its maximal ranks
 	Context& c = *x.ctx;
 	XTT_REQUIRE(!x.op, "ADF needs a TT tensor");
@@ -411,7 +466,7 @@ AdfResult adf(Tensor& x, const int64_t* positions, const double* values, long lo
 	for (long long s = 0; s < N; ++s) ny2 += values[s] * values[s];
 	const double norm_y = std::sqrt(ny2);
 	move_core(x, 0, false);  // canonicalize_left (adf.cpp:582)
-	AdfData D(c, x, positions, values, N);
+	AdfData D(c, x, positions, values, N, precision != XTT_PRECISION_FP64);
 	AdfResult out;
 	double residual_norm = DBL_MAX, last_residual_norm = DBL_MAX;
 	double dec1 = 0, dec2 = 0, dec3 = 0;
@@ -441,6 +496,15 @@ AdfResult adf(Tensor& x, const int64_t* positions, const double* values, long lo
 		}
 	}
 	out.residual = residual_norm;
+	out.checked_residual = residual_norm;
+	if (D.f32) {
+		// FP64 check of the FP32 form: ||P(x) - y|| / ||y|| from FP64 entries of the FP64 cores
+		std::vector<double> e(N);
+		entries(x, positions, N, e.data());
+		double s2 = 0;
+		for (long long i = 0; i < N; ++i) s2 += (e[i] - values[i]) * (e[i] - values[i]);
+		out.checked_residual = std::sqrt(s2) / norm_y;
+	}
 	return out;
 }
 

@@ -221,10 +221,15 @@ struct MixedParams {
 	double tol;
 	int max_refine;
 	int* flag;               // 1 when the FP64 target was not reached, else 0
+	int* sticky;             // set once FP32 corrections stalled; later solves skip them
 };
 
 template <class Grp>
 __global__ void __launch_bounds__(kGemmThreads) k_cg_mixed(MixedParams a, Grp grp, int* out_i, double* out_d) {
+	if (a.sticky && __ldcg(a.sticky) != 0) {  // an earlier solve of this sweep showed FP32 does not help
+		if (blockIdx.x == 0 && threadIdx.x == 0) *a.flag = 1;
+		return;
+	}
 	__shared__ union U {
 		GemmSmem<double> d;
 		GemmSmem<float> f;
@@ -279,7 +284,9 @@ __global__ void __launch_bounds__(kGemmThreads) k_cg_mixed(MixedParams a, Grp gr
 		out_i[0] += iters;
 		out_i[1] += refs;
 		out_d[0] = rel;
-		if (a.flag) *a.flag = (reached || bb == 0.0) ? 0 : 1;
+		const int failed = (reached || bb == 0.0) ? 0 : 1;
+		if (a.flag) *a.flag = failed;
+		if (failed && a.sticky) *a.sticky = 1;
 	}
 	if (Grp::kCluster) grp.sync();
 }
@@ -428,6 +435,7 @@ CgResult local_solve(Context& c, const LocalShape& s, const double* L, const dou
 		m.tol = tol;
 		m.max_refine = 12;
 		m.flag = flag;
+		m.sticky = c.d_ints + 11;
 		{
 			ProfScope ps(c, "cg_mixed");
 			if (!(use_cluster && launch_cluster(k_cg_mixed<ClusterGroup>, P, c.stream, m, cgrp, oi, od))) {
@@ -757,7 +765,8 @@ AlsReport als(const Tensor& A, Tensor& x, const Tensor& b, const AlsOptions& o) 
 	double energy = s.energy(cur), last_e = 1e101, last_e2 = 1e102;
 	record(3);
 	int half = 0;
-	XTT_CUDA(cudaMemsetAsync(c.d_ints + 8, 0, 2 * sizeof(int), c.stream));  // CG counters of this solve
+	// CG counters of this solve, the mixed solves' flag and the sticky FP64 switch
+	XTT_CUDA(cudaMemsetAsync(c.d_ints + 8, 0, 4 * sizeof(int), c.stream));
 	while (true) {
 		const LocalShape sh = s.shape(cur);
 		const long long n = sh.dim();

@@ -119,6 +119,7 @@ struct BInstance {
 	double* ws;
 	BShared& sh;
 	int iters = 0;
+	bool fp32_stalled = false;  // once set, this instance's remaining solves run in FP64
 
 	__device__ double* Lop(int k) const { return ws + a.lay.L + sh.opoff[k]; }
 	__device__ double* Rop(int k) const { return ws + a.lay.R + sh.opoff[k]; }
@@ -261,7 +262,8 @@ struct BInstance {
 		iters += it;
 	}
 	// Mixed: FP32 CG corrections on FP32 copies of the operands, FP64 residuals.
-	__device__ void cg_mixed(int k) {
+	// returns false when the FP32 corrections stalled (the FP64 CG finished the solve)
+	__device__ bool cg_mixed(int k) {
 		const CcShape s = shape(k);
 		const long long n = (long long)s.ra * s.n1 * s.rb;
 		double *x = ws + a.lay.v, *b = ws + a.lay.bloc, *q = ws + a.lay.q;
@@ -340,6 +342,7 @@ struct BInstance {
 		}
 		if (!reached) cg64(k);  // from the best mixed iterate
 		if (bb == 0) blk_copy(x, b, n);
+		return reached;
 	}
 
 	__device__ void solve(int id) {
@@ -410,8 +413,8 @@ struct BInstance {
 		while (true) {
 			rhs(cur);
 			blk_copy(ws + a.lay.v, I.x[cur], csize(cur));
-			if (a.precision == XTT_PRECISION_FP64) cg64(cur);
-			else cg_mixed(cur);
+			if (a.precision == XTT_PRECISION_FP64 || fp32_stalled) cg64(cur);
+			else fp32_stalled = !cg_mixed(cur);
 			blk_copy(I.x[cur], ws + a.lay.v, csize(cur));
 			if ((!inc && cur == first) || (inc && cur == last - 1)) {
 				++half;

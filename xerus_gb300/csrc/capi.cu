@@ -552,10 +552,11 @@ int xtt_adf(xtt_tensor* x, const int64_t* positions, const double* values, int64
             double* final_residual, double* residual_trace, int64_t trace_capacity, int64_t* trace_count) {
 	return guard([&] {
 		ARG(x && positions && values && opt, "NULL argument");
+		ARG(opt->precision == XTT_PRECISION_FP64 || opt->precision == XTT_PRECISION_MIXED, "unknown precision");
 		xtt::AdfResult r = xtt::adf(*x->t, positions, values, num, opt->max_iterations, opt->target_residual,
-		                            opt->min_decrease);
+		                            opt->min_decrease, opt->precision);
 		x->t->ctx->sync();
-		if (final_residual) *final_residual = r.residual;
+		if (final_residual) *final_residual = r.checked_residual;
 		if (residual_trace)
 			for (size_t i = 0; i < r.trace.size() && int64_t(i) < trace_capacity; ++i) residual_trace[i] = r.trace[i];
 		if (trace_count) *trace_count = int64_t(r.trace.size());

@@ -95,6 +95,7 @@ struct CcArgs {
 	int* out_i = nullptr;
 	double* out_d = nullptr;
 	int* flag = nullptr;        // mixed form: 1 when the FP64 target was not reached, else 0
+	int* sticky = nullptr;      // mixed form: set once FP32 corrections stalled; later solves skip them
 	const int* gate = nullptr;  // FP64 form: run only if *gate != 0 (polish after a mixed solve)
 };
 
@@ -314,6 +315,10 @@ __global__ void __launch_bounds__(kCcThreads) k_cg_cluster_f64(CcArgs a) {
 
 // Mixed form: FP32 CG corrections, FP64 residuals and iterate.
 __global__ void __launch_bounds__(kCcThreads) k_cg_cluster_mixed(CcArgs a) {
+	if (a.sticky && __ldcg(a.sticky) != 0) {  // an earlier solve of this sweep showed FP32 does not help
+		if (blockIdx.x == 0 && threadIdx.x == 0) *a.flag = 1;
+		return;
+	}
 	extern __shared__ __align__(16) unsigned char smem[];
 	cgx::cluster_group cl = cgx::this_cluster();
 	const CcShape& s = a.s;
@@ -395,7 +400,9 @@ __global__ void __launch_bounds__(kCcThreads) k_cg_cluster_mixed(CcArgs a) {
 		a.out_i[0] += iters;
 		a.out_i[1] += refs;
 		a.out_d[0] = rel;
-		if (a.flag) *a.flag = (reached || bb == 0.0) ? 0 : 1;
+		const int failed = (reached || bb == 0.0) ? 0 : 1;
+		if (a.flag) *a.flag = failed;
+		if (failed && a.sticky) *a.sticky = 1;
 	}
 	cl.sync();
 }
@@ -480,6 +487,7 @@ bool cluster_local_solve(Context& c, const LocalShape& ls, const double* L, cons
 	a.out_i = c.d_ints + 8;
 	a.out_d = c.d_dbl + 8;
 	a.flag = flag;
+	a.sticky = flag ? c.d_ints + 11 : nullptr;
 	a.gate = gate;
 	bool launched;
 	{

@@ -172,11 +172,14 @@ void op_apply_tt(const Tensor& A, const Tensor& x, Tensor& y);
 
 // ADF for single-point samples (positions: N x d, row-major).
 struct AdfResult {
-	double residual = 0;
+	double residual = 0;          // the iteration's own residual (FP32 in the FP32 form)
+	double checked_residual = 0;  // FP64 residual of the returned x
 	std::vector<double> trace;
 };
+// precision: XTT_PRECISION_FP64, or XTT_PRECISION_MIXED for FP32 stacks and
+// per-sample arithmetic with FP64 cores, QR and final check.
 AdfResult adf(Tensor& x, const int64_t* positions, const double* values, long long N, int64_t max_iter, double target,
-              double min_dec);
+              double min_dec, int precision = XTT_PRECISION_FP64);
 double adf_gradient(const Tensor& x, const int64_t* positions, const double* values, long long N,
                     std::vector<double>& grad);
 
