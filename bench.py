@@ -188,22 +188,24 @@ def bench_adf(xg, ctx, torch, stream, iters, peak, cpu):
     xg._lib.load().xtt_random_normal(0.0, 1e-6, N, noise.ctypes.data_as(xg._lib.c_double_p))
     m.measuredValues = m.measuredValues + noise
     x0 = xg.TTTensor.random([n] * d, r, ctx=ctx)
-    xg.ADFVariant(2, 0.0, 1.0)(x0.copy(), m)  # warm-up
-    x = x0.copy()
-    torch.cuda.synchronize()
-    e0, e1 = _events(torch, stream)
-    e0.record(stream)
-    res = xg.ADFVariant(iters, 0.0, 1.0)(x, m)
-    e1.record(stream)
-    torch.cuda.synchronize()
-    ms = e0.elapsed_time(e1) / iters
-    # per iteration: stack updates, residuals, gradient scatter and slice norms over all positions,
-    # N d w (5 r + 4) bytes (w = 8)
-    alg = N * d * 8 * (5 * r + 4)
-    out = {"workload": "ADF d=10 n=8 rank 6, 200000 samples, FP64", "iterations": iters, "ms_per_iteration": ms,
-           "samples_per_s": N / (ms / 1e3), "final_residual": res,
-           "roofline": {"bound": "hbm", "achieved": alg / (ms / 1e3) / 1e9, "peak": peak, "unit": "GB/s",
-                        "frac": alg / (ms / 1e3) / 1e9 / peak, "algorithmic_bytes_per_iteration": alg}}
+    out = {"workload": "ADF d=10 n=8 rank 6, 200000 samples", "iterations": iters}
+    for name, prec, w in (("fp64", xg.FP64, 8), ("fp32", xg.MIXED, 4)):
+        xg.ADFVariant(2, 0.0, 1.0, precision=prec)(x0.copy(), m)  # warm-up
+        x = x0.copy()
+        torch.cuda.synchronize()
+        e0, e1 = _events(torch, stream)
+        e0.record(stream)
+        res = xg.ADFVariant(iters, 0.0, 1.0, precision=prec)(x, m)
+        e1.record(stream)
+        torch.cuda.synchronize()
+        ms = e0.elapsed_time(e1) / iters
+        # per iteration: stack updates, residuals, gradient scatter and slice norms over all
+        # positions, N d w (5 r + 4) bytes (w = 8 in FP64, 4 with FP32 stacks)
+        alg = N * d * w * (5 * r + 4)
+        out[name] = {"ms_per_iteration": ms, "samples_per_s": N / (ms / 1e3), "final_residual_fp64_checked": res,
+                     "roofline": {"bound": "hbm", "achieved": alg / (ms / 1e3) / 1e9, "peak": peak, "unit": "GB/s",
+                                  "frac": alg / (ms / 1e3) / 1e9 / peak, "algorithmic_bytes_per_iteration": alg}}
+    out["fp32_speedup_vs_fp64"] = out["fp64"]["ms_per_iteration"] / out["fp32"]["ms_per_iteration"]
     if cpu:
         from oracle import xtt_oracle as o
         xh = o.TT(x0.get_cores(), x0.canonicalized, x0.corePosition)

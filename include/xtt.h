@@ -246,6 +246,10 @@ typedef struct xtt_adf_options {
 	int64_t max_iterations;          /* ADFVariant::maxIterations (adf.h:233), 0 = unlimited */
 	double target_residual;          /* ADFVariant::targetResidualNorm (adf.h:234) */
 	double min_decrease;             /* ADFVariant::minimalResidualNormDecrease (adf.h:235) */
+	int32_t precision;               /* XTT_PRECISION_FP64; XTT_PRECISION_MIXED: FP32 stacks and per-sample
+	                                    arithmetic, FP64 cores and QR, FP64-checked final residual (no
+	                                    reference counterpart) */
+	int32_t reserved;
 } xtt_adf_options;
 
 /* ADFVariant(maxIter, target, minDecrease)(x, SinglePointMeasurementSet{positions, values})

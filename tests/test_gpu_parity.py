@@ -322,6 +322,23 @@ def test_adf_cfg5_positions_gradient_and_first_iterations(ctx, golden):
     assert rel_err(perf.residuals, z["cfg5_perf_residual"][:5]) < 1e-9
 
 
+def test_adf_fp32_form_tracks_fp64(ctx, golden):
+    """The FP32 form (FP32 stacks and per-sample arithmetic, FP64 cores and QR)
+    follows the FP64 trajectory to FP32 accuracy over the first iterations, and its
+    returned residual is the FP64 check of the returned x."""
+    z = golden("adf")
+    _, m, x = _adf_inputs(ctx, [4, 5, 3, 5, 4, 3], 3, 2000)
+    x32 = x.copy()
+    p64, p32 = xg.PerformanceData(), xg.PerformanceData()
+    xg.ADFVariant(8, 0.0, 1.0)(x, m, p64)
+    res32 = xg.ADFVariant(8, 0.0, 1.0, precision=xg.MIXED)(x32, m, p32)
+    assert rel_err(p32.residuals[:4], p64.residuals[:4]) < 1e-4
+    assert rel_err(p64.residuals[:4], z["small_perf_residual"][:4]) < 1e-10
+    e = x32.entries(m.positions)
+    chk = np.linalg.norm(e - m.measuredValues) / np.linalg.norm(m.measuredValues)
+    assert abs(res32 / chk - 1) < 1e-10
+
+
 def test_adf_gradient_central_differences(ctx):
     xg.seed(7)
     dims = [3, 4, 3, 2]

@@ -547,7 +547,13 @@ struct Qc2Layout {
 	__host__ __device__ size_t part() const { return sw() + nw; }
 	__host__ __device__ size_t partn() const { return part() + 8 * 256; }
 	__host__ __device__ size_t coef() const { return partn() + 8; }
-	__host__ __device__ size_t total() const { return coef() + 4; }
+	// column pivoting: exchanged (norm below the diagonal, diagonal entry) pairs per column,
+	// their cluster totals, and the permutation (ints)
+	__host__ __device__ size_t pslot() const { return coef() + 4; }
+	__host__ __device__ size_t tb() const { return pslot() + 4 * size_t(nw); }
+	__host__ __device__ size_t td() const { return tb() + nw; }
+	__host__ __device__ size_t perm() const { return td() + nw; }
+	__host__ __device__ size_t total() const { return perm() + size_t(nw + 1) / 2 + 1; }
 };
 
 // Column-chunk geometry of the thread-per-(column, row group) mapping.
@@ -576,6 +582,12 @@ __global__ void __launch_bounds__(kQ2Threads) k_qr_cl2(QrArgs a, Qc2Layout lay) 
 	double* part = sm + lay.part();
 	double* partn = sm + lay.partn();
 	double* coef = sm + lay.coef();
+	double* pslot = sm + lay.pslot();
+	double* tb = sm + lay.tb();
+	double* td = sm + lay.td();
+	int* perm = reinterpret_cast<int*>(sm + lay.perm());
+	__shared__ double s_best[kQ2Threads / 32];
+	__shared__ int s_bidx[kQ2Threads / 32];
 	auto w = [&](int il, int c) -> double& { return W[(long long)il * ldw + c]; };
 	auto lo_of = [&](int g) { return min(max(g - r0, 0), nl); };
 
@@ -583,8 +595,17 @@ __global__ void __launch_bounds__(kQ2Threads) k_qr_cl2(QrArgs a, Qc2Layout lay) 
 		const int il = int(e / nw), c = int(e % nw), gi = r0 + il;
 		w(il, c) = a.transpose ? a.A[(long long)c * a.lda + gi] : a.A[(long long)gi * a.lda + c];
 	}
+	for (int c = tid; c < nw; c += kQ2Threads) perm[c] = c;
 	__syncthreads();
-	if (warp == 0) {
+	if (a.pivot) {
+		// column 0's exchange: per column the norm below row 0 and the row-0 entry
+		for (int c = tid; c < nw; c += kQ2Threads) {
+			double sb = 0;
+			for (int il = lo_of(1); il < nl; ++il) sb = fma(w(il, c), w(il, c), sb);
+			pslot[2 * c] = sb;
+			pslot[2 * c + 1] = (0 >= r0 && 0 < r1) ? w(0 - r0, c) : 0.0;
+		}
+	} else if (warp == 0) {
 		double s = 0;
 		for (int il = lo_of(1) + lane; il < nl; il += 32) s = fma(w(il, 0), w(il, 0), s);
 #pragma unroll
@@ -596,6 +617,63 @@ __global__ void __launch_bounds__(kQ2Threads) k_qr_cl2(QrArgs a, Qc2Layout lay) 
 		const int par = j & 1;
 		double* vp = vecw + par * nw;
 		double* sl = slot + par * 2;
+		if (a.pivot) {
+			double* ps = pslot + par * 2 * nw;
+			cl.sync();
+			for (int c = j + tid; c < nw; c += kQ2Threads) {
+				tb[c] = cluster_sum_at(cl, ps, 2 * c, P);
+				td[c] = cluster_sum_at(cl, ps, 2 * c + 1, P);
+			}
+			__syncthreads();
+			// pivot: the first column of largest remaining norm (idamax order), identical in every CTA
+			double best = -1.0;
+			int bi = nw;
+			for (int c = j + tid; c < nw; c += kQ2Threads) {
+				const double v = tb[c] + td[c] * td[c];
+				if (v > best) { best = v; bi = c; }
+			}
+#pragma unroll
+			for (int o = 16; o > 0; o >>= 1) {
+				const double ob = __shfl_xor_sync(0xffffffffu, best, o);
+				const int oi = __shfl_xor_sync(0xffffffffu, bi, o);
+				if (ob > best || (ob == best && oi < bi)) { best = ob; bi = oi; }
+			}
+			if (lane == 0) { s_best[warp] = best; s_bidx[warp] = bi; }
+			__syncthreads();
+			int pv = nw;
+			{
+				double b = -1.0;
+				for (int t = 0; t < kQ2Threads / 32; ++t)
+					if (s_best[t] > b || (s_best[t] == b && s_bidx[t] < pv)) { b = s_best[t]; pv = s_bidx[t]; }
+			}
+			if (pv != j && pv < nw) {
+				for (int il = tid; il < nl; il += kQ2Threads) {
+					const double t = w(il, j);
+					w(il, j) = w(il, pv);
+					w(il, pv) = t;
+				}
+				__syncthreads();
+				if (tid == 0) {
+					double t = tb[j]; tb[j] = tb[pv]; tb[pv] = t;
+					t = td[j]; td[j] = td[pv]; td[pv] = t;
+					const int q = perm[j]; perm[j] = perm[pv]; perm[pv] = q;
+				}
+			}
+			__syncthreads();
+			if (tid == 0) {
+				const double xn2 = tb[j], alpha = td[j];
+				double tt = 0, scal = 1.0, beta = alpha;
+				if (xn2 != 0.0) {
+					beta = -copysign(sqrt(alpha * alpha + xn2), alpha);
+					tt = (beta - alpha) / beta;
+					scal = 1.0 / (alpha - beta);
+				}
+				tau[j] = tt;
+				coef[0] = scal;
+				coef[1] = beta;
+				coef[2] = tt;
+			}
+		} else {
 		if (tid == 0) {
 			sl[0] = coef[3];
 			sl[1] = (j >= r0 && j < r1) ? w(j - r0, j) : 0.0;
@@ -621,6 +699,7 @@ __global__ void __launch_bounds__(kQ2Threads) k_qr_cl2(QrArgs a, Qc2Layout lay) 
 				coef[1] = beta;
 				coef[2] = tt;
 			}
+		}
 		}
 		__syncthreads();
 		const double scal = coef[0], tj = coef[2];
@@ -666,8 +745,10 @@ __global__ void __launch_bounds__(kQ2Threads) k_qr_cl2(QrArgs a, Qc2Layout lay) 
 			if (ci < Cc && h == 0) sw[c0 + cb + ci] = tj * s;
 		}
 		__syncthreads();
-		// update, and the partial norm of column j+1 below its diagonal
+		// update, and the partial norms below row j+1 for the next column step (pivoting: of every
+		// remaining column, with the row-(j+1) entries; else of column j+1 only)
 		int G0 = 1;
+		double* psn = pslot + ((j + 1) & 1) * 2 * nw;
 		for (int cb = 0; cb < C; cb += 256) {
 			const ColMap cm(C, cb);
 			if (cb == 0) G0 = cm.G;
@@ -681,7 +762,19 @@ __global__ void __launch_bounds__(kQ2Threads) k_qr_cl2(QrArgs a, Qc2Layout lay) 
 					w(il, c) = u;
 					if (r0 + il > j + 1) ns = fma(u, u, ns);
 				}
-				if (c == j + 1) partn[g] = ns;
+				if (a.pivot) part[g * 256 + ci] = ns;
+				else if (c == j + 1) partn[g] = ns;
+			}
+			if (a.pivot) {
+				__syncthreads();
+				if (tid < cm.Cc) {
+					const int c = c0 + cb + tid;
+					double sb = 0;
+					for (int gg = 0; gg < cm.G; ++gg) sb += part[gg * 256 + tid];
+					psn[2 * c] = sb;
+					psn[2 * c + 1] = (j + 1 >= r0 && j + 1 < r1) ? w(j + 1 - r0, c) : 0.0;
+				}
+				__syncthreads();
 			}
 		}
 		__syncthreads();
@@ -693,14 +786,32 @@ __global__ void __launch_bounds__(kQ2Threads) k_qr_cl2(QrArgs a, Qc2Layout lay) 
 		}
 		__syncthreads();
 	}
-	const int rank = kq;
+	int rank = kq;
+	if (a.pivot) {
+		// the reference's rank rule on R's diagonal, gathered from its owners (|R_kk| < 16 eps R_00)
+		cl.sync();
+		for (int k = tid; k < kq; k += kQ2Threads) {
+			const int owner = k / mb;
+			tb[k] = cl.map_shared_rank(W, owner)[(long long)(k - owner * mb) * ldw + k];
+		}
+		__syncthreads();
+		if (tid == 0) {
+			int rk = kq;
+			for (int k = 1; k < kq; ++k)
+				if (fabs(tb[k]) < 16.0 * DBL_EPSILON * tb[0]) { rk = k; break; }
+			coef[3] = double(rk);
+		}
+		__syncthreads();
+		rank = int(coef[3]);
+		cl.sync();  // the diagonal reads are done before anything rewrites W
+	}
 	if (me == 0 && tid == 0 && a.rank_out) *a.rank_out = rank;
 	for (long long e = tid; e < (long long)nl * nw; e += kQ2Threads) {
 		const int il = int(e / nw), c = int(e % nw), r = r0 + il;
 		if (r >= rank) continue;
 		const double v = (r <= c) ? w(il, c) : 0.0;
-		if (!a.transpose) a.C[(long long)r * nw + c] = v;
-		else a.C[(long long)c * rank + r] = v;
+		if (!a.transpose) a.C[(long long)r * nw + perm[c]] = v;
+		else a.C[(long long)perm[c] * rank + r] = v;
 	}
 	if (!a.want_q) {
 		cl.sync();  // every CTA's shared memory stays alive until all remote reads are done
@@ -832,7 +943,7 @@ void launch_qr(const QrArgs& a, cudaStream_t s) {
 			return;
 		}
 	}
-	if (!a.pivot) {
+	{
 		Qc2Layout l2;
 		const int P2 = qr_cl2_size(mw, nw, l2);
 		if (P2 > 1) {
