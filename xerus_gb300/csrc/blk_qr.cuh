@@ -8,6 +8,24 @@ namespace xtt {
 
 constexpr int kBlkQrMaxCols = 64;
 
+// Householder scalars of dlarfg from alpha and ||x||^2 below the diagonal:
+// beta = -sign(alpha) sqrt(alpha^2 + xn2), tau = (beta - alpha) / beta,
+// scal = 1 / (alpha - beta). With q = alpha - beta, tau = -q^2 / (beta q) and
+// scal = beta / (beta q): one division instead of two (a dependent FP64 division
+// costs ~400 cycles on GB300). Agrees with the two-division form to a few ulp.
+__device__ __forceinline__ void reflector_scalars(double alpha, double xn2, double& beta, double& tau, double& scal) {
+	beta = alpha;
+	tau = 0.0;
+	scal = 1.0;
+	if (xn2 != 0.0) {
+		beta = -copysign(sqrt(fma(alpha, alpha, xn2)), alpha);
+		const double q = alpha - beta;
+		const double inv = 1.0 / (beta * q);
+		tau = -(q * q) * inv;
+		scal = beta * inv;
+	}
+}
+
 struct BlkQrSmem {
 	double red[32];
 	double coef[4];
@@ -36,12 +54,8 @@ __device__ inline void blk_qr(const double* A, long long lda, int m, int n, int 
 		const double xn2 = block_sum(part, sh.red);
 		if (tid == 0) {
 			const double alpha = w(j, j);
-			double t = 0, scal = 1.0, beta = alpha;
-			if (xn2 != 0.0) {
-				beta = -copysign(sqrt(alpha * alpha + xn2), alpha);
-				t = (beta - alpha) / beta;
-				scal = 1.0 / (alpha - beta);
-			}
+			double t, scal, beta;
+			reflector_scalars(alpha, xn2, beta, t, scal);
 			sh.tau[j] = t;
 			sh.coef[0] = scal;
 			sh.coef[1] = beta;
