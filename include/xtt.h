@@ -167,6 +167,24 @@ int xtt_entries(const xtt_tensor* x, const int64_t* positions, int64_t count, do
 int xtt_dot_noalloc(int64_t order, const int64_t* dims, const int64_t* x_ranks, const double* x_cores,
                     const int64_t* y_ranks, const double* y_cores, double* result, void* stream);
 
+/* ----------------------------------------------------------------- files */
+/* xerus's binary data files for TTTensor / TTOperator: misc::save_to_file /
+ * load_from_file (include/xerus/misc/fileIO.h:103-162) with the TTNetwork,
+ * TensorNetwork and Tensor stream writers (src/xerus/ttNetwork.cpp:1454-1488,
+ * src/xerus/tensorNetwork.cpp:1429-1500, src/xerus/tensor.cpp:1781-1830). Files
+ * written here are byte-identical to the reference's for the same tensor; files
+ * from the reference load here (dense or sparse components; binary format only). */
+int xtt_tensor_save(const xtt_tensor* t, const char* path);
+int xtt_tensor_load(xtt_context* ctx, const char* path, xtt_tensor** out);
+/* The same format from / into host memory. encode: size receives the byte
+ * count; buffer may be NULL to query it. decode: dims (order) and ranks
+ * (order + 1) are written if both are non-NULL, cores if non-NULL. */
+int xtt_file_encode(int is_operator, int64_t order, const int64_t* dims, const int64_t* ranks, const double* cores,
+                    int canonicalized, int64_t core_position, uint8_t* buffer, int64_t capacity, int64_t* size);
+int xtt_file_decode(const uint8_t* buffer, int64_t size, int* is_operator, int64_t* order, int64_t* dims,
+                    int64_t* ranks, int64_t dims_capacity, double* cores, int64_t cores_capacity, int64_t* cores_count,
+                    int* canonicalized, int64_t* core_position);
+
 /* ------------------------------------------------------------------- ALS */
 typedef struct xtt_als_options {
 	int32_t sites;                   /* ALSVariant::sites: 1 = ALS, 2 = DMRG (als.h:112) */

@@ -15,6 +15,7 @@
 #include <cstdio>
 #include <cstring>
 #include <fstream>
+#include <iterator>
 #include <random>
 #include <string>
 #include <vector>
@@ -608,6 +609,36 @@ static void adf_case(const std::string& tag, const std::vector<size_t>& dims, si
 static void case_adf() { adf_case("small", {4, 5, 3, 5, 4, 3}, 3, 2000, 30, true, true); }
 static void case_adf_cfg5() { adf_case("cfg5", std::vector<size_t>(10, 8), 6, 200000, 50, false, true); }
 
+// xerus's own binary file format (misc::save_to_file): the bytes of files written
+// by the reference, with the numbers they hold, for byte-exact writer/reader tests.
+static void save_file_bytes(const std::string& name, const std::string& path) {
+	std::ifstream f(path, std::ios::binary);
+	std::vector<uint8_t> bytes((std::istreambuf_iterator<char>(f)), std::istreambuf_iterator<char>());
+	save(name, bytes);
+}
+
+static void case_fileio() {
+	reseed();
+	TTTensor x = TTTensor::random({3, 4, 2, 5}, {2, 7, 3});
+	save_tt("x", x);
+	misc::save_to_file(x, g_out + "/x.xrs");
+	save_file_bytes("x_bytes", g_out + "/x.xrs");
+	TTTensor y = x;
+	y.move_core(2);
+	save_tt("y", y);
+	misc::save_to_file(y, g_out + "/y.xrs");
+	save_file_bytes("y_bytes", g_out + "/y.xrs");
+	TTTensor z = x + x;  // a sum is not canonical
+	save_tt("z", z);
+	save<int64_t>("z_canon", {int64_t(z.canonicalized), int64_t(z.corePosition)});
+	misc::save_to_file(z, g_out + "/z.xrs");
+	save_file_bytes("z_bytes", g_out + "/z.xrs");
+	TTOperator A = laplace_operator(4, 3, nullptr, false);
+	save_op("A", A);
+	misc::save_to_file(A, g_out + "/A.xrs");
+	save_file_bytes("A_bytes", g_out + "/A.xrs");
+}
+
 int main(int argc, char** argv) {
 	if (argc != 3) {
 		std::fprintf(stderr, "usage: %s <case> <outdir>\n", argv[0]);
@@ -624,6 +655,7 @@ int main(int argc, char** argv) {
 	else if (c == "dmrg") case_dmrg();
 	else if (c == "adf") case_adf();
 	else if (c == "adf_cfg5") case_adf_cfg5();
+	else if (c == "fileio") case_fileio();
 	else {
 		std::fprintf(stderr, "unknown case %s\n", c.c_str());
 		return 2;

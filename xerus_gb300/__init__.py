@@ -9,6 +9,7 @@ frob_norm, TTTensor.random, move_core, round, ALS_SPD / DMRG_SPD / ASD_SPD
 There is no CPU fallback: without the built library or a GPU, calls raise.
 """
 import ctypes
+import os
 import sys
 
 import numpy as np
@@ -17,7 +18,7 @@ from . import _lib as L
 
 __all__ = ["Context", "TTTensor", "TTOperator", "frob_norm", "dot", "residual", "ALSVariant", "ALS_SPD", "DMRG_SPD",
            "ASD_SPD", "ADFVariant", "ADF", "SinglePointMeasurementSet", "PerformanceData", "seed", "EPSILON",
-           "XttError", "FP64", "MIXED", "als_batch"]
+           "XttError", "FP64", "MIXED", "als_batch", "save_to_file", "load_from_file", "file_encode", "file_decode"]
 
 EPSILON = 8 * np.finfo(np.float64).eps  # include/xerus/basic.h:50
 FP64, MIXED = 0, 1
@@ -286,6 +287,64 @@ class TTOperator(_TT):
         t = TTOperator(dims, [1] + [int(c.shape[3]) for c in cores], ctx=ctx)
         t.set_cores(cores)
         return t
+
+
+def save_to_file(x, path):
+    """misc::save_to_file(x, path) in xerus's binary format (include/xerus/misc/fileIO.h:103-162)."""
+    L.check(x.lib.xtt_tensor_save(x.handle, os.fsencode(path)))
+
+
+def load_from_file(path, ctx=None):
+    """misc::load_from_file for a TTTensor or TTOperator data file; returns the device tensor."""
+    ctx = ctx or Context.default()
+    h = ctypes.c_void_p()
+    L.check(ctx.lib.xtt_tensor_load(ctx.handle, os.fsencode(path), ctypes.byref(h)))
+    # the kind is the file's header line, which the load has just validated
+    with open(path, "rb") as f:
+        op = f.readline().startswith(b"Xerus xerus::TTNetwork<true>")
+    return (TTOperator if op else TTTensor)(ctx=ctx, _handle=h)
+
+
+def file_encode(cores, is_operator=False, canonicalized=False, core_position=0):
+    """Bytes of xerus's binary data file for the given cores (host only)."""
+    lib = L.load()
+    d = len(cores)
+    dims = [int(c.shape[1]) for c in cores]
+    ranks = [1] + [int(c.shape[-1]) for c in cores]
+    flat = np.ascontiguousarray(np.concatenate([np.asarray(c, dtype=np.float64).ravel() for c in cores]))
+    dv, pd = _i64(dims)
+    rv, pr = _i64(ranks)
+    size = ctypes.c_int64()
+    L.check(lib.xtt_file_encode(int(bool(is_operator)), d, pd, pr, flat.ctypes.data_as(L.c_double_p),
+                                int(bool(canonicalized)), int(core_position), None, 0, ctypes.byref(size)))
+    buf = np.zeros(size.value, dtype=np.uint8)
+    L.check(lib.xtt_file_encode(int(bool(is_operator)), d, pd, pr, flat.ctypes.data_as(L.c_double_p),
+                                int(bool(canonicalized)), int(core_position), buf.ctypes.data_as(ctypes.c_void_p),
+                                buf.size, ctypes.byref(size)))
+    return buf.tobytes()
+
+
+def file_decode(data):
+    """(cores, is_operator, canonicalized, core_position) of a xerus binary data file's bytes (host only)."""
+    lib = L.load()
+    buf = np.frombuffer(bytes(data), dtype=np.uint8)
+    op, order, cnt, canon, pos = ctypes.c_int(), ctypes.c_int64(), ctypes.c_int64(), ctypes.c_int(), ctypes.c_int64()
+    args = (buf.ctypes.data_as(ctypes.c_void_p), buf.size, ctypes.byref(op), ctypes.byref(order))
+    L.check(lib.xtt_file_decode(*args, None, None, 0, None, 0, ctypes.byref(cnt), ctypes.byref(canon),
+                                ctypes.byref(pos)))
+    dims = np.zeros(order.value, dtype=np.int64)
+    ranks = np.zeros(order.value + 1, dtype=np.int64)
+    flat = np.zeros(cnt.value)
+    L.check(lib.xtt_file_decode(*args, dims.ctypes.data_as(L.c_int64_p), ranks.ctypes.data_as(L.c_int64_p),
+                                order.value, flat.ctypes.data_as(L.c_double_p), flat.size, ctypes.byref(cnt),
+                                ctypes.byref(canon), ctypes.byref(pos)))
+    cores, off = [], 0
+    for k in range(order.value):
+        shp = (ranks[k], dims[k], dims[k], ranks[k + 1]) if op.value else (ranks[k], dims[k], ranks[k + 1])
+        sz = int(np.prod(shp))
+        cores.append(flat[off:off + sz].reshape(shp))
+        off += sz
+    return cores, bool(op.value), bool(canon.value), int(pos.value)
 
 
 def frob_norm(x):

@@ -78,6 +78,12 @@ _SIGNATURES = {
     "xtt_context_profile_get": (ctypes.c_int, [VP, ctypes.c_char_p, c_int64_p, c_double_p]),
     "xtt_context_set_cg_path": (ctypes.c_int, [VP, ctypes.c_int]),
     "xtt_context_profile_work": (ctypes.c_int, [VP, ctypes.c_char_p, c_double_p, c_double_p]),
+    "xtt_tensor_save": (ctypes.c_int, [VP, ctypes.c_char_p]),
+    "xtt_tensor_load": (ctypes.c_int, [VP, ctypes.c_char_p, ctypes.POINTER(VP)]),
+    "xtt_file_encode": (ctypes.c_int, [ctypes.c_int, ctypes.c_int64, c_int64_p, c_int64_p, c_double_p, ctypes.c_int,
+                                       ctypes.c_int64, ctypes.c_void_p, ctypes.c_int64, c_int64_p]),
+    "xtt_file_decode": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int64, c_int_p, c_int64_p, c_int64_p, c_int64_p,
+                                       ctypes.c_int64, c_double_p, ctypes.c_int64, c_int64_p, c_int_p, c_int64_p]),
     "xtt_als_batch": (ctypes.c_int, [VP, ctypes.c_int64, ctypes.POINTER(VP), ctypes.POINTER(VP), ctypes.POINTER(VP),
                                      ctypes.POINTER(AlsOptions), ctypes.c_int, c_double_p, c_int64_p,
                                      ctypes.POINTER(BatchReport)]),

@@ -252,6 +252,89 @@ int xtt_tensor_get_cores(const xtt_tensor* t, double* host, int64_t count) {
 	});
 }
 
+int xtt_file_encode(int is_operator, int64_t order, const int64_t* dims, const int64_t* ranks, const double* cores,
+                    int canonicalized, int64_t core_position, uint8_t* buffer, int64_t capacity, int64_t* size) {
+	return guard([&] {
+		ARG(dims && ranks && cores && size, "NULL argument");
+		ARG(order > 0 && order < (1 << 20), "order must be positive");
+		std::vector<int64_t> dv(dims, dims + order), rv(ranks, ranks + order + 1);
+		const std::vector<uint8_t> b = xtt::tt_file_encode(is_operator != 0, dv, rv, cores, canonicalized != 0,
+		                                                   core_position);
+		*size = int64_t(b.size());
+		if (buffer) {
+			ARG(capacity >= int64_t(b.size()), "buffer too small");
+			std::memcpy(buffer, b.data(), b.size());
+		}
+	});
+}
+
+int xtt_file_decode(const uint8_t* buffer, int64_t size, int* is_operator, int64_t* order, int64_t* dims,
+                    int64_t* ranks, int64_t dims_capacity, double* cores, int64_t cores_capacity, int64_t* cores_count,
+                    int* canonicalized, int64_t* core_position) {
+	return guard([&] {
+		ARG(buffer && size >= 0 && is_operator && order && cores_count && canonicalized && core_position,
+		    "NULL argument");
+		const xtt::TtFile f = xtt::tt_file_decode(buffer, size_t(size));
+		*is_operator = f.op ? 1 : 0;
+		*order = int64_t(f.dims.size());
+		*cores_count = int64_t(f.cores.size());
+		*canonicalized = f.canonicalized ? 1 : 0;
+		*core_position = f.core_position;
+		if (dims && ranks) {
+			ARG(dims_capacity >= int64_t(f.dims.size()), "dims capacity too small");
+			std::copy(f.dims.begin(), f.dims.end(), dims);
+			std::copy(f.ranks.begin(), f.ranks.end(), ranks);
+		}
+		if (cores) {
+			ARG(cores_capacity >= int64_t(f.cores.size()), "cores capacity too small");
+			std::copy(f.cores.begin(), f.cores.end(), cores);
+		}
+	});
+}
+
+int xtt_tensor_save(const xtt_tensor* t, const char* path) {
+	return guard([&] {
+		ARG(t && path, "NULL argument");
+		const xtt::Tensor& x = *t->t;
+		std::vector<double> h(x.total_size());
+		size_t off = 0;
+		for (int k = 0; k < x.d; ++k) {
+			XTT_CUDA(cudaMemcpyAsync(h.data() + off, x.core[k], x.core_size(k) * sizeof(double), cudaMemcpyDeviceToHost,
+			                         x.ctx->stream));
+			off += x.core_size(k);
+		}
+		x.ctx->sync();
+		xtt::write_file(path, xtt::tt_file_encode(x.op, x.dims, x.ranks, h.data(), x.canonicalized, x.core_position));
+	});
+}
+
+int xtt_tensor_load(xtt_context* ctx, const char* path, xtt_tensor** out) {
+	return guard([&] {
+		ARG(ctx && path && out, "NULL argument");
+		*out = nullptr;
+		const std::vector<uint8_t> b = xtt::read_file(path);
+		const xtt::TtFile f = xtt::tt_file_decode(b.data(), b.size());
+		auto* x = new xtt::Tensor(ctx->c, f.op, int(f.dims.size()), f.dims.data(), f.ranks.data());
+		ctx->c->tensors++;
+		auto* h = new xtt_tensor{x};
+		try {
+			size_t off = 0;
+			for (int k = 0; k < x->d; ++k) {
+				XTT_CUDA(cudaMemcpyAsync(x->core[k], f.cores.data() + off, x->core_size(k) * sizeof(double),
+				                         cudaMemcpyHostToDevice, x->ctx->stream));
+				off += x->core_size(k);
+			}
+			x->ctx->sync();
+		} catch (...) {
+			xtt_tensor_destroy(h);
+			throw;
+		}
+		x->canonicalized = f.canonicalized;
+		x->core_position = f.core_position;
+		*out = h;
+	});
+}
+
 int xtt_tensor_assign(xtt_tensor* t, const int64_t* ranks, const double* host, int64_t count) {
 	return guard([&] {
 		ARG(t && ranks && host, "NULL argument");

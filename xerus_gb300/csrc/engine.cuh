@@ -167,6 +167,20 @@ void entries(const Tensor& x, const int64_t* positions, int64_t count, double* o
 bool exceeds_maximal_ranks(const Tensor& x);
 std::vector<int64_t> reduce_to_maximal_ranks(std::vector<int64_t> ranks, const std::vector<int64_t>& dims);
 
+// xerus's binary data file of a TTTensor / TTOperator (fileio.cu).
+struct TtFile {
+	bool op = false;
+	std::vector<int64_t> dims, ranks;  // ranks d+1
+	std::vector<double> cores;         // row-major cores, concatenated
+	bool canonicalized = false;
+	int64_t core_position = 0;
+};
+std::vector<uint8_t> tt_file_encode(bool op, const std::vector<int64_t>& dims, const std::vector<int64_t>& ranks,
+                                    const double* cores, bool canonicalized, int64_t core_position);
+TtFile tt_file_decode(const uint8_t* data, size_t size);
+std::vector<uint8_t> read_file(const std::string& path);
+void write_file(const std::string& path, const std::vector<uint8_t>& bytes);
+
 // y <- A x as a TT (cores R_k r_k), allocating y's cores.
 void op_apply_tt(const Tensor& A, const Tensor& x, Tensor& y);
 
