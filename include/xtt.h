@@ -145,6 +145,16 @@ int xtt_frob_norm(const xtt_tensor* x, double* out);
 /* ||A x - b|| / ||b|| in FP64, through an orthogonalising sweep of the TT A x - b
  * (no cancellation). Replaces ALSVariant's residual_f (src/xerus/algorithms/als.cpp:258-261). */
 int xtt_residual(const xtt_tensor* A, const xtt_tensor* x, const xtt_tensor* b, double* out);
+/* A(i/2, j/2) * x(j&0) cast to a TT: the TTStack product (src/xerus/ttStack.cpp:47-173,
+ * src/xerus/ttNetwork.cpp:886-967) with core ranks R_k r_k; x a TT tensor (out a TT
+ * tensor) or a TT operator (out a TT operator, A x as operators). out is created on
+ * x's context; it is canonicalised (rank-revealing move_core) at A's core position
+ * when A is canonical, as the reference's stack cast does. */
+int xtt_apply(const xtt_tensor* A, const xtt_tensor* x, xtt_tensor** out);
+/* x += alpha y: TTNetwork::operator+= (alpha = 1) and operator-= (alpha = -1)
+ * (src/xerus/ttNetwork.cpp:796-856); block cores of ranks r + s, then, when x was
+ * canonical, a rank-revealing move_core back to its core position. */
+int xtt_add(xtt_tensor* x, const xtt_tensor* y, double alpha);
 /* Entries of x at `count` multi-indices (count*order int64, row-major):
  * SinglePointMeasurementSet::measure(TensorNetwork) (src/xerus/measurments.cpp:125-153). */
 int xtt_entries(const xtt_tensor* x, const int64_t* positions, int64_t count, double* out);
@@ -202,6 +212,11 @@ typedef struct xtt_als_options {
 	int32_t exact_environment;       /* DMRG only: 0 reproduces the reference's decreasing half-sweep, which
 	                                    contracts core k (not k+1) into the right environment
 	                                    (src/xerus/algorithms/als.cpp:371); 1 contracts core k+1 */
+	int32_t assume_spd;              /* ALSVariant::assumeSPD (als.h:115), default 1. 0: least squares
+	                                    ||A x - b|| through the projections of A^T A and A^T b (ALS, DMRG,
+	                                    ASD; als.cpp:184-215); the energy is then the residual */
+	int32_t use_residual;            /* ALSVariant::useResidualForEndCriterion (als.h:116) */
+	int32_t reserved;
 } xtt_als_options;
 
 typedef struct xtt_als_report {
@@ -216,12 +231,16 @@ typedef struct xtt_als_report {
 
 int xtt_als_default_options(xtt_als_options* opt);
 /* ALSVariant::solve(A, x, b, numHalfSweeps, convergenceEpsilon, perfData)
- * (src/xerus/algorithms/als.cpp:483-553, include/xerus/algorithms/als.h:152-207)
- * for a symmetric positive definite operator. x is updated in place. The traces
- * (optional, trace_capacity entries each) receive, per recorded point, the
- * residual (if record_residuals) and the flags of PerformanceData (0, 1 = half
- * sweep, 3 = full sweep; include/xerus/algorithms/als.h:109-110); energies gets
- * the energy at the end of every half-sweep. */
+ * (src/xerus/algorithms/als.cpp:483-553, include/xerus/algorithms/als.h:152-207),
+ * for a symmetric positive definite operator (assume_spd = 1) or any operator
+ * (assume_spd = 0). A = NULL is the operator-free form x ~ b (the overloads
+ * without an operator, als.h:181-206; sites = 1 only). x is updated in place.
+ * The traces (optional, trace_capacity entries each) receive, per recorded
+ * point, the residual (if record_residuals: ||A x - b|| / ||b||, or ||x - b||
+ * without an operator, as the reference's PerformanceData) and the flags of
+ * PerformanceData (0, 1 = half sweep, 3 = full sweep; als.h:109-110); energies
+ * gets the energy at the end of every half-sweep. report->residual is always
+ * relative (||x - b|| / ||b|| without an operator). */
 int xtt_als(const xtt_tensor* A, xtt_tensor* x, const xtt_tensor* b, const xtt_als_options* opt,
             xtt_als_report* report, double* residual_trace, int64_t* flag_trace, double* energy_trace,
             int64_t trace_capacity);

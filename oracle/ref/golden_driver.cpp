@@ -136,9 +136,14 @@ static std::vector<int64_t> ranks_of(const TTTensor& x) {
 // 1D Laplacian-sum operator sum_i I x..x (L + V_i) x..x I as a TT operator.
 // rank 2: cores [[L+V, I]], [[I,0],[L+V_k,I]], [[I],[L+V]]; V = nullptr means no potential.
 // rank 3 (potential carried in its own channel): [[L+V_0, I, I]], [[I,0,0],[L,I,0],[V_k,0,I]], [[I],[L],[V]].
-static TTOperator laplace_operator(size_t d, size_t n, const std::vector<std::vector<double>>* V, bool rank3, double shift = 0.0) {
+static TTOperator laplace_operator(size_t d, size_t n, const std::vector<std::vector<double>>* V, bool rank3, double shift = 0.0,
+                                   double convection = 0.0) {
 	TTOperator A(std::vector<size_t>(2 * d, n));
-	auto L = [&](size_t i, size_t j) { return (i == j ? 2.0 : 0.0) - ((i + 1 == j || j + 1 == i) ? 1.0 : 0.0); };
+	// tridiag(-1, 2, -1), plus convection * tridiag(-1, 0, 1) (not symmetric when convection != 0)
+	auto L = [&](size_t i, size_t j) {
+		return (i == j ? 2.0 : 0.0) - ((i + 1 == j || j + 1 == i) ? 1.0 : 0.0) +
+		       convection * ((i + 1 == j ? 1.0 : 0.0) - (j + 1 == i ? 1.0 : 0.0));
+	};
 	auto I = [&](size_t i, size_t j) { return i == j ? 1.0 : 0.0; };
 	auto Vd = [&](size_t k, size_t i, size_t j) { return (V && i == j) ? (*V)[k][i] : 0.0; };
 	const size_t R = rank3 ? 3 : 2;
@@ -476,6 +481,63 @@ static void case_als() {
 	run_als("rag_hs6", als, A3, x3, b3, 6, rpos);
 }
 
+// ALSVariant::operator()(x, b, ...) without an operator: minimises ||x - b||.
+static void run_approx(const std::string& tag, const ALSVariant& variant, TTTensor x, const TTTensor& b, size_t halfSweeps,
+                       const std::vector<std::vector<size_t>>& pos) {
+	PerformanceData perf(false, true);
+	const double energy = variant(x, b, halfSweeps, perf);
+	std::vector<int64_t> flags;
+	save(tag + "_perf_residual", perf_residuals(perf, &flags));
+	save(tag + "_perf_flags", flags);
+	save_scalar(tag + "_energy", energy);
+	save_scalar(tag + "_final_distance", frob_norm(x - b));
+	save(tag + "_ranks", ranks_of(x));
+	save_probes(tag + "_x", x, pos);
+}
+
+static void case_als_nonspd() {
+	// Non-symmetric operator: sum over modes of L + 0.6 * tridiag(-1, 0, 1) (rank 2), d=6, n=4.
+	reseed();
+	const size_t d = 6, n = 4;
+	const std::vector<size_t> dims(d, n);
+	TTOperator A = laplace_operator(d, n, nullptr, false, 0.0, 0.6);
+	TTTensor b = TTTensor::random(dims, 3);
+	TTTensor x = TTTensor::random(dims, 4);
+	x /= frob_norm(x);
+	save_op("A", A);
+	save_tt("b", b);
+	save_tt("x0", x);
+	auto pos = probe_positions(dims, 200, 29);
+	ALSVariant als = ALS;
+	als.convergenceEpsilon = 0.0;
+	run_als("als_hs6", als, A, x, b, 6, pos);
+	ALSVariant asd = ASD;
+	asd.convergenceEpsilon = 0.0;
+	run_als("asd_hs6", asd, A, x, b, 6, pos);
+	ALSVariant dmrg = DMRG;
+	dmrg.convergenceEpsilon = 0.0;
+	run_als("dmrg_hs3", dmrg, A, x, b, 3, pos);
+	// default variant: stops on |d residual| < 1e-6
+	run_als("als_default", ALS, A, x, b, 40, pos);
+	// SPD operator with the residual as the end criterion (useResidualForEndCriterion)
+	TTOperator As = laplace_operator(d, n, nullptr, false);
+	save_op("A_spd", As);
+	ALSVariant res = ALS_SPD;
+	res.useResidualForEndCriterion = true;
+	run_als("spd_useres", res, As, x, b, 20, pos);
+	// without an operator: x (rank 3) approximates c (rank 6)
+	TTTensor c = TTTensor::random(dims, 6);
+	TTTensor y = TTTensor::random(dims, 3);
+	save_tt("c", c);
+	save_tt("y0", y);
+	ALSVariant approx = ALS;
+	approx.convergenceEpsilon = 0.0;
+	run_approx("free_hs4", approx, y, c, 4, pos);
+	ALSVariant approx_res = ALS;
+	approx_res.useResidualForEndCriterion = true;
+	run_approx("free_useres", approx_res, y, c, 10, pos);
+}
+
 static void case_dmrg() {
 	reseed();
 	const size_t d = 8, n = 4;
@@ -656,6 +718,7 @@ int main(int argc, char** argv) {
 	else if (c == "adf") case_adf();
 	else if (c == "adf_cfg5") case_adf_cfg5();
 	else if (c == "fileio") case_fileio();
+	else if (c == "als_nonspd") case_als_nonspd();
 	else {
 		std::fprintf(stderr, "unknown case %s\n", c.c_str());
 		return 2;

@@ -563,6 +563,46 @@ def _push_right_rhs(Rb, bc, xc):
     return np.einsum("sic,tid,cd->st", bc, xc, Rb, optimize=True)
 
 
+# non-symmetric operators: the stacks carry A^T A and A^T b (als.cpp:184-215, 392-399, 414-420)
+def _push_left_op4(L, xc, ac):
+    # L'(c1..c4) = sum L(a1..a4) x(a1,n1,c1) A(a2,n2,n1,c2) A(a3,n2,n3,c3) x(a4,n3,c4)
+    return np.einsum("wxyz,wia,xjib,yjkc,zkd->abcd", L, xc, ac, ac, xc, optimize=True)
+
+
+def _push_right_op4(R, xc, ac):
+    return np.einsum("wia,xjib,yjkc,zkd,abcd->wxyz", xc, ac, ac, xc, R, optimize=True)
+
+
+def _push_left_rhs3(Lb, bc, ac, xc):
+    # Lb'(c1,c2,c3) = sum Lb(a1,a2,a3) b(a1,n1,c1) A(a2,n1,n2,c2) x(a3,n2,c3)
+    return np.einsum("stu,sia,tijb,ujc->abc", Lb, bc, ac, xc, optimize=True)
+
+
+def _push_right_rhs3(Rb, bc, ac, xc):
+    return np.einsum("sia,tijb,ujc,abc->stu", bc, ac, xc, Rb, optimize=True)
+
+
+def local_operator_normal(L, Acores, R):
+    """construct_local_operator for a non-symmetric A (als.cpp:392-399): the
+    projection of A^T A, rows (a, i.., b), columns (a', j.., b')."""
+    if len(Acores) == 1:
+        op = np.einsum("xkqa,kmil,qmjp,ylpb->xiyajb", L, Acores[0], Acores[0], R, optimize=True)
+    else:
+        a0, a1 = Acores
+        op = np.einsum("rkqc,kmil,qmjp,lotu,pozv,suve->ritscjze", L, a0, a0, a1, a1, R, optimize=True)
+    half = op.ndim // 2
+    N = int(np.prod(op.shape[:half]))
+    return op.reshape(N, N), op.shape[half:]
+
+
+def local_rhs_normal(Lb, bcores, Acores, Rb):
+    """construct_local_RHS for a non-symmetric A (als.cpp:414-420): projection of A^T b."""
+    if len(bcores) == 1:
+        return np.einsum("ska,sit,kijl,tlb->ajb", Lb, bcores[0], Acores[0], Rb, optimize=True)
+    return np.einsum("ska,sit,kijl,tmu,lmzv,uvb->ajzb", Lb, bcores[0], Acores[0], bcores[1], Acores[1], Rb,
+                     optimize=True)
+
+
 def local_operator(L, Acores, R):
     """Dense local operator of construct_local_operator (als.cpp:383-401):
     rows (a, i_1..i_s, b), columns (a', j_1..j_s, b')."""
@@ -618,11 +658,27 @@ def als_spd(A: TTOp, x: TT, b: TT, sites: int = 1, num_half_sweeps: int = 0, con
             solver: str = "lapack", preserve_core_position: bool = True, track_residual: bool = False,
             residual_target: float | None = None, canonical_signs: bool = False,
             exact_environment: bool = False) -> ALSResult:
-    """ALSVariant::solve for an SPD operator (src/xerus/algorithms/als.cpp:483-553).
+    """ALSVariant::solve for an SPD operator (ALS_SPD, DMRG_SPD, ASD_SPD); see ``als``."""
+    return als(A, x, b, sites, num_half_sweeps, conv_eps, solver, preserve_core_position, track_residual,
+               residual_target, canonical_signs, exact_environment, assume_spd=True)
+
+
+def als(A: TTOp | None, x: TT, b: TT, sites: int = 1, num_half_sweeps: int = 0, conv_eps: float = 1e-6,
+        solver: str = "lapack", preserve_core_position: bool = True, track_residual: bool = False,
+        residual_target: float | None = None, canonical_signs: bool = False,
+        exact_environment: bool = False, assume_spd: bool = True, use_residual: bool = False) -> ALSResult:
+    """ALSVariant::solve (src/xerus/algorithms/als.cpp:483-553).
 
     ``x`` is updated in place. ``solver`` is "lapack" (lapack_solver, als.cpp:43-71)
-    or "asd" (ASD_solver, als.cpp:73-92). With ``track_residual`` the accurate
-    relative residual is recorded where the reference records perfData.
+    or "asd" (ASD_solver, als.cpp:73-92). ``assume_spd`` False is the
+    non-symmetric form (ALS, DMRG, ASD): the stacks carry A^T A and A^T b
+    (als.cpp:184-215) and the energy is the residual computed from them
+    (als.cpp:282-297). ``A`` None minimises ||x - b|| (the operator-free
+    overloads, als.h:181-206): the local update is the projected b
+    (als.cpp:540-543), the energy 0.5 |x_k|^2 - <x, b> and the residual ||x - b||
+    (als.cpp:299-319). ``use_residual`` is useResidualForEndCriterion.
+    With ``track_residual`` the value the reference adds to its PerformanceData
+    (residual_f, als.cpp:255-320) is recorded after every micro-step.
     Two sites: the decreasing half-sweep contracts core ``cur`` into the right
     environment (als.cpp:371) as the reference does, which makes later half-
     sweeps depend on the sign gauge of the split's singular vectors;
@@ -631,6 +687,10 @@ def als_spd(A: TTOp, x: TT, b: TT, sites: int = 1, num_half_sweeps: int = 0, con
     ``residual_target`` stops at the end of the first half-sweep whose residual
     is at or below it (a time-to-residual measurement, not a reference feature)."""
     d = x.d
+    free = A is None
+    normal = not free and not assume_spd
+    if free and sites != 1:
+        raise ValueError("approximation dmrg not implemented yet")  # als.cpp:539
     target_rank = list(x.ranks)
     norm_b = frob_norm(b)
     canon_end, core_end = x.canonicalized, x.core_position
@@ -672,63 +732,113 @@ def als_spd(A: TTOp, x: TT, b: TT, sites: int = 1, num_half_sweeps: int = 0, con
         if canon_end and core_end >= last:
             x.canonicalized, x.core_position = True, last - 1
         move_core(x, first, keep_rank=True)
+
+    # stack slices (localOperatorSlice / localRhsSlice, als.cpp:184-215)
+    def push_op(side, E, k):
+        if normal:
+            return (_push_left_op4 if side == "L" else _push_right_op4)(E, x.cores[k], A.cores[k])
+        return (_push_left_op if side == "L" else _push_right_op)(E, x.cores[k], A.cores[k])
+
+    def push_rhs(side, E, k):
+        if normal:
+            return (_push_left_rhs3 if side == "L" else _push_right_rhs3)(E, b.cores[k], A.cores[k], x.cores[k])
+        return (_push_left_rhs if side == "L" else _push_right_rhs)(E, b.cores[k], x.cores[k])
+
     # prepare_stacks (als.cpp:217-253)
-    Lop, Rop = [np.ones((1, 1, 1))], [np.ones((1, 1, 1))]
-    Lb, Rb = [np.ones((1, 1))], [np.ones((1, 1))]
+    one_op = np.ones((1, 1, 1, 1)) if normal else np.ones((1, 1, 1))
+    one_rhs = np.ones((1, 1, 1)) if normal else np.ones((1, 1))
+    Lop, Rop, Lb, Rb = [one_op], [one_op], [one_rhs], [one_rhs]
     for i in range(d - 1, first + sites - 1, -1):
-        Rop.append(_push_right_op(Rop[-1], x.cores[i], A.cores[i]))
-        Rb.append(_push_right_rhs(Rb[-1], b.cores[i], x.cores[i]))
+        if not free:
+            Rop.append(push_op("R", Rop[-1], i))
+        Rb.append(push_rhs("R", Rb[-1], i))
     for i in range(first):
-        Lop.append(_push_left_op(Lop[-1], x.cores[i], A.cores[i]))
-        Lb.append(_push_left_rhs(Lb[-1], b.cores[i], x.cores[i]))
+        if not free:
+            Lop.append(push_op("L", Lop[-1], i))
+        Lb.append(push_rhs("L", Lb[-1], i))
     cur = first
     inc = True
 
-    def energy_f():
-        # |0.5 <x,Ax> - <x,b>| from the stacks (als.cpp:265-278)
-        xAx, bx = Lop[-1], Lb[-1]
+    def stack_terms():
+        # full contractions <x, A x> (<Ax, Ax>) and <x, b> (<b, A x>) through the current stacks
+        bx = Lb[-1]
         for i in range(sites):
-            xAx = _push_left_op(xAx, x.cores[cur + i], A.cores[cur + i])
-            bx = _push_left_rhs(bx, b.cores[cur + i], x.cores[cur + i])
-        return abs(0.5 * float(np.sum(xAx * Rop[-1])) - float(np.sum(bx * Rb[-1])))
+            bx = push_rhs("L", bx, cur + i)
+        xb = float(np.sum(bx * Rb[-1]))
+        if free:
+            return None, xb
+        xAx = Lop[-1]
+        for i in range(sites):
+            xAx = push_op("L", xAx, cur + i)
+        return float(np.sum(xAx * Rop[-1])), xb
+
+    def residual_f():
+        if free:
+            return orthogonal_norm(tt_add(x, tt_scale(b, -1.0)))
+        if normal:
+            xAtAx, bAx = stack_terms()
+            return np.sqrt(xAtAx - 2 * bAx + norm_b ** 2) / norm_b
+        return residual(A, x, b)
+
+    def energy_f():
+        if normal or use_residual:
+            return residual_f()
+        xAx, xb = stack_terms()
+        if free:
+            return 0.5 * float(np.sum(x.cores[cur] * x.cores[cur])) - xb
+        return abs(0.5 * xAx - xb)  # |0.5 <x,Ax> - <x,b>| (als.cpp:265-278)
 
     res = ALSResult(energy=0.0)
 
     def record(flag):
         if track_residual:
-            res.residuals.append(residual(A, x, b))
+            res.residuals.append(residual_f())
             res.flags.append(flag)
 
     energy, last_e, last_e2 = energy_f(), 1e101, 1e102
     record(FLAG_FINISHED_FULLSWEEP)
     half = 0
     while True:
-        # local operator L . A_k [. A_k+1] . R and rhs (als.cpp:383-423)
-        M, shape_x = local_operator(Lop[-1], A.cores[cur:cur + sites], Rop[-1])
-        N = M.shape[0]
-        rhs = local_rhs(Lb[-1], b.cores[cur:cur + sites], Rb[-1]).reshape(N)
-        if solver == "asd":
-            xv = x.cores[cur].reshape(N)
-            grad = rhs - M @ xv
-            alpha = float(grad @ grad) / float(grad @ (M @ grad))
-            x.cores[cur] = (xv + alpha * grad).reshape(shape_x)
+        if free:
+            # x_k = the projection of b (als.cpp:540-543)
+            x.cores[cur] = local_rhs(Lb[-1], b.cores[cur:cur + 1], Rb[-1])
         else:
-            xv = dense_solve(M, rhs).reshape(shape_x)
-            if sites == 1:
-                x.cores[cur] = xv
+            # local operator and rhs (als.cpp:383-423)
+            if normal:
+                M, shape_x = local_operator_normal(Lop[-1], A.cores[cur:cur + sites], Rop[-1])
+                rhs = local_rhs_normal(Lb[-1], b.cores[cur:cur + sites], A.cores[cur:cur + sites], Rb[-1])
             else:
-                a_, j1, j2, b_ = xv.shape
-                U, S, Vt = svd_trunc(xv.reshape(a_ * j1, j2 * b_), target_rank[cur], EPSILON, canonical_signs)
-                s = len(S)
-                if inc:
-                    x.cores[cur] = U.reshape(a_, j1, s)
-                    x.cores[cur + 1] = (S[:, None] * Vt).reshape(s, j2, b_)
+                M, shape_x = local_operator(Lop[-1], A.cores[cur:cur + sites], Rop[-1])
+                rhs = local_rhs(Lb[-1], b.cores[cur:cur + sites], Rb[-1])
+            N = M.shape[0]
+            rhs = rhs.reshape(N)
+            if solver == "asd":
+                xv = x.cores[cur].reshape(N)
+                grad = rhs - M @ xv
+                if normal:
+                    # grad <- A_loc^T grad, alpha = ||grad|| / ||A_loc grad|| (als.cpp:86-89)
+                    grad = M.T @ grad
+                    alpha = float(np.linalg.norm(grad)) / float(np.linalg.norm(M @ grad))
                 else:
-                    x.cores[cur] = (U * S[None, :]).reshape(a_, j1, s)
-                    x.cores[cur + 1] = Vt.reshape(s, j2, b_)
-                # set_component on a non-core position clears the canonical flag (ttNetwork.cpp:491)
-                if not (x.canonicalized and x.core_position == cur + 1):
-                    x.canonicalized = False
+                    alpha = float(grad @ grad) / float(grad @ (M @ grad))
+                x.cores[cur] = (xv + alpha * grad).reshape(shape_x)
+            else:
+                xv = dense_solve(M, rhs).reshape(shape_x)
+                if sites == 1:
+                    x.cores[cur] = xv
+                else:
+                    a_, j1, j2, b_ = xv.shape
+                    U, S, Vt = svd_trunc(xv.reshape(a_ * j1, j2 * b_), target_rank[cur], EPSILON, canonical_signs)
+                    s = len(S)
+                    if inc:
+                        x.cores[cur] = U.reshape(a_, j1, s)
+                        x.cores[cur + 1] = (S[:, None] * Vt).reshape(s, j2, b_)
+                    else:
+                        x.cores[cur] = (U * S[None, :]).reshape(a_, j1, s)
+                        x.cores[cur + 1] = Vt.reshape(s, j2, b_)
+                    # set_component on a non-core position clears the canonical flag (ttNetwork.cpp:491)
+                    if not (x.canonicalized and x.core_position == cur + 1):
+                        x.canonicalized = False
         # check_for_end_of_sweep (als.cpp:426-475)
         if (not inc and cur == first) or (inc and cur == last - sites):
             half += 1
@@ -750,19 +860,21 @@ def als_spd(A: TTOp, x: TT, b: TT, sites: int = 1, num_half_sweeps: int = 0, con
         if inc:
             if sites == 1:
                 move_core(x, cur + 1, keep_rank=True)
-            Rop.pop()
+            if not free:
+                Rop.pop()
+                Lop.append(push_op("L", Lop[-1], cur))
             Rb.pop()
-            Lop.append(_push_left_op(Lop[-1], x.cores[cur], A.cores[cur]))
-            Lb.append(_push_left_rhs(Lb[-1], b.cores[cur], x.cores[cur]))
+            Lb.append(push_rhs("L", Lb[-1], cur))
             cur += 1
         else:
             if sites == 1:
                 move_core(x, cur - 1, keep_rank=True)
-            Lop.pop()
-            Lb.pop()
             kc = cur + 1 if (sites == 2 and exact_environment) else cur
-            Rop.append(_push_right_op(Rop[-1], x.cores[kc], A.cores[kc]))
-            Rb.append(_push_right_rhs(Rb[-1], b.cores[kc], x.cores[kc]))
+            if not free:
+                Lop.pop()
+                Rop.append(push_op("R", Rop[-1], kc))
+            Lb.pop()
+            Rb.append(push_rhs("R", Rb[-1], kc))
             cur -= 1
 
 

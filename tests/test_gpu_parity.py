@@ -250,6 +250,69 @@ def test_dmrg_spd(ctx, golden):
     assert rel_err(x.entries(z["d8_r4_hs4_x_probe_pos"]), o.tt_entries(ref, z["d8_r4_hs4_x_probe_pos"])) < 1e-9
 
 
+# Non-symmetric operator (Laplacian sum + 0.6 * convection, d=6, n=4), useResidualForEndCriterion
+# and the operator-free form (x of rank 3 approximates b of rank 6), against the reference.
+NONSPD_RUNS = {
+    # tag: (variant, half-sweeps, convergenceEpsilon 0)
+    "als_hs6": ("ALS", 6, True),
+    "asd_hs6": ("ASD", 6, True),
+    "als_default": ("ALS", 40, False),
+    "spd_useres": ("ALS_SPD", 20, False),
+    "free_hs4": ("ALS", 4, True),
+    "free_useres": ("ALS", 10, False),
+}
+
+
+@pytest.mark.parametrize("tag", list(NONSPD_RUNS))
+def test_als_nonspd_and_operator_free_match_reference(ctx, golden, tag):
+    """The non-symmetric sweep contracts A^T A and A^T b as TT operators of rank R^2 and
+    R s (the reference contracts two copies of A in 4-leg stacks; the projections are the
+    same). The reference's non-symmetric ASD step (alpha = ||g|| / ||M g||, als.cpp:86-89)
+    diverges on this operator; it is reproduced as it is."""
+    z = golden("als_nonspd")
+    name, hs, eps0 = NONSPD_RUNS[tag]
+    v = getattr(xg, name).copy()
+    if eps0:
+        v.convergenceEpsilon = 0.0
+    v.useResidualForEndCriterion = tag.endswith("useres")
+    perf = xg.PerformanceData()
+    if tag.startswith("free"):
+        x, b = dev_tt(ctx, tt_of(z, "y0")), dev_tt(ctx, tt_of(z, "c"))
+        energy = v(x, b, hs, perf)
+    else:
+        A = dev_op(ctx, op_of(z, "A_spd" if tag == "spd_useres" else "A"))
+        x, b = dev_tt(ctx, tt_of(z, "x0")), dev_tt(ctx, tt_of(z, "b"))
+        energy = v(A, x, b, hs, perf)
+    ref_e = z[tag + "_energy"][0]
+    assert abs(energy / ref_e - 1) < 1e-9, (energy, ref_e)
+    assert [1] + x.ranks() + [1] == list(z[tag + "_ranks"])
+    pr, mine = z[tag + "_perf_residual"], np.array(perf.residuals)
+    assert len(mine) == len(pr)
+    assert list(perf.flags) == list(z[tag + "_perf_flags"])
+    err = np.abs(mine / pr - 1)
+    assert err.max() < 1e-9, (err.max(), int(err.argmax()))
+    assert rel_err(x.entries(z[tag + "_x_probe_pos"]), z[tag + "_x_probe_val"]) < 1e-8
+
+
+def test_dmrg_nonspd(ctx, golden):
+    """Two-site non-symmetric sweep: the first half-sweep against the reference (later
+    half-sweeps depend on the singular vectors' sign gauge, as for DMRG_SPD), all three
+    against the oracle in the device's gauge."""
+    z = golden("als_nonspd")
+    Ah, bh, xh = op_of(z, "A"), tt_of(z, "b"), tt_of(z, "x0")
+    A, b, x = dev_op(ctx, Ah), dev_tt(ctx, bh), dev_tt(ctx, xh)
+    v = xg.DMRG.copy()
+    v.convergenceEpsilon = 0.0
+    perf = xg.PerformanceData()
+    energy = v(A, x, b, 3, perf)
+    assert [1] + x.ranks() + [1] == list(z["dmrg_hs3_ranks"])
+    assert rel_err(perf.residuals[:4], z["dmrg_hs3_perf_residual"][:4]) < 1e-9
+    ref = xh.copy()
+    r = o.als(Ah, ref, bh, 2, 3, 0.0, track_residual=True, canonical_signs=True, assume_spd=False)
+    assert abs(energy / r.energy - 1) < 1e-9
+    assert rel_err(x.entries(z["dmrg_hs3_x_probe_pos"]), o.tt_entries(ref, z["dmrg_hs3_x_probe_pos"])) < 1e-8
+
+
 def test_dmrg_spd_potential_d20(ctx, golden):
     """Laplacian + potential, rank-3 operator, d=20, n=8, rank 8. The first
     half-sweep against the oracle (pinned to the reference); the corrected

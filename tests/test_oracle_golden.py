@@ -135,6 +135,42 @@ def test_dmrg_spd_small(golden):
     assert rel_err(res.residuals, z["d8_r4_hs4_perf_residual"]) < 1e-8
 
 
+# Non-symmetric operator (Laplacian sum + 0.6 * convection), the operator-free
+# form (x approximates b) and useResidualForEndCriterion, against the reference.
+NONSPD_RUNS = {
+    # tag: (oracle keyword arguments)
+    "als_hs6": dict(num_half_sweeps=6, conv_eps=0.0, assume_spd=False),
+    "asd_hs6": dict(num_half_sweeps=6, conv_eps=0.0, assume_spd=False, solver="asd"),
+    "dmrg_hs3": dict(num_half_sweeps=3, conv_eps=0.0, assume_spd=False, sites=2),
+    "als_default": dict(num_half_sweeps=40, assume_spd=False),
+    "spd_useres": dict(num_half_sweeps=20, use_residual=True),
+    "free_hs4": dict(num_half_sweeps=4, conv_eps=0.0),
+    "free_useres": dict(num_half_sweeps=10, use_residual=True),
+}
+
+
+def nonspd_inputs(z, tag):
+    """(A, x0, b) of a run in the non-SPD fixture (A None for the operator-free runs)."""
+    if tag.startswith("free"):
+        return None, tt_of(z, "y0"), tt_of(z, "c")
+    return op_of(z, "A_spd" if tag == "spd_useres" else "A"), tt_of(z, "x0"), tt_of(z, "b")
+
+
+@pytest.mark.parametrize("tag", list(NONSPD_RUNS))
+def test_als_nonspd_and_operator_free(golden, tag):
+    z = golden("als_nonspd")
+    A, x, b = nonspd_inputs(z, tag)
+    res = o.als(A, x, b, track_residual=True, **NONSPD_RUNS[tag])
+    assert abs(res.energy / z[tag + "_energy"][0] - 1) < 1e-11
+    assert [1] + x.ranks + [1] == list(z[tag + "_ranks"])
+    assert rel_err(o.tt_entries(x, z[tag + "_x_probe_pos"]), z[tag + "_x_probe_val"]) < 1e-12
+    # the value the reference adds to PerformanceData after every micro-step
+    pr = z[tag + "_perf_residual"]
+    assert len(res.residuals) == len(pr)
+    assert rel_err(res.residuals, pr) < 1e-12
+    assert list(res.flags) == list(z[tag + "_perf_flags"])
+
+
 @pytest.mark.slow
 def test_dmrg_spd_potential_d20(golden):
     z = golden("dmrg")

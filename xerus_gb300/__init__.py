@@ -16,9 +16,9 @@ import numpy as np
 
 from . import _lib as L
 
-__all__ = ["Context", "TTTensor", "TTOperator", "frob_norm", "dot", "residual", "ALSVariant", "ALS_SPD", "DMRG_SPD",
+__all__ = ["Context", "TTTensor", "TTOperator", "frob_norm", "dot", "residual", "ALSVariant", "ALS", "ALS_SPD", "DMRG", "DMRG_SPD", "ASD",
            "ASD_SPD", "ADFVariant", "ADF", "SinglePointMeasurementSet", "PerformanceData", "seed", "EPSILON",
-           "XttError", "FP64", "MIXED", "als_batch", "save_to_file", "load_from_file", "file_encode", "file_decode"]
+           "XttError", "FP64", "MIXED", "als_batch", "apply", "save_to_file", "load_from_file", "file_encode", "file_decode"]
 
 EPSILON = 8 * np.finfo(np.float64).eps  # include/xerus/basic.h:50
 FP64, MIXED = 0, 1
@@ -209,6 +209,44 @@ class _TT:
     def __itruediv__(self, f):
         return self.__imul__(1.0 / f)
 
+    def __mul__(self, f):
+        if not isinstance(f, (int, float, np.integer, np.floating)):
+            return NotImplemented
+        y = self.copy()
+        y *= f
+        return y
+
+    __rmul__ = __mul__
+
+    def __truediv__(self, f):
+        return self * (1.0 / f)
+
+    def __neg__(self):
+        return self * -1.0
+
+    # -- TTNetwork::operator+= / -= (src/xerus/ttNetwork.cpp:796-856)
+    def __iadd__(self, other):
+        if other is self:
+            other = other.copy()
+        L.check(self.lib.xtt_add(self.handle, other.handle, 1.0))
+        return self
+
+    def __isub__(self, other):
+        if other is self:
+            other = other.copy()
+        L.check(self.lib.xtt_add(self.handle, other.handle, -1.0))
+        return self
+
+    def __add__(self, other):
+        y = self.copy()
+        y += other
+        return y
+
+    def __sub__(self, other):
+        y = self.copy()
+        y -= other
+        return y
+
     # -- TTNetwork operations
     def move_core(self, position, keepRank=False):
         L.check(self.lib.xtt_move_core(self.handle, int(position), int(bool(keepRank))))
@@ -282,11 +320,25 @@ class TTOperator(_TT):
     is_operator = True
 
     @staticmethod
-    def from_cores(cores, ctx=None):
+    def from_cores(cores, ctx=None, canonicalized=False, core_position=0):
         dims = [int(c.shape[1]) for c in cores]
         t = TTOperator(dims, [1] + [int(c.shape[3]) for c in cores], ctx=ctx)
         t.set_cores(cores)
+        t.set_canonical(canonicalized, core_position)
         return t
+
+    def __matmul__(self, x):
+        """A(i/2, j/2) * x(j&0) (or A * B for an operator B) as a TT; see ``apply``."""
+        return apply(self, x)
+
+
+def apply(A, x):
+    """The TT of A x: xerus's TTStack product cast to a TTTensor (TTOperator for an
+    operator x), src/xerus/ttStack.cpp:47-173; canonicalised at A's core position
+    when A is canonical."""
+    h = ctypes.c_void_p()
+    L.check(x.lib.xtt_apply(A.handle, x.handle, ctypes.byref(h)))
+    return type(x)(ctx=x.ctx, _handle=h)
 
 
 def save_to_file(x, path):
@@ -377,7 +429,9 @@ class PerformanceData:
 
 
 class ALSVariant:
-    """xerus::ALSVariant for SPD operators (include/xerus/algorithms/als.h:37-207)."""
+    """xerus::ALSVariant (include/xerus/algorithms/als.h:37-207): SPD operators
+    (assumeSPD), any operator (least squares through A^T A), or no operator
+    (x approximates b)."""
 
     FLAG_FINISHED_HALFSWEEP = 1
     FLAG_FINISHED_FULLSWEEP = 3
@@ -420,12 +474,22 @@ class ALSVariant:
         o.max_rank = int(self.max_rank)
         o.svd_epsilon = float(self.svd_epsilon)
         o.exact_environment = int(bool(self.exact_environment))
+        o.assume_spd = int(bool(self.assumeSPD))
+        o.use_residual = int(bool(self.useResidualForEndCriterion))
         return o
 
-    def __call__(self, A, x, b, arg=None, perfData=None):
-        """ALS(A, x, b[, numHalfSweeps: int | convergenceEpsilon: float][, perfData]) -> energy."""
-        if not self.assumeSPD:
-            raise NotImplementedError("only the SPD variants (ALS_SPD, DMRG_SPD, ASD_SPD) run on the device")
+    def __call__(self, *args):
+        """ALS(A, x, b[, numHalfSweeps: int | convergenceEpsilon: float][, perfData]) -> energy,
+        or without an operator ALS(x, b[, ...]) minimising ||x - b|| (als.h:152-206)."""
+        if len(args) >= 2 and isinstance(args[0], TTTensor):
+            A, rest = None, args
+        else:
+            A, rest = args[0], args[1:]
+        if len(rest) < 2 or len(rest) > 4:
+            raise TypeError("ALSVariant(A, x, b[, numHalfSweeps | convergenceEpsilon][, perfData])")
+        x, b = rest[0], rest[1]
+        arg = rest[2] if len(rest) > 2 else None
+        perfData = rest[3] if len(rest) > 3 else None
         if isinstance(arg, PerformanceData):
             arg, perfData = None, arg
         hs, eps = self.numHalfSweeps, self.convergenceEpsilon
@@ -438,7 +502,7 @@ class ALSVariant:
         rep = L.AlsReport()
         cap = 4096
         res, flags, en = np.zeros(cap), np.zeros(cap, dtype=np.int64), np.zeros(cap)
-        L.check(x.lib.xtt_als(A.handle, x.handle, b.handle, ctypes.byref(o), ctypes.byref(rep),
+        L.check(x.lib.xtt_als(A.handle if A is not None else None, x.handle, b.handle, ctypes.byref(o), ctypes.byref(rep),
                               res.ctypes.data_as(L.c_double_p), flags.ctypes.data_as(L.c_int64_p),
                               en.ctypes.data_as(L.c_double_p), cap))
         self.last_report = rep
@@ -473,8 +537,12 @@ def als_batch(As, xs, bs, variant=None, numHalfSweeps=8, autotune=False):
                     "ctas": rep.ctas}
 
 
+# the global variants (src/xerus/algorithms/als.cpp:556-563)
+ALS = ALSVariant(1, 0, "lapack", False)
 ALS_SPD = ALSVariant(1, 0, "lapack", True)
+DMRG = ALSVariant(2, 0, "lapack", False)
 DMRG_SPD = ALSVariant(2, 0, "lapack", True)
+ASD = ALSVariant(1, 0, "asd", False)
 ASD_SPD = ALSVariant(1, 0, "asd", True)
 
 

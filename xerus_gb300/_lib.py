@@ -30,6 +30,9 @@ class AlsOptions(ctypes.Structure):
         ("max_rank", ctypes.c_int32),
         ("svd_epsilon", ctypes.c_double),
         ("exact_environment", ctypes.c_int32),
+        ("assume_spd", ctypes.c_int32),
+        ("use_residual", ctypes.c_int32),
+        ("reserved", ctypes.c_int32),
     ]
 
 
@@ -78,6 +81,8 @@ _SIGNATURES = {
     "xtt_context_profile_get": (ctypes.c_int, [VP, ctypes.c_char_p, c_int64_p, c_double_p]),
     "xtt_context_set_cg_path": (ctypes.c_int, [VP, ctypes.c_int]),
     "xtt_context_profile_work": (ctypes.c_int, [VP, ctypes.c_char_p, c_double_p, c_double_p]),
+    "xtt_apply": (ctypes.c_int, [VP, VP, ctypes.POINTER(VP)]),
+    "xtt_add": (ctypes.c_int, [VP, VP, ctypes.c_double]),
     "xtt_tensor_save": (ctypes.c_int, [VP, ctypes.c_char_p]),
     "xtt_tensor_load": (ctypes.c_int, [VP, ctypes.c_char_p, ctypes.POINTER(VP)]),
     "xtt_file_encode": (ctypes.c_int, [ctypes.c_int, ctypes.c_int64, c_int64_p, c_int64_p, c_double_p, ctypes.c_int,

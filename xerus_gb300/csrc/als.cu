@@ -11,6 +11,7 @@
 #include <algorithm>
 #include <cmath>
 #include <cstring>
+#include <memory>
 
 #include <cooperative_groups.h>
 
@@ -541,8 +542,58 @@ __global__ void k_sub(double* out, const double* a, const double* b, long long n
 		out[i] = a[i] - b[i];
 }
 
-__global__ void k_energy(double* out, const double* dd, int sxq, int sxb) {
-	out[0] = fabs(0.5 * dd[sxq] - dd[sxb]);
+// v += (||g|| / ||M g||) g: the non-symmetric ASD step (als.cpp:86-89), squared norms in dd
+__global__ void k_asd_step_normal(double* v, const double* g, long long n, const double* dd, int s0, int s1) {
+	const double alpha = sqrt(dd[s0]) / sqrt(dd[s1]);
+	for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x)
+		v[i] += alpha * g[i];
+}
+
+enum AlsMode { kSpd = 0, kNormal = 1, kFree = 2 };
+
+// e = 0.5 <v, M v> - <v, b_loc> (M v = v without an operator). SPD: |e| (als.cpp:265-278);
+// non-symmetric: sqrt(<Ax, Ax> - 2 <b, Ax> + ||b||^2) / ||b|| = sqrt(2 e + ||b||^2) / ||b||
+// (als.cpp:282-296), clamped at 0 where rounding makes the radicand negative; free: e (als.cpp:306-318).
+__global__ void k_energy(double* out, const double* dd, int sxq, int sxb, int mode, double nb) {
+	const double e = 0.5 * dd[sxq] - dd[sxb];
+	out[0] = mode == kSpd ? fabs(e) : mode == kNormal ? sqrt(fmax(0.0, 2.0 * e + nb * nb)) / nb : e;
+}
+
+// One core of A^T A as a TT operator of rank K^2 (the product the non-symmetric local operator
+// contracts, als.cpp:392-399): B((p q), i, j, (p' q')) = sum_m A(p, m, i, p') A(q, m, j, q').
+__global__ void k_normal_op_core(double* B, const double* A, int K, int L, int n) {
+	const long long total = (long long)K * K * n * n * L * L;
+	for (long long e = blockIdx.x * (long long)blockDim.x + threadIdx.x; e < total; e += (long long)gridDim.x * blockDim.x) {
+		long long t = e;
+		const int q2 = int(t % L); t /= L;
+		const int p2 = int(t % L); t /= L;
+		const int j = int(t % n); t /= n;
+		const int i = int(t % n); t /= n;
+		const int q = int(t % K);
+		const int p = int(t / K);
+		double acc = 0;
+		for (int m = 0; m < n; ++m)
+			acc = fma(A[((size_t(p) * n + m) * n + i) * L + p2], A[((size_t(q) * n + m) * n + j) * L + q2], acc);
+		B[e] = acc;
+	}
+}
+
+// One core of A^T b as a TT of rank s K (the non-symmetric local right-hand side, als.cpp:414-420):
+// C((s p), j, (s' p')) = sum_i b(s, i, s') A(p, i, j, p').
+__global__ void k_normal_rhs_core(double* C, const double* b, const double* A, int Q0, int Q1, int K, int L, int n) {
+	const long long total = (long long)Q0 * K * n * Q1 * L;
+	for (long long e = blockIdx.x * (long long)blockDim.x + threadIdx.x; e < total; e += (long long)gridDim.x * blockDim.x) {
+		long long t = e;
+		const int p2 = int(t % L); t /= L;
+		const int s2 = int(t % Q1); t /= Q1;
+		const int j = int(t % n); t /= n;
+		const int p = int(t % K);
+		const int s0 = int(t / K);
+		double acc = 0;
+		for (int i = 0; i < n; ++i)
+			acc = fma(b[(size_t(s0) * n + i) * Q1 + s2], A[((size_t(p) * n + i) * n + j) * L + p2], acc);
+		C[e] = acc;
+	}
 }
 
 static unsigned blocks_for(long long n) { return unsigned(std::max<long long>(1, std::min<long long>((n + 255) / 256, 2048))); }
@@ -555,17 +606,20 @@ struct Stacks {
 	std::vector<double*> Lop, Rop, Lb, Rb;
 };
 
+// A and b are what the sweep contracts: the SPD operator and b; A^T A and A^T b for a
+// non-symmetric operator; without an operator, a rank-1 placeholder whose cores are never read.
 struct AlsState {
 	Context& c;
 	const Tensor& A;
 	Tensor& x;
 	const Tensor& b;
 	const AlsOptions& o;
-	int d, S;
+	int d, S, mode;
+	double nb;  // ||b|| of the caller's b
 	Stacks st;
-	double *v, *bloc, *q, *grad;
-	AlsState(Context& cc, const Tensor& AA, Tensor& xx, const Tensor& bb, const AlsOptions& oo)
-	    : c(cc), A(AA), x(xx), b(bb), o(oo), d(xx.d), S(oo.sites) {}
+	double *v, *bloc, *q, *grad, *q2;
+	AlsState(Context& cc, const Tensor& AA, Tensor& xx, const Tensor& bb, const AlsOptions& oo, int md, double norm_b)
+	    : c(cc), A(AA), x(xx), b(bb), o(oo), d(xx.d), S(oo.sites), mode(md), nb(norm_b) {}
 
 	LocalShape shape(int cur) const {
 		LocalShape s;
@@ -580,8 +634,9 @@ struct AlsState {
 		return s;
 	}
 	void push_left(int k) {
-		push_left_op(c, st.Lop[k], x.core[k], A.core[k], st.Lop[k + 1], x.ranks[k], A.ranks[k], x.dims[k],
-		             x.ranks[k + 1], A.ranks[k + 1]);
+		if (mode != kFree)
+			push_left_op(c, st.Lop[k], x.core[k], A.core[k], st.Lop[k + 1], x.ranks[k], A.ranks[k], x.dims[k],
+			             x.ranks[k + 1], A.ranks[k + 1]);
 		push_left_rhs(c, st.Lb[k], b.core[k], x.core[k], st.Lb[k + 1], b.ranks[k], x.ranks[k], x.dims[k], b.ranks[k + 1],
 		              x.ranks[k + 1]);
 	}
@@ -593,8 +648,9 @@ struct AlsState {
 		                           x.dims[kc] == x.dims[slot]),
 		            "index dimensions do not coincide (the two-site decreasing sweep contracts core k into the right "
 		            "environment of bond k+2, which needs equal neighbouring ranks)");
-		push_right_op(c, st.Rop[slot + 1], x.core[kc], A.core[kc], st.Rop[slot], x.ranks[kc], A.ranks[kc], x.dims[kc],
-		              x.ranks[kc + 1], A.ranks[kc + 1]);
+		if (mode != kFree)
+			push_right_op(c, st.Rop[slot + 1], x.core[kc], A.core[kc], st.Rop[slot], x.ranks[kc], A.ranks[kc],
+			              x.dims[kc], x.ranks[kc + 1], A.ranks[kc + 1]);
 		push_right_rhs(c, st.Rb[slot + 1], b.core[kc], x.core[kc], st.Rb[slot], b.ranks[kc], x.ranks[kc], x.dims[kc],
 		               b.ranks[kc + 1], x.ranks[kc + 1]);
 	}
@@ -621,13 +677,17 @@ struct AlsState {
 		          b.ranks[cur], b.ranks[cur + 1], S == 2 ? b.ranks[cur + 2] : 1, s.n1, s.n2);
 	}
 	const double* A2(int cur) const { return S == 2 ? A.core[cur + 1] : nullptr; }
-	// |0.5 <v, M v> - <v, b_loc>| with v, b_loc current  (als.cpp:265-278)
+	// energy_f from the stacks with v, b_loc current (als.cpp:255-320, see k_energy)
 	double energy(int cur) {
 		const LocalShape s = shape(cur);
-		local_matvec(c, s, st.Lop[cur], A.core[cur], A2(cur), st.Rop[cur + S], v, q);
-		dot_async(c, v, q, size_t(s.dim()), 4);
+		if (mode == kFree) {
+			dot_async(c, v, v, size_t(s.dim()), 4);
+		} else {
+			local_matvec(c, s, st.Lop[cur], A.core[cur], A2(cur), st.Rop[cur + S], v, q);
+			dot_async(c, v, q, size_t(s.dim()), 4);
+		}
 		dot_async(c, v, bloc, size_t(s.dim()), 5);
-		k_energy<<<1, 1, 0, c.stream>>>(c.d_dbl + 6, c.d_dbl, 4, 5);
+		k_energy<<<1, 1, 0, c.stream>>>(c.d_dbl + 6, c.d_dbl, 4, 5, mode, nb);
 		XTT_CUDA(cudaGetLastError());
 		c.count_launch();
 		XTT_CUDA(cudaMemcpyAsync(c.h_dbl + 6, c.d_dbl + 6, sizeof(double), cudaMemcpyDeviceToHost, c.stream));
@@ -638,15 +698,49 @@ struct AlsState {
 
 }  // namespace
 
-AlsReport als(const Tensor& A, Tensor& x, const Tensor& b, const AlsOptions& o) {
+// The sweep's operator and right-hand side for a non-symmetric A: A^T A and A^T b core by core.
+static void normal_equations(Context& c, const Tensor& A, const Tensor& b, std::unique_ptr<Tensor>& B,
+                             std::unique_ptr<Tensor>& C) {
+	const int d = A.d;
+	std::vector<int64_t> rB(d + 1), rC(d + 1);
+	for (int k = 0; k <= d; ++k) {
+		rB[k] = A.ranks[k] * A.ranks[k];
+		rC[k] = b.ranks[k] * A.ranks[k];
+	}
+	B.reset(new Tensor(&c, true, d, A.dims.data(), rB.data()));
+	C.reset(new Tensor(&c, false, d, A.dims.data(), rC.data()));
+	for (int k = 0; k < d; ++k) {
+		const int K = int(A.ranks[k]), L = int(A.ranks[k + 1]), n = int(A.dims[k]);
+		k_normal_op_core<<<blocks_for((long long)B->core_size(k)), 256, 0, c.stream>>>(B->core[k], A.core[k], K, L, n);
+		k_normal_rhs_core<<<blocks_for((long long)C->core_size(k)), 256, 0, c.stream>>>(
+		    C->core[k], b.core[k], A.core[k], int(b.ranks[k]), int(b.ranks[k + 1]), K, L, n);
+		c.count_launch(2);
+	}
+	XTT_CUDA(cudaGetLastError());
+}
+
+AlsReport als(const Tensor* Ap, Tensor& x, const Tensor& b, const AlsOptions& o) {
 	// ALSVariant::solve, src/xerus/algorithms/als.cpp:483-553
 	Context& c = *x.ctx;
-	XTT_REQUIRE(A.op && !x.op && !b.op, "ALS needs a TT operator, a TT tensor x and a TT tensor b");
-	XTT_REQUIRE(x.d > 0 && x.dims == b.dims && A.dims == x.dims && A.d == x.d, "dimensions of A, x and b must match");
+	XTT_REQUIRE(!x.op && !b.op && (!Ap || Ap->op), "ALS needs a TT operator, a TT tensor x and a TT tensor b");
+	XTT_REQUIRE(x.d > 0 && x.dims == b.dims && (!Ap || (Ap->dims == x.dims && Ap->d == x.d)),
+	            "dimensions of A, x and b must match");
 	XTT_REQUIRE(o.sites == 1 || o.sites == 2, "sites must be 1 or 2");
 	XTT_REQUIRE(!(o.local_solver == 1 && o.sites != 1), "ASD only defined for single site alternation");
+	XTT_REQUIRE(Ap || o.sites == 1, "approximation dmrg not implemented yet");  // als.cpp:539
 	XTT_REQUIRE(o.sites <= x.d, "more sites than components");
 	const int d = x.d, S = o.sites;
+	const int mode = !Ap ? kFree : o.assume_spd ? kSpd : kNormal;
+	// the operator and right-hand side the sweep contracts
+	std::unique_ptr<Tensor> Bn, Cn;
+	if (mode == kNormal) normal_equations(c, *Ap, b, Bn, Cn);
+	if (mode == kFree) {
+		const std::vector<int64_t> ones(d + 1, 1);
+		Bn.reset(new Tensor(&c, true, d, x.dims.data(), ones.data()));
+	}
+	const Tensor& A = mode == kSpd ? *Ap : *Bn;
+	const Tensor& bw = mode == kNormal ? *Cn : b;
+	const double norm_b = mode == kNormal ? frob_norm(b) : 0.0;
 	AlsReport rep;
 	std::vector<int64_t> target(x.ranks.begin() + 1, x.ranks.end() - 1);
 	const bool canon_end = x.canonicalized;
@@ -716,13 +810,13 @@ AlsReport als(const Tensor& A, Tensor& x, const Tensor& b, const AlsOptions& o) 
 		auto red = reduce_to_maximal_ranks(inner, nn);
 		for (int k = 1; k < d; ++k) rmax[k] = std::max(x.ranks[k], red[k - 1]);
 	}
-	AlsState s(c, A, x, b, o);
+	AlsState s(c, A, x, bw, o, mode, norm_b);
 	// stacks: one buffer per family, a slot per bond 0..d
 	{
 		std::vector<size_t> oop(d + 2, 0), orh(d + 2, 0);
 		for (int k = 0; k <= d; ++k) {
-			oop[k + 1] = oop[k] + size_t(rmax[k] * A.ranks[k] * rmax[k]);
-			orh[k + 1] = orh[k] + size_t(b.ranks[k] * rmax[k]);
+			oop[k + 1] = oop[k] + (mode == kFree ? 1 : size_t(rmax[k] * A.ranks[k] * rmax[k]));
+			orh[k + 1] = orh[k] + size_t(bw.ranks[k] * rmax[k]);
 		}
 		double* L = c.scratch<double>(S_ALS_FIRST + 0, oop[d + 1]);
 		double* R = c.scratch<double>(S_ALS_FIRST + 1, oop[d + 1]);
@@ -747,6 +841,7 @@ AlsReport als(const Tensor& A, Tensor& x, const Tensor& b, const AlsOptions& o) 
 		s.bloc = c.scratch<double>(S_ALS_FIRST + 5, maxdim);
 		s.q = c.scratch<double>(S_ALS_FIRST + 6, maxdim);
 		s.grad = c.scratch<double>(S_ALS_FIRST + 7, maxdim);
+		s.q2 = mode == kNormal && o.local_solver == 1 ? c.scratch<double>(S_ALS_FIRST + 8, maxdim) : nullptr;
 	}
 	for (int i = d - 1; i > first + S - 1; --i) s.push_right(i, i);
 	for (int i = 0; i < first; ++i) s.push_left(i);
@@ -754,15 +849,33 @@ AlsReport als(const Tensor& A, Tensor& x, const Tensor& b, const AlsOptions& o) 
 	int cur = first;
 	bool inc = true;
 	const int max_it_opt = int(std::min<int64_t>(o.local_max_iterations, int64_t(1) << 30));
+	// FP64 residual of the caller's problem: ||A x - b|| / ||b||, or ||x - b|| / ||b|| without an operator
+	auto true_residual = [&] { return residual(Ap, x, b); };
+	// what the reference adds to PerformanceData (residual_f, als.cpp:255-320): the relative
+	// residual (here also for a non-symmetric A, which the reference evaluates from its stacks as
+	// sqrt(<Ax,Ax> - 2<b,Ax> + ||b||^2) / ||b||), or ||x - b|| without an operator
+	double nb_free = -1;
+	auto trace_value = [&] {
+		const double r = true_residual();
+		if (mode != kFree) return r;
+		if (nb_free < 0) nb_free = frob_norm(b);
+		return r * nb_free;
+	};
 	auto record = [&](int64_t flag) {
 		if (o.record_residuals) {
-			rep.residuals.push_back(residual(A, x, b));
+			rep.residuals.push_back(trace_value());
 			rep.flags.push_back(flag);
 		}
 	};
-	s.gather_block(cur);
+	// energy_f (als.cpp:255-320): with useResidualForEndCriterion the residual (a non-symmetric
+	// operator always uses its stack residual)
+	auto energy_f = [&](int k) {
+		if (o.use_residual && mode != kNormal) return trace_value();
+		s.gather_block(k);
+		return s.energy(k);
+	};
 	s.rhs(cur);
-	double energy = s.energy(cur), last_e = 1e101, last_e2 = 1e102;
+	double energy = energy_f(cur), last_e = 1e101, last_e2 = 1e102;
 	record(3);
 	int half = 0;
 	// CG counters of this solve, the mixed solves' flag and the sticky FP64 switch
@@ -772,7 +885,23 @@ AlsReport als(const Tensor& A, Tensor& x, const Tensor& b, const AlsOptions& o) 
 		const long long n = sh.dim();
 		s.rhs(cur);
 		s.gather_block(cur);
-		if (o.local_solver == 1) {
+		if (mode == kFree) {
+			// x_k = the projected b (als.cpp:540-543)
+			copy_d2d(c, s.v, s.bloc, size_t(n));
+		} else if (o.local_solver == 1 && mode == kNormal) {
+			// ASD_solver for a non-symmetric A (als.cpp:80-89): g = M^T (b_loc - M v) with M = the
+			// local A^T A (symmetric), v += (||g|| / ||M g||) g
+			local_matvec(c, sh, s.st.Lop[cur], A.core[cur], nullptr, s.st.Rop[cur + 1], s.v, s.q);
+			k_sub<<<blocks_for(n), 256, 0, c.stream>>>(s.grad, s.bloc, s.q, n);
+			c.count_launch();
+			local_matvec(c, sh, s.st.Lop[cur], A.core[cur], nullptr, s.st.Rop[cur + 1], s.grad, s.q);
+			local_matvec(c, sh, s.st.Lop[cur], A.core[cur], nullptr, s.st.Rop[cur + 1], s.q, s.q2);
+			dot_async(c, s.q, s.q, size_t(n), 10);
+			dot_async(c, s.q2, s.q2, size_t(n), 11);
+			k_asd_step_normal<<<blocks_for(n), 256, 0, c.stream>>>(s.v, s.q, n, c.d_dbl, 10, 11);
+			c.count_launch();
+			XTT_CUDA(cudaGetLastError());
+		} else if (o.local_solver == 1) {
 			// ASD_solver (als.cpp:73-92): one exact line-search gradient step
 			local_matvec(c, sh, s.st.Lop[cur], A.core[cur], nullptr, s.st.Rop[cur + 1], s.v, s.q);
 			k_sub<<<blocks_for(n), 256, 0, c.stream>>>(s.grad, s.bloc, s.q, n);
@@ -833,13 +962,12 @@ AlsReport als(const Tensor& A, Tensor& x, const Tensor& b, const AlsOptions& o) 
 			++half;
 			last_e2 = last_e;
 			last_e = energy;
-			s.gather_block(cur);
-			energy = s.energy(cur);
+			energy = energy_f(cur);
 			rep.energies.push_back(energy);
 			record(inc ? 1 : 3);
 			bool target_met = false;
 			if (o.residual_target > 0) {
-				rep.residual = o.record_residuals ? rep.residuals.back() : residual(A, x, b);
+				rep.residual = true_residual();
 				target_met = rep.residual <= o.residual_target;
 			}
 			if (half == o.num_half_sweeps || std::fabs(last_e - energy) < o.convergence_epsilon ||
@@ -865,7 +993,8 @@ AlsReport als(const Tensor& A, Tensor& x, const Tensor& b, const AlsOptions& o) 
 	}
 	rep.energy = energy;
 	rep.half_sweeps = half;
-	if (o.record_residuals && !rep.residuals.empty()) rep.residual = rep.residuals.back();
+	if (o.record_residuals && !rep.residuals.empty())
+		rep.residual = mode == kFree ? rep.residuals.back() / nb_free : rep.residuals.back();
 	XTT_CUDA(cudaMemcpyAsync(c.h_ints + 8, c.d_ints + 8, 2 * sizeof(int), cudaMemcpyDeviceToHost, c.stream));
 	c.sync();
 	rep.local_iterations = c.h_ints[8];
@@ -880,7 +1009,7 @@ double als_energy_gradient(const Tensor& A, const Tensor& x, const Tensor& b, st
 	XTT_REQUIRE(A.op && !x.op && !b.op && x.dims == b.dims && A.dims == x.dims, "dimensions of A, x and b must match");
 	const int d = x.d;
 	AlsOptions o;
-	AlsState s(c, A, const_cast<Tensor&>(x), b, o);
+	AlsState s(c, A, const_cast<Tensor&>(x), b, o, kSpd, 0.0);
 	std::vector<size_t> oop(d + 2, 0), orh(d + 2, 0);
 	for (int k = 0; k <= d; ++k) {
 		oop[k + 1] = oop[k] + size_t(x.ranks[k] * A.ranks[k] * x.ranks[k]);

@@ -267,6 +267,8 @@ struct AlsOptions {
 	int max_rank = 0;
 	double svd_epsilon = 0;
 	bool exact_environment = false;  // 2 sites: push core k+1 (not k) in decreasing sweeps
+	bool assume_spd = true;          // false: least squares through A^T A and A^T b (ALS, DMRG, ASD)
+	bool use_residual = false;       // useResidualForEndCriterion (als.h:116)
 };
 
 struct AlsReport {
@@ -276,7 +278,8 @@ struct AlsReport {
 	std::vector<int64_t> flags;
 };
 
-AlsReport als(const Tensor& A, Tensor& x, const Tensor& b, const AlsOptions& o);
+// A null: the operator-free form, x minimises ||x - b|| (one site only).
+AlsReport als(const Tensor* A, Tensor& x, const Tensor& b, const AlsOptions& o);
 
 // Batched one-site ALS_SPD over independent instances in one persistent launch
 // (batch.cu). x[i] is updated in place; each x[i] must have maximal-reduced ranks.

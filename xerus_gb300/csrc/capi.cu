@@ -540,6 +540,8 @@ int xtt_als_default_options(xtt_als_options* o) {
 		o->max_rank = 0;
 		o->svd_epsilon = 0;
 		o->exact_environment = 0;
+		o->assume_spd = 1;
+		o->use_residual = 0;
 	});
 }
 
@@ -558,6 +560,8 @@ static xtt::AlsOptions to_options(const xtt_als_options* opt) {
 	o.max_rank = opt->max_rank;
 	o.svd_epsilon = opt->svd_epsilon;
 	o.exact_environment = opt->exact_environment != 0;
+	o.assume_spd = opt->assume_spd != 0;
+	o.use_residual = opt->use_residual != 0;
 	return o;
 }
 
@@ -567,6 +571,8 @@ int xtt_als_batch(xtt_context* ctx, int64_t count, const xtt_tensor* const* A, x
 	return guard([&] {
 		ARG(ctx && A && x && b && opt, "NULL argument");
 		ARG(count > 0 && count <= (int64_t(1) << 24), "count must be in 1..2^24");
+		ARG(opt->assume_spd, "the batched sweep runs the SPD variant only");
+		ARG(!opt->use_residual, "the batched sweep uses the energy criterion");
 		ARG(opt->local_tolerance > 0 && opt->local_tolerance < 1, "local_tolerance must be in (0, 1)");
 		ARG(opt->precision == XTT_PRECISION_FP64 || opt->precision == XTT_PRECISION_MIXED, "unknown precision");
 		ARG(opt->record_residuals == 0 && opt->residual_target == 0, "batch: no residual traces or targets");
@@ -596,10 +602,10 @@ int xtt_als(const xtt_tensor* A, xtt_tensor* x, const xtt_tensor* b, const xtt_a
             xtt_als_report* report, double* residual_trace, int64_t* flag_trace, double* energy_trace,
             int64_t trace_capacity) {
 	return guard([&] {
-		ARG(A && x && b && opt, "NULL argument");
+		ARG(x && b && opt, "NULL argument");
 		ARG(opt->local_tolerance > 0 && opt->local_tolerance < 1, "local_tolerance must be in (0, 1)");
 		ARG(opt->precision == XTT_PRECISION_FP64 || opt->precision == XTT_PRECISION_MIXED, "unknown precision");
-		xtt::AlsReport r = xtt::als(*A->t, *x->t, *b->t, to_options(opt));
+		xtt::AlsReport r = xtt::als(A ? A->t : nullptr, *x->t, *b->t, to_options(opt));
 		if (report) {
 			report->energy = r.energy;
 			report->residual = r.residual;
@@ -615,6 +621,38 @@ int xtt_als(const xtt_tensor* A, xtt_tensor* x, const xtt_tensor* b, const xtt_a
 			for (size_t i = 0; i < r.flags.size() && int64_t(i) < trace_capacity; ++i) flag_trace[i] = r.flags[i];
 		if (energy_trace)
 			for (size_t i = 0; i < r.energies.size() && int64_t(i) < trace_capacity; ++i) energy_trace[i] = r.energies[i];
+	});
+}
+
+int xtt_apply(const xtt_tensor* A, const xtt_tensor* x, xtt_tensor** out) {
+	return guard([&] {
+		ARG(A && x && out, "NULL argument");
+		*out = nullptr;
+		const xtt::Tensor& xs = *x->t;
+		ARG(A->t->op, "A must be a TT operator");
+		ARG(A->t->d == xs.d && A->t->dims == xs.dims, "operator and tensor dimensions differ");
+		ARG(A->t->ctx == xs.ctx, "A and x live on different contexts");
+		std::vector<int64_t> r(xs.d + 1);
+		for (int k = 0; k <= xs.d; ++k) r[k] = A->t->ranks[k] * xs.ranks[k];
+		auto* y = new xtt::Tensor(xs.ctx, xs.op, xs.d, xs.dims.data(), r.data());
+		xs.ctx->tensors++;
+		auto* h = new xtt_tensor{y};
+		try {
+			xtt::tt_apply(*A->t, xs, *y);
+		} catch (...) {
+			xtt_tensor_destroy(h);
+			throw;
+		}
+		*out = h;
+	});
+}
+
+int xtt_add(xtt_tensor* x, const xtt_tensor* y, double alpha) {
+	return guard([&] {
+		ARG(x && y, "NULL argument");
+		ARG(x->t->ctx == y->t->ctx, "x and y live on different contexts");
+		ARG(x != y, "x and y must be different tensors (copy y first)");
+		xtt::tt_add(*x->t, *y->t, alpha);
 	});
 }
 

@@ -163,6 +163,8 @@ double dot(const Tensor& x, const Tensor& y);
 double frob_norm(const Tensor& x);
 double orthogonal_norm(Tensor& x);  // destroys x's gauge (QR sweep), returns ||x||
 double residual(const Tensor& A, const Tensor& x, const Tensor& b);
+// ||x - b|| / ||b|| (A null: the identity)
+double residual(const Tensor* A, const Tensor& x, const Tensor& b);
 void entries(const Tensor& x, const int64_t* positions, int64_t count, double* out);
 bool exceeds_maximal_ranks(const Tensor& x);
 std::vector<int64_t> reduce_to_maximal_ranks(std::vector<int64_t> ranks, const std::vector<int64_t>& dims);
@@ -183,6 +185,10 @@ void write_file(const std::string& path, const std::vector<uint8_t>& bytes);
 
 // y <- A x as a TT (cores R_k r_k), allocating y's cores.
 void op_apply_tt(const Tensor& A, const Tensor& x, Tensor& y);
+// y = A x (x a TT tensor or operator); canonicalised at A's core position when A is canonical.
+void tt_apply(const Tensor& A, const Tensor& x, Tensor& y);
+// x += f y; a canonical x is canonicalised again (rank-revealing) at its core position.
+void tt_add(Tensor& x, const Tensor& y, double f);
 
 // ADF for single-point samples (positions: N x d, row-major).
 struct AdfResult {

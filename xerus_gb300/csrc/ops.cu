@@ -765,10 +765,52 @@ void op_apply_tt(const Tensor& A, const Tensor& x, Tensor& y) {
 	y.canonicalized = false;
 }
 
-// Block core of p - q (TT sum of p and -q, src/xerus/ttNetwork.cpp:796-856):
-// out (P0+Q0 or 1, n, P1+Q1 or 1) with p in the leading block, -q (first core) / q in the trailing one.
+// One core of the operator product A B (TTStack<true> contracted, src/xerus/ttStack.cpp:47-173):
+// C((k l), i, j, (k' l')) = sum_m A(k, i, m, k') B(l, m, j, l').
+__global__ void k_op_op(double* C, const double* A, const double* B, int K, int L, int Kb, int Lb, int n) {
+	const size_t total = size_t(K) * Kb * n * n * L * Lb;
+	for (size_t e = blockIdx.x * size_t(blockDim.x) + threadIdx.x; e < total; e += size_t(gridDim.x) * blockDim.x) {
+		size_t t = e;
+		const int l2 = int(t % Lb); t /= Lb;
+		const int k2 = int(t % L); t /= L;
+		const int j = int(t % n); t /= n;
+		const int i = int(t % n); t /= n;
+		const int l = int(t % Kb);
+		const int k = int(t / Kb);
+		double s = 0;
+		for (int m = 0; m < n; ++m)
+			s = fma(A[((size_t(k) * n + i) * n + m) * L + k2], B[((size_t(l) * n + m) * n + j) * Lb + l2], s);
+		C[e] = s;
+	}
+}
+
+void tt_apply(const Tensor& A, const Tensor& x, Tensor& y) {
+	// A(i/2, j/2) * x(j&0) cast to a TT (TTStack, src/xerus/ttStack.cpp:47-173; specialised
+	// contraction, src/xerus/ttNetwork.cpp:886-967): core ranks R_k r_k, and the result is
+	// canonicalised (rank-revealing move_core) at A's core position when A is canonical.
+	XTT_REQUIRE(A.op && A.d == x.d && A.dims == x.dims && y.d == x.d && y.op == x.op && y.dims == x.dims,
+	            "operator and tensor dimensions differ");
+	Context& c = *x.ctx;
+	if (!x.op) {
+		op_apply_tt(A, x, y);
+	} else {
+		for (int k = 0; k < x.d; ++k) {
+			const int K = int(A.ranks[k]), L = int(A.ranks[k + 1]), Kb = int(x.ranks[k]), Lb = int(x.ranks[k + 1]);
+			const int n = int(x.dims[k]);
+			y.reshape_core(k, int64_t(K) * Kb, int64_t(L) * Lb);
+			k_op_op<<<grid_for(y.core_size(k)), 256, 0, c.stream>>>(y.core[k], A.core[k], x.core[k], K, L, Kb, Lb, n);
+			c.count_launch();
+		}
+		XTT_CUDA(cudaGetLastError());
+	}
+	y.canonicalized = false;
+	if (A.canonicalized) move_core(y, A.core_position, false);
+}
+
+// Block core of p + f q (TT sum, src/xerus/ttNetwork.cpp:796-847): out (P0+Q0 or 1, n, P1+Q1 or 1)
+// with p in the leading block and q in the trailing one, q scaled by f in the first core.
 __global__ void k_block_core(double* out, const double* p, const double* q, int P0, int P1, int Q0, int Q1, int n,
-                             int first, int last) {
+                             int first, int last, double f) {
 	const int O0 = first ? 1 : P0 + Q0, O1 = last ? 1 : P1 + Q1;
 	const size_t total = size_t(O0) * n * O1;
 	for (size_t e = blockIdx.x * size_t(blockDim.x) + threadIdx.x; e < total; e += size_t(gridDim.x) * blockDim.x) {
@@ -779,25 +821,57 @@ __global__ void k_block_core(double* out, const double* p, const double* q, int 
 		// p block at (0.., 0..)
 		if (o0 < P0 && o1 < P1) v += p[(size_t(o0) * n + i) * P1 + o1];
 		const int q0 = first ? o0 : o0 - P0, q1 = last ? o1 : o1 - P1;
-		if (q0 >= 0 && q0 < Q0 && q1 >= 0 && q1 < Q1) v += (first ? -1.0 : 1.0) * q[(size_t(q0) * n + i) * Q1 + q1];
+		if (q0 >= 0 && q0 < Q0 && q1 >= 0 && q1 < Q1) v += (first ? f : 1.0) * q[(size_t(q0) * n + i) * Q1 + q1];
 		out[e] = v;
 	}
 }
 
-double residual(const Tensor& A, const Tensor& x, const Tensor& b) {
-	// ||A x - b|| / ||b|| (src/xerus/algorithms/als.cpp:258-261) without cancellation. The block
+void tt_add(Tensor& x, const Tensor& y, double f) {
+	// x += f y (TTNetwork::operator+= / -=, src/xerus/ttNetwork.cpp:796-856): block cores of
+	// ranks r + s; a canonical x is canonicalised again at its core position (rank-revealing
+	// move_core), which can lower the ranks.
+	XTT_REQUIRE(x.op == y.op && x.d == y.d && x.dims == y.dims, "The dimensions in TT sum must coincide");
+	Context& c = *x.ctx;
+	const int d = x.d;
+	const bool canon = x.canonicalized;
+	const int64_t pos = x.core_position;
+	for (int k = 0; k < d; ++k) {
+		const int n = int(x.n(k));
+		const int P0 = int(x.ranks[k]), P1 = int(x.ranks[k + 1]), Q0 = int(y.ranks[k]), Q1 = int(y.ranks[k + 1]);
+		const int first = k == 0, last = k == d - 1;
+		const int O0 = first ? 1 : P0 + Q0, O1 = last ? 1 : P1 + Q1;
+		const size_t ny = size_t(O0) * n * O1;
+		double* T = c.scratch<double>(S_GEMM_A, ny);
+		k_block_core<<<grid_for(ny), 256, 0, c.stream>>>(T, x.core[k], y.core[k], P0, P1, Q0, Q1, n, first, last, f);
+		c.count_launch();
+		XTT_CUDA(cudaGetLastError());
+		x.reshape_core(k, O0, O1);
+		copy_d2d(c, x.core[k], T, ny);
+	}
+	x.canonicalized = false;
+	if (canon && d > 1) move_core(x, pos, false);
+	else if (canon) x.canonicalized = true;  // one component: component(0) += (ttNetwork.cpp:809-812)
+}
+
+double residual(const Tensor& A, const Tensor& x, const Tensor& b) { return residual(&A, x, b); }
+
+double residual(const Tensor* Ap, const Tensor& x, const Tensor& b) {
+	// ||A x - b|| / ||b|| (src/xerus/algorithms/als.cpp:258-261; A null: ||x - b|| / ||b||,
+	// als.cpp:301) without cancellation. The block
 	// cores Y_k of y = A x - b (TT sum, src/xerus/ttNetwork.cpp:796-856) are formed one at a time
 	// and orthogonalised from both ends at once: cores 0..mid-1 left to right on the context's
 	// stream (Householder QR, only the triangular factor R is carried), cores d-1..mid+1 right to
 	// left on the aux stream (LQ, only the factor L is carried). The two halves meet at core mid:
 	// ||y|| = ||R Y_mid L||. Neither the residual TT nor any orthogonal factor is stored.
-	XTT_REQUIRE(x.dims == b.dims && A.dims == x.dims && A.op && !x.op && !b.op, "x and b dimensions differ");
+	XTT_REQUIRE(x.dims == b.dims && !x.op && !b.op && (!Ap || (Ap->dims == x.dims && Ap->op)),
+	            "x and b dimensions differ");
 	Context& c = *x.ctx;
 	const int d = x.d;
 	const double nb = frob_norm(b);
+	auto opr = [&](int k) -> int64_t { return Ap ? Ap->ranks[k] : 1; };
 	size_t cap_core = 1, cap_r = 1;
 	for (int k = 0; k < d; ++k) {
-		const size_t p0 = size_t(A.ranks[k] * x.ranks[k] + b.ranks[k]), p1 = size_t(A.ranks[k + 1] * x.ranks[k + 1] + b.ranks[k + 1]);
+		const size_t p0 = size_t(opr(k) * x.ranks[k] + b.ranks[k]), p1 = size_t(opr(k + 1) * x.ranks[k + 1] + b.ranks[k + 1]);
 		cap_core = std::max(cap_core, p0 * size_t(x.dims[k]) * p1);
 		cap_r = std::max({cap_r, p0 * p1, p0 * p0, p1 * p1});
 	}
@@ -818,15 +892,20 @@ double residual(const Tensor& A, const Tensor& x, const Tensor& b) {
 	};
 	// block core k of A x - b into f.Y on the current stream
 	auto block = [&](int k, const Bufs& f) {
-		const int K = int(A.ranks[k]), L = int(A.ranks[k + 1]), ra = int(x.ranks[k]), rb = int(x.ranks[k + 1]);
+		const int K = int(opr(k)), L = int(opr(k + 1)), ra = int(x.ranks[k]), rb = int(x.ranks[k + 1]);
 		const int n = int(x.dims[k]);
 		const int P0 = K * ra, P1 = L * rb, Q0 = int(b.ranks[k]), Q1 = int(b.ranks[k + 1]);
 		const int first = k == 0, last = k == d - 1;
 		const int O0 = first ? 1 : P0 + Q0, O1 = last ? 1 : P1 + Q1;
 		const size_t nax = size_t(P0) * n * P1, ny = size_t(O0) * n * O1;
-		k_op_apply<<<grid_for(nax), 256, 0, c.stream>>>(f.ax, A.core[k], x.core[k], K, L, n, ra, rb);
-		k_block_core<<<grid_for(ny), 256, 0, c.stream>>>(f.Y, f.ax, b.core[k], P0, P1, Q0, Q1, n, first, last);
-		c.count_launch(2);
+		if (Ap) {
+			k_op_apply<<<grid_for(nax), 256, 0, c.stream>>>(f.ax, Ap->core[k], x.core[k], K, L, n, ra, rb);
+			c.count_launch();
+		} else {
+			copy_d2d(c, f.ax, x.core[k], nax);
+		}
+		k_block_core<<<grid_for(ny), 256, 0, c.stream>>>(f.Y, f.ax, b.core[k], P0, P1, Q0, Q1, n, first, last, -1.0);
+		c.count_launch();
 		XTT_CUDA(cudaGetLastError());
 		return Dims{n, O0, O1};
 	};
