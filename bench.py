@@ -205,6 +205,12 @@ def bench_adf(xg, ctx, torch, stream, iters, peak, cpu):
         out[name] = {"ms_per_iteration": ms, "samples_per_s": N / (ms / 1e3), "final_residual_fp64_checked": res,
                      "roofline": {"bound": "hbm", "achieved": alg / (ms / 1e3) / 1e9, "peak": peak, "unit": "GB/s",
                                   "frac": alg / (ms / 1e3) / 1e9 / peak, "algorithmic_bytes_per_iteration": alg}}
+        # where an iteration's time goes: a separate run with per-class CUDA-event timing
+        ctx.profile(True)
+        xg.ADFVariant(iters, 0.0, 1.0, precision=prec)(x0.copy(), m)
+        ctx.profile(False)
+        out[name]["kernel_ms_per_iteration"] = {k: ctx.profile_get(k)[1] / iters for k in
+                                                ("adf_res_grad", "adf_slicenorm", "adf_stack", "qr", "gemm")}
     out["fp32_speedup_vs_fp64"] = out["fp64"]["ms_per_iteration"] / out["fp32"]["ms_per_iteration"]
     if cpu:
         from oracle import xtt_oracle as o

@@ -538,6 +538,52 @@ static void case_als_nonspd() {
 	run_approx("free_useres", approx_res, y, c, 10, pos);
 }
 
+static void save_full(const std::string& name, const TTTensor& x) {
+	Tensor full(x);
+	std::vector<double> f(full.size);
+	for (size_t i = 0; i < full.size; ++i) f[i] = full[i];
+	save(name + "_full", f);
+	save(name + "_ranks", ranks_of(x));
+	save<int64_t>(name + "_canon", {int64_t(x.canonicalized), int64_t(x.corePosition)});
+}
+
+static void case_arith() {
+	// TT sums (operator+=, operator-=) and operator products (TTStack casts), d=5, n=4.
+	reseed();
+	const size_t d = 5, n = 4;
+	const std::vector<size_t> dims(d, n);
+	TTTensor x = TTTensor::random(dims, 3);
+	TTTensor y = TTTensor::random(dims, 2);
+	TTOperator Ar = TTOperator::random(std::vector<size_t>(2 * d, n), 2);
+	TTOperator A = laplace_operator(d, n, nullptr, false, 0.0, 0.6);
+	save_tt("x", x);
+	save_tt("y", y);
+	save_op("Ar", Ar);
+	save_op("A", A);
+	save<int64_t>("Ar_canon", {int64_t(Ar.canonicalized), int64_t(Ar.corePosition)});
+	save<int64_t>("A_canon", {int64_t(A.canonicalized), int64_t(A.corePosition)});
+	save_full("sum", x + y);
+	save_full("diff", x - y);
+	save_full("twice", x + x);
+	Index i, j, k;
+	TTTensor p;
+	p(i & 0) = A(i / 2, j / 2) * x(j & 0);
+	save_full("Ax", p);
+	TTTensor q;
+	q(i & 0) = Ar(i / 2, j / 2) * x(j & 0);
+	save_full("Arx", q);
+	save_full("Ax_plus_x", p + x);
+	TTOperator AA;
+	AA(i / 2, k / 2) = A(i / 2, j / 2) * Ar(j / 2, k / 2);
+	std::vector<int64_t> ar;
+	for (size_t r : AA.ranks()) ar.push_back(int64_t(r));
+	save("AAr_ranks", ar);
+	save<int64_t>("AAr_canon", {int64_t(AA.canonicalized), int64_t(AA.corePosition)});
+	TTTensor w;
+	w(i & 0) = AA(i / 2, j / 2) * x(j & 0);
+	save_full("AAr_x", w);
+}
+
 static void case_dmrg() {
 	reseed();
 	const size_t d = 8, n = 4;
@@ -719,6 +765,7 @@ int main(int argc, char** argv) {
 	else if (c == "adf_cfg5") case_adf_cfg5();
 	else if (c == "fileio") case_fileio();
 	else if (c == "als_nonspd") case_als_nonspd();
+	else if (c == "arith") case_arith();
 	else {
 		std::fprintf(stderr, "unknown case %s\n", c.c_str());
 		return 2;

@@ -895,6 +895,205 @@ __global__ void __launch_bounds__(kQ2Threads) k_qr_cl2(QrArgs a, Qc2Layout lay) 
 	cl.sync();
 }
 
+// Unpivoted Householder QR / LQ across a cluster with ONE cluster barrier per
+// column. Rows are split over the CTAs as in k_qr_cl2. Each step needs, summed
+// over the cluster, the column's squared norm below the diagonal (sigma), its
+// diagonal entry (alpha), and for every trailing column c the dot product with
+// the column below the diagonal (D_c) and c's diagonal-row entry (E_c). With
+// v = [1; x * scal], the reflector's product with column c is
+// v^T a_c = E_c + scal D_c, so all of them come from one exchange instead of a
+// norm exchange followed by a dot-product exchange. Each CTA writes its
+// partials for step j+1 into its own shared memory (two parities) while
+// finishing step j; after the barrier every CTA reads the P partials of the
+// fields it needs from the other CTAs and sums them in rank order, so all CTAs
+// form bit-identical reflectors. Q (if wanted) is accumulated backwards
+// (dorg2r order) with the same exchange, one barrier per reflector.
+constexpr int kQ1Threads = 256;
+
+struct Qc1Layout {
+	int P, mb, nw, kq, ldw, S;  // S: fields per parity (sigma, alpha, D_c, E_c)
+	__host__ __device__ size_t red() const { return size_t(mb) * ldw; }
+	__host__ __device__ size_t tot() const { return red() + 2 * size_t(S); }
+	__host__ __device__ size_t tau() const { return tot() + size_t(S); }
+	__host__ __device__ size_t part() const { return tau() + kq; }
+	__host__ __device__ size_t total() const { return part() + 8 * 256; }
+};
+
+__global__ void __launch_bounds__(kQ1Threads) k_qr_cl1(QrArgs a, Qc1Layout lay) {
+	namespace cg = cooperative_groups;
+	cg::cluster_group cl = cg::this_cluster();
+	const int P = lay.P, me = int(cl.block_rank());
+	const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+	const int mw = a.transpose ? a.n : a.m, nw = lay.nw, kq = lay.kq, mb = lay.mb, ldw = lay.ldw, S = lay.S;
+	const int r0 = me * mb, r1 = min(mw, r0 + mb), nl = max(0, r1 - r0);
+	extern __shared__ double sm[];
+	double* W = sm;
+	double* red = sm + lay.red();
+	double* tot = sm + lay.tot();
+	double* tau = sm + lay.tau();
+	double* part = sm + lay.part();
+	auto w = [&](int il, int c) -> double& { return W[(long long)il * ldw + c]; };
+	auto lo_of = [&](int g) { return min(max(g - r0, 0), nl); };
+
+	for (long long e = tid; e < (long long)nl * nw; e += kQ1Threads) {
+		const int il = int(e / nw), c = int(e % nw), gi = r0 + il;
+		w(il, c) = a.transpose ? a.A[(long long)c * a.lda + gi] : a.A[(long long)gi * a.lda + c];
+	}
+	__syncthreads();
+
+	// this CTA's partials of step jn (rows > jn) into its own slot of parity jn & 1:
+	// field 0 sigma, 1 alpha, 2 + c D_c, 2 + nw + c E_c
+	auto publish = [&](int jn) {
+		double* slot = red + (jn & 1) * size_t(S);
+		const int lo = lo_of(jn + 1), nrows = nl - lo, C = nw - jn;  // columns jn (sigma) .. nw-1
+		const bool owner = jn >= r0 && jn < r1;
+		for (int cb = 0; cb < C; cb += 256) {
+			const ColMap cm(C, cb);
+			const int g = warp / cm.ncw, ci = (warp % cm.ncw) * 32 + lane, chunk = (nrows + cm.G - 1) / cm.G;
+			if (g < cm.G && ci < cm.Cc) {
+				const int c = jn + cb + ci, ia = lo + g * chunk, ib = min(nl, ia + chunk);
+				part[g * 256 + ci] = chain4(ia, ib, [&](int il) { return w(il, jn) * w(il, c); });
+			}
+			__syncthreads();
+			if (tid < cm.Cc) {
+				const int c = jn + cb + tid;
+				double sd = 0;
+				for (int gg = 0; gg < cm.G; ++gg) sd += part[gg * 256 + tid];
+				slot[c == jn ? 0 : 2 + c] = sd;
+				slot[c == jn ? 1 : 2 + nw + c] = owner ? w(jn - r0, c) : 0.0;
+			}
+			__syncthreads();
+		}
+	};
+	// cluster totals into tot[], rank order: fields 0, 1 (if head), then [2 + c0, 2 + c0 + C)
+	// and, if head, [2 + nw + c0, 2 + nw + c0 + C)
+	auto gather = [&](int par, bool head, int c0, int C) {
+		const int nv = head ? 2 + 2 * C : C;
+		for (int v = tid; v < nv; v += kQ1Threads) {
+			const int f = !head ? 2 + c0 + v : v < 2 ? v : v < 2 + C ? 2 + c0 + (v - 2) : 2 + nw + c0 + (v - 2 - C);
+			double a0 = 0, a1 = 0, a2 = 0, a3 = 0;
+			int q = 0;
+			for (; q + 3 < P; q += 4) {
+				a0 += cl.map_shared_rank(red, q + 0)[par * S + f];
+				a1 += cl.map_shared_rank(red, q + 1)[par * S + f];
+				a2 += cl.map_shared_rank(red, q + 2)[par * S + f];
+				a3 += cl.map_shared_rank(red, q + 3)[par * S + f];
+			}
+			for (; q < P; ++q) a0 += cl.map_shared_rank(red, q)[par * S + f];
+			tot[f] = (a0 + a1) + (a2 + a3);
+		}
+	};
+
+	publish(0);
+	for (int j = 0; j < kq; ++j) {
+		const int par = j & 1;
+		cl.sync();
+		// totals: sigma, alpha (fields 0, 1), D_c and E_c of the trailing columns
+		const int c0 = j + 1, C = nw - c0;
+		gather(par, true, c0, C);
+		__syncthreads();
+		double beta, tt, scal;
+		reflector_scalars(tot[1], tot[0], beta, tt, scal);
+		if (tid == 0) tau[j] = tt;
+		// trailing columns, rows >= j: a_c -= tau (E_c + scal D_c) v, v = [1; x scal]
+		const int lo = lo_of(j), nrows = nl - lo;
+		for (int cb = 0; cb < C; cb += 256) {
+			const ColMap cm(C, cb);
+			const int g = warp / cm.ncw, ci = (warp % cm.ncw) * 32 + lane, chunk = (nrows + cm.G - 1) / cm.G;
+			if (g < cm.G && ci < cm.Cc) {
+				const int c = c0 + cb + ci, ia = lo + g * chunk, ib = min(nl, ia + chunk);
+				const double wc = tt * fma(scal, tot[2 + c], tot[2 + nw + c]);
+				for (int il = ia; il < ib; ++il) {
+					const double v = (r0 + il == j) ? 1.0 : w(il, j) * scal;
+					w(il, c) = fma(-wc, v, w(il, c));
+				}
+			}
+		}
+		__syncthreads();
+		// the reflector below the diagonal, R_jj; then the next step's partials (columns > j)
+		for (int il = lo_of(j + 1) + tid; il < nl; il += kQ1Threads) w(il, j) *= scal;
+		if (tid == 0 && j >= r0 && j < r1) w(j - r0, j) = beta;
+		if (j + 1 < kq) publish(j + 1);
+	}
+	const int rank = kq;
+	if (me == 0 && tid == 0 && a.rank_out) *a.rank_out = rank;
+	__syncthreads();
+	for (long long e = tid; e < (long long)nl * nw; e += kQ1Threads) {
+		const int il = int(e / nw), c = int(e % nw), r = r0 + il;
+		if (r >= rank) continue;
+		const double v = (r <= c) ? w(il, c) : 0.0;
+		if (!a.transpose) a.C[(long long)r * nw + c] = v;
+		else a.C[(long long)c * rank + r] = v;
+	}
+	cl.sync();  // every CTA has read the last partials before they are rewritten or freed
+	if (!a.want_q) return;
+	// Q in place, backward accumulation of the reflectors (dorg2r)
+	for (int j = rank - 1; j >= 0; --j) {
+		const double tj = tau[j];
+		const int c0 = j + 1, C = rank - c0, lo = lo_of(j + 1), nrows = nl - lo, par = j & 1;
+		if (C > 0) {
+			double* slot = red + par * size_t(S);
+			for (int cb = 0; cb < C; cb += 256) {
+				const ColMap cm(C, cb);
+				const int g = warp / cm.ncw, ci = (warp % cm.ncw) * 32 + lane, chunk = (nrows + cm.G - 1) / cm.G;
+				if (g < cm.G && ci < cm.Cc) {
+					const int c = c0 + cb + ci, ia = lo + g * chunk, ib = min(nl, ia + chunk);
+					part[g * 256 + ci] = chain4(ia, ib, [&](int il) { return w(il, j) * w(il, c); });
+				}
+				__syncthreads();
+				if (tid < cm.Cc) {
+					double sd = 0;
+					for (int gg = 0; gg < cm.G; ++gg) sd += part[gg * 256 + tid];
+					slot[2 + c0 + cb + tid] = sd;
+				}
+				__syncthreads();
+			}
+			cl.sync();
+			gather(par, false, c0, C);
+			__syncthreads();
+			for (int cb = 0; cb < C; cb += 256) {
+				const ColMap cm(C, cb);
+				const int g = warp / cm.ncw, ci = (warp % cm.ncw) * 32 + lane, chunk = (nrows + cm.G - 1) / cm.G;
+				if (g < cm.G && ci < cm.Cc) {
+					const int c = c0 + cb + ci, ia = lo + g * chunk, ib = min(nl, ia + chunk);
+					const double wc = tj * tot[2 + c];
+					for (int il = ia; il < ib; ++il) w(il, c) = fma(-wc, w(il, j), w(il, c));
+					if (g == 0 && j >= r0 && j < r1) w(j - r0, c) = -wc;
+				}
+			}
+			__syncthreads();
+		}
+		for (int il = tid; il < nl; il += kQ1Threads) {
+			const int gi = r0 + il;
+			if (gi > j) w(il, j) *= -tj;
+			else if (gi == j) w(il, j) = 1.0 - tj;
+			else w(il, j) = 0.0;
+		}
+		__syncthreads();
+	}
+	for (long long e = tid; e < (long long)nl * rank; e += kQ1Threads) {
+		const int il = int(e / rank), c = int(e % rank), gi = r0 + il;
+		const double v = w(il, c);
+		if (!a.transpose) a.Q[(long long)gi * rank + c] = v;
+		else a.Q[(long long)c * mw + gi] = v;
+	}
+	cl.sync();  // every CTA's partials stay alive until the last remote reads are done
+}
+
+static int qr_cl1_size(int mw, int nw, Qc1Layout& lay) {
+	if (mw < 48 || nw < 8) return 0;
+	int P = std::min(16, (mw + 15) / 16);
+	lay.mb = (mw + P - 1) / P;
+	P = (mw + lay.mb - 1) / lay.mb;
+	lay.P = P;
+	lay.nw = nw;
+	lay.kq = std::min(mw, nw);
+	lay.ldw = nw | 1;
+	lay.S = 2 + 2 * nw;
+	if (lay.total() * sizeof(double) > kDynSmemMax) return 0;
+	return P;
+}
+
 static int qr_cl2_size(int mw, int nw, Qc2Layout& lay) {
 	if (mw < 48 || nw < 8) return 0;
 	int P = std::min(16, (mw + 15) / 16);
@@ -946,6 +1145,36 @@ void launch_qr(const QrArgs& a, cudaStream_t s) {
 			k_qr_small<<<1, kQrSmallThreads, bytes, s>>>(a);
 			XTT_CUDA(cudaGetLastError());
 			return;
+		}
+	}
+	if (!a.pivot) {
+		Qc1Layout l1;
+		const int P1 = qr_cl1_size(mw, nw, l1);
+		if (P1 > 1) {
+			static bool attr1 = false;
+			if (!attr1) {
+				XTT_CUDA(cudaFuncSetAttribute(k_qr_cl1, cudaFuncAttributeMaxDynamicSharedMemorySize, int(kDynSmemMax)));
+				XTT_CUDA(cudaFuncSetAttribute(k_qr_cl1, cudaFuncAttributeNonPortableClusterSizeAllowed, 1));
+				attr1 = true;
+			}
+			cudaLaunchConfig_t cfg = {};
+			cfg.gridDim = dim3(P1);
+			cfg.blockDim = dim3(kQ1Threads);
+			cfg.dynamicSmemBytes = l1.total() * sizeof(double);
+			cfg.stream = s;
+			cudaLaunchAttribute at[1];
+			at[0].id = cudaLaunchAttributeClusterDimension;
+			at[0].val.clusterDim.x = P1;
+			at[0].val.clusterDim.y = 1;
+			at[0].val.clusterDim.z = 1;
+			cfg.attrs = at;
+			cfg.numAttrs = 1;
+			int clusters = 0;
+			if (cudaOccupancyMaxActiveClusters(&clusters, k_qr_cl1, &cfg) == cudaSuccess && clusters > 0) {
+				XTT_CUDA(cudaLaunchKernelEx(&cfg, k_qr_cl1, a, l1));
+				return;
+			}
+			cudaGetLastError();
 		}
 	}
 	{

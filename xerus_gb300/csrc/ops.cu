@@ -835,9 +835,10 @@ void tt_add(Tensor& x, const Tensor& y, double f) {
 	const int d = x.d;
 	const bool canon = x.canonicalized;
 	const int64_t pos = x.core_position;
+	const std::vector<int64_t> xr = x.ranks;  // reshape_core below rewrites x.ranks as it goes
 	for (int k = 0; k < d; ++k) {
 		const int n = int(x.n(k));
-		const int P0 = int(x.ranks[k]), P1 = int(x.ranks[k + 1]), Q0 = int(y.ranks[k]), Q1 = int(y.ranks[k + 1]);
+		const int P0 = int(xr[k]), P1 = int(xr[k + 1]), Q0 = int(y.ranks[k]), Q1 = int(y.ranks[k + 1]);
 		const int first = k == 0, last = k == d - 1;
 		const int O0 = first ? 1 : P0 + Q0, O1 = last ? 1 : P1 + Q1;
 		const size_t ny = size_t(O0) * n * O1;
