@@ -15,9 +15,10 @@
 //   G[:,i,:] = sum_{s: i_s = i} res_s F_{k-1}[s] (x) B_{k+1}[s]       (calculate_projected_gradient)
 //   nrm_i   = sum_{s: i_s = i} (F_{k-1}[s]^T G[:, i_s, :] B_{k+1}[s])^2 (calculate_slicewise_norm_A_projGrad)
 //   X_k[:, i, :] += (||G_i||^2 / nrm_i) G_i                           (update_x)
-// The gradient and slice norms are reduced deterministically: each warp
-// accumulates its contiguous chunk of samples in registers in a fixed order,
-// and the per-warp partials are summed in a fixed order by a second kernel.
+// The gradient and slice norms are reduced deterministically: each warp (each
+// thread, for the slice norms) accumulates its contiguous chunk of samples in a
+// fixed order, each block sums its warps (threads) in a fixed order, and the
+// per-block partials are summed in a fixed order by a second kernel.
 #include <algorithm>
 #include <cfloat>
 #include <cmath>
@@ -26,8 +27,6 @@
 
 namespace xtt {
 
-constexpr int kAdfThreads = 64;  // two warps: the per-warp accumulators stay under 48 KB of static smem
-constexpr int kAdfWarpsPerBlock = kAdfThreads / 32;
 constexpr int kAdfMaxR = 8;        // fast path: ranks <= 8
 constexpr int kAdfMaxSlices = 16;  // fast path: mode sizes <= 16
 constexpr int kAdfPairsPerLane = 2;  // r0 * r1 <= 64
@@ -45,27 +44,43 @@ struct AdfLevelT {
 };
 using AdfLevel = AdfLevelT<double>;
 
-// res_s (optional write), and per-warp partials of G (r0, n, r1) and of sum res^2.
+// res_s (optional write), and per-block partials of G (r0, n, r1) and of sum res^2.
 // mode 0: res_s = y_s - <F, X_i B>; mode 1: res_s given in `res` (read only).
 // Each warp walks its chunk of samples 32 at a time: lane s stages its sample's
-// F, B, index and residual in the warp's shared memory, then every lane (one or
-// two (a, c) pairs) adds res_j F_j[a] B_j[c] into slice i_j of the warp's
-// gradient accumulator, sample by sample in order (deterministic). One FP64
-// multiply-add per pair and sample: GB300's FP64 pipe is the bound.
+// index, res_s F[s] (premultiplied) and B[s] in the warp's shared memory (one
+// row per rank index, lanes contiguous: conflict-free), then the lanes own the
+// (a, c) pairs and add res_j F_j[a] B_j[c] into slice i_j of the warp's gradient
+// accumulator, sample by sample in order: one multiply-add per pair and sample.
+// The block's warps are summed in a fixed order at the end (deterministic).
+constexpr int kAdfResThreads = 128;
+constexpr int kAdfResWarps = kAdfResThreads / 32;
+
 template <class S>
-__global__ void __launch_bounds__(kAdfThreads) k_adf_res_grad(AdfLevelT<S> L, const S* y, S* res, int mode,
-                                                               double* gpart, double* rrpart, long long chunk) {
-	__shared__ S Xs[kAdfMaxR * kAdfMaxSlices * kAdfMaxR];
-	__shared__ S Gw[kAdfWarpsPerBlock][kAdfMaxSlices * kAdfMaxR * kAdfMaxR];
-	__shared__ S Fw[kAdfWarpsPerBlock][32 * kAdfMaxR];
-	__shared__ S Bw[kAdfWarpsPerBlock][32 * kAdfMaxR];
-	__shared__ S Rw[kAdfWarpsPerBlock][32];
-	__shared__ int Iw[kAdfWarpsPerBlock][32];
+struct AdfResSmem {
+	// offsets (elements of S) into the dynamic shared memory
+	int P, n, r0, r1;
+	__host__ __device__ int xs() const { return 0; }
+	__host__ __device__ int g(int w) const { return r0 * n * r1 + w * n * P; }
+	__host__ __device__ int rf(int w) const { return g(kAdfResWarps) + w * (r0 + r1) * 33; }
+	__host__ __device__ int bb(int w) const { return rf(w) + r0 * 33; }
+	__host__ __device__ int total() const { return rf(kAdfResWarps); }
+};
+
+template <class S>
+__global__ void __launch_bounds__(kAdfResThreads) k_adf_res_grad(AdfLevelT<S> L, const S* y, S* res, int mode,
+                                                                  double* gpart, double* rrpart, long long chunk) {
+	extern __shared__ __align__(16) unsigned char adf_raw[];
+	S* sm = reinterpret_cast<S*>(adf_raw);
+	__shared__ int Iw[kAdfResWarps][32];
+	__shared__ double rrw[kAdfResWarps];
 	const int lane = threadIdx.x & 31, wib = threadIdx.x >> 5;
-	const long long warp = (long long)blockIdx.x * kAdfWarpsPerBlock + wib;
 	const int r0 = L.r0, n = L.n, r1 = L.r1, P = r0 * r1;
+	AdfResSmem<S> lay{P, n, r0, r1};
+	S* Xs = sm + lay.xs();
+	S* G = sm + lay.g(wib);
+	S* RF = sm + lay.rf(wib);
+	S* BB = sm + lay.bb(wib);
 	for (int e = threadIdx.x; e < r0 * n * r1; e += blockDim.x) Xs[e] = S(L.X[e]);
-	S* G = Gw[wib];
 	for (int e = lane; e < n * P; e += 32) G[e] = S(0);
 	__syncthreads();
 	int pa[kAdfPairsPerLane], pc[kAdfPairsPerLane];
@@ -76,23 +91,28 @@ __global__ void __launch_bounds__(kAdfThreads) k_adf_res_grad(AdfLevelT<S> L, co
 		pc[t] = p < P ? p - pa[t] * r1 : 0;
 	}
 	double rr = 0.0;
-	const long long s0 = warp * chunk, s1 = min(L.N, s0 + chunk);
+	const long long s0 = ((long long)blockIdx.x * kAdfResWarps + wib) * chunk, s1 = min(L.N, s0 + chunk);
 	for (long long base = s0; base < s1; base += 32) {
 		const long long s = base + lane;
 		if (s < s1) {
 			const int idx = L.pos[s];
-			S* f = Fw[wib] + lane * kAdfMaxR;
-			S* b = Bw[wib] + lane * kAdfMaxR;
-			for (int a = 0; a < r0; ++a) f[a] = L.F ? L.F[a * L.N + s] : S(1);
-			for (int c = 0; c < r1; ++c) b[c] = L.B ? L.B[c * L.N + s] : S(1);
+			S f[kAdfMaxR], b[kAdfMaxR];
+#pragma unroll
+			for (int a = 0; a < kAdfMaxR; ++a) f[a] = a < r0 ? (L.F ? L.F[a * L.N + s] : S(1)) : S(0);
+#pragma unroll
+			for (int c = 0; c < kAdfMaxR; ++c) b[c] = c < r1 ? (L.B ? L.B[c * L.N + s] : S(1)) : S(0);
 			S rs;
 			if (mode == 0) {
 				S v = S(0);
-				for (int a = 0; a < r0; ++a) {
+#pragma unroll
+				for (int a = 0; a < kAdfMaxR; ++a) {
+					if (a >= r0) break;
 					S t = S(0);
 					const S* xr = Xs + (a * n + idx) * r1;
-					for (int c = 0; c < r1; ++c) t += xr[c] * b[c];
-					v += f[a] * t;
+#pragma unroll
+					for (int c = 0; c < kAdfMaxR; ++c)
+						if (c < r1) t = fma(xr[c], b[c], t);
+					v = fma(f[a], t, v);
 				}
 				rs = y[s] - v;
 				res[s] = rs;
@@ -100,33 +120,42 @@ __global__ void __launch_bounds__(kAdfThreads) k_adf_res_grad(AdfLevelT<S> L, co
 				rs = res[s];
 			}
 			rr += double(rs) * double(rs);
-			Rw[wib][lane] = rs;
+#pragma unroll
+			for (int a = 0; a < kAdfMaxR; ++a)
+				if (a < r0) RF[a * 33 + lane] = rs * f[a];
+#pragma unroll
+			for (int c = 0; c < kAdfMaxR; ++c)
+				if (c < r1) BB[c * 33 + lane] = b[c];
 			Iw[wib][lane] = idx;
 		}
 		__syncwarp();
 		const int cnt = int((s1 - base) < 32 ? (s1 - base) : 32);
 		for (int j = 0; j < cnt; ++j) {
-			const int ij = Iw[wib][j];
-			const S rj = Rw[wib][j];
-			const S* fj = Fw[wib] + j * kAdfMaxR;
-			const S* bj = Bw[wib] + j * kAdfMaxR;
-			S* gi = G + ij * P;
+			S* gi = G + Iw[wib][j] * P;
 #pragma unroll
 			for (int t = 0; t < kAdfPairsPerLane; ++t) {
 				const int p = lane + 32 * t;
-				if (p < P) gi[p] += (rj * fj[pa[t]]) * bj[pc[t]];
+				if (p < P) gi[p] = fma(RF[pa[t] * 33 + j], BB[pc[t] * 33 + j], gi[p]);
 			}
 		}
 		__syncwarp();
 	}
-	// per-warp partials: G stored (r0, n, r1)
-	double* gp = gpart + warp * (long long)r0 * n * r1;
-	for (int e = lane; e < n * P; e += 32) {
-		const int i = e / P, p = e - i * P, a = p / r1, c = p - a * r1;
-		gp[(a * n + i) * r1 + c] = double(G[e]);
-	}
 	rr = warp_sum(rr);
-	if (lane == 0 && rrpart) rrpart[warp] = rr;
+	if (lane == 0) rrw[wib] = rr;
+	__syncthreads();
+	// the block's partial: its warps' accumulators in warp order, stored (r0, n, r1)
+	double* gp = gpart + (long long)blockIdx.x * r0 * n * r1;
+	for (int e = threadIdx.x; e < n * P; e += blockDim.x) {
+		double t = 0;
+		for (int q = 0; q < kAdfResWarps; ++q) t += double(sm[lay.g(q) + e]);
+		const int i = e / P, p = e - i * P, a = p / r1, c = p - a * r1;
+		gp[(a * n + i) * r1 + c] = t;
+	}
+	if (threadIdx.x == 0 && rrpart) {
+		double t = 0;
+		for (int q = 0; q < kAdfResWarps; ++q) t += rrw[q];
+		rrpart[blockIdx.x] = t;
+	}
 }
 
 // Generic (slow) path for shapes beyond the fast path: residual per sample,
@@ -173,34 +202,49 @@ static void sum_parts(Context& c, const double* part, long long parts, int len, 
 	c.count_launch();
 }
 
-// slice norms: nrm_i = sum_{s: i_s = i} (F[s]^T G[:, i_s, :] B[s])^2, per-warp partials (n values)
+// slice norms: nrm_i = sum_{s: i_s = i} (F[s]^T G[:, i_s, :] B[s])^2, per-block partials
+// (n values). Every thread walks its samples with a per-thread accumulator per slice in
+// shared memory (its own column: conflict-free); the block sums them in thread order.
+constexpr int kAdfNormThreads = 256;
+
 template <class S>
-__global__ void __launch_bounds__(kAdfThreads) k_adf_slicenorm(AdfLevelT<S> L, const double* G, double* npart,
-                                                                long long chunk) {
+__global__ void __launch_bounds__(kAdfNormThreads) k_adf_slicenorm(AdfLevelT<S> L, const double* G, double* npart,
+                                                                    long long chunk) {
 	__shared__ S Gs[kAdfMaxR * kAdfMaxSlices * kAdfMaxR];
-	__shared__ S Aw[kAdfWarpsPerBlock][kAdfMaxSlices][33];  // lane-private accumulators per slice
-	const int lane = threadIdx.x & 31, wib = threadIdx.x >> 5;
-	const long long warp = (long long)blockIdx.x * kAdfWarpsPerBlock + wib;
-	const int r0 = L.r0, n = L.n, r1 = L.r1;
-	for (int e = threadIdx.x; e < r0 * n * r1; e += blockDim.x) Gs[e] = S(G[e]);
-	for (int i = 0; i < kAdfMaxSlices; ++i) Aw[wib][i][lane] = S(0);
+	__shared__ S Acc[kAdfMaxSlices][kAdfNormThreads];
+	const int r0 = L.r0, n = L.n, r1 = L.r1, tid = threadIdx.x;
+	for (int e = tid; e < r0 * n * r1; e += blockDim.x) Gs[e] = S(G[e]);
+	for (int i = 0; i < n; ++i) Acc[i][tid] = S(0);
 	__syncthreads();
-	const long long s0 = warp * chunk, s1 = min(L.N, s0 + chunk);
-	for (long long s = s0 + lane; s < s1; s += 32) {
+	const long long s0 = (long long)blockIdx.x * chunk, s1 = min(L.N, s0 + chunk);
+	for (long long s = s0 + tid; s < s1; s += blockDim.x) {
 		const int idx = L.pos[s];
+		S f[kAdfMaxR], b[kAdfMaxR];
+#pragma unroll
+		for (int a = 0; a < kAdfMaxR; ++a) f[a] = a < r0 ? (L.F ? L.F[a * L.N + s] : S(1)) : S(0);
+#pragma unroll
+		for (int c = 0; c < kAdfMaxR; ++c) b[c] = c < r1 ? (L.B ? L.B[c * L.N + s] : S(1)) : S(0);
 		S v = S(0);
-		for (int a = 0; a < r0; ++a) {
+#pragma unroll
+		for (int a = 0; a < kAdfMaxR; ++a) {
+			if (a >= r0) break;
 			S t = S(0);
 			const S* gr = Gs + (a * n + idx) * r1;
-			for (int c = 0; c < r1; ++c) t += gr[c] * (L.B ? L.B[c * L.N + s] : S(1));
-			v += (L.F ? L.F[a * L.N + s] : S(1)) * t;
+#pragma unroll
+			for (int c = 0; c < kAdfMaxR; ++c)
+				if (c < r1) t = fma(gr[c], b[c], t);
+			v = fma(f[a], t, v);
 		}
-		Aw[wib][idx][lane] += v * v;
+		Acc[idx][tid] = fma(v, v, Acc[idx][tid]);
 	}
-	__syncwarp();
-	for (int i = 0; i < n; ++i) {
-		const double t = warp_sum(double(Aw[wib][i][lane]));
-		if (lane == 0) npart[warp * n + i] = t;
+	__syncthreads();
+	// per slice: the block's threads in order (one warp per slice, lanes strided, then a fixed tree)
+	const int lane = tid & 31, warp = tid >> 5;
+	for (int i = warp; i < n; i += kAdfNormThreads / 32) {
+		double t = 0;
+		for (int q = lane; q < kAdfNormThreads; q += 32) t += double(Acc[i][q]);
+		t = warp_sum(t);
+		if (lane == 0) npart[(long long)blockIdx.x * n + i] = t;
 	}
 }
 
@@ -298,7 +342,7 @@ struct AdfData {
 	float *y32 = nullptr, *res32 = nullptr;
 	std::vector<float*> F32, B32;
 	double *gpart = nullptr, *npart = nullptr, *rrpart = nullptr, *G = nullptr, *nrm = nullptr, *rr = nullptr;
-	long long warps = 0, chunk = 0;
+	long long chunk = 0, res_blocks = 0, norm_chunk = 0, norm_blocks = 0;
 	bool fast = true;
 
 	AdfData(Context& cc, Tensor& xx, const int64_t* positions, const double* values, long long n, bool want_f32 = false)
@@ -355,12 +399,14 @@ struct AdfData {
 				bo += size_t(x.ranks[k]) * N;
 			}
 		}
-		warps = std::max<long long>(1, std::min<long long>((N + 255) / 256, (long long)c.num_sms * 16));
-		warps = (warps + kAdfWarpsPerBlock - 1) / kAdfWarpsPerBlock * kAdfWarpsPerBlock;
-		chunk = (N + warps - 1) / warps;
-		gpart = c.scratch<double>(S_ADF_FIRST + 3, size_t(warps) * maxr * maxn * maxr);
-		npart = c.scratch<double>(S_ADF_FIRST + 4, size_t(warps) * maxn);
-		rrpart = c.scratch<double>(S_ADF_FIRST + 5, size_t(warps));
+		// res_grad: warps of 64 samples, kAdfResWarps per block; slice norms: 1024 samples per block
+		chunk = 64;
+		res_blocks = std::max<long long>(1, (N + chunk * kAdfResWarps - 1) / (chunk * kAdfResWarps));
+		norm_chunk = 1024;
+		norm_blocks = std::max<long long>(1, (N + norm_chunk - 1) / norm_chunk);
+		gpart = c.scratch<double>(S_ADF_FIRST + 3, size_t(res_blocks) * maxr * maxn * maxr);
+		npart = c.scratch<double>(S_ADF_FIRST + 4, size_t(norm_blocks) * maxn);
+		rrpart = c.scratch<double>(S_ADF_FIRST + 5, size_t(res_blocks));
 		G = c.scratch<double>(S_ADF_FIRST + 6, size_t(maxr) * maxn * maxr);
 		nrm = c.scratch<double>(S_ADF_FIRST + 7, size_t(maxn) + 8);
 		rr = nrm + maxn;
@@ -379,21 +425,32 @@ struct AdfData {
 		return L;
 	}
 	AdfLevel level(int k, const double* X) const { return level<double>(k, X, F, B); }
-	unsigned blocks() const { return unsigned(warps / kAdfWarpsPerBlock); }
+	template <class S>
+	size_t res_smem(int k) const {
+		AdfResSmem<S> l{int(x.ranks[k] * x.ranks[k + 1]), int(x.dims[k]), int(x.ranks[k]), int(x.ranks[k + 1])};
+		return size_t(l.total()) * sizeof(S);
+	}
 	// res (mode 0) or given res (mode 1), G into Gout, and sum res^2 into rr[0]
 	void res_grad(int k, int mode, const double* X, double* Gout, double gscale) {
 		const int len = int(x.ranks[k] * x.dims[k] * x.ranks[k + 1]);
 		if (fast) {
+			static bool attr = false;
+			if (!attr) {
+				const int mx = 100 * 1024;
+				XTT_CUDA(cudaFuncSetAttribute(k_adf_res_grad<float>, cudaFuncAttributeMaxDynamicSharedMemorySize, mx));
+				XTT_CUDA(cudaFuncSetAttribute(k_adf_res_grad<double>, cudaFuncAttributeMaxDynamicSharedMemorySize, mx));
+				attr = true;
+			}
 			ProfScope ps(c, "adf_res_grad");
 			if (f32)
-				k_adf_res_grad<float><<<blocks(), kAdfThreads, 0, c.stream>>>(level<float>(k, X, F32, B32), y32, res32,
-				                                                              mode, gpart, rrpart, chunk);
+				k_adf_res_grad<float><<<unsigned(res_blocks), kAdfResThreads, res_smem<float>(k), c.stream>>>(
+				    level<float>(k, X, F32, B32), y32, res32, mode, gpart, rrpart, chunk);
 			else
-				k_adf_res_grad<double><<<blocks(), kAdfThreads, 0, c.stream>>>(level(k, X), y, res, mode, gpart, rrpart,
-				                                                               chunk);
+				k_adf_res_grad<double><<<unsigned(res_blocks), kAdfResThreads, res_smem<double>(k), c.stream>>>(
+				    level(k, X), y, res, mode, gpart, rrpart, chunk);
 			c.count_launch();
-			sum_parts(c, gpart, warps, len, Gout, gscale);
-			sum_parts(c, rrpart, warps, 1, rr, 1.0);
+			sum_parts(c, gpart, res_blocks, len, Gout, gscale);
+			sum_parts(c, rrpart, res_blocks, 1, rr, 1.0);
 		} else {
 			const AdfLevel L = level(k, X);
 			if (mode == 0) k_adf_res_generic<<<std::max<long long>(1, std::min<long long>((N + 255) / 256, 4096)), 256, 0, c.stream>>>(L, y, res);
@@ -409,12 +466,13 @@ struct AdfData {
 		if (fast) {
 			ProfScope ps(c, "adf_slicenorm");
 			if (f32)
-				k_adf_slicenorm<float><<<blocks(), kAdfThreads, 0, c.stream>>>(level<float>(k, x.core[k], F32, B32), G,
-				                                                               npart, chunk);
+				k_adf_slicenorm<float><<<unsigned(norm_blocks), kAdfNormThreads, 0, c.stream>>>(
+				    level<float>(k, x.core[k], F32, B32), G, npart, norm_chunk);
 			else
-				k_adf_slicenorm<double><<<blocks(), kAdfThreads, 0, c.stream>>>(level(k, x.core[k]), G, npart, chunk);
+				k_adf_slicenorm<double><<<unsigned(norm_blocks), kAdfNormThreads, 0, c.stream>>>(level(k, x.core[k]), G,
+				                                                                                  npart, norm_chunk);
 			c.count_launch();
-			sum_parts(c, npart, warps, int(x.dims[k]), nrm, 1.0);
+			sum_parts(c, npart, norm_blocks, int(x.dims[k]), nrm, 1.0);
 		} else {
 			k_adf_slicenorm_generic<<<1, 32, 0, c.stream>>>(level(k, x.core[k]), G, nrm);
 			c.count_launch();

@@ -916,7 +916,14 @@ struct Qc1Layout {
 	__host__ __device__ size_t tot() const { return red() + 2 * size_t(S); }
 	__host__ __device__ size_t tau() const { return tot() + size_t(S); }
 	__host__ __device__ size_t part() const { return tau() + kq; }
-	__host__ __device__ size_t total() const { return part() + 8 * 256; }
+	// column pivoting: partial column norms (vn1, vn2 of dlaqp2), this CTA's partial squared
+	// norms for exact (re)computation, R's diagonal, the permutation and recompute flags (ints)
+	__host__ __device__ size_t vn1() const { return part() + 8 * 256; }
+	__host__ __device__ size_t vn2() const { return vn1() + nw; }
+	__host__ __device__ size_t rec() const { return vn2() + nw; }
+	__host__ __device__ size_t beta() const { return rec() + nw; }
+	__host__ __device__ size_t ints() const { return beta() + kq; }
+	__host__ __device__ size_t total() const { return ints() + size_t(nw) + 2; }
 };
 
 __global__ void __launch_bounds__(kQ1Threads) k_qr_cl1(QrArgs a, Qc1Layout lay) {
@@ -932,6 +939,14 @@ __global__ void __launch_bounds__(kQ1Threads) k_qr_cl1(QrArgs a, Qc1Layout lay) 
 	double* tot = sm + lay.tot();
 	double* tau = sm + lay.tau();
 	double* part = sm + lay.part();
+	double* vn1 = sm + lay.vn1();
+	double* vn2 = sm + lay.vn2();
+	double* rec = sm + lay.rec();
+	double* betas = sm + lay.beta();
+	int* perm = reinterpret_cast<int*>(sm + lay.ints());
+	int* flag = perm + nw;  // nw recompute flags, then the "any" flag
+	__shared__ double s_best[kQ1Threads / 32];
+	__shared__ int s_bidx[kQ1Threads / 32];
 	auto w = [&](int il, int c) -> double& { return W[(long long)il * ldw + c]; };
 	auto lo_of = [&](int g) { return min(max(g - r0, 0), nl); };
 
@@ -940,6 +955,70 @@ __global__ void __launch_bounds__(kQ1Threads) k_qr_cl1(QrArgs a, Qc1Layout lay) 
 		w(il, c) = a.transpose ? a.A[(long long)c * a.lda + gi] : a.A[(long long)gi * a.lda + c];
 	}
 	__syncthreads();
+
+	// pivoting (dlaqp2 order): exact squared norms of columns [c0, nw) over rows >= row0,
+	// summed over the cluster into `out` (one barrier), only where sel(c)
+	auto exact_norms = [&](int c0, int row0, auto sel, auto out) {
+		const int lo = lo_of(row0);
+		for (int c = c0 + tid; c < nw; c += kQ1Threads) {
+			double a0 = 0, a1 = 0;
+			int il = lo;
+			for (; il + 1 < nl; il += 2) {
+				a0 = fma(w(il, c), w(il, c), a0);
+				a1 = fma(w(il + 1, c), w(il + 1, c), a1);
+			}
+			if (il < nl) a0 = fma(w(il, c), w(il, c), a0);
+			rec[c] = a0 + a1;
+		}
+		__syncthreads();
+		cl.sync();
+		for (int c = c0 + tid; c < nw; c += kQ1Threads) {
+			if (!sel(c)) continue;
+			double t = 0;
+			for (int q = 0; q < P; ++q) t += cl.map_shared_rank(rec, q)[c];
+			out(c, t);
+		}
+		__syncthreads();
+	};
+	// the first column of largest vn1 in [c0, nw) (idamax order), swapped into column c0
+	auto pivot_into = [&](int c0) {
+		double best = -1.0;
+		int bi = nw;
+		for (int c = c0 + tid; c < nw; c += kQ1Threads)
+			if (vn1[c] > best) { best = vn1[c]; bi = c; }
+#pragma unroll
+		for (int o = 16; o > 0; o >>= 1) {
+			const double ob = __shfl_xor_sync(0xffffffffu, best, o);
+			const int oi = __shfl_xor_sync(0xffffffffu, bi, o);
+			if (ob > best || (ob == best && oi < bi)) { best = ob; bi = oi; }
+		}
+		if (lane == 0) { s_best[warp] = best; s_bidx[warp] = bi; }
+		__syncthreads();
+		int pv = nw;
+		{
+			double b = -1.0;
+			for (int t = 0; t < kQ1Threads / 32; ++t)
+				if (s_best[t] > b || (s_best[t] == b && s_bidx[t] < pv)) { b = s_best[t]; pv = s_bidx[t]; }
+		}
+		if (pv != c0 && pv < nw) {
+			for (int il = tid; il < nl; il += kQ1Threads) {
+				const double t = w(il, c0);
+				w(il, c0) = w(il, pv);
+				w(il, pv) = t;
+			}
+			if (tid == 0) {
+				double t = vn1[c0]; vn1[c0] = vn1[pv]; vn1[pv] = t;
+				t = vn2[c0]; vn2[c0] = vn2[pv]; vn2[pv] = t;
+				const int q = perm[c0]; perm[c0] = perm[pv]; perm[pv] = q;
+			}
+		}
+		__syncthreads();
+	};
+	if (a.pivot) {
+		for (int c = tid; c < nw; c += kQ1Threads) perm[c] = c;
+		exact_norms(0, 0, [](int) { return true; }, [&](int c, double t) { vn1[c] = vn2[c] = sqrt(t); });
+		pivot_into(0);
+	}
 
 	// this CTA's partials of step jn (rows > jn) into its own slot of parity jn & 1:
 	// field 0 sigma, 1 alpha, 2 + c D_c, 2 + nw + c E_c
@@ -1010,20 +1089,53 @@ __global__ void __launch_bounds__(kQ1Threads) k_qr_cl1(QrArgs a, Qc1Layout lay) 
 			}
 		}
 		__syncthreads();
+		if (tid == 0) betas[j] = beta;
+		if (a.pivot && j + 1 < kq) {
+			// downdate the partial norms with the new row j (R_jc = E_c - wc), recomputing
+			// them exactly where the downdate lost accuracy (dlaqp2, tol3z = sqrt(eps))
+			if (tid == 0) flag[nw] = 0;
+			__syncthreads();
+			const double tol3z = sqrt(DBL_EPSILON / 2);
+			for (int c = c0 + tid; c < nw; c += kQ1Threads) {
+				flag[c] = 0;
+				if (vn1[c] != 0.0) {
+					const double e = tot[2 + nw + c];
+					const double rjc = e - tt * fma(scal, tot[2 + c], e);
+					const double q = fabs(rjc) / vn1[c];
+					const double temp = fmax(0.0, 1.0 - q * q);
+					const double r = vn1[c] / vn2[c];
+					if (temp * r * r <= tol3z) {
+						flag[c] = 1;
+						flag[nw] = 1;
+					} else {
+						vn1[c] *= sqrt(temp);
+					}
+				}
+			}
+			__syncthreads();
+			if (flag[nw])
+				exact_norms(c0, j + 1, [&](int c) { return flag[c] != 0; },
+				            [&](int c, double t) { vn1[c] = vn2[c] = sqrt(t); });
+			pivot_into(c0);
+		}
 		// the reflector below the diagonal, R_jj; then the next step's partials (columns > j)
 		for (int il = lo_of(j + 1) + tid; il < nl; il += kQ1Threads) w(il, j) *= scal;
 		if (tid == 0 && j >= r0 && j < r1) w(j - r0, j) = beta;
 		if (j + 1 < kq) publish(j + 1);
 	}
-	const int rank = kq;
-	if (me == 0 && tid == 0 && a.rank_out) *a.rank_out = rank;
 	__syncthreads();
+	int rank = kq;
+	if (a.pivot)  // the reference's rank rule on R's diagonal: |R_kk| < 16 eps R_00 (signed R_00)
+		for (int k = 1; k < kq; ++k)
+			if (fabs(betas[k]) < 16.0 * DBL_EPSILON * betas[0]) { rank = k; break; }
+	if (me == 0 && tid == 0 && a.rank_out) *a.rank_out = rank;
 	for (long long e = tid; e < (long long)nl * nw; e += kQ1Threads) {
 		const int il = int(e / nw), c = int(e % nw), r = r0 + il;
 		if (r >= rank) continue;
 		const double v = (r <= c) ? w(il, c) : 0.0;
-		if (!a.transpose) a.C[(long long)r * nw + c] = v;
-		else a.C[(long long)c * rank + r] = v;
+		const int pc = a.pivot ? perm[c] : c;
+		if (!a.transpose) a.C[(long long)r * nw + pc] = v;
+		else a.C[(long long)pc * rank + r] = v;
 	}
 	cl.sync();  // every CTA has read the last partials before they are rewritten or freed
 	if (!a.want_q) return;
@@ -1120,6 +1232,66 @@ __global__ void __launch_bounds__(kQrSmallThreads) k_qr_small(QrArgs a) {
 	if (threadIdx.x == 0 && a.rank_out) *a.rank_out = mw < nw ? mw : nw;
 }
 
+// transfer_core with keepRank for small cores in one launch: Householder QR of
+// core `from` (LQ when moving left) in shared memory, Q written back in place,
+// and the triangular factor absorbed into core `to` (R * core_to moving right,
+// core_to * L moving left). The rank is unchanged (it never exceeds the other
+// dimension of the factored matrix).
+__global__ void __launch_bounds__(kQrSmallThreads) k_transfer_small(TransferArgs t) {
+	extern __shared__ double sm_t[];
+	__shared__ BlkQrSmem sh;
+	const int tid = threadIdx.x;
+	if (t.right) {
+		const int mw = t.r0 * t.nf, nw = t.r1, n2 = t.nt * t.r2;
+		double* W = sm_t;
+		double* C = W + size_t(mw) * nw;
+		double* T = C + size_t(nw) * nw;
+		for (int e = tid; e < nw * n2; e += blockDim.x) T[e] = t.to[e];
+		blk_qr(t.from, nw, mw, nw, 0, W, C, t.from, true, sh);
+		for (int e = tid; e < nw * n2; e += blockDim.x) {
+			const int i = e / n2, c = e - i * n2;
+			double acc = 0;
+			for (int k = i; k < nw; ++k) acc = fma(C[i * nw + k], T[k * n2 + c], acc);
+			t.to[e] = acc;
+		}
+	} else {
+		const int nw = t.r0, mw = t.nf * t.r1, m2 = t.rt * t.nt;
+		double* W = sm_t;
+		double* C = W + size_t(mw) * nw;
+		double* T = C + size_t(nw) * nw;
+		for (int e = tid; e < m2 * nw; e += blockDim.x) T[e] = t.to[e];
+		blk_qr(t.from, mw, t.r0, mw, 1, W, C, t.from, true, sh);
+		for (int e = tid; e < m2 * nw; e += blockDim.x) {
+			const int i = e / nw, c = e - i * nw;
+			double acc = 0;
+			for (int k = c; k < nw; ++k) acc = fma(T[i * nw + k], C[k * nw + c], acc);
+			t.to[e] = acc;
+		}
+	}
+}
+
+static size_t transfer_small_bytes(const TransferArgs& t) {
+	const int mw = t.right ? t.r0 * t.nf : t.nf * t.r1, nw = t.right ? t.r1 : t.r0;
+	const long long other = t.right ? (long long)t.nt * t.r2 : (long long)t.rt * t.nt;
+	if (mw < nw || !(mw < 48 || nw < 8) || nw > kBlkQrMaxCols || mw > kQrSmallMaxRows) return 0;
+	const size_t bytes = (size_t(mw) * nw + size_t(nw) * nw + size_t(nw) * other) * sizeof(double);
+	return bytes > kDynSmemMax ? 0 : bytes;
+}
+
+bool transfer_small_fits(const TransferArgs& t) { return transfer_small_bytes(t) > 0; }
+
+void launch_transfer_small(const TransferArgs& t, cudaStream_t s) {
+	const size_t bytes = transfer_small_bytes(t);
+	XTT_REQUIRE(bytes > 0, "internal: transfer_core shapes do not fit the one-launch kernel");
+	static bool attr = false;
+	if (!attr) {
+		XTT_CUDA(cudaFuncSetAttribute(k_transfer_small, cudaFuncAttributeMaxDynamicSharedMemorySize, int(kDynSmemMax)));
+		attr = true;
+	}
+	k_transfer_small<<<1, kQrSmallThreads, bytes, s>>>(t);
+	XTT_CUDA(cudaGetLastError());
+}
+
 // Cluster geometry for an mw x nw factorisation: 0 CTAs if the one-CTA kernel is used.
 static int qr_cluster_size(int mw, int nw, QcLayout& lay) {
 	if (mw < 48 || nw < 8) return 0;
@@ -1147,7 +1319,7 @@ void launch_qr(const QrArgs& a, cudaStream_t s) {
 			return;
 		}
 	}
-	if (!a.pivot) {
+	{
 		Qc1Layout l1;
 		const int P1 = qr_cl1_size(mw, nw, l1);
 		if (P1 > 1) {

@@ -54,6 +54,18 @@ inline double qr_work_flops(const QrArgs& a) {
 
 // Launchers (stream-ordered, asynchronous).
 void launch_qr(const QrArgs& a, cudaStream_t s);
+
+// transfer_core with keepRank of a small core in one launch (QR / LQ of core `from`, Q in
+// place, the triangular factor absorbed into core `to`), for the shapes transfer_small_fits accepts.
+struct TransferArgs {
+	double* from = nullptr;
+	double* to = nullptr;
+	int r0 = 0, nf = 0, r1 = 0;  // core from (r0, nf, r1)
+	int rt = 0, nt = 0, r2 = 0;  // core to: (r1, nt, r2) moving right, (rt, nt, r0) moving left
+	int right = 1;
+};
+bool transfer_small_fits(const TransferArgs& t);
+void launch_transfer_small(const TransferArgs& t, cudaStream_t s);
 size_t qr_work_doubles(int m, int n);        // global workspace needed (0 if shared memory suffices)
 void launch_svd(const SvdArgs& a, cudaStream_t s);
 size_t svd_work_doubles(int m, int n);

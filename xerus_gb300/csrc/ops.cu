@@ -464,6 +464,23 @@ bool exceeds_maximal_ranks(const Tensor& x) {
 void transfer_core(Tensor& x, int from, int to, bool rr) {
 	Context& c = *x.ctx;
 	const int64_t r0 = x.ranks[from], nf = x.n(from), r1 = x.ranks[from + 1];
+	if (!rr) {
+		// small cores: factorisation and absorption in one launch, ranks unchanged
+		TransferArgs t;
+		t.from = x.core[from];
+		t.to = x.core[to];
+		t.r0 = int(r0); t.nf = int(nf); t.r1 = int(r1);
+		t.right = to == from + 1;
+		t.rt = int(x.ranks[to]); t.nt = int(x.n(to)); t.r2 = int(x.ranks[to + 1]);
+		if (transfer_small_fits(t)) {
+			QrArgs q;  // for the declared work only
+			q.m = t.right ? int(r0 * nf) : int(r0); q.n = t.right ? int(r1) : int(nf * r1); q.transpose = t.right ? 0 : 1;
+			ProfScope ps(c, "qr", qr_work_bytes(q), qr_work_flops(q));
+			launch_transfer_small(t, c.stream);
+			c.count_launch();
+			return;
+		}
+	}
 	QrArgs a;
 	if (to == from + 1) {
 		const int m = int(r0 * nf), n = int(r1), kq = std::min(m, n);
