@@ -296,6 +296,22 @@ typedef struct xtt_adf_options {
 int xtt_adf(xtt_tensor* x, const int64_t* positions, const double* values, int64_t num,
             const xtt_adf_options* opt, double* final_residual, double* residual_trace,
             int64_t trace_capacity, int64_t* trace_count);
+
+/* RankOneMeasurementSet (include/xerus/measurments.h:94-140): a sample is
+ * <x, u_1 (x) ... (x) u_d> for vectors u_k of length n_k; `vectors` holds each
+ * sample's vectors concatenated (num x sum n_k doubles, row-major).
+ * xtt_random_rank_one: RankOneMeasurementSet::random(num, dims)
+ * (src/xerus/measurments.cpp:522-544): Gaussian vectors from the library's random
+ * state (Tensor::random per mode), sorted as the reference sorts them.
+ * xtt_entries_rank_one: RankOneMeasurementSet::measure(TensorNetwork).
+ * xtt_adf_rank_one: ADFVariant(maxIter, target, minDecrease)(x, RankOneMeasurementSet)
+ * (src/xerus/algorithms/adf.cpp:233-288, 333-357, 405-408, 481-487), FP64 only, ranks
+ * <= 8 and mode sizes <= 16 on the device. */
+int xtt_random_rank_one(int64_t num, int64_t order, const int64_t* dims, double* vectors);
+int xtt_entries_rank_one(const xtt_tensor* x, const double* vectors, int64_t count, double* out);
+int xtt_adf_rank_one(xtt_tensor* x, const double* vectors, const double* values, int64_t num,
+                     const xtt_adf_options* opt, double* final_residual, double* residual_trace,
+                     int64_t trace_capacity, int64_t* trace_count);
 /* Loss 0.5 ||P_Omega(x) - y||^2 and its gradient with respect to every core of x
  * (adjoint of the sampled-entry map; at the core position it is minus
  * ADF's projected gradient, src/xerus/algorithms/adf.cpp:359-396). */

@@ -715,6 +715,37 @@ static void adf_case(const std::string& tag, const std::vector<size_t>& dims, si
 }
 
 static void case_adf() { adf_case("small", {4, 5, 3, 5, 4, 3}, 3, 2000, 30, true, true); }
+
+// ADF on rank-one measurements: <x, u_1 (x) ... (x) u_d> with Gaussian vectors u_k
+// (RankOneMeasurementSet::random draws them with Tensor::random and sorts the samples).
+static void case_adf_rankone() {
+	reseed();
+	const std::vector<size_t> dims{4, 5, 4, 5};
+	TTTensor target = TTTensor::random(dims, 2);
+	RankOneMeasurementSet m = RankOneMeasurementSet::random(300, target);
+	TTTensor x = TTTensor::random(dims, 2);
+	save_tt("target", target);
+	save_tt("x0", x);
+	std::vector<double> vec;
+	for (auto& p : m.positions)
+		for (auto& t : p) {
+			Tensor u = t;
+			u.use_dense_representation();
+			for (size_t i = 0; i < u.size; ++i) vec.push_back(u[i]);
+		}
+	size_t sum_n = 0;
+	for (auto n : dims) sum_n += n;
+	save("vectors", vec, {m.size(), sum_n});
+	save("values", m.measuredValues);
+	PerformanceData perf(false, true);
+	ADFVariant adf(25, 0.0, 1.0);
+	const double res = adf(x, m, perf);
+	save("perf_residual", perf_residuals(perf));
+	save_scalar("final_residual", res);
+	save_tt("x_final", x);
+	auto pos = probe_positions(dims, 100, 31);
+	save_probes("x_final", x, pos);
+}
 static void case_adf_cfg5() { adf_case("cfg5", std::vector<size_t>(10, 8), 6, 200000, 50, false, true); }
 
 // xerus's own binary file format (misc::save_to_file): the bytes of files written
@@ -766,6 +797,7 @@ int main(int argc, char** argv) {
 	else if (c == "fileio") case_fileio();
 	else if (c == "als_nonspd") case_als_nonspd();
 	else if (c == "arith") case_arith();
+	else if (c == "adf_rankone") case_adf_rankone();
 	else {
 		std::fprintf(stderr, "unknown case %s\n", c.c_str());
 		return 2;

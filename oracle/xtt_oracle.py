@@ -1026,6 +1026,77 @@ def adf(x: TT, positions, values, max_iter: int = 0, target: float = 1e-8, min_d
     return ADFSolver(x, positions, values, max_iter, target, min_dec).solve()
 
 
+# --------------------------------------------------------------------------- rank-one measurements
+
+
+def _split_vectors(vectors, dims):
+    """(N, sum n_k) rows -> per mode (N, n_k) blocks."""
+    out, off = [], 0
+    for n in dims:
+        out.append(np.asarray(vectors[:, off:off + n], dtype=np.float64))
+        off += n
+    return out
+
+
+def rank_one_random(num: int, dims, rs: RandomEngine) -> np.ndarray:
+    """RankOneMeasurementSet::create_random_positions (measurments.cpp:522-544): per sample
+    and mode a Tensor::random({n}) (n draws of the stateful default normal distribution),
+    then sort(true) with internal::comp (measurments.cpp:330-347, 549-...): samples ordered
+    mode by mode, entry by entry, DEcreasing at the first difference."""
+    dims = list(dims)
+    rows = [np.concatenate([rs.normal.draw(rs.eng, n) for n in dims]) for _ in range(num)]
+    rows.sort(key=lambda r: tuple(-v for v in r))
+    return np.array(rows).reshape(num, sum(dims))
+
+
+def rank_one_measure(x: TT, vectors) -> np.ndarray:
+    """RankOneMeasurementSet::measure(TensorNetwork): <x, u_1 (x) ... (x) u_d> per sample."""
+    us = _split_vectors(np.asarray(vectors), x.dims)
+    v = np.ones((us[0].shape[0], 1))
+    for k, c in enumerate(x.cores):
+        v = np.einsum("sa,si,aib->sb", v, us[k], c, optimize=True)
+    return v[:, 0]
+
+
+class ADFRankOneSolver(ADFSolver):
+    """ADFVariant::InternalSolver<RankOneMeasurementSet> (adf.cpp:233-288, 333-357, 405-408,
+    481-487): the stacks contract each core with the sample's vector for its mode (the mixed
+    component sum_i u[i] X[:, i, :]); the gradient takes every entry of the vector; the norm
+    of the projected gradient is one total (position_or_zero gives slot 0); update_x takes one
+    step for the whole core. Random Gaussian vectors never share prefixes, so both stack
+    sides count N updates and the backward side evaluates (adf.cpp:295, 420)."""
+
+    def __init__(self, x: TT, vectors: np.ndarray, values: np.ndarray, max_iter: int, target: float, min_dec: float):
+        vectors = np.asarray(vectors, dtype=np.float64)
+        self.us = _split_vectors(vectors, x.dims)
+        N = vectors.shape[0]
+        super().__init__(x, np.zeros((N, x.d), dtype=np.int64), values, max_iter, target, min_dec)
+        self.fwd_updates = [N] * self.d
+        self.bwd_updates = [N] * self.d
+
+    def _slices(self, core, k):
+        return np.einsum("si,aib->sab", self.us[k], core, optimize=True)
+
+    def projected_gradient(self, k):
+        f, b = self.fstack(k - 1), self.bstack(k + 1)
+        return np.einsum("s,si,sa,sc->aic", self.res, self.us[k], f, b, optimize=True)
+
+    def slicewise_norm(self, k, G):
+        tmp = self.update_backward(k, G)
+        cur = np.einsum("sa,sa->s", self.fstack(k - 1), tmp)
+        out = np.zeros(G.shape[1])
+        out[0] = float(np.sum(cur ** 2))
+        return out
+
+    def update_x(self, k, G, norms):
+        pyr = float(np.sum(G * G))
+        self.x.cores[k] = self.x.cores[k] + (pyr / float(np.sum(norms))) * G
+
+
+def adf_rank_one(x: TT, vectors, values, max_iter: int = 0, target: float = 1e-8, min_dec: float = 0.999) -> ADFResult:
+    return ADFRankOneSolver(x, vectors, values, max_iter, target, min_dec).solve()
+
+
 def adf_loss_gradient(x: TT, positions, values):
     """Gradient of 0.5 * ||P_Omega(x) - y||^2 with respect to every core (no gauge
     condition), by the same stacks: dL/dX_k[a,i,b] = -sum_{s: i_s=i} res_s F_{k-1}[s,a] B_{k+1}[s,b]."""

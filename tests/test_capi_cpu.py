@@ -66,3 +66,19 @@ def test_version_and_error_without_gpu(libpath):
     # argument checks run on the host and fail loudly before touching a device
     assert lib.xtt_context_create(0, None) == 1
     assert b"NULL" in lib.xtt_last_error()
+
+
+def test_rank_one_random_matches_reference(libpath, golden):
+    """RankOneMeasurementSet::random on the host: the reference's Gaussian vectors in its
+    sort order, after a TTTensor::random draw (same engine and normal distribution)."""
+    import numpy as np
+    import xerus_gb300 as xg
+    z = golden("adf_rankone")
+    dims = [4, 5, 4, 5]
+    xg.seed(0xBAADF00D)
+    # the target's cores consume the first draws: 1*4*2 + 2*5*2 + 2*4*2 + 2*5*1
+    burn = np.zeros(8 + 20 + 16 + 10)
+    xg._lib.load().xtt_random_normal(0.0, 1.0, burn.size, burn.ctypes.data_as(xg._lib.c_double_p))
+    m = xg.RankOneMeasurementSet.random(300, dims)
+    np.testing.assert_array_equal(m.vectors, z["vectors"])
+    assert [list(map(len, p)) for p in m.positions[:1]] == [dims]

@@ -368,6 +368,27 @@ def test_adf_small(ctx, golden):
     assert abs(res / z["small_final_residual"][0] - 1) < 1e-6
 
 
+def test_adf_rank_one_matches_reference(ctx, golden):
+    """ADF on rank-one measurements (RankOneMeasurementSet): the reference's trajectory and
+    final iterate; the device measurement of the target against the reference's values."""
+    z = golden("adf_rankone")
+    dims = [4, 5, 4, 5]
+    t = dev_tt(ctx, tt_of(z, "target"))
+    m = xg.RankOneMeasurementSet(z["vectors"], None, dims)
+    m.measure(t)
+    assert rel_err(m.measuredValues, z["values"]) < 1e-12
+    m = xg.RankOneMeasurementSet(z["vectors"], z["values"], dims)
+    x = dev_tt(ctx, tt_of(z, "x0"))
+    perf = xg.PerformanceData()
+    res = xg.ADFVariant(25, 0.0, 1.0)(x, m, perf)
+    pr = z["perf_residual"]
+    assert len(perf.residuals) == len(pr)
+    assert rel_err(perf.residuals[:10], pr[:10]) < 1e-10
+    assert rel_err(perf.residuals, pr) < 1e-8
+    assert abs(res / z["final_residual"][0] - 1) < 1e-8
+    assert rel_err(x.entries(z["x_final_probe_pos"]), z["x_final_probe_val"]) < 1e-8
+
+
 def test_adf_cfg5_positions_gradient_and_first_iterations(ctx, golden):
     z = golden("adf_cfg5")
     _, m, x = _adf_inputs(ctx, [8] * 10, 6, 200000)

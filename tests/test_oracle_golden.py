@@ -216,3 +216,20 @@ def test_adf_cfg5_positions_and_gradient(golden):
     s.solve(first_sweep_log=log)
     assert rel_err(np.concatenate([g.ravel() for g, _ in log]), z["cfg5_grad_sweep"]) < REL_TOL
     assert rel_err(np.concatenate([n for _, n in log]), z["cfg5_slicenorm_sweep"]) < 1e-10
+
+
+def test_adf_rank_one(golden):
+    """RankOneMeasurementSet::random (Gaussian vectors, the reference's sort order) and
+    ADF on rank-one measurements, against the reference run."""
+    z = golden("adf_rankone")
+    rs = o.RandomEngine()
+    dims = [4, 5, 4, 5]
+    target = o.tt_random(dims, 2, rs)
+    assert np.array_equal(np.concatenate([c.ravel() for c in target.cores]), z["target_cores"])
+    vec = o.rank_one_random(300, dims, rs)
+    assert np.array_equal(vec, z["vectors"])
+    assert rel_err(o.rank_one_measure(target, vec), z["values"]) < 1e-13
+    x = tt_of(z, "x0")
+    res = o.adf_rank_one(x, z["vectors"], z["values"], 25, 0.0, 1.0)
+    assert rel_err(res.residuals, z["perf_residual"]) < 1e-10
+    assert rel_err(o.tt_entries(x, z["x_final_probe_pos"]), z["x_final_probe_val"]) < 1e-10

@@ -17,7 +17,7 @@ import numpy as np
 from . import _lib as L
 
 __all__ = ["Context", "TTTensor", "TTOperator", "frob_norm", "dot", "residual", "ALSVariant", "ALS", "ALS_SPD", "DMRG", "DMRG_SPD", "ASD",
-           "ASD_SPD", "ADFVariant", "ADF", "SinglePointMeasurementSet", "PerformanceData", "seed", "EPSILON",
+           "ASD_SPD", "ADFVariant", "ADF", "SinglePointMeasurementSet", "RankOneMeasurementSet", "PerformanceData", "seed", "EPSILON",
            "XttError", "FP64", "MIXED", "als_batch", "apply", "save_to_file", "load_from_file", "file_encode", "file_decode"]
 
 EPSILON = 8 * np.finfo(np.float64).eps  # include/xerus/basic.h:50
@@ -574,8 +574,54 @@ class SinglePointMeasurementSet:
         return float(np.sqrt(np.sum(self.measuredValues ** 2)))
 
 
+class RankOneMeasurementSet:
+    """xerus::RankOneMeasurementSet (include/xerus/measurments.h:94-140): sample s is
+    <x, u_1 (x) ... (x) u_d>. `positions[s][k]` is u_k of sample s; the vectors are held
+    concatenated per sample in `vectors` (N x sum n_k)."""
+
+    def __init__(self, vectors=None, measuredValues=None, dims=None):
+        self.vectors = np.zeros((0, 0)) if vectors is None else np.ascontiguousarray(vectors, dtype=np.float64)
+        self.dims = [int(v) for v in dims] if dims is not None else None
+        self.measuredValues = np.zeros(self.vectors.shape[0]) if measuredValues is None else \
+            np.asarray(measuredValues, dtype=np.float64)
+
+    @staticmethod
+    def random(num, dims_or_solution):
+        """random(num, dims) or random(num, solution) (measured on the solution)."""
+        sol = dims_or_solution if isinstance(dims_or_solution, _TT) else None
+        dims = [int(v) for v in (sol.dimensions if sol is not None else dims_or_solution)]
+        out = np.zeros((int(num), sum(dims)))
+        d, pd = _i64(dims)
+        L.check(L.load().xtt_random_rank_one(int(num), len(dims), pd, out.ctypes.data_as(L.c_double_p)))
+        m = RankOneMeasurementSet(out, None, dims)
+        if sol is not None:
+            m.measure(sol)
+        return m
+
+    @property
+    def positions(self):
+        offs = np.cumsum([0] + self.dims)
+        return [[self.vectors[s, offs[k]:offs[k + 1]] for k in range(len(self.dims))] for s in range(self.size())]
+
+    def size(self):
+        return int(self.vectors.shape[0])
+
+    def degree(self):
+        return len(self.dims) if self.dims else 0
+
+    def measure(self, tt):
+        out = np.zeros(self.size())
+        L.check(tt.lib.xtt_entries_rank_one(tt.handle, self.vectors.ctypes.data_as(L.c_double_p), self.size(),
+                                            out.ctypes.data_as(L.c_double_p)))
+        self.measuredValues = out
+
+    def frob_norm(self):
+        return float(np.sqrt(np.sum(self.measuredValues ** 2)))
+
+
 class ADFVariant:
-    """xerus::ADFVariant (include/xerus/algorithms/adf.h:39-266) for single-point samples."""
+    """xerus::ADFVariant (include/xerus/algorithms/adf.h:39-266) for single-point and
+    rank-one measurement sets."""
 
     def __init__(self, maxIterations, targetResidualNorm, minimalResidualNormDecrease, precision=None):
         self.maxIterations = maxIterations
@@ -585,15 +631,20 @@ class ADFVariant:
         self.precision = FP64 if precision is None else precision
 
     def __call__(self, x, measurements, perfData=None):
-        pos, pp = _i64(measurements.positions)
         val, pv = _f64(measurements.measuredValues)
         o = L.AdfOptions(int(self.maxIterations), float(self.targetResidualNorm),
                          float(self.minimalResidualNormDecrease), int(self.precision), 0)
         cap = max(16, int(self.maxIterations) + 2 if self.maxIterations else 100000)
         trace = np.zeros(cap)
         fin, cnt = ctypes.c_double(), ctypes.c_int64()
-        L.check(x.lib.xtt_adf(x.handle, pp, pv, pos.shape[0], ctypes.byref(o), ctypes.byref(fin),
-                              trace.ctypes.data_as(L.c_double_p), cap, ctypes.byref(cnt)))
+        if isinstance(measurements, RankOneMeasurementSet):
+            vec, pu = _f64(measurements.vectors)
+            L.check(x.lib.xtt_adf_rank_one(x.handle, pu, pv, vec.shape[0], ctypes.byref(o), ctypes.byref(fin),
+                                           trace.ctypes.data_as(L.c_double_p), cap, ctypes.byref(cnt)))
+        else:
+            pos, pp = _i64(measurements.positions)
+            L.check(x.lib.xtt_adf(x.handle, pp, pv, pos.shape[0], ctypes.byref(o), ctypes.byref(fin),
+                                  trace.ctypes.data_as(L.c_double_p), cap, ctypes.byref(cnt)))
         if perfData is not None:
             perfData.residuals = list(trace[:min(cnt.value, cap)])
         return fin.value

@@ -82,6 +82,10 @@ _SIGNATURES = {
     "xtt_context_set_cg_path": (ctypes.c_int, [VP, ctypes.c_int]),
     "xtt_context_profile_work": (ctypes.c_int, [VP, ctypes.c_char_p, c_double_p, c_double_p]),
     "xtt_apply": (ctypes.c_int, [VP, VP, ctypes.POINTER(VP)]),
+    "xtt_random_rank_one": (ctypes.c_int, [ctypes.c_int64, ctypes.c_int64, c_int64_p, c_double_p]),
+    "xtt_entries_rank_one": (ctypes.c_int, [VP, c_double_p, ctypes.c_int64, c_double_p]),
+    "xtt_adf_rank_one": (ctypes.c_int, [VP, c_double_p, c_double_p, ctypes.c_int64, ctypes.POINTER(AdfOptions),
+                                        c_double_p, c_double_p, ctypes.c_int64, c_int64_p]),
     "xtt_add": (ctypes.c_int, [VP, VP, ctypes.c_double]),
     "xtt_tensor_save": (ctypes.c_int, [VP, ctypes.c_char_p]),
     "xtt_tensor_load": (ctypes.c_int, [VP, ctypes.c_char_p, ctypes.POINTER(VP)]),

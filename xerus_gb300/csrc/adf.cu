@@ -566,6 +566,340 @@ AdfResult adf(Tensor& x, const int64_t* positions, const double* values, long lo
 	return out;
 }
 
+// ------------------------------------------------------------ rank-one measurements
+//
+// ADFVariant::InternalSolver<RankOneMeasurementSet> (adf.cpp:233-288, 333-357, 405-408,
+// 481-487): a sample is <x, u_1 (x) ... (x) u_d> with a vector u_k per mode, so a stack
+// update contracts the core with the sample's mixed component sum_i u_k[i] X_k[:, i, :];
+// the projected gradient takes every entry of u_k; the slice norms collapse into one
+// total (position_or_zero is 0) and update_x takes one step for the whole core. The
+// vectors are stored mode-major (entry i of sample s at i*N + s), like the stacks.
+
+constexpr int kR1Threads = 128;
+constexpr int kR1Warps = kR1Threads / 32;
+constexpr int kR1MaxN = 16;
+
+struct R1Level {
+	const double* U;  // this mode's vectors: n x N
+	const double* F;  // F_{k-1}: r0 x N (nullptr: the constant 1)
+	const double* B;  // B_{k+1}: r1 x N (nullptr: the constant 1)
+	const double* X;  // core (r0, n, r1)
+	int r0, n, r1;
+	long long N;
+};
+
+// <f, M(u) b> for one sample with the core (or gradient) in shared memory
+__device__ __forceinline__ double r1_value(const double* Xs, const R1Level& L, long long s, const double* f,
+                                           const double* b) {
+	double v = 0.0;
+	for (int a = 0; a < L.r0; ++a) {
+		double t = 0.0;
+		for (int i = 0; i < L.n; ++i) {
+			const double* xr = Xs + (a * L.n + i) * L.r1;
+			double w = 0.0;
+			for (int c = 0; c < L.r1; ++c) w = fma(xr[c], b[c], w);
+			t = fma(L.U[(long long)i * L.N + s], w, t);
+		}
+		v = fma(f[a], t, v);
+	}
+	return v;
+}
+
+// B_k[a][s] = sum_i u[i] sum_c X[a,i,c] B_{k+1}[c][s]  (update_backward_stack, adf.cpp:234-249)
+__global__ void k_r1_backward(R1Level L, double* Bo) {
+	extern __shared__ double xs_r1[];
+	for (int e = threadIdx.x; e < L.r0 * L.n * L.r1; e += blockDim.x) xs_r1[e] = L.X[e];
+	__syncthreads();
+	for (long long s = blockIdx.x * (long long)blockDim.x + threadIdx.x; s < L.N; s += (long long)gridDim.x * blockDim.x) {
+		double b[kAdfMaxR];
+		for (int c = 0; c < L.r1; ++c) b[c] = L.B ? L.B[c * L.N + s] : 1.0;
+		for (int a = 0; a < L.r0; ++a) {
+			double t = 0.0;
+			for (int i = 0; i < L.n; ++i) {
+				const double* xr = xs_r1 + (a * L.n + i) * L.r1;
+				double w = 0.0;
+				for (int c = 0; c < L.r1; ++c) w = fma(xr[c], b[c], w);
+				t = fma(L.U[(long long)i * L.N + s], w, t);
+			}
+			Bo[a * L.N + s] = t;
+		}
+	}
+}
+
+// F_k[c][s] = sum_a F_{k-1}[a][s] sum_i u[i] X[a,i,c]  (update_forward_stack, adf.cpp:271-288)
+__global__ void k_r1_forward(R1Level L, double* Fo) {
+	extern __shared__ double xs_r1[];
+	for (int e = threadIdx.x; e < L.r0 * L.n * L.r1; e += blockDim.x) xs_r1[e] = L.X[e];
+	__syncthreads();
+	for (long long s = blockIdx.x * (long long)blockDim.x + threadIdx.x; s < L.N; s += (long long)gridDim.x * blockDim.x) {
+		double f[kAdfMaxR], u[kR1MaxN];
+		for (int a = 0; a < L.r0; ++a) f[a] = L.F ? L.F[a * L.N + s] : 1.0;
+		for (int i = 0; i < L.n; ++i) u[i] = L.U[(long long)i * L.N + s];
+		for (int c = 0; c < L.r1; ++c) {
+			double t = 0.0;
+			for (int a = 0; a < L.r0; ++a) {
+				double w = 0.0;
+				for (int i = 0; i < L.n; ++i) w = fma(u[i], xs_r1[(a * L.n + i) * L.r1 + c], w);
+				t = fma(f[a], w, t);
+			}
+			Fo[c * L.N + s] = t;
+		}
+	}
+}
+
+// res_s and per-block partials of G (r0, n, r1) and sum res^2 (calculate_residual,
+// calculate_projected_gradient with perform_dyadic_product, adf.cpp:290-357). Lanes own the
+// (a, c) pairs and, for them, every slice i in registers; samples are staged 32 at a time
+// (res F premultiplied, B, u) and added in order; warps summed in order (deterministic).
+__global__ void __launch_bounds__(kR1Threads) k_r1_res_grad(R1Level L, const double* y, double* res, double* gpart,
+                                                            double* rrpart, long long chunk) {
+	extern __shared__ double sm_r1[];
+	const int lane = threadIdx.x & 31, wib = threadIdx.x >> 5;
+	const int r0 = L.r0, n = L.n, r1 = L.r1, P = r0 * r1;
+	double* Xs = sm_r1;                                   // r0 n r1
+	double* RF = Xs + r0 * n * r1 + wib * (r0 + r1 + n) * 33;  // per warp: r0 + r1 + n rows of 33
+	double* BB = RF + r0 * 33;
+	double* UU = BB + r1 * 33;
+	double* Gw = Xs + r0 * n * r1 + kR1Warps * (r0 + r1 + n) * 33;  // per warp n P, for the block sum
+	__shared__ double rrw[kR1Warps];
+	for (int e = threadIdx.x; e < r0 * n * r1; e += blockDim.x) Xs[e] = L.X[e];
+	__syncthreads();
+	int pa[kAdfPairsPerLane], pc[kAdfPairsPerLane];
+	double acc[kAdfPairsPerLane][kR1MaxN];
+#pragma unroll
+	for (int t = 0; t < kAdfPairsPerLane; ++t) {
+		const int p = lane + 32 * t;
+		pa[t] = p < P ? p / r1 : 0;
+		pc[t] = p < P ? p - pa[t] * r1 : 0;
+#pragma unroll
+		for (int i = 0; i < kR1MaxN; ++i) acc[t][i] = 0.0;
+	}
+	double rr = 0.0;
+	const long long s0 = ((long long)blockIdx.x * kR1Warps + wib) * chunk, s1 = min(L.N, s0 + chunk);
+	for (long long base = s0; base < s1; base += 32) {
+		const long long s = base + lane;
+		if (s < s1) {
+			double f[kAdfMaxR], b[kAdfMaxR];
+			for (int a = 0; a < r0; ++a) f[a] = L.F ? L.F[a * L.N + s] : 1.0;
+			for (int c = 0; c < r1; ++c) b[c] = L.B ? L.B[c * L.N + s] : 1.0;
+			const double rs = y[s] - r1_value(Xs, L, s, f, b);
+			res[s] = rs;
+			rr = fma(rs, rs, rr);
+			for (int a = 0; a < r0; ++a) RF[a * 33 + lane] = rs * f[a];
+			for (int c = 0; c < r1; ++c) BB[c * 33 + lane] = b[c];
+			for (int i = 0; i < n; ++i) UU[i * 33 + lane] = L.U[(long long)i * L.N + s];
+		}
+		__syncwarp();
+		const int cnt = int((s1 - base) < 32 ? (s1 - base) : 32);
+		for (int j = 0; j < cnt; ++j) {
+#pragma unroll
+			for (int t = 0; t < kAdfPairsPerLane; ++t) {
+				if (lane + 32 * t >= P) continue;
+				const double q = RF[pa[t] * 33 + j] * BB[pc[t] * 33 + j];
+#pragma unroll
+				for (int i = 0; i < kR1MaxN; ++i)
+					if (i < n) acc[t][i] = fma(q, UU[i * 33 + j], acc[t][i]);
+			}
+		}
+		__syncwarp();
+	}
+	// the warp's accumulators into shared memory, then the block sum in warp order
+	double* gw = Gw + wib * n * P;
+#pragma unroll
+	for (int t = 0; t < kAdfPairsPerLane; ++t) {
+		const int p = lane + 32 * t;
+		if (p >= P) continue;
+#pragma unroll
+		for (int i = 0; i < kR1MaxN; ++i)
+			if (i < n) gw[i * P + p] = acc[t][i];
+	}
+	rr = warp_sum(rr);
+	if (lane == 0) rrw[wib] = rr;
+	__syncthreads();
+	double* gp = gpart + (long long)blockIdx.x * r0 * n * r1;
+	for (int e = threadIdx.x; e < n * P; e += blockDim.x) {
+		double t = 0;
+		for (int q = 0; q < kR1Warps; ++q) t += Gw[q * n * P + e];
+		const int i = e / P, p = e - i * P, a = p / r1, c = p - a * r1;
+		gp[(a * n + i) * r1 + c] = t;
+	}
+	if (threadIdx.x == 0) {
+		double t = 0;
+		for (int q = 0; q < kR1Warps; ++q) t += rrw[q];
+		rrpart[blockIdx.x] = t;
+	}
+}
+
+// per-block partials of sum_s <F[s], M_G(u_s) B[s]>^2 (calculate_slicewise_norm_A_projGrad
+// with every sample in slot 0, adf.cpp:413-465)
+__global__ void __launch_bounds__(kR1Threads) k_r1_norm(R1Level L, const double* G, double* npart, long long chunk) {
+	__shared__ double Gs[kAdfMaxR * kR1MaxN * kAdfMaxR];
+	__shared__ double red[32];
+	for (int e = threadIdx.x; e < L.r0 * L.n * L.r1; e += blockDim.x) Gs[e] = G[e];
+	__syncthreads();
+	double acc = 0.0;
+	const long long s0 = (long long)blockIdx.x * chunk, s1 = min(L.N, s0 + chunk);
+	for (long long s = s0 + threadIdx.x; s < s1; s += blockDim.x) {
+		double f[kAdfMaxR], b[kAdfMaxR];
+		for (int a = 0; a < L.r0; ++a) f[a] = L.F ? L.F[a * L.N + s] : 1.0;
+		for (int c = 0; c < L.r1; ++c) b[c] = L.B ? L.B[c * L.N + s] : 1.0;
+		const double v = r1_value(Gs, L, s, f, b);
+		acc = fma(v, v, acc);
+	}
+	acc = block_sum(acc, red);
+	if (threadIdx.x == 0) npart[blockIdx.x] = acc;
+}
+
+// X += (||G||^2 / nrm) G  (update_x for rank-one sets, adf.cpp:481-487); one block
+__global__ void k_r1_update(double* X, const double* G, const double* nrm, int len) {
+	__shared__ double sc[32];
+	double s = 0.0;
+	for (int e = threadIdx.x; e < len; e += blockDim.x) s = fma(G[e], G[e], s);
+	const double step = block_sum(s, sc) / nrm[0];
+	for (int e = threadIdx.x; e < len; e += blockDim.x) X[e] = fma(step, G[e], X[e]);
+}
+
+AdfResult adf_rank_one(Tensor& x, const double* vectors, const double* values, long long N, int64_t max_iter,
+                       double target, double min_dec) {
+	// ADFVariant::InternalSolver<RankOneMeasurementSet>::solve (adf.cpp:489-604) with x at its ranks
+	Context& c = *x.ctx;
+	XTT_REQUIRE(!x.op, "ADF needs a TT tensor");
+	XTT_REQUIRE(N > 0, "need at very least one measurement");
+	const int d = x.d;
+	int64_t maxr = 1, maxn = 1, sum_n = 0;
+	for (int k = 0; k <= d; ++k) maxr = std::max(maxr, x.ranks[k]);
+	for (int k = 0; k < d; ++k) {
+		maxn = std::max(maxn, x.dims[k]);
+		sum_n += x.dims[k];
+	}
+	XTT_REQUIRE(maxr <= kAdfMaxR && maxn <= kR1MaxN && maxr * maxr <= 32 * kAdfPairsPerLane,
+	            "rank-one ADF on the device needs ranks <= 8 and mode sizes <= 16");
+	double ny2 = 0;
+	for (long long s = 0; s < N; ++s) ny2 += values[s] * values[s];
+	const double norm_y = std::sqrt(ny2);
+	move_core(x, 0, false);  // canonicalize_left (adf.cpp:582)
+	// device data: vectors mode-major, values, residuals, stacks, partials
+	std::vector<double> hu(size_t(sum_n) * N);
+	std::vector<size_t> uoff(d, 0);
+	for (int k = 1; k < d; ++k) uoff[k] = uoff[k - 1] + size_t(x.dims[k - 1]) * N;
+	for (long long s = 0; s < N; ++s) {
+		size_t col = 0;
+		for (int k = 0; k < d; ++k)
+			for (int64_t i = 0; i < x.dims[k]; ++i, ++col) hu[uoff[k] + size_t(i) * N + s] = vectors[size_t(s) * sum_n + col];
+	}
+	double* U = c.scratch<double>(S_ADF_FIRST + 13, hu.size());
+	double* y = c.scratch<double>(S_ADF_FIRST + 1, N);
+	double* res = c.scratch<double>(S_ADF_FIRST + 2, N);
+	XTT_CUDA(cudaMemcpyAsync(U, hu.data(), hu.size() * sizeof(double), cudaMemcpyHostToDevice, c.stream));
+	XTT_CUDA(cudaMemcpyAsync(y, values, N * sizeof(double), cudaMemcpyHostToDevice, c.stream));
+	size_t fo = 0, bo = 0;
+	for (int k = 0; k < d; ++k) {
+		fo += size_t(x.ranks[k + 1]) * N;
+		bo += size_t(x.ranks[k]) * N;
+	}
+	double* Fa = c.scratch<double>(S_ADF_FIRST + 8, fo);
+	double* Ba = c.scratch<double>(S_ADF_FIRST + 9, bo);
+	std::vector<double*> F(d), B(d);
+	fo = bo = 0;
+	for (int k = 0; k < d; ++k) {
+		F[k] = Fa + fo;
+		B[k] = Ba + bo;
+		fo += size_t(x.ranks[k + 1]) * N;
+		bo += size_t(x.ranks[k]) * N;
+	}
+	const long long chunk = 64, res_blocks = std::max<long long>(1, (N + chunk * kR1Warps - 1) / (chunk * kR1Warps));
+	const long long norm_chunk = 1024, norm_blocks = std::max<long long>(1, (N + norm_chunk - 1) / norm_chunk);
+	double* gpart = c.scratch<double>(S_ADF_FIRST + 3, size_t(res_blocks) * maxr * maxn * maxr);
+	double* npart = c.scratch<double>(S_ADF_FIRST + 4, size_t(norm_blocks));
+	double* rrpart = c.scratch<double>(S_ADF_FIRST + 5, size_t(res_blocks));
+	double* G = c.scratch<double>(S_ADF_FIRST + 6, size_t(maxr) * maxn * maxr);
+	double* nrm = c.scratch<double>(S_ADF_FIRST + 7, 2);
+	double* rr = nrm + 1;
+	auto level = [&](int k, const double* X) {
+		R1Level L;
+		L.U = U + uoff[k];
+		L.F = k > 0 ? F[k - 1] : nullptr;
+		L.B = k + 1 < d ? B[k + 1] : nullptr;
+		L.X = X;
+		L.r0 = int(x.ranks[k]);
+		L.n = int(x.dims[k]);
+		L.r1 = int(x.ranks[k + 1]);
+		L.N = N;
+		return L;
+	};
+	const unsigned sbl = unsigned(std::max<long long>(1, std::min<long long>((N + 255) / 256, (long long)c.num_sms * 8)));
+	auto backward = [&](int k) {
+		const R1Level L = level(k, x.core[k]);
+		ProfScope ps(c, "adf_stack");
+		k_r1_backward<<<sbl, 256, size_t(L.r0) * L.n * L.r1 * sizeof(double), c.stream>>>(L, B[k]);
+		XTT_CUDA(cudaGetLastError());
+		c.count_launch();
+	};
+	auto forward = [&](int k) {
+		const R1Level L = level(k, x.core[k]);
+		ProfScope ps(c, "adf_stack");
+		k_r1_forward<<<sbl, 256, size_t(L.r0) * L.n * L.r1 * sizeof(double), c.stream>>>(L, F[k]);
+		XTT_CUDA(cudaGetLastError());
+		c.count_launch();
+	};
+	static bool attr = false;
+	if (!attr) {
+		XTT_CUDA(cudaFuncSetAttribute(k_r1_res_grad, cudaFuncAttributeMaxDynamicSharedMemorySize, 100 * 1024));
+		attr = true;
+	}
+	auto res_grad = [&](int k) {
+		const R1Level L = level(k, x.core[k]);
+		const int P = L.r0 * L.r1, len = L.r0 * L.n * L.r1;
+		const size_t smem = (size_t(len) + size_t(kR1Warps) * (L.r0 + L.r1 + L.n) * 33 + size_t(kR1Warps) * L.n * P) *
+		                    sizeof(double);
+		ProfScope ps(c, "adf_res_grad");
+		k_r1_res_grad<<<unsigned(res_blocks), kR1Threads, smem, c.stream>>>(L, y, res, gpart, rrpart, chunk);
+		XTT_CUDA(cudaGetLastError());
+		c.count_launch();
+		sum_parts(c, gpart, res_blocks, len, G, 1.0);
+		sum_parts(c, rrpart, res_blocks, 1, rr, 1.0);
+	};
+	AdfResult out;
+	double residual_norm = DBL_MAX, last_residual_norm = DBL_MAX;
+	double dec1 = 0, dec2 = 0, dec3 = 0;
+	for (int64_t it = 0; max_iter == 0 || it < max_iter; ++it) {
+		move_core(x, 0, true);
+		for (int k = d - 1; k > 0; --k) backward(k);
+		res_grad(0);
+		XTT_CUDA(cudaMemcpyAsync(c.h_dbl + 30, rr, sizeof(double), cudaMemcpyDeviceToHost, c.stream));
+		c.sync();
+		last_residual_norm = residual_norm;
+		residual_norm = std::sqrt(c.h_dbl[30]) / norm_y;
+		out.trace.push_back(residual_norm);
+		const double dec4 = dec3;
+		dec3 = dec2;
+		dec2 = dec1;
+		dec1 = residual_norm / last_residual_norm;
+		if (residual_norm < target || dec1 * dec2 * dec3 * dec4 > std::pow(min_dec, 4)) break;
+		for (int k = 0; k < d; ++k) {
+			if (k > 0) res_grad(k);
+			{
+				const R1Level L = level(k, x.core[k]);
+				ProfScope ps(c, "adf_slicenorm");
+				k_r1_norm<<<unsigned(norm_blocks), kR1Threads, 0, c.stream>>>(L, G, npart, norm_chunk);
+				XTT_CUDA(cudaGetLastError());
+				c.count_launch();
+				sum_parts(c, npart, norm_blocks, 1, nrm, 1.0);
+			}
+			k_r1_update<<<1, 128, 0, c.stream>>>(x.core[k], G, nrm, int(x.core_size(k)));
+			XTT_CUDA(cudaGetLastError());
+			c.count_launch();
+			if (k + 1 < d) {
+				move_core(x, k + 1, true);
+				forward(k);
+			}
+		}
+	}
+	out.residual = residual_norm;
+	out.checked_residual = residual_norm;
+	return out;
+}
+
 double adf_gradient(const Tensor& xc, const int64_t* positions, const double* values, long long N,
                     std::vector<double>& grad) {
 	// loss 0.5 ||P(x) - y||^2 and d loss / d X_k = -sum_s res_s F_{k-1}[s] (x) e_{i_s} (x) B_{k+1}[s]

@@ -684,6 +684,59 @@ int xtt_adf(xtt_tensor* x, const int64_t* positions, const double* values, int64
 	});
 }
 
+int xtt_random_rank_one(int64_t num, int64_t order, const int64_t* dims, double* out) {
+	return guard([&] {
+		ARG(dims && (out || num == 0) && order > 0, "NULL argument");
+		double total = 1;
+		int64_t sum_n = 0;
+		for (int64_t k = 0; k < order; ++k) {
+			ARG(dims[k] > 0, "dimension 0 is not valid");
+			total *= double(dims[k]);
+			sum_n += dims[k];
+		}
+		ARG(total >= double(num), "It's impossible to perform as many measurements as requested.");
+		// RankOneMeasurementSet::create_random_positions (measurments.cpp:522-544): a
+		// Tensor::random({n}) per sample and mode from the default normal distribution, then
+		// sort(true) with internal::comp (measurments.cpp:330-347, 549-...): mode by mode,
+		// entry by entry, the larger value first
+		auto& dist = dist_for(0.0, 1.0);
+		std::vector<std::vector<double>> rows(static_cast<size_t>(num), std::vector<double>(static_cast<size_t>(sum_n)));
+		for (auto& r : rows)
+			for (auto& v : r) v = dist(g_engine);
+		std::stable_sort(rows.begin(), rows.end(), [](const std::vector<double>& a, const std::vector<double>& b) {
+			for (size_t i = 0; i < a.size(); ++i) {
+				if (a[i] > b[i]) return true;
+				if (a[i] < b[i]) return false;
+			}
+			return false;
+		});
+		for (int64_t s = 0; s < num; ++s) std::copy(rows[s].begin(), rows[s].end(), out + s * sum_n);
+	});
+}
+
+int xtt_entries_rank_one(const xtt_tensor* x, const double* vectors, int64_t count, double* out) {
+	return guard([&] {
+		ARG(x && (count == 0 || (vectors && out)), "NULL argument");
+		xtt::entries_rank_one(*x->t, vectors, count, out);
+	});
+}
+
+int xtt_adf_rank_one(xtt_tensor* x, const double* vectors, const double* values, int64_t num,
+                     const xtt_adf_options* opt, double* final_residual, double* residual_trace,
+                     int64_t trace_capacity, int64_t* trace_count) {
+	return guard([&] {
+		ARG(x && vectors && values && opt, "NULL argument");
+		ARG(opt->precision == XTT_PRECISION_FP64, "rank-one ADF runs in FP64");
+		xtt::AdfResult r = xtt::adf_rank_one(*x->t, vectors, values, num, opt->max_iterations, opt->target_residual,
+		                                     opt->min_decrease);
+		x->t->ctx->sync();
+		if (final_residual) *final_residual = r.checked_residual;
+		if (residual_trace)
+			for (size_t i = 0; i < r.trace.size() && int64_t(i) < trace_capacity; ++i) residual_trace[i] = r.trace[i];
+		if (trace_count) *trace_count = int64_t(r.trace.size());
+	});
+}
+
 int xtt_adf_gradient(const xtt_tensor* x, const int64_t* positions, const double* values, int64_t num, double* loss,
                      double* grad, int64_t count) {
 	return guard([&] {

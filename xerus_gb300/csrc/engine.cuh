@@ -200,6 +200,12 @@ struct AdfResult {
 // per-sample arithmetic with FP64 cores, QR and final check.
 AdfResult adf(Tensor& x, const int64_t* positions, const double* values, long long N, int64_t max_iter, double target,
               double min_dec, int precision = XTT_PRECISION_FP64);
+// ADF on rank-one measurements (RankOneMeasurementSet): vectors holds, per sample, the
+// concatenated vectors u_1 .. u_d (N x sum n_k, row-major). FP64.
+AdfResult adf_rank_one(Tensor& x, const double* vectors, const double* values, long long N, int64_t max_iter,
+                       double target, double min_dec);
+// RankOneMeasurementSet::measure(TensorNetwork): <x, u_1 (x) ... (x) u_d> per sample.
+void entries_rank_one(const Tensor& x, const double* vectors, int64_t count, double* out);
 double adf_gradient(const Tensor& x, const int64_t* positions, const double* values, long long N,
                     std::vector<double>& grad);
 

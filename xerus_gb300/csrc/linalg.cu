@@ -916,7 +916,7 @@ struct Qc1Layout {
 	__host__ __device__ size_t tot() const { return red() + 2 * size_t(S); }
 	__host__ __device__ size_t tau() const { return tot() + size_t(S); }
 	__host__ __device__ size_t part() const { return tau() + kq; }
-	// column pivoting: partial column norms (vn1, vn2 of dlaqp2), this CTA's partial squared
+	// column pivoting: squared partial column norms (vn1^2, vn2^2 of dlaqp2), this CTA's partial squared
 	// norms for exact (re)computation, R's diagonal, the permutation and recompute flags (ints)
 	__host__ __device__ size_t vn1() const { return part() + 8 * 256; }
 	__host__ __device__ size_t vn2() const { return vn1() + nw; }
@@ -980,7 +980,8 @@ __global__ void __launch_bounds__(kQ1Threads) k_qr_cl1(QrArgs a, Qc1Layout lay) 
 		}
 		__syncthreads();
 	};
-	// the first column of largest vn1 in [c0, nw) (idamax order), swapped into column c0
+	// the first column of largest vn1 in [c0, nw) (idamax order; vn1 holds squares, same order),
+	// swapped into column c0
 	auto pivot_into = [&](int c0) {
 		double best = -1.0;
 		int bi = nw;
@@ -1016,7 +1017,7 @@ __global__ void __launch_bounds__(kQ1Threads) k_qr_cl1(QrArgs a, Qc1Layout lay) 
 	};
 	if (a.pivot) {
 		for (int c = tid; c < nw; c += kQ1Threads) perm[c] = c;
-		exact_norms(0, 0, [](int) { return true; }, [&](int c, double t) { vn1[c] = vn2[c] = sqrt(t); });
+		exact_norms(0, 0, [](int) { return true; }, [&](int c, double t) { vn1[c] = vn2[c] = t; });
 		pivot_into(0);
 	}
 
@@ -1046,10 +1047,16 @@ __global__ void __launch_bounds__(kQ1Threads) k_qr_cl1(QrArgs a, Qc1Layout lay) 
 	};
 	// cluster totals into tot[], rank order: fields 0, 1 (if head), then [2 + c0, 2 + c0 + C)
 	// and, if head, [2 + nw + c0, 2 + nw + c0 + C)
+	// (alpha and E_c are nonzero only in the CTA owning the diagonal row: read there, not summed)
 	auto gather = [&](int par, bool head, int c0, int C) {
 		const int nv = head ? 2 + 2 * C : C;
+		const int owner = min((c0 - 1) / mb, P - 1);
 		for (int v = tid; v < nv; v += kQ1Threads) {
 			const int f = !head ? 2 + c0 + v : v < 2 ? v : v < 2 + C ? 2 + c0 + (v - 2) : 2 + nw + c0 + (v - 2 - C);
+			if (head && (f == 1 || f >= 2 + nw)) {
+				tot[f] = cl.map_shared_rank(red, owner)[par * S + f];
+				continue;
+			}
 			double a0 = 0, a1 = 0, a2 = 0, a3 = 0;
 			int q = 0;
 			for (; q + 3 < P; q += 4) {
@@ -1074,6 +1081,10 @@ __global__ void __launch_bounds__(kQ1Threads) k_qr_cl1(QrArgs a, Qc1Layout lay) 
 		double beta, tt, scal;
 		reflector_scalars(tot[1], tot[0], beta, tt, scal);
 		if (tid == 0) tau[j] = tt;
+		// the reflector below the diagonal (v = x scal) and R_jj
+		for (int il = lo_of(j + 1) + tid; il < nl; il += kQ1Threads) w(il, j) *= scal;
+		if (tid == 0 && j >= r0 && j < r1) w(j - r0, j) = beta;
+		__syncthreads();
 		// trailing columns, rows >= j: a_c -= tau (E_c + scal D_c) v, v = [1; x scal]
 		const int lo = lo_of(j), nrows = nl - lo;
 		for (int cb = 0; cb < C; cb += 256) {
@@ -1082,17 +1093,17 @@ __global__ void __launch_bounds__(kQ1Threads) k_qr_cl1(QrArgs a, Qc1Layout lay) 
 			if (g < cm.G && ci < cm.Cc) {
 				const int c = c0 + cb + ci, ia = lo + g * chunk, ib = min(nl, ia + chunk);
 				const double wc = tt * fma(scal, tot[2 + c], tot[2 + nw + c]);
-				for (int il = ia; il < ib; ++il) {
-					const double v = (r0 + il == j) ? 1.0 : w(il, j) * scal;
-					w(il, c) = fma(-wc, v, w(il, c));
-				}
+				for (int il = ia; il < ib; ++il) w(il, c) = fma(-wc, (r0 + il == j) ? 1.0 : w(il, j), w(il, c));
 			}
 		}
 		__syncthreads();
 		if (tid == 0) betas[j] = beta;
 		if (a.pivot && j + 1 < kq) {
 			// downdate the partial norms with the new row j (R_jc = E_c - wc), recomputing
-			// them exactly where the downdate lost accuracy (dlaqp2, tol3z = sqrt(eps))
+			// them exactly where the downdate lost accuracy (dlaqp2, tol3z = sqrt(eps)). The
+			// norms are kept squared: dlaqp2's test temp (vn1/vn2)^2 <= tol3z with
+			// temp = 1 - (R_jc/vn1)^2 is (vn1^2 - R_jc^2) / vn2^2 <= tol3z, and its update
+			// vn1 sqrt(temp) is sqrt(vn1^2 - R_jc^2): no division or square root per column.
 			if (tid == 0) flag[nw] = 0;
 			__syncthreads();
 			const double tol3z = sqrt(DBL_EPSILON / 2);
@@ -1101,26 +1112,22 @@ __global__ void __launch_bounds__(kQ1Threads) k_qr_cl1(QrArgs a, Qc1Layout lay) 
 				if (vn1[c] != 0.0) {
 					const double e = tot[2 + nw + c];
 					const double rjc = e - tt * fma(scal, tot[2 + c], e);
-					const double q = fabs(rjc) / vn1[c];
-					const double temp = fmax(0.0, 1.0 - q * q);
-					const double r = vn1[c] / vn2[c];
-					if (temp * r * r <= tol3z) {
+					const double nsq = fmax(0.0, fma(-rjc, rjc, vn1[c]));
+					if (nsq <= tol3z * vn2[c]) {
 						flag[c] = 1;
 						flag[nw] = 1;
 					} else {
-						vn1[c] *= sqrt(temp);
+						vn1[c] = nsq;
 					}
 				}
 			}
 			__syncthreads();
 			if (flag[nw])
 				exact_norms(c0, j + 1, [&](int c) { return flag[c] != 0; },
-				            [&](int c, double t) { vn1[c] = vn2[c] = sqrt(t); });
+				            [&](int c, double t) { vn1[c] = vn2[c] = t; });
 			pivot_into(c0);
 		}
-		// the reflector below the diagonal, R_jj; then the next step's partials (columns > j)
-		for (int il = lo_of(j + 1) + tid; il < nl; il += kQ1Threads) w(il, j) *= scal;
-		if (tid == 0 && j >= r0 && j < r1) w(j - r0, j) = beta;
+		// the next step's partials (columns > j)
 		if (j + 1 < kq) publish(j + 1);
 	}
 	__syncthreads();

@@ -1028,6 +1028,67 @@ __global__ void k_entries(const double* const* cores, const int64_t* ranks, cons
 	}
 }
 
+// One block per sample: v <- v * sum_i u_k[i] x_k[:, i, :] (RankOneMeasurementSet::measure,
+// src/xerus/measurments.cpp:397-...); u holds each sample's concatenated vectors (row stride su).
+__global__ void k_entries_r1(const double* const* cores, const int64_t* ranks, const int64_t* dims, int d,
+                             const double* u, long long su, int64_t count, double* out, int maxr) {
+	extern __shared__ double buf[];
+	double* v = buf;
+	double* w = buf + maxr;
+	for (int64_t s = blockIdx.x; s < count; s += gridDim.x) {
+		if (threadIdx.x == 0) v[0] = 1.0;
+		__syncthreads();
+		const double* us = u + s * su;
+		for (int k = 0; k < d; ++k) {
+			const int r0 = int(ranks[k]), r1 = int(ranks[k + 1]), n = int(dims[k]);
+			const double* c = cores[k];
+			for (int b = threadIdx.x; b < r1; b += blockDim.x) {
+				double acc = 0;
+				for (int a = 0; a < r0; ++a) {
+					double t = 0;
+					for (int i = 0; i < n; ++i) t = fma(us[i], c[(size_t(a) * n + i) * r1 + b], t);
+					acc = fma(v[a], t, acc);
+				}
+				w[b] = acc;
+			}
+			__syncthreads();
+			for (int b = threadIdx.x; b < r1; b += blockDim.x) v[b] = w[b];
+			__syncthreads();
+			us += n;
+		}
+		if (threadIdx.x == 0) out[s] = v[0];
+		__syncthreads();
+	}
+}
+
+void entries_rank_one(const Tensor& x, const double* vectors, int64_t count, double* out) {
+	XTT_REQUIRE(!x.op, "measurements of a TT operator are not supported");
+	Context& c = *x.ctx;
+	if (count == 0) return;
+	int64_t maxr = 1, su = 0;
+	for (auto r : x.ranks) maxr = std::max(maxr, r);
+	for (auto n : x.dims) su += n;
+	const size_t meta = size_t(x.d) * 2 + 1;
+	int64_t* dmeta = c.scratch<int64_t>(S_ENT_META, meta);
+	std::vector<int64_t> hm(meta);
+	for (int k = 0; k < x.d; ++k) hm[k] = x.dims[k];
+	for (int k = 0; k <= x.d; ++k) hm[x.d + k] = x.ranks[k];
+	double** dcores = c.scratch<double*>(S_ENT_CORES, x.d);
+	std::vector<double*> hc(x.core.begin(), x.core.end());
+	double* du = c.scratch<double>(S_ADF_FIRST + 14, size_t(count) * su);
+	double* dout = c.scratch<double>(S_ENT_OUT, count);
+	XTT_CUDA(cudaMemcpyAsync(dmeta, hm.data(), hm.size() * sizeof(int64_t), cudaMemcpyHostToDevice, c.stream));
+	XTT_CUDA(cudaMemcpyAsync(dcores, hc.data(), hc.size() * sizeof(double*), cudaMemcpyHostToDevice, c.stream));
+	XTT_CUDA(cudaMemcpyAsync(du, vectors, sizeof(double) * count * su, cudaMemcpyHostToDevice, c.stream));
+	const unsigned blocks = unsigned(std::min<int64_t>(count, 8192));
+	k_entries_r1<<<blocks, 128, 2 * maxr * sizeof(double), c.stream>>>(dcores, dmeta + x.d, dmeta, x.d, du, su, count,
+	                                                                    dout, int(maxr));
+	XTT_CUDA(cudaGetLastError());
+	c.count_launch();
+	XTT_CUDA(cudaMemcpyAsync(out, dout, sizeof(double) * count, cudaMemcpyDeviceToHost, c.stream));
+	c.sync();
+}
+
 void entries(const Tensor& x, const int64_t* positions, int64_t count, double* out) {
 	XTT_REQUIRE(!x.op, "entries of a TT operator are not supported");
 	Context& c = *x.ctx;
