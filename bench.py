@@ -46,6 +46,7 @@ def parse():
     p.add_argument("--batch-count", type=int, default=4096)
     p.add_argument("--only", choices=["round", "adf", "batch", "dmrg"],
                    help="run one secondary workload alone and print its JSON (for profiling)")
+    p.add_argument("--adf-iterations", type=int, default=50, help="ADF iterations per timed run")
     return p.parse_args()
 
 
@@ -455,7 +456,7 @@ def run_gpu(args):
         cpu = not args.no_cpu_baseline
         wl = {}
         wl["round_dot_d32_r64"] = bench_round_dot(xg, ctx, torch, stream, 3, cpu)
-        wl["adf_d10_n8_r6_200k"] = bench_adf(xg, ctx, torch, stream, 50, peak, cpu)
+        wl["adf_d10_n8_r6_200k"] = bench_adf(xg, ctx, torch, stream, args.adf_iterations, peak, cpu)
         wl["batch_als_cfg4"] = bench_batch(xg, ctx, args.batch_count, 2)
         line["workloads"] = wl
     return line
@@ -553,7 +554,7 @@ def run_only(args):
     if args.only == "round":
         return bench_round_dot(xg, ctx, torch, stream, args.steps, cpu)
     if args.only == "adf":
-        return bench_adf(xg, ctx, torch, stream, 50, peaks.get("hbm_gbs", 6800.0), cpu)
+        return bench_adf(xg, ctx, torch, stream, args.adf_iterations, peaks.get("hbm_gbs", 6800.0), cpu)
     if args.only == "batch":
         return bench_batch(xg, ctx, args.batch_count, args.steps)
     return bench_dmrg(xg, ctx, torch, stream, 2)

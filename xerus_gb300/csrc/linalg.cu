@@ -923,10 +923,16 @@ struct Qc1Layout {
 	__host__ __device__ size_t rec() const { return vn2() + nw; }
 	__host__ __device__ size_t beta() const { return rec() + nw; }
 	__host__ __device__ size_t ints() const { return beta() + kq; }
-	__host__ __device__ size_t total() const { return ints() + size_t(nw) + 2; }
+	// Q by the compact WY form (wy = 1): the Gram totals of the reflectors (strict upper
+	// part), V's top kq x kq block, and V T for this CTA's rows
+	int wy;
+	__host__ __device__ size_t gram() const { return ints() + size_t(nw) + 2; }
+	__host__ __device__ size_t vt() const { return gram() + (wy ? size_t(kq) * (kq - 1) / 2 : 0); }
+	__host__ __device__ size_t wr() const { return vt() + (wy ? size_t(kq) * kq : 0); }
+	__host__ __device__ size_t total() const { return wr() + (wy ? size_t(mb) * kq : 0); }
 };
 
-__global__ void __launch_bounds__(kQ1Threads) k_qr_cl1(QrArgs a, Qc1Layout lay) {
+__global__ void __launch_bounds__(kQ1Threads, 1) k_qr_cl1(QrArgs a, Qc1Layout lay) {
 	namespace cg = cooperative_groups;
 	cg::cluster_group cl = cg::this_cluster();
 	const int P = lay.P, me = int(cl.block_rank());
@@ -1146,6 +1152,91 @@ __global__ void __launch_bounds__(kQ1Threads) k_qr_cl1(QrArgs a, Qc1Layout lay) 
 	}
 	cl.sync();  // every CTA has read the last partials before they are rewritten or freed
 	if (!a.want_q) return;
+	if (lay.wy) {
+		// Q = [I; 0] - V T V_top^T with the UT transform T^{-1} = diag(1/tau) + striu(V^T V)
+		// (Joffrain, Low, Quintana-Orti, van de Geijn, Van Zee, "Accumulating Householder
+		// transformations, revisited", 2006): one Gram reduction over the cluster and
+		// CTA-local triangular work replace the reflector-by-reflector accumulation.
+		const int n = rank, np = n * (n - 1) / 2;
+		double* gt = sm + lay.gram();
+		double* vt = sm + lay.vt();
+		double* wr = sm + lay.wr();
+		auto vv = [&](int il, int j) -> double {
+			const int gi = r0 + il;
+			return gi == j ? 1.0 : (gi > j ? w(il, j) : 0.0);
+		};
+		// this CTA's partial Gram of the reflectors, pair p = j (j - 1) / 2 + l for l < j
+		for (int p = tid; p < np; p += kQ1Threads) {
+			int j = int((1.0f + sqrtf(1.0f + 8.0f * float(p))) * 0.5f);
+			while (j * (j - 1) / 2 > p) --j;
+			while ((j + 1) * j / 2 <= p) ++j;
+			const int l = p - j * (j - 1) / 2;
+			double a0 = 0, a1 = 0;
+			int il = lo_of(j);
+			for (; il + 1 < nl; il += 2) {
+				a0 = fma(vv(il, l), vv(il, j), a0);
+				a1 = fma(vv(il + 1, l), vv(il + 1, j), a1);
+			}
+			if (il < nl) a0 = fma(vv(il, l), vv(il, j), a0);
+			part[p] = a0 + a1;
+		}
+		__syncthreads();
+		cl.sync();
+		// totals of this CTA's share of the pairs (rank order), and V's top block from its owners
+		const int bs = (np + P - 1) / P, p0 = me * bs, p1 = min(np, p0 + bs);
+		for (int p = p0 + tid; p < p1; p += kQ1Threads) {
+			double t0 = 0, t1 = 0;
+			int q = 0;
+			for (; q + 1 < P; q += 2) {
+				t0 += cl.map_shared_rank(part, q)[p];
+				t1 += cl.map_shared_rank(part, q + 1)[p];
+			}
+			if (q < P) t0 += cl.map_shared_rank(part, q)[p];
+			gt[p] = t0 + t1;
+		}
+		for (int e = tid; e < n * n; e += kQ1Threads) {
+			const int c = e / n, j = e - c * n;
+			double v = c == j ? 1.0 : 0.0;
+			if (c > j) {
+				const int ow = c / mb;
+				v = cl.map_shared_rank(W, ow)[(long long)(c - ow * mb) * ldw + j];
+			}
+			vt[e] = v;
+		}
+		__syncthreads();
+		cl.sync();
+		// the other CTAs' shares of the Gram totals
+		for (int p = tid; p < np; p += kQ1Threads)
+			if (p < p0 || p >= p1) gt[p] = cl.map_shared_rank(gt, min(p / bs, P - 1))[p];
+		// wr = V_rows T: forward substitution on wr T^{-1} = V_rows, column by column
+		for (int e = tid; e < nl * n; e += kQ1Threads) {
+			const int il = e / n, j = e - il * n;
+			wr[e] = j == 0 ? tau[0] * vv(il, 0) : vv(il, j);
+		}
+		__syncthreads();
+		for (int j = 0; j + 1 < n; ++j) {
+			const int m = n - j - 1;
+			for (int e = tid; e < nl * m; e += kQ1Threads) {
+				const int il = e / m, l = j + 1 + (e - il * m);
+				const double t = fma(-wr[il * n + j], gt[l * (l - 1) / 2 + j], wr[il * n + l]);
+				wr[il * n + l] = l == j + 1 ? tau[l] * t : t;
+			}
+			__syncthreads();
+		}
+		// Q_rows = E_rows - wr V_top^T (V_top unit lower triangular)
+		for (int e = tid; e < nl * n; e += kQ1Threads) {
+			const int il = e / n, c = e - il * n;
+			double a0 = 0, a1 = 0;
+			int j = 0;
+			for (; j + 1 <= c; j += 2) {
+				a0 = fma(wr[il * n + j], vt[c * n + j], a0);
+				a1 = fma(wr[il * n + j + 1], vt[c * n + j + 1], a1);
+			}
+			if (j <= c) a0 = fma(wr[il * n + j], vt[c * n + j], a0);
+			w(il, c) = (r0 + il == c ? 1.0 : 0.0) - (a0 + a1);
+		}
+		__syncthreads();
+	} else {
 	// Q in place, backward accumulation of the reflectors (dorg2r)
 	for (int j = rank - 1; j >= 0; --j) {
 		const double tj = tau[j];
@@ -1190,16 +1281,17 @@ __global__ void __launch_bounds__(kQ1Threads) k_qr_cl1(QrArgs a, Qc1Layout lay) 
 		}
 		__syncthreads();
 	}
+	}
 	for (long long e = tid; e < (long long)nl * rank; e += kQ1Threads) {
 		const int il = int(e / rank), c = int(e % rank), gi = r0 + il;
 		const double v = w(il, c);
 		if (!a.transpose) a.Q[(long long)gi * rank + c] = v;
 		else a.Q[(long long)c * mw + gi] = v;
 	}
-	cl.sync();  // every CTA's partials stay alive until the last remote reads are done
+	cl.sync();  // every CTA's shared memory stays alive until the last remote reads are done
 }
 
-static int qr_cl1_size(int mw, int nw, Qc1Layout& lay) {
+static int qr_cl1_size(int mw, int nw, bool want_q, Qc1Layout& lay) {
 	if (mw < 48 || nw < 8) return 0;
 	int P = std::min(16, (mw + 15) / 16);
 	lay.mb = (mw + P - 1) / P;
@@ -1209,6 +1301,8 @@ static int qr_cl1_size(int mw, int nw, Qc1Layout& lay) {
 	lay.kq = std::min(mw, nw);
 	lay.ldw = nw | 1;
 	lay.S = 2 + 2 * nw;
+	lay.wy = want_q && lay.kq <= 64 ? 1 : 0;  // the partial Gram fits the 2048-entry `part` region
+	if (lay.wy && lay.total() * sizeof(double) > kDynSmemMax) lay.wy = 0;
 	if (lay.total() * sizeof(double) > kDynSmemMax) return 0;
 	return P;
 }
@@ -1328,7 +1422,7 @@ void launch_qr(const QrArgs& a, cudaStream_t s) {
 	}
 	{
 		Qc1Layout l1;
-		const int P1 = qr_cl1_size(mw, nw, l1);
+		const int P1 = qr_cl1_size(mw, nw, a.want_q != 0, l1);
 		if (P1 > 1) {
 			static bool attr1 = false;
 			if (!attr1) {
