@@ -172,12 +172,21 @@ __device__ CgOut cg_body(const CgParams<T>& a, GemmSmem<T>& sm, Grp& grp) {
 		if (!matvec_dev(a.plan, a.p, a.q, a.p, sm, grp, blk)) return out;
 		const double pAp = grp.total(double(blk), ok);
 		if (!ok) return out;
-		if (!(pAp > 0.0) || !isfinite(pAp)) {
+		// the test and the division once per CTA (in every thread they would queue on the
+		// FP64 pipe), broadcast through shared memory
+		__shared__ double s_ab[2];
+		__shared__ int s_good;
+		if (threadIdx.x == 0) {
+			s_good = pAp > 0.0 && isfinite(pAp);
+			s_ab[0] = s_good ? rr / pAp : 0.0;
+		}
+		__syncthreads();
+		if (!s_good) {
 			// an FP32 correction solve just stops: the FP64 refinement around it decides
 			if (sizeof(T) == 8 && cg_breakdown_is_error(rr, bb)) grp.record(DEV_BREAKDOWN);
 			break;
 		}
-		const double alpha = rr / pAp;
+		const double alpha = s_ab[0];
 		double l = 0;
 		for (long long i = gt; i < a.n; i += gs) {
 			a.x[i] += T(alpha) * a.p[i];
@@ -188,7 +197,9 @@ __device__ CgOut cg_body(const CgParams<T>& a, GemmSmem<T>& sm, Grp& grp) {
 		l = block_sum(l, sc);
 		const double rrn = grp.total(l, ok);
 		if (!ok) return out;
-		const double beta = rrn / rr;
+		if (threadIdx.x == 0) s_ab[1] = rrn / rr;
+		__syncthreads();
+		const double beta = s_ab[1];
 		rr = rrn;
 		for (long long i = gt; i < a.n; i += gs) a.p[i] = a.r[i] + T(beta) * a.p[i];
 		if (!grp.sync()) return out;
@@ -270,10 +281,10 @@ __global__ void __launch_bounds__(kGemmThreads) k_cg_mixed(MixedParams a, Grp gr
 			break;
 		}
 		if (ref == a.max_refine) break;
-		const double nr = sqrt(rr);
+		const double nr = sqrt(rr), inr = 1.0 / nr;
 		rr_prev = rr;
 		nr_prev = nr;
-		for (long long i = gt; i < a.n; i += gs) const_cast<float*>(a.inner.b)[i] = float(a.q64[i] / nr);
+		for (long long i = gt; i < a.n; i += gs) const_cast<float*>(a.inner.b)[i] = float(a.q64[i] * inr);
 		if (!grp.sync()) break;
 		const CgOut o = cg_body(a.inner, sm.f, grp);
 		iters += o.iterations;

@@ -238,11 +238,19 @@ struct BInstance {
 		while (bb > 0 && rr > tol2 && it < maxit) {
 			cc_matvec(s, s.rb, mp, q);
 			const double pAp = dot(p, q, n);
-			if (!(pAp > 0.0) || !isfinite(pAp)) {
+			// the test and the division once per CTA (FP64 pipe), broadcast through shared memory
+			__shared__ double s_ab[2];
+			__shared__ int s_good;
+			if (threadIdx.x == 0) {
+				s_good = pAp > 0.0 && isfinite(pAp);
+				s_ab[0] = s_good ? rr / pAp : 0.0;
+			}
+			__syncthreads();
+			if (!s_good) {
 				if (threadIdx.x == 0 && cg_breakdown_is_error(rr, bb)) record_status(a.status, DEV_BREAKDOWN);
 				break;
 			}
-			const double alpha = rr / pAp;
+			const double alpha = s_ab[0];
 			double l = 0;
 			for (long long e = threadIdx.x; e < n; e += blockDim.x) {
 				x[e] = fma(alpha, p[e], x[e]);
@@ -251,7 +259,9 @@ struct BInstance {
 				l = fma(v, v, l);
 			}
 			const double rrn = block_sum(l, sh.red);
-			const double beta = rrn / rr;
+			if (threadIdx.x == 0) s_ab[1] = rrn / rr;
+			__syncthreads();
+			const double beta = s_ab[1];
 			rr = rrn;
 			for (long long e = threadIdx.x; e < n; e += blockDim.x) p[e] = fma(beta, p[e], r[e]);
 			__syncthreads();
@@ -299,12 +309,12 @@ struct BInstance {
 				break;
 			}
 			if (ref == a.max_refine) break;
-			const double nr = sqrt(rr64);
+			const double nr = sqrt(rr64), inr = 1.0 / nr;
 			rr_prev = rr64;
 			nr_prev = nr;
 			float bl = 0;
 			for (long long e = threadIdx.x; e < n; e += blockDim.x) {
-				const float v = float(q[e] / nr);
+				const float v = float(q[e] * inr);
 				bf[e] = v;
 				xf[e] = 0.f;
 				rf[e] = v;

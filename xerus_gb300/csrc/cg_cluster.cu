@@ -180,6 +180,8 @@ __device__ int cc_cg(const CcShape& s, int me, int P, int b0, int bwl, const Mv<
                      double& rel) {
 	const int tid = threadIdx.x, n = s.M1() * bwl, M1 = s.M1(), ldp = s.ldp();
 	__shared__ T sc[32];
+	__shared__ T s_ab[2];
+	__shared__ bool s_ok;
 	if (zero_guess) {
 		for (int e = tid; e < n; e += blockDim.x) {
 			x[e] = T(0);
@@ -230,13 +232,29 @@ __device__ int cc_cg(const CcShape& s, int me, int P, int b0, int bwl, const Mv<
 		T l = 0;
 		for (int e = tid; e < n; e += blockDim.x) l = fma(p[e], q[e], l);
 		const T pAp = cc_total(block_sum(l, sc), s_pap, bcast, me, P);
-		if (!(pAp > T(0)) || !isfinite(double(pAp))) {
+		T alpha;
+		bool ok;
+		if (sizeof(T) == 8) {
+			// FP64: the test and the division once per CTA (redundant copies in every thread
+			// would queue on GB300's FP64 pipe), broadcast through shared memory
+			if (tid == 0) {
+				const bool good = pAp > T(0) && isfinite(double(pAp));
+				s_ab[0] = good ? rr / pAp : T(0);
+				s_ok = good;
+			}
+			__syncthreads();
+			alpha = s_ab[0];
+			ok = s_ok;
+		} else {
+			ok = pAp > T(0) && isfinite(double(pAp));
+			alpha = ok ? rr / pAp : T(0);
+		}
+		if (!ok) {
 			// an FP32 correction solve just stops: the FP64 refinement around it decides
 			if (sizeof(T) == 8 && tid == 0 && me == 0 && cg_breakdown_is_error(double(rr), double(bb)))
 				record_status(status, DEV_BREAKDOWN);
 			break;
 		}
-		const T alpha = rr / pAp;
 		l = 0;
 		for (int e = tid; e < n; e += blockDim.x) {
 			x[e] = fma(alpha, p[e], x[e]);
@@ -245,7 +263,14 @@ __device__ int cc_cg(const CcShape& s, int me, int P, int b0, int bwl, const Mv<
 			l = fma(v, v, l);
 		}
 		const T rrn = cc_total(block_sum(l, sc), s_rr, bcast, me, P);
-		const T beta = rrn / rr;
+		T beta;
+		if (sizeof(T) == 8) {
+			if (tid == 0) s_ab[1] = rrn / rr;
+			__syncthreads();
+			beta = s_ab[1];
+		} else {
+			beta = rrn / rr;
+		}
 		rr = rrn;
 		for (int e = tid; e < n; e += blockDim.x) p[e] = fma(beta, p[e], r[e]);
 		__syncthreads();
@@ -380,10 +405,10 @@ __global__ void __launch_bounds__(kCcThreads) k_cg_cluster_mixed(CcArgs a) {
 			break;
 		}
 		if (ref == a.max_refine) break;
-		const double nr = sqrt(rr);
+		const double nr = sqrt(rr), inr = 1.0 / nr;
 		rr_prev = rr;
 		nr_prev = nr;
-		for (int e = tid; e < n; e += kCcThreads) v.b[e] = float(r64[e] / nr);
+		for (int e = tid; e < n; e += kCcThreads) v.b[e] = float(r64[e] * inr);
 		__syncthreads();  // the FP32 CG below overwrites the region that held the FP64 iterate
 		double irel = 0;
 		iters += cc_cg<float>(s, me, P, b0, bwl, v.mv(s), v.pf, v.x, v.r, v.p, v.q, v.b, true, a.inner_tol,

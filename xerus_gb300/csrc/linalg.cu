@@ -951,8 +951,9 @@ __global__ void __launch_bounds__(kQ1Threads, 1) k_qr_cl1(QrArgs a, Qc1Layout la
 	double* betas = sm + lay.beta();
 	int* perm = reinterpret_cast<int*>(sm + lay.ints());
 	int* flag = perm + nw;  // nw recompute flags, then the "any" flag
-	__shared__ double s_best[kQ1Threads / 32];
+	__shared__ long long s_best[kQ1Threads / 32];
 	__shared__ int s_bidx[kQ1Threads / 32];
+	__shared__ double s_coef[3];
 	auto w = [&](int il, int c) -> double& { return W[(long long)il * ldw + c]; };
 	auto lo_of = [&](int g) { return min(max(g - r0, 0), nl); };
 
@@ -987,15 +988,18 @@ __global__ void __launch_bounds__(kQ1Threads, 1) k_qr_cl1(QrArgs a, Qc1Layout la
 		__syncthreads();
 	};
 	// the first column of largest vn1 in [c0, nw) (idamax order; vn1 holds squares, same order),
-	// swapped into column c0
+	// swapped into column c0. vn1 >= 0, so its IEEE bit patterns order like its values: the
+	// search compares 64-bit integers (FP64 comparisons occupy GB300's slow FP64 pipe).
 	auto pivot_into = [&](int c0) {
-		double best = -1.0;
+		long long best = -1;
 		int bi = nw;
-		for (int c = c0 + tid; c < nw; c += kQ1Threads)
-			if (vn1[c] > best) { best = vn1[c]; bi = c; }
+		for (int c = c0 + tid; c < nw; c += kQ1Threads) {
+			const long long v = __double_as_longlong(vn1[c]);
+			if (v > best) { best = v; bi = c; }
+		}
 #pragma unroll
 		for (int o = 16; o > 0; o >>= 1) {
-			const double ob = __shfl_xor_sync(0xffffffffu, best, o);
+			const long long ob = __shfl_xor_sync(0xffffffffu, best, o);
 			const int oi = __shfl_xor_sync(0xffffffffu, bi, o);
 			if (ob > best || (ob == best && oi < bi)) { best = ob; bi = oi; }
 		}
@@ -1003,7 +1007,7 @@ __global__ void __launch_bounds__(kQ1Threads, 1) k_qr_cl1(QrArgs a, Qc1Layout la
 		__syncthreads();
 		int pv = nw;
 		{
-			double b = -1.0;
+			long long b = -1;
 			for (int t = 0; t < kQ1Threads / 32; ++t)
 				if (s_best[t] > b || (s_best[t] == b && s_bidx[t] < pv)) { b = s_best[t]; pv = s_bidx[t]; }
 		}
@@ -1084,9 +1088,18 @@ __global__ void __launch_bounds__(kQ1Threads, 1) k_qr_cl1(QrArgs a, Qc1Layout la
 		const int c0 = j + 1, C = nw - c0;
 		gather(par, true, c0, C);
 		__syncthreads();
-		double beta, tt, scal;
-		reflector_scalars(tot[1], tot[0], beta, tt, scal);
-		if (tid == 0) tau[j] = tt;
+		// the reflector's scalars, once per CTA (a square root and a division: redundant
+		// copies in every thread would queue on the FP64 pipe)
+		if (tid == 0) {
+			double b0, t0, s0;
+			reflector_scalars(tot[1], tot[0], b0, t0, s0);
+			s_coef[0] = b0;
+			s_coef[1] = t0;
+			s_coef[2] = s0;
+			tau[j] = t0;
+		}
+		__syncthreads();
+		const double beta = s_coef[0], tt = s_coef[1], scal = s_coef[2];
 		// the reflector below the diagonal (v = x scal) and R_jj
 		for (int il = lo_of(j + 1) + tid; il < nl; il += kQ1Threads) w(il, j) *= scal;
 		if (tid == 0 && j >= r0 && j < r1) w(j - r0, j) = beta;
