@@ -436,9 +436,9 @@ def run_gpu(args):
     if top in ("qr", "gemm") and classes.get(top, {}).get("GB_per_s"):
         c_ = classes[top]
         ach = c_["GB_per_s"]
-        line["roofline"] = {"kernel": {"qr": "k_qr_cl2 / k_qr (FP64 Householder)", "gemm": "k_gemm_sk (FP64)"}[top],
+        line["roofline"] = {"kernel": {"qr": "k_qr_cl1 / k_qr_small (FP64 Householder)", "gemm": "k_gemm_sk (FP64)"}[top],
                             "bound": "hbm", "achieved": ach, "peak": peaks.get("hbm_gbs", 6800.0), "unit": "GB/s",
-                            "frac": ach / peaks.get("hbm_gbs", 6800.0), "traffic": read_profile_traffic("qr_cl2_als_d8_r32"),
+                            "frac": ach / peaks.get("hbm_gbs", 6800.0), "traffic": read_profile_traffic("qr_cl1_als_d8_r32"),
                             "peak_source": "of measured" if "hbm_gbs" in peaks else "of fallback",
                             "algorithmic_bytes_per_launch": c_["bytes_per_step"] / c_["launches_per_step"],
                             "algorithmic_flops_per_launch": c_["flops_per_step"] / c_["launches_per_step"],

@@ -297,6 +297,16 @@ int xtt_adf(xtt_tensor* x, const int64_t* positions, const double* values, int64
             const xtt_adf_options* opt, double* final_residual, double* residual_trace,
             int64_t trace_capacity, int64_t* trace_count);
 
+/* GeometricCGVariant(numSteps, convergenceEpsilon, assumeSPD, SubmanifoldRetractionI,
+ * ProjectiveVectorTransport)(A, x, b, numSteps, perfData) (src/xerus/algorithms/cg.cpp:34-120,
+ * retractions.cpp, steepestDescent.cpp:37-80): Riemannian CG on the TT manifold of x's
+ * ranks; A = NULL minimises ||x - b||. x must be canonical at core 0 (as the reference
+ * requires) and is updated in place. residual receives ||b - A x|| (absolute, what the
+ * reference returns); residual_trace the residual before the first and after every step. */
+int xtt_geometric_cg(const xtt_tensor* A, xtt_tensor* x, const xtt_tensor* b, int64_t num_steps,
+                     double convergence_epsilon, int assume_spd, double* residual, double* residual_trace,
+                     int64_t trace_capacity, int64_t* trace_count);
+
 /* RankOneMeasurementSet (include/xerus/measurments.h:94-140): a sample is
  * <x, u_1 (x) ... (x) u_d> for vectors u_k of length n_k; `vectors` holds each
  * sample's vectors concatenated (num x sum n_k doubles, row-major).

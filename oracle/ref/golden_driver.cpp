@@ -584,6 +584,39 @@ static void case_arith() {
 	save_full("AAr_x", w);
 }
 
+// Riemannian CG on the fixed-rank TT manifold (GeometricCGVariant, algorithms/cg.cpp) with
+// SubmanifoldRetractionI and ProjectiveVectorTransport (algorithms/retractions.cpp).
+static void run_gcg(const std::string& tag, const GeometricCGVariant& v, const TTOperator* A, TTTensor x,
+                    const TTTensor& b, size_t steps, const std::vector<std::vector<size_t>>& pos) {
+	PerformanceData perf(false, true);
+	const double res = A ? v(*A, x, b, steps, perf) : v(x, b, steps, perf);
+	save(tag + "_perf_residual", perf_residuals(perf));
+	save_scalar(tag + "_residual", res);
+	save(tag + "_ranks", ranks_of(x));
+	save_probes(tag + "_x", x, pos);
+	save_tt(tag + "_x", x);
+}
+
+static void case_gcg() {
+	reseed();
+	const size_t d = 5, n = 3;
+	const std::vector<size_t> dims(d, n);
+	TTOperator A = laplace_operator(d, n, nullptr, false, 1.0);
+	TTOperator An = laplace_operator(d, n, nullptr, false, 1.0, 0.4);
+	TTTensor b = TTTensor::random(dims, 2);
+	TTTensor x = TTTensor::random(dims, 2);
+	save_op("A", A);
+	save_op("An", An);
+	save_tt("b", b);
+	save_tt("x0", x);
+	auto pos = probe_positions(dims, 100, 37);
+	GeometricCGVariant spd = GeometricCG;
+	spd.assumeSymmetricPositiveDefiniteOperator = true;
+	run_gcg("spd", spd, &A, x, b, 12, pos);
+	run_gcg("ls", GeometricCG, &An, x, b, 12, pos);
+	run_gcg("free", GeometricCG, nullptr, x, b, 8, pos);
+}
+
 static void case_dmrg() {
 	reseed();
 	const size_t d = 8, n = 4;
@@ -798,6 +831,7 @@ int main(int argc, char** argv) {
 	else if (c == "als_nonspd") case_als_nonspd();
 	else if (c == "arith") case_arith();
 	else if (c == "adf_rankone") case_adf_rankone();
+	else if (c == "gcg") case_gcg();
 	else {
 		std::fprintf(stderr, "unknown case %s\n", c.c_str());
 		return 2;

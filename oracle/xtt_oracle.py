@@ -1119,3 +1119,196 @@ def adf_loss_gradient(x: TT, positions, values):
         np.add.at(G, pos[:, k], outer)
         grads.append(G.transpose(1, 0, 2).copy())
     return 0.5 * float(np.sum(res ** 2)), grads
+
+
+# --------------------------------------------------------------------------- Riemannian CG
+
+
+def pseudo_inverse(M: np.ndarray) -> np.ndarray:
+    """pseudo_inverse(M, 1) (tensor.cpp:1568-1574): SVD truncated at EPSILON * S[0]
+    (calculate_svd's rule), inverted singular values."""
+    U, S, Vt = svd_trunc(np.asarray(M, dtype=np.float64), max(M.shape), EPSILON)
+    return Vt.T @ np.diag(1.0 / S) @ U.T
+
+
+def _tt_copy_at0(x: TT) -> TT:
+    y = x.copy()
+    move_core(y, 0, keep_rank=True)
+    return y
+
+
+class Tangent:
+    """TTTangentVector (retractions.cpp): components shaped like the base's cores, the
+    base kept canonical at position 0."""
+
+    def __init__(self, base: TT, comps):
+        self.base = base
+        self.comps = comps
+
+    def scaled(self, f: float) -> "Tangent":
+        return Tangent(self.base, [f * c for c in self.comps])
+
+    def plus(self, other: "Tangent", f: float = 1.0) -> "Tangent":
+        return Tangent(self.base, [a + f * b for a, b in zip(self.comps, other.comps)])
+
+    def dot(self, other: "Tangent") -> float:
+        """TTTangentVector::scalar_product (retractions.cpp:143-155)."""
+        left = np.ones((1, 1))
+        out = 0.0
+        d = len(self.comps)
+        for i in range(d):
+            out += float(np.einsum("ab,anc,bnc->", left, self.comps[i], other.comps[i], optimize=True))
+            if i + 1 < d:
+                u = self.base.cores[i]
+                left = np.einsum("ab,anc,bnd->cd", left, u, u, optimize=True)
+        return out
+
+    def norm(self) -> float:
+        return math.sqrt(self.dot(self))
+
+    def _blocks(self, first_plus_base: bool) -> TT:
+        d = len(self.comps)
+        U, V = self.base.cores, self.comps
+        if d == 1:
+            return TT([V[0] + U[0] if first_plus_base else V[0].copy()])
+        cores = []
+        for i in range(d):
+            r0, n, r1 = U[i].shape
+            if i == 0:
+                c = np.zeros((1, n, 2 * r1))
+                c[:, :, :r1] = U[0]
+                c[:, :, r1:] = U[0] + V[0] if first_plus_base else V[0]
+            elif i + 1 < d:
+                c = np.zeros((2 * r0, n, 2 * r1))
+                c[:r0, :, :r1] = U[i]
+                c[:r0, :, r1:] = V[i]
+                c[r0:, :, r1:] = U[i]
+            else:
+                c = np.zeros((2 * r0, n, 1))
+                c[:r0] = V[i]
+                c[r0:] = U[i]
+            cores.append(c)
+        t = TT(cores, canonicalized=False)
+        move_core(t, 0, keep_rank=False)
+        return t
+
+    def to_tt(self) -> TT:
+        """TTTangentVector::operator TTTensor (retractions.cpp:186-201)."""
+        return self._blocks(False)
+
+    def added_to_base(self) -> TT:
+        """TTTangentVector::added_to_base (retractions.cpp:203-219)."""
+        return self._blocks(True)
+
+
+def tangent_project(base: TT, direction: TT) -> Tangent:
+    """TTTangentVector(base, direction) (retractions.cpp:57-103): the projection of
+    `direction` onto the tangent space of the fixed-rank manifold at `base`."""
+    if not (base.canonicalized and base.core_position == 0):
+        raise ValueError("projection onto tangent plane is only implemented for core position 0 at the moment")
+    U = _tt_copy_at0(base)
+    d = U.d
+    UV, UU = [np.ones((1, 1))], [np.ones((1, 1))]
+    for i in range(d - 1):
+        UV.append(np.einsum("ab,anc,bnd->cd", UV[-1], U.cores[i], direction.cores[i], optimize=True))
+        UU.append(np.einsum("ab,anc,bnd->cd", UU[-1], U.cores[i], U.cores[i], optimize=True))
+    right = np.ones((1, 1))
+    comps = [None] * d
+    for i in range(d - 1, -1, -1):
+        u, dcore = U.cores[i], direction.cores[i]
+        inv = pseudo_inverse(UU[i])
+        V = np.einsum("as,sb,bnc,dc->and", inv, UV[i], dcore, right, optimize=True)
+        if i != 0:
+            utv = np.einsum("anc,bnc->ab", V, u, optimize=True)
+            V = V - np.einsum("ab,bnc->anc", utv, u, optimize=True)
+            right = np.einsum("anc,bnd,cd->ab", u, dcore, right, optimize=True)
+        comps[i] = V
+    return Tangent(U, comps)
+
+
+def submanifold_retraction(x: TT, change: Tangent) -> None:
+    """SubmanifoldRetractionI (retractions.cpp:228-236): every core plus its component,
+    then move_core(0, keepRank)."""
+    for i in range(x.d):
+        x.cores[i] = x.cores[i] + change.comps[i]
+    x.canonicalized = x.d == 1
+    move_core(x, 0, keep_rank=True)
+
+
+def _op_transpose(A: TTOp) -> TTOp:
+    return TTOp([c.transpose(0, 2, 1, 3).copy() for c in A.cores])
+
+
+def geometric_cg(A: TTOp | None, x: TT, b: TT, num_steps: int = 0, conv_eps: float = 1e-8,
+                 assume_spd: bool = False) -> tuple[float, list]:
+    """GeometricCGVariant::solve (algorithms/cg.cpp:34-120) with SubmanifoldRetractionI,
+    ProjectiveVectorTransport and line_search (steepestDescent.cpp:37-80). x is updated in
+    place; returns (final residual ||b - A x||, residual after every step)."""
+    norm_b = orthogonal_norm(b)
+    trace = []
+    state = {}
+
+    def calc_residual():
+        ax = x.copy() if A is None else op_apply(A, x)
+        res = tt_add(b, tt_scale(ax, -1.0))   # b - A x; b canonical: canonicalised again
+        state["res"] = res
+        return orthogonal_norm(res)
+
+    def update_gradient():
+        res = state["res"]
+        g = res if (assume_spd or A is None) else op_apply(_op_transpose(A), res)
+        state["grad"] = tangent_project(x, g)
+        state["gnorm"] = state["grad"].norm()
+
+    def line_search(alpha, direction, derivative, residual, change=0.8):
+        dir_norm = direction.norm()
+        curr = alpha / change
+        old = x.copy()
+        submanifold_retraction(x, direction.scaled(curr / dir_norm))
+        best_res = calc_residual()
+        best_alpha, best_x = curr, x.copy()
+        while True:
+            curr *= change
+            x.cores, x.canonicalized, x.core_position = [c.copy() for c in old.cores], old.canonicalized, old.core_position
+            submanifold_retraction(x, direction.scaled(curr / dir_norm))
+            new_res = calc_residual()
+            if new_res < best_res:
+                best_res, best_alpha, best_x = new_res, curr, x.copy()
+            else:
+                break
+        x.cores, x.canonicalized, x.core_position = best_x.cores, best_x.canonicalized, best_x.core_position
+        alpha = best_alpha
+        while alpha > 1e-16 and best_res > residual - 1e-4 * alpha / dir_norm * derivative:
+            alpha *= change
+            x.cores, x.canonicalized, x.core_position = [c.copy() for c in old.cores], old.canonicalized, old.core_position
+            submanifold_retraction(x, direction.scaled(alpha / dir_norm))
+            best_res = calc_residual()
+        state["res_norm_after"] = best_res
+        return alpha, best_res
+
+    curr = calc_residual()
+    last = 1e100
+    trace.append(curr)
+    update_gradient()
+    direction = state["grad"]
+    alpha = 1.0
+    steps = 0
+    while ((num_steps == 0 or steps < num_steps) and curr / norm_b > conv_eps
+           and abs(last - curr) / norm_b > conv_eps and abs(1 - curr / last) / norm_b > conv_eps):
+        steps += 1
+        grad = state["grad"]
+        derivative = grad.dot(direction) / direction.norm()
+        if derivative <= 0:
+            direction = grad
+            derivative = grad.norm()
+            alpha = 1.0
+        alpha, curr = line_search(alpha, direction, derivative, curr)
+        # as in the reference, the gradient below uses the residual TT of the last x the line
+        # search evaluated, which is a rejected trial unless the Armijo loop ran
+        trace.append(curr)
+        old_dir = tangent_project(x, direction.to_tt())        # ProjectiveVectorTransport
+        old_gnorm = state["gnorm"]
+        update_gradient()
+        beta = state["gnorm"] / old_gnorm
+        direction = state["grad"].plus(old_dir, beta)
+    return curr, trace

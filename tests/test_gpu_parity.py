@@ -368,6 +368,25 @@ def test_adf_small(ctx, golden):
     assert abs(res / z["small_final_residual"][0] - 1) < 1e-6
 
 
+@pytest.mark.parametrize("tag,op,spd,steps", [("spd", "A", True, 12), ("ls", "An", False, 12), ("free", None, False, 8)])
+def test_geometric_cg_matches_reference(ctx, golden, tag, op, spd, steps):
+    """Riemannian CG (GeometricCG): the reference's residual after every step and its final
+    iterate. The line search compares residuals, so a rounding-level difference can in
+    principle pick another step length; on these cases it does not."""
+    z = golden("gcg")
+    A = dev_op(ctx, op_of(z, op)) if op else None
+    x = dev_tt(ctx, tt_of(z, "x0"))
+    b = dev_tt(ctx, tt_of(z, "b"))
+    v = xg.GeometricCGVariant(0, 1e-8, spd)
+    perf = xg.PerformanceData()
+    res = v(A, x, b, steps, perf) if A is not None else v(x, b, steps, perf)
+    assert abs(res / z[tag + "_residual"][0] - 1) < 1e-9
+    assert len(perf.residuals) == len(z[tag + "_perf_residual"])
+    assert rel_err(perf.residuals, z[tag + "_perf_residual"]) < 1e-9
+    assert [1] + x.ranks() + [1] == list(z[tag + "_ranks"])
+    assert rel_err(x.entries(z[tag + "_x_probe_pos"]), z[tag + "_x_probe_val"]) < 1e-8
+
+
 def test_adf_rank_one_matches_reference(ctx, golden):
     """ADF on rank-one measurements (RankOneMeasurementSet): the reference's trajectory and
     final iterate; the device measurement of the target against the reference's values."""

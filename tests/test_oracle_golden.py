@@ -233,3 +233,17 @@ def test_adf_rank_one(golden):
     res = o.adf_rank_one(x, z["vectors"], z["values"], 25, 0.0, 1.0)
     assert rel_err(res.residuals, z["perf_residual"]) < 1e-10
     assert rel_err(o.tt_entries(x, z["x_final_probe_pos"]), z["x_final_probe_val"]) < 1e-10
+
+
+@pytest.mark.parametrize("tag,op,spd,steps", [("spd", "A", True, 12), ("ls", "An", False, 12), ("free", None, False, 8)])
+def test_geometric_cg(golden, tag, op, spd, steps):
+    """GeometricCGVariant with the submanifold retraction and projective vector transport:
+    SPD operator (gradient b - A x), least squares (A^T (b - A x)) and no operator."""
+    z = golden("gcg")
+    A = op_of(z, op) if op else None
+    x, b = tt_of(z, "x0"), tt_of(z, "b")
+    res, trace = o.geometric_cg(A, x, b, steps, 1e-8, spd)
+    assert abs(res / z[tag + "_residual"][0] - 1) < 1e-12
+    assert rel_err(trace, z[tag + "_perf_residual"]) < 1e-12
+    assert [1] + x.ranks + [1] == list(z[tag + "_ranks"])
+    assert rel_err(o.tt_entries(x, z[tag + "_x_probe_pos"]), z[tag + "_x_probe_val"]) < 1e-12

@@ -17,7 +17,7 @@ import numpy as np
 from . import _lib as L
 
 __all__ = ["Context", "TTTensor", "TTOperator", "frob_norm", "dot", "residual", "ALSVariant", "ALS", "ALS_SPD", "DMRG", "DMRG_SPD", "ASD",
-           "ASD_SPD", "ADFVariant", "ADF", "SinglePointMeasurementSet", "RankOneMeasurementSet", "PerformanceData", "seed", "EPSILON",
+           "ASD_SPD", "ADFVariant", "ADF", "SinglePointMeasurementSet", "RankOneMeasurementSet", "GeometricCGVariant", "GeometricCG", "PerformanceData", "seed", "EPSILON",
            "XttError", "FP64", "MIXED", "als_batch", "apply", "save_to_file", "load_from_file", "file_encode", "file_decode"]
 
 EPSILON = 8 * np.finfo(np.float64).eps  # include/xerus/basic.h:50
@@ -572,6 +572,49 @@ class SinglePointMeasurementSet:
 
     def frob_norm(self):
         return float(np.sqrt(np.sum(self.measuredValues ** 2)))
+
+
+class GeometricCGVariant:
+    """xerus::GeometricCGVariant (include/xerus/algorithms/cg.h:41-134) with the submanifold
+    retraction and projective vector transport (GeometricCG): Riemannian CG on the TT
+    manifold of x's ranks. Called as v(A, x, b[, numSteps | convergenceEpsilon][, perfData])
+    or without an operator v(x, b, ...); returns ||b - A x||."""
+
+    def __init__(self, numSteps=0, convergenceEpsilon=1e-8, assumeSymmetricPositiveDefiniteOperator=False):
+        self.numSteps = numSteps
+        self.convergenceEpsilon = convergenceEpsilon
+        self.assumeSymmetricPositiveDefiniteOperator = assumeSymmetricPositiveDefiniteOperator
+
+    def copy(self):
+        return GeometricCGVariant(self.numSteps, self.convergenceEpsilon, self.assumeSymmetricPositiveDefiniteOperator)
+
+    def __call__(self, *args):
+        if len(args) >= 2 and isinstance(args[0], TTTensor):
+            A, rest = None, args
+        else:
+            A, rest = args[0], args[1:]
+        x, b = rest[0], rest[1]
+        arg = rest[2] if len(rest) > 2 else None
+        perfData = rest[3] if len(rest) > 3 else None
+        if isinstance(arg, PerformanceData):
+            arg, perfData = None, arg
+        steps, eps = self.numSteps, self.convergenceEpsilon
+        if isinstance(arg, (int, np.integer)):
+            steps = int(arg)
+        elif isinstance(arg, (float, np.floating)):
+            eps = float(arg)
+        cap = max(16, steps + 2 if steps else 100000)
+        trace = np.zeros(cap)
+        res, cnt = ctypes.c_double(), ctypes.c_int64()
+        L.check(x.lib.xtt_geometric_cg(A.handle if A is not None else None, x.handle, b.handle, int(steps), float(eps),
+                                       int(bool(self.assumeSymmetricPositiveDefiniteOperator)), ctypes.byref(res),
+                                       trace.ctypes.data_as(L.c_double_p), cap, ctypes.byref(cnt)))
+        if perfData is not None:
+            perfData.residuals = list(trace[:min(cnt.value, cap)])
+        return res.value
+
+
+GeometricCG = GeometricCGVariant(0, 1e-8, False)
 
 
 class RankOneMeasurementSet:

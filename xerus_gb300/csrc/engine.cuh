@@ -200,6 +200,14 @@ struct AdfResult {
 // per-sample arithmetic with FP64 cores, QR and final check.
 AdfResult adf(Tensor& x, const int64_t* positions, const double* values, long long N, int64_t max_iter, double target,
               double min_dec, int precision = XTT_PRECISION_FP64);
+// Riemannian CG on the fixed-rank TT manifold (GeometricCGVariant with the submanifold
+// retraction and projective vector transport); A null: minimise ||x - b||.
+struct RiemannReport {
+	double residual = 0;         // ||b - A x|| of the result (absolute, as the reference returns)
+	int64_t steps = 0;
+	std::vector<double> trace;   // residual before the first step and after every step
+};
+RiemannReport geometric_cg(const Tensor* A, Tensor& x, const Tensor& b, int64_t num_steps, double eps, bool assume_spd);
 // ADF on rank-one measurements (RankOneMeasurementSet): vectors holds, per sample, the
 // concatenated vectors u_1 .. u_d (N x sum n_k, row-major). FP64.
 AdfResult adf_rank_one(Tensor& x, const double* vectors, const double* values, long long N, int64_t max_iter,
