@@ -306,6 +306,12 @@ int xtt_adf(xtt_tensor* x, const int64_t* positions, const double* values, int64
 int xtt_geometric_cg(const xtt_tensor* A, xtt_tensor* x, const xtt_tensor* b, int64_t num_steps,
                      double convergence_epsilon, int assume_spd, double* residual, double* residual_trace,
                      int64_t trace_capacity, int64_t* trace_count);
+/* SteepestDescentVariant(numSteps, convergenceEpsilon, assumeSPD, SubmanifoldRetractionII)
+ * (src/xerus/algorithms/steepestDescent.cpp:83-175): same arguments and results as
+ * xtt_geometric_cg (the stopping tests are absolute, as in the reference). */
+int xtt_steepest_descent(const xtt_tensor* A, xtt_tensor* x, const xtt_tensor* b, int64_t num_steps,
+                         double convergence_epsilon, int assume_spd, double* residual, double* residual_trace,
+                         int64_t trace_capacity, int64_t* trace_count);
 
 /* RankOneMeasurementSet (include/xerus/measurments.h:94-140): a sample is
  * <x, u_1 (x) ... (x) u_d> for vectors u_k of length n_k; `vectors` holds each

@@ -615,6 +615,20 @@ static void case_gcg() {
 	run_gcg("spd", spd, &A, x, b, 12, pos);
 	run_gcg("ls", GeometricCG, &An, x, b, 12, pos);
 	run_gcg("free", GeometricCG, nullptr, x, b, 8, pos);
+	// steepest descent with the submanifold retraction (algorithms/steepestDescent.cpp)
+	auto run_sd = [&](const std::string& tag, const SteepestDescentVariant& v, const TTOperator* Ap, size_t steps) {
+		TTTensor y = x;
+		PerformanceData perf(false, true);
+		const double res = Ap ? v(*Ap, y, b, steps, perf) : v(y, b, steps, perf);
+		save(tag + "_perf_residual", perf_residuals(perf));
+		save_scalar(tag + "_residual", res);
+		save_probes(tag + "_x", y, pos);
+	};
+	SteepestDescentVariant sds = SteepestDescent;
+	sds.assumeSymmetricPositiveDefiniteOperator = true;
+	run_sd("sd_spd", sds, &A, 10);
+	run_sd("sd_ls", SteepestDescent, &An, 10);
+	run_sd("sd_free", SteepestDescent, nullptr, 6);
 }
 
 static void case_dmrg() {

@@ -1312,3 +1312,38 @@ def geometric_cg(A: TTOp | None, x: TT, b: TT, num_steps: int = 0, conv_eps: flo
         beta = state["gnorm"] / old_gnorm
         direction = state["grad"].plus(old_dir, beta)
     return curr, trace
+
+
+def steepest_descent(A: TTOp | None, x: TT, b: TT, num_steps: int = 0, conv_eps: float = 1e-8,
+                     assume_spd: bool = False) -> tuple[float, list]:
+    """SteepestDescentVariant::solve (algorithms/steepestDescent.cpp:83-175) with
+    SubmanifoldRetractionII (retractions.cpp:222-225: project the TT step onto the tangent
+    space at x, then the submanifold retraction). Absolute stopping tests, step doubling
+    and halving as in the reference; returns (||b - A x||, residual after every step)."""
+    def residual_tt():
+        ax = x.copy() if A is None else op_apply(A, x)
+        return tt_add(b, tt_scale(ax, -1.0))
+
+    res = residual_tt()
+    curr, last = orthogonal_norm(res.copy()), 1e100
+    trace = [curr]
+    alpha, steps = 1.0, 0
+    while ((num_steps == 0 or steps < num_steps) and curr > conv_eps and abs(last - curr) > conv_eps
+           and abs(1 - curr / last) > conv_eps):
+        steps += 1
+        y = res if (A is None or assume_spd) else op_apply(_op_transpose(A), res)
+        old = x.copy()
+        w = tangent_project(x, y)
+        alpha *= 2
+        submanifold_retraction(x, w.scaled(alpha))
+        last = curr
+        res = residual_tt()
+        curr = orthogonal_norm(res.copy())
+        while alpha > 1e-30 and last < curr:
+            alpha /= 2
+            x.cores, x.canonicalized, x.core_position = [c.copy() for c in old.cores], old.canonicalized, old.core_position
+            submanifold_retraction(x, w.scaled(alpha))
+            res = residual_tt()
+            curr = orthogonal_norm(res.copy())
+        trace.append(curr)
+    return curr, trace

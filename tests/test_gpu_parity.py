@@ -387,6 +387,21 @@ def test_geometric_cg_matches_reference(ctx, golden, tag, op, spd, steps):
     assert rel_err(x.entries(z[tag + "_x_probe_pos"]), z[tag + "_x_probe_val"]) < 1e-8
 
 
+@pytest.mark.parametrize("tag,op,spd,steps", [("sd_spd", "A", True, 10), ("sd_ls", "An", False, 10),
+                                              ("sd_free", None, False, 6)])
+def test_steepest_descent_matches_reference(ctx, golden, tag, op, spd, steps):
+    z = golden("gcg")
+    A = dev_op(ctx, op_of(z, op)) if op else None
+    x = dev_tt(ctx, tt_of(z, "x0"))
+    b = dev_tt(ctx, tt_of(z, "b"))
+    v = xg.SteepestDescentVariant(0, 1e-8, spd)
+    perf = xg.PerformanceData()
+    res = v(A, x, b, steps, perf) if A is not None else v(x, b, steps, perf)
+    assert abs(res / z[tag + "_residual"][0] - 1) < 1e-9
+    assert rel_err(perf.residuals, z[tag + "_perf_residual"]) < 1e-9
+    assert rel_err(x.entries(z[tag + "_x_probe_pos"]), z[tag + "_x_probe_val"]) < 1e-8
+
+
 def test_adf_rank_one_matches_reference(ctx, golden):
     """ADF on rank-one measurements (RankOneMeasurementSet): the reference's trajectory and
     final iterate; the device measurement of the target against the reference's values."""

@@ -247,3 +247,16 @@ def test_geometric_cg(golden, tag, op, spd, steps):
     assert rel_err(trace, z[tag + "_perf_residual"]) < 1e-12
     assert [1] + x.ranks + [1] == list(z[tag + "_ranks"])
     assert rel_err(o.tt_entries(x, z[tag + "_x_probe_pos"]), z[tag + "_x_probe_val"]) < 1e-12
+
+
+@pytest.mark.parametrize("tag,op,spd,steps", [("sd_spd", "A", True, 10), ("sd_ls", "An", False, 10),
+                                              ("sd_free", None, False, 6)])
+def test_steepest_descent(golden, tag, op, spd, steps):
+    """SteepestDescentVariant with SubmanifoldRetractionII."""
+    z = golden("gcg")
+    A = op_of(z, op) if op else None
+    x, b = tt_of(z, "x0"), tt_of(z, "b")
+    res, trace = o.steepest_descent(A, x, b, steps, 1e-8, spd)
+    assert abs(res / z[tag + "_residual"][0] - 1) < 1e-12
+    assert rel_err(trace, z[tag + "_perf_residual"]) < 1e-12
+    assert rel_err(o.tt_entries(x, z[tag + "_x_probe_pos"]), z[tag + "_x_probe_val"]) < 1e-12

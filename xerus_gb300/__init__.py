@@ -17,7 +17,7 @@ import numpy as np
 from . import _lib as L
 
 __all__ = ["Context", "TTTensor", "TTOperator", "frob_norm", "dot", "residual", "ALSVariant", "ALS", "ALS_SPD", "DMRG", "DMRG_SPD", "ASD",
-           "ASD_SPD", "ADFVariant", "ADF", "SinglePointMeasurementSet", "RankOneMeasurementSet", "GeometricCGVariant", "GeometricCG", "PerformanceData", "seed", "EPSILON",
+           "ASD_SPD", "ADFVariant", "ADF", "SinglePointMeasurementSet", "RankOneMeasurementSet", "GeometricCGVariant", "GeometricCG", "SteepestDescentVariant", "SteepestDescent", "PerformanceData", "seed", "EPSILON",
            "XttError", "FP64", "MIXED", "als_batch", "apply", "save_to_file", "load_from_file", "file_encode", "file_decode"]
 
 EPSILON = 8 * np.finfo(np.float64).eps  # include/xerus/basic.h:50
@@ -580,13 +580,15 @@ class GeometricCGVariant:
     manifold of x's ranks. Called as v(A, x, b[, numSteps | convergenceEpsilon][, perfData])
     or without an operator v(x, b, ...); returns ||b - A x||."""
 
+    _entry = "xtt_geometric_cg"
+
     def __init__(self, numSteps=0, convergenceEpsilon=1e-8, assumeSymmetricPositiveDefiniteOperator=False):
         self.numSteps = numSteps
         self.convergenceEpsilon = convergenceEpsilon
         self.assumeSymmetricPositiveDefiniteOperator = assumeSymmetricPositiveDefiniteOperator
 
     def copy(self):
-        return GeometricCGVariant(self.numSteps, self.convergenceEpsilon, self.assumeSymmetricPositiveDefiniteOperator)
+        return type(self)(self.numSteps, self.convergenceEpsilon, self.assumeSymmetricPositiveDefiniteOperator)
 
     def __call__(self, *args):
         if len(args) >= 2 and isinstance(args[0], TTTensor):
@@ -606,15 +608,26 @@ class GeometricCGVariant:
         cap = max(16, steps + 2 if steps else 100000)
         trace = np.zeros(cap)
         res, cnt = ctypes.c_double(), ctypes.c_int64()
-        L.check(x.lib.xtt_geometric_cg(A.handle if A is not None else None, x.handle, b.handle, int(steps), float(eps),
-                                       int(bool(self.assumeSymmetricPositiveDefiniteOperator)), ctypes.byref(res),
-                                       trace.ctypes.data_as(L.c_double_p), cap, ctypes.byref(cnt)))
+        L.check(getattr(x.lib, self._entry)(A.handle if A is not None else None, x.handle, b.handle, int(steps),
+                                            float(eps), int(bool(self.assumeSymmetricPositiveDefiniteOperator)),
+                                            ctypes.byref(res), trace.ctypes.data_as(L.c_double_p), cap,
+                                            ctypes.byref(cnt)))
         if perfData is not None:
             perfData.residuals = list(trace[:min(cnt.value, cap)])
         return res.value
 
 
 GeometricCG = GeometricCGVariant(0, 1e-8, False)
+
+
+class SteepestDescentVariant(GeometricCGVariant):
+    """xerus::SteepestDescentVariant (include/xerus/algorithms/steepestDescent.h) with the
+    submanifold retraction (SteepestDescent); same calls as GeometricCGVariant."""
+
+    _entry = "xtt_steepest_descent"
+
+
+SteepestDescent = SteepestDescentVariant(0, 1e-8, False)
 
 
 class RankOneMeasurementSet:

@@ -699,6 +699,21 @@ int xtt_geometric_cg(const xtt_tensor* A, xtt_tensor* x, const xtt_tensor* b, in
 	});
 }
 
+int xtt_steepest_descent(const xtt_tensor* A, xtt_tensor* x, const xtt_tensor* b, int64_t num_steps,
+                         double convergence_epsilon, int assume_spd, double* residual, double* residual_trace,
+                         int64_t trace_capacity, int64_t* trace_count) {
+	return guard([&] {
+		ARG(x && b, "NULL argument");
+		ARG(num_steps >= 0, "num_steps must be >= 0");
+		const xtt::RiemannReport r =
+		    xtt::steepest_descent(A ? A->t : nullptr, *x->t, *b->t, num_steps, convergence_epsilon, assume_spd != 0);
+		if (residual) *residual = r.residual;
+		if (residual_trace)
+			for (size_t i = 0; i < r.trace.size() && int64_t(i) < trace_capacity; ++i) residual_trace[i] = r.trace[i];
+		if (trace_count) *trace_count = int64_t(r.trace.size());
+	});
+}
+
 int xtt_random_rank_one(int64_t num, int64_t order, const int64_t* dims, double* out) {
 	return guard([&] {
 		ARG(dims && (out || num == 0) && order > 0, "NULL argument");

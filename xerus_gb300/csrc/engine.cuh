@@ -208,6 +208,9 @@ struct RiemannReport {
 	std::vector<double> trace;   // residual before the first step and after every step
 };
 RiemannReport geometric_cg(const Tensor* A, Tensor& x, const Tensor& b, int64_t num_steps, double eps, bool assume_spd);
+// SteepestDescentVariant with SubmanifoldRetractionII (absolute stopping tests, as the reference)
+RiemannReport steepest_descent(const Tensor* A, Tensor& x, const Tensor& b, int64_t num_steps, double eps,
+                               bool assume_spd);
 // ADF on rank-one measurements (RankOneMeasurementSet): vectors holds, per sample, the
 // concatenated vectors u_1 .. u_d (N x sum n_k, row-major). FP64.
 AdfResult adf_rank_one(Tensor& x, const double* vectors, const double* values, long long N, int64_t max_iter,

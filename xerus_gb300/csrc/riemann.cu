@@ -419,4 +419,76 @@ RiemannReport geometric_cg(const Tensor* A, Tensor& x, const Tensor& b, int64_t 
 	return rep;
 }
 
+RiemannReport steepest_descent(const Tensor* A, Tensor& x, const Tensor& b, int64_t num_steps, double eps,
+                               bool assume_spd) {
+	// SteepestDescentVariant::solve (src/xerus/algorithms/steepestDescent.cpp:83-175) with
+	// SubmanifoldRetractionII (retractions.cpp:222-225)
+	Context& c = *x.ctx;
+	XTT_REQUIRE(!x.op && !b.op && x.dims == b.dims && (!A || (A->op && A->dims == x.dims)),
+	            "dimensions of A, x and b must match");
+	const int d = x.d;
+	RiemannReport rep;
+	std::unique_ptr<Tensor> At;
+	if (A && !assume_spd) {
+		At.reset(new Tensor(&c, true, d, A->dims.data(), A->ranks.data()));
+		for (int k = 0; k < d; ++k) {
+			k_op_transpose<<<grid_of(A->core_size(k)), 256, 0, c.stream>>>(At->core[k], A->core[k], int(A->ranks[k]),
+			                                                                int(A->dims[k]), int(A->ranks[k + 1]));
+			c.count_launch();
+		}
+		XTT_CUDA(cudaGetLastError());
+	}
+	std::unique_ptr<Tensor> residual;
+	auto update_residual = [&]() -> double {
+		std::unique_ptr<Tensor> ax;
+		if (A) {
+			std::vector<int64_t> r(d + 1);
+			for (int k = 0; k <= d; ++k) r[k] = A->ranks[k] * x.ranks[k];
+			ax.reset(new Tensor(&c, false, d, x.dims.data(), r.data()));
+			tt_apply(*A, x, *ax);
+		} else {
+			ax = clone(x);
+		}
+		residual = clone(b);
+		tt_add(*residual, *ax, -1.0);
+		std::unique_ptr<Tensor> t = clone(*residual);
+		return orthogonal_norm(*t);
+	};
+	double curr = update_residual(), last = 1e100, alpha = 1.0;
+	rep.trace.push_back(curr);
+	int64_t steps = 0;
+	while ((num_steps == 0 || steps < num_steps) && curr > eps && std::fabs(last - curr) > eps &&
+	       std::fabs(1.0 - curr / last) > eps) {
+		++steps;
+		std::unique_ptr<Tensor> y;
+		if (At) {
+			std::vector<int64_t> r(d + 1);
+			for (int k = 0; k <= d; ++k) r[k] = At->ranks[k] * residual->ranks[k];
+			y.reset(new Tensor(&c, false, d, x.dims.data(), r.data()));
+			tt_apply(*At, *residual, *y);
+		} else {
+			y = clone(*residual);
+		}
+		// the retraction projects the step at the current x; halving keeps the same base
+		std::unique_ptr<Tensor> old = clone(x);
+		const Base base = make_base(x);
+		const Tangent w = project(c, base, *y);
+		alpha *= 2;
+		retract(c, x, w, alpha);
+		last = curr;
+		curr = update_residual();
+		while (alpha > 1e-30 && last < curr) {
+			alpha /= 2;
+			x.copy_from(*old);
+			retract(c, x, w, alpha);
+			curr = update_residual();
+		}
+		rep.trace.push_back(curr);
+	}
+	rep.residual = curr;
+	rep.steps = steps;
+	c.sync();
+	return rep;
+}
+
 }  // namespace xtt
