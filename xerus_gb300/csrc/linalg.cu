@@ -1574,6 +1574,13 @@ __global__ void __launch_bounds__(kSvdThreads) k_svd(SvdArgs a, int use_smem) {
 		B[e] = tall ? a.X[(long long)i * a.ldx + c] : a.X[(long long)c * a.ldx + i];
 	}
 	for (long long e = tid; e < (long long)q * q; e += blockDim.x) V[e] = (e / q == e % q) ? 1.0 : 0.0;
+	__shared__ double s_red[32];
+	double nl = 0;
+	for (long long e = tid; e < (long long)p * q; e += blockDim.x) nl = fma(B[e], B[e], nl);
+	// pairs with a column below 0.1 eps ||A||_F need no rotation: such columns end as singular
+	// values far under every truncation threshold (8 eps S_0 >= 8 eps ||A||_F / sqrt(q)), and
+	// rotating rounding noise against them keeps the sweep from converging
+	const double negl = block_sum(nl, s_red) * (0.01 * DBL_EPSILON * DBL_EPSILON);
 	__syncthreads();
 	const double tol = DBL_EPSILON * sqrt(double(p));
 	int sweep = 0;
@@ -1599,7 +1606,7 @@ __global__ void __launch_bounds__(kSvdThreads) k_svd(SvdArgs a, int use_smem) {
 				al = warp_sum(al);
 				be = warp_sum(be);
 				ga = warp_sum(ga);
-				if (ga != 0.0 && fabs(ga) > tol * sqrt(al * be)) {
+				if (ga != 0.0 && fmin(al, be) > negl && fabs(ga) > tol * sqrt(al * be)) {
 					double c, s;
 					jacobi_rotation(al, be, ga, c, s);
 					for (int r = lane; r < p; r += 32) {
@@ -1755,6 +1762,21 @@ __global__ void __launch_bounds__(kSvcThreads) k_svd_cluster(SvdArgs a, SvcLayou
 		}
 	}
 	__syncthreads();
+	// ||A||_F^2 over the cluster (see k_svd: pairs with a negligible column are not rotated)
+	__shared__ double s_red[32];
+	{
+		double nl = 0;
+		const double* b0 = sm + lay.buf(0);
+		for (long long e = tid; e < (long long)cpc * cw; e += blockDim.x)
+			if (int(e % cw) < p) nl = fma(b0[e], b0[e], nl);
+		nl = block_sum(nl, s_red);
+		cl.sync();  // every CTA runs before the first remote store
+		if (tid < P) cl.map_shared_rank(sig, tid)[me] = nl;
+		cl.sync();
+	}
+	double na2 = 0;
+	for (int c = 0; c < P; ++c) na2 += sig[c];
+	const double negl = na2 * (0.01 * DBL_EPSILON * DBL_EPSILON);
 	const double tol = DBL_EPSILON * sqrt(double(p));
 	int cur = 0, t = 0, sweep = 0;
 	bool converged = (q < 2);
@@ -1779,7 +1801,7 @@ __global__ void __launch_bounds__(kSvcThreads) k_svd_cluster(SvdArgs a, SvcLayou
 			al = warp_sum(al);
 			be = warp_sum(be);
 			ga = warp_sum(ga);
-			if (ga != 0.0 && fabs(ga) > tol * sqrt(al * be)) {
+			if (ga != 0.0 && fmin(al, be) > negl && fabs(ga) > tol * sqrt(al * be)) {
 				double c, sn;
 				jacobi_rotation(al, be, ga, c, sn);
 				for (int r = lane; r < p + q; r += 32) {
