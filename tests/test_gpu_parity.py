@@ -127,6 +127,37 @@ def test_round_cfg2(ctx, golden):
     assert rel_err(y.entries(r["cfg2_round_probe_pos"]), r["cfg2_round_probe_val"]) < REL_TOL
 
 
+def test_svd_paths_agree(ctx):
+    """The DMRG split through the QR-preconditioned Jacobi SVD (the default; tall
+    128 x 128 and wide 64 x 128 splits at rank 16) and through plain one-sided
+    Jacobi: same ranks, same energies, the same iterate to the local CG tolerance."""
+    out = {}
+    try:
+        for path in ("jacobi", "auto"):
+            ctx.set_svd_path(path)
+            d, n = 12, 8
+            rng = np.random.default_rng(7)
+            V = [rng.uniform(0.0, 1.0, n) for _ in range(d)]
+            xg.seed(11)
+            A = xg.TTOperator.from_cores(xg.laplacian_cores(d, n, potentials=V, rank3=True), ctx=ctx)
+            b = xg.TTTensor.random([n] * d, 4, ctx=ctx)
+            xd = xg.TTTensor.random([n] * d, 16, ctx=ctx)
+            xd /= xd.frob_norm()
+            v = xg.DMRG_SPD.copy()
+            v.convergenceEpsilon = 0.0
+            v.exact_environment = True
+            e = v(A, xd, b, 2)
+            out[path] = (xd, e, xd.ranks())
+    finally:
+        ctx.set_svd_path("auto")
+    assert out["auto"][2] == out["jacobi"][2]
+    assert abs(out["auto"][1] / out["jacobi"][1] - 1) < 1e-10
+    # the local systems' solutions reach norms ~1e7 here; rounding-level changes of
+    # a core move the iterate by ~1e-8 relative, within the local CG tolerance
+    xa, xj = out["auto"][0], out["jacobi"][0]
+    assert (xa - xj).frob_norm() / xj.frob_norm() < 1e-6
+
+
 def test_round_eps_and_max_ranks(ctx, golden):
     r = golden("round")
     e = tt_of(r, "eps_in", canonicalized=False)

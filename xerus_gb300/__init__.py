@@ -75,6 +75,10 @@ class Context:
         """'auto' (cluster-resident CG where the local system fits) or 'grid'."""
         L.check(self.lib.xtt_context_set_cg_path(self.handle, {"auto": 0, "grid": 1}[path]))
 
+    def set_svd_path(self, path):
+        """'auto' (QR-preconditioned Jacobi where it fits) or 'jacobi' (plain one-sided Jacobi)."""
+        L.check(self.lib.xtt_context_set_svd_path(self.handle, {"auto": 0, "jacobi": 1}[path]))
+
     def profile_get(self, name):
         """(launches, milliseconds) of a kernel class since profiling started."""
         n, ms = ctypes.c_int64(), ctypes.c_double()

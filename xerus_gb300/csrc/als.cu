@@ -941,15 +941,9 @@ AlsReport als(const Tensor* Ap, Tensor& x, const Tensor& b, const AlsOptions& o)
 			double* U = c.scratch<double>(S_SVD_U, size_t(m) * q);
 			double* Sv = c.scratch<double>(S_SVD_S, size_t(q));
 			double* Vt = c.scratch<double>(S_SVD_VT, size_t(q) * nn);
-			const size_t wk = svd_work_doubles(m, nn);
 			a.X = s.v; a.ldx = nn; a.m = m; a.n = nn; a.max_rank = mr; a.eps = eps;
-			a.work = wk ? c.scratch<double>(S_SVD_WORK, wk) : nullptr;
 			a.U = U; a.S = Sv; a.Vt = Vt; a.rank_out = c.d_ints + 1; a.status = c.d_status;
-			{
-				ProfScope ps(c, "svd");
-				launch_svd(a, c.stream);
-			}
-			c.count_launch();
+			run_svd(c, a, true);
 			const int rk = c.read_int(1);
 			XTT_REQUIRE(rk <= rmax[cur + 1], "DMRG split rank exceeds the stack capacity");
 			if (inc) {

@@ -144,6 +144,14 @@ int xtt_context_set_cg_path(xtt_context* ctx, int path) {
 	});
 }
 
+int xtt_context_set_svd_path(xtt_context* ctx, int path) {
+	return guard([&] {
+		ARG(ctx, "ctx is NULL");
+		ARG(path == XTT_SVD_PATH_AUTO || path == XTT_SVD_PATH_JACOBI, "unknown SVD path");
+		ctx->c->svd_path = path;
+	});
+}
+
 int xtt_context_profile_get(xtt_context* ctx, const char* name, int64_t* launches, double* milliseconds) {
 	return guard([&] {
 		ARG(ctx && name && launches && milliseconds, "NULL argument");

@@ -34,6 +34,7 @@ struct Context {
 	double* h_dbl = nullptr;       // pinned mirror
 	long long launches = 0;
 	int cg_path = XTT_CG_PATH_AUTO;  // xtt_cg_path: which local CG kernel family runs
+	int svd_path = XTT_SVD_PATH_AUTO;  // xtt_svd_path: QR-preconditioned or plain Jacobi SVD
 	// batched ALS: the CUDA graph of the last batch launch (replayed while its
 	// signature holds), its pinned descriptor staging, and autotuned launch shapes
 	unsigned long long batch_key = 0;
@@ -109,9 +110,10 @@ enum ScratchId : int {
 	S_ROUND_X, S_ROUND_QA, S_ROUND_QB, S_ROUND_CA, S_ROUND_CB, S_ZIP_M, S_ZIP_T, S_ZIP_M2,
 	S_RES_CORE0, S_RES_CORE1, S_RES_R, S_RED, S_ENT_META, S_ENT_CORES, S_ENT_OUT,
 	S_RES_CORE0B, S_RES_CORE1B, S_RES_RB, S_QR_WORKB, S_BATCH_META, S_BATCH_WORK, S_BATCH_BACKUP,
-	S_ALS_FIRST = 32,
-	S_ADF_FIRST = 96,
-	S_MAX = 160
+	S_SVD_PC_Q, S_SVD_PC_C, S_SVD_PC_UV, S_SVD_PC_QRW,
+	S_ALS_FIRST = 40,
+	S_ADF_FIRST = 104,
+	S_MAX = 168
 };
 
 struct Tensor {
@@ -148,6 +150,13 @@ void gemm_f(Context& c, const Gemm<float>& g);
 void copy_d2d(Context& c, double* dst, const double* src, size_t count);
 void fill(Context& c, double* dst, double v, size_t count);
 void scale(Context& c, double* x, double f, size_t count);
+// Truncated SVD a.X = a.U diag(a.S) a.Vt on the context's stream (kernel class "svd").
+// `graded`: the caller expects a decaying spectrum (a DMRG two-site solution); then,
+// where it fits and svd_path allows, QR-preconditioned Jacobi runs (a third of the
+// plain sweeps there; on unstructured matrices, e.g. rounding a random TT, it saves
+// no sweeps and its QR costs more than it saves). The workspace (a.work) is taken
+// from the context's scratch here.
+void run_svd(Context& c, SvdArgs& a, bool graded = false);
 void scale_rows(Context& c, double* X, const double* S, int rows, int cols);  // X (rows x cols) *= S[row]
 void scale_cols(Context& c, double* X, const double* S, int rows, int cols);  // X (rows x cols) *= S[col]
 // Sum of squares of x into ctx.d_dbl[slot] (deterministic two-level reduction).

@@ -176,7 +176,7 @@ __global__ void __launch_bounds__(kQrThreads) k_qr(QrArgs a, int use_smem) {
 	__syncthreads();
 	if (tid == 0) {
 		int rank = kq;
-		if (a.pivot) {
+		if (a.pivot && a.rank_rule) {
 			const double r00 = w(0, 0);
 			for (int k = 1; k < kq; ++k)
 				if (fabs(w(k, k)) < 16.0 * DBL_EPSILON * r00) { rank = k; break; }
@@ -451,7 +451,7 @@ __global__ void __launch_bounds__(kQcThreads) k_qr_cluster(QrArgs a, QcLayout la
 	__syncthreads();
 	if (tid == 0) {
 		int rank = kq;
-		if (a.pivot) {
+		if (a.pivot && a.rank_rule) {
 			const double r00 = diag[0];
 			for (int k = 1; k < kq; ++k)
 				if (fabs(diag[k]) < 16.0 * DBL_EPSILON * r00) { rank = k; break; }
@@ -792,7 +792,7 @@ __global__ void __launch_bounds__(kQ2Threads) k_qr_cl2(QrArgs a, Qc2Layout lay) 
 		__syncthreads();
 	}
 	int rank = kq;
-	if (a.pivot) {
+	if (a.pivot && a.rank_rule) {
 		// the reference's rank rule on R's diagonal, gathered from its owners (|R_kk| < 16 eps R_00)
 		cl.sync();
 		for (int k = tid; k < kq; k += kQ2Threads) {
@@ -1151,7 +1151,7 @@ __global__ void __launch_bounds__(kQ1Threads, 1) k_qr_cl1(QrArgs a, Qc1Layout la
 	}
 	__syncthreads();
 	int rank = kq;
-	if (a.pivot)  // the reference's rank rule on R's diagonal: |R_kk| < 16 eps R_00 (signed R_00)
+	if (a.pivot && a.rank_rule)  // the reference's rank rule on R's diagonal: |R_kk| < 16 eps R_00 (signed R_00)
 		for (int k = 1; k < kq; ++k)
 			if (fabs(betas[k]) < 16.0 * DBL_EPSILON * betas[0]) { rank = k; break; }
 	if (me == 0 && tid == 0 && a.rank_out) *a.rank_out = rank;
@@ -1562,7 +1562,7 @@ __global__ void __launch_bounds__(kSvdThreads) k_svd(SvdArgs a, int use_smem) {
 	extern __shared__ double dyn[];
 	__shared__ int s_rot, s_rank;
 	const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5, nwarps = blockDim.x >> 5;
-	const bool tall = a.m >= a.n;
+	const bool tall = a.m > a.n || (a.m == a.n && !a.orth_rows);
 	const int p = tall ? a.m : a.n, q = tall ? a.n : a.m;
 	const int qe = q + (q & 1);
 	double* sig = dyn;
@@ -1733,7 +1733,7 @@ __global__ void __launch_bounds__(kSvcThreads) k_svd_cluster(SvdArgs a, SvcLayou
 	const int me = int(cl.block_rank()), tid = threadIdx.x, lane = tid & 31, warp = tid >> 5, nwarps = blockDim.x >> 5;
 	const int p = lay.p, q = lay.q, qe = lay.qe, P = lay.P, ppc = lay.ppc, cpc = lay.cpc;
 	const size_t cw = lay.colw();
-	const bool tall = a.m >= a.n;
+	const bool tall = a.m > a.n || (a.m == a.n && !a.orth_rows);
 	double* sig = sm + lay.sig();
 	double* flg = sm + lay.flg();
 	int* order = reinterpret_cast<int*>(sm + lay.ord());
@@ -1985,6 +1985,120 @@ void launch_svd(const SvdArgs& a, cudaStream_t s) {
 		attr = true;
 	}
 	k_svd<<<1, kSvdThreads, use_smem ? full : aux, s>>>(a, use_smem);
+	XTT_CUDA(cudaGetLastError());
+}
+
+// ------------------------------------------------------------ QR-preconditioned SVD
+
+constexpr int kSvdPcThreads = 256;
+constexpr int kSvdPcMaxDim = 4096;  // the left epilogue stages m + k <= 4608 doubles (36 KB)
+
+// m >= n: X = Q C, C = U_c S Vt_c, so U = Q U_c (m x rank) and Vt = Vt_c (already in
+// place). CTA j forms column j of U (one warp per row, lanes over Q's row), then fixes
+// the sign gauge: the largest |entry| of the column (lowest index on ties) positive,
+// with row j of Vt flipped alike.
+__global__ void __launch_bounds__(kSvdPcThreads) k_svd_pc_left(const double* __restrict__ Q, int m, int k,
+                                                              const double* __restrict__ Uc, const int* rank_ptr,
+                                                              double* __restrict__ U, double* __restrict__ Vt, int n) {
+	const int j = blockIdx.x, rank = *rank_ptr;
+	if (j >= rank) return;
+	extern __shared__ double sm[];
+	double* uc = sm;      // k
+	double* col = sm + k;  // m
+	__shared__ double s_best[kSvdPcThreads / 32], s_val[kSvdPcThreads / 32];
+	__shared__ int s_idx[kSvdPcThreads / 32];
+	const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5, nwarps = blockDim.x >> 5;
+	for (int l = tid; l < k; l += blockDim.x) uc[l] = Uc[(long long)l * rank + j];
+	__syncthreads();
+	for (int i = warp; i < m; i += nwarps) {
+		const double* qr = Q + (long long)i * k;
+		double acc = 0.0;
+		for (int l = lane; l < k; l += 32) acc = fma(qr[l], uc[l], acc);
+#pragma unroll
+		for (int o = 16; o > 0; o >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, o);
+		if (lane == 0) col[i] = acc;
+	}
+	__syncthreads();
+	double best = -1.0, val = 0.0;
+	int bi = 1 << 30;
+	for (int i = tid; i < m; i += blockDim.x)
+		if (fabs(col[i]) > best) { best = fabs(col[i]); val = col[i]; bi = i; }
+#pragma unroll
+	for (int o = 16; o > 0; o >>= 1) {
+		const double ob = __shfl_xor_sync(0xffffffffu, best, o);
+		const double ov = __shfl_xor_sync(0xffffffffu, val, o);
+		const int oi = __shfl_xor_sync(0xffffffffu, bi, o);
+		if (ob > best || (ob == best && oi < bi)) { best = ob; val = ov; bi = oi; }
+	}
+	if (lane == 0) { s_best[warp] = best; s_val[warp] = val; s_idx[warp] = bi; }
+	__syncthreads();
+	if (tid == 0) {
+		for (int w = 1; w < nwarps; ++w)
+			if (s_best[w] > s_best[0] || (s_best[w] == s_best[0] && s_idx[w] < s_idx[0])) {
+				s_best[0] = s_best[w]; s_val[0] = s_val[w]; s_idx[0] = s_idx[w];
+			}
+	}
+	__syncthreads();
+	const double sg = s_val[0] < 0.0 ? -1.0 : 1.0;
+	for (int i = tid; i < m; i += blockDim.x) U[(long long)i * rank + j] = sg * col[i];
+	if (sg < 0.0)
+		for (int c = tid; c < n; c += blockDim.x) Vt[(long long)j * n + c] = -Vt[(long long)j * n + c];
+}
+
+// m < n: X = C Q, C = U_c S Vt_c, so U = U_c (written in place, its gauge is already
+// the one wanted) and Vt = Vt_c Q (rank x n). CTA j forms row j, threads over Q's row.
+__global__ void __launch_bounds__(kSvdPcThreads) k_svd_pc_right(const double* __restrict__ Q, int k, int n,
+                                                               const double* __restrict__ Vtc, const int* rank_ptr,
+                                                               double* __restrict__ Vt) {
+	const int j = blockIdx.x, rank = *rank_ptr;
+	if (j >= rank) return;
+	extern __shared__ double vr[];  // k
+	for (int l = threadIdx.x; l < k; l += blockDim.x) vr[l] = Vtc[(long long)j * k + l];
+	__syncthreads();
+	for (int c = threadIdx.x; c < n; c += blockDim.x) {
+		double acc = 0.0;
+		for (int l = 0; l < k; ++l) acc = fma(vr[l], Q[(long long)l * n + c], acc);
+		Vt[(long long)j * n + c] = acc;
+	}
+}
+
+bool svd_pc_fits(int m, int n) {
+	const int k = std::min(m, n);
+	SvcLayout lay;
+	return k >= 32 && std::max(m, n) <= kSvdPcMaxDim && svd_cluster_size(k, k, lay) > 1;
+}
+
+void svd_pc_workspace(int m, int n, size_t& q, size_t& c, size_t& qr_work, size_t& svd_work) {
+	const int k = std::min(m, n);
+	q = size_t(m) * n;
+	c = size_t(k) * k;
+	qr_work = m >= n ? qr_work_doubles(m, n) : qr_work_doubles(n, m);
+	svd_work = svd_work_doubles(k, k);
+}
+
+void launch_svd_pc(const SvdArgs& a, const SvdPcWork& w, cudaStream_t s) {
+	const int m = a.m, n = a.n, k = std::min(m, n);
+	XTT_REQUIRE(svd_pc_fits(m, n) && a.rank_out && w.q && w.c, "preconditioned SVD: shape or workspace not covered");
+	const bool tall = m >= n;
+	XTT_REQUIRE(tall ? w.u != nullptr : w.vt != nullptr, "preconditioned SVD: workspace missing");
+	// X P = Q R, all k rows of R kept (pivoting only): tall X = Q C (C = R P^T, k x k),
+	// wide X = C Q with the factorisation of X^T (C = P R^T)
+	QrArgs qa;
+	qa.A = a.X; qa.lda = a.ldx; qa.m = m; qa.n = n; qa.transpose = tall ? 0 : 1; qa.pivot = 1; qa.rank_rule = 0;
+	qa.work = w.qr_work; qa.Q = w.q; qa.C = w.c; qa.rank_out = nullptr; qa.want_q = 1;
+	launch_qr(qa, s);
+	// Jacobi on R^T: the rows of C when tall, the columns of C (= P R^T) when wide
+	SvdArgs sa = a;
+	sa.X = w.c; sa.ldx = k; sa.m = k; sa.n = k; sa.work = w.svd_work; sa.orth_rows = tall ? 1 : 0;
+	sa.U = tall ? w.u : a.U;
+	sa.Vt = tall ? a.Vt : w.vt;
+	launch_svd(sa, s);
+	if (tall) {
+		const size_t smem = size_t(k + m) * sizeof(double);
+		k_svd_pc_left<<<k, kSvdPcThreads, smem, s>>>(w.q, m, k, w.u, a.rank_out, a.U, a.Vt, n);
+	} else {
+		k_svd_pc_right<<<k, kSvdPcThreads, size_t(k) * sizeof(double), s>>>(w.q, k, n, w.vt, a.rank_out, a.Vt);
+	}
 	XTT_CUDA(cudaGetLastError());
 }
 

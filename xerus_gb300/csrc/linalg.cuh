@@ -22,6 +22,7 @@ struct QrArgs {
 	double* C = nullptr;
 	int* rank_out = nullptr;    // device int
 	int want_q = 1;             // 0: only C (the triangular factor) is written, Q is not formed
+	int rank_rule = 1;          // 0 with pivot: keep all min(m, n) rows of R (pivoting only)
 };
 
 struct SvdArgs {
@@ -37,6 +38,7 @@ struct SvdArgs {
 	int* rank_out = nullptr;
 	int* status = nullptr;
 	int max_sweeps = 60;
+	int orth_rows = 0;          // square X only: orthogonalise the rows (Jacobi on X^T) instead of the columns
 };
 
 // Algorithmic work of one factorisation: operand bytes read and written once
@@ -69,5 +71,24 @@ void launch_transfer_small(const TransferArgs& t, cudaStream_t s);
 size_t qr_work_doubles(int m, int n);        // global workspace needed (0 if shared memory suffices)
 void launch_svd(const SvdArgs& a, cudaStream_t s);
 size_t svd_work_doubles(int m, int n);
+
+// Truncated SVD of X (m x n) preconditioned by a column-pivoted QR (Drmac and Veselic,
+// "New fast and accurate Jacobi SVD algorithm", SIAM J. Matrix Anal. Appl. 29 (2008)):
+// X P = Q R, then one-sided Jacobi on R^T, whose columns (the rows of a pivoted R) are
+// graded and nearly orthogonal, so it converges in a few sweeps where Jacobi on X takes
+// tens. Same outputs, rank rule and sign gauge (largest |entry| of each left vector
+// positive) as launch_svd. Workspace: svd_pc_work_doubles(m, n). Returns false (nothing
+// launched) when the shape is not covered; the caller then uses launch_svd.
+struct SvdPcWork {
+	double* q = nullptr;   // m x k or k x n (k = min(m, n))
+	double* c = nullptr;   // k x k
+	double* u = nullptr;   // k x k
+	double* vt = nullptr;  // k x k
+	double* qr_work = nullptr;
+	double* svd_work = nullptr;
+};
+bool svd_pc_fits(int m, int n);
+void svd_pc_workspace(int m, int n, size_t& q, size_t& c, size_t& qr_work, size_t& svd_work);
+void launch_svd_pc(const SvdArgs& a, const SvdPcWork& w, cudaStream_t s);
 
 }  // namespace xtt

@@ -564,6 +564,27 @@ void move_core(Tensor& x, int64_t pos, bool keep_rank) {
 
 // ------------------------------------------------------------ round
 
+void run_svd(Context& c, SvdArgs& a, bool graded) {
+	ProfScope ps(c, "svd");
+	if (graded && c.svd_path == XTT_SVD_PATH_AUTO && svd_pc_fits(a.m, a.n)) {
+		size_t nq, nc, nqr, nsv;
+		svd_pc_workspace(a.m, a.n, nq, nc, nqr, nsv);
+		SvdPcWork w;
+		w.q = c.scratch<double>(S_SVD_PC_Q, nq);
+		w.c = c.scratch<double>(S_SVD_PC_C, nc);
+		(a.m >= a.n ? w.u : w.vt) = c.scratch<double>(S_SVD_PC_UV, nc);
+		w.qr_work = nqr ? c.scratch<double>(S_SVD_PC_QRW, nqr) : nullptr;
+		w.svd_work = nsv ? c.scratch<double>(S_SVD_WORK, nsv) : nullptr;
+		launch_svd_pc(a, w, c.stream);
+		c.count_launch(3);
+		return;
+	}
+	const size_t wk = svd_work_doubles(a.m, a.n);
+	a.work = wk ? c.scratch<double>(S_SVD_WORK, wk) : nullptr;
+	launch_svd(a, c.stream);
+	c.count_launch();
+}
+
 static int svd_into(Context& c, const double* X, int m, int n, int max_rank, double eps, double*& U, double*& S,
                     double*& Vt) {
 	const int q = std::min(m, n);
@@ -572,14 +593,8 @@ static int svd_into(Context& c, const double* X, int m, int n, int max_rank, dou
 	Vt = c.scratch<double>(S_SVD_VT, size_t(q) * n);
 	SvdArgs a;
 	a.X = X; a.ldx = n; a.m = m; a.n = n; a.max_rank = max_rank; a.eps = eps;
-	const size_t wk = svd_work_doubles(m, n);
-	a.work = wk ? c.scratch<double>(S_SVD_WORK, wk) : nullptr;
 	a.U = U; a.S = S; a.Vt = Vt; a.rank_out = c.d_ints + 1; a.status = c.d_status;
-	{
-		ProfScope ps(c, "svd");
-		launch_svd(a, c.stream);
-	}
-	c.count_launch();
+	run_svd(c, a);
 	return c.read_int(1);
 }
 
