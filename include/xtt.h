@@ -221,7 +221,10 @@ typedef struct xtt_als_options {
 	double svd_epsilon;              /* DMRG only, with max_rank > 0: relative singular value cutoff */
 	int32_t exact_environment;       /* DMRG only: 0 reproduces the reference's decreasing half-sweep, which
 	                                    contracts core k (not k+1) into the right environment
-	                                    (src/xerus/algorithms/als.cpp:371); 1 contracts core k+1 */
+	                                    (src/xerus/algorithms/als.cpp:371); 1 contracts core k+1, and the
+	                                    last split of each half-sweep leaves S on the side the next one
+	                                    starts from, so every environment is orthonormal and the local
+	                                    systems keep the operator's condition number */
 	int32_t assume_spd;              /* ALSVariant::assumeSPD (als.h:115), default 1. 0: least squares
 	                                    ||A x - b|| through the projections of A^T A and A^T b (ALS, DMRG,
 	                                    ASD; als.cpp:184-215); the energy is then the residual */

@@ -830,7 +830,11 @@ def als(A: TTOp | None, x: TT, b: TT, sites: int = 1, num_half_sweeps: int = 0, 
                     a_, j1, j2, b_ = xv.shape
                     U, S, Vt = svd_trunc(xv.reshape(a_ * j1, j2 * b_), target_rank[cur], EPSILON, canonical_signs)
                     s = len(S)
-                    if inc:
+                    # exact environment: the last split of a half-sweep leaves the singular
+                    # values on the side the next half-sweep solves first, so the environment
+                    # it builds from this pair stays orthonormal
+                    at_end = (inc and cur == last - sites) or (not inc and cur == first)
+                    if inc != (exact_environment and at_end):
                         x.cores[cur] = U.reshape(a_, j1, s)
                         x.cores[cur + 1] = (S[:, None] * Vt).reshape(s, j2, b_)
                     else:

@@ -946,7 +946,11 @@ AlsReport als(const Tensor* Ap, Tensor& x, const Tensor& b, const AlsOptions& o)
 			run_svd(c, a, true);
 			const int rk = c.read_int(1);
 			XTT_REQUIRE(rk <= rmax[cur + 1], "DMRG split rank exceeds the stack capacity");
-			if (inc) {
+			// exact environment: the last split of a half-sweep leaves S on the side the next
+			// half-sweep solves first, so the environment it builds from this pair stays
+			// orthonormal (otherwise its local systems inherit cond(S)^2)
+			const bool at_end = (inc && cur == last - S) || (!inc && cur == first);
+			if (inc != (o.exact_environment && at_end)) {
 				x.reshape_core(cur, ra, rk);
 				copy_d2d(c, x.core[cur], U, size_t(m) * rk);
 				scale_rows(c, Vt, Sv, rk, nn);
