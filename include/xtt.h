@@ -89,6 +89,16 @@ int xtt_context_set_cg_path(xtt_context* ctx, int path);
 typedef enum xtt_svd_path { XTT_SVD_PATH_AUTO = 0, XTT_SVD_PATH_JACOBI = 1 } xtt_svd_path;
 int xtt_context_set_svd_path(xtt_context* ctx, int path);
 
+/* C (m x n) = A (m x k) B (k x n) on the tensor cores (tcgen05 TF32 MMAs, FP32
+ * accumulation in tensor memory), FP64 row-major device matrices with leading
+ * dimensions lda, ldb, ldc; terms = 3 splits each operand into two TF32 parts
+ * (FP32-level products), terms = 1 is plain TF32. The building block of the
+ * precision forms (no reference counterpart: the reference multiplies in FP64
+ * through BLAS, src/xerus/blasLapackWrapper.cpp:96-147); exposed to check it
+ * against an FP64 product. Asynchronous on the context's stream. */
+int xtt_gemm_tc(xtt_context* ctx, int64_t m, int64_t n, int64_t k, const double* A, int64_t lda, const double* B,
+                int64_t ldb, double* C, int64_t ldc, int32_t terms);
+
 /* ---------------------------------------------------------------- tensors */
 /* TTNetwork(dims) + set_component: a device TT with the given ranks (order+1
  * entries, r_0 = r_d = 1), all cores zero, not canonical.

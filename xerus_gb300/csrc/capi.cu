@@ -144,6 +144,23 @@ int xtt_context_set_cg_path(xtt_context* ctx, int path) {
 	});
 }
 
+int xtt_gemm_tc(xtt_context* ctx, int64_t m, int64_t n, int64_t k, const double* A, int64_t lda, const double* B,
+                int64_t ldb, double* C, int64_t ldc, int32_t terms) {
+	return guard([&] {
+		ARG(ctx && A && B && C, "NULL argument");
+		ARG(m > 0 && n > 0 && k > 0 && m < (1 << 30) && n < (1 << 30) && k < (1 << 30), "illegal GEMM size");
+		ARG(lda >= k && ldb >= n && ldc >= n, "leading dimension smaller than the row");
+		ARG(terms == 1 || terms == 3, "terms must be 1 or 3");
+		xtt::Gemm<double> g;
+		g.M = int(m); g.N = int(n); g.K = int(k);
+		g.A = A; g.sAm = lda; g.sAk = 1;
+		g.B = B; g.sBk = ldb; g.sBn = 1;
+		g.C = C; g.sCm = ldc; g.sCn = 1;
+		g.lens((m - 1) * lda + k, (k - 1) * ldb + n, (m - 1) * ldc + n);
+		xtt::gemm_tc(*ctx->c, g, terms);
+	});
+}
+
 int xtt_context_set_svd_path(xtt_context* ctx, int path) {
 	return guard([&] {
 		ARG(ctx, "ctx is NULL");

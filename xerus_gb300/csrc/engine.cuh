@@ -143,6 +143,10 @@ struct Tensor {
 // Host-side validation of a GEMM descriptor against its operand lengths (throws).
 template <class T>
 void check_gemm(const Gemm<T>& g);
+// The same GEMM on the tensor cores (tcgen05, TF32 products, FP32 accumulation;
+// terms = 3: split TF32 with FP32-level products, terms = 1: plain TF32).
+template <class T>
+void gemm_tc(Context& c, const Gemm<T>& g, int terms);
 
 // Stream-ordered helpers.
 void gemm(Context& c, const Gemm<double>& g);

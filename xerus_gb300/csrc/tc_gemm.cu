@@ -1,0 +1,176 @@
+// Tensor-core (tcgen05, TF32 with FP32 accumulation) tile GEMM for the
+// contractions of the precision forms: the strided batched Gemm<T> descriptor of
+// the sweep engine, C = alpha A B + beta C, operands FP64 or FP32 in global
+// memory. A 128 x 64 output tile per CTA accumulates in 64 tensor-memory columns;
+// 32-deep K chunks are staged (converted on the fly) into a double-buffered
+// shared-memory ring while the previous chunk's MMAs run, one thread issues the
+// MMAs and commits each chunk to the stage's mbarrier.
+//
+// terms = 3 is split TF32: each operand is a = hi + lo with hi = tf32(a) and
+// lo = tf32(a - hi), and A B ~ hi_A hi_B + hi_A lo_B + lo_A hi_B (the lo lo term
+// is below FP32 rounding) — FP32-level products at three MMAs per step.
+// terms = 1 is plain TF32 (11-bit mantissa products).
+#include "engine.cuh"
+#include "tc.cuh"
+
+namespace xtt {
+
+namespace {
+
+constexpr int kTcThreads = 128;  // 4 warps: warp w owns TMEM lanes (= tile rows) 32w .. 32w + 31
+constexpr int kTcM = 128, kTcN = 64;
+constexpr int kTileABytes = kTcM * tc::kTileK * 4;  // 16 KB
+constexpr int kTileBBytes = kTcN * tc::kTileK * 4;  // 8 KB
+
+template <int NT>
+__host__ __device__ constexpr int stage_bytes() {
+	return (NT == 3 ? 2 : 1) * (kTileABytes + kTileBBytes);
+}
+
+template <class T, int NT>
+__global__ void __launch_bounds__(kTcThreads) k_tc_gemm(Gemm<T> g, int* status) {
+	extern __shared__ __align__(1024) unsigned char tsm[];
+	__shared__ __align__(8) uint64_t bar[2];
+	__shared__ uint32_t s_tmem;
+	__shared__ int s_ok;
+	constexpr int SB = stage_bytes<NT>();
+	const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+	const long long tn = (g.N + kTcN - 1) / kTcN, tm = (g.M + kTcM - 1) / kTcM;
+	const long long b = blockIdx.x / (tm * tn), rem = blockIdx.x - b * tm * tn;
+	const int m0 = int(rem / tn) * kTcM, n0 = int(rem % tn) * kTcN;
+	const T* A = g.A + b * g.sAb;
+	const T* B = g.B + b * g.sBb;
+	if (warp == 0) tc::tmem_alloc(&s_tmem, kTcN);
+	if (tid == 0) {
+		tc::mbar_init(&bar[0], 1);
+		tc::mbar_init(&bar[1], 1);
+		tc::mbar_fence_init();
+		s_ok = 1;
+	}
+	tc::fence_before_sync();
+	__syncthreads();
+	tc::fence_after_sync();
+	const uint32_t tmem = s_tmem;
+	const uint32_t base = tc::smem_u32(tsm);
+	const bool a_kfast = g.sAk == 1, b_kfast = g.sBk == 1;
+	const int nk = (g.K + tc::kTileK - 1) / tc::kTileK;
+	constexpr uint32_t idesc = tc::idesc_tf32(kTcM, kTcN);
+	for (int kc = 0; kc < nk; ++kc) {
+		const int st = kc & 1;
+		if (kc >= 2) {
+			if (tid == 0 && s_ok && !tc::mbar_wait(&bar[st], uint32_t(((kc - 2) >> 1) & 1))) s_ok = 0;
+			__syncthreads();  // the MMAs that read this stage are done
+		}
+		unsigned char* sa = tsm + st * SB;
+		unsigned char* sb = sa + (NT == 3 ? 2 : 1) * kTileABytes;
+		const int k0 = kc * tc::kTileK;
+		for (int e = tid; e < kTcM * tc::kTileK; e += kTcThreads) {
+			const int m = a_kfast ? (e >> 5) : (e & (kTcM - 1));
+			const int k = a_kfast ? (e & 31) : (e >> 7);
+			const int gm = m0 + m, gk = k0 + k;
+			const double v = (gm < g.M && gk < g.K) ? double(A[g.offA(gm, gk)]) : 0.0;
+			const float hi = tc::to_tf32(float(v));
+			const uint32_t off = tc::tile_offset(m, k);
+			*reinterpret_cast<float*>(sa + off) = hi;
+			if (NT == 3) *reinterpret_cast<float*>(sa + kTileABytes + off) = tc::to_tf32(float(v - double(hi)));
+		}
+		for (int e = tid; e < kTcN * tc::kTileK; e += kTcThreads) {
+			const int n = b_kfast ? (e >> 5) : (e & (kTcN - 1));
+			const int k = b_kfast ? (e & 31) : (e >> 6);
+			const int gn = n0 + n, gk = k0 + k;
+			const double v = (gn < g.N && gk < g.K) ? double(B[g.offB(gk, gn)]) : 0.0;
+			const float hi = tc::to_tf32(float(v));
+			const uint32_t off = tc::tile_offset(n, k);
+			*reinterpret_cast<float*>(sb + off) = hi;
+			if (NT == 3) *reinterpret_cast<float*>(sb + kTileBBytes + off) = tc::to_tf32(float(v - double(hi)));
+		}
+		tc::fence_async_smem();
+		__syncthreads();
+		if (tid == 0 && s_ok) {
+			tc::fence_after_sync();
+			const uint32_t a_hi = base + st * SB, b_hi = a_hi + (NT == 3 ? 2 : 1) * kTileABytes;
+#pragma unroll
+			for (int s = 0; s < tc::kTileK / 8; ++s) {
+				const uint32_t ko = uint32_t(s) * 2 * tc::kCoreBytes;
+				const bool first = (kc == 0 && s == 0);
+				tc::mma_tf32(tmem, tc::smem_desc(a_hi + ko), tc::smem_desc(b_hi + ko), idesc, !first);
+				if (NT == 3) {
+					tc::mma_tf32(tmem, tc::smem_desc(a_hi + ko), tc::smem_desc(b_hi + kTileBBytes + ko), idesc, true);
+					tc::mma_tf32(tmem, tc::smem_desc(a_hi + kTileABytes + ko), tc::smem_desc(b_hi + ko), idesc, true);
+				}
+			}
+			tc::mma_commit(&bar[st]);
+		}
+	}
+	if (tid == 0 && s_ok && nk > 0 && !tc::mbar_wait(&bar[(nk - 1) & 1], uint32_t(((nk - 1) >> 1) & 1))) s_ok = 0;
+	__syncthreads();
+	tc::fence_after_sync();
+	const bool ok = s_ok != 0;
+	if (ok) {
+		const int m = m0 + warp * 32 + lane;
+		const T* C0 = g.C + b * g.sCb;
+		T* C = g.C + b * g.sCb;
+#pragma unroll
+		for (int c = 0; c < kTcN; c += 16) {
+			float v[16];
+			if (nk > 0) {
+				tc::tmem_ld16(tmem + (uint32_t(warp * 32) << 16) + uint32_t(c), v);
+			} else {
+#pragma unroll
+				for (int i = 0; i < 16; ++i) v[i] = 0.f;
+			}
+			if (m < g.M) {
+#pragma unroll
+				for (int i = 0; i < 16; ++i) {
+					const int n = n0 + c + i;
+					if (n < g.N) {
+						const long long o = g.offC(m, n);
+						const T r = g.alpha * T(v[i]);
+						C[o] = g.beta == T(0) ? r : r + g.beta * C0[o];
+					}
+				}
+			}
+		}
+	} else if (tid == 0) {
+		record_status(status, DEV_TIMEOUT);
+	}
+	tc::fence_before_sync();
+	__syncthreads();
+	if (warp == 0) {
+		tc::fence_after_sync();
+		tc::tmem_dealloc(tmem, kTcN);
+	}
+}
+
+template <class T, int NT>
+void launch_tc(Context& c, const Gemm<T>& g) {
+	static bool attr = false;
+	const int smem = 2 * stage_bytes<NT>() + 1024;
+	if (!attr) {
+		XTT_CUDA(cudaFuncSetAttribute(k_tc_gemm<T, NT>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem));
+		attr = true;
+	}
+	const long long tiles = (long long)g.batch * ((g.M + kTcM - 1) / kTcM) * ((g.N + kTcN - 1) / kTcN);
+	XTT_REQUIRE(tiles < (1ll << 31), "GEMM too large");
+	k_tc_gemm<T, NT><<<unsigned(tiles), kTcThreads, smem, c.stream>>>(g, c.d_status);
+	XTT_CUDA(cudaGetLastError());
+}
+
+}  // namespace
+
+template <class T>
+void gemm_tc(Context& c, const Gemm<T>& g, int terms) {
+	if (g.M <= 0 || g.N <= 0 || g.batch <= 0) return;
+	check_gemm(g);
+	XTT_REQUIRE(!g.D, "internal: the tensor-core GEMM has no C.*D epilogue");
+	XTT_REQUIRE(terms == 1 || terms == 3, "internal: tensor-core GEMM terms must be 1 or 3");
+	const double mn = double(g.batch) * g.M * g.N, mk = double(g.M) * g.K, kn = double(g.K) * g.N;
+	ProfScope ps(c, "gemm_tc", double(sizeof(T)) * (double(g.batch) * (mk + kn) + mn), 2.0 * mn * g.K * terms);
+	if (terms == 3) launch_tc<T, 3>(c, g);
+	else launch_tc<T, 1>(c, g);
+	c.count_launch();
+}
+template void gemm_tc<double>(Context&, const Gemm<double>&, int);
+template void gemm_tc<float>(Context&, const Gemm<float>&, int);
+
+}  // namespace xtt
