@@ -44,7 +44,7 @@ def parse():
     p.add_argument("--workloads", default="all", choices=["all", "headline"],
                    help="all: also time TT round/dot (d=32 r=64), ADF (d=10, 200k samples) and the 4096-instance batch")
     p.add_argument("--batch-count", type=int, default=4096)
-    p.add_argument("--only", choices=["round", "adf", "batch", "dmrg"],
+    p.add_argument("--only", choices=["round", "adf", "batch", "dmrg", "tc"],
                    help="run one secondary workload alone and print its JSON (for profiling)")
     p.add_argument("--adf-iterations", type=int, default=50, help="ADF iterations per timed run")
     return p.parse_args()
@@ -458,6 +458,7 @@ def run_gpu(args):
         wl["round_dot_d32_r64"] = bench_round_dot(xg, ctx, torch, stream, 3, cpu)
         wl["adf_d10_n8_r6_200k"] = bench_adf(xg, ctx, torch, stream, args.adf_iterations, peak, cpu)
         wl["batch_als_cfg4"] = bench_batch(xg, ctx, args.batch_count, 2)
+        wl["als_tc_d20_n8_r128"] = bench_tc_als(xg, ctx, torch, stream, peaks)
         line["workloads"] = wl
     return line
 
@@ -540,6 +541,62 @@ def bench_dmrg(xg, ctx, torch, stream, half_sweeps):
     return out
 
 
+def bench_tc_als(xg, ctx, torch, stream, peaks, rank=128, half_sweeps=2, reps=2):
+    """Ranks >= 64: one-site ALS_SPD on the configuration-3 operator (d=20, n=8,
+    Laplacian sum plus a diagonal potential, operator rank 3; rhs rank 4), random
+    rank-`rank` start, `half_sweeps` half-sweeps. FP64 form vs the mixed form, whose
+    local solves there run on the tensor cores (FP64 refinement of FP32 CG with
+    split-TF32 tcgen05 operator stages). CUDA events on the context's stream, no
+    profiling in the timed runs; one profiled mixed run for the tensor-core GEMM's
+    class figures."""
+    d, n = 20, 8
+    rng = np.random.default_rng(SEED)
+    V = [rng.uniform(0.0, 1.0, n) for _ in range(d)]
+    xg.seed(SEED)
+    A = xg.TTOperator.from_cores(xg.laplacian_cores(d, n, potentials=V, rank3=True), ctx=ctx)
+    b = xg.TTTensor.random([n] * d, 4, ctx=ctx)
+    x0 = xg.TTTensor.random([n] * d, rank, ctx=ctx)
+    x0 /= x0.frob_norm()
+    out = {"workload": f"ALS_SPD d=20 n=8 (configuration-3 operator, rank 3), rhs rank 4, x rank {rank}, "
+                       f"{half_sweeps} half-sweeps", "local_unknowns": rank * n * rank}
+    for name, prec in (("fp64", xg.FP64), ("mixed", xg.MIXED)):
+        v = xg.ALS_SPD.copy()
+        v.convergenceEpsilon = 0.0
+        v.precision = prec
+        v(A, x0.copy(), b, 1)  # warm-up
+        ts = []
+        for _ in range(reps):
+            x = x0.copy()
+            torch.cuda.synchronize()
+            e0, e1 = _events(torch, stream)
+            e0.record(stream)
+            en = v(A, x, b, half_sweeps)
+            e1.record(stream)
+            torch.cuda.synchronize()
+            ts.append(e0.elapsed_time(e1))
+        out[name] = {"ms": statistics.mean(ts), "energy": en, "residual": xg.residual(A, x, b),
+                     "cg_iterations": v.last_report.local_iterations, "refinements": v.last_report.refinements}
+    out["mixed_speedup_vs_fp64"] = out["fp64"]["ms"] / out["mixed"]["ms"]
+    v = xg.ALS_SPD.copy()
+    v.convergenceEpsilon = 0.0
+    v.precision = xg.MIXED
+    ctx.profile(True)
+    v(A, x0.copy(), b, half_sweeps)
+    ctx.profile(False)
+    nl, ms = ctx.profile_get("gemm_tc")
+    by, fl = ctx.profile_work("gemm_tc")
+    tf32_peak = 0.5 * peaks.get("bf16_tflops", 1900.0)
+    ach = fl / (ms / 1e3) / 1e12 if ms > 0 else 0.0
+    out["classes_ms"] = {k: ctx.profile_get(k)[1] for k in ("cg_tc", "cg_fp64", "gemm_tc", "gemm", "qr")}
+    out["roofline_gemm_tc"] = {"kernel": "k_tc_gemm (tcgen05 kind::tf32, 3 MMAs per step)", "bound": "tensor",
+                               "launches": nl, "avg_launch_ms": ms / max(nl, 1),
+                               "algorithmic_flops_per_launch": fl / max(nl, 1), "achieved": ach,
+                               "peak": tf32_peak, "unit": "TFLOP/s", "frac": ach / tf32_peak,
+                               "peak_source": "half of measured bf16 (dense TF32 runs at half the BF16 rate)",
+                               "note": "latency-bound: 4-48 output tiles per stage at these shapes"}
+    return out
+
+
 def run_only(args):
     import torch
     import xerus_gb300 as xg
@@ -557,6 +614,8 @@ def run_only(args):
         return bench_adf(xg, ctx, torch, stream, args.adf_iterations, peaks.get("hbm_gbs", 6800.0), cpu)
     if args.only == "batch":
         return bench_batch(xg, ctx, args.batch_count, args.steps)
+    if args.only == "tc":
+        return bench_tc_als(xg, ctx, torch, stream, peaks)
     return bench_dmrg(xg, ctx, torch, stream, 2)
 
 

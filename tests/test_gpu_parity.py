@@ -218,12 +218,14 @@ def test_als_ragged_dims(ctx, golden):
 
 @pytest.mark.parametrize("precision", ["fp64", "mixed"])
 def test_cg_paths_agree(ctx, golden, precision):
-    """The cluster-resident local CG (default where the local system fits) and the
-    grid-wide kernel give the reference's energy on the rank-32 workload."""
+    """The cluster-resident local CG (default where the local system fits), the
+    grid-wide kernel and (mixed precision) the tensor-core form give the
+    reference's energy on the rank-32 workload."""
     z = golden("als")
     out = {}
+    paths = ("grid", "auto", "tensor") if precision == "mixed" else ("grid", "auto")
     try:
-        for path in ("grid", "auto"):
+        for path in paths:
             ctx.set_cg_path(path)
             A, b, x = dev_op(ctx, op_of(z, "A")), dev_tt(ctx, tt_of(z, "b_r32")), dev_tt(ctx, tt_of(z, "x0_r32"))
             v = xg.ALS_SPD.copy()
@@ -234,8 +236,34 @@ def test_cg_paths_agree(ctx, golden, precision):
             assert abs(out[path][0] / z["r32_hs2_energy"][0] - 1) < REL_TOL
     finally:
         ctx.set_cg_path("auto")
-    # both iterates sit at the local-solve noise floor (1e-13 per local CG), far below 1e-8
-    assert max(out["grid"][1], out["auto"][1]) < 1e-10
+    # every iterate sits at the local-solve noise floor (1e-13 per local CG), far below 1e-8
+    assert max(out[p][1] for p in paths) < 1e-10
+
+
+def test_als_tensor_core_form_at_rank_64(ctx, golden):
+    """Mixed precision at ranks >= 64 takes the tensor-core form by default (FP64
+    refinement of FP32 CG with split-TF32 tcgen05 operator stages): after two
+    half-sweeps from the same start it gives the FP64 form's energy and iterate."""
+    z = golden("als")
+    out = {}
+    for prec in (xg.FP64, xg.MIXED):
+        A, b = dev_op(ctx, op_of(z, "A")), dev_tt(ctx, tt_of(z, "b_r32"))
+        xg.seed(21)
+        x = xg.TTTensor.random([4] * 8, 64, ctx=ctx)
+        x /= x.frob_norm()
+        v = xg.ALS_SPD.copy()
+        v.convergenceEpsilon = 0.0
+        v.precision = prec
+        ctx.profile(True)
+        e = v(A, x, b, 2)
+        ctx.profile(False)
+        out[prec] = (e, x, xg.residual(A, x, b), ctx.profile_get("cg_tc")[0])
+    assert max(x.ranks()) == 64
+    assert out[xg.MIXED][3] > 0 and out[xg.FP64][3] == 0  # the tensor-core form ran (mixed only)
+    assert abs(out[xg.MIXED][0] / out[xg.FP64][0] - 1) < 1e-10
+    xm, xd = out[xg.MIXED][1], out[xg.FP64][1]
+    assert (xm - xd).frob_norm() / xd.frob_norm() < 1e-8
+    assert out[xg.MIXED][2] < 1e-8
 
 
 def test_als_mixed_precision_matches_fp64(ctx, golden):

@@ -72,8 +72,10 @@ class Context:
         return by.value, fl.value
 
     def set_cg_path(self, path):
-        """'auto' (cluster-resident CG where the local system fits) or 'grid'."""
-        L.check(self.lib.xtt_context_set_cg_path(self.handle, {"auto": 0, "grid": 1}[path]))
+        """'auto' (cluster-resident CG where the local system fits; the tensor-core
+        precision form for mixed solves at ranks >= 64), 'grid', or 'tensor' (the
+        tensor-core precision form for every mixed solve)."""
+        L.check(self.lib.xtt_context_set_cg_path(self.handle, {"auto": 0, "grid": 1, "tensor": 2}[path]))
 
     def set_svd_path(self, path):
         """'auto' (QR-preconditioned Jacobi where it fits) or 'jacobi' (plain one-sided Jacobi)."""

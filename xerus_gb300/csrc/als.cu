@@ -351,6 +351,206 @@ static void to_float(Context& c, float* out, const double* in, size_t n) {
 	c.count_launch();
 }
 
+
+// ------------------------------------------------------------ tensor-core mixed solve
+//
+// The precision form of the local solve for large local systems (a rank of 64 or
+// more at the site): iterative refinement against the FP64 residual r = b - M x,
+// whose correction M d = r / ||r|| is solved by CG in FP32 vectors with every
+// operator stage on the tensor cores (split TF32, FP32-level products, FP32
+// accumulation). The host drives the iterations; the CG scalars stay on the
+// device (sums over fixed per-block partials, so every run adds in the same order),
+// and the host reads the residual every kTcCheck iterations.
+
+constexpr int kTcVecThreads = 256;
+constexpr int kTcCheck = 4;
+
+__device__ double sum_partials(const double* part, int G, double* red) {
+	double s = 0;
+	for (int i = threadIdx.x; i < G; i += blockDim.x) s += part[i];
+	return block_sum(s, red);
+}
+
+// part[block] = sum a . b
+__global__ void __launch_bounds__(kTcVecThreads) k_tdot(const float* a, const float* b, long long n, double* part) {
+	__shared__ double red[32];
+	double s = 0;
+	for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x)
+		s = fma(double(a[i]), double(b[i]), s);
+	s = block_sum(s, red);
+	if (threadIdx.x == 0) part[blockIdx.x] = s;
+}
+
+// alpha = rr / (p . q); x += alpha p; r -= alpha q; part2[block] = sum r_new . r_new
+__global__ void __launch_bounds__(kTcVecThreads) k_tcg_step1(float* x, float* r, const float* p, const float* q,
+                                                              long long n, const double* part_pq, int G,
+                                                              const double* rr, double* part2, int* status) {
+	__shared__ double red[32];
+	__shared__ float s_alpha;
+	const double pq = sum_partials(part_pq, G, red);
+	if (threadIdx.x == 0) {
+		const bool good = pq > 0.0 && isfinite(pq);
+		// p = 0 after an exact solve is not a breakdown; p^T M p <= 0 otherwise is
+		if (!good && blockIdx.x == 0 && !(pq == 0.0 && *rr == 0.0)) record_status(status, DEV_BREAKDOWN);
+		s_alpha = good ? float(*rr / pq) : 0.f;
+	}
+	__syncthreads();
+	const float alpha = s_alpha;
+	double s = 0;
+	for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x) {
+		x[i] = fmaf(alpha, p[i], x[i]);
+		const float rv = fmaf(-alpha, q[i], r[i]);
+		r[i] = rv;
+		s = fma(double(rv), double(rv), s);
+	}
+	s = block_sum(s, red);
+	if (threadIdx.x == 0) part2[blockIdx.x] = s;
+}
+
+// rr_new = sum part2; p = r + (rr_new / rr) p; rr_out = rr_new (another slot than rr)
+__global__ void __launch_bounds__(kTcVecThreads) k_tcg_step2(float* p, const float* r, long long n,
+                                                              const double* part2, int G, const double* rr,
+                                                              double* rr_out) {
+	__shared__ double red[32];
+	const double rn = sum_partials(part2, G, red);
+	const float beta = *rr > 0.0 ? float(rn / *rr) : 0.f;
+	for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x)
+		p[i] = fmaf(beta, p[i], r[i]);
+	if (blockIdx.x == 0 && threadIdx.x == 0) *rr_out = rn;
+}
+
+// r = b - q (FP64), part[block] = sum r . r
+__global__ void __launch_bounds__(kTcVecThreads) k_tres(double* r, const double* b, const double* q, long long n,
+                                                         double* part) {
+	__shared__ double red[32];
+	double s = 0;
+	for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x) {
+		const double v = b[i] - q[i];
+		r[i] = v;
+		s = fma(v, v, s);
+	}
+	s = block_sum(s, red);
+	if (threadIdx.x == 0) part[blockIdx.x] = s;
+}
+
+__global__ void __launch_bounds__(kTcVecThreads) k_tsum_partials(const double* part, int G, double* out) {
+	__shared__ double red[32];
+	const double s = sum_partials(part, G, red);
+	if (threadIdx.x == 0) *out = s;
+}
+
+// CG start: r = p = f32(r64 * inr), x = 0
+__global__ void k_tcg_init(float* x, float* r, float* p, const double* r64, double inr, long long n) {
+	for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x) {
+		const float v = float(r64[i] * inr);
+		r[i] = v;
+		p[i] = v;
+		x[i] = 0.f;
+	}
+}
+
+// x64 += f * d
+__global__ void k_tcg_apply(double* x, const float* d, double f, long long n) {
+	for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x)
+		x[i] = fma(f, double(d[i]), x[i]);
+}
+
+__global__ void k_add_counters(int* out, int iters, int refs) {
+	out[0] += iters;
+	out[1] += refs;
+}
+
+// Whether the tensor-core precision form takes this local system.
+static bool use_tc_solve(const Context& c, const LocalShape& s, int precision) {
+	if (precision != XTT_PRECISION_MIXED) return false;
+	if (c.cg_path == XTT_CG_PATH_TENSOR) return true;
+	return c.cg_path == XTT_CG_PATH_AUTO && std::max(s.ra, s.rb) >= 64;
+}
+
+// Returns false when the refinement stalled (x then holds its best iterate and
+// the caller finishes in FP64).
+static bool tc_mixed_solve(Context& c, const LocalShape& s, const MatvecPlan<double>& p64, const MatvecPlan<float>& p32,
+                           const double* b, double* x, double tol, int max_iter, double bb) {
+	const long long n = s.dim();
+	const int G = int(std::max<long long>(1, std::min<long long>(2ll * c.num_sms, (n + kTcVecThreads - 1) / kTcVecThreads)));
+	double* part = c.scratch<double>(S_ALS_FIRST + 26, 2 * size_t(G));
+	double* part2 = part + G;
+	double* r64 = c.scratch<double>(S_ALS_FIRST + 23, size_t(n));
+	double* q64 = c.scratch<double>(S_ALS_FIRST + 25, size_t(n));
+	float* v = c.scratch<float>(S_ALS_FIRST + 31, 4 * size_t(n));
+	float *dx = v, *r = v + n, *p = v + 2 * n, *q = v + 3 * n;
+	double* sc = c.d_dbl + 40;  // [0], [1]: ping-pong rr; [2]: FP64 residual norm^2
+	MatvecPlan<double> m64 = p64;
+	m64.g[0].B = x;
+	m64.g[m64.ns - 1].C = q64;
+	MatvecPlan<float> m32 = p32;
+	m32.g[0].B = p;
+	m32.g[m32.ns - 1].C = q;
+	const unsigned VB = unsigned(G);
+	auto read_dbl = [&](double* d) {
+		XTT_CUDA(cudaMemcpyAsync(c.h_dbl + 40, d, sizeof(double), cudaMemcpyDeviceToHost, c.stream));
+		c.sync();
+		return c.h_dbl[40];
+	};
+	const double inner_tol = 1e-5;
+	int iters = 0, refs = 0;
+	double rr_prev = 0, nr_prev = 0;
+	bool ok = false;
+	for (int ref = 0; ref <= 12; ++ref) {
+		{
+			ProfScope ps(c, "cg_fp64");
+			for (int i = 0; i < m64.ns; ++i) gemm(c, m64.g[i]);
+			k_tres<<<VB, kTcVecThreads, 0, c.stream>>>(r64, b, q64, n, part);
+			k_tsum_partials<<<1, kTcVecThreads, 0, c.stream>>>(part, G, sc + 2);
+			c.count_launch(2);
+			XTT_CUDA(cudaGetLastError());
+		}
+		const double rr = read_dbl(sc + 2);
+		if (ref > 0 && !(rr < rr_prev)) {
+			// the correction did not help: take it back, leave the rest to FP64 CG
+			k_tcg_apply<<<VB, kTcVecThreads, 0, c.stream>>>(x, dx, -nr_prev, n);
+			c.count_launch();
+			break;
+		}
+		if (rr <= tol * tol * bb) {
+			ok = true;
+			break;
+		}
+		if (ref == 12) break;
+		const double nr = std::sqrt(rr);
+		rr_prev = rr;
+		nr_prev = nr;
+		ProfScope ps(c, "cg_tc");
+		k_tcg_init<<<VB, kTcVecThreads, 0, c.stream>>>(dx, r, p, r64, 1.0 / nr, n);
+		k_tdot<<<VB, kTcVecThreads, 0, c.stream>>>(r, r, n, part2);
+		k_tsum_partials<<<1, kTcVecThreads, 0, c.stream>>>(part2, G, sc + 0);
+		c.count_launch(3);
+		int it = 0;
+		while (it < max_iter) {
+			for (int j = 0; j < kTcCheck && it < max_iter; ++j, ++it) {
+				for (int i = 0; i < m32.ns; ++i) gemm_tc(c, m32.g[i], 3);
+				double* rr_in = sc + (it & 1);
+				double* rr_out = sc + ((it + 1) & 1);
+				k_tdot<<<VB, kTcVecThreads, 0, c.stream>>>(p, q, n, part);
+				k_tcg_step1<<<VB, kTcVecThreads, 0, c.stream>>>(dx, r, p, q, n, part, G, rr_in, part2, c.d_status);
+				k_tcg_step2<<<VB, kTcVecThreads, 0, c.stream>>>(p, r, n, part2, G, rr_in, rr_out);
+				c.count_launch(3);
+				XTT_CUDA(cudaGetLastError());
+			}
+			const double rin = read_dbl(sc + (it & 1));  // the normalised start has |r| = 1
+			if (!(rin > inner_tol * inner_tol)) break;
+		}
+		iters += it;
+		k_tcg_apply<<<VB, kTcVecThreads, 0, c.stream>>>(x, dx, nr, n);
+		c.count_launch();
+		++refs;
+	}
+	k_add_counters<<<1, 1, 0, c.stream>>>(c.d_ints + 8, iters, refs);
+	c.count_launch();
+	XTT_CUDA(cudaGetLastError());
+	return ok;
+}
+
 CgResult local_solve(Context& c, const LocalShape& s, const double* L, const double* A1, const double* A2,
                      const double* R, const double* b, double* x, double tol, int max_iter, int precision) {
 	const long long n = s.dim();
@@ -403,7 +603,29 @@ CgResult local_solve(Context& c, const LocalShape& s, const double* L, const dou
 		fp64_solve(nullptr);
 		return res;
 	}
-	if (c.cg_path != XTT_CG_PATH_GRID &&
+	if (use_tc_solve(c, s, precision)) {
+		// FP32 copies of the environments and operator cores, the FP32 operator on the tensor cores
+		const size_t nL = size_t(s.ra) * s.K0 * s.ra, nA1 = size_t(s.K0) * s.n1 * s.n1 * s.K1;
+		const size_t nA2 = s.sites == 2 ? size_t(s.K1) * s.n2 * s.n2 * s.K2 : 0;
+		const size_t nR = size_t(s.rb) * (s.sites == 2 ? s.K2 : s.K1) * s.rb;
+		float* f = c.scratch<float>(S_ALS_FIRST + 27, nL + nA1 + nA2 + nR + 4);
+		to_float(c, f, L, nL);
+		to_float(c, f + nL, A1, nA1);
+		if (nA2) to_float(c, f + nL + nA1, A2, nA2);
+		to_float(c, f + nL + nA1 + nA2, R, nR);
+		float* u1 = c.scratch<float>(S_ALS_FIRST + 28, matvec_tmp_elems(s, 0));
+		float* u2 = c.scratch<float>(S_ALS_FIRST + 29, matvec_tmp_elems(s, 1));
+		float* u3 = c.scratch<float>(S_ALS_FIRST + 30, matvec_tmp_elems(s, 2));
+		const MatvecPlan<float> p32 =
+		    make_matvec_plan<float>(s, f, f + nL, nA2 ? f + nL + nA1 : nullptr, f + nL + nA1 + nA2, u1, u2, u3);
+		dot_async(c, b, b, size_t(n), 12);
+		XTT_CUDA(cudaMemcpyAsync(c.h_dbl + 12, c.d_dbl + 12, sizeof(double), cudaMemcpyDeviceToHost, c.stream));
+		c.sync();
+		const double bb = c.h_dbl[12];
+		if (bb == 0.0 || !tc_mixed_solve(c, s, p64, p32, b, x, tol, max_iter, bb)) fp64_solve(nullptr);
+		return res;
+	}
+	if (c.cg_path != XTT_CG_PATH_GRID && c.cg_path != XTT_CG_PATH_TENSOR &&
 	    cluster_local_solve(c, s, L, A1, A2, R, b, x, tol, max_iter, precision, flag, nullptr)) {
 		fp64_solve(flag);  // FP64 polish, a no-op unless the mixed solve fell short
 		return res;

@@ -139,7 +139,7 @@ int xtt_context_profile_work(xtt_context* ctx, const char* name, double* bytes, 
 int xtt_context_set_cg_path(xtt_context* ctx, int path) {
 	return guard([&] {
 		ARG(ctx, "ctx is NULL");
-		ARG(path == XTT_CG_PATH_AUTO || path == XTT_CG_PATH_GRID, "unknown CG path");
+		ARG(path == XTT_CG_PATH_AUTO || path == XTT_CG_PATH_GRID || path == XTT_CG_PATH_TENSOR, "unknown CG path");
 		ctx->c->cg_path = path;
 	});
 }
