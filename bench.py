@@ -459,6 +459,7 @@ def run_gpu(args):
         wl["adf_d10_n8_r6_200k"] = bench_adf(xg, ctx, torch, stream, args.adf_iterations, peak, cpu)
         wl["batch_als_cfg4"] = bench_batch(xg, ctx, args.batch_count, 2)
         wl["als_tc_d20_n8_r128"] = bench_tc_als(xg, ctx, torch, stream, peaks)
+        wl["dmrg_cfg3_d20_n8"] = bench_dmrg(xg, ctx, torch, stream, 16)
         line["workloads"] = wl
     return line
 
@@ -507,9 +508,11 @@ def run_reference(args):
 
 
 def bench_dmrg(xg, ctx, torch, stream, half_sweeps):
-    """Configuration 3 at the reference's fixed-rank behaviour: two-site DMRG_SPD on
-    the d=20, n=8 Laplacian sum plus a diagonal potential U[0,1] per mode (operator
-    rank 3), random rank-16 start; `half_sweeps` half-sweeps, FP64 and mixed."""
+    """Configuration 3: two-site DMRG_SPD on the d=20, n=8 Laplacian sum plus a
+    diagonal potential U[0,1] per mode (operator rank 3), random rank-16 start,
+    ranks free to grow to 128 with SVD cutoff 1e-10, run until the FP64 residual
+    reaches 1e-8 (checked after every half-sweep) or `half_sweeps` half-sweeps;
+    FP64 and mixed forms, exact (orthonormal) environments."""
     d, n = 20, 8
     rng = np.random.default_rng(SEED)
     V = [rng.uniform(0.0, 1.0, n) for _ in range(d)]
@@ -518,14 +521,16 @@ def bench_dmrg(xg, ctx, torch, stream, half_sweeps):
     b = xg.TTTensor.random([n] * d, 4, ctx=ctx)
     x0 = xg.TTTensor.random([n] * d, 16, ctx=ctx)
     x0 /= x0.frob_norm()
-    out = {"workload": f"DMRG_SPD d=20 n=8, operator rank 3, rank 16 (fixed), {half_sweeps} half-sweeps, "
-                       "exact right environments (the reference's own decreasing sweep stops at the rank-8 ends)",
-           "local_unknowns": 16 * n * n * 16}
+    out = {"workload": "DMRG_SPD d=20 n=8, operator rank 3, rank-16 start, max rank 128, SVD eps 1e-10, "
+                       f"to residual 1e-8 (at most {half_sweeps} half-sweeps), exact environments"}
     for name, prec in (("fp64", xg.FP64), ("mixed", xg.MIXED)):
         v = xg.DMRG_SPD.copy()
         v.convergenceEpsilon = 0.0
         v.precision = prec
         v.exact_environment = True
+        v.max_rank = 128
+        v.svd_epsilon = 1e-10
+        v.residual_target = 1e-8
         v(A, x0.copy(), b, 1)  # warm-up
         x = x0.copy()
         torch.cuda.synchronize()
@@ -535,8 +540,19 @@ def bench_dmrg(xg, ctx, torch, stream, half_sweeps):
         e1.record(stream)
         torch.cuda.synchronize()
         ms = e0.elapsed_time(e1)
-        out[name] = {"ms": ms, "ms_per_half_sweep": ms / half_sweeps, "energy": en,
+        out[name] = {"ms": ms, "half_sweeps": v.last_report.half_sweeps, "energy": en, "max_rank": max(x.ranks()),
                      "cg_iterations": v.last_report.local_iterations, "residual": xg.residual(A, x, b)}
+    v = xg.DMRG_SPD.copy()
+    v.convergenceEpsilon = 0.0
+    v.precision = xg.MIXED
+    v.exact_environment = True
+    v.max_rank = 128
+    v.svd_epsilon = 1e-10
+    v.residual_target = 1e-8
+    ctx.profile(True)
+    v(A, x0.copy(), b, half_sweeps)
+    ctx.profile(False)
+    out["mixed_classes_ms"] = {k: ctx.profile_get(k)[1] for k in ("cg_mixed", "cg_fp64", "cg_tc", "gemm", "qr", "svd")}
     out["mixed_speedup_vs_fp64"] = out["fp64"]["ms"] / out["mixed"]["ms"]
     return out
 
@@ -616,7 +632,7 @@ def run_only(args):
         return bench_batch(xg, ctx, args.batch_count, args.steps)
     if args.only == "tc":
         return bench_tc_als(xg, ctx, torch, stream, peaks)
-    return bench_dmrg(xg, ctx, torch, stream, 2)
+    return bench_dmrg(xg, ctx, torch, stream, 16)
 
 
 def main():

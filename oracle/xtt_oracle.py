@@ -657,16 +657,18 @@ class ALSResult:
 def als_spd(A: TTOp, x: TT, b: TT, sites: int = 1, num_half_sweeps: int = 0, conv_eps: float = 1e-6,
             solver: str = "lapack", preserve_core_position: bool = True, track_residual: bool = False,
             residual_target: float | None = None, canonical_signs: bool = False,
-            exact_environment: bool = False) -> ALSResult:
+            exact_environment: bool = False, max_rank: int = 0, svd_epsilon: float = 0.0) -> ALSResult:
     """ALSVariant::solve for an SPD operator (ALS_SPD, DMRG_SPD, ASD_SPD); see ``als``."""
     return als(A, x, b, sites, num_half_sweeps, conv_eps, solver, preserve_core_position, track_residual,
-               residual_target, canonical_signs, exact_environment, assume_spd=True)
+               residual_target, canonical_signs, exact_environment, assume_spd=True, max_rank=max_rank,
+               svd_epsilon=svd_epsilon)
 
 
 def als(A: TTOp | None, x: TT, b: TT, sites: int = 1, num_half_sweeps: int = 0, conv_eps: float = 1e-6,
         solver: str = "lapack", preserve_core_position: bool = True, track_residual: bool = False,
         residual_target: float | None = None, canonical_signs: bool = False,
-        exact_environment: bool = False, assume_spd: bool = True, use_residual: bool = False) -> ALSResult:
+        exact_environment: bool = False, assume_spd: bool = True, use_residual: bool = False,
+        max_rank: int = 0, svd_epsilon: float = 0.0) -> ALSResult:
     """ALSVariant::solve (src/xerus/algorithms/als.cpp:483-553).
 
     ``x`` is updated in place. ``solver`` is "lapack" (lapack_solver, als.cpp:43-71)
@@ -685,7 +687,10 @@ def als(A: TTOp | None, x: TT, b: TT, sites: int = 1, num_half_sweeps: int = 0, 
     ``canonical_signs`` selects the device's gauge instead of LAPACK's, and
     ``exact_environment`` contracts core ``cur + 1`` (gauge-invariant).
     ``residual_target`` stops at the end of the first half-sweep whose residual
-    is at or below it (a time-to-residual measurement, not a reference feature)."""
+    is at or below it (a time-to-residual measurement, not a reference feature).
+    ``max_rank`` > 0 (two sites) lets the split grow ranks up to that cap (and
+    the bond's maximal rank) with relative cutoff ``svd_epsilon`` — the device's
+    rank-growth extension; the reference keeps the ranks of x."""
     d = x.d
     free = A is None
     normal = not free and not assume_spd
@@ -797,6 +802,11 @@ def als(A: TTOp | None, x: TT, b: TT, sites: int = 1, num_half_sweeps: int = 0, 
 
     energy, last_e, last_e2 = energy_f(), 1e101, 1e102
     record(FLAG_FINISHED_FULLSWEEP)
+    # rank bounds of the growth extension (fixed at x's ranks otherwise)
+    rmax = list(x.ranks)  # rmax[k]: the bond between cores k and k + 1
+    if sites == 2 and max_rank > 0:
+        red = reduce_to_maximal_ranks([max_rank] * (d - 1), x.dims)
+        rmax = [max(r, q) for r, q in zip(x.ranks, red)]
     half = 0
     while True:
         if free:
@@ -828,7 +838,11 @@ def als(A: TTOp | None, x: TT, b: TT, sites: int = 1, num_half_sweeps: int = 0, 
                     x.cores[cur] = xv
                 else:
                     a_, j1, j2, b_ = xv.shape
-                    U, S, Vt = svd_trunc(xv.reshape(a_ * j1, j2 * b_), target_rank[cur], EPSILON, canonical_signs)
+                    if max_rank > 0:
+                        U, S, Vt = svd_trunc(xv.reshape(a_ * j1, j2 * b_), min(max_rank, rmax[cur]), svd_epsilon,
+                                             canonical_signs)
+                    else:
+                        U, S, Vt = svd_trunc(xv.reshape(a_ * j1, j2 * b_), target_rank[cur], EPSILON, canonical_signs)
                     s = len(S)
                     # exact environment: the last split of a half-sweep leaves the singular
                     # values on the side the next half-sweep solves first, so the environment

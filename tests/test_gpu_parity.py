@@ -158,6 +158,41 @@ def test_svd_paths_agree(ctx):
     assert (xa - xj).frob_norm() / xj.frob_norm() < 1e-6
 
 
+@pytest.mark.parametrize("svd_path", ["auto", "jacobi"])
+def test_dmrg_rank_growth(ctx, svd_path):
+    """DMRG with rank growth (max rank 12, SVD cutoff 1e-8, exact environments) on a
+    d=8, n=4 Laplacian with potential: ranks exact, energy and entries against the
+    oracle, through both SVD paths (the preconditioned one drops the rows of the
+    pivoted R far below the cutoff)."""
+    d, n = 8, 4
+    rng = np.random.default_rng(3)
+    V = [rng.uniform(0.0, 1.0, n) for _ in range(d)]
+    cores = xg.laplacian_cores(d, n, potentials=V, rank3=True)
+    xg.seed(5)
+    b = xg.TTTensor.random([n] * d, 3, ctx=ctx)
+    x0 = xg.TTTensor.random([n] * d, 4, ctx=ctx)
+    x0 /= x0.frob_norm()
+    Ah, bh, xh = o.TTOp([np.array(c) for c in cores]), host_tt(b), host_tt(x0)
+    try:
+        ctx.set_svd_path(svd_path)
+        A, x = xg.TTOperator.from_cores(cores, ctx=ctx), x0.copy()
+        v = xg.DMRG_SPD.copy()
+        v.convergenceEpsilon = 0.0
+        v.exact_environment = True
+        v.max_rank = 12
+        v.svd_epsilon = 1e-8
+        energy = v(A, x, b, 3)
+    finally:
+        ctx.set_svd_path("auto")
+    ref = xh.copy()
+    r = o.als_spd(Ah, ref, bh, 2, 3, 0.0, exact_environment=True, max_rank=12, svd_epsilon=1e-8)
+    assert x.ranks() == ref.ranks
+    assert max(x.ranks()) == 12
+    assert abs(energy / r.energy - 1) < 1e-10
+    pos = np.random.default_rng(9).integers(0, n, size=(64, d))
+    assert rel_err(x.entries(pos), o.tt_entries(ref, pos)) < 1e-8
+
+
 def test_round_eps_and_max_ranks(ctx, golden):
     r = golden("round")
     e = tt_of(r, "eps_in", canonicalized=False)

@@ -179,7 +179,7 @@ __global__ void __launch_bounds__(kQrThreads) k_qr(QrArgs a, int use_smem) {
 		if (a.pivot && a.rank_rule) {
 			const double r00 = w(0, 0);
 			for (int k = 1; k < kq; ++k)
-				if (fabs(w(k, k)) < 16.0 * DBL_EPSILON * r00) { rank = k; break; }
+				if (fabs(w(k, k)) < a.rank_tol * r00) { rank = k; break; }
 		}
 		s_rank = rank;
 		if (a.rank_out) *a.rank_out = rank;
@@ -454,7 +454,7 @@ __global__ void __launch_bounds__(kQcThreads) k_qr_cluster(QrArgs a, QcLayout la
 		if (a.pivot && a.rank_rule) {
 			const double r00 = diag[0];
 			for (int k = 1; k < kq; ++k)
-				if (fabs(diag[k]) < 16.0 * DBL_EPSILON * r00) { rank = k; break; }
+				if (fabs(diag[k]) < a.rank_tol * r00) { rank = k; break; }
 		}
 		s_rank = rank;
 		if (me == 0 && a.rank_out) *a.rank_out = rank;
@@ -803,7 +803,7 @@ __global__ void __launch_bounds__(kQ2Threads) k_qr_cl2(QrArgs a, Qc2Layout lay) 
 		if (tid == 0) {
 			int rk = kq;
 			for (int k = 1; k < kq; ++k)
-				if (fabs(tb[k]) < 16.0 * DBL_EPSILON * tb[0]) { rk = k; break; }
+				if (fabs(tb[k]) < a.rank_tol * tb[0]) { rk = k; break; }
 			coef[3] = double(rk);
 		}
 		__syncthreads();
@@ -1153,7 +1153,7 @@ __global__ void __launch_bounds__(kQ1Threads, 1) k_qr_cl1(QrArgs a, Qc1Layout la
 	int rank = kq;
 	if (a.pivot && a.rank_rule)  // the reference's rank rule on R's diagonal: |R_kk| < 16 eps R_00 (signed R_00)
 		for (int k = 1; k < kq; ++k)
-			if (fabs(betas[k]) < 16.0 * DBL_EPSILON * betas[0]) { rank = k; break; }
+			if (fabs(betas[k]) < a.rank_tol * betas[0]) { rank = k; break; }
 	if (me == 0 && tid == 0 && a.rank_out) *a.rank_out = rank;
 	for (long long e = tid; e < (long long)nl * nw; e += kQ1Threads) {
 		const int il = int(e / nw), c = int(e % nw), r = r0 + il;
@@ -2076,28 +2076,54 @@ void svd_pc_workspace(int m, int n, size_t& q, size_t& c, size_t& qr_work, size_
 	svd_work = svd_work_doubles(k, k);
 }
 
-void launch_svd_pc(const SvdArgs& a, const SvdPcWork& w, cudaStream_t s) {
+double svd_pc_row_tol(const SvdArgs& a) {
+	// Rows of the pivoted R with |R_kk| < tol |R_00| are dropped before the Jacobi sweeps.
+	// The dropped block has Frobenius norm <= sqrt(k) tol |R_00| <= sqrt(k) tol S[0], so
+	// with tol = 1e-3 eps / sqrt(k) it moves every singular value by at most 1e-3 of the
+	// truncation threshold eps S[0]. Only for cutoffs well above rounding (eps >= 1e-12);
+	// at the fixed-rank cutoff (8 machine epsilons) every row is kept.
+	const int k = std::min(a.m, a.n);
+	return a.eps >= 1e-12 ? 1e-3 * a.eps / std::sqrt(double(k)) : 0.0;
+}
+
+void launch_svd_pc_qr(const SvdArgs& a, const SvdPcWork& w, int* kept, cudaStream_t s) {
+	const int m = a.m, n = a.n;
+	XTT_REQUIRE(svd_pc_fits(m, n) && w.q && w.c && kept, "preconditioned SVD: shape or workspace not covered");
+	// X P = Q R: tall X = Q C (C = R P^T), wide X = C Q with the factorisation of X^T (C = P R^T);
+	// `kept` receives the number of rows of R kept
+	const double tol = svd_pc_row_tol(a);
+	QrArgs qa;
+	qa.A = a.X; qa.lda = a.ldx; qa.m = m; qa.n = n; qa.transpose = m >= n ? 0 : 1; qa.pivot = 1;
+	qa.rank_rule = tol > 0.0 ? 1 : 0;
+	qa.rank_tol = tol;
+	qa.work = w.qr_work; qa.Q = w.q; qa.C = w.c; qa.rank_out = kept; qa.want_q = 1;
+	launch_qr(qa, s);
+}
+
+void launch_svd_pc(const SvdArgs& a, const SvdPcWork& w, int kk, cudaStream_t s) {
 	const int m = a.m, n = a.n, k = std::min(m, n);
-	XTT_REQUIRE(svd_pc_fits(m, n) && a.rank_out && w.q && w.c, "preconditioned SVD: shape or workspace not covered");
+	XTT_REQUIRE(a.rank_out && kk >= 1 && kk <= k, "preconditioned SVD: rank output missing or kept rows out of range");
 	const bool tall = m >= n;
 	XTT_REQUIRE(tall ? w.u != nullptr : w.vt != nullptr, "preconditioned SVD: workspace missing");
-	// X P = Q R, all k rows of R kept (pivoting only): tall X = Q C (C = R P^T, k x k),
-	// wide X = C Q with the factorisation of X^T (C = P R^T)
-	QrArgs qa;
-	qa.A = a.X; qa.lda = a.ldx; qa.m = m; qa.n = n; qa.transpose = tall ? 0 : 1; qa.pivot = 1; qa.rank_rule = 0;
-	qa.work = w.qr_work; qa.Q = w.q; qa.C = w.c; qa.rank_out = nullptr; qa.want_q = 1;
-	launch_qr(qa, s);
-	// Jacobi on R^T: the rows of C when tall, the columns of C (= P R^T) when wide
+	// Jacobi on R^T: tall, C is kk x n and its rows are orthogonalised (the kernel's wide
+	// orientation; orth_rows when square); wide, C is m x kk and its columns are
 	SvdArgs sa = a;
-	sa.X = w.c; sa.ldx = k; sa.m = k; sa.n = k; sa.work = w.svd_work; sa.orth_rows = tall ? 1 : 0;
+	sa.X = w.c;
+	sa.m = tall ? kk : m;
+	sa.n = tall ? n : kk;
+	sa.ldx = sa.n;
+	sa.work = w.svd_work;
+	sa.orth_rows = (tall && kk == n) ? 1 : 0;
 	sa.U = tall ? w.u : a.U;
 	sa.Vt = tall ? a.Vt : w.vt;
 	launch_svd(sa, s);
 	if (tall) {
-		const size_t smem = size_t(k + m) * sizeof(double);
-		k_svd_pc_left<<<k, kSvdPcThreads, smem, s>>>(w.q, m, k, w.u, a.rank_out, a.U, a.Vt, n);
+		// U = Q U_c: Q is m x kk (ld kk), U_c kk x rank
+		const size_t smem = size_t(kk + m) * sizeof(double);
+		k_svd_pc_left<<<kk, kSvdPcThreads, smem, s>>>(w.q, m, kk, w.u, a.rank_out, a.U, a.Vt, n);
 	} else {
-		k_svd_pc_right<<<k, kSvdPcThreads, size_t(k) * sizeof(double), s>>>(w.q, k, n, w.vt, a.rank_out, a.Vt);
+		// V^T = Vt_c Q: Vt_c is rank x kk, Q kk x n
+		k_svd_pc_right<<<kk, kSvdPcThreads, size_t(kk) * sizeof(double), s>>>(w.q, kk, n, w.vt, a.rank_out, a.Vt);
 	}
 	XTT_CUDA(cudaGetLastError());
 }

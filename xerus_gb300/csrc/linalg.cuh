@@ -23,6 +23,7 @@ struct QrArgs {
 	int* rank_out = nullptr;    // device int
 	int want_q = 1;             // 0: only C (the triangular factor) is written, Q is not formed
 	int rank_rule = 1;          // 0 with pivot: keep all min(m, n) rows of R (pivoting only)
+	double rank_tol = 16 * 2.220446049250313e-16;  // the rank rule: first k with |R_kk| < rank_tol R_00
 };
 
 struct SvdArgs {
@@ -77,8 +78,7 @@ size_t svd_work_doubles(int m, int n);
 // X P = Q R, then one-sided Jacobi on R^T, whose columns (the rows of a pivoted R) are
 // graded and nearly orthogonal, so it converges in a few sweeps where Jacobi on X takes
 // tens. Same outputs, rank rule and sign gauge (largest |entry| of each left vector
-// positive) as launch_svd. Workspace: svd_pc_work_doubles(m, n). Returns false (nothing
-// launched) when the shape is not covered; the caller then uses launch_svd.
+// positive) as launch_svd. Workspace sizes: svd_pc_workspace; shapes: svd_pc_fits.
 struct SvdPcWork {
 	double* q = nullptr;   // m x k or k x n (k = min(m, n))
 	double* c = nullptr;   // k x k
@@ -89,6 +89,12 @@ struct SvdPcWork {
 };
 bool svd_pc_fits(int m, int n);
 void svd_pc_workspace(int m, int n, size_t& q, size_t& c, size_t& qr_work, size_t& svd_work);
-void launch_svd_pc(const SvdArgs& a, const SvdPcWork& w, cudaStream_t s);
+// Phase 1: the pivoted QR; writes to the device int `kept` how many rows of R the
+// Jacobi phase needs (rows below a tolerance tied to a.eps are dropped, see
+// svd_pc_row_tol). Phase 2 (the caller has read `kept` to the host): Jacobi and
+// the factors.
+double svd_pc_row_tol(const SvdArgs& a);
+void launch_svd_pc_qr(const SvdArgs& a, const SvdPcWork& w, int* kept, cudaStream_t s);
+void launch_svd_pc(const SvdArgs& a, const SvdPcWork& w, int kept, cudaStream_t s);
 
 }  // namespace xtt

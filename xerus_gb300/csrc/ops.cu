@@ -575,7 +575,9 @@ void run_svd(Context& c, SvdArgs& a, bool graded) {
 		(a.m >= a.n ? w.u : w.vt) = c.scratch<double>(S_SVD_PC_UV, nc);
 		w.qr_work = nqr ? c.scratch<double>(S_SVD_PC_QRW, nqr) : nullptr;
 		w.svd_work = nsv ? c.scratch<double>(S_SVD_WORK, nsv) : nullptr;
-		launch_svd_pc(a, w, c.stream);
+		launch_svd_pc_qr(a, w, c.d_ints + 4, c.stream);
+		const int kept = c.read_int(4);  // rows of the pivoted R the Jacobi phase needs
+		launch_svd_pc(a, w, kept, c.stream);
 		c.count_launch(3);
 		return;
 	}

@@ -74,10 +74,18 @@ __global__ void __launch_bounds__(kTcThreads) k_tc_gemm(Gemm<T> g, int* status, 
 	// tabulated once so that the staging loops do no index division; -1 marks padding
 	long long* moffA = reinterpret_cast<long long*>(tsm + 2 * SB);
 	long long* noffB = moffA + kTcM;
-	long long* koffA = noffB + kTcN;
+	long long* moffC = noffB + kTcN;
+	long long* noffC = moffC + kTcM;
+	long long* koffA = noffC + kTcN;
 	long long* koffB = koffA + (size_t)cpk * tc::kTileK;
-	for (int i = tid; i < kTcM; i += kTcThreads) moffA[i] = m0 + i < g.M ? g.offA(m0 + i, 0) : -1;
-	for (int i = tid; i < kTcN; i += kTcThreads) noffB[i] = n0 + i < g.N ? g.offB(0, n0 + i) : -1;
+	for (int i = tid; i < kTcM; i += kTcThreads) {
+		moffA[i] = m0 + i < g.M ? g.offA(m0 + i, 0) : -1;
+		moffC[i] = m0 + i < g.M ? g.offC(m0 + i, 0) : -1;
+	}
+	for (int i = tid; i < kTcN; i += kTcThreads) {
+		noffB[i] = n0 + i < g.N ? g.offB(0, n0 + i) : -1;
+		noffC[i] = n0 + i < g.N ? g.offC(0, n0 + i) : -1;
+	}
 	for (int i = tid; i < nk * tc::kTileK; i += kTcThreads) {
 		const int gk = kc0 * tc::kTileK + i;
 		koffA[i] = gk < g.K ? g.offA(0, gk) : -1;
@@ -159,6 +167,7 @@ __global__ void __launch_bounds__(kTcThreads) k_tc_gemm(Gemm<T> g, int* status, 
 	const bool ok = s_ok != 0;
 	if (ok) {
 		const int m = m0 + warp * 32 + lane;
+		const long long om = moffC[warp * 32 + lane];
 		const T* C0 = g.C + b * g.sCb;
 		T* C = g.C + b * g.sCb;
 		// split K: raw partial sums, dense (batch, M, N) per split, summed by k_tc_reduce
@@ -180,7 +189,7 @@ __global__ void __launch_bounds__(kTcThreads) k_tc_gemm(Gemm<T> g, int* status, 
 						if (P) {
 							P[(size_t)m * g.N + n] = v[i];
 						} else {
-							const long long o = g.offC(m, n);
+							const long long o = om + noffC[c + i];
 							const T r = g.alpha * T(v[i]);
 							C[o] = g.beta == T(0) ? r : r + g.beta * C0[o];
 						}
@@ -222,7 +231,7 @@ void launch_tc(Context& c, const Gemm<T>& g) {
 	constexpr int kMaxChunks = 64;  // K offsets tabulated per CTA: at most 64 chunks (2048 K)
 	if (!attr) {
 		XTT_CUDA(cudaFuncSetAttribute(k_tc_gemm<T, NT>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-		                              2 * stage_bytes<NT>() + int(sizeof(long long)) * (kTcM + kTcN + 2 * kMaxChunks * tc::kTileK)));
+		                              2 * stage_bytes<NT>() + int(sizeof(long long)) * (2 * (kTcM + kTcN) + 2 * kMaxChunks * tc::kTileK)));
 		attr = true;
 	}
 	const long long tiles = (long long)g.batch * ((g.M + kTcM - 1) / kTcM) * ((g.N + kTcN - 1) / kTcN);
@@ -237,7 +246,7 @@ void launch_tc(Context& c, const Gemm<T>& g) {
 	const int cpk = (nk + S - 1) / S;
 	S = std::max(1, (nk + cpk - 1) / cpk);
 	XTT_REQUIRE(S == 1 || S * partial_elems <= (1ll << 27), "tensor-core GEMM: K too long for its split-K workspace");
-	const int smem = 2 * stage_bytes<NT>() + int(sizeof(long long)) * (kTcM + kTcN + 2 * cpk * tc::kTileK);
+	const int smem = 2 * stage_bytes<NT>() + int(sizeof(long long)) * (2 * (kTcM + kTcN) + 2 * cpk * tc::kTileK);
 	float* part = S > 1 ? c.scratch<float>(S_GEMM_TC_WORK, size_t(S) * partial_elems) : nullptr;
 	k_tc_gemm<T, NT><<<dim3(unsigned(tiles), unsigned(S)), kTcThreads, smem, c.stream>>>(g, c.d_status, cpk, part);
 	XTT_CUDA(cudaGetLastError());
