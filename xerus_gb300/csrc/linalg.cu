@@ -1550,12 +1550,16 @@ size_t svd_work_doubles(int m, int n) {
 // zeta = (be - al) / (2 ga)), written with zeta's division folded into t:
 // t = sign(zeta) |2 ga| / (|be - al| + sqrt((be - al)^2 + 4 ga^2)), c = rsqrt(1 + t^2),
 // s = c t. Fewer dependent FP64 divisions (each ~400 cycles on GB300).
-__device__ __forceinline__ void jacobi_rotation(double al, double be, double ga, double& c, double& s) {
+__device__ __forceinline__ void jacobi_rotation(double al, double be, double ga, double& c, double& s, double& t) {
 	const double dba = be - al, g2 = 2.0 * ga;
 	const double sg = (dba >= 0.0 ? 1.0 : -1.0) * (ga >= 0.0 ? 1.0 : -1.0);
-	const double t = sg * fabs(g2) / (fabs(dba) + sqrt(fma(dba, dba, g2 * g2)));
+	t = sg * fabs(g2) / (fabs(dba) + sqrt(fma(dba, dba, g2 * g2)));
 	c = rsqrt(fma(t, t, 1.0));
 	s = c * t;
+}
+__device__ __forceinline__ void jacobi_rotation(double al, double be, double ga, double& c, double& s) {
+	double t;
+	jacobi_rotation(al, be, ga, c, s, t);
 }
 
 __global__ void __launch_bounds__(kSvdThreads) k_svd(SvdArgs a, int use_smem) {
@@ -1709,7 +1713,8 @@ constexpr int kSvcThreads = 256;
 
 struct SvcLayout {
 	int p, q, qe, P, ppc, cpc;
-	__host__ __device__ size_t colw() const { return size_t(p) + q; }
+	// a column slot: the B part [0, p), the V part [p, p + q), its squared norm at p + q
+	__host__ __device__ size_t colw() const { return size_t(p) + q + 1; }
 	__host__ __device__ size_t buf(int b) const { return size_t(b) * cpc * colw(); }
 	__host__ __device__ size_t sig() const { return 2 * size_t(cpc) * colw(); }
 	__host__ __device__ size_t flg() const { return sig() + qe; }
@@ -1738,7 +1743,6 @@ __global__ void __launch_bounds__(kSvcThreads) k_svd_cluster(SvdArgs a, SvcLayou
 	double* flg = sm + lay.flg();
 	int* order = reinterpret_cast<int*>(sm + lay.ord());
 	__shared__ int s_rank, s_stop;
-	__shared__ const double* s_src[64];
 	// slot s of this CTA at step t: its tournament position
 	auto slot_pos = [&](int s) {
 		const int pr = me * ppc + (s >> 1);
@@ -1777,39 +1781,79 @@ __global__ void __launch_bounds__(kSvcThreads) k_svd_cluster(SvdArgs a, SvcLayou
 	double na2 = 0;
 	for (int c = 0; c < P; ++c) na2 += sig[c];
 	const double negl = na2 * (0.01 * DBL_EPSILON * DBL_EPSILON);
-	const double tol = DBL_EPSILON * sqrt(double(p));
+	const double tol2 = DBL_EPSILON * DBL_EPSILON * double(p);  // rotate when |ga| > eps sqrt(p) sqrt(al be)
 	int cur = 0, t = 0, sweep = 0;
 	bool converged = (q < 2);
 	bool rot = false;
 	long long steps_left = (long long)a.max_sweeps * (qe - 1);
+	// where the column in this CTA's slot `sl` at step t sits at step tn (push target)
+	auto dest_of = [&](int sl, int tn, int nb) {
+		const int c = svc_col(slot_pos(sl), t, qe);
+		const int k = svc_pos(c, tn, qe);
+		const int opr = k < qe / 2 ? k : qe - 1 - k;
+		const int oc = opr / ppc, os = 2 * (opr % ppc) + (k < qe / 2 ? 0 : 1);
+		return cl.map_shared_rank(sm + lay.buf(nb), oc) + (size_t)os * cw;
+	};
 	while (!converged && steps_left > 0) {
 		double* bc = sm + lay.buf(cur);
+		const int tn = (t + 1) % (qe - 1);
+		// each warp rotates its pair and stores the two columns straight into the slots they
+		// occupy at the next step (remote stores into the other buffer; no separate exchange)
 		for (int lp = warp; lp < ppc; lp += nwarps) {
 			const int pr = me * ppc + lp;
 			if (pr >= qe / 2) continue;
 			const int i = svc_col(pr, t, qe), j = svc_col(qe - 1 - pr, t, qe);
-			if (i >= q || j >= q) continue;
-			double* bi = bc + (size_t)(2 * lp) * cw;
-			double* bj = bc + (size_t)(2 * lp + 1) * cw;
-			double al = 0, be = 0, ga = 0;
-			for (int r = lane; r < p; r += 32) {
-				const double x = bi[r], y = bj[r];
-				al = fma(x, x, al);
-				be = fma(y, y, be);
-				ga = fma(x, y, ga);
+			const double* bi = bc + (size_t)(2 * lp) * cw;
+			const double* bj = bc + (size_t)(2 * lp + 1) * cw;
+			double* di = dest_of(2 * lp, tn, cur ^ 1);
+			double* dj = dest_of(2 * lp + 1, tn, cur ^ 1);
+			bool rotate = false;
+			double c = 1.0, sn = 0.0, tr = 0.0, al = 0.0, be = 0.0, ga = 0.0;
+			if (i < q && j < q) {
+				// squared column norms: computed at the first step of a sweep, then carried
+				// with the columns and updated by each rotation (al - t ga, be + t ga), so
+				// a step needs one dot product instead of three (FP64 pipe)
+				if (t == 0) {
+					for (int r = lane; r < p; r += 32) {
+						const double x = bi[r], y = bj[r];
+						al = fma(x, x, al);
+						be = fma(y, y, be);
+						ga = fma(x, y, ga);
+					}
+					al = warp_sum(al);
+					be = warp_sum(be);
+				} else {
+					for (int r = lane; r < p; r += 32) ga = fma(bi[r], bj[r], ga);
+					al = bi[p + q];
+					be = bj[p + q];
+				}
+				ga = warp_sum(ga);
+				rotate = ga != 0.0 && fmin(al, be) > negl && ga * ga > tol2 * al * be;
+				if (rotate) jacobi_rotation(al, be, ga, c, sn, tr);
+			} else {
+				al = bi[p + q];
+				be = bj[p + q];
 			}
-			al = warp_sum(al);
-			be = warp_sum(be);
-			ga = warp_sum(ga);
-			if (ga != 0.0 && fmin(al, be) > negl && fabs(ga) > tol * sqrt(al * be)) {
-				double c, sn;
-				jacobi_rotation(al, be, ga, c, sn);
+			if (rotate) {
 				for (int r = lane; r < p + q; r += 32) {
 					const double x = bi[r], y = bj[r];
-					bi[r] = c * x - sn * y;
-					bj[r] = sn * x + c * y;
+					di[r] = c * x - sn * y;
+					dj[r] = sn * x + c * y;
+				}
+				if (lane == 0) {
+					di[p + q] = fma(-tr, ga, al);
+					dj[p + q] = fma(tr, ga, be);
 				}
 				rot = true;
+			} else {
+				for (int r = lane; r < p + q; r += 32) {
+					di[r] = bi[r];
+					dj[r] = bj[r];
+				}
+				if (lane == 0) {
+					di[p + q] = al;
+					dj[p + q] = be;
+				}
 			}
 		}
 		const bool last_step = (t == qe - 2);
@@ -1821,13 +1865,15 @@ __global__ void __launch_bounds__(kSvcThreads) k_svd_cluster(SvdArgs a, SvcLayou
 			__syncthreads();
 			if (tid < P) cl.map_shared_rank(flg, tid)[me] = double(s_rot);
 		}
-		cl.sync();
+		cl.sync();  // every column of step tn is in place
 		--steps_left;
+		cur ^= 1;
+		t = tn;
 		if (last_step) {
 			++sweep;
 			if (tid == 0) {
 				int any = 0;
-				for (int c = 0; c < P; ++c) any |= flg[c] != 0.0;
+				for (int c2 = 0; c2 < P; ++c2) any |= flg[c2] != 0.0;
 				s_stop = any ? 0 : 1;
 			}
 			__syncthreads();
@@ -1835,30 +1881,6 @@ __global__ void __launch_bounds__(kSvcThreads) k_svd_cluster(SvdArgs a, SvcLayou
 			rot = false;
 			if (converged) break;  // uniform: every CTA read the same flags
 		}
-		// pull the columns of the next step
-		const int tn = (t + 1) % (qe - 1);
-		if (tid < cpc) {
-			const int pr = me * ppc + (tid >> 1);
-			const double* src = nullptr;
-			if (pr < qe / 2) {
-				const int c = svc_col(slot_pos(tid), tn, qe);
-				const int k = svc_pos(c, t, qe);
-				const int opr = k < qe / 2 ? k : qe - 1 - k;
-				const int oc = opr / ppc, os = 2 * (opr % ppc) + (k < qe / 2 ? 0 : 1);
-				src = cl.map_shared_rank(sm + lay.buf(cur), oc) + (size_t)os * cw;
-			}
-			s_src[tid] = src;
-		}
-		__syncthreads();
-		double* bn = sm + lay.buf(cur ^ 1);
-		for (long long e = tid; e < (long long)cpc * cw; e += blockDim.x) {
-			const int s = int(e / cw), off = int(e % cw);
-			const double* src = s_src[s];
-			bn[e] = src ? src[off] : 0.0;
-		}
-		__syncthreads();
-		cur ^= 1;
-		t = tn;
 	}
 	if (!converged && me == 0 && tid == 0) record_status(a.status, DEV_NOT_CONVERGED);
 	// singular values of this CTA's columns, pushed to every CTA
