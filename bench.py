@@ -158,6 +158,37 @@ def bench_round_dot(xg, ctx, torch, stream, steps, cpu):
                 t[name].append(e0.elapsed_time(e1))
     out = {"workload": "TT move_core + round(32) + dot, d=32 n=4 rank 64, FP64", "ranks_after_round": x.ranks()[:4],
            "ms": {k: statistics.mean(v) for k, v in t.items()}}
+    # precision forms: the contractions on the tensor cores (QR and SVD stay FP64);
+    # singular-value, norm and dot-product errors against the FP64 form
+    x = x0.copy()
+    sp64 = np.array(x.round(32, spectra=True))
+    nrm64, dot64 = x.frob_norm(), xg.dot(x0, y)
+    forms = {}
+    try:
+        for form in ("tf32x3", "tf32"):
+            ctx.set_contraction_precision(form)
+            tf = {"move_core": [], "round": [], "dot": []}
+            for i in range(steps + 1):
+                x = x0.copy()
+                torch.cuda.synchronize()
+                for name, fn in (("move_core", lambda: x.move_core(d - 1)), ("round", lambda: x.round(32)),
+                                 ("dot", lambda: xg.dot(x0, y))):
+                    e0, e1 = _events(torch, stream)
+                    e0.record(stream)
+                    fn()
+                    e1.record(stream)
+                    torch.cuda.synchronize()
+                    if i > 0:
+                        tf[name].append(e0.elapsed_time(e1))
+            x = x0.copy()
+            sp = np.array(x.round(32, spectra=True))
+            forms[form] = {"ms": {k: statistics.mean(v) for k, v in tf.items()},
+                           "singular_value_rel_err_max": float(np.max(np.abs(sp - sp64) / np.abs(sp64))),
+                           "norm_rel_err": abs(x.frob_norm() / nrm64 - 1), "dot_rel_err": abs(xg.dot(x0, y) / dot64 - 1),
+                           "dot_err_over_norms": abs(xg.dot(x0, y) - dot64) / (x0.frob_norm() * y.frob_norm())}
+    finally:
+        ctx.set_contraction_precision("fp64")
+    out["precision_forms"] = forms
     if cpu:
         from oracle import xtt_oracle as o
         xh = o.TT(x0.get_cores(), x0.canonicalized, x0.corePosition)

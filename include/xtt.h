@@ -92,6 +92,15 @@ int xtt_context_set_cg_path(xtt_context* ctx, int path);
 typedef enum xtt_svd_path { XTT_SVD_PATH_AUTO = 0, XTT_SVD_PATH_JACOBI = 1 } xtt_svd_path;
 int xtt_context_set_svd_path(xtt_context* ctx, int path);
 
+/* Precision form of xtt_round, xtt_move_core and xtt_dot (TTNetwork::round,
+ * move_core and the TT dot product, include/xerus/ttNetwork.h:330-420): 0 keeps
+ * every contraction FP64 (the reference's arithmetic); 3 runs the contractions
+ * (R absorption, bond products, singular-vector absorption, the dot-product
+ * zipper) as split-TF32 tensor-core GEMMs with FP32 accumulation, 1 as plain TF32.
+ * The QR and SVD factorisations stay FP64 in every form. Other entry points
+ * (the solvers) always contract in FP64. */
+int xtt_context_set_contraction_precision(xtt_context* ctx, int terms);
+
 /* C (m x n) = A (m x k) B (k x n) on the tensor cores (tcgen05 TF32 MMAs, FP32
  * accumulation in tensor memory), FP64 row-major device matrices with leading
  * dimensions lda, ldb, ldc; terms = 3 splits each operand into two TF32 parts

@@ -193,6 +193,37 @@ def test_dmrg_rank_growth(ctx, svd_path):
     assert rel_err(x.entries(pos), o.tt_entries(ref, pos)) < 1e-8
 
 
+@pytest.mark.parametrize("form,tol", [("tf32x3", 1e-4), ("tf32", 1e-2)])
+def test_round_dot_precision_forms(ctx, golden, form, tol):
+    """Configuration 2's precision forms: the contractions of move_core, round and dot
+    on the tensor cores (QR and SVD FP64). Same ranks; singular values, norm and dot
+    product within the form's error of the FP64 results: per contraction split TF32
+    errs ~5e-7 (FP32 accumulation over K = 256), TF32 ~5e-4, and the 31 absorptions
+    of a d=32 sweep compound them (measured 1.4e-5 and ~3e-3)."""
+    r = golden("round")
+    xg.seed(0xBAADF00D)
+    x = xg.TTTensor.random([4] * 32, 64, 0.0, 0.125, ctx=ctx)
+    y = xg.TTTensor.random([4] * 32, 64, 0.0, 0.125, ctx=ctx)
+    d64 = xg.dot(x, y)
+    try:
+        ctx.set_contraction_precision(form)
+        z = x.copy()
+        sp = np.array(z.round(32, spectra=True))
+        dt = xg.dot(x, y)
+        ctx.profile(True)
+        xg.dot(x, y)
+        ctx.profile(False)
+        assert ctx.profile_get("gemm_tc")[0] > 0  # the contractions ran on the tensor cores
+    finally:
+        ctx.set_contraction_precision("fp64")
+    assert [1] + z.ranks() + [1] == list(r["cfg2_round_ranks"])
+    assert np.max(np.abs(sp - r["cfg2_round_spectra"]) / np.abs(r["cfg2_round_spectra"])) < tol
+    assert abs(z.frob_norm() / r["cfg2_round_norm"][0] - 1) < tol
+    # the dot of independent tensors is far below |x| |y| (cancellation): its error is
+    # measured on the scale of the accumulated products
+    assert abs(dt - d64) / (x.frob_norm() * y.frob_norm()) < tol
+
+
 def test_round_eps_and_max_ranks(ctx, golden):
     r = golden("round")
     e = tt_of(r, "eps_in", canonicalized=False)

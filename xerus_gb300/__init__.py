@@ -77,6 +77,11 @@ class Context:
         tensor-core precision form for every mixed solve)."""
         L.check(self.lib.xtt_context_set_cg_path(self.handle, {"auto": 0, "grid": 1, "tensor": 2}[path]))
 
+    def set_contraction_precision(self, form):
+        """Precision form of round / move_core / dot: 'fp64', 'tf32x3' (split TF32 on the
+        tensor cores) or 'tf32'. QR and SVD stay FP64."""
+        L.check(self.lib.xtt_context_set_contraction_precision(self.handle, {"fp64": 0, "tf32x3": 3, "tf32": 1}[form]))
+
     def set_svd_path(self, path):
         """'auto' (QR-preconditioned Jacobi where it fits) or 'jacobi' (plain one-sided Jacobi)."""
         L.check(self.lib.xtt_context_set_svd_path(self.handle, {"auto": 0, "jacobi": 1}[path]))

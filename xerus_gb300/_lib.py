@@ -81,6 +81,7 @@ _SIGNATURES = {
     "xtt_context_profile_get": (ctypes.c_int, [VP, ctypes.c_char_p, c_int64_p, c_double_p]),
     "xtt_context_set_cg_path": (ctypes.c_int, [VP, ctypes.c_int]),
     "xtt_context_set_svd_path": (ctypes.c_int, [VP, ctypes.c_int]),
+    "xtt_context_set_contraction_precision": (ctypes.c_int, [VP, ctypes.c_int]),
     "xtt_gemm_tc": (ctypes.c_int, [VP, ctypes.c_int64, ctypes.c_int64, ctypes.c_int64, VP, ctypes.c_int64, VP,
                                    ctypes.c_int64, VP, ctypes.c_int64, ctypes.c_int32]),
     "xtt_context_profile_work": (ctypes.c_int, [VP, ctypes.c_char_p, c_double_p, c_double_p]),

@@ -161,6 +161,14 @@ int xtt_gemm_tc(xtt_context* ctx, int64_t m, int64_t n, int64_t k, const double*
 	});
 }
 
+int xtt_context_set_contraction_precision(xtt_context* ctx, int terms) {
+	return guard([&] {
+		ARG(ctx, "ctx is NULL");
+		ARG(terms == 0 || terms == 1 || terms == 3, "contraction precision must be 0 (FP64), 3 (split TF32) or 1 (TF32)");
+		ctx->c->contraction_terms = terms;
+	});
+}
+
 int xtt_context_set_svd_path(xtt_context* ctx, int path) {
 	return guard([&] {
 		ARG(ctx, "ctx is NULL");
@@ -498,6 +506,7 @@ int xtt_random_positions(int64_t num, int64_t order, const int64_t* dims, int64_
 int xtt_move_core(xtt_tensor* x, int64_t position, int keep_rank) {
 	return guard([&] {
 		ARG(x, "NULL argument");
+		xtt::ContractionPrecisionScope ps(*x->t->ctx);
 		xtt::move_core(*x->t, position, keep_rank != 0);
 		x->t->ctx->sync();
 	});
@@ -509,6 +518,7 @@ int xtt_round(xtt_tensor* x, const int64_t* max_ranks, double eps, double* spect
 		ARG(x && (max_ranks || x->t->d == 1), "NULL argument");
 		std::vector<int64_t> mr(max_ranks, max_ranks + (x->t->d - 1));
 		std::vector<double> sp;
+		xtt::ContractionPrecisionScope ps(*x->t->ctx);
 		xtt::round_tt(*x->t, mr, eps, spectra ? &sp : nullptr);
 		x->t->ctx->sync();
 		if (spectra) {
@@ -523,6 +533,7 @@ int xtt_dot(const xtt_tensor* x, const xtt_tensor* y, double* out) {
 	return guard([&] {
 		ARG(x && y && out, "NULL argument");
 		ARG(x->t->ctx == y->t->ctx, "tensors belong to different contexts");
+		xtt::ContractionPrecisionScope ps(*x->t->ctx);
 		*out = xtt::dot(*x->t, *y->t);
 	});
 }

@@ -35,6 +35,11 @@ struct Context {
 	long long launches = 0;
 	int cg_path = XTT_CG_PATH_AUTO;  // xtt_cg_path: which local CG kernel family runs
 	int svd_path = XTT_SVD_PATH_AUTO;  // xtt_svd_path: QR-preconditioned or plain Jacobi SVD
+	// precision form of round / move_core / dot (xtt_context_set_contraction_precision):
+	// 0 FP64 GEMMs; 3 split TF32, 1 TF32 on the tensor cores. Applied only while
+	// `tc_active` is set, which those three entry points do for their duration.
+	int contraction_terms = 0;
+	int tc_active = 0;
 	// batched ALS: the CUDA graph of the last batch launch (replayed while its
 	// signature holds), its pinned descriptor staging, and autotuned launch shapes
 	unsigned long long batch_key = 0;
@@ -94,6 +99,14 @@ struct ProfScope {
 	cudaEvent_t a = nullptr, b = nullptr;
 	ProfScope(Context& cc, const char* n, double bytes = 0, double flops = 0);
 	~ProfScope();
+};
+
+// Applies the context's contraction precision for its scope (round, move_core, dot).
+struct ContractionPrecisionScope {
+	Context& c;
+	int saved;
+	explicit ContractionPrecisionScope(Context& cc) : c(cc), saved(cc.tc_active) { c.tc_active = c.contraction_terms; }
+	~ContractionPrecisionScope() { c.tc_active = saved; }
 };
 
 // Issues the launches of its scope on the context's aux stream.

@@ -309,6 +309,10 @@ static void launch_gemm_sk(Context& c, const Gemm<T>& g) {
 
 void gemm(Context& c, const Gemm<double>& g) {
 	if (g.M <= 0 || g.N <= 0 || g.batch <= 0) return;
+	if (c.tc_active && !g.D && g.K > 0) {  // precision form: the contraction on the tensor cores
+		gemm_tc(c, g, c.tc_active);
+		return;
+	}
 	check_gemm(g);
 	const double mn = double(g.batch) * g.M * g.N, mk = double(g.M) * g.K, kn = double(g.K) * g.N;
 	ProfScope ps(c, "gemm", 8.0 * (double(g.batch) * (mk + kn) + mn), 2.0 * mn * g.K);
