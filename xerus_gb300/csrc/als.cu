@@ -16,6 +16,7 @@
 #include <cooperative_groups.h>
 
 #include "als.cuh"
+#include "tc_tiles.cuh"
 
 namespace xtt {
 
@@ -109,8 +110,16 @@ struct CgOut {
 	double rel_residual;
 };
 
-template <class T, class Grp>
-__device__ bool matvec_dev(const MatvecPlan<T>& plan, const T* in, T* out, const T* dotv, GemmSmem<T>& sm, Grp& grp,
+// Tile engines of the persistent solvers: CUDA-core tiles (FP64 / FP32) or the
+// tensor-core engine (tc::TcEngine, FP32 stages).
+template <class T>
+struct CoreTiles {
+	GemmSmem<T>* sm;
+	__device__ T tiles(const Gemm<T>& g, long long start, long long stride) { return gemm_tiles(g, start, stride, *sm); }
+};
+
+template <class T, class Grp, class E>
+__device__ bool matvec_dev(const MatvecPlan<T>& plan, const T* in, T* out, const T* dotv, E& eng, Grp& grp,
                            T& blk_dot) {
 	for (int s = 0; s < plan.ns; ++s) {
 		Gemm<T> g = plan.g[s];
@@ -119,15 +128,15 @@ __device__ bool matvec_dev(const MatvecPlan<T>& plan, const T* in, T* out, const
 			g.C = out;
 			g.D = dotv;
 		}
-		const T part = gemm_tiles(g, grp.rank(), grp.size(), sm);
+		const T part = eng.tiles(g, grp.rank(), grp.size());
 		if (s == plan.ns - 1) blk_dot = part;
 		else if (!grp.sync()) return false;
 	}
 	return true;
 }
 
-template <class T, class Grp>
-__device__ CgOut cg_body(const CgParams<T>& a, GemmSmem<T>& sm, Grp& grp) {
+template <class T, class Grp, class E>
+__device__ CgOut cg_body(const CgParams<T>& a, E& sm, Grp& grp) {
 	__shared__ double sc[32];
 	CgOut out{0, 0, 0.0};
 	const long long gt = grp.rank() * (long long)blockDim.x + threadIdx.x;
@@ -215,7 +224,8 @@ template <class T, class Grp>
 __global__ void __launch_bounds__(kGemmThreads) k_cg(CgParams<T> a, Grp grp, int* out_i, double* out_d) {
 	if (a.gate && __ldcg(a.gate) == 0) return;  // uniform: every block reads the same flag
 	__shared__ GemmSmem<T> sm;
-	const CgOut o = cg_body(a, sm, grp);
+	CoreTiles<T> eng{&sm};
+	const CgOut o = cg_body(a, eng, grp);
 	if (grp.rank() == 0 && threadIdx.x == 0) {  // counters accumulate over a sweep
 		out_i[0] += o.iterations;
 		out_d[0] = o.rel_residual;
@@ -234,19 +244,11 @@ struct MixedParams {
 	int max_refine;
 	int* flag;               // 1 when the FP64 target was not reached, else 0
 	int* sticky;             // set once FP32 corrections stalled; later solves skip them
+	int* status = nullptr;   // device status (the tensor-core engine's bounded waits)
 };
 
-template <class Grp>
-__global__ void __launch_bounds__(kGemmThreads) k_cg_mixed(MixedParams a, Grp grp, int* out_i, double* out_d) {
-	if (a.sticky && __ldcg(a.sticky) != 0) {  // an earlier solve of this sweep showed FP32 does not help
-		if (blockIdx.x == 0 && threadIdx.x == 0) *a.flag = 1;
-		return;
-	}
-	__shared__ union U {
-		GemmSmem<double> d;
-		GemmSmem<float> f;
-		__device__ U() {}
-	} sm;
+template <class Grp, class E64, class E32>
+__device__ void mixed_body(const MixedParams& a, E64& e64, E32& e32, Grp& grp, int* out_i, double* out_d) {
 	__shared__ double sc[32];
 	const long long gt = grp.rank() * (long long)blockDim.x + threadIdx.x;
 	const long long gs = (long long)grp.size() * blockDim.x;
@@ -259,7 +261,7 @@ __global__ void __launch_bounds__(kGemmThreads) k_cg_mixed(MixedParams a, Grp gr
 	bool reached = false;
 	for (int ref = 0; ok && ref <= a.max_refine; ++ref) {
 		double dummy;
-		if (!matvec_dev(a.p64, a.x, a.q64, (const double*)nullptr, sm.d, grp, dummy)) break;
+		if (!matvec_dev(a.p64, a.x, a.q64, (const double*)nullptr, e64, grp, dummy)) break;
 		if (!grp.sync()) break;
 		double l = 0;
 		for (long long i = gt; i < a.n; i += gs) {
@@ -286,7 +288,7 @@ __global__ void __launch_bounds__(kGemmThreads) k_cg_mixed(MixedParams a, Grp gr
 		nr_prev = nr;
 		for (long long i = gt; i < a.n; i += gs) const_cast<float*>(a.inner.b)[i] = float(a.q64[i] * inr);
 		if (!grp.sync()) break;
-		const CgOut o = cg_body(a.inner, sm.f, grp);
+		const CgOut o = cg_body(a.inner, e32, grp);
 		iters += o.iterations;
 		for (long long i = gt; i < a.n; i += gs) a.x[i] += nr * double(a.inner.x[i]);
 		if (!grp.sync()) break;
@@ -300,7 +302,58 @@ __global__ void __launch_bounds__(kGemmThreads) k_cg_mixed(MixedParams a, Grp gr
 		if (a.flag) *a.flag = failed;
 		if (failed && a.sticky) *a.sticky = 1;
 	}
+}
+
+template <class Grp>
+__global__ void __launch_bounds__(kGemmThreads) k_cg_mixed(MixedParams a, Grp grp, int* out_i, double* out_d) {
+	if (a.sticky && __ldcg(a.sticky) != 0) {  // an earlier solve of this sweep showed FP32 does not help
+		if (blockIdx.x == 0 && threadIdx.x == 0) *a.flag = 1;
+		return;
+	}
+	__shared__ union U {
+		GemmSmem<double> d;
+		GemmSmem<float> f;
+		__device__ U() {}
+	} sm;
+	CoreTiles<double> e64{&sm.d};
+	CoreTiles<float> e32{&sm.f};
+	mixed_body(a, e64, e32, grp, out_i, out_d);
 	if (Grp::kCluster) grp.sync();
+}
+
+// The same solve with the FP32 CG's operator stages on the tensor cores: every CTA
+// holds kPN tensor-memory columns and two mbarriers for the whole launch.
+__global__ void __launch_bounds__(kGemmThreads) k_cg_mixed_tc(MixedParams a, GridGroup grp, int* out_i, double* out_d) {
+	if (a.sticky && __ldcg(a.sticky) != 0) {
+		if (blockIdx.x == 0 && threadIdx.x == 0) *a.flag = 1;
+		return;
+	}
+	extern __shared__ __align__(1024) unsigned char tc_dyn[];
+	__shared__ GemmSmem<double> sm64;
+	__shared__ __align__(8) uint64_t bars[2];
+	__shared__ uint32_t s_tmem;
+	__shared__ int s_ok;
+	__shared__ float fred[32];
+	const int warp = threadIdx.x >> 5;
+	if (warp == 0) tc::tmem_alloc(&s_tmem, tc::kPN);
+	if (threadIdx.x == 0) {
+		tc::mbar_init(&bars[0], 1);
+		tc::mbar_init(&bars[1], 1);
+		tc::mbar_fence_init();
+		s_ok = 1;
+	}
+	tc::fence_before_sync();
+	__syncthreads();
+	tc::fence_after_sync();
+	tc::TcEngine e32{tc_dyn, bars, &s_ok, fred, s_tmem, 0u, a.status};
+	CoreTiles<double> e64{&sm64};
+	mixed_body(a, e64, e32, grp, out_i, out_d);
+	tc::fence_before_sync();
+	__syncthreads();
+	if (warp == 0) {
+		tc::fence_after_sync();
+		tc::tmem_dealloc(s_tmem, tc::kPN);
+	}
 }
 
 template <class F>
@@ -618,6 +671,51 @@ CgResult local_solve(Context& c, const LocalShape& s, const double* L, const dou
 		float* u3 = c.scratch<float>(S_ALS_FIRST + 30, matvec_tmp_elems(s, 2));
 		const MatvecPlan<float> p32 =
 		    make_matvec_plan<float>(s, f, f + nL, nA2 ? f + nL + nA1 : nullptr, f + nL + nA1 + nA2, u1, u2, u3);
+		bool persistent = true;  // the engine tabulates K offsets for at most 512 per stage
+		for (int i = 0; i < p32.ns; ++i) persistent = persistent && p32.g[i].K <= tc::kPMaxChunks * tc::kTileK;
+		if (persistent) {
+			// one cooperative launch: FP64 refinement, FP32 CG with tensor-core operator stages
+			MixedParams m;
+			m.p64 = p64;
+			m.inner.plan = p32;
+			float* v = c.scratch<float>(S_ALS_FIRST + 31, 5 * size_t(n));
+			m.inner.x = v;
+			m.inner.r = v + n;
+			m.inner.p = v + 2 * n;
+			m.inner.q = v + 3 * n;
+			m.inner.b = v + 4 * n;
+			m.inner.n = n;
+			m.inner.max_iter = max_iter;
+			m.inner.tol = 1e-5;  // split-TF32 products: FP32-level
+			m.inner.zero_guess = 1;
+			m.x = x;
+			m.q64 = c.scratch<double>(S_ALS_FIRST + 25, n);
+			m.b = b;
+			m.n = n;
+			m.tol = tol;
+			m.max_refine = 12;
+			m.flag = flag;
+			m.sticky = c.d_ints + 11;
+			m.status = c.d_status;
+			const int smem = tc::kPSmem + 1024;
+			static bool attr = false;
+			if (!attr) {
+				XTT_CUDA(cudaFuncSetAttribute(k_cg_mixed_tc, cudaFuncAttributeMaxDynamicSharedMemorySize, smem));
+				attr = true;
+			}
+			int occ = 0;
+			XTT_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, k_cg_mixed_tc, kGemmThreads, smem));
+			const int G = std::max(1, occ) * c.num_sms;
+			GridGroup g{GridBarrier{c.d_barrier, c.d_barrier + 1, c.d_status}, c.scratch<double>(S_ALS_FIRST + 26, 2 * size_t(G)), 0};
+			void* args[] = {&m, &g, &oi, &od};
+			{
+				ProfScope ps(c, "cg_tc");
+				XTT_CUDA(cudaLaunchCooperativeKernel((void*)k_cg_mixed_tc, dim3(G), dim3(kGemmThreads), args, smem, c.stream));
+			}
+			c.count_launch();
+			fp64_solve(flag);  // FP64 polish, a no-op unless the mixed solve fell short
+			return res;
+		}
 		dot_async(c, b, b, size_t(n), 12);
 		XTT_CUDA(cudaMemcpyAsync(c.h_dbl + 12, c.d_dbl + 12, sizeof(double), cudaMemcpyDeviceToHost, c.stream));
 		c.sync();
