@@ -115,7 +115,8 @@ struct CgOut {
 template <class T>
 struct CoreTiles {
 	GemmSmem<T>* sm;
-	__device__ T tiles(const Gemm<T>& g, long long start, long long stride) { return gemm_tiles(g, start, stride, *sm); }
+	template <class Grp>
+	__device__ T tiles(const Gemm<T>& g, Grp& grp) { return gemm_tiles(g, grp.rank(), grp.size(), *sm); }
 };
 
 template <class T, class Grp, class E>
@@ -128,7 +129,7 @@ __device__ bool matvec_dev(const MatvecPlan<T>& plan, const T* in, T* out, const
 			g.C = out;
 			g.D = dotv;
 		}
-		const T part = eng.tiles(g, grp.rank(), grp.size());
+		const T part = eng.tiles(g, grp);
 		if (s == plan.ns - 1) blk_dot = part;
 		else if (!grp.sync()) return false;
 	}
@@ -245,6 +246,7 @@ struct MixedParams {
 	int* flag;               // 1 when the FP64 target was not reached, else 0
 	int* sticky;             // set once FP32 corrections stalled; later solves skip them
 	int* status = nullptr;   // device status (the tensor-core engine's bounded waits)
+	float* part = nullptr;   // the tensor-core engine's split-K partials
 };
 
 template <class Grp, class E64, class E32>
@@ -345,7 +347,7 @@ __global__ void __launch_bounds__(kGemmThreads) k_cg_mixed_tc(MixedParams a, Gri
 	tc::fence_before_sync();
 	__syncthreads();
 	tc::fence_after_sync();
-	tc::TcEngine e32{tc_dyn, bars, &s_ok, fred, s_tmem, 0u, a.status};
+	tc::TcEngine e32{tc_dyn, bars, &s_ok, fred, s_tmem, 0u, a.status, a.part};
 	CoreTiles<double> e64{&sm64};
 	mixed_body(a, e64, e32, grp, out_i, out_d);
 	tc::fence_before_sync();
@@ -706,6 +708,9 @@ CgResult local_solve(Context& c, const LocalShape& s, const double* L, const dou
 			int occ = 0;
 			XTT_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, k_cg_mixed_tc, kGemmThreads, smem));
 			const int G = std::max(1, occ) * c.num_sms;
+			long long part_elems = 1;
+			for (int i = 0; i < p32.ns; ++i) part_elems = std::max(part_elems, tc::split_k_partials(p32.g[i], G));
+			m.part = c.scratch<float>(S_ALS_FIRST + 9, size_t(part_elems));
 			GridGroup g{GridBarrier{c.d_barrier, c.d_barrier + 1, c.d_status}, c.scratch<double>(S_ALS_FIRST + 26, 2 * size_t(G)), 0};
 			void* args[] = {&m, &g, &oi, &od};
 			{

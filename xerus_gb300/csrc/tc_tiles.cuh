@@ -1,9 +1,11 @@
 // Tensor-core tile engine for the FP32 GEMM stages of a persistent (cooperative)
 // kernel: the same operand staging and tcgen05 TF32 MMAs as k_tc_gemm, driven by
 // the 256 threads of a CTA that keeps its tensor-memory accumulator and its two
-// mbarriers for the whole launch. Tiles of one stage are taken round-robin by the
-// CTAs of the grid (no split K); the caller separates stages with a grid barrier.
-// Split TF32 only (hi*hi + hi*lo + lo*hi per K step, FP32-level products).
+// mbarriers for the whole launch. Work items of one stage (output tiles, split
+// along K when the tiles alone leave CTAs idle) are taken round-robin by the CTAs
+// of the grid; split partials are summed in split order after a grid barrier.
+// The caller separates stages with a grid barrier. Split TF32 only (hi*hi +
+// hi*lo + lo*hi per K step, FP32-level products).
 #pragma once
 
 #include "gemm.cuh"
@@ -20,6 +22,27 @@ constexpr int kPMaxChunks = 16;  // K <= 512 per stage
 // dynamic shared memory the engine uses (after 1024-byte alignment)
 constexpr int kPSmem = 2 * kPStage + int(sizeof(long long)) * (2 * (kPM + kPN) + 2 * kPMaxChunks * kTileK);
 
+// Split of a stage along K: S parts of cpk chunks (identical on the host, which sizes
+// the partials workspace, and on the device).
+__host__ __device__ inline void split_k(const Gemm<float>& g, int grid, int& S, int& cpk) {
+	const long long tiles = (long long)g.batch * ((g.M + kPM - 1) / kPM) * ((g.N + kPN - 1) / kPN);
+	const int nk = (g.K + kTileK - 1) / kTileK;
+	S = 1;
+	if (tiles < grid && nk > 1) {
+		const long long want = (grid + tiles - 1) / tiles;
+		S = int(want < 8 ? want : 8);
+		if (S > nk) S = nk;
+	}
+	cpk = (nk + S - 1) / S;
+	S = cpk > 0 ? (nk + cpk - 1) / cpk : 1;
+}
+__host__ __device__ inline long long split_k_partials(const Gemm<float>& g, int grid) {
+	int S, cpk;
+	split_k(g, grid, S, cpk);
+	const long long tiles = (long long)g.batch * ((g.M + kPM - 1) / kPM) * ((g.N + kPN - 1) / kPN);
+	return S > 1 ? (long long)S * tiles * kPM * kPN : 0;
+}
+
 struct TcEngine {
 	unsigned char* smem;  // kPSmem bytes, 1024-aligned
 	uint64_t* bar;        // two initialised mbarriers
@@ -28,10 +51,13 @@ struct TcEngine {
 	uint32_t tmem;        // kPN tensor-memory columns
 	uint32_t gc;          // chunks committed by this CTA so far
 	int* status;
+	float* part;          // split-K partials (split_k_partials floats for the largest stage)
 
-	// Tiles start, start + stride, ... of g; returns, in thread 0, sum over them of C .* D
-	// (when g.D is set), else 0.
-	__device__ float tiles(const Gemm<float>& g, long long start, long long stride) {
+	// One stage over the grid; returns the sum over this CTA's outputs of C .* D
+	// (when g.D is set), else 0. Ends with every C element written by its CTA (the
+	// caller's grid barrier publishes them).
+	template <class Grp>
+	__device__ float tiles(const Gemm<float>& g, Grp& grp) {
 		const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
 		constexpr int AE = kPM * kTileK / kPThreads, BE = kPN * kTileK / kPThreads;
 		constexpr uint32_t idesc = idesc_tf32(kPM, kPN);
@@ -43,10 +69,15 @@ struct TcEngine {
 		long long* koffB = koffA + kPMaxChunks * kTileK;
 		const uint32_t base = smem_u32(smem);
 		const long long tn = (g.N + kPN - 1) / kPN, tm = (g.M + kPM - 1) / kPM, nt = (long long)g.batch * tm * tn;
-		const int nk = (g.K + kTileK - 1) / kTileK;
+		const int nk_all = (g.K + kTileK - 1) / kTileK;
 		const bool a_kfast = g.sAk == 1, b_kfast = g.sBk == 1;
+		int S, cpk;
+		split_k(g, grp.size(), S, cpk);
 		float dsum = 0.f;
-		for (long long tile = start; tile < nt; tile += stride) {
+		for (long long item = grp.rank(); item < nt * S; item += grp.size()) {
+			const long long tile = item % nt;
+			const int ks = int(item / nt);
+			const int kb = ks * cpk, nk = min(nk_all, kb + cpk) - kb;
 			const long long b = tile / (tm * tn), rem = tile - b * tm * tn;
 			const int m0 = int(rem / tn) * kPM, n0 = int(rem % tn) * kPN;
 			const float* A = g.A + b * g.sAb;
@@ -61,8 +92,9 @@ struct TcEngine {
 				noffC[i] = n0 + i < g.N ? g.offC(0, n0 + i) : -1;
 			}
 			for (int i = tid; i < nk * kTileK; i += kPThreads) {
-				koffA[i] = i < g.K ? g.offA(0, i) : -1;
-				koffB[i] = i < g.K ? g.offB(i, 0) : -1;
+				const int gk = kb * kTileK + i;
+				koffA[i] = gk < g.K ? g.offA(0, gk) : -1;
+				koffB[i] = gk < g.K ? g.offB(gk, 0) : -1;
 			}
 			__syncthreads();
 			for (int kc = 0; kc < nk; ++kc) {
@@ -141,11 +173,15 @@ struct TcEngine {
 				const long long om = moffC[ml];
 				float* C = g.C + b * g.sCb;
 				const float* D = g.D ? g.D + b * g.sCb : nullptr;
+				float* P = S > 1 ? part + ((size_t)ks * nt + tile) * (kPM * kPN) + (size_t)ml * kPN : nullptr;
 #pragma unroll
 				for (int c = 0; c < 32; c += 16) {
 					float v[16];
 					tmem_ld16(tmem + (uint32_t(q * 32) << 16) + uint32_t(h * 32 + c), v);
-					if (m < g.M) {
+					if (P) {
+#pragma unroll
+						for (int i = 0; i < 16; ++i) P[h * 32 + c + i] = v[i];
+					} else if (m < g.M) {
 #pragma unroll
 						for (int i = 0; i < 16; ++i) {
 							const int nl = h * 32 + c + i;
@@ -163,6 +199,25 @@ struct TcEngine {
 			}
 			fence_before_sync();
 			__syncthreads();  // accumulator read and tables consumed before the next tile
+		}
+		if (S > 1) {
+			// a timed-out barrier has recorded its status; the later ones then return at once
+			grp.sync();
+			const long long mn = (long long)g.M * g.N, total = (long long)g.batch * mn;
+			for (long long e = grp.rank() * (long long)kPThreads + tid; e < total;
+			     e += (long long)grp.size() * kPThreads) {
+				const long long b = e / mn, r = e - b * mn;
+				const int m = int(r / g.N), n = int(r - (long long)m * g.N);
+				const long long tile = (b * tm + m / kPM) * tn + n / kPN;
+				const size_t loc = (size_t)(m % kPM) * kPN + (n % kPN);
+				float sacc = 0.f;
+				for (int k = 0; k < S; ++k) sacc += part[((size_t)k * nt + tile) * (kPM * kPN) + loc];
+				float* C = g.C + b * g.sCb;
+				const long long o = g.offC(m, n);
+				const float rr = g.beta == 0.f ? g.alpha * sacc : fmaf(g.alpha, sacc, g.beta * C[o]);
+				C[o] = rr;
+				if (g.D) dsum = fmaf(rr, g.D[b * g.sCb + o], dsum);
+			}
 		}
 		return g.D ? block_sum(dsum, red) : 0.f;
 	}
