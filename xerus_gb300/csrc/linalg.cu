@@ -1562,6 +1562,37 @@ __device__ __forceinline__ void jacobi_rotation(double al, double be, double ga,
 	jacobi_rotation(al, be, ga, c, s, t);
 }
 
+// The same rotation with fewer FP64 instructions (GB300's FP64 pipe retires about
+// one warp instruction per 60 cycles and SM partition): t is the root of
+// F(t) = ga t^2 + (be - al) t - ga with |t| <= 1; an FP32 estimate (inputs scaled by
+// a power of two through their exponent bits) is refined by two Newton steps in
+// FP64 whose divisions use the FP32 reciprocal of F'(t0) (each step squares the
+// relative error, 1e-7 -> 1e-14 -> rounding); c = 1/sqrt(1 + t^2) likewise from the
+// FP32 rsqrt with two FP64 Newton steps, s = c t.
+__device__ __forceinline__ void jacobi_rotation_fast(double al, double be, double ga, double& c, double& s,
+                                                     double& t) {
+	const double dba = be - al;
+	const long long ed = (__double_as_longlong(dba) >> 52) & 0x7ff, eg = (__double_as_longlong(ga) >> 52) & 0x7ff;
+	const long long e = ed > eg ? ed : eg;
+	const double sc = __longlong_as_double((2046 - e) << 52);  // 2^(1023 - e): the larger input to [1, 2)
+	const float df = float(dba * sc), gf = float(ga * sc);
+	const float hf = sqrtf(fmaf(df, df, 4.f * gf * gf));
+	float tf = 2.f * fabsf(gf) / (fabsf(df) + hf);
+	if ((df < 0.f) != (gf < 0.f)) tf = -tf;
+	const float fp = fmaf(2.f * gf, tf, df);  // F'(t0) / sc
+	const double r = double(1.f / fp) * sc;    // ~ 1 / F'(t0)
+	double tt = double(tf);
+	tt = fma(-fma(fma(ga, tt, dba), tt, -ga), r, tt);
+	tt = fma(-fma(fma(ga, tt, dba), tt, -ga), r, tt);
+	const double u = fma(tt, tt, 1.0), hu = 0.5 * u;
+	double y = double(rsqrtf(float(u)));
+	y = y * fma(-hu, y * y, 1.5);
+	y = y * fma(-hu, y * y, 1.5);
+	t = tt;
+	c = y;
+	s = y * tt;
+}
+
 __global__ void __launch_bounds__(kSvdThreads) k_svd(SvdArgs a, int use_smem) {
 	extern __shared__ double dyn[];
 	__shared__ int s_rot, s_rank;
@@ -1829,7 +1860,7 @@ __global__ void __launch_bounds__(kSvcThreads) k_svd_cluster(SvdArgs a, SvcLayou
 				}
 				ga = warp_sum(ga);
 				rotate = ga != 0.0 && fmin(al, be) > negl && ga * ga > tol2 * al * be;
-				if (rotate) jacobi_rotation(al, be, ga, c, sn, tr);
+				if (rotate) jacobi_rotation_fast(al, be, ga, c, sn, tr);
 			} else {
 				al = bi[p + q];
 				be = bj[p + q];
