@@ -332,6 +332,32 @@ def test_als_tensor_core_form_at_rank_64(ctx, golden):
     assert out[xg.MIXED][2] < 1e-8
 
 
+def test_tensor_core_form_deep_stages(ctx, golden):
+    """A rank-10 operator (5 A) at x rank 64: the right-environment stage has K = 640,
+    deeper than the cooperative engine tabulates, so the tensor-core form runs its
+    stages as separate launches (host-driven CG); same energy as the FP64 form."""
+    z = golden("als")
+    A1 = dev_op(ctx, op_of(z, "A"))
+    A = A1 + A1 + A1 + A1 + A1
+    assert max(A.ranks()) == 10
+    b = dev_tt(ctx, tt_of(z, "b_r32"))
+    out = {}
+    for prec in (xg.FP64, xg.MIXED):
+        xg.seed(21)
+        x = xg.TTTensor.random([4] * 8, 64, ctx=ctx)
+        x /= x.frob_norm()
+        v = xg.ALS_SPD.copy()
+        v.convergenceEpsilon = 0.0
+        v.precision = prec
+        ctx.profile(True)
+        e = v(A, x, b, 2)
+        ctx.profile(False)
+        out[prec] = (e, xg.residual(A, x, b), ctx.profile_get("gemm_tc")[0])
+    assert out[xg.MIXED][2] > 0  # the separate-launch tensor-core GEMMs ran
+    assert abs(out[xg.MIXED][0] / out[xg.FP64][0] - 1) < 1e-10
+    assert out[xg.MIXED][1] < 1e-8
+
+
 def test_als_mixed_precision_matches_fp64(ctx, golden):
     z = golden("als")
     A, b = dev_op(ctx, op_of(z, "A")), dev_tt(ctx, tt_of(z, "b_r32"))
