@@ -334,7 +334,7 @@ __global__ void __launch_bounds__(kGemmThreads) k_cg_mixed_tc(MixedParams a, Gri
 	__shared__ GemmSmem<double> sm64;
 	__shared__ __align__(8) uint64_t bars[2];
 	__shared__ uint32_t s_tmem;
-	__shared__ int s_ok;
+	__shared__ int s_ok, s_last;
 	__shared__ float fred[32];
 	const int warp = threadIdx.x >> 5;
 	if (warp == 0) tc::tmem_alloc(&s_tmem, tc::kPN);
@@ -343,13 +343,17 @@ __global__ void __launch_bounds__(kGemmThreads) k_cg_mixed_tc(MixedParams a, Gri
 		tc::mbar_init(&bars[1], 1);
 		tc::mbar_fence_init();
 		s_ok = 1;
+		s_last = -1;
 	}
 	tc::fence_before_sync();
 	__syncthreads();
 	tc::fence_after_sync();
-	tc::TcEngine e32{tc_dyn, bars, &s_ok, fred, s_tmem, 0u, a.status, a.part};
+	tc::TcEngine e32{tc_dyn, bars, &s_ok, &s_last, fred, s_tmem, 0u, a.status, a.part};
 	CoreTiles<double> e64{&sm64};
 	mixed_body(a, e64, e32, grp, out_i, out_d);
+	__syncthreads();
+	// a wait gave up: wait (bounded) once more for the MMAs in flight before freeing TMEM
+	if (threadIdx.x == 0 && !s_ok && s_last >= 0) tc::mbar_wait(&bars[s_last & 1], uint32_t((s_last >> 1) & 1));
 	tc::fence_before_sync();
 	__syncthreads();
 	if (warp == 0) {

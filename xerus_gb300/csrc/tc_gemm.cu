@@ -45,7 +45,7 @@ __global__ void __launch_bounds__(kTcThreads) k_tc_gemm(Gemm<T> g, int* status, 
 	extern __shared__ __align__(1024) unsigned char tsm[];
 	__shared__ __align__(8) uint64_t bar[2];
 	__shared__ uint32_t s_tmem;
-	__shared__ int s_ok;
+	__shared__ int s_ok, s_last;  // s_last: the last chunk committed (-1: none)
 	constexpr int SB = stage_bytes<NT>();
 	constexpr int AE = kTcM * tc::kTileK / kTcThreads, BE = kTcN * tc::kTileK / kTcThreads;
 	const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
@@ -60,6 +60,7 @@ __global__ void __launch_bounds__(kTcThreads) k_tc_gemm(Gemm<T> g, int* status, 
 		tc::mbar_init(&bar[1], 1);
 		tc::mbar_fence_init();
 		s_ok = 1;
+		s_last = -1;
 	}
 	tc::fence_before_sync();
 	__syncthreads();
@@ -159,6 +160,7 @@ __global__ void __launch_bounds__(kTcThreads) k_tc_gemm(Gemm<T> g, int* status, 
 				}
 			}
 			tc::mma_commit(&bar[st]);
+			s_last = kc;
 		}
 	}
 	if (tid == 0 && s_ok && nk > 0 && !tc::mbar_wait(&bar[(nk - 1) & 1], uint32_t(((nk - 1) >> 1) & 1))) s_ok = 0;
@@ -199,6 +201,8 @@ __global__ void __launch_bounds__(kTcThreads) k_tc_gemm(Gemm<T> g, int* status, 
 		}
 	} else if (tid == 0) {
 		record_status(status, DEV_TIMEOUT);
+		// a wait gave up: wait (bounded) once more for the MMAs in flight before freeing TMEM
+		if (s_last >= 0) tc::mbar_wait(&bar[s_last & 1], uint32_t((s_last >> 1) & 1));
 	}
 	tc::fence_before_sync();
 	__syncthreads();

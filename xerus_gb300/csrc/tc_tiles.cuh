@@ -47,6 +47,7 @@ struct TcEngine {
 	unsigned char* smem;  // kPSmem bytes, 1024-aligned
 	uint64_t* bar;        // two initialised mbarriers
 	int* s_ok;            // shared flag: 0 once a wait gave up
+	int* s_last;          // shared: the last chunk index committed (-1: none)
 	float* red;           // 32 floats of shared scratch
 	uint32_t tmem;        // kPN tensor-memory columns
 	uint32_t gc;          // chunks committed by this CTA so far
@@ -160,6 +161,7 @@ struct TcEngine {
 						mma_tf32(tmem, smem_desc(a_hi + kPTileA + ko), smem_desc(b_hi + ko), idesc, true);
 					}
 					mma_commit(&bar[st]);
+					*s_last = int(mygc);
 				}
 			}
 			gc += uint32_t(nk);
