@@ -82,13 +82,14 @@ int xtt_context_profile_work(xtt_context* ctx, const char* name, double* bytes, 
 typedef enum xtt_cg_path { XTT_CG_PATH_AUTO = 0, XTT_CG_PATH_GRID = 1, XTT_CG_PATH_TENSOR = 2 } xtt_cg_path;
 int xtt_context_set_cg_path(xtt_context* ctx, int path);
 
-/* Which SVD runs the DMRG split of xtt_als (the reference calls LAPACK's dgesdd,
- * src/xerus/blasLapackWrapper.cpp:288-340). AUTO: a column-pivoted QR, then one-sided
- * Jacobi on R^T, which converges in a third of the sweeps on the split's decaying
- * spectra, where the smaller side is 32..512; else plain one-sided Jacobi. JACOBI:
- * always plain one-sided Jacobi. xtt_round and xtt_move_core always use plain Jacobi.
- * Both keep the same singular values, truncation rule and sign gauge; results agree to
- * rounding. */
+/* Which SVD runs the truncations (the reference calls LAPACK's dgesdd,
+ * src/xerus/blasLapackWrapper.cpp:288-340). AUTO: for the DMRG split of xtt_als a
+ * column-pivoted QR, then one-sided Jacobi on R^T (a third of the sweeps on the
+ * split's decaying spectra); for xtt_round (and splits the QR path does not take)
+ * FP32 Jacobi sweeps in one CTA, orthogonalised in FP64, then the FP64 Jacobi from
+ * that start (a few sweeps); where the smaller side is 32..512. JACOBI: always plain
+ * FP64 one-sided Jacobi. All keep the same singular values, truncation rule and sign
+ * gauge; results agree to rounding. */
 typedef enum xtt_svd_path { XTT_SVD_PATH_AUTO = 0, XTT_SVD_PATH_JACOBI = 1 } xtt_svd_path;
 int xtt_context_set_svd_path(xtt_context* ctx, int path);
 

@@ -130,7 +130,9 @@ def test_round_cfg2(ctx, golden):
 def test_svd_paths_agree(ctx):
     """The DMRG split through the QR-preconditioned Jacobi SVD (the default; tall
     128 x 128 and wide 64 x 128 splits at rank 16) and through plain one-sided
-    Jacobi: same ranks, same energies, the same iterate to the local CG tolerance."""
+    Jacobi: same ranks, same energies, the same iterate to the local CG tolerance.
+    Rounding through the mixed-precision Jacobi (the default) and plain Jacobi:
+    same ranks, spectra and tensor to rounding."""
     out = {}
     try:
         for path in ("jacobi", "auto"):
@@ -147,9 +149,16 @@ def test_svd_paths_agree(ctx):
             v.convergenceEpsilon = 0.0
             v.exact_environment = True
             e = v(A, xd, b, 2)
-            out[path] = (xd, e, xd.ranks())
+            xg.seed(0xBAADF00D)
+            xr = xg.TTTensor.random([4] * 32, 64, 0.0, 0.125, ctx=ctx)
+            sp = np.array(xr.round(32, spectra=True))
+            out[path] = (xd, e, xd.ranks(), xr, sp)
     finally:
         ctx.set_svd_path("auto")
+    # rounding: the mixed-precision Jacobi (AUTO) and plain FP64 Jacobi
+    assert out["auto"][3].ranks() == out["jacobi"][3].ranks()
+    assert np.max(np.abs(out["auto"][4] - out["jacobi"][4]) / out["jacobi"][4]) < 1e-12
+    assert (out["auto"][3] - out["jacobi"][3]).frob_norm() / out["jacobi"][3].frob_norm() < 1e-12
     assert out["auto"][2] == out["jacobi"][2]
     assert abs(out["auto"][1] / out["jacobi"][1] - 1) < 1e-10
     # the local systems' solutions reach norms ~1e7 here; rounding-level changes of

@@ -109,6 +109,14 @@ struct ContractionPrecisionScope {
 	~ContractionPrecisionScope() { c.tc_active = saved; }
 };
 
+// Keeps the engine's contractions FP64 for its scope (factorisation internals).
+struct Fp64ContractionScope {
+	Context& c;
+	int saved;
+	explicit Fp64ContractionScope(Context& cc) : c(cc), saved(cc.tc_active) { c.tc_active = 0; }
+	~Fp64ContractionScope() { c.tc_active = saved; }
+};
+
 // Issues the launches of its scope on the context's aux stream.
 struct OnAux {
 	Context& c;
@@ -123,10 +131,11 @@ enum ScratchId : int {
 	S_ROUND_X, S_ROUND_QA, S_ROUND_QB, S_ROUND_CA, S_ROUND_CB, S_ZIP_M, S_ZIP_T, S_ZIP_M2,
 	S_RES_CORE0, S_RES_CORE1, S_RES_R, S_RED, S_ENT_META, S_ENT_CORES, S_ENT_OUT,
 	S_RES_CORE0B, S_RES_CORE1B, S_RES_RB, S_QR_WORKB, S_BATCH_META, S_BATCH_WORK, S_BATCH_BACKUP,
-	S_SVD_PC_Q, S_SVD_PC_C, S_SVD_PC_UV, S_SVD_PC_QRW, S_GEMM_TC_WORK,
-	S_ALS_FIRST = 40,
-	S_ADF_FIRST = 104,
-	S_MAX = 168
+	S_SVD_PC_Q, S_SVD_PC_C, S_SVD_PC_UV, S_SVD_PC_QRW, S_GEMM_TC_WORK, S_SVD_PC_CT, S_SVD_PC_UT,
+	S_SVD_MX_W32, S_SVD_MX_W, S_SVD_MX_W2, S_SVD_MX_G, S_SVD_MX_B0,
+	S_ALS_FIRST = 48,
+	S_ADF_FIRST = 112,
+	S_MAX = 176
 };
 
 struct Tensor {

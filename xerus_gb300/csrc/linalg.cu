@@ -1608,7 +1608,10 @@ __global__ void __launch_bounds__(kSvdThreads) k_svd(SvdArgs a, int use_smem) {
 		const int c = int(e / p), i = int(e % p);
 		B[e] = tall ? a.X[(long long)i * a.ldx + c] : a.X[(long long)c * a.ldx + i];
 	}
-	for (long long e = tid; e < (long long)q * q; e += blockDim.x) V[e] = (e / q == e % q) ? 1.0 : 0.0;
+	for (long long e = tid; e < (long long)q * q; e += blockDim.x) {
+		const int c = int(e / q), i = int(e % q);
+		V[e] = (tall && a.V0) ? a.V0[(long long)i * q + c] : (c == i ? 1.0 : 0.0);
+	}
 	__shared__ double s_red[32];
 	double nl = 0;
 	for (long long e = tid; e < (long long)p * q; e += blockDim.x) nl = fma(B[e], B[e], nl);
@@ -1788,8 +1791,9 @@ __global__ void __launch_bounds__(kSvcThreads) k_svd_cluster(SvdArgs a, SvcLayou
 			double v = 0.0;
 			if (pr < qe / 2) {
 				const int c = svc_col(slot_pos(s), 0, qe);
-				if (c < q) {
+				if (c < q && off < p + q) {
 					if (off < p) v = tall ? a.X[(long long)off * a.ldx + c] : a.X[(long long)c * a.ldx + off];
+					else if (tall && a.V0) v = a.V0[(long long)(off - p) * q + c];
 					else v = (off - p == c) ? 1.0 : 0.0;
 				}
 			}
@@ -2153,31 +2157,233 @@ void launch_svd_pc_qr(const SvdArgs& a, const SvdPcWork& w, int* kept, cudaStrea
 	launch_qr(qa, s);
 }
 
-void launch_svd_pc(const SvdArgs& a, const SvdPcWork& w, int kk, cudaStream_t s) {
+// B (cols x rows, row-major) = A^T for A rows x cols with leading dimension lda.
+__global__ void k_transpose_d(const double* __restrict__ A, int rows, int cols, long long lda, double* __restrict__ B) {
+	__shared__ double tile[32][33];
+	const int r0 = blockIdx.y * 32, c0 = blockIdx.x * 32;
+	for (int y = threadIdx.y; y < 32; y += blockDim.y) {
+		const int r = r0 + y, c = c0 + threadIdx.x;
+		if (r < rows && c < cols) tile[y][threadIdx.x] = A[(long long)r * lda + c];
+	}
+	__syncthreads();
+	for (int y = threadIdx.y; y < 32; y += blockDim.y) {
+		const int c = c0 + y, r = r0 + threadIdx.x;
+		if (r < rows && c < cols) B[(long long)c * rows + r] = tile[threadIdx.x][y];
+	}
+}
+
+// m >= n: X = Q C', C' (kk x n) = Ct^T, and the Jacobi SVD of the tall Ct = U_t S Vt_t
+// gives C' = Vt_t^T S U_t^T: U = Q Vt_t^T (m x rank) and Vt = U_t^T (rank x n). CTA j
+// forms column j of U (one warp per row), fixes the sign gauge on it (largest |entry|
+// positive, lowest index on ties) and writes row j of Vt with the same sign.
+__global__ void __launch_bounds__(kSvdPcThreads) k_svd_pc_left_t(const double* __restrict__ Q, int m, int kk,
+                                                                const double* __restrict__ Vtt,
+                                                                const double* __restrict__ Ut, const int* rank_ptr,
+                                                                double* __restrict__ U, double* __restrict__ Vt, int n) {
+	const int j = blockIdx.x, rank = *rank_ptr;
+	if (j >= rank) return;
+	extern __shared__ double sm[];
+	double* uc = sm;        // kk
+	double* col = sm + kk;  // m
+	__shared__ double s_best[kSvdPcThreads / 32], s_val[kSvdPcThreads / 32];
+	__shared__ int s_idx[kSvdPcThreads / 32];
+	const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5, nwarps = blockDim.x >> 5;
+	for (int l = tid; l < kk; l += blockDim.x) uc[l] = Vtt[(long long)j * kk + l];
+	__syncthreads();
+	for (int i = warp; i < m; i += nwarps) {
+		const double* qr = Q + (long long)i * kk;
+		double acc = 0.0;
+		for (int l = lane; l < kk; l += 32) acc = fma(qr[l], uc[l], acc);
+#pragma unroll
+		for (int o = 16; o > 0; o >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, o);
+		if (lane == 0) col[i] = acc;
+	}
+	__syncthreads();
+	double best = -1.0, val = 0.0;
+	int bi = 1 << 30;
+	for (int i = tid; i < m; i += blockDim.x)
+		if (fabs(col[i]) > best) { best = fabs(col[i]); val = col[i]; bi = i; }
+#pragma unroll
+	for (int o = 16; o > 0; o >>= 1) {
+		const double ob = __shfl_xor_sync(0xffffffffu, best, o);
+		const double ov = __shfl_xor_sync(0xffffffffu, val, o);
+		const int oi = __shfl_xor_sync(0xffffffffu, bi, o);
+		if (ob > best || (ob == best && oi < bi)) { best = ob; val = ov; bi = oi; }
+	}
+	if (lane == 0) { s_best[warp] = best; s_val[warp] = val; s_idx[warp] = bi; }
+	__syncthreads();
+	if (tid == 0) {
+		for (int w = 1; w < nwarps; ++w)
+			if (s_best[w] > s_best[0] || (s_best[w] == s_best[0] && s_idx[w] < s_idx[0])) {
+				s_best[0] = s_best[w]; s_val[0] = s_val[w]; s_idx[0] = s_idx[w];
+			}
+	}
+	__syncthreads();
+	const double sg = s_val[0] < 0.0 ? -1.0 : 1.0;
+	for (int i = tid; i < m; i += blockDim.x) U[(long long)i * rank + j] = sg * col[i];
+	for (int c = tid; c < n; c += blockDim.x) Vt[(long long)j * n + c] = sg * Ut[(long long)c * rank + j];
+}
+
+SvdArgs svd_pc_jacobi(const SvdArgs& a, const SvdPcWork& w, int kk, cudaStream_t s) {
 	const int m = a.m, n = a.n, k = std::min(m, n);
 	XTT_REQUIRE(a.rank_out && kk >= 1 && kk <= k, "preconditioned SVD: rank output missing or kept rows out of range");
 	const bool tall = m >= n;
-	XTT_REQUIRE(tall ? w.u != nullptr : w.vt != nullptr, "preconditioned SVD: workspace missing");
-	// Jacobi on R^T: tall, C is kk x n and its rows are orthogonalised (the kernel's wide
-	// orientation; orth_rows when square); wide, C is m x kk and its columns are
+	XTT_REQUIRE(tall ? (w.u && w.ct && w.ut) : w.vt != nullptr, "preconditioned SVD: workspace missing");
+	// Jacobi on R^T, always on the columns of a tall matrix: m >= n, C' (kk x n) is
+	// transposed into Ct (n x kk); m < n, C (m x kk) is used as it is
 	SvdArgs sa = a;
-	sa.X = w.c;
-	sa.m = tall ? kk : m;
-	sa.n = tall ? n : kk;
-	sa.ldx = sa.n;
 	sa.work = w.svd_work;
-	sa.orth_rows = (tall && kk == n) ? 1 : 0;
-	sa.U = tall ? w.u : a.U;
-	sa.Vt = tall ? a.Vt : w.vt;
-	launch_svd(sa, s);
+	sa.orth_rows = 0;
+	sa.V0 = nullptr;
 	if (tall) {
-		// U = Q U_c: Q is m x kk (ld kk), U_c kk x rank
+		const dim3 grid((n + 31) / 32, (kk + 31) / 32), block(32, 8);
+		k_transpose_d<<<grid, block, 0, s>>>(w.c, kk, n, n, w.ct);
+		XTT_CUDA(cudaGetLastError());
+		sa.X = w.ct;
+		sa.m = n;
+		sa.n = kk;
+		sa.ldx = kk;
+		sa.U = w.ut;  // n x rank
+		sa.Vt = w.u;  // rank x kk
+	} else {
+		sa.X = w.c;
+		sa.m = m;
+		sa.n = kk;
+		sa.ldx = kk;
+		sa.U = a.U;   // U = U_c, its gauge already the one wanted
+		sa.Vt = w.vt;
+	}
+	return sa;
+}
+
+void svd_pc_finish(const SvdArgs& a, const SvdPcWork& w, int kk, cudaStream_t s) {
+	const int m = a.m, n = a.n;
+	if (m >= n) {
 		const size_t smem = size_t(kk + m) * sizeof(double);
-		k_svd_pc_left<<<kk, kSvdPcThreads, smem, s>>>(w.q, m, kk, w.u, a.rank_out, a.U, a.Vt, n);
+		k_svd_pc_left_t<<<kk, kSvdPcThreads, smem, s>>>(w.q, m, kk, w.u, w.ut, a.rank_out, a.U, a.Vt, n);
 	} else {
 		// V^T = Vt_c Q: Vt_c is rank x kk, Q kk x n
 		k_svd_pc_right<<<kk, kSvdPcThreads, size_t(kk) * sizeof(double), s>>>(w.q, kk, n, w.vt, a.rank_out, a.Vt);
 	}
+	XTT_CUDA(cudaGetLastError());
+}
+
+// ------------------------------------------------------------ FP32 Jacobi stage
+
+constexpr int kSvf32Threads = 1024;
+
+bool svd_f32_fits(int p, int q) {
+	return q >= 2 && p >= q && (size_t(p) * q + size_t(q) * q) * sizeof(float) <= kDynSmemMax;
+}
+
+// One CTA: B (p x q, column-major) and V (q x q, column-major) in FP32 shared memory;
+// round-robin one-sided Jacobi, one warp per pair, until a sweep rotates nothing at
+// the FP32 threshold (or max_sweeps); W = V written row-major. The input is scaled by
+// the power of two that brings its largest entry to [0.5, 1), so squares and sums
+// stay in FP32 range. Its purpose is a starting rotation for the FP64 sweeps: the
+// FP64 Jacobi started from X W converges in a few sweeps.
+__global__ void __launch_bounds__(kSvf32Threads) k_svd_f32(const double* __restrict__ X, long long ldx, int p, int q,
+                                                          float* __restrict__ W, int max_sweeps) {
+	extern __shared__ float fsm[];
+	float* B = fsm;
+	float* V = fsm + (size_t)p * q;
+	__shared__ double d_red[32];
+	__shared__ float f_red[32];
+	__shared__ int s_rot;
+	const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5, nwarps = blockDim.x >> 5;
+	// scale: the exponent of max |X| (non-negative doubles order like their bit patterns)
+	long long mx = 0;
+	for (long long e = tid; e < (long long)p * q; e += blockDim.x) {
+		const int i = int(e / q), c = int(e % q);
+		const long long bits = __double_as_longlong(X[(long long)i * ldx + c]) & 0x7fffffffffffffffLL;
+		mx = bits > mx ? bits : mx;
+	}
+	{
+		double dm = __longlong_as_double(mx);
+#pragma unroll
+		for (int o = 16; o > 0; o >>= 1) dm = fmax(dm, __shfl_xor_sync(0xffffffffu, dm, o));
+		if (lane == 0) d_red[warp] = dm;
+		__syncthreads();
+		if (tid == 0) {
+			double m2 = 0;
+			for (int w = 0; w < nwarps; ++w) m2 = fmax(m2, d_red[w]);
+			d_red[0] = m2;
+		}
+		__syncthreads();
+	}
+	const long long ex = (__double_as_longlong(d_red[0]) >> 52) & 0x7ff;
+	const double scale = ex > 0 ? __longlong_as_double((2045 - ex) << 52) : 1.0;  // 2^(1022 - ex)
+	for (long long e = tid; e < (long long)p * q; e += blockDim.x) {
+		const int i = int(e / q), c = int(e % q);
+		B[(size_t)c * p + i] = float(X[(long long)i * ldx + c] * scale);
+	}
+	for (long long e = tid; e < (long long)q * q; e += blockDim.x) V[e] = (e / q == e % q) ? 1.f : 0.f;
+	__syncthreads();
+	float fl = 0.f;
+	for (long long e = tid; e < (long long)p * q; e += blockDim.x) fl = fmaf(B[e], B[e], fl);
+	const float fro = block_sum(fl, f_red);
+	const float negl = fro * 1e-12f;
+	const float tol = 4.f * sqrtf(float(p)) * FLT_EPSILON;
+	const int qe = q + (q & 1);
+	for (int sweep = 0; sweep < max_sweeps; ++sweep) {
+		if (tid == 0) s_rot = 0;
+		__syncthreads();
+		for (int t = 0; t < qe - 1; ++t) {
+			for (int lp = warp; lp < qe / 2; lp += nwarps) {
+				const int i = svc_col(lp, t, qe), j = svc_col(qe - 1 - lp, t, qe);
+				if (i >= q || j >= q) continue;
+				float* bi = B + (size_t)i * p;
+				float* bj = B + (size_t)j * p;
+				float al = 0.f, be = 0.f, ga = 0.f;
+				for (int r = lane; r < p; r += 32) {
+					const float x = bi[r], y = bj[r];
+					al = fmaf(x, x, al);
+					be = fmaf(y, y, be);
+					ga = fmaf(x, y, ga);
+				}
+				al = warp_sum(al);
+				be = warp_sum(be);
+				ga = warp_sum(ga);
+				if (ga != 0.f && fminf(al, be) > negl && fabsf(ga) > tol * sqrtf(al * be)) {
+					const float dba = be - al, g2 = 2.f * ga;
+					float tt = fabsf(g2) / (fabsf(dba) + sqrtf(fmaf(dba, dba, g2 * g2)));
+					if ((dba < 0.f) != (ga < 0.f)) tt = -tt;
+					const float cs = rsqrtf(fmaf(tt, tt, 1.f)), sn = cs * tt;
+					for (int r = lane; r < p; r += 32) {
+						const float x = bi[r], y = bj[r];
+						bi[r] = cs * x - sn * y;
+						bj[r] = sn * x + cs * y;
+					}
+					float* vi = V + (size_t)i * q;
+					float* vj = V + (size_t)j * q;
+					for (int r = lane; r < q; r += 32) {
+						const float x = vi[r], y = vj[r];
+						vi[r] = cs * x - sn * y;
+						vj[r] = sn * x + cs * y;
+					}
+					if (lane == 0) s_rot = 1;
+				}
+			}
+			__syncthreads();
+		}
+		if (s_rot == 0) break;  // uniform: read after the last step's barrier
+		__syncthreads();         // everyone has read s_rot before it is reset
+	}
+	for (long long e = tid; e < (long long)q * q; e += blockDim.x) {
+		const int i = int(e / q), c = int(e % q);
+		W[e] = V[(size_t)c * q + i];
+	}
+}
+
+void launch_svd_f32(const double* X, long long ldx, int p, int q, float* W, cudaStream_t s) {
+	XTT_REQUIRE(svd_f32_fits(p, q), "internal: FP32 Jacobi stage does not fit one CTA");
+	static bool attr = false;
+	if (!attr) {
+		XTT_CUDA(cudaFuncSetAttribute(k_svd_f32, cudaFuncAttributeMaxDynamicSharedMemorySize, int(kDynSmemMax)));
+		attr = true;
+	}
+	const size_t smem = (size_t(p) * q + size_t(q) * q) * sizeof(float);
+	k_svd_f32<<<1, kSvf32Threads, smem, s>>>(X, ldx, p, q, W, 30);
 	XTT_CUDA(cudaGetLastError());
 }
 

@@ -40,6 +40,8 @@ struct SvdArgs {
 	int* status = nullptr;
 	int max_sweeps = 60;
 	int orth_rows = 0;          // square X only: orthogonalise the rows (Jacobi on X^T) instead of the columns
+	const double* V0 = nullptr; // columns orthogonalised (tall): the starting right factor (n x n row-major)
+	                            // instead of the identity; X is then X_orig V0 and V = V0 J
 };
 
 // Algorithmic work of one factorisation: operand bytes read and written once
@@ -84,6 +86,8 @@ struct SvdPcWork {
 	double* c = nullptr;   // k x k
 	double* u = nullptr;   // k x k
 	double* vt = nullptr;  // k x k
+	double* ct = nullptr;  // k x k (m >= n: the transposed factor)
+	double* ut = nullptr;  // k x k (m >= n: the Jacobi left factor)
 	double* qr_work = nullptr;
 	double* svd_work = nullptr;
 };
@@ -91,10 +95,19 @@ bool svd_pc_fits(int m, int n);
 void svd_pc_workspace(int m, int n, size_t& q, size_t& c, size_t& qr_work, size_t& svd_work);
 // Phase 1: the pivoted QR; writes to the device int `kept` how many rows of R the
 // Jacobi phase needs (rows below a tolerance tied to a.eps are dropped, see
-// svd_pc_row_tol). Phase 2 (the caller has read `kept` to the host): Jacobi and
-// the factors.
+// svd_pc_row_tol). Phase 2 (the caller has read `kept` to the host): svd_pc_jacobi
+// returns the arguments of the Jacobi SVD (always of a tall matrix: R^T or P R^T),
+// the caller runs it, and svd_pc_finish forms the factors of X.
 double svd_pc_row_tol(const SvdArgs& a);
 void launch_svd_pc_qr(const SvdArgs& a, const SvdPcWork& w, int* kept, cudaStream_t s);
-void launch_svd_pc(const SvdArgs& a, const SvdPcWork& w, int kept, cudaStream_t s);
+SvdArgs svd_pc_jacobi(const SvdArgs& a, const SvdPcWork& w, int kept, cudaStream_t s);
+void svd_pc_finish(const SvdArgs& a, const SvdPcWork& w, int kept, cudaStream_t s);
+
+// FP32 stage of the mixed-precision Jacobi: one-sided Jacobi in FP32 on the columns of
+// the p x q matrix X (row-major, ld ldx; scaled by a power of two into FP32 range) in
+// one CTA, to FP32 orthogonality; writes the accumulated rotations W (q x q
+// row-major, FP32). svd_f32_fits: the shape fits one CTA's shared memory.
+bool svd_f32_fits(int p, int q);
+void launch_svd_f32(const double* X, long long ldx, int p, int q, float* W, cudaStream_t s);
 
 }  // namespace xtt

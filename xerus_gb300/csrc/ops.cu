@@ -568,6 +568,79 @@ void move_core(Tensor& x, int64_t pos, bool keep_rank) {
 
 // ------------------------------------------------------------ round
 
+__global__ void k_f2d(double* out, const float* in, size_t n) {
+	for (size_t i = blockIdx.x * size_t(blockDim.x) + threadIdx.x; i < n; i += size_t(gridDim.x) * blockDim.x)
+		out[i] = double(in[i]);
+}
+
+// One-sided Jacobi of a.X (through launch_svd). Mixed precision where it fits (svd_path
+// AUTO, columns orthogonalised, 32..: one CTA holds the matrix in FP32): FP32 sweeps to
+// FP32 orthogonality in one CTA give a rotation W32; two Newton-Schulz steps in FP64,
+// W <- 1.5 W - 0.5 W (W^T W), make it orthogonal to rounding (each squares the 1e-7
+// defect); the FP64 cluster Jacobi then starts from X W with V = W and needs only the
+// few sweeps of its quadratic phase. Same singular values, truncation and gauge.
+// `mixed` false: plain FP64 Jacobi (after the QR preconditioning, whose R^T already
+// converges in 6-10 sweeps, the FP32 stage measured slower than it saves).
+static void jacobi(Context& c, SvdArgs& a, bool mixed) {
+	const bool tall = a.m > a.n || (a.m == a.n && !a.orth_rows);
+	const int p = tall ? a.m : a.n, q = tall ? a.n : a.m;
+	if (mixed && c.svd_path == XTT_SVD_PATH_AUTO && tall && !a.V0 && q >= 32 && svd_f32_fits(p, q)) {
+		Fp64ContractionScope fp64(c);
+		const size_t qq = size_t(q) * q;
+		float* w32 = c.scratch<float>(S_SVD_MX_W32, qq);
+		launch_svd_f32(a.X, a.ldx, p, q, w32, c.stream);
+		double* W = c.scratch<double>(S_SVD_MX_W, qq);
+		double* W2 = c.scratch<double>(S_SVD_MX_W2, qq);
+		double* G = c.scratch<double>(S_SVD_MX_G, qq);
+		k_f2d<<<unsigned(std::min<size_t>(1024, (qq + 255) / 256)), 256, 0, c.stream>>>(W, w32, qq);
+		c.count_launch(2);
+		XTT_CUDA(cudaGetLastError());
+		for (int it = 0; it < 2; ++it) {
+			Gemm<double> g1;  // G = W^T W
+			g1.M = q; g1.N = q; g1.K = q;
+			g1.A = W; g1.sAm = 1; g1.sAk = q;
+			g1.B = W; g1.sBk = q; g1.sBn = 1;
+			g1.C = G; g1.sCm = q; g1.sCn = 1;
+			g1.lens((long long)qq, (long long)qq, (long long)qq);
+			gemm(c, g1);
+			copy_d2d(c, W2, W, qq);
+			Gemm<double> g2;  // W2 = 1.5 W - 0.5 W G
+			g2.M = q; g2.N = q; g2.K = q;
+			g2.A = W; g2.sAm = q; g2.sAk = 1;
+			g2.B = G; g2.sBk = q; g2.sBn = 1;
+			g2.C = W2; g2.sCm = q; g2.sCn = 1;
+			g2.alpha = -0.5; g2.beta = 1.5;
+			g2.lens((long long)qq, (long long)qq, (long long)qq);
+			gemm(c, g2);
+			std::swap(W, W2);
+		}
+		double* B0 = c.scratch<double>(S_SVD_MX_B0, size_t(p) * q);
+		Gemm<double> g3;  // B0 = X W
+		g3.M = p; g3.N = q; g3.K = q;
+		g3.A = a.X; g3.sAm = a.ldx; g3.sAk = 1;
+		g3.B = W; g3.sBk = q; g3.sBn = 1;
+		g3.C = B0; g3.sCm = q; g3.sCn = 1;
+		g3.lens((long long)(p - 1) * a.ldx + q, (long long)qq, (long long)p * q);
+		gemm(c, g3);
+		SvdArgs b = a;
+		b.X = B0;
+		b.ldx = q;
+		b.m = p;
+		b.n = q;
+		b.orth_rows = 0;
+		b.V0 = W;
+		const size_t wk = svd_work_doubles(p, q);
+		b.work = wk ? c.scratch<double>(S_SVD_WORK, wk) : nullptr;
+		launch_svd(b, c.stream);
+		c.count_launch();
+		return;
+	}
+	const size_t wk = svd_work_doubles(a.m, a.n);
+	a.work = wk ? c.scratch<double>(S_SVD_WORK, wk) : nullptr;
+	launch_svd(a, c.stream);
+	c.count_launch();
+}
+
 void run_svd(Context& c, SvdArgs& a, bool graded) {
 	ProfScope ps(c, "svd");
 	if (graded && c.svd_path == XTT_SVD_PATH_AUTO && svd_pc_fits(a.m, a.n)) {
@@ -577,18 +650,21 @@ void run_svd(Context& c, SvdArgs& a, bool graded) {
 		w.q = c.scratch<double>(S_SVD_PC_Q, nq);
 		w.c = c.scratch<double>(S_SVD_PC_C, nc);
 		(a.m >= a.n ? w.u : w.vt) = c.scratch<double>(S_SVD_PC_UV, nc);
+		if (a.m >= a.n) {
+			w.ct = c.scratch<double>(S_SVD_PC_CT, nc);
+			w.ut = c.scratch<double>(S_SVD_PC_UT, nc);
+		}
 		w.qr_work = nqr ? c.scratch<double>(S_SVD_PC_QRW, nqr) : nullptr;
 		w.svd_work = nsv ? c.scratch<double>(S_SVD_WORK, nsv) : nullptr;
 		launch_svd_pc_qr(a, w, c.d_ints + 4, c.stream);
 		const int kept = c.read_int(4);  // rows of the pivoted R the Jacobi phase needs
-		launch_svd_pc(a, w, kept, c.stream);
+		SvdArgs sa = svd_pc_jacobi(a, w, kept, c.stream);
+		jacobi(c, sa, false);
+		svd_pc_finish(a, w, kept, c.stream);
 		c.count_launch(3);
 		return;
 	}
-	const size_t wk = svd_work_doubles(a.m, a.n);
-	a.work = wk ? c.scratch<double>(S_SVD_WORK, wk) : nullptr;
-	launch_svd(a, c.stream);
-	c.count_launch();
+	jacobi(c, a, true);
 }
 
 static int svd_into(Context& c, const double* X, int m, int n, int max_rank, double eps, double*& U, double*& S,
