@@ -2323,6 +2323,9 @@ __global__ void __launch_bounds__(kSvf32Threads) k_svd_f32(const double* __restr
 	for (long long e = tid; e < (long long)p * q; e += blockDim.x) fl = fmaf(B[e], B[e], fl);
 	const float fro = block_sum(fl, f_red);
 	const float negl = fro * 1e-12f;
+	// a start for the FP64 sweeps, not an SVD: FP32-level orthogonality, at most 12
+	// sweeps (near FP32 rounding the sweeps would go on rotating noise; an FP64 sweep
+	// costs about ten of these, so the FP32 stage goes as far as it usefully can)
 	const float tol = 4.f * sqrtf(float(p)) * FLT_EPSILON;
 	const int qe = q + (q & 1);
 	for (int sweep = 0; sweep < max_sweeps; ++sweep) {
@@ -2383,7 +2386,7 @@ void launch_svd_f32(const double* X, long long ldx, int p, int q, float* W, cuda
 		attr = true;
 	}
 	const size_t smem = (size_t(p) * q + size_t(q) * q) * sizeof(float);
-	k_svd_f32<<<1, kSvf32Threads, smem, s>>>(X, ldx, p, q, W, 30);
+	k_svd_f32<<<1, kSvf32Threads, smem, s>>>(X, ldx, p, q, W, 12);
 	XTT_CUDA(cudaGetLastError());
 }
 
