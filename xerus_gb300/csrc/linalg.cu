@@ -1593,6 +1593,12 @@ __device__ __forceinline__ void jacobi_rotation_fast(double al, double be, doubl
 	s = y * tt;
 }
 
+// The cluster Jacobi stops after a sweep whose rotations all had |ga| / sqrt(al be)
+// below kQuadStop: in the quadratic phase the next sweep's off-diagonals are of order
+// kQuadStop^2 sqrt(q), below the rotation threshold eps sqrt(p), so the sweep that
+// would only confirm convergence is skipped.
+constexpr double kQuadStop2 = 1e-18;  // kQuadStop = 1e-9
+
 __global__ void __launch_bounds__(kSvdThreads) k_svd(SvdArgs a, int use_smem) {
 	extern __shared__ double dyn[];
 	__shared__ int s_rot, s_rank;
@@ -1819,7 +1825,7 @@ __global__ void __launch_bounds__(kSvcThreads) k_svd_cluster(SvdArgs a, SvcLayou
 	const double tol2 = DBL_EPSILON * DBL_EPSILON * double(p);  // rotate when |ga| > eps sqrt(p) sqrt(al be)
 	int cur = 0, t = 0, sweep = 0;
 	bool converged = (q < 2);
-	bool rot = false;
+	bool rot = false, big = false;
 	long long steps_left = (long long)a.max_sweeps * (qe - 1);
 	// where the column in this CTA's slot `sl` at step t sits at step tn (push target)
 	auto dest_of = [&](int sl, int tn, int nb) {
@@ -1880,6 +1886,7 @@ __global__ void __launch_bounds__(kSvcThreads) k_svd_cluster(SvdArgs a, SvcLayou
 					dj[p + q] = fma(tr, ga, be);
 				}
 				rot = true;
+				big = big || ga * ga >= kQuadStop2 * al * be;
 			} else {
 				for (int r = lane; r < p + q; r += 32) {
 					di[r] = bi[r];
@@ -1893,10 +1900,11 @@ __global__ void __launch_bounds__(kSvcThreads) k_svd_cluster(SvdArgs a, SvcLayou
 		}
 		const bool last_step = (t == qe - 2);
 		if (last_step) {
+			// 0: no rotation in the sweep, 1: only rotations below kQuadStop, 2: a larger one
 			__shared__ int s_rot;
 			if (tid == 0) s_rot = 0;
 			__syncthreads();
-			if (rot) s_rot = 1;
+			if (rot) atomicMax(&s_rot, big ? 2 : 1);
 			__syncthreads();
 			if (tid < P) cl.map_shared_rank(flg, tid)[me] = double(s_rot);
 		}
@@ -1907,13 +1915,16 @@ __global__ void __launch_bounds__(kSvcThreads) k_svd_cluster(SvdArgs a, SvcLayou
 		if (last_step) {
 			++sweep;
 			if (tid == 0) {
-				int any = 0;
-				for (int c2 = 0; c2 < P; ++c2) any |= flg[c2] != 0.0;
-				s_stop = any ? 0 : 1;
+				double worst = 0;
+				for (int c2 = 0; c2 < P; ++c2) worst = fmax(worst, flg[c2]);
+				// a sweep whose rotations were all below kQuadStop leaves off-diagonals of
+				// order kQuadStop^2 (quadratic phase), under the rotation threshold: done
+				s_stop = worst < 1.5 ? 1 : 0;
 			}
 			__syncthreads();
 			converged = s_stop != 0;
 			rot = false;
+			big = false;
 			if (converged) break;  // uniform: every CTA read the same flags
 		}
 	}
