@@ -233,6 +233,30 @@ def test_round_dot_precision_forms(ctx, golden, form, tol):
     assert abs(dt - d64) / (x.frob_norm() * y.frob_norm()) < tol
 
 
+@pytest.mark.parametrize("svd_path", ["auto", "jacobi"])
+def test_round_odd_shapes(ctx, svd_path):
+    """Rounding with odd bond sizes (37 x 37 bonds of a d=8, n=3 TT of rank 37)
+    through the mixed-precision Jacobi (AUTO) and plain Jacobi: ranks exact,
+    spectra and entries against the oracle's LAPACK-based round."""
+    d, n, r = 8, 3, 37
+    rng = np.random.default_rng(17)
+    ranks = [1] + [min(r, n ** k, n ** (d - k)) for k in range(1, d)] + [1]
+    cores = [rng.standard_normal((ranks[k], n, ranks[k + 1])) / np.sqrt(ranks[k] * n) for k in range(d)]
+    xh = o.TT([c.copy() for c in cores])
+    try:
+        ctx.set_svd_path(svd_path)
+        x = xg.TTTensor.from_cores(cores, ctx=ctx)
+        sp = np.array(x.round(20, spectra=True))
+    finally:
+        ctx.set_svd_path("auto")
+    spr = []
+    o.tt_round(xh, 20, o.EPSILON, spr)
+    assert x.ranks() == xh.ranks
+    assert rel_err(sp, np.concatenate(spr)) < 1e-10
+    pos = np.random.default_rng(3).integers(0, n, size=(50, d))
+    assert rel_err(x.entries(pos), o.tt_entries(xh, pos)) < 1e-10
+
+
 def test_round_eps_and_max_ranks(ctx, golden):
     r = golden("round")
     e = tt_of(r, "eps_in", canonicalized=False)
