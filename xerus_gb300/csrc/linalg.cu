@@ -1850,30 +1850,29 @@ __global__ void __launch_bounds__(kSvcThreads) k_svd_cluster(SvdArgs a, SvcLayou
 			double* dj = dest_of(2 * lp + 1, tn, cur ^ 1);
 			bool rotate = false;
 			double c = 1.0, sn = 0.0, tr = 0.0, al = 0.0, be = 0.0, ga = 0.0;
-			if (i < q && j < q) {
-				// squared column norms: computed at the first step of a sweep, then carried
-				// with the columns and updated by each rotation (al - t ga, be + t ga), so
-				// a step needs one dot product instead of three (FP64 pipe)
-				if (t == 0) {
-					for (int r = lane; r < p; r += 32) {
-						const double x = bi[r], y = bj[r];
-						al = fma(x, x, al);
-						be = fma(y, y, be);
-						ga = fma(x, y, ga);
-					}
-					al = warp_sum(al);
-					be = warp_sum(be);
-				} else {
-					for (int r = lane; r < p; r += 32) ga = fma(bi[r], bj[r], ga);
-					al = bi[p + q];
-					be = bj[p + q];
+			// squared column norms: computed at the first step of a sweep (for every column,
+			// also one paired with the padding column of an odd count), then carried with
+			// the columns and updated by each rotation (al - t ga, be + t ga), so a step
+			// needs one dot product instead of three (FP64 pipe)
+			if (t == 0) {
+				for (int r = lane; r < p; r += 32) {
+					const double x = bi[r], y = bj[r];
+					al = fma(x, x, al);
+					be = fma(y, y, be);
+					ga = fma(x, y, ga);
 				}
+				al = warp_sum(al);
+				be = warp_sum(be);
+			} else {
+				if (i < q && j < q)
+					for (int r = lane; r < p; r += 32) ga = fma(bi[r], bj[r], ga);
+				al = bi[p + q];
+				be = bj[p + q];
+			}
+			if (i < q && j < q) {
 				ga = warp_sum(ga);
 				rotate = ga != 0.0 && fmin(al, be) > negl && ga * ga > tol2 * al * be;
 				if (rotate) jacobi_rotation_fast(al, be, ga, c, sn, tr);
-			} else {
-				al = bi[p + q];
-				be = bj[p + q];
 			}
 			if (rotate) {
 				for (int r = lane; r < p + q; r += 32) {
