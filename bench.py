@@ -539,7 +539,7 @@ def run_reference(args):
 
 
 def bench_dmrg(xg, ctx, torch, stream, half_sweeps):
-    """Configuration 3: two-site DMRG_SPD on the d=20, n=8 Laplacian sum plus a
+    """Two-site DMRG_SPD on the d=20, n=8 Laplacian sum plus a
     diagonal potential U[0,1] per mode (operator rank 3), random rank-16 start,
     ranks free to grow to 128 with SVD cutoff 1e-10, run until the FP64 residual
     reaches 1e-8 (checked after every half-sweep) or `half_sweeps` half-sweeps;
@@ -589,7 +589,7 @@ def bench_dmrg(xg, ctx, torch, stream, half_sweeps):
 
 
 def bench_tc_als(xg, ctx, torch, stream, peaks, rank=128, half_sweeps=2, reps=2):
-    """Ranks >= 64: one-site ALS_SPD on the configuration-3 operator (d=20, n=8,
+    """Ranks >= 64: one-site ALS_SPD on the DMRG workload's operator (d=20, n=8,
     Laplacian sum plus a diagonal potential, operator rank 3; rhs rank 4), random
     rank-`rank` start, `half_sweeps` half-sweeps. FP64 form vs the mixed form, whose
     local solves there run on the tensor cores (FP64 refinement of FP32 CG with
@@ -604,7 +604,7 @@ def bench_tc_als(xg, ctx, torch, stream, peaks, rank=128, half_sweeps=2, reps=2)
     b = xg.TTTensor.random([n] * d, 4, ctx=ctx)
     x0 = xg.TTTensor.random([n] * d, rank, ctx=ctx)
     x0 /= x0.frob_norm()
-    out = {"workload": f"ALS_SPD d=20 n=8 (configuration-3 operator, rank 3), rhs rank 4, x rank {rank}, "
+    out = {"workload": f"ALS_SPD d=20 n=8 (Laplacian sum + diagonal potential, operator rank 3), rhs rank 4, x rank {rank}, "
                        f"{half_sweeps} half-sweeps", "local_unknowns": rank * n * rank}
     for name, prec in (("fp64", xg.FP64), ("mixed", xg.MIXED)):
         v = xg.ALS_SPD.copy()
