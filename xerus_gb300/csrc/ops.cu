@@ -699,24 +699,27 @@ static void round_edge(Tensor& x, int from, int to, int64_t max_rank, double eps
 		a.A = x.core[from]; a.lda = nFc; a.m = mF; a.n = nFc; a.transpose = 1; a.pivot = 1;
 		a.work = wk ? c.scratch<double>(S_QR_WORK, wk) : nullptr;
 		a.Q = QF; a.C = CA; a.rank_out = c.d_ints + 2;
-		{
-			ProfScope ps(c, "qr", qr_work_bytes(a), qr_work_flops(a));
-			launch_qr(a, c.stream);
-		}
-		c.count_launch();
+		// the two factorisations are independent: T's on the aux stream, F's on the main one
+		c.fork();
 		const int mT = int(rT * nT), nTc = int(r);
 		double* QT = c.scratch<double>(S_ROUND_QB, size_t(mT) * std::min(mT, nTc));
 		double* CB = c.scratch<double>(S_ROUND_CB, size_t(std::min(mT, nTc)) * nTc);
 		wk = qr_work_doubles(mT, nTc);
 		QrArgs b;
 		b.A = x.core[to]; b.lda = nTc; b.m = mT; b.n = nTc; b.transpose = 0; b.pivot = 1;
-		b.work = wk ? c.scratch<double>(S_ROUND_X, wk) : nullptr;  // not S_QR_WORK: may run concurrently in the future
+		b.work = wk ? c.scratch<double>(S_ROUND_X, wk) : nullptr;  // not S_QR_WORK: runs beside a
 		b.Q = QT; b.C = CB; b.rank_out = c.d_ints + 3;
 		{
-			ProfScope ps(c, "qr", qr_work_bytes(a), qr_work_flops(a));
+			OnAux aux(c);
+			ProfScope ps(c, "qr", qr_work_bytes(b), qr_work_flops(b));
 			launch_qr(b, c.stream);
 		}
-		c.count_launch();
+		{
+			ProfScope ps(c, "qr", qr_work_bytes(a), qr_work_flops(a));
+			launch_qr(a, c.stream);
+		}
+		c.count_launch(2);
+		c.join();
 		const int ka = c.read_int(2), kb = c.read_int(3);
 		double* X = c.scratch<double>(S_GEMM_B, size_t(ka) * kb);
 		Gemm<double> g;
