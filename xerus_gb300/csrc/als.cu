@@ -973,12 +973,18 @@ struct AlsState {
 		s.K2 = S == 2 ? int(A.ranks[cur + 2]) : 1;
 		return s;
 	}
+	// the operator and rhs pushes are independent (separate scratch): rhs on the aux stream
 	void push_left(int k) {
+		c.fork();
+		{
+			OnAux aux(c);
+			push_left_rhs(c, st.Lb[k], b.core[k], x.core[k], st.Lb[k + 1], b.ranks[k], x.ranks[k], x.dims[k],
+			              b.ranks[k + 1], x.ranks[k + 1]);
+		}
 		if (mode != kFree)
 			push_left_op(c, st.Lop[k], x.core[k], A.core[k], st.Lop[k + 1], x.ranks[k], A.ranks[k], x.dims[k],
 			             x.ranks[k + 1], A.ranks[k + 1]);
-		push_left_rhs(c, st.Lb[k], b.core[k], x.core[k], st.Lb[k + 1], b.ranks[k], x.ranks[k], x.dims[k], b.ranks[k + 1],
-		              x.ranks[k + 1]);
+		c.join();
 	}
 	// right environment of bond `slot` from bond slot+1 and core kc
 	void push_right(int slot, int kc) {
@@ -988,11 +994,16 @@ struct AlsState {
 		                           x.dims[kc] == x.dims[slot]),
 		            "index dimensions do not coincide (the two-site decreasing sweep contracts core k into the right "
 		            "environment of bond k+2, which needs equal neighbouring ranks)");
+		c.fork();
+		{
+			OnAux aux(c);
+			push_right_rhs(c, st.Rb[slot + 1], b.core[kc], x.core[kc], st.Rb[slot], b.ranks[kc], x.ranks[kc],
+			               x.dims[kc], b.ranks[kc + 1], x.ranks[kc + 1]);
+		}
 		if (mode != kFree)
 			push_right_op(c, st.Rop[slot + 1], x.core[kc], A.core[kc], st.Rop[slot], x.ranks[kc], A.ranks[kc],
 			              x.dims[kc], x.ranks[kc + 1], A.ranks[kc + 1]);
-		push_right_rhs(c, st.Rb[slot + 1], b.core[kc], x.core[kc], st.Rb[slot], b.ranks[kc], x.ranks[kc], x.dims[kc],
-		               b.ranks[kc + 1], x.ranks[kc + 1]);
+		c.join();
 	}
 	// v <- current local block (core cur, or core cur * core cur+1)
 	void gather_block(int cur) {
