@@ -75,8 +75,9 @@ int xtt_context_profile_work(xtt_context* ctx, const char* name, double* bytes, 
  * src/xerus/algorithms/als.cpp:43-71). AUTO: one thread-block cluster with all
  * operands in shared memory when the local system fits (up to 16 CTAs), else
  * the grid-wide cooperative kernel; for mixed-precision solves at a site whose
- * rank is 64 or more, the tensor-core form (FP64 refinement of FP32 CG whose
- * operator stages run as split-TF32 tcgen05 GEMMs). GRID: always the grid-wide
+ * rank is 64 or more or whose local system has 16384 unknowns or more, the
+ * tensor-core form (FP64 refinement of FP32 CG whose operator stages run as
+ * split-TF32 tcgen05 GEMMs). GRID: always the grid-wide
  * kernel. TENSOR: the tensor-core form for every mixed-precision solve. Results
  * agree to the CG tolerance; the choice only changes speed. */
 typedef enum xtt_cg_path { XTT_CG_PATH_AUTO = 0, XTT_CG_PATH_GRID = 1, XTT_CG_PATH_TENSOR = 2 } xtt_cg_path;

@@ -73,8 +73,8 @@ class Context:
 
     def set_cg_path(self, path):
         """'auto' (cluster-resident CG where the local system fits; the tensor-core
-        precision form for mixed solves at ranks >= 64), 'grid', or 'tensor' (the
-        tensor-core precision form for every mixed solve)."""
+        precision form for mixed solves at ranks >= 64 or from 16384 unknowns), 'grid',
+        or 'tensor' (the tensor-core precision form for every mixed solve)."""
         L.check(self.lib.xtt_context_set_cg_path(self.handle, {"auto": 0, "grid": 1, "tensor": 2}[path]))
 
     def set_contraction_precision(self, form):

@@ -523,7 +523,9 @@ __global__ void k_add_counters(int* out, int iters, int refs) {
 static bool use_tc_solve(const Context& c, const LocalShape& s, int precision) {
 	if (precision != XTT_PRECISION_MIXED) return false;
 	if (c.cg_path == XTT_CG_PATH_TENSOR) return true;
-	return c.cg_path == XTT_CG_PATH_AUTO && std::max(s.ra, s.rb) >= 64;
+	// measured: the cluster-resident CG wins at 4096 unknowns (rank-32 one-site ALS), the
+	// tensor-core form from 16384 (two-site DMRG at rank 16) and at ranks >= 64
+	return c.cg_path == XTT_CG_PATH_AUTO && (std::max(s.ra, s.rb) >= 64 || s.dim() >= 16384);
 }
 
 // Returns false when the refinement stalled (x then holds its best iterate and
