@@ -206,7 +206,9 @@ int xtt_entries(const xtt_tensor* x, const int64_t* positions, int64_t count, do
  * `stream` (a cudaStream_t, NULL = legacy default stream). Limits: every rank
  * <= 128 and every mode size <= 16, else XTT_ERR_CAPACITY before any launch.
  * The first call on a device looks up the array's device address; make it
- * before any stream capture on that device. All calls share the array:
+ * before any stream capture on that device. The address is kept for the life of
+ * the process: resetting the device (cudaDeviceReset) after that first call is
+ * not supported. All calls share the array:
  * calls whose kernels may overlap on the GPU race and must be serialised. */
 int xtt_dot_noalloc(int64_t order, const int64_t* dims, const int64_t* x_ranks, const double* x_cores,
                     const int64_t* y_ranks, const double* y_cores, double* result, void* stream);
@@ -333,6 +335,20 @@ typedef struct xtt_adf_options {
 int xtt_adf(xtt_tensor* x, const int64_t* positions, const double* values, int64_t num,
             const xtt_adf_options* opt, double* final_residual, double* residual_trace,
             int64_t trace_capacity, int64_t* trace_count);
+
+/* ADFVariant(maxIter, target, minDecrease)(x, SinglePointMeasurementSet, maxRanks)
+ * (include/xerus/algorithms/adf.h:263-266, src/xerus/algorithms/adf.cpp:566-604): x may
+ * start below max_ranks (order-1 inner ranks, reduced to the maximal ranks). Whenever a
+ * run at the current ranks stops early (stagnation) with the residual above the target
+ * and ranks below max_ranks, a random rank-one TT from the library's random state
+ * (xtt_random_seed), scaled to 1e-6 ||x||, is added and x is rounded to max_ranks
+ * (adf.cpp:590-602); the iteration count carries on. The traces receive, per recorded
+ * point (PerformanceData), the relative residual, the iteration count and the order-1
+ * inner ranks (rank_trace: trace_capacity x (order-1)); each may be NULL. */
+int xtt_adf_max_ranks(xtt_tensor* x, const int64_t* positions, const double* values, int64_t num,
+                      const int64_t* max_ranks, const xtt_adf_options* opt, double* final_residual,
+                      double* residual_trace, int64_t* iteration_trace, int64_t* rank_trace, int64_t trace_capacity,
+                      int64_t* trace_count);
 
 /* GeometricCGVariant(numSteps, convergenceEpsilon, assumeSPD, SubmanifoldRetractionI,
  * ProjectiveVectorTransport)(A, x, b, numSteps, perfData) (src/xerus/algorithms/cg.cpp:34-120,

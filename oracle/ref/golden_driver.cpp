@@ -4,7 +4,8 @@
 //
 //   golden_driver <case> <outdir>
 //
-// Cases: rng, tt_random, dot, movecore, round, als, dmrg, adf, adf_cfg5, timing_*.
+// Cases: rng, tt_random, dot, movecore, round, als, dmrg, adf, adf_cfg5, fileio, als_nonspd,
+// arith, adf_rankone, gcg, adf_rankinc, qc_gap, timing_*.
 // Every case seeds xerus::misc::randomEngine with 0xBAADF00D and resets
 // xerus::misc::defaultNormalDistribution (dropping a cached polar variate) first,
 // so a case's draws do not depend on the cases run before it.
@@ -795,6 +796,94 @@ static void case_adf_rankone() {
 }
 static void case_adf_cfg5() { adf_case("cfg5", std::vector<size_t>(10, 8), 6, 200000, 50, false, true); }
 
+// ADF with rank increase: the ADFVariant::operator() overload taking maxRanks
+// (adf.h:263-266, adf.cpp:590-602). x starts at rank 1 below a rank-3 target;
+// each stagnation (minimal decrease 0.99) adds a 1e-6-scaled rank-1 random TT
+// (target residual 1e-10, above the rounding floor)
+// drawn from the library's random state and rounds to maxRanks. The random state
+// is reseeded with 0x5EED right before the call so the device can replay it.
+static void case_adf_rankinc() {
+	reseed();
+	const std::vector<size_t> dims{4, 5, 3, 5, 4, 3};
+	TTTensor target = TTTensor::random(dims, 3);
+	const size_t N = 1500;
+	SinglePointMeasurementSet m = SinglePointMeasurementSet::random(N, dims);
+	m.measure(target);
+	TTTensor x = TTTensor::random(dims, 1);
+	save_tt("x0", x);
+	std::vector<int64_t> pos;
+	for (auto& p : m.positions)
+		for (auto i : p) pos.push_back(int64_t(i));
+	save("positions", pos, {N, dims.size()});
+	save("values", m.measuredValues);
+	const std::vector<size_t> maxRanks(dims.size() - 1, 3);
+	misc::randomEngine.seed(0x5EED);
+	misc::defaultNormalDistribution.reset();
+	PerformanceData perf(false, true);
+	ADFVariant adf(120, 1e-10, 0.99);
+	const double res = adf(x, m, maxRanks, perf);
+	std::vector<int64_t> iters, ranks;
+	for (auto& dp : perf.data) {
+		iters.push_back(int64_t(dp.iterationCount));
+		for (auto r : dp.ranks) ranks.push_back(int64_t(r));
+	}
+	save("perf_residual", perf_residuals(perf));
+	save("perf_iteration", iters);
+	save("perf_ranks", ranks, {perf.data.size(), dims.size() - 1});
+	save_scalar("final_residual", res);
+	save_tt("x_final", x);
+	save_probes("x_final", x, probe_positions(dims, 100, 37));
+}
+
+// Rank-revealing QC / CQ with a clear gap: z = x (+) s w stacks x and a scaled
+// independent TT w in block cores (the sum x + s w). With s = 1e-13 the w part's
+// R_kk sit near 1e-13 R_00, far above the cutoff 16 eps R_00 and far above
+// rounding, so they are kept; with s = 1e-17 they sit far below the cutoff and are
+// dropped wherever R_00 > 0 (blasLapackWrapper.cpp:269,343 compare with the signed
+// R_00). Either way the rank decision does not depend on rounding.
+static TTTensor block_sum2(const TTTensor& x, const TTTensor& w, double s) {
+	const size_t d = x.degree();
+	TTTensor z(x.dimensions);
+	for (size_t k = 0; k < d; ++k) {
+		Tensor a = x.get_component(k), b = w.get_component(k);
+		a.use_dense_representation();
+		b.use_dense_representation();
+		const size_t ra0 = a.dimensions[0], n = a.dimensions[1], ra1 = a.dimensions[2];
+		const size_t rb0 = b.dimensions[0], rb1 = b.dimensions[2];
+		const size_t R0 = k == 0 ? 1 : ra0 + rb0, R1 = k + 1 == d ? 1 : ra1 + rb1;
+		Tensor c({R0, n, R1}, Tensor::Representation::Dense);
+		for (size_t i = 0; i < ra0; ++i)
+			for (size_t j = 0; j < n; ++j)
+				for (size_t l = 0; l < ra1; ++l) c[(i * n + j) * R1 + l] = a[(i * n + j) * ra1 + l];
+		const size_t o0 = k == 0 ? 0 : ra0, o1 = k + 1 == d ? 0 : ra1;
+		for (size_t i = 0; i < rb0; ++i)
+			for (size_t j = 0; j < n; ++j)
+				for (size_t l = 0; l < rb1; ++l)
+					c[((o0 + i) * n + j) * R1 + o1 + l] += (k == 0 ? s : 1.0) * b[(i * n + j) * rb1 + l];
+		z.set_component(k, c);
+	}
+	return z;
+}
+
+static void case_qc_gap() {
+	reseed();
+	const std::vector<size_t> dims{4, 3, 5, 4, 3, 4, 3};
+	TTTensor x = TTTensor::random(dims, {3, 5, 6, 5, 4, 3});
+	TTTensor w = TTTensor::random(dims, {2, 3, 3, 4, 2, 2});
+	auto pos = probe_positions(dims, 100, 41);
+	for (const auto& tag : {std::string("keep"), std::string("drop")}) {
+		const double s = tag == "keep" ? 1e-13 : 1e-17;
+		TTTensor z = block_sum2(x, w, s);
+		save_tt(tag + "_z", z);
+		for (size_t p : {dims.size() - 1, size_t(0), size_t(3)}) {
+			TTTensor y = z;
+			y.move_core(p, false);
+			save(tag + "_qc_to" + std::to_string(p) + "_ranks", ranks_of(y));
+			save_probes(tag + "_qc_to" + std::to_string(p), y, pos);
+		}
+	}
+}
+
 // xerus's own binary file format (misc::save_to_file): the bytes of files written
 // by the reference, with the numbers they hold, for byte-exact writer/reader tests.
 static void save_file_bytes(const std::string& name, const std::string& path) {
@@ -846,6 +935,8 @@ int main(int argc, char** argv) {
 	else if (c == "arith") case_arith();
 	else if (c == "adf_rankone") case_adf_rankone();
 	else if (c == "gcg") case_gcg();
+	else if (c == "adf_rankinc") case_adf_rankinc();
+	else if (c == "qc_gap") case_qc_gap();
 	else {
 		std::fprintf(stderr, "unknown case %s\n", c.c_str());
 		return 2;

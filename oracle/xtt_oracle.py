@@ -928,6 +928,8 @@ class ADFResult:
     residual_norm: float
     residuals: list = field(default_factory=list)
     iterations: int = 0
+    ranks: list = field(default_factory=list)           # x's inner ranks at every recorded point
+    iteration_log: list = field(default_factory=list)   # PerformanceData's iteration count per point
 
 
 class ADFSolver:
@@ -1017,17 +1019,18 @@ class ADFSolver:
             self.B[k] = self.update_backward(k, self.x.cores[k])
         self.calculate_residual(0)
 
-    def solve(self, first_sweep_log=None) -> ADFResult:
-        """solve() + solve_with_current_ranks() (adf.cpp:489-542, 566-604) without rank increase
-        (the case when x already has its maximal ranks)."""
-        move_core(self.x, 0, keep_rank=False)      # canonicalize_left
-        out = ADFResult(residual_norm=0.0)
+    def solve_with_current_ranks(self, out: ADFResult, first_sweep_log=None) -> None:
+        """solve_with_current_ranks (adf.cpp:489-542): the three earlier decrease ratios
+        start at 0 on every call; iteration, residualNorm and lastResidualNorm are
+        members and carry over between calls."""
         dec = [0.0, 0.0, 0.0]
         while self.max_iter == 0 or self.iteration < self.max_iter:
             self.begin_iteration()
             self.last_residual_norm = self.residual_norm
             self.residual_norm = math.sqrt(float(np.sum(self.res ** 2))) / self.norm_y
             out.residuals.append(self.residual_norm)
+            out.ranks.append(list(self.x.ranks))
+            out.iteration_log.append(self.iteration)
             d4 = dec[2]
             dec = [self.residual_norm / self.last_residual_norm, dec[0], dec[1]]
             if self.residual_norm < self.target or dec[0] * dec[1] * dec[2] * d4 > self.min_dec ** 4:
@@ -1035,13 +1038,45 @@ class ADFSolver:
             for k in range(self.d):
                 self.sweep_step(k, first_sweep_log if self.iteration == 0 else None)
             self.iteration += 1
+
+    def increase_ranks(self, max_ranks, rs: "RandomEngine") -> None:
+        """The rank-increasing step of solve() (adf.cpp:590-599): core to 0, add a rank-1
+        random TT scaled to 1e-6 ||x|| (TTTensor::random, which draws from the library's
+        random state and ends with move_core(0)), round to the maximal ranks."""
+        x = self.x
+        move_core(x, 0, keep_rank=True)
+        rnd = tt_random(x.dims, [1] * (x.d - 1), rs)
+        scale = (1e-6 * frob_norm(x)) * (1.0 / frob_norm(rnd))
+        y = tt_add(x, tt_scale(rnd, scale))
+        tt_round(y, max_ranks)
+        x.cores, x.canonicalized, x.core_position = y.cores, y.canonicalized, y.core_position
+        self.F, self.B = {}, {}
+
+    def solve(self, first_sweep_log=None, max_ranks=None, rs: "RandomEngine | None" = None) -> ADFResult:
+        """solve() (adf.cpp:566-604): canonicalize_left, one run at the current ranks, then,
+        with max_ranks (the ADFVariant::operator() overload taking maxRanks, adf.h:263-266),
+        rank increases until the target residual, the maximal ranks or the iteration cap."""
+        move_core(self.x, 0, keep_rank=False)      # canonicalize_left
+        out = ADFResult(residual_norm=0.0)
+        self.solve_with_current_ranks(out, first_sweep_log)
+        if max_ranks is not None:
+            mr = reduce_to_maximal_ranks(list(max_ranks), self.x.dims)
+            while (self.residual_norm > self.target and list(self.x.ranks) != mr
+                   and (self.max_iter == 0 or self.iteration < self.max_iter)):
+                self.increase_ranks(mr, rs)
+                self.solve_with_current_ranks(out)
         out.residual_norm = self.residual_norm
         out.iterations = self.iteration
         return out
 
 
-def adf(x: TT, positions, values, max_iter: int = 0, target: float = 1e-8, min_dec: float = 0.999) -> ADFResult:
-    return ADFSolver(x, positions, values, max_iter, target, min_dec).solve()
+def adf(x: TT, positions, values, max_iter: int = 0, target: float = 1e-8, min_dec: float = 0.999,
+        max_ranks=None, rs: "RandomEngine | None" = None) -> ADFResult:
+    """ADFVariant(max_iter, target, min_dec)(x, measurements[, maxRanks]); with max_ranks the
+    rank increases draw their random TTs from rs."""
+    if max_ranks is not None and rs is None:
+        raise ValueError("the rank-increasing ADF needs the random state it draws from")
+    return ADFSolver(x, positions, values, max_iter, target, min_dec).solve(max_ranks=max_ranks, rs=rs)
 
 
 # --------------------------------------------------------------------------- rank-one measurements

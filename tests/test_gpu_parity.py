@@ -84,6 +84,22 @@ def test_dot_and_norm_cfg2(ctx, golden):
     assert abs(a.frob_norm() / np.sqrt(o.tt_dot(tt_of(z, "small_a"), tt_of(z, "small_a"))) - 1) < REL_TOL
 
 
+@pytest.mark.parametrize("tag", ["keep", "drop"])
+def test_qc_rank_rule_with_clear_gap_exact(ctx, golden, tag):
+    """Rank-revealing move_core on x + s w stacked in block cores: s = 1e-13 puts the w
+    part's R_kk near 1e-13 R_00 (kept: far above 16 eps R_00 and above rounding),
+    s = 1e-17 far below the cutoff (dropped wherever R_00 > 0, the reference's signed
+    rule). The decisions are not rounding-level, so the ranks must equal the
+    reference's exactly, in both sweep directions and to an inner core."""
+    z = golden("qc_gap")
+    zz = tt_of(z, f"{tag}_z", canonicalized=False)
+    for p in (6, 0, 3):
+        y = dev_tt(ctx, zz)
+        y.move_core(p, False)
+        assert [1] + y.ranks() + [1] == list(z[f"{tag}_qc_to{p}_ranks"])
+        assert rel_err(y.entries(z[f"{tag}_qc_to{p}_probe_pos"]), z[f"{tag}_qc_to{p}_probe_val"]) < 1e-9
+
+
 def test_move_core_qr_and_rank_revealing(ctx, golden):
     z = golden("movecore")
     for p in (5, 2, 0, 3):
@@ -584,6 +600,30 @@ def test_steepest_descent_matches_reference(ctx, golden, tag, op, spd, steps):
     assert abs(res / z[tag + "_residual"][0] - 1) < 1e-9
     assert rel_err(perf.residuals, z[tag + "_perf_residual"]) < 1e-9
     assert rel_err(x.entries(z[tag + "_x_probe_pos"]), z[tag + "_x_probe_val"]) < 1e-8
+
+
+def test_adf_rank_increase_matches_reference(ctx, golden):
+    """ADFVariant(120, 1e-10, 0.99)(x, measurements, maxRanks) from a rank-1 start
+    (adf.cpp:566-604): two rank increases, each a rank-1 random TT from the library's
+    random state (reseeded with 0x5EED as the reference was), scaled to 1e-6 ||x||,
+    then round(maxRanks). Ranks and iteration counts exact at every recorded point;
+    residuals to rounding until the second increase, whose new 1e-6-sized directions
+    carry ~1e-10 relative rounding that the later iterations amplify (1e-6 then, the
+    spread the reference itself shows across OpenMP thread counts)."""
+    z = golden("adf_rankinc")
+    m = xg.SinglePointMeasurementSet(z["positions"], z["values"])
+    x = dev_tt(ctx, tt_of(z, "x0"))
+    xg.seed(0x5EED)
+    perf = xg.PerformanceData()
+    res = xg.ADFVariant(120, 1e-10, 0.99)(x, m, [3] * 5, perf)
+    assert list(perf.iterations) == list(z["perf_iteration"])
+    assert perf.ranks == z["perf_ranks"].tolist()
+    r, rr = np.array(perf.residuals), z["perf_residual"]
+    assert np.max(np.abs(r[:18] / rr[:18] - 1)) < 1e-10
+    assert np.max(np.abs(r / rr - 1)) < 1e-6
+    assert abs(res / z["final_residual"][0] - 1) < 1e-6
+    assert [1] + x.ranks() + [1] == list(z["x_final_ranks"])
+    assert rel_err(x.entries(z["x_final_probe_pos"]), z["x_final_probe_val"]) < 1e-8
 
 
 def test_adf_rank_one_matches_reference(ctx, golden):

@@ -260,3 +260,40 @@ def test_steepest_descent(golden, tag, op, spd, steps):
     assert abs(res / z[tag + "_residual"][0] - 1) < 1e-12
     assert rel_err(trace, z[tag + "_perf_residual"]) < 1e-12
     assert rel_err(o.tt_entries(x, z[tag + "_x_probe_pos"]), z[tag + "_x_probe_val"]) < 1e-12
+
+
+def test_adf_rank_increase(golden):
+    """ADFVariant(120, 1e-10, 0.99)(x, measurements, maxRanks) from a rank-1 start: two
+    rank increases (1e-6-scaled rank-1 random TTs from the random state reseeded with
+    0x5EED, then round(maxRanks)); ranks and iteration counts exact at every recorded
+    point, residuals point by point."""
+    z = golden("adf_rankinc")
+    x = tt_of(z, "x0")
+    rs = o.RandomEngine(0x5EED)
+    res = o.adf(x, z["positions"], z["values"], 120, 1e-10, 0.99, max_ranks=[3] * 5, rs=rs)
+    assert res.iteration_log == list(z["perf_iteration"])
+    assert res.ranks == z["perf_ranks"].tolist()
+    # Residuals point by point: to rounding through the first rank increase; each
+    # increase adds directions of size 1e-6 ||x||, which rounding at 1e-16 ||x||
+    # perturbs by 1e-10 relative, and the iterations after the second one amplify
+    # that (the reference itself moves ~1e-6 with its OpenMP thread count).
+    r, rr = np.array(res.residuals), z["perf_residual"]
+    assert np.max(np.abs(r[:18] / rr[:18] - 1)) < 1e-12
+    assert np.max(np.abs(r / rr - 1)) < 1e-6
+    assert abs(res.residual_norm / z["final_residual"][0] - 1) < 1e-6
+    assert [1] + x.ranks + [1] == list(z["x_final_ranks"])
+    assert rel_err(o.tt_entries(x, z["x_final_probe_pos"]), z["x_final_probe_val"]) < 1e-9, \
+        rel_err(o.tt_entries(x, z["x_final_probe_pos"]), z["x_final_probe_val"])
+
+
+@pytest.mark.parametrize("tag", ["keep", "drop"])
+def test_qc_rank_rule_with_clear_gap(golden, tag):
+    """Rank-revealing move_core on x + s w (block cores): with s = 1e-13 the w part is
+    kept, with s = 1e-17 dropped where R_00 > 0; exact ranks either way."""
+    z = golden("qc_gap")
+    zz = tt_of(z, f"{tag}_z", canonicalized=False)
+    for p in (6, 0, 3):
+        y = zz.copy()
+        o.move_core(y, p, keep_rank=False)
+        assert [1] + y.ranks + [1] == list(z[f"{tag}_qc_to{p}_ranks"])
+        assert rel_err(o.tt_entries(y, z[f"{tag}_qc_to{p}_probe_pos"]), z[f"{tag}_qc_to{p}_probe_val"]) < REL_TOL

@@ -5,8 +5,9 @@ entry point keeps its intermediates in a fixed array inside the library.
 
 Checked through the C ABI against xtt_dot (which allocates scratch through its
 context), on two calls in a row and on a second pair of tensors, and the
-capacity limit is rejected before any launch. This file is collected last so a
-failure here cannot hide failures elsewhere.
+capacity limit is rejected before any launch; after a warm-up call, further calls
+leave the device's free memory unchanged (they allocate nothing). This file is
+collected last so a failure here cannot hide failures elsewhere.
 """
 import ctypes
 
@@ -82,3 +83,32 @@ def test_noalloc_dot_rejects_sizes_beyond_the_limit(ctx):
     host = np.zeros(8)
     hptr = ctypes.c_void_p(host.ctypes.data)
     assert lib.xtt_dot_noalloc(2, p(dims), p(ranks), hptr, p(ranks), ptr, ptr, None) == 1  # host memory refused
+
+
+def test_noalloc_dot_allocates_nothing(ctx):
+    """After a warm-up call (which looks up the array's address and loads the kernels),
+    repeated calls leave the device's free memory exactly unchanged."""
+    import xerus_gb300 as xg
+    lib = xg._lib.load()
+    stream = torch.cuda.current_stream().cuda_stream
+    xg.seed(13)
+    dims = [4, 4, 4, 4, 4, 4]
+    x = xg.TTTensor.random(dims, [4, 16, 32, 16, 4], ctx=ctx)
+    y = xg.TTTensor.random(dims, [4, 8, 24, 8, 4], ctx=ctx)
+    want = xg.dot(x, y)
+    xd, xr = _device_copy(x)
+    yd, yr = _device_copy(y)
+    out = torch.zeros(1, dtype=torch.float64, device="cuda")
+    d = np.array(dims, dtype=np.int64)
+    p = lambda a: a.ctypes.data_as(ctypes.POINTER(ctypes.c_int64))
+    args = (len(dims), p(d), p(xr), ctypes.c_void_p(xd.data_ptr()), p(yr), ctypes.c_void_p(yd.data_ptr()),
+            ctypes.c_void_p(out.data_ptr()), ctypes.c_void_p(stream))
+    assert lib.xtt_dot_noalloc(*args) == 0, lib.xtt_last_error()
+    torch.cuda.synchronize()
+    free_before, _ = torch.cuda.mem_get_info()
+    for _ in range(5):
+        assert lib.xtt_dot_noalloc(*args) == 0, lib.xtt_last_error()
+    torch.cuda.synchronize()
+    free_after, _ = torch.cuda.mem_get_info()
+    assert free_after == free_before
+    assert abs(float(out.item()) - want) <= 1e-12 * abs(want)

@@ -697,13 +697,41 @@ class ADFVariant:
         # FP64, or MIXED: FP32 stacks and per-sample arithmetic, FP64 cores, QR and final check
         self.precision = FP64 if precision is None else precision
 
-    def __call__(self, x, measurements, perfData=None):
+    def __call__(self, x, measurements, maxRanks=None, perfData=None):
+        """ADFVariant::operator()(x, measurements[, maxRanks], perfData) (adf.h:248-266).
+        With maxRanks, x may start at lower ranks and grows toward them (rank increases
+        draw from the library's random state, see seed())."""
+        if isinstance(maxRanks, PerformanceData):
+            maxRanks, perfData = None, maxRanks
         val, pv = _f64(measurements.measuredValues)
         o = L.AdfOptions(int(self.maxIterations), float(self.targetResidualNorm),
                          float(self.minimalResidualNormDecrease), int(self.precision), 0)
         cap = max(16, int(self.maxIterations) + 2 if self.maxIterations else 100000)
         trace = np.zeros(cap)
         fin, cnt = ctypes.c_double(), ctypes.c_int64()
+        if maxRanks is not None:
+            if isinstance(measurements, RankOneMeasurementSet):
+                raise NotImplementedError("maxRanks is supported for SinglePointMeasurementSet")
+            d = len(x.dimensions)
+            mr = [int(maxRanks)] * (d - 1) if np.isscalar(maxRanks) else [int(v) for v in maxRanks]
+            if len(mr) != d - 1:
+                raise ValueError("maxRanks needs one entry per inner bond")
+            # every rank increase records one more point than its iterations
+            cap = max(cap, 2 * cap + 2 * (d + 1))
+            trace = np.zeros(cap)
+            its = np.zeros(cap, dtype=np.int64)
+            rks = np.zeros((cap, d - 1), dtype=np.int64)
+            pos, pp = _i64(measurements.positions)
+            mra, pm = _i64(mr)
+            L.check(x.lib.xtt_adf_max_ranks(x.handle, pp, pv, pos.shape[0], pm, ctypes.byref(o), ctypes.byref(fin),
+                                            trace.ctypes.data_as(L.c_double_p), its.ctypes.data_as(L.c_int64_p),
+                                            rks.ctypes.data_as(L.c_int64_p), cap, ctypes.byref(cnt)))
+            if perfData is not None:
+                m = min(cnt.value, cap)
+                perfData.residuals = list(trace[:m])
+                perfData.iterations = list(its[:m])
+                perfData.ranks = rks[:m].tolist()
+            return fin.value
         if isinstance(measurements, RankOneMeasurementSet):
             vec, pu = _f64(measurements.vectors)
             L.check(x.lib.xtt_adf_rank_one(x.handle, pu, pv, vec.shape[0], ctypes.byref(o), ctypes.byref(fin),

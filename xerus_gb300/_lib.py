@@ -135,6 +135,9 @@ _SIGNATURES = {
     "xtt_als_energy_gradient": (ctypes.c_int, [VP, VP, VP, c_double_p, c_double_p, ctypes.c_int64]),
     "xtt_adf": (ctypes.c_int, [VP, c_int64_p, c_double_p, ctypes.c_int64, ctypes.POINTER(AdfOptions), c_double_p,
                                c_double_p, ctypes.c_int64, c_int64_p]),
+    "xtt_adf_max_ranks": (ctypes.c_int, [VP, c_int64_p, c_double_p, ctypes.c_int64, c_int64_p,
+                                         ctypes.POINTER(AdfOptions), c_double_p, c_double_p, c_int64_p, c_int64_p,
+                                         ctypes.c_int64, c_int64_p]),
     "xtt_adf_gradient": (ctypes.c_int, [VP, c_int64_p, c_double_p, ctypes.c_int64, c_double_p, c_double_p,
                                         ctypes.c_int64]),
 }

@@ -434,13 +434,9 @@ struct AdfData {
 	void res_grad(int k, int mode, const double* X, double* Gout, double gscale) {
 		const int len = int(x.ranks[k] * x.dims[k] * x.ranks[k + 1]);
 		if (fast) {
-			static bool attr = false;
-			if (!attr) {
-				const int mx = 100 * 1024;
-				XTT_CUDA(cudaFuncSetAttribute(k_adf_res_grad<float>, cudaFuncAttributeMaxDynamicSharedMemorySize, mx));
-				XTT_CUDA(cudaFuncSetAttribute(k_adf_res_grad<double>, cudaFuncAttributeMaxDynamicSharedMemorySize, mx));
-				attr = true;
-			}
+			const int mx = 100 * 1024;
+			func_attr_once(k_adf_res_grad<float>, cudaFuncAttributeMaxDynamicSharedMemorySize, mx);
+			func_attr_once(k_adf_res_grad<double>, cudaFuncAttributeMaxDynamicSharedMemorySize, mx);
 			ProfScope ps(c, "adf_res_grad");
 			if (f32)
 				k_adf_res_grad<float><<<unsigned(res_blocks), kAdfResThreads, res_smem<float>(k), c.stream>>>(
@@ -515,47 +511,76 @@ struct AdfData {
 }  // namespace
 
 AdfResult adf(Tensor& x, const int64_t* positions, const double* values, long long N, int64_t max_iter,
-              double target, double min_dec, int precision) {
-	// ADFVariant::InternalSolver::solve / solve_with_current_ranks (adf.cpp:489-604), x at its maximal ranks
+              double target, double min_dec, int precision, const std::vector<int64_t>* max_ranks,
+              const std::function<void(Tensor&)>& add_random_rank_one) {
+	// ADFVariant::InternalSolver::solve (adf.cpp:566-604) with solve_with_current_ranks
+	// (adf.cpp:489-542). Without max_ranks x keeps its ranks; with them (the operator()
+	// overload taking maxRanks, adf.h:263-266) every run that stops early at lower ranks is
+	// followed by a rank increase (adf.cpp:590-602) and another run.
 	Context& c = *x.ctx;
 	XTT_REQUIRE(!x.op, "ADF needs a TT tensor");
 	XTT_REQUIRE(N > 0, "need at very least one measurement");
+	XTT_REQUIRE(!max_ranks || int(max_ranks->size()) == x.d - 1, "maxRanks needs one entry per inner bond");
 	double ny2 = 0;
 	for (long long s = 0; s < N; ++s) ny2 += values[s] * values[s];
 	const double norm_y = std::sqrt(ny2);
 	move_core(x, 0, false);  // canonicalize_left (adf.cpp:582)
-	AdfData D(c, x, positions, values, N, precision != XTT_PRECISION_FP64);
 	AdfResult out;
+	// members of the reference's solver: they carry over between runs at different ranks
 	double residual_norm = DBL_MAX, last_residual_norm = DBL_MAX;
-	double dec1 = 0, dec2 = 0, dec3 = 0;
+	int64_t it = 0;
+	bool f32 = false;
 	const int d = x.d;
-	for (int64_t it = 0; max_iter == 0 || it < max_iter; ++it) {
-		move_core(x, 0, true);
-		for (int k = d - 1; k > 0; --k) D.backward(k);
-		D.res_grad(0, 0, x.core[0], D.G, 1.0);
-		last_residual_norm = residual_norm;
-		residual_norm = std::sqrt(D.read_rr()) / norm_y;
-		out.trace.push_back(residual_norm);
-		const double dec4 = dec3;
-		dec3 = dec2;
-		dec2 = dec1;
-		dec1 = residual_norm / last_residual_norm;
-		if (residual_norm < target || dec1 * dec2 * dec3 * dec4 > std::pow(min_dec, 4)) break;
-		for (int k = 0; k < d; ++k) {
-			if (k > 0) D.res_grad(k, 0, x.core[k], D.G, 1.0);
-			D.slicenorm(k);
-			k_adf_update<<<1, 128, 0, c.stream>>>(x.core[k], D.G, D.nrm, int(x.ranks[k]), int(x.dims[k]), int(x.ranks[k + 1]));
-			XTT_CUDA(cudaGetLastError());
-			c.count_launch();
-			if (k + 1 < d) {
-				move_core(x, k + 1, true);
-				D.forward(k);
+	auto inner_ranks = [&] { return std::vector<int64_t>(x.ranks.begin() + 1, x.ranks.end() - 1); };
+	auto solve_with_current_ranks = [&] {
+		// the stacks are sized for the current ranks (resize_stack_tensors, adf.cpp:194-204)
+		AdfData D(c, x, positions, values, N, precision != XTT_PRECISION_FP64);
+		f32 = D.f32;
+		double dec1 = 0, dec2 = 0, dec3 = 0;
+		for (; max_iter == 0 || it < max_iter; ++it) {
+			move_core(x, 0, true);
+			for (int k = d - 1; k > 0; --k) D.backward(k);
+			D.res_grad(0, 0, x.core[0], D.G, 1.0);
+			last_residual_norm = residual_norm;
+			residual_norm = std::sqrt(D.read_rr()) / norm_y;
+			out.trace.push_back(residual_norm);
+			out.trace_iteration.push_back(it);
+			out.trace_ranks.push_back(inner_ranks());
+			const double dec4 = dec3;
+			dec3 = dec2;
+			dec2 = dec1;
+			dec1 = residual_norm / last_residual_norm;
+			if (residual_norm < target || dec1 * dec2 * dec3 * dec4 > std::pow(min_dec, 4)) break;
+			for (int k = 0; k < d; ++k) {
+				if (k > 0) D.res_grad(k, 0, x.core[k], D.G, 1.0);
+				D.slicenorm(k);
+				k_adf_update<<<1, 128, 0, c.stream>>>(x.core[k], D.G, D.nrm, int(x.ranks[k]), int(x.dims[k]),
+				                                      int(x.ranks[k + 1]));
+				XTT_CUDA(cudaGetLastError());
+				c.count_launch();
+				if (k + 1 < d) {
+					move_core(x, k + 1, true);
+					D.forward(k);
+				}
 			}
+		}
+	};
+	solve_with_current_ranks();
+	if (max_ranks) {
+		XTT_REQUIRE(bool(add_random_rank_one), "the rank increase needs a source of random rank-one tensors");
+		const std::vector<int64_t> mr = reduce_to_maximal_ranks(*max_ranks, x.dims);
+		while (residual_norm > target && inner_ranks() != mr && (max_iter == 0 || it < max_iter)) {
+			// x += 1e-6 ||x|| r / ||r|| for a random rank-one TT r, then round(maxRanks)
+			move_core(x, 0, true);
+			add_random_rank_one(x);
+			round_tt(x, mr, kXerusEpsilon, nullptr);
+			solve_with_current_ranks();
 		}
 	}
 	out.residual = residual_norm;
 	out.checked_residual = residual_norm;
-	if (D.f32) {
+	out.iterations = it;
+	if (f32) {
 		// FP64 check of the FP32 form: ||P(x) - y|| / ||y|| from FP64 entries of the FP64 cores
 		std::vector<double> e(N);
 		entries(x, positions, N, e.data());
@@ -842,11 +867,7 @@ AdfResult adf_rank_one(Tensor& x, const double* vectors, const double* values, l
 		XTT_CUDA(cudaGetLastError());
 		c.count_launch();
 	};
-	static bool attr = false;
-	if (!attr) {
-		XTT_CUDA(cudaFuncSetAttribute(k_r1_res_grad, cudaFuncAttributeMaxDynamicSharedMemorySize, 100 * 1024));
-		attr = true;
-	}
+	func_attr_once(k_r1_res_grad, cudaFuncAttributeMaxDynamicSharedMemorySize, 100 * 1024);
 	auto res_grad = [&](int k) {
 		const R1Level L = level(k, x.core[k]);
 		const int P = L.r0 * L.r1, len = L.r0 * L.n * L.r1;

@@ -373,11 +373,7 @@ static int coop_grid(F kernel, Context& c, long long work_blocks) {
 // Launches `kernel` as one cluster of P CTAs if the device can schedule it; returns false otherwise.
 template <class K, class... Args>
 static bool launch_cluster(K kernel, int P, cudaStream_t s, Args... args) {
-	static bool attr = false;
-	if (!attr) {
-		XTT_CUDA(cudaFuncSetAttribute(kernel, cudaFuncAttributeNonPortableClusterSizeAllowed, 1));
-		attr = true;
-	}
+	func_attr_once(kernel, cudaFuncAttributeNonPortableClusterSizeAllowed, 1);
 	cudaLaunchConfig_t cfg = {};
 	cfg.gridDim = dim3(P);
 	cfg.blockDim = dim3(kGemmThreads);
@@ -706,11 +702,7 @@ CgResult local_solve(Context& c, const LocalShape& s, const double* L, const dou
 			m.sticky = c.d_ints + 11;
 			m.status = c.d_status;
 			const int smem = tc::kPSmem + 1024;
-			static bool attr = false;
-			if (!attr) {
-				XTT_CUDA(cudaFuncSetAttribute(k_cg_mixed_tc, cudaFuncAttributeMaxDynamicSharedMemorySize, smem));
-				attr = true;
-			}
+			func_attr_once(k_cg_mixed_tc, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
 			int occ = 0;
 			XTT_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, k_cg_mixed_tc, kGemmThreads, smem));
 			const int G = std::max(1, occ) * c.num_sms;

@@ -43,6 +43,25 @@ std::normal_distribution<double>& dist_for(double mean, double stddev) {
 	return g_custom;
 }
 
+// TTNetwork::random's fill (include/xerus/ttNetwork.h:128-155): every core in order,
+// row-major, one draw per entry from the library engine, then move_core(0) with
+// rank-revealing QR. t has its (maximal-reduced) ranks already.
+void fill_random(xtt::Tensor& t, double mean, double stddev) {
+	auto& dist = dist_for(mean, stddev);
+	std::vector<double> host;
+	for (int k = 0; k < t.d; ++k) {
+		host.resize(t.core_size(k));
+		for (auto& v : host) v = dist(g_engine);
+		XTT_CUDA(cudaMemcpyAsync(t.core[k], host.data(), host.size() * sizeof(double), cudaMemcpyHostToDevice,
+		                         t.ctx->stream));
+		XTT_CUDA(cudaStreamSynchronize(t.ctx->stream));
+	}
+	t.canonicalized = (t.d == 1);
+	t.core_position = 0;
+	xtt::move_core(t, 0, false);
+	t.ctx->sync();
+}
+
 }  // namespace
 
 namespace xtt {
@@ -68,6 +87,7 @@ int xtt_context_create(int device, xtt_context** out) {
 	return guard([&] {
 		ARG(out, "out is NULL");
 		*out = nullptr;
+		xtt::DeviceScope dev_scope(device);
 		auto* c = new xtt::Context(device);
 		*out = new xtt_context{c};
 	});
@@ -82,6 +102,7 @@ static void release_context(xtt::Context* c) {
 
 int xtt_context_destroy(xtt_context* ctx) {
 	return guard([&] {
+		xtt::DeviceScope dev_scope(ctx ? ctx->c->device : -1);
 		if (!ctx) return;
 		ctx->c->closing = true;
 		release_context(ctx->c);
@@ -91,6 +112,7 @@ int xtt_context_destroy(xtt_context* ctx) {
 
 int xtt_context_set_stream(xtt_context* ctx, void* stream) {
 	return guard([&] {
+		xtt::DeviceScope dev_scope(ctx ? ctx->c->device : -1);
 		ARG(ctx, "ctx is NULL");
 		XTT_CUDA(cudaStreamSynchronize(ctx->c->stream));
 		ctx->c->stream = stream ? static_cast<cudaStream_t>(stream) : ctx->c->own;
@@ -99,6 +121,7 @@ int xtt_context_set_stream(xtt_context* ctx, void* stream) {
 
 int xtt_context_synchronize(xtt_context* ctx) {
 	return guard([&] {
+		xtt::DeviceScope dev_scope(ctx ? ctx->c->device : -1);
 		ARG(ctx, "ctx is NULL");
 		ctx->c->sync();
 	});
@@ -106,6 +129,7 @@ int xtt_context_synchronize(xtt_context* ctx) {
 
 int xtt_context_kernel_launches(xtt_context* ctx, int64_t* count) {
 	return guard([&] {
+		xtt::DeviceScope dev_scope(ctx ? ctx->c->device : -1);
 		ARG(ctx && count, "NULL argument");
 		*count = ctx->c->launches;
 	});
@@ -113,6 +137,7 @@ int xtt_context_kernel_launches(xtt_context* ctx, int64_t* count) {
 
 int xtt_context_profile(xtt_context* ctx, int enable) {
 	return guard([&] {
+		xtt::DeviceScope dev_scope(ctx ? ctx->c->device : -1);
 		ARG(ctx, "ctx is NULL");
 		xtt::Context& c = *ctx->c;
 		c.resolve_profile();
@@ -123,6 +148,7 @@ int xtt_context_profile(xtt_context* ctx, int enable) {
 
 int xtt_context_profile_work(xtt_context* ctx, const char* name, double* bytes, double* flops) {
 	return guard([&] {
+		xtt::DeviceScope dev_scope(ctx ? ctx->c->device : -1);
 		ARG(ctx && name && bytes && flops, "NULL argument");
 		xtt::Context& c = *ctx->c;
 		c.resolve_profile();
@@ -138,6 +164,7 @@ int xtt_context_profile_work(xtt_context* ctx, const char* name, double* bytes, 
 
 int xtt_context_set_cg_path(xtt_context* ctx, int path) {
 	return guard([&] {
+		xtt::DeviceScope dev_scope(ctx ? ctx->c->device : -1);
 		ARG(ctx, "ctx is NULL");
 		ARG(path == XTT_CG_PATH_AUTO || path == XTT_CG_PATH_GRID || path == XTT_CG_PATH_TENSOR, "unknown CG path");
 		ctx->c->cg_path = path;
@@ -147,6 +174,7 @@ int xtt_context_set_cg_path(xtt_context* ctx, int path) {
 int xtt_gemm_tc(xtt_context* ctx, int64_t m, int64_t n, int64_t k, const double* A, int64_t lda, const double* B,
                 int64_t ldb, double* C, int64_t ldc, int32_t terms) {
 	return guard([&] {
+		xtt::DeviceScope dev_scope(ctx ? ctx->c->device : -1);
 		ARG(ctx && A && B && C, "NULL argument");
 		ARG(m > 0 && n > 0 && k > 0 && m < (1 << 30) && n < (1 << 30) && k < (1 << 30), "illegal GEMM size");
 		ARG(lda >= k && ldb >= n && ldc >= n, "leading dimension smaller than the row");
@@ -163,6 +191,7 @@ int xtt_gemm_tc(xtt_context* ctx, int64_t m, int64_t n, int64_t k, const double*
 
 int xtt_context_set_contraction_precision(xtt_context* ctx, int terms) {
 	return guard([&] {
+		xtt::DeviceScope dev_scope(ctx ? ctx->c->device : -1);
 		ARG(ctx, "ctx is NULL");
 		ARG(terms == 0 || terms == 1 || terms == 3, "contraction precision must be 0 (FP64), 3 (split TF32) or 1 (TF32)");
 		ctx->c->contraction_terms = terms;
@@ -171,6 +200,7 @@ int xtt_context_set_contraction_precision(xtt_context* ctx, int terms) {
 
 int xtt_context_set_svd_path(xtt_context* ctx, int path) {
 	return guard([&] {
+		xtt::DeviceScope dev_scope(ctx ? ctx->c->device : -1);
 		ARG(ctx, "ctx is NULL");
 		ARG(path == XTT_SVD_PATH_AUTO || path == XTT_SVD_PATH_JACOBI, "unknown SVD path");
 		ctx->c->svd_path = path;
@@ -179,6 +209,7 @@ int xtt_context_set_svd_path(xtt_context* ctx, int path) {
 
 int xtt_context_profile_get(xtt_context* ctx, const char* name, int64_t* launches, double* milliseconds) {
 	return guard([&] {
+		xtt::DeviceScope dev_scope(ctx ? ctx->c->device : -1);
 		ARG(ctx && name && launches && milliseconds, "NULL argument");
 		xtt::Context& c = *ctx->c;
 		c.resolve_profile();
@@ -195,6 +226,7 @@ int xtt_context_profile_get(xtt_context* ctx, const char* name, int64_t* launche
 int xtt_tensor_create(xtt_context* ctx, int is_operator, int64_t order, const int64_t* dims, const int64_t* ranks,
                       xtt_tensor** out) {
 	return guard([&] {
+		xtt::DeviceScope dev_scope(ctx ? ctx->c->device : -1);
 		ARG(ctx && dims && ranks && out, "NULL argument");
 		ARG(order > 0 && order < (1 << 20), "order must be positive");
 		*out = nullptr;
@@ -206,6 +238,7 @@ int xtt_tensor_create(xtt_context* ctx, int is_operator, int64_t order, const in
 
 int xtt_tensor_destroy(xtt_tensor* t) {
 	return guard([&] {
+		xtt::DeviceScope dev_scope(t ? t->t->ctx->device : -1);
 		if (!t) return;
 		xtt::Context* c = t->t->ctx;
 		delete t->t;
@@ -217,6 +250,7 @@ int xtt_tensor_destroy(xtt_tensor* t) {
 
 int xtt_tensor_copy(const xtt_tensor* src, xtt_tensor** out) {
 	return guard([&] {
+		xtt::DeviceScope dev_scope(src ? src->t->ctx->device : -1);
 		ARG(src && out, "NULL argument");
 		const xtt::Tensor& s = *src->t;
 		auto* t = new xtt::Tensor(s.ctx, s.op, s.d, s.dims.data(), s.ranks.data());
@@ -256,6 +290,7 @@ int xtt_tensor_size(const xtt_tensor* t, int64_t* count) {
 
 int xtt_tensor_set_cores(xtt_tensor* t, const double* host, int64_t count) {
 	return guard([&] {
+		xtt::DeviceScope dev_scope(t ? t->t->ctx->device : -1);
 		ARG(t && host, "NULL argument");
 		xtt::Tensor& x = *t->t;
 		ARG(count == int64_t(x.total_size()), "count does not match the tensor size");
@@ -272,6 +307,7 @@ int xtt_tensor_set_cores(xtt_tensor* t, const double* host, int64_t count) {
 
 int xtt_tensor_get_cores(const xtt_tensor* t, double* host, int64_t count) {
 	return guard([&] {
+		xtt::DeviceScope dev_scope(t ? t->t->ctx->device : -1);
 		ARG(t && host, "NULL argument");
 		const xtt::Tensor& x = *t->t;
 		ARG(count == int64_t(x.total_size()), "count does not match the tensor size");
@@ -327,6 +363,7 @@ int xtt_file_decode(const uint8_t* buffer, int64_t size, int* is_operator, int64
 
 int xtt_tensor_save(const xtt_tensor* t, const char* path) {
 	return guard([&] {
+		xtt::DeviceScope dev_scope(t ? t->t->ctx->device : -1);
 		ARG(t && path, "NULL argument");
 		const xtt::Tensor& x = *t->t;
 		std::vector<double> h(x.total_size());
@@ -343,6 +380,7 @@ int xtt_tensor_save(const xtt_tensor* t, const char* path) {
 
 int xtt_tensor_load(xtt_context* ctx, const char* path, xtt_tensor** out) {
 	return guard([&] {
+		xtt::DeviceScope dev_scope(ctx ? ctx->c->device : -1);
 		ARG(ctx && path && out, "NULL argument");
 		*out = nullptr;
 		const std::vector<uint8_t> b = xtt::read_file(path);
@@ -370,6 +408,7 @@ int xtt_tensor_load(xtt_context* ctx, const char* path, xtt_tensor** out) {
 
 int xtt_tensor_assign(xtt_tensor* t, const int64_t* ranks, const double* host, int64_t count) {
 	return guard([&] {
+		xtt::DeviceScope dev_scope(t ? t->t->ctx->device : -1);
 		ARG(t && ranks && host, "NULL argument");
 		xtt::Tensor& x = *t->t;
 		ARG(ranks[0] == 1 && ranks[x.d] == 1, "boundary ranks must be 1");
@@ -410,6 +449,7 @@ int xtt_tensor_set_canonical(xtt_tensor* t, int canonicalized, int64_t core_posi
 
 int xtt_tensor_scale(xtt_tensor* t, double f) {
 	return guard([&] {
+		xtt::DeviceScope dev_scope(t ? t->t->ctx->device : -1);
 		ARG(t, "NULL argument");
 		xtt::Tensor& x = *t->t;
 		const int k = x.canonicalized ? int(x.core_position) : 0;
@@ -437,6 +477,7 @@ int xtt_random_normal(double mean, double stddev, int64_t count, double* out) {
 int xtt_tensor_random(xtt_context* ctx, int64_t order, const int64_t* dims, const int64_t* inner_ranks, double mean,
                       double stddev, xtt_tensor** out) {
 	return guard([&] {
+		xtt::DeviceScope dev_scope(ctx ? ctx->c->device : -1);
 		ARG(ctx && dims && out && (order == 1 || inner_ranks), "NULL argument");
 		ARG(order > 0, "order must be positive");
 		*out = nullptr;
@@ -450,19 +491,7 @@ int xtt_tensor_random(xtt_context* ctx, int64_t order, const int64_t* dims, cons
 		ctx->c->tensors++;
 		xtt_tensor* h = new xtt_tensor{t};
 		try {
-			auto& dist = dist_for(mean, stddev);
-			std::vector<double> host;
-			for (int k = 0; k < t->d; ++k) {
-				host.resize(t->core_size(k));
-				for (auto& v : host) v = dist(g_engine);
-				XTT_CUDA(cudaMemcpyAsync(t->core[k], host.data(), host.size() * sizeof(double), cudaMemcpyHostToDevice,
-				                         t->ctx->stream));
-				XTT_CUDA(cudaStreamSynchronize(t->ctx->stream));
-			}
-			t->canonicalized = (order == 1);
-			t->core_position = 0;
-			xtt::move_core(*t, 0, false);
-			t->ctx->sync();
+			fill_random(*t, mean, stddev);
 		} catch (...) {
 			delete t;
 			delete h;
@@ -505,6 +534,7 @@ int xtt_random_positions(int64_t num, int64_t order, const int64_t* dims, int64_
 
 int xtt_move_core(xtt_tensor* x, int64_t position, int keep_rank) {
 	return guard([&] {
+		xtt::DeviceScope dev_scope(x ? x->t->ctx->device : -1);
 		ARG(x, "NULL argument");
 		xtt::ContractionPrecisionScope ps(*x->t->ctx);
 		xtt::move_core(*x->t, position, keep_rank != 0);
@@ -515,6 +545,7 @@ int xtt_move_core(xtt_tensor* x, int64_t position, int keep_rank) {
 int xtt_round(xtt_tensor* x, const int64_t* max_ranks, double eps, double* spectra, int64_t spectra_capacity,
               int64_t* spectra_count) {
 	return guard([&] {
+		xtt::DeviceScope dev_scope(x ? x->t->ctx->device : -1);
 		ARG(x && (max_ranks || x->t->d == 1), "NULL argument");
 		std::vector<int64_t> mr(max_ranks, max_ranks + (x->t->d - 1));
 		std::vector<double> sp;
@@ -531,6 +562,7 @@ int xtt_round(xtt_tensor* x, const int64_t* max_ranks, double eps, double* spect
 
 int xtt_dot(const xtt_tensor* x, const xtt_tensor* y, double* out) {
 	return guard([&] {
+		xtt::DeviceScope dev_scope(x ? x->t->ctx->device : -1);
 		ARG(x && y && out, "NULL argument");
 		ARG(x->t->ctx == y->t->ctx, "tensors belong to different contexts");
 		xtt::ContractionPrecisionScope ps(*x->t->ctx);
@@ -540,6 +572,7 @@ int xtt_dot(const xtt_tensor* x, const xtt_tensor* y, double* out) {
 
 int xtt_frob_norm(const xtt_tensor* x, double* out) {
 	return guard([&] {
+		xtt::DeviceScope dev_scope(x ? x->t->ctx->device : -1);
 		ARG(x && out, "NULL argument");
 		*out = xtt::frob_norm(*x->t);
 	});
@@ -547,6 +580,7 @@ int xtt_frob_norm(const xtt_tensor* x, double* out) {
 
 int xtt_residual(const xtt_tensor* A, const xtt_tensor* x, const xtt_tensor* b, double* out) {
 	return guard([&] {
+		xtt::DeviceScope dev_scope(x ? x->t->ctx->device : -1);
 		ARG(A && x && b && out, "NULL argument");
 		*out = xtt::residual(*A->t, *x->t, *b->t);
 	});
@@ -554,6 +588,7 @@ int xtt_residual(const xtt_tensor* A, const xtt_tensor* x, const xtt_tensor* b, 
 
 int xtt_entries(const xtt_tensor* x, const int64_t* positions, int64_t count, double* out) {
 	return guard([&] {
+		xtt::DeviceScope dev_scope(x ? x->t->ctx->device : -1);
 		ARG(x && (count == 0 || (positions && out)), "NULL argument");
 		xtt::entries(*x->t, positions, count, out);
 	});
@@ -605,6 +640,7 @@ int xtt_als_batch(xtt_context* ctx, int64_t count, const xtt_tensor* const* A, x
                   const xtt_tensor* const* b, const xtt_als_options* opt, int autotune, double* energies,
                   int64_t* local_iterations, xtt_batch_report* report) {
 	return guard([&] {
+		xtt::DeviceScope dev_scope(ctx ? ctx->c->device : -1);
 		ARG(ctx && A && x && b && opt, "NULL argument");
 		ARG(count > 0 && count <= (int64_t(1) << 24), "count must be in 1..2^24");
 		ARG(opt->assume_spd, "the batched sweep runs the SPD variant only");
@@ -638,6 +674,7 @@ int xtt_als(const xtt_tensor* A, xtt_tensor* x, const xtt_tensor* b, const xtt_a
             xtt_als_report* report, double* residual_trace, int64_t* flag_trace, double* energy_trace,
             int64_t trace_capacity) {
 	return guard([&] {
+		xtt::DeviceScope dev_scope(x ? x->t->ctx->device : -1);
 		ARG(x && b && opt, "NULL argument");
 		ARG(opt->local_tolerance > 0 && opt->local_tolerance < 1, "local_tolerance must be in (0, 1)");
 		ARG(opt->precision == XTT_PRECISION_FP64 || opt->precision == XTT_PRECISION_MIXED, "unknown precision");
@@ -662,6 +699,7 @@ int xtt_als(const xtt_tensor* A, xtt_tensor* x, const xtt_tensor* b, const xtt_a
 
 int xtt_apply(const xtt_tensor* A, const xtt_tensor* x, xtt_tensor** out) {
 	return guard([&] {
+		xtt::DeviceScope dev_scope(x ? x->t->ctx->device : -1);
 		ARG(A && x && out, "NULL argument");
 		*out = nullptr;
 		const xtt::Tensor& xs = *x->t;
@@ -685,6 +723,7 @@ int xtt_apply(const xtt_tensor* A, const xtt_tensor* x, xtt_tensor** out) {
 
 int xtt_add(xtt_tensor* x, const xtt_tensor* y, double alpha) {
 	return guard([&] {
+		xtt::DeviceScope dev_scope(x ? x->t->ctx->device : -1);
 		ARG(x && y, "NULL argument");
 		ARG(x->t->ctx == y->t->ctx, "x and y live on different contexts");
 		ARG(x != y, "x and y must be different tensors (copy y first)");
@@ -695,6 +734,7 @@ int xtt_add(xtt_tensor* x, const xtt_tensor* y, double alpha) {
 int xtt_als_energy_gradient(const xtt_tensor* A, const xtt_tensor* x, const xtt_tensor* b, double* energy,
                             double* grad, int64_t count) {
 	return guard([&] {
+		xtt::DeviceScope dev_scope(x ? x->t->ctx->device : -1);
 		ARG(A && x && b && energy, "NULL argument");
 		std::vector<double> g;
 		*energy = xtt::als_energy_gradient(*A->t, *x->t, *b->t, g);
@@ -708,6 +748,7 @@ int xtt_als_energy_gradient(const xtt_tensor* A, const xtt_tensor* x, const xtt_
 int xtt_adf(xtt_tensor* x, const int64_t* positions, const double* values, int64_t num, const xtt_adf_options* opt,
             double* final_residual, double* residual_trace, int64_t trace_capacity, int64_t* trace_count) {
 	return guard([&] {
+		xtt::DeviceScope dev_scope(x ? x->t->ctx->device : -1);
 		ARG(x && positions && values && opt, "NULL argument");
 		ARG(opt->precision == XTT_PRECISION_FP64 || opt->precision == XTT_PRECISION_MIXED, "unknown precision");
 		xtt::AdfResult r = xtt::adf(*x->t, positions, values, num, opt->max_iterations, opt->target_residual,
@@ -720,10 +761,45 @@ int xtt_adf(xtt_tensor* x, const int64_t* positions, const double* values, int64
 	});
 }
 
+int xtt_adf_max_ranks(xtt_tensor* x, const int64_t* positions, const double* values, int64_t num,
+                      const int64_t* max_ranks, const xtt_adf_options* opt, double* final_residual,
+                      double* residual_trace, int64_t* iteration_trace, int64_t* rank_trace, int64_t trace_capacity,
+                      int64_t* trace_count) {
+	return guard([&] {
+		xtt::DeviceScope dev_scope(x ? x->t->ctx->device : -1);
+		ARG(x && positions && values && opt && max_ranks, "NULL argument");
+		ARG(opt->precision == XTT_PRECISION_FP64 || opt->precision == XTT_PRECISION_MIXED, "unknown precision");
+		xtt::Tensor& t = *x->t;
+		const std::vector<int64_t> mr(max_ranks, max_ranks + (t.d - 1));
+		for (auto v : mr) ARG(v > 0, "maximal ranks must be positive");
+		// adf.cpp:592-595: rnd = TTTensor::random(dims, 1) from the library's random state,
+		// x += (1e-6 ||x||) rnd / ||rnd|| (the factor applied to rnd's core 0)
+		auto add_random_rank_one = [](xtt::Tensor& xx) {
+			const std::vector<int64_t> ones(size_t(xx.d) + 1, 1);
+			xtt::Tensor rnd(xx.ctx, false, xx.d, xx.dims.data(), ones.data());
+			fill_random(rnd, 0.0, 1.0);
+			const double f = (1e-6 * xtt::frob_norm(xx)) * (1.0 / xtt::frob_norm(rnd));
+			xtt::scale(*rnd.ctx, rnd.core[0], f, rnd.core_size(0));
+			xtt::tt_add(xx, rnd, 1.0);
+		};
+		xtt::AdfResult r = xtt::adf(t, positions, values, num, opt->max_iterations, opt->target_residual,
+		                            opt->min_decrease, opt->precision, &mr, add_random_rank_one);
+		t.ctx->sync();
+		if (final_residual) *final_residual = r.checked_residual;
+		for (size_t i = 0; i < r.trace.size() && int64_t(i) < trace_capacity; ++i) {
+			if (residual_trace) residual_trace[i] = r.trace[i];
+			if (iteration_trace) iteration_trace[i] = r.trace_iteration[i];
+			if (rank_trace) std::copy(r.trace_ranks[i].begin(), r.trace_ranks[i].end(), rank_trace + i * (t.d - 1));
+		}
+		if (trace_count) *trace_count = int64_t(r.trace.size());
+	});
+}
+
 int xtt_geometric_cg(const xtt_tensor* A, xtt_tensor* x, const xtt_tensor* b, int64_t num_steps,
                      double convergence_epsilon, int assume_spd, double* residual, double* residual_trace,
                      int64_t trace_capacity, int64_t* trace_count) {
 	return guard([&] {
+		xtt::DeviceScope dev_scope(x ? x->t->ctx->device : -1);
 		ARG(x && b, "NULL argument");
 		ARG(num_steps >= 0, "num_steps must be >= 0");
 		const xtt::RiemannReport r =
@@ -739,6 +815,7 @@ int xtt_steepest_descent(const xtt_tensor* A, xtt_tensor* x, const xtt_tensor* b
                          double convergence_epsilon, int assume_spd, double* residual, double* residual_trace,
                          int64_t trace_capacity, int64_t* trace_count) {
 	return guard([&] {
+		xtt::DeviceScope dev_scope(x ? x->t->ctx->device : -1);
 		ARG(x && b, "NULL argument");
 		ARG(num_steps >= 0, "num_steps must be >= 0");
 		const xtt::RiemannReport r =
@@ -782,6 +859,7 @@ int xtt_random_rank_one(int64_t num, int64_t order, const int64_t* dims, double*
 
 int xtt_entries_rank_one(const xtt_tensor* x, const double* vectors, int64_t count, double* out) {
 	return guard([&] {
+		xtt::DeviceScope dev_scope(x ? x->t->ctx->device : -1);
 		ARG(x && (count == 0 || (vectors && out)), "NULL argument");
 		xtt::entries_rank_one(*x->t, vectors, count, out);
 	});
@@ -791,6 +869,7 @@ int xtt_adf_rank_one(xtt_tensor* x, const double* vectors, const double* values,
                      const xtt_adf_options* opt, double* final_residual, double* residual_trace,
                      int64_t trace_capacity, int64_t* trace_count) {
 	return guard([&] {
+		xtt::DeviceScope dev_scope(x ? x->t->ctx->device : -1);
 		ARG(x && vectors && values && opt, "NULL argument");
 		ARG(opt->precision == XTT_PRECISION_FP64, "rank-one ADF runs in FP64");
 		xtt::AdfResult r = xtt::adf_rank_one(*x->t, vectors, values, num, opt->max_iterations, opt->target_residual,
@@ -806,6 +885,7 @@ int xtt_adf_rank_one(xtt_tensor* x, const double* vectors, const double* values,
 int xtt_adf_gradient(const xtt_tensor* x, const int64_t* positions, const double* values, int64_t num, double* loss,
                      double* grad, int64_t count) {
 	return guard([&] {
+		xtt::DeviceScope dev_scope(x ? x->t->ctx->device : -1);
 		ARG(x && positions && values && loss, "NULL argument");
 		std::vector<double> g;
 		*loss = xtt::adf_gradient(*x->t, positions, values, num, g);

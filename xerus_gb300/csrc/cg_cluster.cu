@@ -457,12 +457,15 @@ static bool cc_plan(const LocalShape& ls, bool mixed, CcArgs& a) {
 
 template <class K>
 static bool cc_launch(K kernel, const CcArgs& a, cudaStream_t st) {
+	// function attributes and occupancy are per device: the caches are keyed by it
 	static std::mutex mu;
-	static std::map<std::tuple<const void*, int, size_t>, bool> ok_cache;
-	static std::map<const void*, size_t> smem_set;
-	const auto key = std::make_tuple((const void*)kernel, a.P, a.lay.total);
+	static std::map<std::tuple<int, const void*, int, size_t>, bool> ok_cache;
+	static std::map<std::pair<int, const void*>, size_t> smem_set;
+	int dev = 0;
+	XTT_CUDA(cudaGetDevice(&dev));
+	const auto key = std::make_tuple(dev, (const void*)kernel, a.P, a.lay.total);
 	std::lock_guard<std::mutex> g(mu);
-	size_t& cur = smem_set[(const void*)kernel];
+	size_t& cur = smem_set[std::make_pair(dev, (const void*)kernel)];
 	if (cur < a.lay.total) {
 		if (cur == 0) XTT_CUDA(cudaFuncSetAttribute(kernel, cudaFuncAttributeNonPortableClusterSizeAllowed, 1));
 		XTT_CUDA(cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, int(a.lay.total)));

@@ -31,6 +31,35 @@ struct Error : std::runtime_error {
 			                                     __FILE__ + ":" + std::to_string(__LINE__));                  \
 	} while (0)
 
+// Makes `device` current for the scope's lifetime and restores the previous device
+// afterwards (device < 0: no change). Every entry point switches to the device of the
+// context it works on, so one host thread can drive contexts on several GPUs.
+struct DeviceScope {
+	int prev = -1;
+	explicit DeviceScope(int device) {
+		if (device < 0) return;
+		int cur = -1;
+		XTT_CUDA(cudaGetDevice(&cur));
+		if (cur != device) {
+			XTT_CUDA(cudaSetDevice(device));
+			prev = cur;
+		}
+	}
+	~DeviceScope() {
+		if (prev >= 0) cudaSetDevice(prev);
+	}
+	DeviceScope(const DeviceScope&) = delete;
+	DeviceScope& operator=(const DeviceScope&) = delete;
+};
+
+// cudaFuncSetAttribute acts on the current device only: applies (kernel, attribute,
+// value) once per device, thread-safe (defined in ops.cu).
+void func_attr_once(const void* kernel, cudaFuncAttribute attr, int value);
+template <class K>
+inline void func_attr_once(K* kernel, cudaFuncAttribute attr, int value) {
+	func_attr_once(reinterpret_cast<const void*>(kernel), attr, value);
+}
+
 // Device-side status word of a context: kernels record the first failure here
 // instead of trapping, the host reads it after synchronising.
 enum DeviceStatus : int {

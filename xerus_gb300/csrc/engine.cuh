@@ -11,6 +11,7 @@
 #include <cstdint>
 #include <string>
 #include <utility>
+#include <functional>
 #include <vector>
 
 #include "common.cuh"
@@ -229,12 +230,20 @@ void tt_add(Tensor& x, const Tensor& y, double f);
 struct AdfResult {
 	double residual = 0;          // the iteration's own residual (FP32 in the FP32 form)
 	double checked_residual = 0;  // FP64 residual of the returned x
-	std::vector<double> trace;
+	int64_t iterations = 0;       // the solver's iteration counter at the end
+	std::vector<double> trace;    // PerformanceData: residual, iteration count and inner ranks per point
+	std::vector<int64_t> trace_iteration;
+	std::vector<std::vector<int64_t>> trace_ranks;
 };
+// xerus's EPSILON (include/xerus/basic.h:50), the default cutoff of TTNetwork::round
+constexpr double kXerusEpsilon = 8 * 2.220446049250313e-16;
 // precision: XTT_PRECISION_FP64, or XTT_PRECISION_MIXED for FP32 stacks and
-// per-sample arithmetic with FP64 cores, QR and final check.
+// per-sample arithmetic with FP64 cores, QR and final check. max_ranks (d-1 inner
+// ranks) switches on the rank increase; add_random_rank_one then adds
+// 1e-6 ||x|| r / ||r|| for a fresh random rank-one TT r to x (canonical at core 0).
 AdfResult adf(Tensor& x, const int64_t* positions, const double* values, long long N, int64_t max_iter, double target,
-              double min_dec, int precision = XTT_PRECISION_FP64);
+              double min_dec, int precision = XTT_PRECISION_FP64, const std::vector<int64_t>* max_ranks = nullptr,
+              const std::function<void(Tensor&)>& add_random_rank_one = {});
 // Riemannian CG on the fixed-rank TT manifold (GeometricCGVariant with the submanifold
 // retraction and projective vector transport); A null: minimise ||x - b||.
 struct RiemannReport {

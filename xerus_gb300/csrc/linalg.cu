@@ -1397,11 +1397,7 @@ bool transfer_small_fits(const TransferArgs& t) { return transfer_small_bytes(t)
 void launch_transfer_small(const TransferArgs& t, cudaStream_t s) {
 	const size_t bytes = transfer_small_bytes(t);
 	XTT_REQUIRE(bytes > 0, "internal: transfer_core shapes do not fit the one-launch kernel");
-	static bool attr = false;
-	if (!attr) {
-		XTT_CUDA(cudaFuncSetAttribute(k_transfer_small, cudaFuncAttributeMaxDynamicSharedMemorySize, int(kDynSmemMax)));
-		attr = true;
-	}
+	func_attr_once(k_transfer_small, cudaFuncAttributeMaxDynamicSharedMemorySize, int(kDynSmemMax));
 	k_transfer_small<<<1, kQrSmallThreads, bytes, s>>>(t);
 	XTT_CUDA(cudaGetLastError());
 }
@@ -1422,11 +1418,7 @@ void launch_qr(const QrArgs& a, cudaStream_t s) {
 	const int mw = a.transpose ? a.n : a.m, nw = a.transpose ? a.m : a.n;
 	if (!a.pivot && (mw < 48 || nw < 8) && nw <= kBlkQrMaxCols && mw <= kQrSmallMaxRows) {
 		const size_t bytes = size_t(mw) * nw * sizeof(double);
-		static bool attr_s = false;
-		if (!attr_s) {
-			XTT_CUDA(cudaFuncSetAttribute(k_qr_small, cudaFuncAttributeMaxDynamicSharedMemorySize, int(kDynSmemMax)));
-			attr_s = true;
-		}
+		func_attr_once(k_qr_small, cudaFuncAttributeMaxDynamicSharedMemorySize, int(kDynSmemMax));
 		if (bytes <= kDynSmemMax) {
 			k_qr_small<<<1, kQrSmallThreads, bytes, s>>>(a);
 			XTT_CUDA(cudaGetLastError());
@@ -1437,12 +1429,8 @@ void launch_qr(const QrArgs& a, cudaStream_t s) {
 		Qc1Layout l1;
 		const int P1 = qr_cl1_size(mw, nw, a.want_q != 0, l1);
 		if (P1 > 1) {
-			static bool attr1 = false;
-			if (!attr1) {
-				XTT_CUDA(cudaFuncSetAttribute(k_qr_cl1, cudaFuncAttributeMaxDynamicSharedMemorySize, int(kDynSmemMax)));
-				XTT_CUDA(cudaFuncSetAttribute(k_qr_cl1, cudaFuncAttributeNonPortableClusterSizeAllowed, 1));
-				attr1 = true;
-			}
+			func_attr_once(k_qr_cl1, cudaFuncAttributeMaxDynamicSharedMemorySize, int(kDynSmemMax));
+			func_attr_once(k_qr_cl1, cudaFuncAttributeNonPortableClusterSizeAllowed, 1);
 			cudaLaunchConfig_t cfg = {};
 			cfg.gridDim = dim3(P1);
 			cfg.blockDim = dim3(kQ1Threads);
@@ -1467,12 +1455,8 @@ void launch_qr(const QrArgs& a, cudaStream_t s) {
 		Qc2Layout l2;
 		const int P2 = qr_cl2_size(mw, nw, l2);
 		if (P2 > 1) {
-			static bool attr2 = false;
-			if (!attr2) {
-				XTT_CUDA(cudaFuncSetAttribute(k_qr_cl2, cudaFuncAttributeMaxDynamicSharedMemorySize, int(kDynSmemMax)));
-				XTT_CUDA(cudaFuncSetAttribute(k_qr_cl2, cudaFuncAttributeNonPortableClusterSizeAllowed, 1));
-				attr2 = true;
-			}
+			func_attr_once(k_qr_cl2, cudaFuncAttributeMaxDynamicSharedMemorySize, int(kDynSmemMax));
+			func_attr_once(k_qr_cl2, cudaFuncAttributeNonPortableClusterSizeAllowed, 1);
 			cudaLaunchConfig_t cfg = {};
 			cfg.gridDim = dim3(P2);
 			cfg.blockDim = dim3(kQ2Threads);
@@ -1496,12 +1480,8 @@ void launch_qr(const QrArgs& a, cudaStream_t s) {
 	QcLayout lay;
 	const int P = qr_cluster_size(mw, nw, lay);
 	if (P > 1) {
-		static bool attr = false;
-		if (!attr) {
-			XTT_CUDA(cudaFuncSetAttribute(k_qr_cluster, cudaFuncAttributeMaxDynamicSharedMemorySize, int(kDynSmemMax)));
-			XTT_CUDA(cudaFuncSetAttribute(k_qr_cluster, cudaFuncAttributeNonPortableClusterSizeAllowed, 1));
-			attr = true;
-		}
+		func_attr_once(k_qr_cluster, cudaFuncAttributeMaxDynamicSharedMemorySize, int(kDynSmemMax));
+		func_attr_once(k_qr_cluster, cudaFuncAttributeNonPortableClusterSizeAllowed, 1);
 		cudaLaunchConfig_t cfg = {};
 		cfg.gridDim = dim3(P);
 		cfg.blockDim = dim3(kQcThreads);
@@ -1526,11 +1506,7 @@ void launch_qr(const QrArgs& a, cudaStream_t s) {
 	const int use_smem = full <= kDynSmemMax ? 1 : 0;
 	XTT_REQUIRE(use_smem || a.work, "QR workspace missing");
 	XTT_REQUIRE(aux <= kDynSmemMax, "QR: too many columns");
-	static bool attr = false;
-	if (!attr) {
-		XTT_CUDA(cudaFuncSetAttribute(k_qr, cudaFuncAttributeMaxDynamicSharedMemorySize, int(kDynSmemMax)));
-		attr = true;
-	}
+	func_attr_once(k_qr, cudaFuncAttributeMaxDynamicSharedMemorySize, int(kDynSmemMax));
 	k_qr<<<1, kQrThreads, use_smem ? full : aux, s>>>(a, use_smem);
 	XTT_CUDA(cudaGetLastError());
 }
@@ -2021,12 +1997,8 @@ void launch_svd(const SvdArgs& a, cudaStream_t s) {
 	SvcLayout lay;
 	const int P = svd_cluster_size(a.m, a.n, lay);
 	if (P > 1) {
-		static bool attr_c = false;
-		if (!attr_c) {
-			XTT_CUDA(cudaFuncSetAttribute(k_svd_cluster, cudaFuncAttributeMaxDynamicSharedMemorySize, int(kDynSmemMax)));
-			XTT_CUDA(cudaFuncSetAttribute(k_svd_cluster, cudaFuncAttributeNonPortableClusterSizeAllowed, 1));
-			attr_c = true;
-		}
+		func_attr_once(k_svd_cluster, cudaFuncAttributeMaxDynamicSharedMemorySize, int(kDynSmemMax));
+		func_attr_once(k_svd_cluster, cudaFuncAttributeNonPortableClusterSizeAllowed, 1);
 		cudaLaunchConfig_t cfg = {};
 		cfg.gridDim = dim3(P);
 		cfg.blockDim = dim3(kSvcThreads);
@@ -2046,11 +2018,7 @@ void launch_svd(const SvdArgs& a, cudaStream_t s) {
 		}
 		cudaGetLastError();
 	}
-	static bool attr = false;
-	if (!attr) {
-		XTT_CUDA(cudaFuncSetAttribute(k_svd, cudaFuncAttributeMaxDynamicSharedMemorySize, int(kDynSmemMax)));
-		attr = true;
-	}
+	func_attr_once(k_svd, cudaFuncAttributeMaxDynamicSharedMemorySize, int(kDynSmemMax));
 	k_svd<<<1, kSvdThreads, use_smem ? full : aux, s>>>(a, use_smem);
 	XTT_CUDA(cudaGetLastError());
 }
@@ -2390,11 +2358,7 @@ __global__ void __launch_bounds__(kSvf32Threads) k_svd_f32(const double* __restr
 
 void launch_svd_f32(const double* X, long long ldx, int p, int q, float* W, cudaStream_t s) {
 	XTT_REQUIRE(svd_f32_fits(p, q), "internal: FP32 Jacobi stage does not fit one CTA");
-	static bool attr = false;
-	if (!attr) {
-		XTT_CUDA(cudaFuncSetAttribute(k_svd_f32, cudaFuncAttributeMaxDynamicSharedMemorySize, int(kDynSmemMax)));
-		attr = true;
-	}
+	func_attr_once(k_svd_f32, cudaFuncAttributeMaxDynamicSharedMemorySize, int(kDynSmemMax));
 	const size_t smem = (size_t(p) * q + size_t(q) * q) * sizeof(float);
 	k_svd_f32<<<1, kSvf32Threads, smem, s>>>(X, ldx, p, q, W, 12);
 	XTT_CUDA(cudaGetLastError());

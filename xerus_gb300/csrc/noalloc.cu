@@ -45,7 +45,9 @@ constexpr int kMaxDevices = 64;
 std::mutex g_setup_mutex;
 double* g_scratch_ptr[kMaxDevices] = {};
 
-// Device address of g_zip_scratch on `device` (looked up once per device).
+// Device address of g_zip_scratch on `device`, looked up once per device and kept for
+// the life of the process: a cudaDeviceReset (or a reset of the primary context) after
+// the first call on a device is not supported, the cached address would be stale.
 double* scratch_on(int device, cudaError_t& err) {
 	std::lock_guard<std::mutex> lock(g_setup_mutex);
 	err = cudaSuccess;
@@ -140,6 +142,9 @@ extern "C" int xtt_dot_noalloc(int64_t order, const int64_t* dims, const int64_t
 	double* M1 = base + kZipM;
 	double* T = base + 2 * kZipM;
 	cudaStream_t s = static_cast<cudaStream_t>(stream);
+	// clear an error an earlier, unrelated call left behind, so that the check after the
+	// launches reports this call's own launch errors only
+	cudaGetLastError();
 	k_zip_start<<<1, 1, 0, s>>>(M0);
 	const double* xc = x_cores;
 	const double* yc = y_cores;

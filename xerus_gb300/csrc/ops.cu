@@ -4,12 +4,29 @@
 #include <algorithm>
 #include <cmath>
 #include <cstring>
+#include <mutex>
+#include <set>
+#include <tuple>
 
 #include <cooperative_groups.h>
 
 #include "engine.cuh"
 
 namespace xtt {
+
+// ------------------------------------------------------------ kernel attributes
+
+void func_attr_once(const void* kernel, cudaFuncAttribute attr, int value) {
+	static std::mutex mu;
+	static std::set<std::tuple<int, const void*, int, int>> done;
+	int dev = 0;
+	XTT_CUDA(cudaGetDevice(&dev));
+	const auto key = std::make_tuple(dev, kernel, int(attr), value);
+	std::lock_guard<std::mutex> lock(mu);
+	if (done.count(key)) return;
+	XTT_CUDA(cudaFuncSetAttribute(kernel, attr, value));
+	done.insert(key);
+}
 
 // ------------------------------------------------------------ context
 
@@ -1062,8 +1079,8 @@ double residual(const Tensor* Ap, const Tensor& x, const Tensor& b) {
 			rl = kq;
 		}
 	}
-	c.join();
-	// left half on the context's stream: carry R (rr x O0_k), starting from [1]
+	// left half on the context's stream, concurrently with the right half: carry R (rr x O0_k),
+	// starting from [1]
 	int64_t rr = 1;
 	fill(c, lb.R, 1.0, 1);
 	for (int k = 0; k < mid; ++k) {
@@ -1080,6 +1097,7 @@ double residual(const Tensor* Ap, const Tensor& x, const Tensor& b) {
 		qr_r_only(lb.Z, m, dm.O1, 0, lb.R);
 		rr = kq;
 	}
+	c.join();  // the meeting reads the right half's carry L
 	// meet at core mid: W = (R Y_mid) L, ||y|| = ||W||
 	const Dims dm = block(mid, lb);
 	Gemm<double> g1;  // Z = R (rr x O0) * Y (O0 x n O1)

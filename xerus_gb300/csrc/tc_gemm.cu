@@ -231,13 +231,9 @@ __global__ void k_tc_reduce(Gemm<T> g, int S, const float* part) {
 
 template <class T, int NT>
 void launch_tc(Context& c, const Gemm<T>& g) {
-	static bool attr = false;
 	constexpr int kMaxChunks = 64;  // K offsets tabulated per CTA: at most 64 chunks (2048 K)
-	if (!attr) {
-		XTT_CUDA(cudaFuncSetAttribute(k_tc_gemm<T, NT>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-		                              2 * stage_bytes<NT>() + int(sizeof(long long)) * (2 * (kTcM + kTcN) + 2 * kMaxChunks * tc::kTileK)));
-		attr = true;
-	}
+	func_attr_once(k_tc_gemm<T, NT>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+	                              2 * stage_bytes<NT>() + int(sizeof(long long)) * (2 * (kTcM + kTcN) + 2 * kMaxChunks * tc::kTileK));
 	const long long tiles = (long long)g.batch * ((g.M + kTcM - 1) / kTcM) * ((g.N + kTcN - 1) / kTcN);
 	XTT_REQUIRE(tiles < (1ll << 31), "GEMM too large");
 	// split K when the tiles alone leave most SMs idle (deterministic: partials reduced in order)
