@@ -254,21 +254,41 @@ def bench_adf(xg, ctx, torch, stream, iters, peak, cpu):
     return out
 
 
+def config4_params(count, seed=SEED):
+    """Shapes of the config-4 batch, instance by instance: (d, n, shift, rhs rank, start
+    rank) with d ~ U{4..16}, n ~ U{2..8}, shift ~ U[0.1, 1], rhs rank ~ U{2..8}, start
+    rank ~ U{4..32} (maximal-reduced when drawn)."""
+    rng = np.random.default_rng(seed)
+    out = []
+    for _ in range(count):
+        d, n = int(rng.integers(4, 17)), int(rng.integers(2, 9))
+        shift = float(rng.uniform(0.1, 1.0))
+        out.append((d, n, shift, int(rng.integers(2, 9)), int(rng.integers(4, 33))))
+    return out
+
+
+def config4_instance(xg, ctx, i, params, seed=SEED):
+    """Instance i of the config-4 batch on the device: its own random state (seed + i),
+    the Laplacian sum plus its shift, a random rhs and a random normalised start."""
+    d, n, shift, rb, rx = params
+    xg.seed(seed + i)
+    A = xg.TTOperator.from_cores(xg.laplacian_cores(d, n, shift=shift), ctx=ctx)
+    b = xg.TTTensor.random([n] * d, rb, ctx=ctx)
+    x = xg.TTTensor.random([n] * d, rx, ctx=ctx)
+    x /= x.frob_norm()
+    return A, x, b
+
+
 def bench_batch(xg, ctx, count, steps):
     """Config-4 batch: `count` independent SPD problems, d ~ U{4..16}, n ~ U{2..8},
     Laplacian sum + shift U[0.1, 1], rhs rank ~ U{2..8}, start rank ~ U{4..32}
     (maximal-reduced), 4 ALS sweeps each, in one persistent launch (CUDA graph)."""
-    rng = np.random.default_rng(SEED)
-    xg.seed(SEED)
     As, xs, bs = [], [], []
-    for i in range(count):
-        d, n = int(rng.integers(4, 17)), int(rng.integers(2, 9))
-        shift = float(rng.uniform(0.1, 1.0))
-        As.append(xg.TTOperator.from_cores(xg.laplacian_cores(d, n, shift=shift), ctx=ctx))
-        bs.append(xg.TTTensor.random([n] * d, int(rng.integers(2, 9)), ctx=ctx))
-        x = xg.TTTensor.random([n] * d, int(rng.integers(4, 33)), ctx=ctx)
-        x /= x.frob_norm()
+    for i, prm in enumerate(config4_params(count)):
+        A, x, b = config4_instance(xg, ctx, i, prm)
+        As.append(A)
         xs.append(x)
+        bs.append(b)
     saved = [(x.get_flat(), x.all_ranks()) for x in xs]
 
     def restore():

@@ -836,8 +836,8 @@ static void case_adf_rankinc() {
 }
 
 // Rank-revealing QC / CQ with a clear gap: z = x (+) s w stacks x and a scaled
-// independent TT w in block cores (the sum x + s w). With s = 1e-13 the w part's
-// R_kk sit near 1e-13 R_00, far above the cutoff 16 eps R_00 and far above
+// independent TT w in block cores (the sum x + s w). With s = 1e-10 the w part's
+// R_kk sit at 1e-13..1e-11 R_00, far above the cutoff 16 eps R_00 and far above
 // rounding, so they are kept; with s = 1e-17 they sit far below the cutoff and are
 // dropped wherever R_00 > 0 (blasLapackWrapper.cpp:269,343 compare with the signed
 // R_00). Either way the rank decision does not depend on rounding.
@@ -865,6 +865,30 @@ static TTTensor block_sum2(const TTTensor& x, const TTTensor& w, double s) {
 	return z;
 }
 
+// Rescales every bond of z by a diagonal D (core k times D on its right index, core k+1
+// times D^-1 on its left): the same tensor, but no core has orthonormal rows or columns,
+// so the pivoted factorisations never choose between columns of equal norm (random TTs
+// come right-orthogonalised, whose equal column norms make the pivot order a matter of
+// rounding).
+static void rescale_bonds(TTTensor& z, uint64_t seed) {
+	std::mt19937_64 rng(seed);
+	std::uniform_real_distribution<double> u(0.5, 2.0);
+	const size_t d = z.degree();
+	for (size_t k = 0; k + 1 < d; ++k) {
+		Tensor a = z.get_component(k), b = z.get_component(k + 1);
+		a.use_dense_representation();
+		b.use_dense_representation();
+		const size_t r = a.dimensions[2], na = a.dimensions[0] * a.dimensions[1], nb = b.dimensions[1] * b.dimensions[2];
+		for (size_t j = 0; j < r; ++j) {
+			const double f = u(rng);
+			for (size_t i = 0; i < na; ++i) a[i * r + j] *= f;
+			for (size_t i = 0; i < nb; ++i) b[j * nb + i] /= f;
+		}
+		z.set_component(k, a);
+		z.set_component(k + 1, b);
+	}
+}
+
 static void case_qc_gap() {
 	reseed();
 	const std::vector<size_t> dims{4, 3, 5, 4, 3, 4, 3};
@@ -872,8 +896,9 @@ static void case_qc_gap() {
 	TTTensor w = TTTensor::random(dims, {2, 3, 3, 4, 2, 2});
 	auto pos = probe_positions(dims, 100, 41);
 	for (const auto& tag : {std::string("keep"), std::string("drop")}) {
-		const double s = tag == "keep" ? 1e-13 : 1e-17;
+		const double s = tag == "keep" ? 1e-10 : 1e-17;
 		TTTensor z = block_sum2(x, w, s);
+		rescale_bonds(z, 43);
 		save_tt(tag + "_z", z);
 		for (size_t p : {dims.size() - 1, size_t(0), size_t(3)}) {
 			TTTensor y = z;

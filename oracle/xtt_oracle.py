@@ -545,22 +545,28 @@ FLAG_FINISHED_FULLSWEEP = 3
 
 def _push_left_op(L, xc, ac):
     # L'(c1,c2,c3) = sum L(a1,a2,a3) x(a1,i,c1) A(a2,i,j,c2) x(a3,j,c3)   (als.cpp:184-200, 247)
-    return np.einsum("xky,xic,kijl,yjm->clm", L, xc, ac, xc, optimize=True)
+    t = np.tensordot(L, xc, axes=([0], [0]))             # (k, y, i, c)
+    t = np.tensordot(t, ac, axes=([0, 2], [0, 1]))       # (y, c, j, l)
+    return np.tensordot(t, xc, axes=([0, 2], [0, 1]))    # (c, l, m)
 
 
 def _push_right_op(R, xc, ac):
     # R'(a1,a2,a3) = sum x(a1,i,c1) A(a2,i,j,c2) x(a3,j,c3) R(c1,c2,c3)   (als.cpp:239)
-    return np.einsum("xic,kijl,yjm,clm->xky", xc, ac, xc, R, optimize=True)
+    t = np.tensordot(xc, R, axes=([2], [0]))             # (x, i, l, m)
+    t = np.tensordot(t, ac, axes=([1, 2], [1, 3]))       # (x, m, k, j)
+    return np.tensordot(t, xc, axes=([1, 3], [2, 1]))    # (x, k, y)
 
 
 def _push_left_rhs(Lb, bc, xc):
     # Lb'(c1,c2) = sum Lb(a1,a2) b(a1,i,c1) x(a2,i,c2)   (als.cpp:202-215, 250)
-    return np.einsum("st,sic,tid->cd", Lb, bc, xc, optimize=True)
+    t = np.tensordot(Lb, bc, axes=([0], [0]))            # (t, i, c)
+    return np.tensordot(t, xc, axes=([0, 1], [0, 1]))    # (c, d)
 
 
 def _push_right_rhs(Rb, bc, xc):
     # Rb'(a1,a2) = sum b(a1,i,c1) x(a2,i,c2) Rb(c1,c2)   (als.cpp:242)
-    return np.einsum("sic,tid,cd->st", bc, xc, Rb, optimize=True)
+    t = np.tensordot(bc, Rb, axes=([2], [0]))            # (s, i, d)
+    return np.tensordot(t, xc, axes=([1, 2], [1, 2]))    # (s, t)
 
 
 # non-symmetric operators: the stacks carry A^T A and A^T b (als.cpp:184-215, 392-399, 414-420)
@@ -613,6 +619,50 @@ def local_operator(L, Acores, R):
     half = op.ndim // 2
     N = int(np.prod(op.shape[:half]))
     return op.reshape(N, N), op.shape[half:]
+
+
+def local_apply(L, Acores, R, v):
+    """The local operator of construct_local_operator (als.cpp:383-401) applied to a
+    local vector v (a, j, b) without forming it: (x, i, y)."""
+    if len(Acores) != 1:
+        raise ValueError("one site only")
+    t = np.tensordot(v, R, axes=([2], [2]))              # (a, j, y, l)
+    t = np.tensordot(t, Acores[0], axes=([1, 3], [2, 3]))  # (a, y, k, i)
+    t = np.tensordot(L, t, axes=([1, 2], [2, 0]))          # (x, y, i)
+    return t.transpose(0, 2, 1)
+
+
+def cg_solve(apply, rhs, tol: float = 1e-15, maxit: int | None = None):
+    """Conjugate gradients on an SPD system to relative residual tol (or until the
+    recomputed residual stops decreasing): the solution of the dense solve to rounding."""
+    n = rhs.size
+    xv = np.zeros(n)
+    r = rhs.copy()
+    p = r.copy()
+    rr = float(r @ r)
+    bb = rr
+    best = rr
+    since = 0
+    for it in range(1, (maxit or 20 * n) + 1):
+        if rr <= tol * tol * bb:
+            break
+        ap = apply(p)
+        alpha = rr / float(p @ ap)
+        xv += alpha * p
+        if it % 50 == 0:
+            r = rhs - apply(xv)   # refresh the recursive residual
+        else:
+            r -= alpha * ap
+        rn = float(r @ r)
+        p = r + (rn / rr) * p
+        rr = rn
+        if rr < 0.5 * best:
+            best, since = rr, 0
+        else:
+            since += 1
+            if since > 200:
+                break
+    return xv
 
 
 def local_rhs(Lb, bcores, Rb):
@@ -817,12 +867,25 @@ def als(A: TTOp | None, x: TT, b: TT, sites: int = 1, num_half_sweeps: int = 0, 
             if normal:
                 M, shape_x = local_operator_normal(Lop[-1], A.cores[cur:cur + sites], Rop[-1])
                 rhs = local_rhs_normal(Lb[-1], b.cores[cur:cur + sites], A.cores[cur:cur + sites], Rb[-1])
+            elif solver == "cg":
+                M = None
+                rhs = local_rhs(Lb[-1], b.cores[cur:cur + sites], Rb[-1])
+                shape_x = rhs.shape
             else:
                 M, shape_x = local_operator(Lop[-1], A.cores[cur:cur + sites], Rop[-1])
                 rhs = local_rhs(Lb[-1], b.cores[cur:cur + sites], Rb[-1])
-            N = M.shape[0]
+            N = rhs.size
             rhs = rhs.reshape(N)
-            if solver == "asd":
+            if solver == "cg":
+                # the exact local solve by matrix-free CG to the rounding floor, for local
+                # systems too large to factor densely (the solution is the same)
+                Lc, Rc, Ac = Lop[-1], Rop[-1], A.cores[cur:cur + sites]
+                xv = cg_solve(lambda v: local_apply(Lc, Ac, Rc, v.reshape(shape_x)).reshape(N), rhs)
+                xv = xv.reshape(shape_x)
+                if sites != 1:
+                    raise ValueError("the matrix-free local solve is for one site")
+                x.cores[cur] = xv
+            elif solver == "asd":
                 xv = x.cores[cur].reshape(N)
                 grad = rhs - M @ xv
                 if normal:

@@ -87,3 +87,65 @@ def test_als_batch_graph_replay_and_autotune(ctx):
     x = insts[0][1].copy()
     ref = o.als_spd(insts[0][0], x, insts[0][2], 1, 4, 0.0)
     assert abs(runs[0][0][0] / ref.energy - 1) < REL_TOL
+
+
+_CFG4 = {}
+
+
+def _config4_reference(ctx, hs):
+    """24 instances of the benchmarked config-4 batch (d <= 16, n <= 8, start rank <= 32):
+    the six with the largest local systems (up to 8192 unknowns) and 18 drawn at random,
+    with the oracle's ALS_SPD result for each (its exact local solve by matrix-free CG,
+    the same solution as the dense factorisation at these sizes), computed once."""
+    if hs in _CFG4:
+        return _CFG4[hs]
+    import bench
+    params = bench.config4_params(4096)
+
+    def local_unknowns(p):
+        d, n, _, _, rx = p
+        rr = o.reduce_to_maximal_ranks([rx] * (d - 1), [n] * d)
+        return max(rr) ** 2 * n
+
+    order = sorted(range(len(params)), key=lambda i: -local_unknowns(params[i]))
+    rng = np.random.default_rng(17)
+    pick = [int(i) for i in order[:6]] + [int(i) for i in rng.choice(order[6:], 18, replace=False)]
+    out = []
+    for i in pick:
+        A, x, b = bench.config4_instance(xg, ctx, i, params[i])
+        Ah = o.TTOp(A.get_cores())
+        xh = o.TT(x.get_cores(), x.canonicalized, x.corePosition)
+        bh = o.TT(b.get_cores(), b.canonicalized, b.corePosition)
+        x0 = xh.copy()
+        ref = o.als_spd(Ah, xh, bh, 1, hs, 0.0, solver="cg")
+        out.append((i, params[i], Ah, x0, bh, ref.energy, xh))
+    _CFG4[hs] = out
+    return out
+
+
+@pytest.mark.parametrize("precision", ["fp64", "mixed"])
+def test_als_batch_matches_oracle_at_config4_sizes(ctx, precision):
+    """The benchmarked batch's own instances at their real sizes, in one batched call:
+    the largest local systems (8192 unknowns in one CTA), uneven orders and ranks under
+    the longest-first schedule. Each instance's energy within 1e-10 of the oracle's,
+    probed entries within 1e-9."""
+    hs = 8
+    cases = _config4_reference(ctx, hs)
+    assert max(p[1] * max(o.reduce_to_maximal_ranks([p[4]] * (p[0] - 1), [p[1]] * p[0])) ** 2
+               for _, p, *_ in cases) == 8192
+    devs = [(xg.TTOperator.from_cores(Ah.cores, ctx=ctx),
+             xg.TTTensor.from_cores(x0.cores, ctx=ctx, canonicalized=x0.canonicalized, core_position=x0.core_position),
+             xg.TTTensor.from_cores(bh.cores, ctx=ctx, canonicalized=bh.canonicalized, core_position=bh.core_position))
+            for _, _, Ah, x0, bh, _, _ in cases]
+    v = xg.ALS_SPD.copy()
+    v.convergenceEpsilon = 0.0
+    if precision == "mixed":
+        v.precision = xg.MIXED
+    en, it, rep = xg.als_batch([t[0] for t in devs], [t[1] for t in devs], [t[2] for t in devs], variant=v,
+                               numHalfSweeps=hs)
+    assert np.all(it > 0)
+    rng = np.random.default_rng(23)
+    for (i, p, _, _, _, e_ref, x_ref), (_, xd, _), e in zip(cases, devs, en):
+        assert abs(e / e_ref - 1) < REL_TOL, (i, p, e, e_ref)
+        pos = np.stack([rng.integers(0, n, 32) for n in x_ref.dims], axis=1).astype(np.int64)
+        assert rel_err(xd.entries(pos), o.tt_entries(x_ref, pos)) < 1e-9, (i, p)

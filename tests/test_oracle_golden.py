@@ -288,8 +288,8 @@ def test_adf_rank_increase(golden):
 
 @pytest.mark.parametrize("tag", ["keep", "drop"])
 def test_qc_rank_rule_with_clear_gap(golden, tag):
-    """Rank-revealing move_core on x + s w (block cores): with s = 1e-13 the w part is
-    kept, with s = 1e-17 dropped where R_00 > 0; exact ranks either way."""
+    """Rank-revealing move_core on x + s w (block cores, bonds rescaled): with s = 1e-10
+    the w part is kept, with s = 1e-17 dropped where R_00 > 0; exact ranks either way."""
     z = golden("qc_gap")
     zz = tt_of(z, f"{tag}_z", canonicalized=False)
     for p in (6, 0, 3):
