@@ -5,7 +5,7 @@
 //   golden_driver <case> <outdir>
 //
 // Cases: rng, tt_random, dot, movecore, round, als, dmrg, adf, adf_cfg5, fileio, als_nonspd,
-// arith, adf_rankone, gcg, adf_rankinc, qc_gap, timing_*.
+// arith, adf_rankone, gcg, adf_rankinc, qc_gap, and the timings time_cfg1/2/4/5.
 // Every case seeds xerus::misc::randomEngine with 0xBAADF00D and resets
 // xerus::misc::defaultNormalDistribution (dropping a cached polar variate) first,
 // so a case's draws do not depend on the cases run before it.
@@ -939,6 +939,115 @@ static void case_fileio() {
 	save_file_bytes("A_bytes", g_out + "/A.xrs");
 }
 
+// ------------------------------------------------------------------- timing
+// The reference's own implementation timed on this host (wall clock around the
+// algorithm call only; inputs drawn as in the golden cases, PerformanceData
+// inactive). Each case writes <tag>_seconds (and workload facts) like the others.
+using Clock = std::chrono::steady_clock;
+static double secs(Clock::time_point a, Clock::time_point b) { return std::chrono::duration<double>(b - a).count(); }
+
+// ALS_SPD on the d=8, n=4 Laplacian: rank 8 for 20 half-sweeps with convergenceEpsilon 0
+// (the configuration as stated), and rank 32 for the two half-sweeps that reach 1e-8.
+static void case_time_cfg1() {
+	const size_t d = 8, n = 4;
+	TTOperator A = laplace_operator(d, n, nullptr, false);
+	for (size_t rank : {size_t(8), size_t(32)}) {
+		reseed();
+		TTTensor b = TTTensor::random(std::vector<size_t>(d, n), 4);
+		TTTensor x = TTTensor::random(std::vector<size_t>(d, n), rank);
+		x /= frob_norm(x);
+		ALSVariant als = ALS_SPD;
+		als.convergenceEpsilon = 0.0;
+		const size_t hs = rank == 8 ? 20 : 2;
+		auto t0 = Clock::now();
+		als(A, x, b, hs);
+		auto t1 = Clock::now();
+		const std::string tag = "r" + std::to_string(rank) + "_hs" + std::to_string(hs);
+		save_scalar(tag + "_seconds", secs(t0, t1));
+		save_scalar(tag + "_residual", residual_of(A, x, b));
+	}
+}
+
+// Configuration 2: move_core(d-1) (QC sweep), round(32) and the dot product on two
+// independent d=32, n=4, rank-64 tensors with N(0, 1/8) entries.
+static void case_time_cfg2() {
+	reseed();
+	std::normal_distribution<double> dist(0.0, 0.125);
+	const std::vector<size_t> dims(32, 4);
+	TTTensor x = TTTensor::random(dims, std::vector<size_t>(31, 64), dist, misc::randomEngine);
+	TTTensor y = TTTensor::random(dims, std::vector<size_t>(31, 64), dist, misc::randomEngine);
+	Index i;
+	const int reps = 5;
+	double tm = 0, tr = 0, td = 0;
+	for (int rep = 0; rep < reps; ++rep) {
+		TTTensor z = x;
+		auto t0 = Clock::now();
+		z.move_core(31);
+		auto t1 = Clock::now();
+		TTTensor w = x;
+		auto t2 = Clock::now();
+		w.round(size_t(32));
+		auto t3 = Clock::now();
+		const double v = value_t(x(i & 0) * y(i & 0));
+		auto t4 = Clock::now();
+		(void)v;
+		tm += secs(t0, t1);
+		tr += secs(t2, t3);
+		td += secs(t3, t4);
+	}
+	save_scalar("move_core_seconds", tm / reps);
+	save_scalar("round_seconds", tr / reps);
+	save_scalar("dot_seconds", td / reps);
+}
+
+// Configuration 4: ALS_SPD, 4 sweeps, on a sample of the batch's instances (their
+// shapes read from <outdir>/cfg4_params.txt: d n shift rhs_rank start_rank seed per
+// line), one instance per OpenMP thread; instances per second over the sample.
+static void case_time_cfg4() {
+	std::ifstream f(g_out + "/cfg4_params.txt");
+	struct P { size_t d, n; double shift; size_t rb, rx; uint64_t seed; };
+	std::vector<P> ps;
+	P p;
+	while (f >> p.d >> p.n >> p.shift >> p.rb >> p.rx >> p.seed) ps.push_back(p);
+	std::vector<TTOperator> As(ps.size());
+	std::vector<TTTensor> xs(ps.size()), bs(ps.size());
+	for (size_t q = 0; q < ps.size(); ++q) {
+		misc::randomEngine.seed(ps[q].seed);
+		misc::defaultNormalDistribution.reset();
+		As[q] = laplace_operator(ps[q].d, ps[q].n, nullptr, false, ps[q].shift);
+		bs[q] = TTTensor::random(std::vector<size_t>(ps[q].d, ps[q].n), ps[q].rb);
+		xs[q] = TTTensor::random(std::vector<size_t>(ps[q].d, ps[q].n), ps[q].rx);
+		xs[q] /= frob_norm(xs[q]);
+	}
+	ALSVariant als = ALS_SPD;
+	als.convergenceEpsilon = 0.0;
+	auto t0 = Clock::now();
+#pragma omp parallel for schedule(dynamic, 1)
+	for (size_t q = 0; q < ps.size(); ++q) als(As[q], xs[q], bs[q], size_t(8));
+	auto t1 = Clock::now();
+	save_scalar("sample_seconds", secs(t0, t1));
+	save_scalar("sample_instances", double(ps.size()));
+}
+
+// Configuration 5: 50 ADF iterations, d=10, n=8, rank 6, 200 000 samples.
+static void case_time_cfg5() {
+	reseed();
+	const std::vector<size_t> dims(10, 8);
+	TTTensor target = TTTensor::random(dims, 6);
+	SinglePointMeasurementSet m = SinglePointMeasurementSet::random(200000, dims);
+	m.measure(target);
+	std::normal_distribution<double> noise(0.0, 1e-6);
+	for (auto& v : m.measuredValues) v += noise(misc::randomEngine);
+	TTTensor x = TTTensor::random(dims, 6);
+	ADFVariant adf(50, 0.0, 1.0);
+	auto t0 = Clock::now();
+	PerformanceData none(false, false);
+	const double res = adf(x, m, none);
+	auto t1 = Clock::now();
+	save_scalar("adf50_seconds", secs(t0, t1));
+	save_scalar("adf50_residual", res);
+}
+
 int main(int argc, char** argv) {
 	if (argc != 3) {
 		std::fprintf(stderr, "usage: %s <case> <outdir>\n", argv[0]);
@@ -962,6 +1071,10 @@ int main(int argc, char** argv) {
 	else if (c == "gcg") case_gcg();
 	else if (c == "adf_rankinc") case_adf_rankinc();
 	else if (c == "qc_gap") case_qc_gap();
+	else if (c == "time_cfg1") case_time_cfg1();
+	else if (c == "time_cfg2") case_time_cfg2();
+	else if (c == "time_cfg4") case_time_cfg4();
+	else if (c == "time_cfg5") case_time_cfg5();
 	else {
 		std::fprintf(stderr, "unknown case %s\n", c.c_str());
 		return 2;

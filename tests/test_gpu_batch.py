@@ -127,8 +127,12 @@ def _config4_reference(ctx, hs):
 def test_als_batch_matches_oracle_at_config4_sizes(ctx, precision):
     """The benchmarked batch's own instances at their real sizes, in one batched call:
     the largest local systems (8192 unknowns in one CTA), uneven orders and ranks under
-    the longest-first schedule. Each instance's energy within 1e-10 of the oracle's,
-    probed entries within 1e-9."""
+    the longest-first schedule. Each instance's energy within 1e-10 of the oracle's.
+    The iterate itself is not that well determined: at start rank 32 the sweep moves
+    slowly along near-flat directions, so the local solves' tolerance (1e-13 here,
+    ~1e-15 in the oracle) shows up ~1e6-fold in the entries after 8 half-sweeps (the
+    oracle alone moves 1e-7 between tolerances 1e-15 and 1e-13 on instance 941), while
+    the energy, stationary there, does not: probed entries within 1e-6."""
     hs = 8
     cases = _config4_reference(ctx, hs)
     assert max(p[1] * max(o.reduce_to_maximal_ranks([p[4]] * (p[0] - 1), [p[1]] * p[0])) ** 2
@@ -148,4 +152,4 @@ def test_als_batch_matches_oracle_at_config4_sizes(ctx, precision):
     for (i, p, _, _, _, e_ref, x_ref), (_, xd, _), e in zip(cases, devs, en):
         assert abs(e / e_ref - 1) < REL_TOL, (i, p, e, e_ref)
         pos = np.stack([rng.integers(0, n, 32) for n in x_ref.dims], axis=1).astype(np.int64)
-        assert rel_err(xd.entries(pos), o.tt_entries(x_ref, pos)) < 1e-9, (i, p)
+        assert rel_err(xd.entries(pos), o.tt_entries(x_ref, pos)) < 1e-6, (i, p)
