@@ -8,8 +8,8 @@ case's ``.npy`` outputs are packed into ``<case>.npz`` here.
     python tests/golden/make_golden.py            # all cases
     python tests/golden/make_golden.py als round  # selected cases
 
-Needs the reference sources at $XERUS_REF (default /root/reference) and SciPy's
-bundled OpenBLAS; the fixtures record the OpenBLAS build they came from.
+Needs the reference sources at $XERUS_REF and SciPy's bundled OpenBLAS; the
+fixtures record the OpenBLAS build they came from.
 """
 import glob
 import os
@@ -26,7 +26,9 @@ CASES = ["rng", "tt_random", "dot", "movecore", "round", "als", "dmrg", "adf", "
 
 def main(argv):
     cases = argv[1:] or CASES
-    ref = os.environ.get("XERUS_REF", "/root/reference")
+    ref = os.environ.get("XERUS_REF")
+    if not ref:
+        raise SystemExit("set XERUS_REF to the xerus source tree")
     subprocess.run(["make", "-j8", f"REF={ref}"], cwd=os.path.join(ROOT, "oracle", "ref"), check=True)
     driver = os.path.join(ROOT, "oracle", "_ref", "golden_driver")
     import scipy
