@@ -366,6 +366,28 @@ int xtt_steepest_descent(const xtt_tensor* A, xtt_tensor* x, const xtt_tensor* b
                          double convergence_epsilon, int assume_spd, double* residual, double* residual_trace,
                          int64_t trace_capacity, int64_t* trace_count);
 
+/* The retractions of src/xerus/algorithms/retractions.cpp for the Riemannian solvers:
+ * SUBMANIFOLD: SubmanifoldRetractionI / II (:222-236), componentwise addition of the
+ * tangent components, then move_core(0, keepRank) - what xtt_geometric_cg and
+ * xtt_steepest_descent use. HOSVD: HOSVDRetractionI / II (:43-55), the step added as a
+ * TT of larger rank (the tangent vector's added_to_base, or x + step), then
+ * round(oldRanks). ALS: ALSRetractionI / II (:57-69), ALSVariant(1, 2, lapack_solver,
+ * false) without an operator fits x (its ranks kept) to that TT. */
+typedef enum xtt_retraction {
+	XTT_RETRACTION_SUBMANIFOLD = 0,
+	XTT_RETRACTION_HOSVD = 1,
+	XTT_RETRACTION_ALS = 2
+} xtt_retraction;
+/* xtt_geometric_cg / xtt_steepest_descent with the retraction chosen
+ * (GeometricCGVariant(..., retraction, ProjectiveVectorTransport), include/xerus/algorithms/cg.h:55-62;
+ * SteepestDescentVariant(..., retraction), include/xerus/algorithms/steepestDescent.h:60-63). */
+int xtt_geometric_cg_retraction(const xtt_tensor* A, xtt_tensor* x, const xtt_tensor* b, int64_t num_steps,
+                                double convergence_epsilon, int assume_spd, int retraction, double* residual,
+                                double* residual_trace, int64_t trace_capacity, int64_t* trace_count);
+int xtt_steepest_descent_retraction(const xtt_tensor* A, xtt_tensor* x, const xtt_tensor* b, int64_t num_steps,
+                                    double convergence_epsilon, int assume_spd, int retraction, double* residual,
+                                    double* residual_trace, int64_t trace_capacity, int64_t* trace_count);
+
 /* RankOneMeasurementSet (include/xerus/measurments.h:94-140): a sample is
  * <x, u_1 (x) ... (x) u_d> for vectors u_k of length n_k; `vectors` holds each
  * sample's vectors concatenated (num x sum n_k doubles, row-major).

@@ -5,7 +5,7 @@
 //   golden_driver <case> <outdir>
 //
 // Cases: rng, tt_random, dot, movecore, round, als, dmrg, adf, adf_cfg5, fileio, als_nonspd,
-// arith, adf_rankone, gcg, adf_rankinc, qc_gap, and the timings time_cfg1/2/4/5.
+// arith, adf_rankone, gcg, adf_rankinc, qc_gap, retractions, and the timings time_cfg1/2/4/5.
 // Every case seeds xerus::misc::randomEngine with 0xBAADF00D and resets
 // xerus::misc::defaultNormalDistribution (dropping a cached polar variate) first,
 // so a case's draws do not depend on the cases run before it.
@@ -632,6 +632,44 @@ static void case_gcg() {
 	run_sd("sd_free", SteepestDescent, nullptr, 6);
 }
 
+// The HOSVD and ALS retractions (retractions.cpp:43-69) in GeometricCG (type I, with the
+// projective vector transport) and SteepestDescent (type II), on the gcg case's inputs.
+static void case_retractions() {
+	reseed();
+	const size_t d = 5, n = 3;
+	const std::vector<size_t> dims(d, n);
+	TTOperator A = laplace_operator(d, n, nullptr, false, 1.0);
+	TTOperator An = laplace_operator(d, n, nullptr, false, 1.0, 0.4);
+	TTTensor b = TTTensor::random(dims, 2);
+	TTTensor x = TTTensor::random(dims, 2);
+	save_op("A", A);
+	save_op("An", An);
+	save_tt("b", b);
+	save_tt("x0", x);
+	auto pos = probe_positions(dims, 100, 47);
+	const std::vector<std::pair<std::string, TTRetractionI>> r1{{"hosvd", HOSVDRetractionI}, {"als", ALSRetractionI}};
+	for (const auto& r : r1) {
+		run_gcg("gcg_" + r.first + "_spd", GeometricCGVariant(0, 1e-8, true, r.second, ProjectiveVectorTransport), &A, x,
+		        b, 8, pos);
+		run_gcg("gcg_" + r.first + "_ls", GeometricCGVariant(0, 1e-8, false, r.second, ProjectiveVectorTransport), &An,
+		        x, b, 8, pos);
+	}
+	const std::vector<std::pair<std::string, TTRetractionII>> r2{{"hosvd", HOSVDRetractionII}, {"als", ALSRetractionII}};
+	for (const auto& r : r2) {
+		for (int spd = 1; spd >= 0; --spd) {
+			TTTensor y = x;
+			PerformanceData perf(false, true);
+			SteepestDescentVariant v(0, 1e-8, spd != 0, r.second);
+			const double res = v(spd ? A : An, y, b, size_t(8), perf);
+			const std::string tag = "sd_" + r.first + (spd ? "_spd" : "_ls");
+			save(tag + "_perf_residual", perf_residuals(perf));
+			save_scalar(tag + "_residual", res);
+			save(tag + "_ranks", ranks_of(y));
+			save_probes(tag + "_x", y, pos);
+		}
+	}
+}
+
 static void case_dmrg() {
 	reseed();
 	const size_t d = 8, n = 4;
@@ -1071,6 +1109,7 @@ int main(int argc, char** argv) {
 	else if (c == "gcg") case_gcg();
 	else if (c == "adf_rankinc") case_adf_rankinc();
 	else if (c == "qc_gap") case_qc_gap();
+	else if (c == "retractions") case_retractions();
 	else if (c == "time_cfg1") case_time_cfg1();
 	else if (c == "time_cfg2") case_time_cfg2();
 	else if (c == "time_cfg4") case_time_cfg4();

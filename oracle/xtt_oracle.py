@@ -1351,13 +1351,43 @@ def submanifold_retraction(x: TT, change: Tangent) -> None:
     move_core(x, 0, keep_rank=True)
 
 
+def _retract_to_ranks(x: TT, y: TT, kind: str) -> None:
+    """HOSVDRetractionI / II (retractions.cpp:43-55): y.round(oldRanks); ALSRetractionI /
+    II (:57-69): ALSVariant(1, 2, lapack_solver, false) without an operator fits x (ranks
+    kept) to y. y is the step added as a TT (added_to_base, or x + step)."""
+    old = list(x.ranks)
+    if kind == "hosvd":
+        tt_round(y, old)
+        x.cores, x.canonicalized, x.core_position = y.cores, y.canonicalized, y.core_position
+    else:
+        als(None, x, y, 1, 2, 1e-6, assume_spd=False)
+
+
+def retraction_i(x: TT, change: Tangent, kind: str = "submanifold") -> None:
+    """Type I retractions of x at change's base along change."""
+    if kind == "submanifold":
+        submanifold_retraction(x, change)
+    else:
+        _retract_to_ranks(x, change.added_to_base(), kind)
+
+
+def retraction_ii(x: TT, step: TT, kind: str = "submanifold") -> None:
+    """Type II retractions of x along the TT step: SubmanifoldRetractionII projects it on
+    the tangent space at x first (retractions.cpp:222-225); the others add it as a TT."""
+    if kind == "submanifold":
+        submanifold_retraction(x, tangent_project(x, step))
+    else:
+        _retract_to_ranks(x, tt_add(x, step), kind)
+
+
 def _op_transpose(A: TTOp) -> TTOp:
     return TTOp([c.transpose(0, 2, 1, 3).copy() for c in A.cores])
 
 
 def geometric_cg(A: TTOp | None, x: TT, b: TT, num_steps: int = 0, conv_eps: float = 1e-8,
-                 assume_spd: bool = False) -> tuple[float, list]:
-    """GeometricCGVariant::solve (algorithms/cg.cpp:34-120) with SubmanifoldRetractionI,
+                 assume_spd: bool = False, retraction: str = "submanifold") -> tuple[float, list]:
+    """GeometricCGVariant::solve (algorithms/cg.cpp:34-120) with SubmanifoldRetractionI
+    (or HOSVDRetractionI / ALSRetractionI: retraction "hosvd" / "als"),
     ProjectiveVectorTransport and line_search (steepestDescent.cpp:37-80). x is updated in
     place; returns (final residual ||b - A x||, residual after every step)."""
     norm_b = orthogonal_norm(b)
@@ -1380,13 +1410,13 @@ def geometric_cg(A: TTOp | None, x: TT, b: TT, num_steps: int = 0, conv_eps: flo
         dir_norm = direction.norm()
         curr = alpha / change
         old = x.copy()
-        submanifold_retraction(x, direction.scaled(curr / dir_norm))
+        retraction_i(x, direction.scaled(curr / dir_norm), retraction)
         best_res = calc_residual()
         best_alpha, best_x = curr, x.copy()
         while True:
             curr *= change
             x.cores, x.canonicalized, x.core_position = [c.copy() for c in old.cores], old.canonicalized, old.core_position
-            submanifold_retraction(x, direction.scaled(curr / dir_norm))
+            retraction_i(x, direction.scaled(curr / dir_norm), retraction)
             new_res = calc_residual()
             if new_res < best_res:
                 best_res, best_alpha, best_x = new_res, curr, x.copy()
@@ -1397,7 +1427,7 @@ def geometric_cg(A: TTOp | None, x: TT, b: TT, num_steps: int = 0, conv_eps: flo
         while alpha > 1e-16 and best_res > residual - 1e-4 * alpha / dir_norm * derivative:
             alpha *= change
             x.cores, x.canonicalized, x.core_position = [c.copy() for c in old.cores], old.canonicalized, old.core_position
-            submanifold_retraction(x, direction.scaled(alpha / dir_norm))
+            retraction_i(x, direction.scaled(alpha / dir_norm), retraction)
             best_res = calc_residual()
         state["res_norm_after"] = best_res
         return alpha, best_res
@@ -1431,11 +1461,12 @@ def geometric_cg(A: TTOp | None, x: TT, b: TT, num_steps: int = 0, conv_eps: flo
 
 
 def steepest_descent(A: TTOp | None, x: TT, b: TT, num_steps: int = 0, conv_eps: float = 1e-8,
-                     assume_spd: bool = False) -> tuple[float, list]:
+                     assume_spd: bool = False, retraction: str = "submanifold") -> tuple[float, list]:
     """SteepestDescentVariant::solve (algorithms/steepestDescent.cpp:83-175) with
     SubmanifoldRetractionII (retractions.cpp:222-225: project the TT step onto the tangent
-    space at x, then the submanifold retraction). Absolute stopping tests, step doubling
-    and halving as in the reference; returns (||b - A x||, residual after every step)."""
+    space at x, then the submanifold retraction), or HOSVDRetractionII / ALSRetractionII.
+    Absolute stopping tests, step doubling and halving as in the reference; returns
+    (||b - A x||, residual after every step)."""
     def residual_tt():
         ax = x.copy() if A is None else op_apply(A, x)
         return tt_add(b, tt_scale(ax, -1.0))
@@ -1449,16 +1480,23 @@ def steepest_descent(A: TTOp | None, x: TT, b: TT, num_steps: int = 0, conv_eps:
         steps += 1
         y = res if (A is None or assume_spd) else op_apply(_op_transpose(A), res)
         old = x.copy()
-        w = tangent_project(x, y)
+        w = tangent_project(x, y) if retraction == "submanifold" else None
+
+        def step(f):
+            if w is not None:
+                submanifold_retraction(x, w.scaled(f))
+            else:
+                retraction_ii(x, tt_scale(y, f), retraction)
+
         alpha *= 2
-        submanifold_retraction(x, w.scaled(alpha))
+        step(alpha)
         last = curr
         res = residual_tt()
         curr = orthogonal_norm(res.copy())
         while alpha > 1e-30 and last < curr:
             alpha /= 2
             x.cores, x.canonicalized, x.core_position = [c.copy() for c in old.cores], old.canonicalized, old.core_position
-            submanifold_retraction(x, w.scaled(alpha))
+            step(alpha)
             res = residual_tt()
             curr = orthogonal_norm(res.copy())
         trace.append(curr)

@@ -630,6 +630,29 @@ def test_adf_rank_increase_matches_reference(ctx, golden):
     assert rel_err(x.entries(z["x_final_probe_pos"]), z["x_final_probe_val"]) < 1e-8
 
 
+@pytest.mark.parametrize("alg,kind,spd", [(a, k, s) for a in ("gcg", "sd") for k in ("hosvd", "als") for s in (True, False)])
+def test_hosvd_and_als_retractions_match_reference(ctx, golden, alg, kind, spd):
+    """GeometricCG (type I retractions, projective vector transport) and SteepestDescent
+    (type II) with the HOSVD retraction (the step added as a TT, rounded back to the old
+    ranks) and the ALS retraction (two operator-free ALS half-sweeps fit x to it),
+    retractions.cpp:43-69: the reference's residual after every step and its final
+    iterate."""
+    z = golden("retractions")
+    A = dev_op(ctx, op_of(z, "A" if spd else "An"))
+    x, b = dev_tt(ctx, tt_of(z, "x0")), dev_tt(ctx, tt_of(z, "b"))
+    r = {"hosvd": xg.HOSVDRetraction, "als": xg.ALSRetraction}[kind]
+    cls = xg.GeometricCGVariant if alg == "gcg" else xg.SteepestDescentVariant
+    v = cls(0, 1e-8, spd, retraction=r)
+    perf = xg.PerformanceData()
+    tag = f"{alg}_{kind}_{'spd' if spd else 'ls'}"
+    res = v(A, x, b, 8, perf)
+    assert len(perf.residuals) == len(z[tag + "_perf_residual"])
+    assert rel_err(perf.residuals, z[tag + "_perf_residual"]) < 1e-9
+    assert abs(res / z[tag + "_residual"][0] - 1) < 1e-9
+    assert [1] + x.ranks() + [1] == list(z[tag + "_ranks"])
+    assert rel_err(x.entries(z[tag + "_x_probe_pos"]), z[tag + "_x_probe_val"]) < 1e-8
+
+
 def test_adf_rank_one_matches_reference(ctx, golden):
     """ADF on rank-one measurements (RankOneMeasurementSet): the reference's trajectory and
     final iterate; the device measurement of the target against the reference's values."""

@@ -297,3 +297,20 @@ def test_qc_rank_rule_with_clear_gap(golden, tag):
         o.move_core(y, p, keep_rank=False)
         assert [1] + y.ranks + [1] == list(z[f"{tag}_qc_to{p}_ranks"])
         assert rel_err(o.tt_entries(y, z[f"{tag}_qc_to{p}_probe_pos"]), z[f"{tag}_qc_to{p}_probe_val"]) < REL_TOL
+
+
+@pytest.mark.parametrize("alg,kind,spd", [(a, k, s) for a in ("gcg", "sd") for k in ("hosvd", "als") for s in (True, False)])
+def test_hosvd_and_als_retractions(golden, alg, kind, spd):
+    """GeometricCG (type I retractions) and SteepestDescent (type II) with the HOSVD and ALS
+    retractions (retractions.cpp:43-69) against the reference's runs: every step's residual
+    and the final iterate."""
+    z = golden("retractions")
+    A = op_of(z, "A" if spd else "An")
+    x, b = tt_of(z, "x0"), tt_of(z, "b")
+    tag = f"{alg}_{kind}_{'spd' if spd else 'ls'}"
+    fn = o.geometric_cg if alg == "gcg" else o.steepest_descent
+    res, trace = fn(A, x, b, 8, 1e-8, spd, retraction=kind)
+    assert rel_err(trace, z[tag + "_perf_residual"]) < 1e-9
+    assert abs(res / z[tag + "_residual"][0] - 1) < 1e-9
+    assert [1] + x.ranks + [1] == list(z[tag + "_ranks"])
+    assert rel_err(o.tt_entries(x, z[tag + "_x_probe_pos"]), z[tag + "_x_probe_val"]) < 1e-8

@@ -17,7 +17,7 @@ import numpy as np
 from . import _lib as L
 
 __all__ = ["Context", "TTTensor", "TTOperator", "frob_norm", "dot", "residual", "ALSVariant", "ALS", "ALS_SPD", "DMRG", "DMRG_SPD", "ASD",
-           "ASD_SPD", "ADFVariant", "ADF", "SinglePointMeasurementSet", "RankOneMeasurementSet", "GeometricCGVariant", "GeometricCG", "SteepestDescentVariant", "SteepestDescent", "PerformanceData", "seed", "EPSILON",
+           "ASD_SPD", "ADFVariant", "ADF", "SinglePointMeasurementSet", "RankOneMeasurementSet", "GeometricCGVariant", "GeometricCG", "SteepestDescentVariant", "SteepestDescent", "SubmanifoldRetraction", "HOSVDRetraction", "ALSRetraction", "PerformanceData", "seed", "EPSILON",
            "XttError", "FP64", "MIXED", "als_batch", "apply", "save_to_file", "load_from_file", "file_encode", "file_decode"]
 
 EPSILON = 8 * np.finfo(np.float64).eps  # include/xerus/basic.h:50
@@ -585,21 +585,31 @@ class SinglePointMeasurementSet:
         return float(np.sqrt(np.sum(self.measuredValues ** 2)))
 
 
+# The retractions of retractions.cpp (xtt_retraction): submanifold (componentwise
+# addition, SubmanifoldRetractionI / II), HOSVD (HOSVDRetractionI / II: round the sum
+# back to the old ranks) and ALS (ALSRetractionI / II: two operator-free ALS half-sweeps).
+SubmanifoldRetraction, HOSVDRetraction, ALSRetraction = 0, 1, 2
+
+
 class GeometricCGVariant:
     """xerus::GeometricCGVariant (include/xerus/algorithms/cg.h:41-134) with the submanifold
     retraction and projective vector transport (GeometricCG): Riemannian CG on the TT
     manifold of x's ranks. Called as v(A, x, b[, numSteps | convergenceEpsilon][, perfData])
     or without an operator v(x, b, ...); returns ||b - A x||."""
 
-    _entry = "xtt_geometric_cg"
+    _entry = "xtt_geometric_cg_retraction"
 
-    def __init__(self, numSteps=0, convergenceEpsilon=1e-8, assumeSymmetricPositiveDefiniteOperator=False):
+    def __init__(self, numSteps=0, convergenceEpsilon=1e-8, assumeSymmetricPositiveDefiniteOperator=False,
+                 retraction=None):
         self.numSteps = numSteps
         self.convergenceEpsilon = convergenceEpsilon
         self.assumeSymmetricPositiveDefiniteOperator = assumeSymmetricPositiveDefiniteOperator
+        # SubmanifoldRetraction (default), HOSVDRetraction or ALSRetraction (retractions.h:59-88)
+        self.retraction = SubmanifoldRetraction if retraction is None else retraction
 
     def copy(self):
-        return type(self)(self.numSteps, self.convergenceEpsilon, self.assumeSymmetricPositiveDefiniteOperator)
+        return type(self)(self.numSteps, self.convergenceEpsilon, self.assumeSymmetricPositiveDefiniteOperator,
+                          self.retraction)
 
     def __call__(self, *args):
         if len(args) >= 2 and isinstance(args[0], TTTensor):
@@ -621,7 +631,8 @@ class GeometricCGVariant:
         res, cnt = ctypes.c_double(), ctypes.c_int64()
         L.check(getattr(x.lib, self._entry)(A.handle if A is not None else None, x.handle, b.handle, int(steps),
                                             float(eps), int(bool(self.assumeSymmetricPositiveDefiniteOperator)),
-                                            ctypes.byref(res), trace.ctypes.data_as(L.c_double_p), cap,
+                                            int(self.retraction), ctypes.byref(res),
+                                            trace.ctypes.data_as(L.c_double_p), cap,
                                             ctypes.byref(cnt)))
         if perfData is not None:
             perfData.residuals = list(trace[:min(cnt.value, cap)])
@@ -635,7 +646,7 @@ class SteepestDescentVariant(GeometricCGVariant):
     """xerus::SteepestDescentVariant (include/xerus/algorithms/steepestDescent.h) with the
     submanifold retraction (SteepestDescent); same calls as GeometricCGVariant."""
 
-    _entry = "xtt_steepest_descent"
+    _entry = "xtt_steepest_descent_retraction"
 
 
 SteepestDescent = SteepestDescentVariant(0, 1e-8, False)

@@ -795,15 +795,21 @@ int xtt_adf_max_ranks(xtt_tensor* x, const int64_t* positions, const double* val
 	});
 }
 
-int xtt_geometric_cg(const xtt_tensor* A, xtt_tensor* x, const xtt_tensor* b, int64_t num_steps,
-                     double convergence_epsilon, int assume_spd, double* residual, double* residual_trace,
-                     int64_t trace_capacity, int64_t* trace_count) {
+static int riemann_call(bool cg, const xtt_tensor* A, xtt_tensor* x, const xtt_tensor* b, int64_t num_steps,
+                        double convergence_epsilon, int assume_spd, int retraction, double* residual,
+                        double* residual_trace, int64_t trace_capacity, int64_t* trace_count) {
 	return guard([&] {
 		xtt::DeviceScope dev_scope(x ? x->t->ctx->device : -1);
 		ARG(x && b, "NULL argument");
 		ARG(num_steps >= 0, "num_steps must be >= 0");
+		ARG(retraction == XTT_RETRACTION_SUBMANIFOLD || retraction == XTT_RETRACTION_HOSVD ||
+		        retraction == XTT_RETRACTION_ALS,
+		    "unknown retraction");
 		const xtt::RiemannReport r =
-		    xtt::geometric_cg(A ? A->t : nullptr, *x->t, *b->t, num_steps, convergence_epsilon, assume_spd != 0);
+		    cg ? xtt::geometric_cg(A ? A->t : nullptr, *x->t, *b->t, num_steps, convergence_epsilon, assume_spd != 0,
+		                           retraction)
+		       : xtt::steepest_descent(A ? A->t : nullptr, *x->t, *b->t, num_steps, convergence_epsilon,
+		                               assume_spd != 0, retraction);
 		if (residual) *residual = r.residual;
 		if (residual_trace)
 			for (size_t i = 0; i < r.trace.size() && int64_t(i) < trace_capacity; ++i) residual_trace[i] = r.trace[i];
@@ -811,20 +817,32 @@ int xtt_geometric_cg(const xtt_tensor* A, xtt_tensor* x, const xtt_tensor* b, in
 	});
 }
 
+int xtt_geometric_cg(const xtt_tensor* A, xtt_tensor* x, const xtt_tensor* b, int64_t num_steps,
+                     double convergence_epsilon, int assume_spd, double* residual, double* residual_trace,
+                     int64_t trace_capacity, int64_t* trace_count) {
+	return riemann_call(true, A, x, b, num_steps, convergence_epsilon, assume_spd, XTT_RETRACTION_SUBMANIFOLD, residual,
+	                    residual_trace, trace_capacity, trace_count);
+}
+
 int xtt_steepest_descent(const xtt_tensor* A, xtt_tensor* x, const xtt_tensor* b, int64_t num_steps,
                          double convergence_epsilon, int assume_spd, double* residual, double* residual_trace,
                          int64_t trace_capacity, int64_t* trace_count) {
-	return guard([&] {
-		xtt::DeviceScope dev_scope(x ? x->t->ctx->device : -1);
-		ARG(x && b, "NULL argument");
-		ARG(num_steps >= 0, "num_steps must be >= 0");
-		const xtt::RiemannReport r =
-		    xtt::steepest_descent(A ? A->t : nullptr, *x->t, *b->t, num_steps, convergence_epsilon, assume_spd != 0);
-		if (residual) *residual = r.residual;
-		if (residual_trace)
-			for (size_t i = 0; i < r.trace.size() && int64_t(i) < trace_capacity; ++i) residual_trace[i] = r.trace[i];
-		if (trace_count) *trace_count = int64_t(r.trace.size());
-	});
+	return riemann_call(false, A, x, b, num_steps, convergence_epsilon, assume_spd, XTT_RETRACTION_SUBMANIFOLD, residual,
+	                    residual_trace, trace_capacity, trace_count);
+}
+
+int xtt_geometric_cg_retraction(const xtt_tensor* A, xtt_tensor* x, const xtt_tensor* b, int64_t num_steps,
+                                double convergence_epsilon, int assume_spd, int retraction, double* residual,
+                                double* residual_trace, int64_t trace_capacity, int64_t* trace_count) {
+	return riemann_call(true, A, x, b, num_steps, convergence_epsilon, assume_spd, retraction, residual, residual_trace,
+	                    trace_capacity, trace_count);
+}
+
+int xtt_steepest_descent_retraction(const xtt_tensor* A, xtt_tensor* x, const xtt_tensor* b, int64_t num_steps,
+                                    double convergence_epsilon, int assume_spd, int retraction, double* residual,
+                                    double* residual_trace, int64_t trace_capacity, int64_t* trace_count) {
+	return riemann_call(false, A, x, b, num_steps, convergence_epsilon, assume_spd, retraction, residual,
+	                    residual_trace, trace_capacity, trace_count);
 }
 
 int xtt_random_rank_one(int64_t num, int64_t order, const int64_t* dims, double* out) {

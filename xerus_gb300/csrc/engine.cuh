@@ -251,10 +251,11 @@ struct RiemannReport {
 	int64_t steps = 0;
 	std::vector<double> trace;   // residual before the first step and after every step
 };
-RiemannReport geometric_cg(const Tensor* A, Tensor& x, const Tensor& b, int64_t num_steps, double eps, bool assume_spd);
+RiemannReport geometric_cg(const Tensor* A, Tensor& x, const Tensor& b, int64_t num_steps, double eps, bool assume_spd,
+                           int retraction = XTT_RETRACTION_SUBMANIFOLD);
 // SteepestDescentVariant with SubmanifoldRetractionII (absolute stopping tests, as the reference)
 RiemannReport steepest_descent(const Tensor* A, Tensor& x, const Tensor& b, int64_t num_steps, double eps,
-                               bool assume_spd);
+                               bool assume_spd, int retraction = XTT_RETRACTION_SUBMANIFOLD);
 // ADF on rank-one measurements (RankOneMeasurementSet): vectors holds, per sample, the
 // concatenated vectors u_1 .. u_d (N x sum n_k, row-major). FP64.
 AdfResult adf_rank_one(Tensor& x, const double* vectors, const double* values, long long N, int64_t max_iter,

@@ -295,9 +295,43 @@ void retract(Context& c, Tensor& x, const Tangent& t, double f) {
 	move_core(x, 0, true);
 }
 
+// The other retractions of retractions.cpp, for both kinds of step: from the
+// point y = x + step (a TT of larger rank: the tangent vector added to its base for
+// type I, x + f y for type II) back to x's ranks.
+//   HOSVD (HOSVDRetractionI / II, retractions.cpp:43-55): y.round(oldRanks).
+//   ALS (ALSRetractionI / II, retractions.cpp:57-69): ALSVariant(1, 2, lapack_solver,
+//   false) without an operator, x (the current point, its ranks kept) fitted to y.
+void retract_to_ranks(Context& c, Tensor& x, std::unique_ptr<Tensor> y, int kind) {
+	(void)c;
+	const std::vector<int64_t> old(x.ranks.begin() + 1, x.ranks.end() - 1);
+	if (kind == XTT_RETRACTION_HOSVD) {
+		round_tt(*y, old, kXerusEpsilon, nullptr);
+		x.copy_from(*y);
+		return;
+	}
+	AlsOptions o;
+	o.sites = 1;
+	o.num_half_sweeps = 2;
+	o.convergence_epsilon = 1e-6;
+	o.preserve_core_position = true;
+	o.assume_spd = false;
+	als(nullptr, x, *y, o);
+}
+
+// Type I retraction of x (at the tangent's base) along f t.
+void retract_i(Context& c, Tensor& x, const Base& B, const Tangent& t, double f, int kind) {
+	if (kind == XTT_RETRACTION_SUBMANIFOLD) {
+		retract(c, x, t, f);
+		return;
+	}
+	const Tangent ft = tangent_combine(c, B, t, f, nullptr, 0.0);
+	retract_to_ranks(c, x, tangent_tt(c, B, ft, true), kind);
+}
+
 }  // namespace
 
-RiemannReport geometric_cg(const Tensor* A, Tensor& x, const Tensor& b, int64_t num_steps, double eps, bool assume_spd) {
+RiemannReport geometric_cg(const Tensor* A, Tensor& x, const Tensor& b, int64_t num_steps, double eps, bool assume_spd,
+                           int retraction) {
 	// GeometricCGVariant::solve (src/xerus/algorithms/cg.cpp:34-120)
 	Context& c = *x.ctx;
 	XTT_REQUIRE(!x.op && !b.op && x.dims == b.dims && (!A || (A->op && A->dims == x.dims)),
@@ -375,14 +409,14 @@ RiemannReport geometric_cg(const Tensor* A, Tensor& x, const Tensor& b, int64_t 
 			const double dir_norm = std::sqrt(tangent_dot(c, base, direction, direction));
 			double ca = alpha / change;
 			std::unique_ptr<Tensor> old = clone(x);
-			retract(c, x, direction, ca / dir_norm);
+			retract_i(c, x, base, direction, ca / dir_norm, retraction);
 			double best_res = calc_residual();
 			double best_alpha = ca;
 			std::unique_ptr<Tensor> best = clone(x);
 			while (true) {
 				ca *= change;
 				x.copy_from(*old);
-				retract(c, x, direction, ca / dir_norm);
+				retract_i(c, x, base, direction, ca / dir_norm, retraction);
 				const double r = calc_residual();
 				if (r < best_res) {
 					best_res = r;
@@ -397,7 +431,7 @@ RiemannReport geometric_cg(const Tensor* A, Tensor& x, const Tensor& b, int64_t 
 			while (alpha > 1e-16 && best_res > curr - 1e-4 * alpha / dir_norm * derivative) {
 				alpha *= change;
 				x.copy_from(*old);
-				retract(c, x, direction, alpha / dir_norm);
+				retract_i(c, x, base, direction, alpha / dir_norm, retraction);
 				best_res = calc_residual();
 			}
 			curr = best_res;
@@ -420,9 +454,9 @@ RiemannReport geometric_cg(const Tensor* A, Tensor& x, const Tensor& b, int64_t 
 }
 
 RiemannReport steepest_descent(const Tensor* A, Tensor& x, const Tensor& b, int64_t num_steps, double eps,
-                               bool assume_spd) {
+                               bool assume_spd, int retraction) {
 	// SteepestDescentVariant::solve (src/xerus/algorithms/steepestDescent.cpp:83-175) with
-	// SubmanifoldRetractionII (retractions.cpp:222-225)
+	// SubmanifoldRetractionII (retractions.cpp:222-225), HOSVDRetractionII or ALSRetractionII
 	Context& c = *x.ctx;
 	XTT_REQUIRE(!x.op && !b.op && x.dims == b.dims && (!A || (A->op && A->dims == x.dims)),
 	            "dimensions of A, x and b must match");
@@ -469,18 +503,32 @@ RiemannReport steepest_descent(const Tensor* A, Tensor& x, const Tensor& b, int6
 		} else {
 			y = clone(*residual);
 		}
-		// the retraction projects the step at the current x; halving keeps the same base
+		// the submanifold retraction projects the step at the current x (halving keeps the
+		// same base); the others round x + alpha y back to x's ranks
 		std::unique_ptr<Tensor> old = clone(x);
-		const Base base = make_base(x);
-		const Tangent w = project(c, base, *y);
+		Base base;
+		Tangent w;
+		if (retraction == XTT_RETRACTION_SUBMANIFOLD) {
+			base = make_base(x);
+			w = project(c, base, *y);
+		}
+		auto step = [&](double f) {
+			if (retraction == XTT_RETRACTION_SUBMANIFOLD) {
+				retract(c, x, w, f);
+			} else {
+				std::unique_ptr<Tensor> z = clone(x);
+				tt_add(*z, *y, f);
+				retract_to_ranks(c, x, std::move(z), retraction);
+			}
+		};
 		alpha *= 2;
-		retract(c, x, w, alpha);
+		step(alpha);
 		last = curr;
 		curr = update_residual();
 		while (alpha > 1e-30 && last < curr) {
 			alpha /= 2;
 			x.copy_from(*old);
-			retract(c, x, w, alpha);
+			step(alpha);
 			curr = update_residual();
 		}
 		rep.trace.push_back(curr);
