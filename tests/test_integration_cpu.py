@@ -2,8 +2,8 @@
 xerus_forwarding.cpp) compiles against the reference's own headers and links
 against the reference library and libxtt.so: every xerus call it makes and every
 C ABI entry point it forwards to exist with the signatures used. A link check
-on the CPU; it needs the xerus sources ($XERUS_REF) and the reference library
-built from them, so it is skipped where they are absent."""
+on the CPU; it needs the xerus sources (__graft_entry__.reference_dir()) and the
+reference library built from them, so it is skipped where they are absent."""
 import os
 import shutil
 import subprocess
@@ -16,9 +16,10 @@ ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
 
 
 def test_forwarding_layer_compiles_and_links(tmp_path):
-    ref = os.environ.get("XERUS_REF")
-    if not ref or not os.path.isdir(os.path.join(ref, "include", "xerus")):
-        pytest.skip("XERUS_REF (the xerus sources) not available")
+    import __graft_entry__
+    ref = __graft_entry__.reference_dir()
+    if not ref:
+        pytest.skip("the xerus sources are not available on this host")
     if not shutil.which("g++"):
         pytest.skip("g++ not available")
     refdir = os.path.join(ROOT, "oracle", "_ref")
