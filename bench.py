@@ -132,6 +132,95 @@ def read_profile_traffic(name):
     return None
 
 
+def read_profile_field(name, field):
+    """A `field: value` line of a committed ncu summary (None if absent)."""
+    path = os.path.join(ROOT, "profiles", f"{name}.md")
+    if not os.path.exists(path):
+        return None
+    for line in open(path):
+        if line.strip().startswith(field + ":"):
+            try:
+                return float(line.split(":", 1)[1].strip().split()[0])
+            except ValueError:
+                return None
+    return None
+
+
+def reference_cpu_times():
+    """The compiled xerus reference timed on the build host by oracle/ref/time_reference.py
+    (the GPU host has no copy of the reference sources to build it): None if absent."""
+    path = os.path.join(ROOT, "oracle", "ref_cpu_times.json")
+    return json.load(open(path)) if os.path.exists(path) else None
+
+
+def ref_leg(key, threads_key, fields):
+    """One configuration's compiled-reference timings, labelled with the host they come from."""
+    t = reference_cpu_times()
+    if not t or key not in t or threads_key not in t[key]:
+        return None
+    out = {f: t[key][threads_key][f] for f in fields if f in t[key][threads_key]}
+    out["kind"] = "reference"
+    out["threads"] = int(threads_key.split("_")[1])
+    out["host"] = f"{t['host']['cpu']} ({t['host']['cores']} cores, {t['host']['machine']}, {t['host']['openblas']}): " \
+                  "the build host, not the GPU host"
+    return out
+
+
+def bench_qr_shape(xg, ctx, reps=20):
+    """The headline's move_core factorisation on its own: Householder QR with Q of a
+    128 x 32 core (rank-32 cores of mode size 4), timed by the context's CUDA events over
+    `reps` launches. Algorithmic bytes: read A, write Q and R (8 (2 m n + n^2))."""
+    m, n = 128, 32
+    xg.seed(1)
+    x = xg.TTTensor.random([m, n], n, ctx=ctx)
+    flat, r = x.get_flat(), x.all_ranks()
+    for _ in range(3):
+        x.set_flat(flat, ranks=r)
+        x.assume_core_position(0)
+        x.move_core(1, True)
+    ctx.profile(True)
+    for _ in range(reps):
+        x.set_flat(flat, ranks=r)
+        x.assume_core_position(0)
+        x.move_core(1, True)
+    nl, ms = ctx.profile_get("qr")
+    ctx.profile(False)
+    per = ms / max(nl, 1)
+    alg = 8.0 * (2 * m * n + n * n)
+    return {"shape": f"{m} x {n} with Q", "launches": nl, "avg_launch_ms": per, "us_per_factorisation": 1e3 * per,
+            "algorithmic_bytes_per_launch": alg, "algorithmic_flops_per_launch": 4.0 * m * n * n - 4.0 * n ** 3 / 3}
+
+
+def bench_cfg1_rank8(xg, ctx, torch, stream, steps):
+    """Configuration 1 as stated: ALS_SPD on the d=8, n=4 Laplacian, x rank 8, 20
+    half-sweeps with convergenceEpsilon 0 (stops at residual ~1.2e-3: rank 8 cannot reach
+    1e-8), FP64 and mixed, with the compiled reference's time beside it."""
+    xg.seed(SEED)
+    A = xg.TTOperator.from_cores(xg.laplacian_cores(8, 4), ctx=ctx)
+    b = xg.TTTensor.random([4] * 8, 4, ctx=ctx)
+    x0 = xg.TTTensor.random([4] * 8, 8, ctx=ctx)
+    x0 /= x0.frob_norm()
+    out = {"workload": "ALS_SPD d=8 n=4 Laplacian, rhs rank 4, x rank 8, 20 half-sweeps, convergenceEpsilon 0"}
+    for name, prec in (("fp64", xg.FP64), ("mixed", xg.MIXED)):
+        v = xg.ALS_SPD.copy()
+        v.convergenceEpsilon = 0.0
+        v.precision = prec
+        times = []
+        for i in range(steps + 2):
+            x = x0.copy()
+            torch.cuda.synchronize()
+            e0, e1 = _events(torch, stream)
+            e0.record(stream)
+            v(A, x, b, 20)
+            e1.record(stream)
+            torch.cuda.synchronize()
+            if i >= 2:
+                times.append(e0.elapsed_time(e1))
+        out[name] = {"ms": statistics.mean(times), "residual": xg.residual(A, x, b), "energy": v.last_report.energy}
+    out["cpu_reference_build_host"] = ref_leg("cfg1", "threads_8", ["r8_hs20_seconds", "r8_hs20_residual"])
+    return out
+
+
 def _events(torch, stream):
     return torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
 
@@ -484,31 +573,48 @@ def run_gpu(args):
                              "GB_per_s": by / (ms / 1e3) / 1e9 if ms > 0 and by else None,
                              "GFLOP_per_s": fl / (ms / 1e3) / 1e9 if ms > 0 and fl else None}
     line["kernel_classes"] = classes
-    if top in ("qr", "gemm") and classes.get(top, {}).get("GB_per_s"):
-        c_ = classes[top]
-        ach = c_["GB_per_s"]
-        line["roofline"] = {"kernel": {"qr": "k_qr_cl1 / k_qr_small (FP64 Householder)", "gemm": "k_gemm_sk (FP64)"}[top],
+    if top == "qr":
+        # the dominant class's most frequent launch (the move_core factorisation of a 128 x 32
+        # core with Q) timed on its own, so achieved bytes, duration and the ncu traffic all
+        # describe the same launch
+        q = bench_qr_shape(xg, ctx)
+        ach = q["algorithmic_bytes_per_launch"] / (q["avg_launch_ms"] / 1e3) / 1e9
+        traffic = read_profile_traffic("qr_cl1_als_d8_r32")
+        line["roofline"] = {"kernel": "k_qr_cl1 (FP64 Householder QR with Q, 128 x 32, 8-CTA cluster)",
                             "bound": "hbm", "achieved": ach, "peak": peaks.get("hbm_gbs", 6800.0), "unit": "GB/s",
-                            "frac": ach / peaks.get("hbm_gbs", 6800.0), "traffic": read_profile_traffic("qr_cl1_als_d8_r32"),
+                            "frac": ach / peaks.get("hbm_gbs", 6800.0), "traffic": traffic,
+                            "traffic_over_algorithmic": traffic / q["algorithmic_bytes_per_launch"] if traffic else None,
                             "peak_source": "of measured" if "hbm_gbs" in peaks else "of fallback",
-                            "algorithmic_bytes_per_launch": c_["bytes_per_step"] / c_["launches_per_step"],
-                            "algorithmic_flops_per_launch": c_["flops_per_step"] / c_["launches_per_step"],
-                            "avg_launch_ms": c_["ms_per_step"] / c_["launches_per_step"],
-                            "launches": int(c_["launches_per_step"] * prof_steps),
+                            "algorithmic_bytes_per_launch": q["algorithmic_bytes_per_launch"],
+                            "algorithmic_flops_per_launch": q["algorithmic_flops_per_launch"],
+                            "avg_launch_ms": q["avg_launch_ms"], "launches": q["launches"],
+                            "us_per_factorisation": q["us_per_factorisation"],
+                            "fp64_pipe_pct": read_profile_field("qr_cl1_als_d8_r32", "fp64_pipe_pct_128x32"),
                             "top_kernel_class_by_time": top,
-                            "note": "latency-bound: per-column FP64 dependency chains and cluster barriers, "
-                                    "L2-resident operands",
+                            "class_launches_per_step": classes["qr"]["launches_per_step"] if "qr" in classes else None,
+                            "note": "latency-bound: one cluster barrier and a dependent FP64 reflector chain per "
+                                    "column; operands in L2 / shared memory, so the HBM fraction is not the limit",
                             "kernel_ms_per_step": {k: v[1] / prof_steps for k, v in prof_mix.items()},
                             "cg_mixed": line["roofline"]}
     if not args.no_cpu_baseline:
         line["cpu_baseline"] = cpu_baseline(A, b, x0, samples=1)
+    line["cpu_reference_build_host"] = ref_leg("cfg1", "threads_8", ["r32_hs2_seconds", "r32_hs2_residual"])
     if args.workloads == "all":
         peak = peaks.get("hbm_gbs", 6800.0)
         cpu = not args.no_cpu_baseline
         wl = {}
+        wl["als_cfg1_rank8_hs20"] = bench_cfg1_rank8(xg, ctx, torch, stream, 5)
         wl["round_dot_d32_r64"] = bench_round_dot(xg, ctx, torch, stream, 3, cpu)
+        wl["round_dot_d32_r64"]["cpu_reference_build_host"] = {
+            t: ref_leg("cfg2", t, ["move_core_seconds", "round_seconds", "dot_seconds"]) for t in ("threads_1", "threads_8")}
         wl["adf_d10_n8_r6_200k"] = bench_adf(xg, ctx, torch, stream, args.adf_iterations, peak, cpu)
+        r5 = ref_leg("cfg5", "threads_8", ["adf50_seconds", "adf50_residual"])
+        if r5:
+            r5["ms_per_iteration"] = r5["adf50_seconds"] * 1e3 / 50
+        wl["adf_d10_n8_r6_200k"]["cpu_reference_build_host"] = r5
         wl["batch_als_cfg4"] = bench_batch(xg, ctx, args.batch_count, 2)
+        wl["batch_als_cfg4"]["cpu_reference_build_host"] = ref_leg(
+            "cfg4", "threads_8", ["instances_per_s", "sample_seconds", "sample_instances", "sample"])
         wl["als_tc_d20_n8_r128"] = bench_tc_als(xg, ctx, torch, stream, peaks)
         wl["dmrg_cfg3_d20_n8"] = bench_dmrg(xg, ctx, torch, stream, 16)
         line["workloads"] = wl
