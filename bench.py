@@ -398,7 +398,7 @@ def bench_batch(xg, ctx, count, steps):
             en, its, rep = xg.als_batch(As, xs, bs, variant=v, numHalfSweeps=8)
             ms.append(rep["milliseconds"])
         t = statistics.mean(ms)
-        out[name] = {"ms": t, "instances_per_s": count / (t / 1e3), "launch": {k: rep[k] for k in ("threads", "ctas_per_sm", "ctas")},
+        out[name] = {"ms": t, "instances_per_s": count / (t / 1e3), "launch": {k: rep[k] for k in ("threads", "ctas_per_sm", "ctas", "tile")},
                      "cg_iterations": int(its.sum()), "energy_sum": float(en.sum())}
     out["mixed_speedup_vs_fp64"] = out["fp64"]["ms"] / out["mixed"]["ms"]
     return out

@@ -98,18 +98,22 @@ int xtt_context_set_svd_path(xtt_context* ctx, int path);
  * move_core and the TT dot product, include/xerus/ttNetwork.h:330-420): 0 keeps
  * every contraction FP64 (the reference's arithmetic); 3 runs the contractions
  * (R absorption, bond products, singular-vector absorption, the dot-product
- * zipper) as split-TF32 tensor-core GEMMs with FP32 accumulation, 1 as plain TF32.
- * The QR and SVD factorisations stay FP64 in every form. Other entry points
- * (the solvers) always contract in FP64. */
+ * zipper) as split-TF32 tensor-core GEMMs with FP32 accumulation (two TF32 pieces
+ * per operand, three products), 6 as split-BF16 GEMMs (three BF16 pieces per
+ * operand, the six products of weight >= 2^-16), 1 as plain TF32. The operands
+ * are split once per GEMM into K-major pieces that TMA (cp.async.bulk.tensor)
+ * streams into the MMAs' shared-memory stages. The QR and SVD factorisations stay
+ * FP64 in every form. Other entry points (the solvers) always contract in FP64. */
 int xtt_context_set_contraction_precision(xtt_context* ctx, int terms);
 
-/* C (m x n) = A (m x k) B (k x n) on the tensor cores (tcgen05 TF32 MMAs, FP32
+/* C (m x n) = A (m x k) B (k x n) on the tensor cores (tcgen05 MMAs, FP32
  * accumulation in tensor memory), FP64 row-major device matrices with leading
- * dimensions lda, ldb, ldc; terms = 3 splits each operand into two TF32 parts
- * (FP32-level products), terms = 1 is plain TF32. The building block of the
- * precision forms (no reference counterpart: the reference multiplies in FP64
- * through BLAS, src/xerus/blasLapackWrapper.cpp:96-147); exposed to check it
- * against an FP64 product. Asynchronous on the context's stream. */
+ * dimensions lda, ldb, ldc; terms = 3 splits each operand into two TF32 pieces
+ * (FP32-level products), 6 into three BF16 pieces (FP32-level products on the
+ * 16-bit MMA path), 1 is plain TF32. The building block of the precision forms
+ * (no reference counterpart: the reference multiplies in FP64 through BLAS,
+ * src/xerus/blasLapackWrapper.cpp:96-147); exposed to check it against an FP64
+ * product. Asynchronous on the context's stream. */
 int xtt_gemm_tc(xtt_context* ctx, int64_t m, int64_t n, int64_t k, const double* A, int64_t lda, const double* B,
                 int64_t ldb, double* C, int64_t ldc, int32_t terms);
 
@@ -293,8 +297,9 @@ int xtt_als(const xtt_tensor* A, xtt_tensor* x, const xtt_tensor* b, const xtt_a
  * (descriptor upload, counter reset, kernel, result download) is captured as a
  * CUDA graph and replayed by later calls with the same batch signature. With
  * autotune = 1 the first call of a signature times the launch shapes
- * (threads x CTAs per SM) on the batch itself, restoring x between trials, and
- * caches the fastest. num_half_sweeps (or, when 0, the energy criterion) is
+ * (threads x CTAs per SM), then the register tile shapes of the GEMMs and of the
+ * local operator at the fastest launch shape, on the batch itself, restoring x
+ * between trials, and caches the fastest. num_half_sweeps (or, when 0, the energy criterion) is
  * capped at 1024 half-sweeps per instance. x[i] is updated in place (and left canonical at its
  * start position if preserve_core_position, else where the sweep ended);
  * energies[i] receives what ALSVariant::operator() returns for instance i. */
@@ -303,7 +308,8 @@ typedef struct xtt_batch_report {
 	int32_t threads;       /* launch shape used */
 	int32_t ctas_per_sm;
 	int32_t ctas;
-	int32_t reserved;
+	int32_t tile;          /* register tiles: 0 one output per thread; 1 GEMM 2 x 2 and local
+	                          operator 2 rows per thread; 2 GEMM 4 x 2 and 4 rows */
 } xtt_batch_report;
 int xtt_als_batch(xtt_context* ctx, int64_t count, const xtt_tensor* const* A, xtt_tensor* const* x,
                   const xtt_tensor* const* b, const xtt_als_options* opt, int autotune, double* energies,

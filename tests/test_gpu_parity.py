@@ -219,12 +219,13 @@ def test_dmrg_rank_growth(ctx, svd_path):
     assert rel_err(x.entries(pos), o.tt_entries(ref, pos)) < 1e-8
 
 
-@pytest.mark.parametrize("form,tol", [("tf32x3", 1e-4), ("tf32", 1e-2)])
+@pytest.mark.parametrize("form,tol", [("tf32x3", 1e-4), ("bf16x3", 1e-4), ("tf32", 1e-2)])
 def test_round_dot_precision_forms(ctx, golden, form, tol):
     """Precision forms of the d=32, n=4, rank-64 rounding: the contractions of move_core, round and dot
     on the tensor cores (QR and SVD FP64). Same ranks; singular values, norm and dot
     product within the form's error of the FP64 results: per contraction split TF32
-    errs ~5e-7 (FP32 accumulation over K = 256), TF32 ~5e-4, and the 31 absorptions
+    errs ~5e-7 (FP32 accumulation over K = 256), as does split BF16 (three pieces, six
+    products), TF32 ~5e-4, and the 31 absorptions
     of a d=32 sweep compound them (measured 1.4e-5 and ~3e-3)."""
     r = golden("round")
     xg.seed(0xBAADF00D)

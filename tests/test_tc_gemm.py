@@ -1,7 +1,8 @@
-"""The tensor-core GEMM (tcgen05 TF32 MMAs, FP32 accumulation in tensor memory)
-against an FP64 product of the same operands, through the C ABI. Tolerances, as
-a fraction of sum_k |A_ik| |B_kj| (the scale of the accumulated products): split
-TF32 (three MMAs per step) 2e-6; plain TF32 2e-3 (11-bit mantissa products)."""
+"""The tensor-core GEMM (TMA-fed operand pieces, tcgen05 TF32 or BF16 MMAs, FP32
+accumulation in tensor memory) against an FP64 product of the same operands,
+through the C ABI. Tolerances, as a fraction of sum_k |A_ik| |B_kj| (the scale of
+the accumulated products): split TF32 (three products per step) and split BF16
+(three pieces, six products) 2e-6; plain TF32 2e-3 (11-bit mantissa products)."""
 import ctypes
 
 import numpy as np
@@ -37,7 +38,7 @@ def run(ctx, A, B, terms, C=None):
 
 @pytest.mark.parametrize("m,n,k", [(128, 64, 32), (128, 64, 256), (300, 200, 100), (7, 5, 3), (1024, 96, 24),
                                    (64, 512, 1000), (256, 130, 8)])
-@pytest.mark.parametrize("terms,tol", [(3, 2e-6), (1, 2e-3)])
+@pytest.mark.parametrize("terms,tol", [(3, 2e-6), (6, 2e-6), (1, 2e-3)])
 def test_gemm_tc_matches_fp64(ctx, m, n, k, terms, tol):
     g = torch.Generator(device="cpu").manual_seed(m * 7919 + n * 31 + k)
     A = torch.randn(m, k, generator=g, dtype=torch.float64).cuda()

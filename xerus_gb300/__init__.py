@@ -79,8 +79,10 @@ class Context:
 
     def set_contraction_precision(self, form):
         """Precision form of round / move_core / dot: 'fp64', 'tf32x3' (split TF32 on the
-        tensor cores) or 'tf32'. QR and SVD stay FP64."""
-        L.check(self.lib.xtt_context_set_contraction_precision(self.handle, {"fp64": 0, "tf32x3": 3, "tf32": 1}[form]))
+        tensor cores), 'bf16x3' (three BF16 pieces, six products) or 'tf32'. QR and SVD
+        stay FP64."""
+        L.check(self.lib.xtt_context_set_contraction_precision(
+            self.handle, {"fp64": 0, "tf32x3": 3, "tf32": 1, "bf16x3": 6}[form]))
 
     def set_svd_path(self, path):
         """'auto' (QR-preconditioned Jacobi where it fits) or 'jacobi' (plain one-sided Jacobi)."""
@@ -528,7 +530,7 @@ class ALSVariant:
 def als_batch(As, xs, bs, variant=None, numHalfSweeps=8, autotune=False):
     """Batched ALS_SPD: solves every (A_i, x_i, b_i) with one-site ALS in one
     persistent launch (x_i updated in place). Returns (energies, local CG
-    iterations, {"milliseconds", "threads", "ctas_per_sm", "ctas"})."""
+    iterations, {"milliseconds", "threads", "ctas_per_sm", "ctas", "tile"})."""
     v = (variant or ALS_SPD).copy()
     n = len(xs)
     if not (len(As) == n == len(bs)) or n == 0:
@@ -545,6 +547,7 @@ def als_batch(As, xs, bs, variant=None, numHalfSweeps=8, autotune=False):
     L.check(ctx.lib.xtt_als_batch(ctx.handle, n, pa, px, pb, ctypes.byref(o), int(bool(autotune)),
                                   en.ctypes.data_as(L.c_double_p), it.ctypes.data_as(L.c_int64_p), ctypes.byref(rep)))
     return en, it, {"milliseconds": rep.milliseconds, "threads": rep.threads, "ctas_per_sm": rep.ctas_per_sm,
+                    "tile": rep.tile,
                     "ctas": rep.ctas}
 
 

@@ -54,7 +54,7 @@ class BatchReport(ctypes.Structure):
         ("threads", ctypes.c_int32),
         ("ctas_per_sm", ctypes.c_int32),
         ("ctas", ctypes.c_int32),
-        ("reserved", ctypes.c_int32),
+        ("tile", ctypes.c_int32),
     ]
 
 

@@ -288,7 +288,7 @@ struct BatchResult {
 	std::vector<int> iterations;
 	std::vector<int> final_pos;
 	double ms = 0;        // device time of the batch launch (CUDA events)
-	int threads = 0, ctas_per_sm = 0, ctas = 0;
+	int threads = 0, ctas_per_sm = 0, ctas = 0, tile = 0;
 };
 BatchResult als_batch(Context& c, const std::vector<const Tensor*>& A, const std::vector<Tensor*>& x,
                       const std::vector<const Tensor*>& b, const AlsOptions& o, bool autotune);

@@ -57,6 +57,7 @@ struct BArgs {
 	double* work = nullptr;
 	BLayout lay;
 	int precision = 0, half_sweeps = 0, max_iter = 0, max_refine = 12, preserve = 1;
+	int tile = 0;  // register tiles: 0 one output per thread, 1 GEMM 2x2 / matvec 2 rows, 2 GEMM 4x2 / matvec 4 rows
 	double conv_eps = 0, tol = 1e-13;
 	double* energy = nullptr;
 	int* iters = nullptr;
@@ -74,9 +75,68 @@ struct BShared {
 
 // ------------------------------------------------------------ block primitives
 
+// C = alpha A B + beta C over the whole CTA, a TM x TN register tile of outputs per
+// thread (each loaded A value used TN times, each B value TM times).
+template <class T, int TM, int TN>
+__device__ void blk_gemm_tiled(const Gemm<T>& g) {
+	if (g.M > 0 && g.N > 0 && g.batch > 0) {
+		const int tm = (g.M + TM - 1) / TM, tn = (g.N + TN - 1) / TN;
+		const long long total = (long long)g.batch * tm * tn;
+		const int Ki = g.Ki ? g.Ki : (g.K > 0 ? g.K : 1);
+		for (long long e = threadIdx.x; e < total; e += blockDim.x) {
+			const int n0 = int(e % tn) * TN;
+			const long long t = e / tn;
+			const int m0 = int(t % tm) * TM;
+			const long long bb = t / tm;
+			const T* Ap[TM];
+			const T* Bp[TN];
+#pragma unroll
+			for (int i = 0; i < TM; ++i) Ap[i] = g.A + bb * g.sAb + g.offA(min(m0 + i, g.M - 1), 0);
+#pragma unroll
+			for (int j = 0; j < TN; ++j) Bp[j] = g.B + bb * g.sBb + g.offB(0, min(n0 + j, g.N - 1));
+			T acc[TM][TN];
+#pragma unroll
+			for (int i = 0; i < TM; ++i)
+#pragma unroll
+				for (int j = 0; j < TN; ++j) acc[i][j] = T(0);
+			for (int ko = 0, k0 = 0; k0 < g.K; ++ko, k0 += Ki) {
+				const int kl = min(Ki, g.K - k0);
+				for (int ki = 0; ki < kl; ++ki) {
+					T av[TM], bv[TN];
+#pragma unroll
+					for (int i = 0; i < TM; ++i) av[i] = Ap[i][ko * g.sAko + ki * g.sAk];
+#pragma unroll
+					for (int j = 0; j < TN; ++j) bv[j] = Bp[j][ko * g.sBko + ki * g.sBk];
+#pragma unroll
+					for (int i = 0; i < TM; ++i)
+#pragma unroll
+						for (int j = 0; j < TN; ++j) acc[i][j] = fma(av[i], bv[j], acc[i][j]);
+				}
+			}
+#pragma unroll
+			for (int i = 0; i < TM; ++i)
+#pragma unroll
+				for (int j = 0; j < TN; ++j)
+					if (m0 + i < g.M && n0 + j < g.N) {
+						T* C = g.C + bb * g.sCb + g.offC(m0 + i, n0 + j);
+						*C = (g.beta == T(0)) ? g.alpha * acc[i][j] : g.alpha * acc[i][j] + g.beta * *C;
+					}
+		}
+	}
+	__syncthreads();
+}
+
 // C = alpha A B + beta C over the whole CTA, one output per thread.
 template <class T>
-__device__ void blk_gemm(const Gemm<T>& g) {
+__device__ void blk_gemm(const Gemm<T>& g, int tile = 0) {
+	if (tile == 1) {
+		blk_gemm_tiled<T, 2, 2>(g);
+		return;
+	}
+	if (tile == 2) {
+		blk_gemm_tiled<T, 4, 2>(g);
+		return;
+	}
 	if (g.M > 0 && g.N > 0 && g.batch > 0) {
 		const long long total = (long long)g.batch * g.M * g.N;
 		const int Ki = g.Ki ? g.Ki : (g.K > 0 ? g.K : 1);
@@ -101,8 +161,8 @@ __device__ void blk_gemm(const Gemm<T>& g) {
 	__syncthreads();
 }
 
-__device__ void blk_chain(const GemmChain& ch) {
-	for (int i = 0; i < ch.ns; ++i) blk_gemm(ch.g[i]);
+__device__ void blk_chain(int tile, const GemmChain& ch) {
+	for (int i = 0; i < ch.ns; ++i) blk_gemm(ch.g[i], tile);
 }
 
 template <class D, class S>
@@ -128,15 +188,15 @@ struct BInstance {
 	__device__ long long csize(int k) const { return (long long)I.rx[k] * I.n[k] * I.rx[k + 1]; }
 
 	__device__ void push_left(int k) {
-		blk_chain(plan_push_left_op(Lop(k), I.x[k], I.A[k], Lop(k + 1), ws + a.lay.s1, ws + a.lay.s2, I.rx[k], I.rA[k],
+		blk_chain(a.tile, plan_push_left_op(Lop(k), I.x[k], I.A[k], Lop(k + 1), ws + a.lay.s1, ws + a.lay.s2, I.rx[k], I.rA[k],
 		                            I.n[k], I.rx[k + 1], I.rA[k + 1]));
-		blk_chain(plan_push_left_rhs(Lb(k), I.b[k], I.x[k], Lb(k + 1), ws + a.lay.s1, I.rb[k], I.rx[k], I.n[k],
+		blk_chain(a.tile, plan_push_left_rhs(Lb(k), I.b[k], I.x[k], Lb(k + 1), ws + a.lay.s1, I.rb[k], I.rx[k], I.n[k],
 		                             I.rb[k + 1], I.rx[k + 1]));
 	}
 	__device__ void push_right(int k) {
-		blk_chain(plan_push_right_op(Rop(k + 1), I.x[k], I.A[k], Rop(k), ws + a.lay.s1, ws + a.lay.s2, I.rx[k],
+		blk_chain(a.tile, plan_push_right_op(Rop(k + 1), I.x[k], I.A[k], Rop(k), ws + a.lay.s1, ws + a.lay.s2, I.rx[k],
 		                             I.rA[k], I.n[k], I.rx[k + 1], I.rA[k + 1]));
-		blk_chain(plan_push_right_rhs(Rb(k + 1), I.b[k], I.x[k], Rb(k), ws + a.lay.s1, I.rb[k], I.rx[k], I.n[k],
+		blk_chain(a.tile, plan_push_right_rhs(Rb(k + 1), I.b[k], I.x[k], Rb(k), ws + a.lay.s1, I.rb[k], I.rx[k], I.n[k],
 		                              I.rb[k + 1], I.rx[k + 1]));
 	}
 	// core k -> Q, R absorbed into core k+1 (move_core to the right, keepRank)
@@ -150,7 +210,7 @@ struct BInstance {
 		g.A = C; g.sAm = nc; g.sAk = 1;
 		g.B = I.x[k + 1]; g.sBk = n2r2; g.sBn = 1;
 		g.C = T; g.sCm = n2r2; g.sCn = 1;
-		blk_gemm(g);
+		blk_gemm(g, a.tile);
 		blk_copy(I.x[k + 1], T, (long long)nc * n2r2);
 		blk_copy(I.x[k], Q, (long long)m * nc);
 	}
@@ -165,7 +225,7 @@ struct BInstance {
 		g.A = I.x[k - 1]; g.sAm = m; g.sAk = 1;
 		g.B = C; g.sBk = m; g.sBn = 1;
 		g.C = T; g.sCm = m; g.sCn = 1;
-		blk_gemm(g);
+		blk_gemm(g, a.tile);
 		blk_copy(I.x[k - 1], T, (long long)rn * m);
 		blk_copy(I.x[k], Q, (long long)m * nc);
 	}
@@ -194,6 +254,13 @@ struct BInstance {
 	__device__ Mv<T> mv(const CcShape& s, const T* pf, const T* L, const T* A, const T* R, T* t1, T* t3) const {
 		return Mv<T>{pf, s.rb, L, s.K0 * s.ra, A, nullptr, R, s.rb, t1, t1, t3};
 	}
+	// the local operator with the batch's register tile (rows per thread of the last stage)
+	template <class T>
+	__device__ void apply(const CcShape& s, const Mv<T>& m, T* out) const {
+		if (a.tile == 1) cc_matvec<T, 2>(s, s.rb, m, out);
+		else if (a.tile == 2) cc_matvec<T, 4>(s, s.rb, m, out);
+		else cc_matvec<T, 1>(s, s.rb, m, out);
+	}
 	__device__ double dot(const double* x, const double* y, long long n) {
 		double l = 0;
 		for (long long e = threadIdx.x; e < n; e += blockDim.x) l = fma(x[e], y[e], l);
@@ -205,12 +272,12 @@ struct BInstance {
 		const long long n = (long long)s.ra * s.n1 * s.rb;
 		double* v = ws + a.lay.v;
 		blk_copy(v, I.x[k], n);
-		cc_matvec(s, s.rb, mv<double>(s, v, Lop(k), I.A[k], Rop(k + 1), ws + a.lay.t1, ws + a.lay.t3), ws + a.lay.q);
+		apply(s, mv<double>(s, v, Lop(k), I.A[k], Rop(k + 1), ws + a.lay.t1, ws + a.lay.t3), ws + a.lay.q);
 		const double vq = dot(v, ws + a.lay.q, n), vb = dot(v, ws + a.lay.bloc, n);
 		return fabs(0.5 * vq - vb);
 	}
 	__device__ void rhs(int k) {
-		blk_chain(plan_local_rhs1(Lb(k), I.b[k], Rb(k + 1), ws + a.lay.bloc, ws + a.lay.s1, I.rx[k], I.rx[k + 1],
+		blk_chain(a.tile, plan_local_rhs1(Lb(k), I.b[k], Rb(k + 1), ws + a.lay.bloc, ws + a.lay.s1, I.rx[k], I.rx[k + 1],
 		                          I.rb[k], I.rb[k + 1], I.n[k]));
 	}
 	// FP64 CG on M v = b_loc from the current v.
@@ -220,7 +287,7 @@ struct BInstance {
 		double *x = ws + a.lay.v, *b = ws + a.lay.bloc, *q = ws + a.lay.q, *r = ws + a.lay.r, *p = ws + a.lay.p;
 		const Mv<double> mx = mv<double>(s, x, Lop(k), I.A[k], Rop(k + 1), ws + a.lay.t1, ws + a.lay.t3);
 		const Mv<double> mp = mv<double>(s, p, Lop(k), I.A[k], Rop(k + 1), ws + a.lay.t1, ws + a.lay.t3);
-		cc_matvec(s, s.rb, mx, q);
+		apply(s, mx, q);
 		double rl = 0, bl = 0;
 		for (long long e = threadIdx.x; e < n; e += blockDim.x) {
 			const double v = b[e] - q[e];
@@ -236,7 +303,7 @@ struct BInstance {
 		int it = 0;
 		CgFloor floor_check;
 		while (bb > 0 && rr > tol2 && it < maxit) {
-			cc_matvec(s, s.rb, mp, q);
+			apply(s, mp, q);
 			const double pAp = dot(p, q, n);
 			// the test and the division once per CTA (FP64 pipe), broadcast through shared memory
 			__shared__ double s_ab[2];
@@ -290,7 +357,7 @@ struct BInstance {
 		bool reached = bb == 0;
 		double rr_prev = 0, nr_prev = 0;
 		for (int ref = 0; ref <= a.max_refine && bb > 0; ++ref) {
-			cc_matvec(s, s.rb, m64, q);
+			apply(s, m64, q);
 			double l = 0;
 			for (long long e = threadIdx.x; e < n; e += blockDim.x) {
 				const double v = b[e] - q[e];
@@ -326,7 +393,7 @@ struct BInstance {
 			const float tol2 = 1e-12f * bbf;  // FP32 inner tolerance 1e-6
 			int it = 0;
 			while (rr > tol2 && it < maxit) {
-				cc_matvec(s, s.rb, m32, qf);
+				apply(s, m32, qf);
 				float lq = 0;
 				for (long long e = threadIdx.x; e < n; e += blockDim.x) lq = fmaf(pf[e], qf[e], lq);
 				const float pAp = block_sum(lq, sh.redf);
@@ -376,7 +443,7 @@ struct BInstance {
 				g.A = I.x[f]; g.sAm = rk; g.sAk = 1;
 				g.B = I.x[f + 1]; g.sBk = n2 * r2; g.sBn = 1;
 				g.C = ws + a.lay.tg; g.sCm = n2 * r2; g.sCn = 1;
-				blk_gemm(g);
+				blk_gemm(g, a.tile);
 				blk_copy(I.x[f + 1], ws + a.lay.tg, (long long)newp * n2 * r2);
 				identity_core(I.x[f], int(prod), nd, newp, 0);
 				prod = newp;
@@ -389,7 +456,7 @@ struct BInstance {
 				g.A = I.x[l - 2]; g.sAm = rk; g.sAk = 1;
 				g.B = I.x[l - 1]; g.sBk = newp; g.sBn = 1;
 				g.C = ws + a.lay.tg; g.sCm = newp; g.sCn = 1;
-				blk_gemm(g);
+				blk_gemm(g, a.tile);
 				blk_copy(I.x[l - 2], ws + a.lay.tg, (long long)r0 * n0 * newp);
 				identity_core(I.x[l - 1], newp, nd, int(prod), 1);
 				prod = newp;
@@ -610,12 +677,13 @@ static BatchResult run_batch(Context& c, const std::vector<BInst>& inst, const s
 		sig = mix(sig, (unsigned long long)I.d);
 		for (int k = 0; k < I.d; ++k) sig = mix(sig, (unsigned long long)(I.n[k] * 4096 + I.rx[k + 1] * 64 + I.rA[k + 1]));
 	}
-	int threads = 256, per_sm = 1;
+	int threads = 256, per_sm = 1, tile = 0;
 	bool have = false;
 	for (auto& t : c.batch_tuned)
-		if (t.first == sig) {
-			threads = t.second.first;
-			per_sm = t.second.second;
+		if (t.sig == sig) {
+			threads = t.threads;
+			per_sm = t.per_sm;
+			tile = t.tile;
 			have = true;
 		}
 	XTT_CUDA(cudaMemcpyAsync(dm, hm, o_energy, cudaMemcpyHostToDevice, c.stream));
@@ -637,40 +705,48 @@ static BatchResult run_batch(Context& c, const std::vector<BInst>& inst, const s
 		k_batch_x_copy<<<std::min(count, 4 * c.num_sms), 256, 0, c.stream>>>(a.inst, doff, count, bk, 1);
 		XTT_CUDA(cudaGetLastError());
 		double best = 1e300;
+		auto trial = [&](int th, int ps, int tl) {
+			const int G = std::max(1, std::min(count, ps * c.num_sms));
+			a.work = c.scratch<double>(S_BATCH_WORK, size_t(G) * lay.total);
+			a.tile = tl;
+			XTT_CUDA(cudaMemsetAsync(a.next, 0, sizeof(int), c.stream));
+			XTT_CUDA(cudaEventRecord(e0, c.stream));
+			k_als_batch<<<G, th, 0, c.stream>>>(a);
+			XTT_CUDA(cudaGetLastError());
+			XTT_CUDA(cudaEventRecord(e1, c.stream));
+			k_batch_x_copy<<<std::min(count, 4 * c.num_sms), 256, 0, c.stream>>>(a.inst, doff, count, bk, 0);
+			c.count_launch(2);
+			XTT_CUDA(cudaEventSynchronize(e1));
+			float ms = 0;
+			XTT_CUDA(cudaEventElapsedTime(&ms, e0, e1));
+			if (ms < best) {
+				best = ms;
+				threads = th;
+				per_sm = ps;
+				tile = tl;
+			}
+		};
+		// launch shapes (threads x resident CTAs per SM) with one output per thread, then the
+		// register tile shapes of the GEMMs and the local operator at the fastest launch shape
 		for (int th : {128, 256, 512}) {
 			int occ = 0;
 			XTT_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, k_als_batch, th, 0));
-			for (int ps : {1, 2, 4}) {
-				if (ps > occ) continue;
-				const int G = std::max(1, std::min(count, ps * c.num_sms));
-				a.work = c.scratch<double>(S_BATCH_WORK, size_t(G) * lay.total);
-				XTT_CUDA(cudaMemsetAsync(a.next, 0, sizeof(int), c.stream));
-				XTT_CUDA(cudaEventRecord(e0, c.stream));
-				k_als_batch<<<G, th, 0, c.stream>>>(a);
-				XTT_CUDA(cudaGetLastError());
-				XTT_CUDA(cudaEventRecord(e1, c.stream));
-				k_batch_x_copy<<<std::min(count, 4 * c.num_sms), 256, 0, c.stream>>>(a.inst, doff, count, bk, 0);
-				c.count_launch(2);
-				XTT_CUDA(cudaEventSynchronize(e1));
-				float ms = 0;
-				XTT_CUDA(cudaEventElapsedTime(&ms, e0, e1));
-				if (ms < best) {
-					best = ms;
-					threads = th;
-					per_sm = ps;
-				}
-			}
+			for (int ps : {1, 2, 4})
+				if (ps <= occ) trial(th, ps, 0);
 		}
+		const int th_best = threads, ps_best = per_sm;
+		for (int tl : {1, 2}) trial(th_best, ps_best, tl);
 		c.sync();
-		c.batch_tuned.push_back({sig, {threads, per_sm}});
+		c.batch_tuned.push_back({sig, threads, per_sm, tile});
 	}
+	a.tile = tile;
 	const int G = std::max(1, std::min(count, per_sm * c.num_sms));
 	a.work = c.scratch<double>(S_BATCH_WORK, size_t(G) * lay.total);
 	// the whole batched sweep as one CUDA graph: descriptor upload, counter reset, kernel, results
 	unsigned long long key = mix(sig, (unsigned long long)(uintptr_t)a.work);
 	key = mix(key, (unsigned long long)(uintptr_t)dm);
 	key = mix(key, (unsigned long long)(uintptr_t)hm);
-	key = mix(key, (unsigned long long)(threads * 16 + per_sm));
+	key = mix(key, (unsigned long long)(threads * 64 + per_sm * 4 + tile));
 	key = mix(key, (unsigned long long)(a.half_sweeps * 7 + a.max_iter * 13 + a.preserve));
 	unsigned long long eb;
 	std::memcpy(&eb, &a.conv_eps, 8);
@@ -707,6 +783,7 @@ static BatchResult run_batch(Context& c, const std::vector<BInst>& inst, const s
 	r.threads = threads;
 	r.ctas_per_sm = per_sm;
 	r.ctas = G;
+	r.tile = tile;
 	r.energy.assign(reinterpret_cast<double*>(hm + o_energy), reinterpret_cast<double*>(hm + o_energy) + count);
 	r.iterations.assign(reinterpret_cast<int*>(hm + o_iters), reinterpret_cast<int*>(hm + o_iters) + count);
 	r.final_pos.assign(reinterpret_cast<int*>(hm + o_pos), reinterpret_cast<int*>(hm + o_pos) + count);

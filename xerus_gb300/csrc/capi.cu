@@ -178,7 +178,7 @@ int xtt_gemm_tc(xtt_context* ctx, int64_t m, int64_t n, int64_t k, const double*
 		ARG(ctx && A && B && C, "NULL argument");
 		ARG(m > 0 && n > 0 && k > 0 && m < (1 << 30) && n < (1 << 30) && k < (1 << 30), "illegal GEMM size");
 		ARG(lda >= k && ldb >= n && ldc >= n, "leading dimension smaller than the row");
-		ARG(terms == 1 || terms == 3, "terms must be 1 or 3");
+		ARG(terms == 1 || terms == 3 || terms == 6, "terms must be 1, 3 or 6");
 		xtt::Gemm<double> g;
 		g.M = int(m); g.N = int(n); g.K = int(k);
 		g.A = A; g.sAm = lda; g.sAk = 1;
@@ -193,7 +193,8 @@ int xtt_context_set_contraction_precision(xtt_context* ctx, int terms) {
 	return guard([&] {
 		xtt::DeviceScope dev_scope(ctx ? ctx->c->device : -1);
 		ARG(ctx, "ctx is NULL");
-		ARG(terms == 0 || terms == 1 || terms == 3, "contraction precision must be 0 (FP64), 3 (split TF32) or 1 (TF32)");
+		ARG(terms == 0 || terms == 1 || terms == 3 || terms == 6,
+		    "contraction precision must be 0 (FP64), 3 (split TF32), 6 (split BF16) or 1 (TF32)");
 		ctx->c->contraction_terms = terms;
 	});
 }
@@ -665,6 +666,7 @@ int xtt_als_batch(xtt_context* ctx, int64_t count, const xtt_tensor* const* A, x
 			report->milliseconds = r.ms;
 			report->threads = r.threads;
 			report->ctas_per_sm = r.ctas_per_sm;
+			report->tile = r.tile;
 			report->ctas = r.ctas;
 		}
 	});

@@ -47,7 +47,11 @@ struct Context {
 	cudaGraphExec_t batch_exec = nullptr;
 	void* batch_host = nullptr;
 	size_t batch_host_bytes = 0;
-	std::vector<std::pair<unsigned long long, std::pair<int, int>>> batch_tuned;
+	struct BatchTuned {
+		unsigned long long sig;
+		int threads, per_sm, tile;
+	};
+	std::vector<BatchTuned> batch_tuned;  // the batch autotuner's choices per batch signature
 	int tensors = 0;        // live tensors created on this context
 	bool closing = false;   // destroy requested; freed when the last tensor goes
 	struct Slot {
@@ -133,7 +137,7 @@ enum ScratchId : int {
 	S_RES_CORE0, S_RES_CORE1, S_RES_R, S_RED, S_ENT_META, S_ENT_CORES, S_ENT_OUT,
 	S_RES_CORE0B, S_RES_CORE1B, S_RES_RB, S_QR_WORKB, S_BATCH_META, S_BATCH_WORK, S_BATCH_BACKUP,
 	S_SVD_PC_Q, S_SVD_PC_C, S_SVD_PC_UV, S_SVD_PC_QRW, S_GEMM_TC_WORK, S_SVD_PC_CT, S_SVD_PC_UT,
-	S_SVD_MX_W32, S_SVD_MX_W, S_SVD_MX_W2, S_SVD_MX_G, S_SVD_MX_B0,
+	S_SVD_MX_W32, S_SVD_MX_W, S_SVD_MX_W2, S_SVD_MX_G, S_SVD_MX_B0, S_TMA_A, S_TMA_B,
 	S_ALS_FIRST = 48,
 	S_ADF_FIRST = 112,
 	S_MAX = 176
@@ -170,6 +174,10 @@ void check_gemm(const Gemm<T>& g);
 // terms = 3: split TF32 with FP32-level products, terms = 1: plain TF32).
 template <class T>
 void gemm_tc(Context& c, const Gemm<T>& g, int terms);
+// The TMA-fed form of gemm_tc (operands split into K-major pieces, streamed by
+// cp.async.bulk.tensor): false if the driver cannot describe them as tensor maps.
+template <class T>
+bool gemm_tc_tma(Context& c, const Gemm<T>& g, int terms);
 
 // Stream-ordered helpers.
 void gemm(Context& c, const Gemm<double>& g);

@@ -62,7 +62,9 @@ struct Mv {
 	T *t1, *t2, *t3;
 };
 
-template <class T>
+// TA: output rows a per thread in the last stage (register tile TA x 1: each t3 value
+// read once for TA rows); the batched sweep's autotuner picks it per batch.
+template <class T, int TA = 1>
 __host__ __device__ void cc_matvec(const CcShape& s, int bwl, const Mv<T>& m, T* out) {
 	const int tid = CC_TID;
 	const int KL = s.KL(), M1 = s.M1(), c1 = bwl * KL, ld3 = s.ld3(), c3 = s.nI() * bwl;
@@ -145,13 +147,33 @@ __host__ __device__ void cc_matvec(const CcShape& s, int bwl, const Mv<T>& m, T*
 	CC_SYNC();
 	// out[a][(i.., bl)] = sum_(k, a') L[a][(k, a')] t3[(k, a')][(i.., bl)]
 	const int KK = s.K0 * s.ra;
-	for (int e = tid; e < s.ra * c3; e += CC_STRIDE) {
-		const int a = e / c3, nu = e - a * c3;
-		const T* lp = m.L + (size_t)a * m.ldl;
-		const T* tp = m.t3 + nu;
-		T acc = T(0);
-		for (int kk = 0; kk < KK; ++kk) acc = fma(lp[kk], tp[(size_t)kk * ld3], acc);
-		out[e] = acc;
+	if (TA == 1) {
+		for (int e = tid; e < s.ra * c3; e += CC_STRIDE) {
+			const int a = e / c3, nu = e - a * c3;
+			const T* lp = m.L + (size_t)a * m.ldl;
+			const T* tp = m.t3 + nu;
+			T acc = T(0);
+			for (int kk = 0; kk < KK; ++kk) acc = fma(lp[kk], tp[(size_t)kk * ld3], acc);
+			out[e] = acc;
+		}
+	} else {
+		const int ga = (s.ra + TA - 1) / TA;
+		for (int e = tid; e < ga * c3; e += CC_STRIDE) {
+			const int a0 = (e / c3) * TA, nu = e - (e / c3) * c3;
+			const T* lp[TA];
+			T acc[TA];
+			for (int i = 0; i < TA; ++i) {
+				lp[i] = m.L + (size_t)(a0 + i < s.ra ? a0 + i : s.ra - 1) * m.ldl;  // rows past ra repeat the last
+				acc[i] = T(0);
+			}
+			const T* tp = m.t3 + nu;
+			for (int kk = 0; kk < KK; ++kk) {
+				const T tv = tp[(size_t)kk * ld3];
+				for (int i = 0; i < TA; ++i) acc[i] = fma(lp[i][kk], tv, acc[i]);
+			}
+			for (int i = 0; i < TA; ++i)
+				if (a0 + i < s.ra) out[(size_t)(a0 + i) * c3 + nu] = acc[i];
+		}
 	}
 	CC_SYNC();
 }

@@ -128,5 +128,59 @@ __device__ __forceinline__ void tmem_ld16(uint32_t taddr, float* v) {
 	for (int i = 0; i < 16; ++i) v[i] = __uint_as_float(r[i]);
 }
 
+// ------------------------------------------------------------------ TMA-fed operands
+// Shared-memory matrix descriptor for a K-major operand tile written by TMA with the
+// 128-byte swizzle: rows of 128 bytes (32 TF32 or 64 BF16 elements of K), 8-row groups
+// 1024 bytes apart (SBO), the leading offset unused for swizzled K-major tiles (1),
+// version 1 (bits 46-48), swizzle mode 2 = 128B (bits 61-63). The tile must start on a
+// 1024-byte boundary; the k-th 32-byte K step of a row starts `32 k` bytes in.
+__device__ __forceinline__ uint64_t smem_desc_sw128(uint32_t addr) {
+	uint64_t d = 0;
+	d |= uint64_t((addr & 0x3FFFF) >> 4);
+	d |= uint64_t(1) << 16;
+	d |= uint64_t(1024 >> 4) << 32;
+	d |= uint64_t(1) << 46;
+	d |= uint64_t(2) << 61;
+	return d;
+}
+
+// Instruction descriptor of kind::f16 with BF16 operands: D = F32 (bits 4-5 = 1),
+// A = B = BF16 (bits 7-9, 10-12 = 1), both K-major, N >> 3 at bits 17-22, M >> 4 at 24-28.
+__host__ __device__ constexpr uint32_t idesc_bf16(int M, int N) {
+	return (1u << 4) | (1u << 7) | (1u << 10) | (uint32_t(N >> 3) << 17) | (uint32_t(M >> 4) << 24);
+}
+
+// D[tmem] (+)= A[smem] * B[smem]^T, M x N x 16 BF16 (one thread issues).
+__device__ __forceinline__ void mma_bf16(uint32_t d_tmem, uint64_t adesc, uint64_t bdesc, uint32_t idesc,
+                                         bool accumulate) {
+	asm volatile(
+	    "{\n\t.reg .pred p;\n\t"
+	    "setp.ne.b32 p, %4, 0;\n\t"
+	    "tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n\t}" ::"r"(d_tmem),
+	    "l"(adesc), "l"(bdesc), "r"(idesc), "r"(accumulate ? 1u : 0u)
+	    : "memory");
+}
+
+// The barrier's current phase also waits for `bytes` of asynchronous copies (this
+// thread's arrival counts as one).
+__device__ __forceinline__ void mbar_arrive_expect_tx(uint64_t* bar, uint32_t bytes) {
+	asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_u32(bar)), "r"(bytes) : "memory");
+}
+
+// A 3-D tile of a tensor map (coordinates innermost first) into shared memory; the
+// copy's bytes complete on `bar`. The innermost coordinate times the element size must
+// be a multiple of 16 bytes (callers pass multiples of the 128-byte box row).
+__device__ __forceinline__ void tma_load_3d(void* dst, const void* tmap, uint64_t* bar, int c0, int c1, int c2) {
+	asm volatile(
+	    "cp.async.bulk.tensor.3d.shared::cluster.global.tile.mbarrier::complete_tx::bytes [%0], [%1, {%2, %3, %4}], "
+	    "[%5];" ::"r"(smem_u32(dst)),
+	    "l"(reinterpret_cast<uint64_t>(tmap)), "r"(c0), "r"(c1), "r"(c2), "r"(smem_u32(bar))
+	    : "memory");
+}
+
+__device__ __forceinline__ void tma_prefetch_desc(const void* tmap) {
+	asm volatile("prefetch.tensormap [%0];" ::"l"(reinterpret_cast<uint64_t>(tmap)) : "memory");
+}
+
 }  // namespace tc
 }  // namespace xtt

@@ -265,9 +265,16 @@ void gemm_tc(Context& c, const Gemm<T>& g, int terms) {
 	if (g.M <= 0 || g.N <= 0 || g.batch <= 0) return;
 	check_gemm(g);
 	XTT_REQUIRE(!g.D, "internal: the tensor-core GEMM has no C.*D epilogue");
-	XTT_REQUIRE(terms == 1 || terms == 3, "internal: tensor-core GEMM terms must be 1 or 3");
+	XTT_REQUIRE(terms == 1 || terms == 3 || terms == 6, "internal: tensor-core GEMM terms must be 1, 3 or 6");
 	const double mn = double(g.batch) * g.M * g.N, mk = double(g.M) * g.K, kn = double(g.K) * g.N;
 	ProfScope ps(c, "gemm_tc", double(sizeof(T)) * (double(g.batch) * (mk + kn) + mn), 2.0 * mn * g.K * terms);
+	// TMA-fed tiles (the operands split once into K-major pieces); the per-thread staged
+	// kernel where the driver cannot describe them as tensor maps
+	if (gemm_tc_tma(c, g, terms)) {
+		c.count_launch();
+		return;
+	}
+	XTT_REQUIRE(terms != 6, "the BF16 split form needs the TMA path");
 	if (terms == 3) launch_tc<T, 3>(c, g);
 	else launch_tc<T, 1>(c, g);
 	c.count_launch();
