@@ -266,23 +266,31 @@ __global__ void k_adf_slicenorm_generic(AdfLevel L, const double* G, double* nrm
 }
 
 // X[:, j, :] += (||G_j||^2 / nrm_j) G_j   (update_x, adf.cpp:468-478); one block
+// update_x (adf.cpp:468-478): X[:, j, :] += (||G_j||^2 / nrm_j) G_j, one warp per slice j
+// (the slices' reductions and divisions are independent chains: on GB300 a dependent FP64
+// operation costs ~64 cycles and a division ~370, so slices in sequence would add up).
 __global__ void k_adf_update(double* X, const double* G, const double* nrm, int r0, int n, int r1) {
-	__shared__ double sc[32];
-	for (int j = 0; j < n; ++j) {
+	const int lane = threadIdx.x & 31;
+	for (int j = threadIdx.x >> 5; j < n; j += blockDim.x >> 5) {
 		double s = 0.0;
-		for (int e = threadIdx.x; e < r0 * r1; e += blockDim.x) {
+		for (int e = lane; e < r0 * r1; e += 32) {
 			const int a = e / r1, c = e % r1;
 			const double g = G[(a * n + j) * r1 + c];
-			s += g * g;
+			s = fma(g, g, s);
 		}
-		const double pyr = block_sum(s, sc);
-		const double step = pyr / nrm[j];
-		for (int e = threadIdx.x; e < r0 * r1; e += blockDim.x) {
+		const double step = warp_sum(s) / nrm[j];
+		for (int e = lane; e < r0 * r1; e += 32) {
 			const int a = e / r1, c = e % r1;
-			X[(a * n + j) * r1 + c] += step * G[(a * n + j) * r1 + c];
+			X[(a * n + j) * r1 + c] = fma(step, G[(a * n + j) * r1 + c], X[(a * n + j) * r1 + c]);
 		}
-		__syncthreads();
 	}
+}
+
+static void adf_update(Context& c, double* X, const double* G, const double* nrm, int r0, int n, int r1) {
+	const int warps = std::min(32, std::max(1, n));
+	k_adf_update<<<1, 32 * warps, 0, c.stream>>>(X, G, nrm, r0, n, r1);
+	XTT_CUDA(cudaGetLastError());
+	c.count_launch();
 }
 
 // F_k[b][s] = sum_a F_{k-1}[a][s] X[a, i_s, b]
@@ -510,6 +518,30 @@ struct AdfData {
 
 }  // namespace
 
+// update_x at core k followed by move_core(k + 1, keepRank) in ONE launch when the core
+// fits the one-warp factorisation (ranks <= 8, at most 128 rows): the step, the QR of the
+// updated core and the absorption of R into core k + 1. False if it does not fit.
+static bool update_and_move_right(Tensor& x, int k, const double* G, const double* nrm) {
+	if (!(x.canonicalized && x.core_position == k)) return false;
+	TransferArgs t;
+	t.from = x.core[k];
+	t.to = x.core[k + 1];
+	t.r0 = int(x.ranks[k]); t.nf = int(x.dims[k]); t.r1 = int(x.ranks[k + 1]);
+	t.rt = t.r1; t.nt = int(x.dims[k + 1]); t.r2 = int(x.ranks[k + 2]);
+	t.right = 1;
+	t.G = G;
+	t.nrm = nrm;
+	if (!transfer_warp_fits(t)) return false;
+	Context& c = *x.ctx;
+	{
+		ProfScope ps(c, "qr");
+		launch_transfer_warp(t, c.stream);
+	}
+	c.count_launch();
+	x.core_position = k + 1;
+	return true;
+}
+
 AdfResult adf(Tensor& x, const int64_t* positions, const double* values, long long N, int64_t max_iter,
               double target, double min_dec, int precision, const std::vector<int64_t>* max_ranks,
               const std::function<void(Tensor&)>& add_random_rank_one) {
@@ -537,10 +569,41 @@ AdfResult adf(Tensor& x, const int64_t* positions, const double* values, long lo
 		AdfData D(c, x, positions, values, N, precision != XTT_PRECISION_FP64);
 		f32 = D.f32;
 		double dec1 = 0, dec2 = 0, dec3 = 0;
-		for (; max_iter == 0 || it < max_iter; ++it) {
+		// From the second iteration at these ranks on, both halves of an iteration repeat
+		// the same launches with the same arguments (core d-1 -> 0, backward stacks,
+		// residual; then the sweep): each is recorded once as a graph and replayed. Not
+		// while per-class profiling times the launches one by one.
+		ReplayGraph start_graph, sweep_graph;
+		const bool graphs = !c.profiling;
+		auto start = [&] {
 			move_core(x, 0, true);
 			for (int k = d - 1; k > 0; --k) D.backward(k);
 			D.res_grad(0, 0, x.core[0], D.G, 1.0);
+		};
+		auto sweep = [&] {
+			for (int k = 0; k < d; ++k) {
+				if (k > 0) D.res_grad(k, 0, x.core[k], D.G, 1.0);
+				D.slicenorm(k);
+				if (k + 1 < d && update_and_move_right(x, k, D.G, D.nrm)) {
+					D.forward(k);
+					continue;
+				}
+				adf_update(c, x.core[k], D.G, D.nrm, int(x.ranks[k]), int(x.dims[k]), int(x.ranks[k + 1]));
+				if (k + 1 < d) {
+					move_core(x, k + 1, true);
+					D.forward(k);
+				}
+			}
+		};
+		int64_t local = 0;  // iterations at these ranks so far
+		for (; max_iter == 0 || it < max_iter; ++it, ++local) {
+			if (graphs && local >= 1 && d > 1) {
+				start_graph.run(c, start);
+				x.canonicalized = true;
+				x.core_position = 0;
+			} else {
+				start();
+			}
 			last_residual_norm = residual_norm;
 			residual_norm = std::sqrt(D.read_rr()) / norm_y;
 			out.trace.push_back(residual_norm);
@@ -551,17 +614,12 @@ AdfResult adf(Tensor& x, const int64_t* positions, const double* values, long lo
 			dec2 = dec1;
 			dec1 = residual_norm / last_residual_norm;
 			if (residual_norm < target || dec1 * dec2 * dec3 * dec4 > std::pow(min_dec, 4)) break;
-			for (int k = 0; k < d; ++k) {
-				if (k > 0) D.res_grad(k, 0, x.core[k], D.G, 1.0);
-				D.slicenorm(k);
-				k_adf_update<<<1, 128, 0, c.stream>>>(x.core[k], D.G, D.nrm, int(x.ranks[k]), int(x.dims[k]),
-				                                      int(x.ranks[k + 1]));
-				XTT_CUDA(cudaGetLastError());
-				c.count_launch();
-				if (k + 1 < d) {
-					move_core(x, k + 1, true);
-					D.forward(k);
-				}
+			if (graphs && local >= 1 && d > 1) {
+				sweep_graph.run(c, sweep);
+				x.canonicalized = true;
+				x.core_position = d - 1;
+			} else {
+				sweep();
 			}
 		}
 	};

@@ -106,6 +106,47 @@ struct ProfScope {
 	~ProfScope();
 };
 
+// Records the launches `body` issues on the context's stream once as a CUDA graph and
+// replays the graph on every later run: for launch sequences that repeat with the same
+// arguments (an ADF sweep at fixed ranks), where issuing ~100 small launches one by one
+// from the host costs more than the kernels. The body must not synchronise or
+// allocate; host-side state it would change must be set by the caller after a replay.
+struct ReplayGraph {
+	cudaGraphExec_t exec = nullptr;
+	int64_t launches = 0;
+	ReplayGraph() = default;
+	ReplayGraph(const ReplayGraph&) = delete;
+	ReplayGraph& operator=(const ReplayGraph&) = delete;
+	~ReplayGraph() {
+		if (exec) cudaGraphExecDestroy(exec);
+	}
+	template <class F>
+	void run(Context& c, F&& body) {
+		if (!exec) {
+			const int64_t l0 = c.launches;
+			cudaGraph_t g = nullptr;
+			XTT_CUDA(cudaStreamBeginCapture(c.stream, cudaStreamCaptureModeThreadLocal));
+			try {
+				body();
+			} catch (...) {
+				cudaGraph_t t = nullptr;
+				cudaStreamEndCapture(c.stream, &t);
+				if (t) cudaGraphDestroy(t);
+				cudaGetLastError();
+				throw;
+			}
+			XTT_CUDA(cudaStreamEndCapture(c.stream, &g));
+			const cudaError_t e = cudaGraphInstantiate(&exec, g, 0);
+			cudaGraphDestroy(g);
+			XTT_CUDA(e);
+			launches = c.launches - l0;  // the body counted its launches once
+		} else {
+			c.count_launch(int(launches));
+		}
+		XTT_CUDA(cudaGraphLaunch(exec, c.stream));
+	}
+};
+
 // Applies the context's contraction precision for its scope (round, move_core, dot).
 struct ContractionPrecisionScope {
 	Context& c;

@@ -1384,6 +1384,214 @@ __global__ void __launch_bounds__(kQrSmallThreads) k_transfer_small(TransferArgs
 	}
 }
 
+// transfer_core with keepRank for narrow cores (at most 8 columns, at most 128 rows) by
+// ONE warp with the matrix in registers: lane l holds rows l, l + 32, .. of every column.
+// The same Householder QR as blk_qr (dlarfg conventions, reflectors below the diagonal,
+// dorg2r's backward Q formation) and the same absorption of R into the neighbour, with
+// warp shuffles in place of block barriers. R goes through 8 x 8 doubles of shared memory.
+// Its use is the ADF sweep, where it also applies the core's gradient step first (one
+// launch instead of two). Measured on GB300: a warp issues FP64 instructions one at a
+// time (~64 cycles each, independent ones included), so a one-warp kernel is bound by its
+// FP64 instruction count; plain moves take the 4-warp block kernel where it fits.
+constexpr int kTwCols = 8, kTwRptMax = 4, kTwMaxSlices = 16;
+
+template <int R>
+__device__ __forceinline__ double tree_sum(const double* v) {
+	if constexpr (R == 1) return v[0];
+	else if constexpr (R == 2) return v[0] + v[1];
+	else if constexpr (R == 3) return (v[0] + v[1]) + v[2];
+	else return (v[0] + v[1]) + (v[2] + v[3]);
+}
+
+__device__ __forceinline__ double warp_sum_d(double v) {
+#pragma unroll
+	for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+	return v;
+}
+
+// RPT rows per lane (mw <= 32 RPT): instantiated for 1..4 so that no lane carries padding
+// rows through the FP64 chains (a warp-wide FP64 instruction occupies GB300's FP64 pipe
+// for ~19 cycles whether or not its lanes hold data).
+template <int kTwRpt>
+__global__ void __launch_bounds__(32) k_transfer_warp(TransferArgs t) {
+	__shared__ double sR[kTwCols][kTwCols];
+	const int lane = threadIdx.x;
+	const int mw = t.right ? t.r0 * t.nf : t.nf * t.r1, nw = t.right ? t.r1 : t.r0;
+	double a[kTwRpt][kTwCols];
+#pragma unroll
+	for (int u = 0; u < kTwRpt; ++u) {
+		const int row = lane + 32 * u;
+#pragma unroll
+		for (int c = 0; c < kTwCols; ++c)
+			a[u][c] = (row < mw && c < nw) ? (t.right ? t.from[row * nw + c] : t.from[c * mw + row]) : 0.0;
+	}
+	if (t.G) {
+		// the ADF step on every slice i of core_from (rows (a, i), i = row mod n): the slice
+		// norms as n independent warp sums, their steps as n independent divisions
+		const int n = t.nf;
+		double g[kTwRpt][kTwCols];
+		double sl[kTwMaxSlices];
+#pragma unroll
+		for (int i = 0; i < kTwMaxSlices; ++i) sl[i] = 0.0;
+#pragma unroll
+		for (int u = 0; u < kTwRpt; ++u) {
+			const int row = lane + 32 * u;
+			double q = 0.0;
+#pragma unroll
+			for (int c = 0; c < kTwCols; ++c) {
+				g[u][c] = (row < mw && c < nw) ? t.G[row * nw + c] : 0.0;
+				q = fma(g[u][c], g[u][c], q);
+			}
+			const int i = row < mw ? row % n : 0;
+#pragma unroll
+			for (int ii = 0; ii < kTwMaxSlices; ++ii)
+				if (ii == i) sl[ii] += q;
+		}
+		double step[kTwMaxSlices];
+#pragma unroll
+		for (int ii = 0; ii < kTwMaxSlices; ++ii) {
+			step[ii] = 0.0;
+			if (ii >= n) continue;
+			step[ii] = warp_sum_d(sl[ii]) / t.nrm[ii];
+		}
+#pragma unroll
+		for (int u = 0; u < kTwRpt; ++u) {
+			const int row = lane + 32 * u;
+			const int i = row < mw ? row % n : 0;
+			double st = 0.0;
+#pragma unroll
+			for (int ii = 0; ii < kTwMaxSlices; ++ii)
+				if (ii == i) st = step[ii];
+#pragma unroll
+			for (int c = 0; c < kTwCols; ++c) a[u][c] = fma(st, g[u][c], a[u][c]);
+		}
+	}
+	double tau[kTwCols];
+#pragma unroll
+	for (int j = 0; j < kTwCols; ++j) {
+		tau[j] = 0.0;
+		if (j >= nw) continue;
+		// ||x||^2 below the diagonal; alpha = a(j, j) sits in lane j (rows j < 8 are in u = 0)
+		double pu[kTwRpt];
+#pragma unroll
+		for (int u = 0; u < kTwRpt; ++u) pu[u] = lane + 32 * u > j ? a[u][j] * a[u][j] : 0.0;
+		const double xn2 = warp_sum_d(tree_sum<kTwRpt>(pu));
+		const double alpha = __shfl_sync(0xffffffffu, a[0][j], j);
+		double beta, tj, scal;
+		reflector_scalars(alpha, xn2, beta, tj, scal);
+		tau[j] = tj;
+#pragma unroll
+		for (int u = 0; u < kTwRpt; ++u)
+			if (lane + 32 * u > j) a[u][j] *= scal;
+		if (lane == j) a[0][j] = beta;
+		// trailing columns: a_c -= tau (a_jc + v^T a_c) v, v = [1; x scal]
+#pragma unroll
+		for (int c = j + 1; c < kTwCols; ++c) {
+			if (c >= nw) continue;
+			double pv[kTwRpt];
+#pragma unroll
+			for (int u = 0; u < kTwRpt; ++u) pv[u] = lane + 32 * u > j ? a[u][j] * a[u][c] : 0.0;
+			if (lane == j) pv[0] = a[0][c];  // v_j = 1 (row j > j is false for u = 0, lane j)
+			const double wc = tj * warp_sum_d(tree_sum<kTwRpt>(pv));
+			if (lane == j) a[0][c] -= wc;
+#pragma unroll
+			for (int u = 0; u < kTwRpt; ++u)
+				if (lane + 32 * u > j) a[u][c] = fma(-wc, a[u][j], a[u][c]);
+		}
+	}
+	// R (rows 0..nw-1 sit in lanes 0..nw-1, u = 0)
+	if (lane < nw) {
+#pragma unroll
+		for (int c = 0; c < kTwCols; ++c) sR[lane][c] = c >= lane ? a[0][c] : 0.0;
+	}
+	__syncwarp();
+	// Q in place of the reflectors (dorg2r, backward)
+#pragma unroll
+	for (int jr = 0; jr < kTwCols; ++jr) {
+		const int j = kTwCols - 1 - jr;
+		if (j >= nw) continue;
+		const double tj = tau[j];
+#pragma unroll
+		for (int c = j + 1; c < kTwCols; ++c) {
+			if (c >= nw) continue;
+			double pv[kTwRpt];
+#pragma unroll
+			for (int u = 0; u < kTwRpt; ++u) pv[u] = lane + 32 * u > j ? a[u][j] * a[u][c] : 0.0;
+			const double wc = tj * warp_sum_d(tree_sum<kTwRpt>(pv));
+#pragma unroll
+			for (int u = 0; u < kTwRpt; ++u)
+				if (lane + 32 * u > j) a[u][c] = fma(-wc, a[u][j], a[u][c]);
+			if (lane == j) a[0][c] = -wc;
+		}
+#pragma unroll
+		for (int u = 0; u < kTwRpt; ++u) {
+			const int row = lane + 32 * u;
+			a[u][j] = row > j ? -tj * a[u][j] : (row == j ? 1.0 - tj : 0.0);
+		}
+	}
+	// the neighbour absorbs R (right: R * core_to; left: core_to * R^T), each lane reading
+	// whole columns (right) or rows (left) of core_to before writing them
+	if (t.right) {
+		const int n2 = t.nt * t.r2;
+		for (int col = lane; col < n2; col += 32) {
+			double v[kTwCols];
+#pragma unroll
+			for (int k = 0; k < kTwCols; ++k) v[k] = k < nw ? t.to[k * n2 + col] : 0.0;
+#pragma unroll
+			for (int i = 0; i < kTwCols; ++i) {
+				if (i >= nw) continue;
+				double acc = 0.0;
+#pragma unroll
+				for (int k = i; k < kTwCols; ++k) acc = fma(sR[i][k], v[k], acc);
+				t.to[i * n2 + col] = acc;
+			}
+		}
+	} else {
+		const int m2 = t.rt * t.nt;
+		for (int row = lane; row < m2; row += 32) {
+			double v[kTwCols];
+#pragma unroll
+			for (int k = 0; k < kTwCols; ++k) v[k] = k < nw ? t.to[row * nw + k] : 0.0;
+#pragma unroll
+			for (int c = 0; c < kTwCols; ++c) {
+				if (c >= nw) continue;
+				double acc = 0.0;
+#pragma unroll
+				for (int k = c; k < kTwCols; ++k) acc = fma(v[k], sR[c][k], acc);
+				t.to[row * nw + c] = acc;
+			}
+		}
+	}
+	// Q: right, core_from (mw x nw); left, Q^T as core_from (nw x mw)
+#pragma unroll
+	for (int u = 0; u < kTwRpt; ++u) {
+		const int row = lane + 32 * u;
+		if (row >= mw) continue;
+#pragma unroll
+		for (int c = 0; c < kTwCols; ++c)
+			if (c < nw) {
+				if (t.right) t.from[row * nw + c] = a[u][c];
+				else t.from[c * mw + row] = a[u][c];
+			}
+	}
+}
+
+bool transfer_warp_fits(const TransferArgs& t) {
+	const int mw = t.right ? t.r0 * t.nf : t.nf * t.r1, nw = t.right ? t.r1 : t.r0;
+	if (t.G && (!t.right || t.nf > kTwMaxSlices)) return false;
+	return nw >= 1 && nw <= kTwCols && mw >= nw && mw <= 32 * kTwRptMax;
+}
+
+void launch_transfer_warp(const TransferArgs& t, cudaStream_t s) {
+	XTT_REQUIRE(transfer_warp_fits(t), "internal: transfer_core shapes do not fit the one-warp kernel");
+	const int mw = t.right ? t.r0 * t.nf : t.nf * t.r1;
+	if (mw <= 32) k_transfer_warp<1><<<1, 32, 0, s>>>(t);
+	else if (mw <= 64) k_transfer_warp<2><<<1, 32, 0, s>>>(t);
+	else if (mw <= 96) k_transfer_warp<3><<<1, 32, 0, s>>>(t);
+	else k_transfer_warp<4><<<1, 32, 0, s>>>(t);
+	XTT_CUDA(cudaGetLastError());
+}
+
 static size_t transfer_small_bytes(const TransferArgs& t) {
 	const int mw = t.right ? t.r0 * t.nf : t.nf * t.r1, nw = t.right ? t.r1 : t.r0;
 	const long long other = t.right ? (long long)t.nt * t.r2 : (long long)t.rt * t.nt;

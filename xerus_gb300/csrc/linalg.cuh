@@ -68,9 +68,16 @@ struct TransferArgs {
 	int r0 = 0, nf = 0, r1 = 0;  // core from (r0, nf, r1)
 	int rt = 0, nt = 0, r2 = 0;  // core to: (r1, nt, r2) moving right, (rt, nt, r0) moving left
 	int right = 1;
+	// optional, moving right by one warp only: first the ADF step core_from[:, i, :] +=
+	// (||G_i||^2 / nrm[i]) G_i on each slice i (G shaped like core_from)
+	const double* G = nullptr;
+	const double* nrm = nullptr;
 };
 bool transfer_small_fits(const TransferArgs& t);
 void launch_transfer_small(const TransferArgs& t, cudaStream_t s);
+// One warp, registers: cores with at most 8 columns (of the factored matrix) and 128 rows.
+bool transfer_warp_fits(const TransferArgs& t);
+void launch_transfer_warp(const TransferArgs& t, cudaStream_t s);
 size_t qr_work_doubles(int m, int n);        // global workspace needed (0 if shared memory suffices)
 void launch_svd(const SvdArgs& a, cudaStream_t s);
 size_t svd_work_doubles(int m, int n);
