@@ -372,6 +372,16 @@ int xtt_steepest_descent(const xtt_tensor* A, xtt_tensor* x, const xtt_tensor* b
                          double convergence_epsilon, int assume_spd, double* residual, double* residual_trace,
                          int64_t trace_capacity, int64_t* trace_count);
 
+/* IHT(x, SinglePointMeasurementSet, perfData) (include/xerus/algorithms/iht.h:32,
+ * src/xerus/algorithms/iht.cpp:29-155) for at most max_iterations iterations (the
+ * reference has no stopping test and runs 10^6). Per iteration the steps beta alpha
+ * (beta = 1/1.1, 1, 1.1, .., < 1.65) of y - P(x) are each taken by one ALS sweep of x
+ * towards x + the step (the rank-(r + N) tensor is never formed); a trial no worse than
+ * the best so far is kept, as in the reference. x keeps its ranks. residual receives
+ * ||y - P(x)|| (absolute), residual_trace the best residual of every iteration. */
+int xtt_iht(xtt_tensor* x, const int64_t* positions, const double* values, int64_t num, int64_t max_iterations,
+            double* residual, double* residual_trace, int64_t trace_capacity, int64_t* trace_count);
+
 /* The retractions of src/xerus/algorithms/retractions.cpp for the Riemannian solvers:
  * SUBMANIFOLD: SubmanifoldRetractionI / II (:222-236), componentwise addition of the
  * tangent components, then move_core(0, keepRank) - what xtt_geometric_cg and

@@ -5,7 +5,7 @@
 //   golden_driver <case> <outdir>
 //
 // Cases: rng, tt_random, dot, movecore, round, als, dmrg, adf, adf_cfg5, fileio, als_nonspd,
-// arith, adf_rankone, gcg, adf_rankinc, qc_gap, retractions, and the timings time_cfg1/2/4/5.
+// arith, adf_rankone, gcg, adf_rankinc, qc_gap, retractions, iht, and the timings time_cfg1/2/4/5.
 // Every case seeds xerus::misc::randomEngine with 0xBAADF00D and resets
 // xerus::misc::defaultNormalDistribution (dropping a cached polar variate) first,
 // so a case's draws do not depend on the cases run before it.
@@ -977,6 +977,50 @@ static void case_fileio() {
 	save_file_bytes("A_bytes", g_out + "/A.xrs");
 }
 
+// IHT (algorithms/iht.cpp:29-155) on a small completion problem. The reference loops
+// 10^6 iterations with no stopping test, so the run is ended from the PerformanceData's
+// error callback, which sees every iterate: it records the iterate's probes and, after
+// the twelfth, throws. The recorded residuals are PerformanceData's (one per iteration).
+struct StopIht {};
+static void case_iht() {
+	reseed();
+	const std::vector<size_t> dims{4, 3, 4, 3, 4};
+	TTTensor target = TTTensor::random(dims, 2);
+	target /= frob_norm(target);
+	const size_t N = 60;
+	SinglePointMeasurementSet m = SinglePointMeasurementSet::random(N, dims);
+	m.measure(target);
+	TTTensor x = TTTensor::random(dims, 2);
+	x /= frob_norm(x);
+	save_tt("x0", x);
+	std::vector<int64_t> pos;
+	for (auto& p : m.positions)
+		for (auto i : p) pos.push_back(int64_t(i));
+	save("positions", pos, {N, dims.size()});
+	save("values", m.measuredValues);
+	const auto probes = probe_positions(dims, 80, 53);
+	std::vector<double> probe_vals;
+	std::vector<int64_t> probe_pos;
+	for (auto& p : probes)
+		for (auto i : p) probe_pos.push_back(int64_t(i));
+	save("probe_pos", probe_pos, {probes.size(), dims.size()});
+	size_t seen = 0;
+	const size_t iters = 12;
+	PerformanceData perf(
+	    [&](const TTTensor& xi) -> double {
+		    for (auto& p : probes) probe_vals.push_back(tt_entry(xi, p));
+		    if (++seen >= iters) throw StopIht();
+		    return 0.0;
+	    },
+	    false, true);
+	try {
+		IHT(x, m, perf);
+	} catch (const StopIht&) {
+	}
+	save("perf_residual", perf_residuals(perf));
+	save("probe_val", probe_vals, {seen, probes.size()});
+}
+
 // ------------------------------------------------------------------- timing
 // The reference's own implementation timed on this host (wall clock around the
 // algorithm call only; inputs drawn as in the golden cases, PerformanceData
@@ -1110,6 +1154,7 @@ int main(int argc, char** argv) {
 	else if (c == "adf_rankinc") case_adf_rankinc();
 	else if (c == "qc_gap") case_qc_gap();
 	else if (c == "retractions") case_retractions();
+	else if (c == "iht") case_iht();
 	else if (c == "time_cfg1") case_time_cfg1();
 	else if (c == "time_cfg2") case_time_cfg2();
 	else if (c == "time_cfg4") case_time_cfg4();

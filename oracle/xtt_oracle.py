@@ -1501,3 +1501,70 @@ def steepest_descent(A: TTOp | None, x: TT, b: TT, num_steps: int = 0, conv_eps:
             curr = orthogonal_norm(res.copy())
         trace.append(curr)
     return curr, trace
+
+
+# --------------------------------------------------------------------------- IHT
+
+
+def iht(x: TT, positions, values, max_iter: int) -> tuple[float, list]:
+    """IHT (algorithms/iht.cpp:29-155) with an iteration cap (the reference loops 10^6 times).
+    Per iteration: the current entries at the samples; for beta = 1/1.1, 1, 1.1, .. (< 1.65)
+    the rank-(r + N) TT largeX = x + sum_s beta alpha (y_s - cur_s) e_{pos_s} (x's cores
+    plus one sparse channel per sample), then ONE ALS sweep of newX (a copy of x, moved to
+    core 0) towards largeX: right stacks of (newX, largeX) from the right, then left to right
+    each core set to its projection of largeX and the core moved on (keepRank). A trial
+    whose residual ||y - P(newX)|| is <= the best so far (initially twice the previous
+    residual) replaces x and scales alpha by its beta. As in the reference, the trials of an
+    iteration after an accepted one start from (and add to) the new x, with the entries
+    `cur` of the iteration's start. Returns (residual, the best residual of every iteration)."""
+    pos = np.asarray(positions, dtype=np.int64)
+    y = np.asarray(values, dtype=np.float64)
+    N, d = pos.shape
+    alpha, residual = 1.0, 1.0
+    trace = []
+    for _ in range(max_iter):
+        cur = tt_entries(x, pos)
+        best, new_alpha = residual * 2, alpha
+        beta = 1 / 1.1
+        while beta < 1.1 * 1.5:
+            w = beta * alpha * (y - cur)
+            nx = x.copy()
+            move_core(nx, 0, keep_rank=True)
+            # right stacks at bonds k (between cores k-1 and k): dense (newX vs x) and
+            # per-sample (newX's right products at the sample), both 1 at bond d
+            D = [None] * (d + 1)
+            S = [None] * (d + 1)
+            D[d] = np.ones((1, 1))
+            S[d] = np.ones((1, N))
+            for k in range(d - 1, 0, -1):
+                D[k] = _iht_push_right(nx.cores[k], x.cores[k], D[k + 1])
+                S[k] = np.einsum("asc,cs->as", nx.cores[k][:, pos[:, k], :], S[k + 1])
+            LD = np.ones((1, 1))
+            LS = None  # per-sample left products (carrying w), from core 1 on
+            for k in range(d):
+                dense = np.einsum("ab,bic,dc->aid", LD, x.cores[k], D[k + 1], optimize=True)
+                right_s = S[k + 1]                              # (r', N)
+                left_s = w[None, :] if k == 0 else LS            # (r, N)
+                sparse = np.zeros_like(dense)
+                outer = np.einsum("as,cs->sac", left_s, right_s)
+                for s in range(N):
+                    sparse[:, pos[s, k], :] += outer[s]
+                nx.cores[k] = dense + sparse
+                if k + 1 < d:
+                    move_core(nx, k + 1, keep_rank=True)
+                    LD = np.einsum("ab,aic,bid->cd", LD, nx.cores[k], x.cores[k], optimize=True)
+                    LS = np.einsum("as,asc->cs", left_s, nx.cores[k][:, pos[:, k], :])
+            r = math.sqrt(float(np.sum((y - tt_entries(nx, pos)) ** 2)))
+            if r <= best:
+                x.cores, x.canonicalized, x.core_position = nx.cores, nx.canonicalized, nx.core_position
+                best, new_alpha = r, alpha * beta
+            beta *= 1.1
+        residual, alpha = best, new_alpha
+        trace.append(best)
+    return residual, trace
+
+
+def _iht_push_right(u, v, D):
+    """next(i1, i2) = sum u(i1, i5, i3) v(i2, i5, i4) D(i3, i4) (iht.cpp:113)."""
+    t = np.tensordot(u, D, axes=([2], [0]))        # (i1, i5, i4)
+    return np.tensordot(t, v, axes=([1, 2], [1, 2]))  # (i1, i2)

@@ -21,7 +21,7 @@ import numpy as np
 
 HERE = os.path.dirname(os.path.abspath(__file__))
 ROOT = os.path.dirname(os.path.dirname(HERE))
-CASES = ["rng", "tt_random", "dot", "movecore", "round", "als", "dmrg", "adf", "adf_cfg5", "fileio", "als_nonspd", "arith", "adf_rankone", "gcg", "adf_rankinc", "qc_gap", "retractions"]
+CASES = ["rng", "tt_random", "dot", "movecore", "round", "als", "dmrg", "adf", "adf_cfg5", "fileio", "als_nonspd", "arith", "adf_rankone", "gcg", "adf_rankinc", "qc_gap", "retractions", "iht"]
 
 
 def main(argv):

@@ -625,8 +625,10 @@ def test_adf_rank_increase_matches_reference(ctx, golden):
     r, rr = np.array(perf.residuals), z["perf_residual"]
     first = list(z["perf_ranks"][:, 0]).index(2)  # the first point after the first increase
     assert np.max(np.abs(r[:first] / rr[:first] - 1)) < 1e-10
-    assert np.max(np.abs(r / rr - 1)) < 1e-6
-    assert abs(res / z["final_residual"][0] - 1) < 1e-6
+    # relative 1e-6, or 1e-15 absolute (relative residuals of ||y|| = 1: the rounding of the
+    # sum of squares over the samples) where the trajectory has fallen to ~1e-10
+    assert np.all(np.abs(r - rr) <= 1e-6 * rr + 1e-15)
+    assert abs(res - z["final_residual"][0]) <= 1e-6 * z["final_residual"][0] + 1e-15
     assert [1] + x.ranks() + [1] == list(z["x_final_ranks"])
     assert rel_err(x.entries(z["x_final_probe_pos"]), z["x_final_probe_val"]) < 1e-8
 
@@ -652,6 +654,20 @@ def test_hosvd_and_als_retractions_match_reference(ctx, golden, alg, kind, spd):
     assert abs(res / z[tag + "_residual"][0] - 1) < 1e-9
     assert [1] + x.ranks() + [1] == list(z[tag + "_ranks"])
     assert rel_err(x.entries(z[tag + "_x_probe_pos"]), z[tag + "_x_probe_val"]) < 1e-8
+
+
+def test_iht_matches_reference(ctx, golden):
+    """IHT (iht.cpp:29-155) capped at 11 iterations: every iteration's best residual and the
+    iterate after the eleventh against the reference's own run (which is stopped from its
+    PerformanceData callback: it has no stopping test)."""
+    z = golden("iht")
+    x = dev_tt(ctx, tt_of(z, "x0"))
+    m = xg.SinglePointMeasurementSet(z["positions"], z["values"])
+    perf = xg.PerformanceData()
+    res = xg.IHT(x, m, perf, maxIterations=11)
+    assert rel_err(perf.residuals, z["perf_residual"]) < 1e-10
+    assert abs(res / z["perf_residual"][-1] - 1) < 1e-10
+    assert rel_err(x.entries(z["probe_pos"]), z["probe_val"][10]) < 1e-9
 
 
 def test_adf_rank_one_matches_reference(ctx, golden):

@@ -314,3 +314,13 @@ def test_hosvd_and_als_retractions(golden, alg, kind, spd):
     assert abs(res / z[tag + "_residual"][0] - 1) < 1e-9
     assert [1] + x.ranks + [1] == list(z[tag + "_ranks"])
     assert rel_err(o.tt_entries(x, z[tag + "_x_probe_pos"]), z[tag + "_x_probe_val"]) < 1e-8
+
+
+def test_iht_matches_reference(golden):
+    """IHT (iht.cpp:29-155), capped at 11 iterations: the reference's residual after every
+    iteration (its PerformanceData) and the probes of its iterate after the eleventh."""
+    z = golden("iht")
+    x = tt_of(z, "x0")
+    res, trace = o.iht(x, z["positions"], z["values"], 11)
+    assert rel_err(trace, z["perf_residual"]) < 1e-12
+    assert rel_err(o.tt_entries(x, z["probe_pos"]), z["probe_val"][10]) < 1e-11

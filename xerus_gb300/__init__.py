@@ -17,7 +17,7 @@ import numpy as np
 from . import _lib as L
 
 __all__ = ["Context", "TTTensor", "TTOperator", "frob_norm", "dot", "residual", "ALSVariant", "ALS", "ALS_SPD", "DMRG", "DMRG_SPD", "ASD",
-           "ASD_SPD", "ADFVariant", "ADF", "SinglePointMeasurementSet", "RankOneMeasurementSet", "GeometricCGVariant", "GeometricCG", "SteepestDescentVariant", "SteepestDescent", "SubmanifoldRetraction", "HOSVDRetraction", "ALSRetraction", "PerformanceData", "seed", "EPSILON",
+           "ASD_SPD", "ADFVariant", "ADF", "IHT", "SinglePointMeasurementSet", "RankOneMeasurementSet", "GeometricCGVariant", "GeometricCG", "SteepestDescentVariant", "SteepestDescent", "SubmanifoldRetraction", "HOSVDRetraction", "ALSRetraction", "PerformanceData", "seed", "EPSILON",
            "XttError", "FP64", "MIXED", "als_batch", "apply", "save_to_file", "load_from_file", "file_encode", "file_decode"]
 
 EPSILON = 8 * np.finfo(np.float64).eps  # include/xerus/basic.h:50
@@ -768,6 +768,21 @@ class ADFVariant:
         L.check(x.lib.xtt_adf_gradient(x.handle, pp, pv, pos.shape[0], ctypes.byref(loss),
                                        g.ctypes.data_as(L.c_double_p), g.size))
         return loss.value, _split(g, x)
+
+
+def IHT(x, measurements, perfData=None, maxIterations=100):
+    """xerus::IHT(x, measurements, perfData) (include/xerus/algorithms/iht.h:32) with an
+    iteration cap (the reference runs 10^6 iterations); returns ||y - P(x)||."""
+    pos, pp = _i64(measurements.positions)
+    val, pv = _f64(measurements.measuredValues)
+    cap = max(1, int(maxIterations))
+    trace = np.zeros(cap)
+    res, cnt = ctypes.c_double(), ctypes.c_int64()
+    L.check(x.lib.xtt_iht(x.handle, pp, pv, pos.shape[0], int(maxIterations), ctypes.byref(res),
+                          trace.ctypes.data_as(L.c_double_p), cap, ctypes.byref(cnt)))
+    if perfData is not None:
+        perfData.residuals = list(trace[:min(cnt.value, cap)])
+    return res.value
 
 
 def _split(flat, x):

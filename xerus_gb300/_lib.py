@@ -95,6 +95,8 @@ _SIGNATURES = {
     "xtt_steepest_descent_retraction": (ctypes.c_int, [VP, VP, VP, ctypes.c_int64, ctypes.c_double, ctypes.c_int,
                                                        ctypes.c_int, c_double_p, c_double_p, ctypes.c_int64,
                                                        c_int64_p]),
+    "xtt_iht": (ctypes.c_int, [VP, c_int64_p, c_double_p, ctypes.c_int64, ctypes.c_int64, c_double_p, c_double_p,
+                               ctypes.c_int64, c_int64_p]),
     "xtt_random_rank_one": (ctypes.c_int, [ctypes.c_int64, ctypes.c_int64, c_int64_p, c_double_p]),
     "xtt_entries_rank_one": (ctypes.c_int, [VP, c_double_p, ctypes.c_int64, c_double_p]),
     "xtt_adf_rank_one": (ctypes.c_int, [VP, c_double_p, c_double_p, ctypes.c_int64, ctypes.POINTER(AdfOptions),

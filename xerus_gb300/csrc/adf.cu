@@ -23,6 +23,7 @@
 #include <cfloat>
 #include <cmath>
 
+#include "als.cuh"
 #include "engine.cuh"
 
 namespace xtt {
@@ -646,6 +647,106 @@ AdfResult adf(Tensor& x, const int64_t* positions, const double* values, long lo
 		for (long long i = 0; i < N; ++i) s2 += (e[i] - values[i]) * (e[i] - values[i]);
 		out.checked_residual = std::sqrt(s2) / norm_y;
 	}
+	return out;
+}
+
+// ------------------------------------------------------------ IHT
+
+__global__ void k_iht_add(double* y, const double* x, long long n) {
+	for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x)
+		y[i] += x[i];
+}
+
+static void run_gemm_chain(Context& c, const GemmChain& ch) {
+	for (int i = 0; i < ch.ns; ++i) gemm(c, ch.g[i]);
+}
+
+IhtResult iht(Tensor& x, const int64_t* positions, const double* values, long long N, int64_t max_iter) {
+	// IHT (src/xerus/algorithms/iht.cpp:29-155) with an iteration cap. largeX = x + sum_s w_s
+	// e_{pos_s} (w_s = beta alpha (y_s - cur_s)) is never formed: its rank-(r + N) block
+	// structure splits every contraction of the ALS sweep into a dense part (the
+	// environments of newX against x: the operator-free ALS stacks and local projection)
+	// and a per-sample part (newX's backward / forward products at the samples, the ADF
+	// stacks, weighted by w_s: ADF's projected-gradient kernel with w in place of the
+	// residual). Each trial: newX = x moved to core 0, right stacks, then left to right
+	// core k = dense + per-sample projection, move on (keepRank), push the left stacks.
+	Context& c = *x.ctx;
+	XTT_REQUIRE(!x.op, "IHT needs a TT tensor");
+	XTT_REQUIRE(N > 0, "need at very least one measurement");
+	XTT_REQUIRE(max_iter >= 0, "max_iter must be >= 0");
+	const int d = x.d;
+	Tensor nx(&c, false, d, x.dims.data(), x.ranks.data());
+	nx.copy_from(x);
+	AdfData D(c, nx, positions, values, N, false);
+	// dense environments (x rank first, newX rank second, as the operator-free ALS stacks)
+	std::vector<size_t> off(d + 2, 0);
+	size_t maxcore = 1, maxr2 = 1;
+	for (int k = 0; k <= d; ++k) {
+		off[k + 1] = off[k] + size_t(x.ranks[k]) * x.ranks[k];
+		maxr2 = std::max(maxr2, size_t(x.ranks[k]) * x.ranks[k]);
+	}
+	for (int k = 0; k < d; ++k) maxcore = std::max(maxcore, x.core_size(k));
+	double* Rb = c.scratch<double>(S_ADF_FIRST + 20, off[d + 1]);
+	double* Lb = c.scratch<double>(S_ADF_FIRST + 21, 2 * maxr2);
+	double* tmp = c.scratch<double>(S_ADF_FIRST + 22, maxcore);
+	double* G = c.scratch<double>(S_ADF_FIRST + 23, maxcore);
+	std::vector<double> cur(N), w(N), e(N);
+	auto resid = [&](const Tensor& t) {
+		entries(t, positions, N, e.data());
+		double s2 = 0;
+		for (long long i = 0; i < N; ++i) s2 += (values[i] - e[i]) * (values[i] - e[i]);
+		return std::sqrt(s2);
+	};
+	IhtResult out;
+	double alpha = 1.0, residual = 1.0;
+	for (int64_t it = 0; it < max_iter; ++it) {
+		entries(x, positions, N, cur.data());
+		double best = residual * 2, new_alpha = alpha;
+		for (double beta = 1 / 1.1; beta < 1.1 * 1.5; beta *= 1.1) {
+			for (long long i = 0; i < N; ++i) w[i] = beta * alpha * (values[i] - cur[i]);
+			XTT_CUDA(cudaMemcpyAsync(D.res, w.data(), N * sizeof(double), cudaMemcpyHostToDevice, c.stream));
+			nx.copy_from(x);
+			move_core(nx, 0, true);
+			fill(c, Rb + off[d], 1.0, 1);
+			for (int k = d - 1; k > 0; --k) {
+				run_gemm_chain(c, plan_push_right_rhs(Rb + off[k + 1], x.core[k], nx.core[k], Rb + off[k], tmp,
+				                                      x.ranks[k], nx.ranks[k], x.dims[k], x.ranks[k + 1],
+				                                      nx.ranks[k + 1]));
+				D.backward(k);
+			}
+			double* lcur = Lb;
+			double* lnext = Lb + maxr2;
+			fill(c, lcur, 1.0, 1);
+			for (int k = 0; k < d; ++k) {
+				const long long len = (long long)nx.core_size(k);
+				run_gemm_chain(c, plan_local_rhs1(lcur, x.core[k], Rb + off[k + 1], nx.core[k], tmp, nx.ranks[k],
+				                                  nx.ranks[k + 1], x.ranks[k], x.ranks[k + 1], x.dims[k]));
+				D.res_grad(k, 1, nx.core[k], G, 1.0);
+				k_iht_add<<<unsigned(std::min<long long>((len + 255) / 256, 1024)), 256, 0, c.stream>>>(nx.core[k], G,
+				                                                                                       len);
+				XTT_CUDA(cudaGetLastError());
+				c.count_launch();
+				if (k + 1 < d) {
+					move_core(nx, k + 1, true);
+					run_gemm_chain(c, plan_push_left_rhs(lcur, x.core[k], nx.core[k], lnext, tmp, x.ranks[k],
+					                                     nx.ranks[k], x.dims[k], x.ranks[k + 1], nx.ranks[k + 1]));
+					std::swap(lcur, lnext);
+					D.forward(k);
+				}
+			}
+			const double r = resid(nx);
+			if (r <= best) {
+				x.copy_from(nx);
+				best = r;
+				new_alpha = alpha * beta;
+			}
+		}
+		residual = best;
+		alpha = new_alpha;
+		out.trace.push_back(best);
+	}
+	c.sync();
+	out.residual = residual;
 	return out;
 }
 

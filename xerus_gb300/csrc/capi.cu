@@ -797,6 +797,24 @@ int xtt_adf_max_ranks(xtt_tensor* x, const int64_t* positions, const double* val
 	});
 }
 
+int xtt_iht(xtt_tensor* x, const int64_t* positions, const double* values, int64_t num, int64_t max_iterations,
+            double* residual, double* residual_trace, int64_t trace_capacity, int64_t* trace_count) {
+	return guard([&] {
+		xtt::DeviceScope dev_scope(x ? x->t->ctx->device : -1);
+		ARG(x && positions && values, "NULL argument");
+		ARG(max_iterations >= 0, "max_iterations must be >= 0");
+		xtt::Tensor& t = *x->t;
+		for (int64_t s = 0; s < num; ++s)
+			for (int k = 0; k < t.d; ++k)
+				ARG(positions[s * t.d + k] >= 0 && positions[s * t.d + k] < t.dims[k], "measurement position out of range");
+		const xtt::IhtResult r = xtt::iht(t, positions, values, num, max_iterations);
+		if (residual) *residual = r.residual;
+		if (residual_trace)
+			for (size_t i = 0; i < r.trace.size() && int64_t(i) < trace_capacity; ++i) residual_trace[i] = r.trace[i];
+		if (trace_count) *trace_count = int64_t(r.trace.size());
+	});
+}
+
 static int riemann_call(bool cg, const xtt_tensor* A, xtt_tensor* x, const xtt_tensor* b, int64_t num_steps,
                         double convergence_epsilon, int assume_spd, int retraction, double* residual,
                         double* residual_trace, int64_t trace_capacity, int64_t* trace_count) {

@@ -293,6 +293,12 @@ constexpr double kXerusEpsilon = 8 * 2.220446049250313e-16;
 AdfResult adf(Tensor& x, const int64_t* positions, const double* values, long long N, int64_t max_iter, double target,
               double min_dec, int precision = XTT_PRECISION_FP64, const std::vector<int64_t>* max_ranks = nullptr,
               const std::function<void(Tensor&)>& add_random_rank_one = {});
+// IHT for single-point samples (positions: N x d, row-major) with an iteration cap.
+struct IhtResult {
+	double residual = 0;          // ||y - P(x)|| of the returned x (absolute, as the reference)
+	std::vector<double> trace;    // the best residual of every iteration
+};
+IhtResult iht(Tensor& x, const int64_t* positions, const double* values, long long N, int64_t max_iter);
 // Riemannian CG on the fixed-rank TT manifold (GeometricCGVariant with the submanifold
 // retraction and projective vector transport); A null: minimise ||x - b||.
 struct RiemannReport {
