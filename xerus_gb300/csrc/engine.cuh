@@ -178,7 +178,8 @@ enum ScratchId : int {
 	S_RES_CORE0, S_RES_CORE1, S_RES_R, S_RED, S_ENT_META, S_ENT_CORES, S_ENT_OUT,
 	S_RES_CORE0B, S_RES_CORE1B, S_RES_RB, S_QR_WORKB, S_BATCH_META, S_BATCH_WORK, S_BATCH_BACKUP,
 	S_SVD_PC_Q, S_SVD_PC_C, S_SVD_PC_UV, S_SVD_PC_QRW, S_GEMM_TC_WORK, S_SVD_PC_CT, S_SVD_PC_UT,
-	S_SVD_MX_W32, S_SVD_MX_W, S_SVD_MX_W2, S_SVD_MX_G, S_SVD_MX_B0, S_TMA_A, S_TMA_B,
+	S_SVD_MX_W32, S_SVD_MX_W, S_SVD_MX_W2, S_SVD_MX_G, S_SVD_MX_B0, S_TMA_A, S_TMA_B, S_SVD_RF_U, S_SVD_RF_V,
+	S_SVD_RF_M,
 	S_ALS_FIRST = 48,
 	S_ADF_FIRST = 112,
 	S_MAX = 176

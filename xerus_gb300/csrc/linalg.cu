@@ -2463,11 +2463,11 @@ bool svd_f32_fits(int p, int q) {
 }
 
 // One CTA: B (p x q, column-major) and V (q x q, column-major) in FP32 shared memory;
-// round-robin one-sided Jacobi, one warp per pair, until a sweep rotates nothing at
-// the FP32 threshold (or max_sweeps); W = V written row-major. The input is scaled by
-// the power of two that brings its largest entry to [0.5, 1), so squares and sums
-// stay in FP32 range. Its purpose is a starting rotation for the FP64 sweeps: the
-// FP64 Jacobi started from X W converges in a few sweeps.
+// round-robin one-sided Jacobi, one half-warp per pair, until a sweep's largest |cos|
+// between paired columns is below 3e-3 (or max_sweeps); W = V written row-major. The
+// input is scaled by the power of two that brings its largest entry to [0.5, 1), so
+// squares and sums stay in FP32 range. Its purpose is a start for the FP64 stage (the
+// product refinement, or Jacobi sweeps that started from X W converge in a few).
 __global__ void __launch_bounds__(kSvf32Threads) k_svd_f32(const double* __restrict__ X, long long ldx, int p, int q,
                                                           float* __restrict__ W, int max_sweeps) {
 	extern __shared__ float fsm[];
@@ -2509,48 +2509,62 @@ __global__ void __launch_bounds__(kSvf32Threads) k_svd_f32(const double* __restr
 	for (long long e = tid; e < (long long)p * q; e += blockDim.x) fl = fmaf(B[e], B[e], fl);
 	const float fro = block_sum(fl, f_red);
 	const float negl = fro * 1e-12f;
-	// a start for the FP64 sweeps, not an SVD: FP32-level orthogonality, at most 12
-	// sweeps (near FP32 rounding the sweeps would go on rotating noise; an FP64 sweep
-	// costs about ten of these, so the FP32 stage goes as far as it usefully can)
-	const float tol = 4.f * sqrtf(float(p)) * FLT_EPSILON;
-	const int qe = q + (q & 1);
+	// a start for the FP64 stage, not an SVD: FP32-level orthogonality, at most 12
+	// sweeps (near FP32 rounding the sweeps would go on rotating noise)
+	const float tol = 4.f * sqrtf(float(p)) * FLT_EPSILON, tol2 = tol * tol;
+	// a sweep whose largest |cos| between paired columns is below 3e-3 leaves them at
+	// FP32 rounding (the sweeps converge quadratically); the next would rotate noise
+	const float big2 = 9e-6f;
+	const int qe = q + (q & 1), half = lane >> 4, hl = lane & 15;
 	for (int sweep = 0; sweep < max_sweeps; ++sweep) {
 		if (tid == 0) s_rot = 0;
 		__syncthreads();
 		for (int t = 0; t < qe - 1; ++t) {
-			for (int lp = warp; lp < qe / 2; lp += nwarps) {
-				const int i = svc_col(lp, t, qe), j = svc_col(qe - 1 - lp, t, qe);
-				if (i >= q || j >= q) continue;
+			// one half-warp per pair: every lane of a warp takes part in its shuffles
+			for (int lp0 = 2 * warp; lp0 < qe / 2; lp0 += 2 * nwarps) {
+				const int lp = lp0 + half;
+				int i = 0, j = 0;
+				bool ok = lp < qe / 2;
+				if (ok) {
+					i = svc_col(lp, t, qe);
+					j = svc_col(qe - 1 - lp, t, qe);
+					ok = i < q && j < q;
+				}
 				float* bi = B + (size_t)i * p;
 				float* bj = B + (size_t)j * p;
 				float al = 0.f, be = 0.f, ga = 0.f;
-				for (int r = lane; r < p; r += 32) {
-					const float x = bi[r], y = bj[r];
-					al = fmaf(x, x, al);
-					be = fmaf(y, y, be);
-					ga = fmaf(x, y, ga);
+				if (ok)
+					for (int r = hl; r < p; r += 16) {
+						const float x = bi[r], y = bj[r];
+						al = fmaf(x, x, al);
+						be = fmaf(y, y, be);
+						ga = fmaf(x, y, ga);
+					}
+#pragma unroll
+				for (int o = 8; o > 0; o >>= 1) {
+					al += __shfl_xor_sync(0xffffffffu, al, o);
+					be += __shfl_xor_sync(0xffffffffu, be, o);
+					ga += __shfl_xor_sync(0xffffffffu, ga, o);
 				}
-				al = warp_sum(al);
-				be = warp_sum(be);
-				ga = warp_sum(ga);
-				if (ga != 0.f && fminf(al, be) > negl && fabsf(ga) > tol * sqrtf(al * be)) {
+				const float ab = al * be, g2s = ga * ga;
+				if (ok && ga != 0.f && fminf(al, be) > negl && g2s > tol2 * ab) {
 					const float dba = be - al, g2 = 2.f * ga;
-					float tt = fabsf(g2) / (fabsf(dba) + sqrtf(fmaf(dba, dba, g2 * g2)));
+					float tt = __fdividef(fabsf(g2), fabsf(dba) + sqrtf(fmaf(dba, dba, g2 * g2)));
 					if ((dba < 0.f) != (ga < 0.f)) tt = -tt;
 					const float cs = rsqrtf(fmaf(tt, tt, 1.f)), sn = cs * tt;
-					for (int r = lane; r < p; r += 32) {
+					for (int r = hl; r < p; r += 16) {
 						const float x = bi[r], y = bj[r];
 						bi[r] = cs * x - sn * y;
 						bj[r] = sn * x + cs * y;
 					}
 					float* vi = V + (size_t)i * q;
 					float* vj = V + (size_t)j * q;
-					for (int r = lane; r < q; r += 32) {
+					for (int r = hl; r < q; r += 16) {
 						const float x = vi[r], y = vj[r];
 						vi[r] = cs * x - sn * y;
 						vj[r] = sn * x + cs * y;
 					}
-					if (lane == 0) s_rot = 1;
+					if (hl == 0 && g2s > big2 * ab) s_rot = 1;
 				}
 			}
 			__syncthreads();
@@ -2568,7 +2582,9 @@ void launch_svd_f32(const double* X, long long ldx, int p, int q, float* W, cuda
 	XTT_REQUIRE(svd_f32_fits(p, q), "internal: FP32 Jacobi stage does not fit one CTA");
 	func_attr_once(k_svd_f32, cudaFuncAttributeMaxDynamicSharedMemorySize, int(kDynSmemMax));
 	const size_t smem = (size_t(p) * q + size_t(q) * q) * sizeof(float);
-	k_svd_f32<<<1, kSvf32Threads, smem, s>>>(X, ldx, p, q, W, 12);
+	// one half-warp per column pair
+	const int qe = q + (q & 1), threads = std::min(kSvf32Threads, std::max(64, 32 * ((qe / 2 + 1) / 2)));
+	k_svd_f32<<<1, threads, smem, s>>>(X, ldx, p, q, W, 12);
 	XTT_CUDA(cudaGetLastError());
 }
 

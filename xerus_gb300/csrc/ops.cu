@@ -593,12 +593,210 @@ __global__ void k_f2d(double* out, const float* in, size_t n) {
 		out[i] = double(in[i]);
 }
 
+// ------------------------------------------------------------ SVD refinement by products
+// Square X = U Sigma V^T from approximate factors (the FP32 Jacobi's V, U from X V) by the
+// Newton-type refinement of Ogita and Aishima ("Iterative refinement for singular value
+// decomposition based on matrix multiplication", J. Comput. Appl. Math. 369, 2020): with
+// U = U^(I + F), V = V^(I + G), the conditions U^T U = I, V^T V = I and U^T X V = Sigma,
+// to first order in F and G, give for R = I - U^T U, S = I - V^T V, T = U^T X V:
+//   sigma_i = T_ii / (1 - (R_ii + S_ii) / 2),  F_ii = R_ii / 2,  G_ii = S_ii / 2,
+//   F_ij = (a s_j + b s_i) / (s_j^2 - s_i^2),  G_ij = (a s_i + b s_j) / (s_j^2 - s_i^2)
+//   with a = T_ij + s_j R_ij, b = T_ji + s_j S_ij (i != j).
+// Each step is four FP64 products (U^T U and V^T V as one batched launch) and an
+// elementwise kernel, with no rotation sweeps (each of whose steps ends in a barrier).
+// The error squares per step: the FP32 start (~1e-4 in the vectors, FP32 rounding over
+// the relative gaps) reaches FP64 rounding in three. Near-equal or near-zero singular
+// values, where first-order corrections are not small, and a last step whose corrections
+// are still above 1e-9 set a flag: the caller then runs the FP64 Jacobi sweeps instead.
+constexpr int kOaSteps = 3;
+
+__device__ __forceinline__ double warp_max(double v) {
+#pragma unroll
+	for (int o = 16; o > 0; o >>= 1) v = fmax(v, __shfl_xor_sync(0xffffffffu, v, o));
+	return v;
+}
+
+// Columns of Y = X V normalised into U (both q x q row-major); a zero column sets the flag.
+__global__ void k_oa_normalize(const double* Y, double* U, int q, int* flag) {
+	const int lane = threadIdx.x & 31, warps = blockDim.x >> 5;
+	for (int c = blockIdx.x * warps + (threadIdx.x >> 5); c < q; c += gridDim.x * warps) {
+		double s = 0;
+		for (int i = lane; i < q; i += 32) s = fma(Y[(long long)i * q + c], Y[(long long)i * q + c], s);
+		s = sqrt(warp_sum(s));
+		if (!(s > 0.0)) {
+			if (lane == 0) atomicExch(flag, 1);
+			continue;
+		}
+		const double inv = 1.0 / s;
+		for (int i = lane; i < q; i += 32) U[(long long)i * q + c] = Y[(long long)i * q + c] * inv;
+	}
+}
+
+// PQ = [U^T U | V^T V], T = U^T X V (q x q each). One row i per block (grid-stride):
+// sigma_i into sig, rows i of I + F and I + G into FG = [I + F | I + G]. The flag is set
+// for a relative gap below 1e-5, a singular value below 1e-13 of the largest, or (last
+// step) a correction above 1e-9.
+__global__ void k_oa_correct(const double* PQ, const double* T, double* FG, double* sig, int q, int last, int* flag) {
+	extern __shared__ double s_sig[];
+	__shared__ double s_max[32];
+	const long long qq = (long long)q * q;
+	const double* P = PQ;
+	const double* Qm = PQ + qq;
+	for (int j = threadIdx.x; j < q; j += blockDim.x) {
+		const double r = 1.0 - P[(long long)j * q + j], t = 1.0 - Qm[(long long)j * q + j];
+		s_sig[j] = T[(long long)j * q + j] / (1.0 - 0.5 * (r + t));
+	}
+	__syncthreads();
+	double mx = 0;
+	for (int j = threadIdx.x; j < q; j += blockDim.x) mx = fmax(mx, fabs(s_sig[j]));
+	mx = warp_max(mx);
+	if ((threadIdx.x & 31) == 0) s_max[threadIdx.x >> 5] = mx;
+	__syncthreads();
+	double smax = 0;
+	for (int w = 0; w < int(blockDim.x >> 5); ++w) smax = fmax(smax, s_max[w]);
+	int bad = 0;
+	for (int i = blockIdx.x; i < q; i += gridDim.x) {
+		const double si = s_sig[i];
+		if (threadIdx.x == 0) {
+			sig[i] = si;
+			if (!(si > 1e-13 * smax)) bad = 1;
+		}
+		for (int j = threadIdx.x; j < q; j += blockDim.x) {
+			const long long ij = (long long)i * q + j, ji = (long long)j * q + i;
+			double f, g;
+			if (i == j) {
+				f = 0.5 * (1.0 - P[ij]);
+				g = 0.5 * (1.0 - Qm[ij]);
+			} else {
+				const double sj = s_sig[j], dif = sj - si;
+				if (!(fabs(dif) > 1e-5 * fmax(fabs(si), fabs(sj)))) {
+					bad = 1;
+					f = g = 0.0;
+				} else {
+					const double a = T[ij] - sj * P[ij], b = T[ji] - sj * Qm[ij], inv = 1.0 / (dif * (sj + si));
+					f = (a * sj + b * si) * inv;
+					g = (a * si + b * sj) * inv;
+				}
+			}
+			if (last && (fabs(f) > 1e-9 || fabs(g) > 1e-9)) bad = 1;
+			FG[ij] = f + (i == j ? 1.0 : 0.0);
+			FG[qq + ij] = g + (i == j ? 1.0 : 0.0);
+		}
+	}
+	if (bad) atomicExch(flag, 1);
+}
+
+// Sort descending, the reference's truncation (rank cap, first j >= 1 with S_j <= eps S_0),
+// the sign gauge (largest |entry| of each kept left vector positive, first on ties), and
+// U (m x rank), S, V^T (rank x n); nothing when the flag is set.
+__global__ void k_oa_finish(const double* UV, const double* sig, int q, SvdArgs a, const int* flag) {
+	if (*flag) return;
+	extern __shared__ int s_order[];
+	__shared__ int s_rank;
+	__shared__ double s_sign[1024];
+	const double* Uh = UV;
+	const double* Vh = UV + (long long)q * q;
+	const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5, nwarps = blockDim.x >> 5;
+	for (int c = tid; c < q; c += blockDim.x) {
+		int pos = 0;
+		for (int o = 0; o < q; ++o) pos += (sig[o] > sig[c]) || (sig[o] == sig[c] && o < c);
+		s_order[pos] = c;
+	}
+	__syncthreads();
+	if (tid == 0) {
+		int rank = q;
+		if (a.max_rank > 0 && a.max_rank < rank) rank = a.max_rank;
+		const double s0 = sig[s_order[0]];
+		for (int j = 1; j < rank; ++j)
+			if (sig[s_order[j]] <= a.eps * s0) { rank = j; break; }
+		s_rank = rank;
+		if (a.rank_out) *a.rank_out = rank;
+	}
+	__syncthreads();
+	const int rank = s_rank;
+	for (int k = warp; k < rank; k += nwarps) {
+		const int c = s_order[k];
+		double best = -1.0, val = 0.0;
+		int bi = 1 << 30;
+		for (int i = lane; i < q; i += 32) {
+			const double u = Uh[(long long)i * q + c];
+			if (fabs(u) > best) { best = fabs(u); val = u; bi = i; }
+		}
+#pragma unroll
+		for (int o = 16; o > 0; o >>= 1) {
+			const double ob = __shfl_xor_sync(0xffffffffu, best, o);
+			const double ov = __shfl_xor_sync(0xffffffffu, val, o);
+			const int oi = __shfl_xor_sync(0xffffffffu, bi, o);
+			if (ob > best || (ob == best && oi < bi)) { best = ob; val = ov; bi = oi; }
+		}
+		if (lane == 0) s_sign[k] = val < 0.0 ? -1.0 : 1.0;
+	}
+	__syncthreads();
+	for (int k = tid; k < rank; k += blockDim.x) a.S[k] = sig[s_order[k]];
+	for (long long e = tid; e < (long long)q * rank; e += blockDim.x) {
+		const int i = int(e / rank), k = int(e % rank);
+		a.U[(long long)i * rank + k] = s_sign[k] * Uh[(long long)i * q + s_order[k]];
+	}
+	for (long long e = tid; e < (long long)rank * q; e += blockDim.x) {
+		const int k = int(e / q), j = int(e % q);
+		a.Vt[(long long)k * q + j] = s_sign[k] * Vh[(long long)j * q + s_order[k]];
+	}
+}
+
+// C = A B for q x q row-major operands (A transposed when ta), `batch` pairs at stride q^2.
+static Gemm<double> sq_gemm(int q, const double* A, bool ta, long long lda, const double* B, double* C, int batch = 1) {
+	const long long qq = (long long)q * q;
+	Gemm<double> g;
+	g.M = q; g.N = q; g.K = q; g.batch = batch;
+	g.A = A; g.sAm = ta ? 1 : lda; g.sAk = ta ? lda : 1; g.sAb = qq;
+	g.B = B; g.sBk = q; g.sBn = 1; g.sBb = qq;
+	g.C = C; g.sCm = q; g.sCn = 1; g.sCb = qq;
+	g.lens((batch - 1) * qq + (long long)(q - 1) * lda + q, batch * qq, batch * qq);
+	return g;
+}
+
+// X (q x q, leading dimension a.ldx) from W (the FP32 Jacobi's right factor, FP64):
+// kOaSteps refinement steps, then the outputs of `a`. False (nothing written) if the
+// flag was set.
+static bool svd_refine_square(Context& c, const SvdArgs& a, const double* W, int q) {
+	XTT_REQUIRE(q <= 1024, "internal: refinement sized for q <= 1024");
+	const size_t qq = size_t(q) * q;
+	double* UV = c.scratch<double>(S_SVD_RF_U, 2 * qq);    // [U | V]
+	double* UV2 = c.scratch<double>(S_SVD_RF_V, 2 * qq);   // the next [U | V]
+	double* M = c.scratch<double>(S_SVD_RF_M, 6 * qq + q);  // [P | Q], Z, T, [I + F | I + G], sigma
+	double *PQ = M, *Z = M + 2 * qq, *T = M + 3 * qq, *FG = M + 4 * qq, *sig = M + 6 * qq;
+	int* flag = c.d_ints + 6;
+	XTT_CUDA(cudaMemsetAsync(flag, 0, sizeof(int), c.stream));
+	copy_d2d(c, UV + qq, W, qq);
+	gemm(c, sq_gemm(q, a.X, false, a.ldx, UV + qq, Z));  // Y = X V
+	k_oa_normalize<<<std::max(1, q / 8), 256, 0, c.stream>>>(Z, UV, q, flag);
+	XTT_CUDA(cudaGetLastError());
+	c.count_launch();
+	for (int it = 0; it < kOaSteps; ++it) {
+		gemm(c, sq_gemm(q, UV, true, q, UV, PQ, 2));       // [U^T U | V^T V]
+		gemm(c, sq_gemm(q, a.X, false, a.ldx, UV + qq, Z));  // X V
+		gemm(c, sq_gemm(q, UV, true, q, Z, T));              // U^T X V
+		k_oa_correct<<<std::min(q, 64), 128, size_t(q) * sizeof(double), c.stream>>>(PQ, T, FG, sig, q,
+		                                                                               it == kOaSteps - 1, flag);
+		XTT_CUDA(cudaGetLastError());
+		c.count_launch();
+		gemm(c, sq_gemm(q, UV, false, q, FG, UV2, 2));  // [U (I + F) | V (I + G)]
+		std::swap(UV, UV2);
+	}
+	k_oa_finish<<<1, 256, size_t(q) * sizeof(int), c.stream>>>(UV, sig, q, a, flag);
+	XTT_CUDA(cudaGetLastError());
+	c.count_launch();
+	return c.read_int(6) == 0;
+}
+
 // One-sided Jacobi of a.X (through launch_svd). Mixed precision where it fits (svd_path
 // AUTO, columns orthogonalised, 32..: one CTA holds the matrix in FP32): FP32 sweeps to
-// FP32 orthogonality in one CTA give a rotation W32; two Newton-Schulz steps in FP64,
-// W <- 1.5 W - 0.5 W (W^T W), make it orthogonal to rounding (each squares the 1e-7
-// defect); the FP64 cluster Jacobi then starts from X W with V = W and needs only the
-// few sweeps of its quadratic phase. Same singular values, truncation and gauge.
+// FP32 orthogonality in one CTA give a rotation W32. Square X: the product refinement
+// above takes it to FP64 accuracy. Otherwise (or when the refinement flags its input):
+// two Newton-Schulz steps in FP64, W <- 1.5 W - 0.5 W (W^T W), make it orthogonal to
+// rounding (each squares the 1e-7 defect); the FP64 cluster Jacobi then starts from X W
+// with V = W and needs only the few sweeps of its quadratic phase. Same singular values,
+// truncation and gauge.
 // `mixed` false: plain FP64 Jacobi (after the QR preconditioning, whose R^T already
 // converges in 6-10 sweeps, the FP32 stage measured slower than it saves).
 static void jacobi(Context& c, SvdArgs& a, bool mixed) {
@@ -608,13 +806,22 @@ static void jacobi(Context& c, SvdArgs& a, bool mixed) {
 		Fp64ContractionScope fp64(c);
 		const size_t qq = size_t(q) * q;
 		float* w32 = c.scratch<float>(S_SVD_MX_W32, qq);
-		launch_svd_f32(a.X, a.ldx, p, q, w32, c.stream);
+		{
+			ProfScope ps(c, "svd_f32");
+			launch_svd_f32(a.X, a.ldx, p, q, w32, c.stream);
+		}
 		double* W = c.scratch<double>(S_SVD_MX_W, qq);
 		double* W2 = c.scratch<double>(S_SVD_MX_W2, qq);
 		double* G = c.scratch<double>(S_SVD_MX_G, qq);
 		k_f2d<<<unsigned(std::min<size_t>(1024, (qq + 255) / 256)), 256, 0, c.stream>>>(W, w32, qq);
 		c.count_launch(2);
 		XTT_CUDA(cudaGetLastError());
+		// square: refine the FP32 factors by products instead of Jacobi sweeps
+		if (p == q && q <= 1024) {
+			ProfScope ps(c, "svd_refine");
+			if (svd_refine_square(c, a, W, q)) return;
+		}
+		ProfScope ps(c, "svd_sweeps");
 		for (int it = 0; it < 2; ++it) {
 			Gemm<double> g1;  // G = W^T W
 			g1.M = q; g1.N = q; g1.K = q;
