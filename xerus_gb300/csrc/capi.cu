@@ -538,6 +538,7 @@ int xtt_move_core(xtt_tensor* x, int64_t position, int keep_rank) {
 		xtt::DeviceScope dev_scope(x ? x->t->ctx->device : -1);
 		ARG(x, "NULL argument");
 		xtt::ContractionPrecisionScope ps(*x->t->ctx);
+		xtt::GramQrScope gram(*x->t->ctx);
 		xtt::move_core(*x->t, position, keep_rank != 0);
 		x->t->ctx->sync();
 	});

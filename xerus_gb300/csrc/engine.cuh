@@ -41,6 +41,7 @@ struct Context {
 	// `tc_active` is set, which those three entry points do for their duration.
 	int contraction_terms = 0;
 	int tc_active = 0;
+	bool gram_qr = false;  // rank-revealing QRs by Cholesky QR where well-conditioned (GramQrScope)
 	// batched ALS: the CUDA graph of the last batch launch (replayed while its
 	// signature holds), its pinned descriptor staging, and autotuned launch shapes
 	unsigned long long batch_key = 0;
@@ -163,6 +164,15 @@ struct Fp64ContractionScope {
 	~Fp64ContractionScope() { c.tc_active = saved; }
 };
 
+// Rank-revealing QRs of its scope by Cholesky QR where well-conditioned (round and the
+// public move_core; the library's internal canonicalisations keep Householder QR).
+struct GramQrScope {
+	Context& c;
+	bool saved;
+	explicit GramQrScope(Context& cc) : c(cc), saved(cc.gram_qr) { c.gram_qr = true; }
+	~GramQrScope() { c.gram_qr = saved; }
+};
+
 // Issues the launches of its scope on the context's aux stream.
 struct OnAux {
 	Context& c;
@@ -179,10 +189,10 @@ enum ScratchId : int {
 	S_RES_CORE0B, S_RES_CORE1B, S_RES_RB, S_QR_WORKB, S_BATCH_META, S_BATCH_WORK, S_BATCH_BACKUP,
 	S_SVD_PC_Q, S_SVD_PC_C, S_SVD_PC_UV, S_SVD_PC_QRW, S_GEMM_TC_WORK, S_SVD_PC_CT, S_SVD_PC_UT,
 	S_SVD_MX_W32, S_SVD_MX_W, S_SVD_MX_W2, S_SVD_MX_G, S_SVD_MX_B0, S_TMA_A, S_TMA_B, S_SVD_RF_U, S_SVD_RF_V,
-	S_SVD_RF_M,
-	S_ALS_FIRST = 48,
-	S_ADF_FIRST = 112,
-	S_MAX = 176
+	S_SVD_RF_M, S_GQ_FIRST,  // 2 x kGqSlots ids from here: the Gram QR's buffers for two concurrent factorisations
+	S_ALS_FIRST = 64,
+	S_ADF_FIRST = 128,
+	S_MAX = 192
 };
 
 struct Tensor {

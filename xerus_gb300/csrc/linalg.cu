@@ -2456,23 +2456,144 @@ void svd_pc_finish(const SvdArgs& a, const SvdPcWork& w, int kk, cudaStream_t s)
 
 // ------------------------------------------------------------ FP32 Jacobi stage
 
-constexpr int kSvf32Threads = 1024;
-
-bool svd_f32_fits(int p, int q) {
-	return q >= 2 && p >= q && (size_t(p) * q + size_t(q) * q) * sizeof(float) <= kDynSmemMax;
+// Column pairs are handled by groups of LPP lanes. Where the shapes allow (p, q <= 64:
+// 4 lanes x 16 entries; <= 128: 8 lanes x 16) each lane keeps its entries of the pair's
+// columns in registers between the dot products and the rotation, and the V columns are
+// fetched before the reductions: a step is one round of independent shared-memory
+// accesses, with fewer warps issuing it (the stage is one CTA, bound by its issue rate).
+// The columns are stored at a stride congruent to LPP mod 32, so the groups of a warp,
+// which hold consecutive columns, read disjoint banks.
+struct Svf32Shape {
+	int lpp, nr;
+};
+__host__ __device__ inline Svf32Shape svf32_shape(int p, int q) {
+	if (p <= 64 && q <= 64) return {4, 16};
+	if (p <= 128 && q <= 128) return {8, 16};
+	return {16, 0};  // entries in loops
+}
+__host__ __device__ inline int svf32_ld(int rows, int lpp) { return rows + ((lpp - rows % 32) % 32 + 32) % 32; }
+__host__ inline int svf32_threads(int q, int lpp) {
+	const int pairs = (q + (q & 1)) / 2, per_warp = 32 / lpp;
+	return std::min(1024, 32 * std::max(2, (pairs + per_warp - 1) / per_warp));
+}
+static size_t svf32_smem(int p, int q) {
+	const Svf32Shape sh = svf32_shape(p, q);
+	return (size_t(svf32_ld(p, sh.lpp)) * q + size_t(svf32_ld(q, sh.lpp)) * q) * sizeof(float);
 }
 
-// One CTA: B (p x q, column-major) and V (q x q, column-major) in FP32 shared memory;
-// round-robin one-sided Jacobi, one half-warp per pair, until a sweep's largest |cos|
-// between paired columns is below 3e-3 (or max_sweeps); W = V written row-major. The
-// input is scaled by the power of two that brings its largest entry to [0.5, 1), so
-// squares and sums stay in FP32 range. Its purpose is a start for the FP64 stage (the
-// product refinement, or Jacobi sweeps that started from X W converge in a few).
-__global__ void __launch_bounds__(kSvf32Threads) k_svd_f32(const double* __restrict__ X, long long ldx, int p, int q,
-                                                          float* __restrict__ W, int max_sweeps) {
+bool svd_f32_fits(int p, int q) { return q >= 2 && p >= q && svf32_smem(p, q) <= kDynSmemMax; }
+
+template <int LPP, int NR>
+__device__ void svd_f32_sweeps(float* B, int ldb, float* V, int ldv, int p, int q, float negl, float tol2, float big2,
+                               int max_sweeps, int& s_rot) {
+	constexpr int kGroups = 32 / LPP;
+	const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5, nwarps = blockDim.x >> 5;
+	const int qe = q + (q & 1), grp = lane / LPP, gl = lane % LPP;
+	for (int sweep = 0; sweep < max_sweeps; ++sweep) {
+		if (tid == 0) s_rot = 0;
+		__syncthreads();
+		for (int t = 0; t < qe - 1; ++t) {
+			// every lane of a warp takes part in its shuffles
+			for (int lp0 = kGroups * warp; lp0 < qe / 2; lp0 += kGroups * nwarps) {
+				const int lp = lp0 + grp;
+				int i = 0, j = 0;
+				bool ok = lp < qe / 2;
+				if (ok) {
+					// svc_col without the division: (k - 1 + t) mod (qe - 1) for k, t < qe - 1
+					const int m = qe - 1, a = lp - 1 + t, b = qe - 2 - lp + t;
+					i = lp == 0 ? 0 : (a >= m ? a - m : a) + 1;
+					j = (b >= m ? b - m : b) + 1;
+					ok = i < q && j < q;
+				}
+				float* bi = B + i * ldb;
+				float* bj = B + j * ldb;
+				float* vi = V + i * ldv;
+				float* vj = V + j * ldv;
+				float al = 0.f, be = 0.f, ga = 0.f;
+				float x[NR > 0 ? NR : 1], y[NR > 0 ? NR : 1], vx[NR > 0 ? NR : 1], vy[NR > 0 ? NR : 1];
+				if constexpr (NR > 0) {
+#pragma unroll
+					for (int u = 0; u < NR; ++u) {
+						const int r = gl + LPP * u;
+						x[u] = ok && r < p ? bi[r] : 0.f;
+						y[u] = ok && r < p ? bj[r] : 0.f;
+						vx[u] = ok && r < q ? vi[r] : 0.f;
+						vy[u] = ok && r < q ? vj[r] : 0.f;
+					}
+#pragma unroll
+					for (int u = 0; u < NR; ++u) {
+						al = fmaf(x[u], x[u], al);
+						be = fmaf(y[u], y[u], be);
+						ga = fmaf(x[u], y[u], ga);
+					}
+				} else if (ok) {
+					for (int r = gl; r < p; r += LPP) {
+						const float a = bi[r], b = bj[r];
+						al = fmaf(a, a, al);
+						be = fmaf(b, b, be);
+						ga = fmaf(a, b, ga);
+					}
+				}
+#pragma unroll
+				for (int o = LPP / 2; o > 0; o >>= 1) {
+					al += __shfl_xor_sync(0xffffffffu, al, o);
+					be += __shfl_xor_sync(0xffffffffu, be, o);
+					ga += __shfl_xor_sync(0xffffffffu, ga, o);
+				}
+				const float ab = al * be, g2s = ga * ga;
+				if (ok && ga != 0.f && fminf(al, be) > negl && g2s > tol2 * ab) {
+					const float dba = be - al, g2 = 2.f * ga;
+					float tt = __fdividef(fabsf(g2), fabsf(dba) + sqrtf(fmaf(dba, dba, g2 * g2)));
+					if ((dba < 0.f) != (ga < 0.f)) tt = -tt;
+					const float cs = rsqrtf(fmaf(tt, tt, 1.f)), sn = cs * tt;
+					if constexpr (NR > 0) {
+#pragma unroll
+						for (int u = 0; u < NR; ++u) {
+							const int r = gl + LPP * u;
+							if (r < p) {
+								bi[r] = cs * x[u] - sn * y[u];
+								bj[r] = sn * x[u] + cs * y[u];
+							}
+							if (r < q) {
+								vi[r] = cs * vx[u] - sn * vy[u];
+								vj[r] = sn * vx[u] + cs * vy[u];
+							}
+						}
+					} else {
+						for (int r = gl; r < p; r += LPP) {
+							const float a = bi[r], b = bj[r];
+							bi[r] = cs * a - sn * b;
+							bj[r] = sn * a + cs * b;
+						}
+						for (int r = gl; r < q; r += LPP) {
+							const float a = vi[r], b = vj[r];
+							vi[r] = cs * a - sn * b;
+							vj[r] = sn * a + cs * b;
+						}
+					}
+					if (gl == 0 && g2s > big2 * ab) s_rot = 1;
+				}
+			}
+			__syncthreads();
+		}
+		if (s_rot == 0) break;  // uniform: read after the last step's barrier
+		__syncthreads();         // everyone has read s_rot before it is reset
+	}
+}
+
+// One CTA: B (p x q, column-major, stride ldb) and V (q x q, column-major, stride ldv) in
+// FP32 shared memory; round-robin one-sided Jacobi until a sweep's largest |cos| between
+// paired columns is below 3e-3 (or max_sweeps); W = V written row-major. The input is
+// scaled by the power of two that brings its largest entry to [0.5, 1), so squares and
+// sums stay in FP32 range. Its purpose is a start for the FP64 stage (the product
+// refinement, or Jacobi sweeps that started from X W converge in a few).
+template <int LPP, int NR>
+__global__ void __launch_bounds__(NR > 0 ? 512 : 1024) k_svd_f32(const double* __restrict__ X, long long ldx, int p,
+                                                                 int q, float* __restrict__ W, int max_sweeps) {
 	extern __shared__ float fsm[];
+	const int ldb = svf32_ld(p, LPP), ldv = svf32_ld(q, LPP);
 	float* B = fsm;
-	float* V = fsm + (size_t)p * q;
+	float* V = fsm + (size_t)ldb * q;
 	__shared__ double d_red[32];
 	__shared__ float f_red[32];
 	__shared__ int s_rot;
@@ -2499,15 +2620,18 @@ __global__ void __launch_bounds__(kSvf32Threads) k_svd_f32(const double* __restr
 	}
 	const long long ex = (__double_as_longlong(d_red[0]) >> 52) & 0x7ff;
 	const double scale = ex > 0 ? __longlong_as_double((2045 - ex) << 52) : 1.0;  // 2^(1022 - ex)
+	float fl = 0.f;
 	for (long long e = tid; e < (long long)p * q; e += blockDim.x) {
 		const int i = int(e / q), c = int(e % q);
-		B[(size_t)c * p + i] = float(X[(long long)i * ldx + c] * scale);
+		const float v = float(X[(long long)i * ldx + c] * scale);
+		B[(size_t)c * ldb + i] = v;
+		fl = fmaf(v, v, fl);
 	}
-	for (long long e = tid; e < (long long)q * q; e += blockDim.x) V[e] = (e / q == e % q) ? 1.f : 0.f;
-	__syncthreads();
-	float fl = 0.f;
-	for (long long e = tid; e < (long long)p * q; e += blockDim.x) fl = fmaf(B[e], B[e], fl);
-	const float fro = block_sum(fl, f_red);
+	for (long long e = tid; e < (long long)q * q; e += blockDim.x) {
+		const int c = int(e / q), i = int(e % q);
+		V[(size_t)c * ldv + i] = c == i ? 1.f : 0.f;
+	}
+	const float fro = block_sum(fl, f_red);  // its barriers also publish B and V
 	const float negl = fro * 1e-12f;
 	// a start for the FP64 stage, not an SVD: FP32-level orthogonality, at most 12
 	// sweeps (near FP32 rounding the sweeps would go on rotating noise)
@@ -2515,76 +2639,25 @@ __global__ void __launch_bounds__(kSvf32Threads) k_svd_f32(const double* __restr
 	// a sweep whose largest |cos| between paired columns is below 3e-3 leaves them at
 	// FP32 rounding (the sweeps converge quadratically); the next would rotate noise
 	const float big2 = 9e-6f;
-	const int qe = q + (q & 1), half = lane >> 4, hl = lane & 15;
-	for (int sweep = 0; sweep < max_sweeps; ++sweep) {
-		if (tid == 0) s_rot = 0;
-		__syncthreads();
-		for (int t = 0; t < qe - 1; ++t) {
-			// one half-warp per pair: every lane of a warp takes part in its shuffles
-			for (int lp0 = 2 * warp; lp0 < qe / 2; lp0 += 2 * nwarps) {
-				const int lp = lp0 + half;
-				int i = 0, j = 0;
-				bool ok = lp < qe / 2;
-				if (ok) {
-					i = svc_col(lp, t, qe);
-					j = svc_col(qe - 1 - lp, t, qe);
-					ok = i < q && j < q;
-				}
-				float* bi = B + (size_t)i * p;
-				float* bj = B + (size_t)j * p;
-				float al = 0.f, be = 0.f, ga = 0.f;
-				if (ok)
-					for (int r = hl; r < p; r += 16) {
-						const float x = bi[r], y = bj[r];
-						al = fmaf(x, x, al);
-						be = fmaf(y, y, be);
-						ga = fmaf(x, y, ga);
-					}
-#pragma unroll
-				for (int o = 8; o > 0; o >>= 1) {
-					al += __shfl_xor_sync(0xffffffffu, al, o);
-					be += __shfl_xor_sync(0xffffffffu, be, o);
-					ga += __shfl_xor_sync(0xffffffffu, ga, o);
-				}
-				const float ab = al * be, g2s = ga * ga;
-				if (ok && ga != 0.f && fminf(al, be) > negl && g2s > tol2 * ab) {
-					const float dba = be - al, g2 = 2.f * ga;
-					float tt = __fdividef(fabsf(g2), fabsf(dba) + sqrtf(fmaf(dba, dba, g2 * g2)));
-					if ((dba < 0.f) != (ga < 0.f)) tt = -tt;
-					const float cs = rsqrtf(fmaf(tt, tt, 1.f)), sn = cs * tt;
-					for (int r = hl; r < p; r += 16) {
-						const float x = bi[r], y = bj[r];
-						bi[r] = cs * x - sn * y;
-						bj[r] = sn * x + cs * y;
-					}
-					float* vi = V + (size_t)i * q;
-					float* vj = V + (size_t)j * q;
-					for (int r = hl; r < q; r += 16) {
-						const float x = vi[r], y = vj[r];
-						vi[r] = cs * x - sn * y;
-						vj[r] = sn * x + cs * y;
-					}
-					if (hl == 0 && g2s > big2 * ab) s_rot = 1;
-				}
-			}
-			__syncthreads();
-		}
-		if (s_rot == 0) break;  // uniform: read after the last step's barrier
-		__syncthreads();         // everyone has read s_rot before it is reset
-	}
+	svd_f32_sweeps<LPP, NR>(B, ldb, V, ldv, p, q, negl, tol2, big2, max_sweeps, s_rot);
 	for (long long e = tid; e < (long long)q * q; e += blockDim.x) {
 		const int i = int(e / q), c = int(e % q);
-		W[e] = V[(size_t)c * q + i];
+		W[e] = V[(size_t)c * ldv + i];
 	}
+}
+
+template <int LPP, int NR>
+static void launch_svd_f32_as(const double* X, long long ldx, int p, int q, float* W, cudaStream_t s) {
+	func_attr_once(k_svd_f32<LPP, NR>, cudaFuncAttributeMaxDynamicSharedMemorySize, int(kDynSmemMax));
+	k_svd_f32<LPP, NR><<<1, svf32_threads(q, LPP), svf32_smem(p, q), s>>>(X, ldx, p, q, W, 12);
 }
 
 void launch_svd_f32(const double* X, long long ldx, int p, int q, float* W, cudaStream_t s) {
 	XTT_REQUIRE(svd_f32_fits(p, q), "internal: FP32 Jacobi stage does not fit one CTA");
-	func_attr_once(k_svd_f32, cudaFuncAttributeMaxDynamicSharedMemorySize, int(kDynSmemMax));
-	const size_t smem = (size_t(p) * q + size_t(q) * q) * sizeof(float);
-	// one half-warp per column pair
-	const int qe = q + (q & 1), threads = std::min(kSvf32Threads, std::max(64, 32 * ((qe / 2 + 1) / 2)));
-	k_svd_f32<<<1, threads, smem, s>>>(X, ldx, p, q, W, 12);
+	const Svf32Shape sh = svf32_shape(p, q);
+	if (sh.lpp == 4) launch_svd_f32_as<4, 16>(X, ldx, p, q, W, s);
+	else if (sh.lpp == 8) launch_svd_f32_as<8, 16>(X, ldx, p, q, W, s);
+	else launch_svd_f32_as<16, 0>(X, ldx, p, q, W, s);
 	XTT_CUDA(cudaGetLastError());
 }
 

@@ -482,6 +482,185 @@ bool exceeds_maximal_ranks(const Tensor& x) {
 	return reduce_to_maximal_ranks(inner, nn) != inner;
 }
 
+// ------------------------------------------------------------ Cholesky QR of well-conditioned cores
+// The rank-revealing factorisations of round (its left-orthogonalisation and the two per
+// bond) by Cholesky QR with Newton-Schulz re-orthogonalisation, all FP64 products but one
+// FP32 Cholesky of a Gram matrix: for the tall A_w (m_w x n_w; A or A^T),
+//   G = A_w^T A_w;  R_32 = chol(G) in FP32, Q_1 = A_w R_32^{-1};
+//   three steps Q <- Q (3 I - Q^T Q) / 2 (each squares the orthogonality defect);
+//   C = Q^T A_w, so A_w = Q C with Q orthonormal to rounding.
+// Householder QR on GB300 is a chain of ~n_w dependent column steps whose FP64 latencies
+// (a reduction, a square root and a division each) and cluster barriers no parallelism
+// hides; here the chain is the FP32 Cholesky only. The factorisation is accepted when
+// every Cholesky pivot keeps 1e-6 of its column's squared norm (kappa(A) below ~1e3,
+// far from the reference's rank rule |R_kk| < 16 eps R_00, which therefore keeps all
+// n_w columns: rank_out = n_w) and the last step's defect max|Q^T Q - I| is below 1e-7
+// (so Q is orthonormal to ~1e-14); otherwise a flag is set and the caller runs the
+// pivoted Householder QR. Q and C differ from Householder's by an orthogonal n_w x n_w
+// factor (Q C is the same): round uses them only through Q C-invariant products.
+constexpr int kGqSlots = 5;  // scratch ids per concurrent factorisation
+constexpr int kGqMaxCols = 128;
+constexpr int kGqNsSteps = 3;
+
+// FP32 Cholesky G = R^T R (G scaled to unit largest diagonal) with R^{-1} built alongside:
+// the symmetric elimination E G E^T = D (E unit lower triangular, its rows updated with
+// the same multipliers as G's) gives R = D^{1/2} E^{-T}, so R^{-1} = E^T D^{-1/2}; written
+// (FP64, scaled back) to Rinv (n x n row-major, zero below the diagonal). One CTA of
+// kGqRows x 32 threads (rows x columns), two barriers per pivot.
+constexpr int kGqRows = 16;
+__global__ void __launch_bounds__(kGqRows * 32) k_gq_chol32(const double* __restrict__ G, int n, double* __restrict__ Rinv,
+                                                   int* flag) {
+	extern __shared__ float gq_s[];
+	const int ld = n + 1, tid = threadIdx.x, tx = tid & 31, ty = tid >> 5;
+	float* S = gq_s;            // n x ld: G, eliminated in its upper triangle
+	float* E = gq_s + n * ld;   // n x ld: the elimination, unit lower triangular
+	__shared__ float s_rs[kGqMaxCols], s_d0[kGqMaxCols], s_inv;
+	__shared__ double s_scale;
+	__shared__ int s_bad;
+	if (tid == 0) {
+		double mx = 0;
+		for (int i = 0; i < n; ++i) mx = fmax(mx, G[(long long)i * n + i]);
+		s_scale = mx > 0 ? 1.0 / mx : 0.0;
+		s_bad = !(mx > 0);
+	}
+	__syncthreads();
+	const double sc = s_scale;
+	for (int e = tid; e < n * n; e += blockDim.x) {
+		const int i = e / n, j = e % n;
+		S[i * ld + j] = float(G[e] * sc);
+		E[i * ld + j] = i == j ? 1.f : 0.f;
+		if (i == j) s_d0[i] = float(G[e] * sc);
+	}
+	__syncthreads();
+	for (int k = 0; k < n; ++k) {
+		if (tid == 0) {
+			float d = S[k * ld + k];
+			if (!(d > 1e-6f * s_d0[k])) {
+				s_bad = 1;
+				d = 1.f;
+			}
+			s_rs[k] = rsqrtf(d);
+			s_inv = 1.f / d;
+		}
+		__syncthreads();
+		const float inv = s_inv;
+		// row k of S and E in registers (column tx + 32 u), then independent row updates
+		float sk[kGqMaxCols / 32], ek[kGqMaxCols / 32];
+#pragma unroll
+		for (int u = 0; u < kGqMaxCols / 32; ++u) {
+			const int j = tx + 32 * u;
+			sk[u] = j < n ? S[k * ld + j] : 0.f;
+			ek[u] = j <= k ? E[k * ld + j] : 0.f;
+		}
+		for (int i = k + 1 + ty; i < n; i += kGqRows) {
+			const float l = S[k * ld + i] * inv;
+#pragma unroll
+			for (int u = 0; u < kGqMaxCols / 32; ++u) {
+				const int j = tx + 32 * u;
+				if (j >= i && j < n) S[i * ld + j] = fmaf(-l, sk[u], S[i * ld + j]);
+				if (j <= k) E[i * ld + j] = fmaf(-l, ek[u], E[i * ld + j]);
+			}
+		}
+		__syncthreads();
+	}
+	const double back = sqrt(sc);
+	for (int e = tid; e < n * n; e += blockDim.x) {
+		const int a = e / n, b = e % n;
+		Rinv[e] = b >= a ? double(E[b * ld + a] * s_rs[b]) * back : 0.0;
+	}
+	if (tid == 0 && s_bad) atomicExch(flag, 1);
+}
+
+// H = (3 I - G) / 2 for the Newton-Schulz step; on the last step the defect gate and
+// the rank. One thread per entry.
+__global__ void k_gq_ns(const double* __restrict__ G, double* __restrict__ H, int n, int last, int* flag, int* rank_out) {
+	int bad = 0;
+	for (int e = blockIdx.x * blockDim.x + threadIdx.x; e < n * n; e += gridDim.x * blockDim.x) {
+		const int i = e / n, j = e % n;
+		const double dev = G[e] - (i == j ? 1.0 : 0.0);
+		if (!(fabs(dev) < 1e-7)) bad = 1;
+		H[e] = (i == j ? 1.0 : 0.0) - 0.5 * dev;
+	}
+	if (last) {
+		if (bad) atomicExch(flag, 1);
+		if (blockIdx.x == 0 && threadIdx.x == 0 && rank_out) *rank_out = n;
+	}
+}
+
+static Gemm<double> gq_gemm(int M, int N, int K, const double* A, long long sAm, long long sAk, long long lenA,
+                            const double* B, long long sBk, long long sBn, long long lenB, double* C, long long sCm,
+                            long long sCn, long long lenC) {
+	Gemm<double> g;
+	g.M = M; g.N = N; g.K = K;
+	g.A = A; g.sAm = sAm; g.sAk = sAk;
+	g.B = B; g.sBk = sBk; g.sBn = sBn;
+	g.C = C; g.sCm = sCm; g.sCn = sCn;
+	g.lens(lenA, lenB, lenC);
+	return g;
+}
+
+static bool gram_qr_fits(const QrArgs& a) {
+	const int mw = a.transpose ? a.n : a.m, nw = a.transpose ? a.m : a.n;
+	return a.pivot && a.want_q && nw >= 16 && nw <= kGqMaxCols && mw >= nw;
+}
+
+// Enqueues the Cholesky QR of `a` (gram_qr_fits) on the context's stream with the scratch
+// of `slot` (0 or 1); `flag` (a device int, cleared here) is set where the caller must
+// run the Householder QR instead. Writes a.Q, a.C and *a.rank_out in a.'s layouts.
+static void gram_qr(Context& c, const QrArgs& a, int slot, int* flag) {
+	Fp64ContractionScope fp64(c);
+	const bool tr = a.transpose != 0;
+	const int mw = tr ? a.n : a.m, nw = tr ? a.m : a.n;
+	const long long sr = tr ? 1 : a.lda, sc = tr ? a.lda : 1;  // A_w[i][j] = A[i sr + j sc]
+	const long long lenA = (long long)(a.m - 1) * a.lda + a.n, nn = (long long)nw * nw, mn = (long long)mw * nw;
+	const int id = S_GQ_FIRST + slot * kGqSlots;
+	double* G = c.scratch<double>(id + 0, nn);
+	double* Ri = c.scratch<double>(id + 1, nn);
+	double* H = c.scratch<double>(id + 2, nn);
+	double* Qa = c.scratch<double>(id + 3, mn);
+	double* Qb = c.scratch<double>(id + 4, mn);
+	XTT_CUDA(cudaMemsetAsync(flag, 0, sizeof(int), c.stream));
+	gemm(c, gq_gemm(nw, nw, mw, a.A, sc, sr, lenA, a.A, sr, sc, lenA, G, nw, 1, nn));  // A_w^T A_w
+	const size_t smem = 2 * size_t(nw) * (nw + 1) * sizeof(float);
+	func_attr_once(k_gq_chol32, cudaFuncAttributeMaxDynamicSharedMemorySize,
+	               int(2 * kGqMaxCols * (kGqMaxCols + 1) * sizeof(float)));
+	k_gq_chol32<<<1, kGqRows * 32, smem, c.stream>>>(G, nw, Ri, flag);
+	XTT_CUDA(cudaGetLastError());
+	c.count_launch();
+	gemm(c, gq_gemm(mw, nw, nw, a.A, sr, sc, lenA, Ri, nw, 1, nn, Qa, nw, 1, mn));  // Q_1 = A_w R^{-1}
+	// the output layouts: tr == 0: Q (m x n_w) ld n_w, C (n_w x n) ld n; tr == 1: Q (n_w x n)
+	// ld n (= Q_w^T), C (m x n_w) ld n_w (= C_w^T)
+	const long long qm = tr ? 1 : nw, qn = tr ? mw : 1;
+	for (int it = 0; it < kGqNsSteps; ++it) {
+		const bool last = it + 1 == kGqNsSteps;
+		gemm(c, gq_gemm(nw, nw, mw, Qa, 1, nw, mn, Qa, nw, 1, mn, G, nw, 1, nn));  // Q^T Q
+		k_gq_ns<<<(unsigned(nn) + 255) / 256, 256, 0, c.stream>>>(G, H, nw, last, flag, a.rank_out);
+		XTT_CUDA(cudaGetLastError());
+		c.count_launch();
+		if (last) gemm(c, gq_gemm(mw, nw, nw, Qa, nw, 1, mn, H, nw, 1, nn, a.Q, qm, qn, mn));
+		else gemm(c, gq_gemm(mw, nw, nw, Qa, nw, 1, mn, H, nw, 1, nn, Qb, nw, 1, mn));
+		std::swap(Qa, Qb);
+	}
+	// C_w = Q_w^T A_w, Q_w read back from a.Q
+	gemm(c, gq_gemm(nw, nw, mw, a.Q, tr ? mw : 1, tr ? 1 : nw, mn, a.A, sr, sc, lenA, a.C, tr ? 1 : nw, tr ? nw : 1,
+	                nn));
+}
+
+// The rank-revealing QR of transfer_core / round: Cholesky QR where the context asks for
+// it and the shape fits, the pivoted Householder QR otherwise or when its gate fails.
+// Leaves the rank in *a.rank_out (not synchronised).
+static void rank_revealing_qr(Context& c, QrArgs& a) {
+	if (c.gram_qr && gram_qr_fits(a)) {
+		ProfScope ps(c, "qr_gram", qr_work_bytes(a), qr_work_flops(a));
+		int* flag = c.d_ints + 12;
+		gram_qr(c, a, 0, flag);
+		if (c.read_int(12) == 0) return;
+	}
+	ProfScope ps(c, "qr", qr_work_bytes(a), qr_work_flops(a));
+	launch_qr(a, c.stream);
+	c.count_launch();
+}
+
 void transfer_core(Tensor& x, int from, int to, bool rr) {
 	Context& c = *x.ctx;
 	const int64_t r0 = x.ranks[from], nf = x.n(from), r1 = x.ranks[from + 1];
@@ -514,11 +693,7 @@ void transfer_core(Tensor& x, int from, int to, bool rr) {
 		a.A = x.core[from]; a.lda = n; a.m = m; a.n = n; a.transpose = 0; a.pivot = rr ? 1 : 0;
 		a.work = wk ? c.scratch<double>(S_QR_WORK, wk) : nullptr;
 		a.Q = Q; a.C = C; a.rank_out = c.d_ints;
-		{
-			ProfScope ps(c, "qr", qr_work_bytes(a), qr_work_flops(a));
-			launch_qr(a, c.stream);
-		}
-		c.count_launch();
+		rank_revealing_qr(c, a);
 		const int rank = rr ? c.read_int(0) : kq;
 		const int64_t nt = x.n(to), r2 = x.ranks[to + 1];
 		// new right neighbour: C (rank x r1) * core_to (r1 x nt*r2)
@@ -543,11 +718,7 @@ void transfer_core(Tensor& x, int from, int to, bool rr) {
 		a.A = x.core[from]; a.lda = n; a.m = m; a.n = n; a.transpose = 1; a.pivot = rr ? 1 : 0;
 		a.work = wk ? c.scratch<double>(S_QR_WORK, wk) : nullptr;
 		a.Q = Q; a.C = C; a.rank_out = c.d_ints;
-		{
-			ProfScope ps(c, "qr", qr_work_bytes(a), qr_work_flops(a));
-			launch_qr(a, c.stream);
-		}
-		c.count_launch();
+		rank_revealing_qr(c, a);
 		const int rank = rr ? c.read_int(0) : kq;
 		const int64_t rt = x.ranks[to], nt = x.n(to);
 		// new left neighbour: core_to (rt*nt x r0) * C (r0 x rank)
@@ -936,17 +1107,38 @@ static void round_edge(Tensor& x, int from, int to, int64_t max_rank, double eps
 		b.A = x.core[to]; b.lda = nTc; b.m = mT; b.n = nTc; b.transpose = 0; b.pivot = 1;
 		b.work = wk ? c.scratch<double>(S_ROUND_X, wk) : nullptr;  // not S_QR_WORK: runs beside a
 		b.Q = QT; b.C = CB; b.rank_out = c.d_ints + 3;
+		const bool gb = c.gram_qr && gram_qr_fits(b), ga = c.gram_qr && gram_qr_fits(a);
 		{
 			OnAux aux(c);
-			ProfScope ps(c, "qr", qr_work_bytes(b), qr_work_flops(b));
-			launch_qr(b, c.stream);
+			if (gb) {
+				ProfScope ps(c, "qr_gram", qr_work_bytes(b), qr_work_flops(b));
+				gram_qr(c, b, 1, c.d_ints + 13);
+			} else {
+				ProfScope ps(c, "qr", qr_work_bytes(b), qr_work_flops(b));
+				launch_qr(b, c.stream);
+				c.count_launch();
+			}
 		}
-		{
+		if (ga) {
+			ProfScope ps(c, "qr_gram", qr_work_bytes(a), qr_work_flops(a));
+			gram_qr(c, a, 0, c.d_ints + 12);
+		} else {
 			ProfScope ps(c, "qr", qr_work_bytes(a), qr_work_flops(a));
 			launch_qr(a, c.stream);
+			c.count_launch();
 		}
-		c.count_launch(2);
 		c.join();
+		// a Cholesky QR whose gate failed: the pivoted Householder QR instead
+		if (ga && c.read_int(12)) {
+			ProfScope ps(c, "qr", qr_work_bytes(a), qr_work_flops(a));
+			launch_qr(a, c.stream);
+			c.count_launch();
+		}
+		if (gb && c.read_int(13)) {
+			ProfScope ps(c, "qr", qr_work_bytes(b), qr_work_flops(b));
+			launch_qr(b, c.stream);
+			c.count_launch();
+		}
 		const int ka = c.read_int(2), kb = c.read_int(3);
 		double* X = c.scratch<double>(S_GEMM_B, size_t(ka) * kb);
 		Gemm<double> g;
@@ -1014,6 +1206,7 @@ void round_tt(Tensor& x, const std::vector<int64_t>& max_ranks, double eps, std:
 	const bool init_canon = x.canonicalized;
 	const int64_t init_pos = x.core_position;
 	const int d = x.d;
+	GramQrScope gram(*x.ctx);
 	move_core(x, d - 1, false);
 	for (int i = 0; i + 1 < d; ++i) round_edge(x, d - 1 - i, d - 2 - i, max_ranks[d - 2 - i], eps, spectra);
 	x.canonicalized = true;
