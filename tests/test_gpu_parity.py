@@ -131,6 +131,27 @@ def test_move_core_qr_and_rank_revealing(ctx, golden):
         assert all(a <= b for a, b in zip(y.ranks(), zz.ranks))
 
 
+def test_move_core_cholesky_qr_cfg2(ctx, golden):
+    """Rank-revealing move_core of the d=32, n=4, rank-64 tensor (its 256 x 64 cores take
+    the Cholesky QR): ranks kept, entries and norm against the reference, cores
+    orthonormal to rounding, in both directions."""
+    z = golden("dot")
+    xg.seed(0xBAADF00D)
+    x = xg.TTTensor.random([4] * 32, 64, 0.0, 0.125, ctx=ctx)
+    for p in (31, 0, 17):
+        x.move_core(p, False)
+        assert x.corePosition == p and [1] + x.ranks() + [1] == list(z["cfg2_ranks_x"])
+        assert rel_err(x.entries(z["cfg2_x_probe_pos"]), z["cfg2_x_probe_val"]) < REL_TOL
+        assert abs(np.linalg.norm(x.get_component(p)) / z["cfg2_norm_x"][0] - 1) < REL_TOL
+        cores = x.get_cores()
+        for k in range(p):
+            m = cores[k].reshape(-1, cores[k].shape[2])
+            assert np.allclose(m.T @ m, np.eye(m.shape[1]), atol=1e-12)
+        for k in range(p + 1, len(cores)):
+            m = cores[k].reshape(cores[k].shape[0], -1)
+            assert np.allclose(m @ m.T, np.eye(m.shape[0]), atol=1e-12)
+
+
 def test_round_cfg2(ctx, golden):
     r = golden("round")
     xg.seed(0xBAADF00D)

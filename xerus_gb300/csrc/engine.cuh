@@ -75,6 +75,7 @@ struct Context {
 	void join();
 	void check_status();              // reads d_status (after a sync) and throws on failure
 	int read_int(int idx);            // sync + d_ints[idx]
+	void read_ints(int lo, int hi);   // sync + d_ints[lo, hi) into h_ints
 	void count_launch(int n = 1) { launches += n; }
 
 	// Optional per-kernel-class timing: CUDA events recorded on the context's

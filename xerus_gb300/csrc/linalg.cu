@@ -2456,34 +2456,42 @@ void svd_pc_finish(const SvdArgs& a, const SvdPcWork& w, int kk, cudaStream_t s)
 
 // ------------------------------------------------------------ FP32 Jacobi stage
 
-// Column pairs are handled by groups of LPP lanes. Where the shapes allow (p, q <= 64:
-// 4 lanes x 16 entries; <= 128: 8 lanes x 16) each lane keeps its entries of the pair's
+// Column pairs are handled by groups of LPP lanes. Where the shapes allow (64 x 64: 8 lanes
+// x 8 entries; p, q <= 64: 4 x 16; <= 128: 8 x 16) each lane keeps its entries of the pair's
 // columns in registers between the dot products and the rotation, and the V columns are
 // fetched before the reductions: a step is one round of independent shared-memory
 // accesses, with fewer warps issuing it (the stage is one CTA, bound by its issue rate).
-// The columns are stored at a stride congruent to LPP mod 32, so the groups of a warp,
-// which hold consecutive columns, read disjoint banks.
+// The columns are stored at a stride congruent to LPP mod 32 (a multiple of 4), so the
+// groups of a warp, which hold consecutive columns, read disjoint banks; for the full
+// shapes (p = q = LPP NR) each lane's entries are contiguous and move as float4.
 struct Svf32Shape {
 	int lpp, nr;
 };
 __host__ __device__ inline Svf32Shape svf32_shape(int p, int q) {
+	if (p == 64 && q == 64) return {8, 8};  // full: 2 warps per SM sub-partition (measured best of 4/8/16 lanes)
 	if (p <= 64 && q <= 64) return {4, 16};
 	if (p <= 128 && q <= 128) return {8, 16};
 	return {16, 0};  // entries in loops
 }
-__host__ __device__ inline int svf32_ld(int rows, int lpp) { return rows + ((lpp - rows % 32) % 32 + 32) % 32; }
+// column stride: congruent to `mod` mod 32 (the full 64 x 64 shape: 16, so the two groups
+// of a quarter-warp, on consecutive columns, take the two halves of the banks)
+__host__ __device__ inline int svf32_ldmod(int p, int q) {
+	return p == 64 && q == 64 ? 16 : svf32_shape(p, q).lpp;
+}
+__host__ __device__ inline int svf32_ld(int rows, int mod) { return rows + ((mod - rows % 32) % 32 + 32) % 32; }
 __host__ inline int svf32_threads(int q, int lpp) {
+	// at least 8 warps for the staging loops (the sweeps use the pairs' warps only)
 	const int pairs = (q + (q & 1)) / 2, per_warp = 32 / lpp;
-	return std::min(1024, 32 * std::max(2, (pairs + per_warp - 1) / per_warp));
+	return std::min(1024, 32 * std::max(8, (pairs + per_warp - 1) / per_warp));
 }
 static size_t svf32_smem(int p, int q) {
-	const Svf32Shape sh = svf32_shape(p, q);
-	return (size_t(svf32_ld(p, sh.lpp)) * q + size_t(svf32_ld(q, sh.lpp)) * q) * sizeof(float);
+	const int mod = svf32_ldmod(p, q);
+	return (size_t(svf32_ld(p, mod)) * q + size_t(svf32_ld(q, mod)) * q) * sizeof(float);
 }
 
 bool svd_f32_fits(int p, int q) { return q >= 2 && p >= q && svf32_smem(p, q) <= kDynSmemMax; }
 
-template <int LPP, int NR>
+template <int LPP, int NR, bool FULL>
 __device__ void svd_f32_sweeps(float* B, int ldb, float* V, int ldv, int p, int q, float negl, float tol2, float big2,
                                int max_sweeps, int& s_rot) {
 	constexpr int kGroups = 32 / LPP;
@@ -2511,7 +2519,33 @@ __device__ void svd_f32_sweeps(float* B, int ldb, float* V, int ldv, int p, int 
 				float* vj = V + j * ldv;
 				float al = 0.f, be = 0.f, ga = 0.f;
 				float x[NR > 0 ? NR : 1], y[NR > 0 ? NR : 1], vx[NR > 0 ? NR : 1], vy[NR > 0 ? NR : 1];
-				if constexpr (NR > 0) {
+				if constexpr (FULL) {
+					// lane gl holds the float4 chunks gl, gl + LPP, ...: 16-byte accesses, a group's
+					// lanes on consecutive chunks
+					if (ok) {
+#pragma unroll
+						for (int u = 0; u < NR; u += 4) {
+							const int r = 4 * (gl + LPP * (u / 4));
+							const float4 a = *reinterpret_cast<const float4*>(bi + r);
+							const float4 b = *reinterpret_cast<const float4*>(bj + r);
+							const float4 c = *reinterpret_cast<const float4*>(vi + r);
+							const float4 e = *reinterpret_cast<const float4*>(vj + r);
+							x[u] = a.x; x[u + 1] = a.y; x[u + 2] = a.z; x[u + 3] = a.w;
+							y[u] = b.x; y[u + 1] = b.y; y[u + 2] = b.z; y[u + 3] = b.w;
+							vx[u] = c.x; vx[u + 1] = c.y; vx[u + 2] = c.z; vx[u + 3] = c.w;
+							vy[u] = e.x; vy[u + 1] = e.y; vy[u + 2] = e.z; vy[u + 3] = e.w;
+						}
+					} else {
+#pragma unroll
+						for (int u = 0; u < NR; ++u) x[u] = y[u] = vx[u] = vy[u] = 0.f;
+					}
+#pragma unroll
+					for (int u = 0; u < NR; ++u) {
+						al = fmaf(x[u], x[u], al);
+						be = fmaf(y[u], y[u], be);
+						ga = fmaf(x[u], y[u], ga);
+					}
+				} else if constexpr (NR > 0) {
 #pragma unroll
 					for (int u = 0; u < NR; ++u) {
 						const int r = gl + LPP * u;
@@ -2546,7 +2580,25 @@ __device__ void svd_f32_sweeps(float* B, int ldb, float* V, int ldv, int p, int 
 					float tt = __fdividef(fabsf(g2), fabsf(dba) + sqrtf(fmaf(dba, dba, g2 * g2)));
 					if ((dba < 0.f) != (ga < 0.f)) tt = -tt;
 					const float cs = rsqrtf(fmaf(tt, tt, 1.f)), sn = cs * tt;
-					if constexpr (NR > 0) {
+					if constexpr (FULL) {
+#pragma unroll
+						for (int u = 0; u < NR; u += 4) {
+							const int r = 4 * (gl + LPP * (u / 4));
+							float4 a, b, c, e;
+							a.x = cs * x[u] - sn * y[u]; a.y = cs * x[u + 1] - sn * y[u + 1];
+							a.z = cs * x[u + 2] - sn * y[u + 2]; a.w = cs * x[u + 3] - sn * y[u + 3];
+							b.x = sn * x[u] + cs * y[u]; b.y = sn * x[u + 1] + cs * y[u + 1];
+							b.z = sn * x[u + 2] + cs * y[u + 2]; b.w = sn * x[u + 3] + cs * y[u + 3];
+							c.x = cs * vx[u] - sn * vy[u]; c.y = cs * vx[u + 1] - sn * vy[u + 1];
+							c.z = cs * vx[u + 2] - sn * vy[u + 2]; c.w = cs * vx[u + 3] - sn * vy[u + 3];
+							e.x = sn * vx[u] + cs * vy[u]; e.y = sn * vx[u + 1] + cs * vy[u + 1];
+							e.z = sn * vx[u + 2] + cs * vy[u + 2]; e.w = sn * vx[u + 3] + cs * vy[u + 3];
+							*reinterpret_cast<float4*>(bi + r) = a;
+							*reinterpret_cast<float4*>(bj + r) = b;
+							*reinterpret_cast<float4*>(vi + r) = c;
+							*reinterpret_cast<float4*>(vj + r) = e;
+						}
+					} else if constexpr (NR > 0) {
 #pragma unroll
 						for (int u = 0; u < NR; ++u) {
 							const int r = gl + LPP * u;
@@ -2587,11 +2639,11 @@ __device__ void svd_f32_sweeps(float* B, int ldb, float* V, int ldv, int p, int 
 // scaled by the power of two that brings its largest entry to [0.5, 1), so squares and
 // sums stay in FP32 range. Its purpose is a start for the FP64 stage (the product
 // refinement, or Jacobi sweeps that started from X W converge in a few).
-template <int LPP, int NR>
+template <int LPP, int NR, bool FULL>
 __global__ void __launch_bounds__(NR > 0 ? 512 : 1024) k_svd_f32(const double* __restrict__ X, long long ldx, int p,
                                                                  int q, float* __restrict__ W, int max_sweeps) {
 	extern __shared__ float fsm[];
-	const int ldb = svf32_ld(p, LPP), ldv = svf32_ld(q, LPP);
+	const int ldb = svf32_ld(p, svf32_ldmod(p, q)), ldv = svf32_ld(q, svf32_ldmod(p, q));
 	float* B = fsm;
 	float* V = fsm + (size_t)ldb * q;
 	__shared__ double d_red[32];
@@ -2600,11 +2652,11 @@ __global__ void __launch_bounds__(NR > 0 ? 512 : 1024) k_svd_f32(const double* _
 	const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5, nwarps = blockDim.x >> 5;
 	// scale: the exponent of max |X| (non-negative doubles order like their bit patterns)
 	long long mx = 0;
-	for (long long e = tid; e < (long long)p * q; e += blockDim.x) {
-		const int i = int(e / q), c = int(e % q);
-		const long long bits = __double_as_longlong(X[(long long)i * ldx + c]) & 0x7fffffffffffffffLL;
-		mx = bits > mx ? bits : mx;
-	}
+	for (int i = warp; i < p; i += nwarps)  // rows by warp, columns by lane: no index division
+		for (int c = lane; c < q; c += 32) {
+			const long long bits = __double_as_longlong(X[(long long)i * ldx + c]) & 0x7fffffffffffffffLL;
+			mx = bits > mx ? bits : mx;
+		}
 	{
 		double dm = __longlong_as_double(mx);
 #pragma unroll
@@ -2621,16 +2673,14 @@ __global__ void __launch_bounds__(NR > 0 ? 512 : 1024) k_svd_f32(const double* _
 	const long long ex = (__double_as_longlong(d_red[0]) >> 52) & 0x7ff;
 	const double scale = ex > 0 ? __longlong_as_double((2045 - ex) << 52) : 1.0;  // 2^(1022 - ex)
 	float fl = 0.f;
-	for (long long e = tid; e < (long long)p * q; e += blockDim.x) {
-		const int i = int(e / q), c = int(e % q);
-		const float v = float(X[(long long)i * ldx + c] * scale);
-		B[(size_t)c * ldb + i] = v;
-		fl = fmaf(v, v, fl);
-	}
-	for (long long e = tid; e < (long long)q * q; e += blockDim.x) {
-		const int c = int(e / q), i = int(e % q);
-		V[(size_t)c * ldv + i] = c == i ? 1.f : 0.f;
-	}
+	for (int i = warp; i < p; i += nwarps)
+		for (int c = lane; c < q; c += 32) {
+			const float v = float(X[(long long)i * ldx + c] * scale);
+			B[c * ldb + i] = v;
+			fl = fmaf(v, v, fl);
+		}
+	for (int c = warp; c < q; c += nwarps)
+		for (int i = lane; i < q; i += 32) V[c * ldv + i] = c == i ? 1.f : 0.f;
 	const float fro = block_sum(fl, f_red);  // its barriers also publish B and V
 	const float negl = fro * 1e-12f;
 	// a start for the FP64 stage, not an SVD: FP32-level orthogonality, at most 12
@@ -2639,25 +2689,26 @@ __global__ void __launch_bounds__(NR > 0 ? 512 : 1024) k_svd_f32(const double* _
 	// a sweep whose largest |cos| between paired columns is below 3e-3 leaves them at
 	// FP32 rounding (the sweeps converge quadratically); the next would rotate noise
 	const float big2 = 9e-6f;
-	svd_f32_sweeps<LPP, NR>(B, ldb, V, ldv, p, q, negl, tol2, big2, max_sweeps, s_rot);
-	for (long long e = tid; e < (long long)q * q; e += blockDim.x) {
-		const int i = int(e / q), c = int(e % q);
-		W[e] = V[(size_t)c * ldv + i];
-	}
+	svd_f32_sweeps<LPP, NR, FULL>(B, ldb, V, ldv, p, q, negl, tol2, big2, max_sweeps, s_rot);
+	for (int i = warp; i < q; i += nwarps)
+		for (int c = lane; c < q; c += 32) W[i * q + c] = V[c * ldv + i];
 }
 
-template <int LPP, int NR>
+template <int LPP, int NR, bool FULL>
 static void launch_svd_f32_as(const double* X, long long ldx, int p, int q, float* W, cudaStream_t s) {
-	func_attr_once(k_svd_f32<LPP, NR>, cudaFuncAttributeMaxDynamicSharedMemorySize, int(kDynSmemMax));
-	k_svd_f32<LPP, NR><<<1, svf32_threads(q, LPP), svf32_smem(p, q), s>>>(X, ldx, p, q, W, 12);
+	func_attr_once(k_svd_f32<LPP, NR, FULL>, cudaFuncAttributeMaxDynamicSharedMemorySize, int(kDynSmemMax));
+	k_svd_f32<LPP, NR, FULL><<<1, svf32_threads(q, LPP), svf32_smem(p, q), s>>>(X, ldx, p, q, W, 12);
 }
 
 void launch_svd_f32(const double* X, long long ldx, int p, int q, float* W, cudaStream_t s) {
 	XTT_REQUIRE(svd_f32_fits(p, q), "internal: FP32 Jacobi stage does not fit one CTA");
 	const Svf32Shape sh = svf32_shape(p, q);
-	if (sh.lpp == 4) launch_svd_f32_as<4, 16>(X, ldx, p, q, W, s);
-	else if (sh.lpp == 8) launch_svd_f32_as<8, 16>(X, ldx, p, q, W, s);
-	else launch_svd_f32_as<16, 0>(X, ldx, p, q, W, s);
+	// FULL: p = q = LPP NR, every register entry is a matrix entry (no bounds tests)
+	if (sh.lpp == 8 && sh.nr == 8) launch_svd_f32_as<8, 8, true>(X, ldx, p, q, W, s);
+	else if (sh.lpp == 4) launch_svd_f32_as<4, 16, false>(X, ldx, p, q, W, s);
+	else if (sh.lpp == 8 && p == 128 && q == 128) launch_svd_f32_as<8, 16, true>(X, ldx, p, q, W, s);
+	else if (sh.lpp == 8) launch_svd_f32_as<8, 16, false>(X, ldx, p, q, W, s);
+	else launch_svd_f32_as<16, 0, false>(X, ldx, p, q, W, s);
 	XTT_CUDA(cudaGetLastError());
 }
 

@@ -157,6 +157,11 @@ int Context::read_int(int idx) {
 	return h_ints[idx];
 }
 
+void Context::read_ints(int lo, int hi) {
+	XTT_CUDA(cudaMemcpyAsync(h_ints + lo, d_ints + lo, sizeof(int) * size_t(hi - lo), cudaMemcpyDeviceToHost, stream));
+	sync();
+}
+
 // ------------------------------------------------------------ tensors
 
 Tensor::Tensor(Context* c, bool is_op, int order, const int64_t* dims_, const int64_t* ranks_)
@@ -506,15 +511,19 @@ constexpr int kGqNsSteps = 3;
 // the symmetric elimination E G E^T = D (E unit lower triangular, its rows updated with
 // the same multipliers as G's) gives R = D^{1/2} E^{-T}, so R^{-1} = E^T D^{-1/2}; written
 // (FP64, scaled back) to Rinv (n x n row-major, zero below the diagonal). One CTA of
-// kGqRows x 32 threads (rows x columns), two barriers per pivot.
+// kGqRows x 32 threads (rows x columns), n <= NMAX; one barrier per pivot, every thread
+// reading the pivot itself, and each thread's updates staged as all loads, then all
+// stores (the compiler cannot reorder shared-memory stores and later loads).
 constexpr int kGqRows = 16;
-__global__ void __launch_bounds__(kGqRows * 32) k_gq_chol32(const double* __restrict__ G, int n, double* __restrict__ Rinv,
-                                                   int* flag) {
+template <int NMAX>
+__global__ void __launch_bounds__(kGqRows * 32) k_gq_chol32(const double* __restrict__ G, int n,
+                                                            double* __restrict__ Rinv, int* flag) {
+	constexpr int U = NMAX / 32, RPT = NMAX / kGqRows;
 	extern __shared__ float gq_s[];
 	const int ld = n + 1, tid = threadIdx.x, tx = tid & 31, ty = tid >> 5;
 	float* S = gq_s;            // n x ld: G, eliminated in its upper triangle
 	float* E = gq_s + n * ld;   // n x ld: the elimination, unit lower triangular
-	__shared__ float s_rs[kGqMaxCols], s_d0[kGqMaxCols], s_inv;
+	__shared__ float s_rs[kGqMaxCols], s_d0[kGqMaxCols];
 	__shared__ double s_scale;
 	__shared__ int s_bad;
 	if (tid == 0) {
@@ -533,32 +542,39 @@ __global__ void __launch_bounds__(kGqRows * 32) k_gq_chol32(const double* __rest
 	}
 	__syncthreads();
 	for (int k = 0; k < n; ++k) {
-		if (tid == 0) {
-			float d = S[k * ld + k];
-			if (!(d > 1e-6f * s_d0[k])) {
-				s_bad = 1;
-				d = 1.f;
-			}
-			s_rs[k] = rsqrtf(d);
-			s_inv = 1.f / d;
+		float d = S[k * ld + k];
+		if (!(d > 1e-6f * s_d0[k])) {
+			if (tid == 0) s_bad = 1;
+			d = 1.f;
 		}
-		__syncthreads();
-		const float inv = s_inv;
-		// row k of S and E in registers (column tx + 32 u), then independent row updates
-		float sk[kGqMaxCols / 32], ek[kGqMaxCols / 32];
+		const float inv = __fdividef(1.f, d);
+		if (tid == 0) s_rs[k] = rsqrtf(d);
+		float sk[U], ek[U], l[RPT], sv[RPT][U], ev[RPT][U];
 #pragma unroll
-		for (int u = 0; u < kGqMaxCols / 32; ++u) {
+		for (int u = 0; u < U; ++u) {
 			const int j = tx + 32 * u;
 			sk[u] = j < n ? S[k * ld + j] : 0.f;
 			ek[u] = j <= k ? E[k * ld + j] : 0.f;
 		}
-		for (int i = k + 1 + ty; i < n; i += kGqRows) {
-			const float l = S[k * ld + i] * inv;
 #pragma unroll
-			for (int u = 0; u < kGqMaxCols / 32; ++u) {
+		for (int rr = 0; rr < RPT; ++rr) {
+			const int i = k + 1 + ty + kGqRows * rr;
+			l[rr] = i < n ? S[k * ld + i] * inv : 0.f;
+#pragma unroll
+			for (int u = 0; u < U; ++u) {
 				const int j = tx + 32 * u;
-				if (j >= i && j < n) S[i * ld + j] = fmaf(-l, sk[u], S[i * ld + j]);
-				if (j <= k) E[i * ld + j] = fmaf(-l, ek[u], E[i * ld + j]);
+				sv[rr][u] = i < n && j >= i && j < n ? S[i * ld + j] : 0.f;
+				ev[rr][u] = i < n && j <= k ? E[i * ld + j] : 0.f;
+			}
+		}
+#pragma unroll
+		for (int rr = 0; rr < RPT; ++rr) {
+			const int i = k + 1 + ty + kGqRows * rr;
+#pragma unroll
+			for (int u = 0; u < U; ++u) {
+				const int j = tx + 32 * u;
+				if (i < n && j >= i && j < n) S[i * ld + j] = fmaf(-l[rr], sk[u], sv[rr][u]);
+				if (i < n && j <= k) E[i * ld + j] = fmaf(-l[rr], ek[u], ev[rr][u]);
 			}
 		}
 		__syncthreads();
@@ -622,9 +638,13 @@ static void gram_qr(Context& c, const QrArgs& a, int slot, int* flag) {
 	XTT_CUDA(cudaMemsetAsync(flag, 0, sizeof(int), c.stream));
 	gemm(c, gq_gemm(nw, nw, mw, a.A, sc, sr, lenA, a.A, sr, sc, lenA, G, nw, 1, nn));  // A_w^T A_w
 	const size_t smem = 2 * size_t(nw) * (nw + 1) * sizeof(float);
-	func_attr_once(k_gq_chol32, cudaFuncAttributeMaxDynamicSharedMemorySize,
-	               int(2 * kGqMaxCols * (kGqMaxCols + 1) * sizeof(float)));
-	k_gq_chol32<<<1, kGqRows * 32, smem, c.stream>>>(G, nw, Ri, flag);
+	if (nw <= 64) {
+		k_gq_chol32<64><<<1, kGqRows * 32, smem, c.stream>>>(G, nw, Ri, flag);
+	} else {
+		func_attr_once(k_gq_chol32<kGqMaxCols>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+		               int(2 * kGqMaxCols * (kGqMaxCols + 1) * sizeof(float)));
+		k_gq_chol32<kGqMaxCols><<<1, kGqRows * 32, smem, c.stream>>>(G, nw, Ri, flag);
+	}
 	XTT_CUDA(cudaGetLastError());
 	c.count_launch();
 	gemm(c, gq_gemm(mw, nw, nw, a.A, sr, sc, lenA, Ri, nw, 1, nn, Qa, nw, 1, mn));  // Q_1 = A_w R^{-1}
@@ -648,17 +668,19 @@ static void gram_qr(Context& c, const QrArgs& a, int slot, int* flag) {
 
 // The rank-revealing QR of transfer_core / round: Cholesky QR where the context asks for
 // it and the shape fits, the pivoted Householder QR otherwise or when its gate fails.
-// Leaves the rank in *a.rank_out (not synchronised).
-static void rank_revealing_qr(Context& c, QrArgs& a) {
+// Returns the rank when the host knows it already (the Cholesky QR keeps all columns),
+// else -1: the rank is then in *a.rank_out (not synchronised).
+static int rank_revealing_qr(Context& c, QrArgs& a) {
 	if (c.gram_qr && gram_qr_fits(a)) {
 		ProfScope ps(c, "qr_gram", qr_work_bytes(a), qr_work_flops(a));
 		int* flag = c.d_ints + 12;
 		gram_qr(c, a, 0, flag);
-		if (c.read_int(12) == 0) return;
+		if (c.read_int(12) == 0) return a.transpose ? a.m : a.n;
 	}
 	ProfScope ps(c, "qr", qr_work_bytes(a), qr_work_flops(a));
 	launch_qr(a, c.stream);
 	c.count_launch();
+	return -1;
 }
 
 void transfer_core(Tensor& x, int from, int to, bool rr) {
@@ -693,8 +715,8 @@ void transfer_core(Tensor& x, int from, int to, bool rr) {
 		a.A = x.core[from]; a.lda = n; a.m = m; a.n = n; a.transpose = 0; a.pivot = rr ? 1 : 0;
 		a.work = wk ? c.scratch<double>(S_QR_WORK, wk) : nullptr;
 		a.Q = Q; a.C = C; a.rank_out = c.d_ints;
-		rank_revealing_qr(c, a);
-		const int rank = rr ? c.read_int(0) : kq;
+		const int known = rank_revealing_qr(c, a);
+		const int rank = known >= 0 ? known : rr ? c.read_int(0) : kq;
 		const int64_t nt = x.n(to), r2 = x.ranks[to + 1];
 		// new right neighbour: C (rank x r1) * core_to (r1 x nt*r2)
 		double* T = c.scratch<double>(S_GEMM_A, size_t(rank) * nt * r2);
@@ -718,8 +740,8 @@ void transfer_core(Tensor& x, int from, int to, bool rr) {
 		a.A = x.core[from]; a.lda = n; a.m = m; a.n = n; a.transpose = 1; a.pivot = rr ? 1 : 0;
 		a.work = wk ? c.scratch<double>(S_QR_WORK, wk) : nullptr;
 		a.Q = Q; a.C = C; a.rank_out = c.d_ints;
-		rank_revealing_qr(c, a);
-		const int rank = rr ? c.read_int(0) : kq;
+		const int known = rank_revealing_qr(c, a);
+		const int rank = known >= 0 ? known : rr ? c.read_int(0) : kq;
 		const int64_t rt = x.ranks[to], nt = x.n(to);
 		// new left neighbour: core_to (rt*nt x r0) * C (r0 x rank)
 		double* T = c.scratch<double>(S_GEMM_A, size_t(rt) * nt * rank);
@@ -904,14 +926,10 @@ __global__ void k_oa_finish(const double* UV, const double* sig, int q, SvdArgs 
 	}
 	__syncthreads();
 	for (int k = tid; k < rank; k += blockDim.x) a.S[k] = sig[s_order[k]];
-	for (long long e = tid; e < (long long)q * rank; e += blockDim.x) {
-		const int i = int(e / rank), k = int(e % rank);
-		a.U[(long long)i * rank + k] = s_sign[k] * Uh[(long long)i * q + s_order[k]];
-	}
-	for (long long e = tid; e < (long long)rank * q; e += blockDim.x) {
-		const int k = int(e / q), j = int(e % q);
-		a.Vt[(long long)k * q + j] = s_sign[k] * Vh[(long long)j * q + s_order[k]];
-	}
+	for (int i = warp; i < q; i += nwarps)  // rows by warp, columns by lane
+		for (int k = lane; k < rank; k += 32) a.U[(long long)i * rank + k] = s_sign[k] * Uh[(long long)i * q + s_order[k]];
+	for (int k = warp; k < rank; k += nwarps)
+		for (int j = lane; j < q; j += 32) a.Vt[(long long)k * q + j] = s_sign[k] * Vh[(long long)j * q + s_order[k]];
 }
 
 // C = A B for q x q row-major operands (A transposed when ta), `batch` pairs at stride q^2.
@@ -1128,18 +1146,24 @@ static void round_edge(Tensor& x, int from, int to, int64_t max_rank, double eps
 			c.count_launch();
 		}
 		c.join();
-		// a Cholesky QR whose gate failed: the pivoted Householder QR instead
-		if (ga && c.read_int(12)) {
+		// one read for the ranks and the Cholesky QRs' gates; a gate that failed: the pivoted
+		// Householder QR instead, and its rank
+		c.read_ints(2, 14);
+		bool again = false;
+		if (ga && c.h_ints[12]) {
 			ProfScope ps(c, "qr", qr_work_bytes(a), qr_work_flops(a));
 			launch_qr(a, c.stream);
 			c.count_launch();
+			again = true;
 		}
-		if (gb && c.read_int(13)) {
+		if (gb && c.h_ints[13]) {
 			ProfScope ps(c, "qr", qr_work_bytes(b), qr_work_flops(b));
 			launch_qr(b, c.stream);
 			c.count_launch();
+			again = true;
 		}
-		const int ka = c.read_int(2), kb = c.read_int(3);
+		if (again) c.read_ints(2, 4);
+		const int ka = c.h_ints[2], kb = c.h_ints[3];
 		double* X = c.scratch<double>(S_GEMM_B, size_t(ka) * kb);
 		Gemm<double> g;
 		g.M = ka; g.N = kb; g.K = int(r);
