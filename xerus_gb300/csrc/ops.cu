@@ -526,20 +526,25 @@ __global__ void __launch_bounds__(kGqRows * 32) k_gq_chol32(const double* __rest
 	__shared__ float s_rs[kGqMaxCols], s_d0[kGqMaxCols];
 	__shared__ double s_scale;
 	__shared__ int s_bad;
-	if (tid == 0) {
+	if (tid < 32) {  // the largest diagonal entry, read by one warp in parallel
 		double mx = 0;
-		for (int i = 0; i < n; ++i) mx = fmax(mx, G[(long long)i * n + i]);
-		s_scale = mx > 0 ? 1.0 / mx : 0.0;
-		s_bad = !(mx > 0);
+		for (int i = tid; i < n; i += 32) mx = fmax(mx, G[(long long)i * n + i]);
+#pragma unroll
+		for (int o = 16; o > 0; o >>= 1) mx = fmax(mx, __shfl_xor_sync(0xffffffffu, mx, o));
+		if (tid == 0) {
+			s_scale = mx > 0 ? 1.0 / mx : 0.0;
+			s_bad = !(mx > 0);
+		}
 	}
 	__syncthreads();
 	const double sc = s_scale;
-	for (int e = tid; e < n * n; e += blockDim.x) {
-		const int i = e / n, j = e % n;
-		S[i * ld + j] = float(G[e] * sc);
-		E[i * ld + j] = i == j ? 1.f : 0.f;
-		if (i == j) s_d0[i] = float(G[e] * sc);
-	}
+	for (int i = ty; i < n; i += kGqRows)  // rows by warp, columns by lane
+		for (int j = tx; j < n; j += 32) {
+			const float v = float(G[(long long)i * n + j] * sc);
+			S[i * ld + j] = v;
+			E[i * ld + j] = i == j ? 1.f : 0.f;
+			if (i == j) s_d0[i] = v;
+		}
 	__syncthreads();
 	for (int k = 0; k < n; ++k) {
 		float d = S[k * ld + k];
@@ -580,10 +585,8 @@ __global__ void __launch_bounds__(kGqRows * 32) k_gq_chol32(const double* __rest
 		__syncthreads();
 	}
 	const double back = sqrt(sc);
-	for (int e = tid; e < n * n; e += blockDim.x) {
-		const int a = e / n, b = e % n;
-		Rinv[e] = b >= a ? double(E[b * ld + a] * s_rs[b]) * back : 0.0;
-	}
+	for (int a = ty; a < n; a += kGqRows)
+		for (int b = tx; b < n; b += 32) Rinv[(long long)a * n + b] = b >= a ? double(E[b * ld + a] * s_rs[b]) * back : 0.0;
 	if (tid == 0 && s_bad) atomicExch(flag, 1);
 }
 
