@@ -244,7 +244,8 @@ void scale(Context& c, double* x, double f, size_t count);
 // plain sweeps there; on unstructured matrices, e.g. rounding a random TT, it saves
 // no sweeps and its QR costs more than it saves). The workspace (a.work) is taken
 // from the context's scratch here.
-void run_svd(Context& c, SvdArgs& a, bool graded = false);
+// Returns the kept rank when the host already read it, else -1 (then it is in *a.rank_out).
+int run_svd(Context& c, SvdArgs& a, bool graded = false);
 void scale_rows(Context& c, double* X, const double* S, int rows, int cols);  // X (rows x cols) *= S[row]
 void scale_cols(Context& c, double* X, const double* S, int rows, int cols);  // X (rows x cols) *= S[col]
 // Sum of squares of x into ctx.d_dbl[slot] (deterministic two-level reduction).

@@ -885,14 +885,18 @@ __global__ void k_oa_correct(const double* PQ, const double* T, double* FG, doub
 // Sort descending, the reference's truncation (rank cap, first j >= 1 with S_j <= eps S_0),
 // the sign gauge (largest |entry| of each kept left vector positive, first on ties), and
 // U (m x rank), S, V^T (rank x n); nothing when the flag is set.
-__global__ void k_oa_finish(const double* UV, const double* sig, int q, SvdArgs a, const int* flag) {
+__global__ void k_oa_finish(const double* UV, const double* sig_g, int q, SvdArgs a, const int* flag) {
 	if (*flag) return;
-	extern __shared__ int s_order[];
+	extern __shared__ double s_fin[];  // sigma (q doubles), then the order (q ints)
+	double* sig = s_fin;
+	int* s_order = reinterpret_cast<int*>(s_fin + q);
 	__shared__ int s_rank;
 	__shared__ double s_sign[1024];
 	const double* Uh = UV;
 	const double* Vh = UV + (long long)q * q;
 	const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5, nwarps = blockDim.x >> 5;
+	for (int c = tid; c < q; c += blockDim.x) sig[c] = sig_g[c];
+	__syncthreads();
 	for (int c = tid; c < q; c += blockDim.x) {
 		int pos = 0;
 		for (int o = 0; o < q; ++o) pos += (sig[o] > sig[c]) || (sig[o] == sig[c] && o < c);
@@ -948,9 +952,13 @@ static Gemm<double> sq_gemm(int q, const double* A, bool ta, long long lda, cons
 }
 
 // X (q x q, leading dimension a.ldx) from W (the FP32 Jacobi's right factor, FP64):
-// kOaSteps refinement steps, then the outputs of `a`. False (nothing written) if the
-// flag was set.
-static bool svd_refine_square(Context& c, const SvdArgs& a, const double* W, int q) {
+// kOaSteps refinement steps, then the outputs of `a`. `ok` false (nothing written) if
+// the flag was set; `rank` the kept rank when it was read with the flag (-1 otherwise).
+struct RefineResult {
+	bool ok;
+	int rank;
+};
+static RefineResult svd_refine_square(Context& c, const SvdArgs& a, const double* W, int q) {
 	XTT_REQUIRE(q <= 1024, "internal: refinement sized for q <= 1024");
 	const size_t qq = size_t(q) * q;
 	double* UV = c.scratch<double>(S_SVD_RF_U, 2 * qq);    // [U | V]
@@ -975,10 +983,16 @@ static bool svd_refine_square(Context& c, const SvdArgs& a, const double* W, int
 		gemm(c, sq_gemm(q, UV, false, q, FG, UV2, 2));  // [U (I + F) | V (I + G)]
 		std::swap(UV, UV2);
 	}
-	k_oa_finish<<<1, 256, size_t(q) * sizeof(int), c.stream>>>(UV, sig, q, a, flag);
+	k_oa_finish<<<1, 256, size_t(q) * (sizeof(double) + sizeof(int)), c.stream>>>(UV, sig, q, a, flag);
 	XTT_CUDA(cudaGetLastError());
 	c.count_launch();
-	return c.read_int(6) == 0;
+	// one host read for the flag and, where it is a context int, the rank
+	const long long ri = a.rank_out ? (long long)(a.rank_out - c.d_ints) : -1;
+	if (ri >= 0 && ri < 64) {
+		c.read_ints(int(std::min<long long>(ri, 6)), int(std::max<long long>(ri, 6)) + 1);
+		return {c.h_ints[6] == 0, c.h_ints[6] == 0 ? c.h_ints[ri] : -1};
+	}
+	return {c.read_int(6) == 0, -1};
 }
 
 // One-sided Jacobi of a.X (through launch_svd). Mixed precision where it fits (svd_path
@@ -991,7 +1005,7 @@ static bool svd_refine_square(Context& c, const SvdArgs& a, const double* W, int
 // truncation and gauge.
 // `mixed` false: plain FP64 Jacobi (after the QR preconditioning, whose R^T already
 // converges in 6-10 sweeps, the FP32 stage measured slower than it saves).
-static void jacobi(Context& c, SvdArgs& a, bool mixed) {
+static int jacobi(Context& c, SvdArgs& a, bool mixed) {
 	const bool tall = a.m > a.n || (a.m == a.n && !a.orth_rows);
 	const int p = tall ? a.m : a.n, q = tall ? a.n : a.m;
 	if (mixed && c.svd_path == XTT_SVD_PATH_AUTO && tall && !a.V0 && q >= 32 && svd_f32_fits(p, q)) {
@@ -1011,7 +1025,8 @@ static void jacobi(Context& c, SvdArgs& a, bool mixed) {
 		// square: refine the FP32 factors by products instead of Jacobi sweeps
 		if (p == q && q <= 1024) {
 			ProfScope ps(c, "svd_refine");
-			if (svd_refine_square(c, a, W, q)) return;
+			const RefineResult rr = svd_refine_square(c, a, W, q);
+			if (rr.ok) return rr.rank;
 		}
 		ProfScope ps(c, "svd_sweeps");
 		for (int it = 0; it < 2; ++it) {
@@ -1052,15 +1067,16 @@ static void jacobi(Context& c, SvdArgs& a, bool mixed) {
 		b.work = wk ? c.scratch<double>(S_SVD_WORK, wk) : nullptr;
 		launch_svd(b, c.stream);
 		c.count_launch();
-		return;
+		return -1;
 	}
 	const size_t wk = svd_work_doubles(a.m, a.n);
 	a.work = wk ? c.scratch<double>(S_SVD_WORK, wk) : nullptr;
 	launch_svd(a, c.stream);
 	c.count_launch();
+	return -1;
 }
 
-void run_svd(Context& c, SvdArgs& a, bool graded) {
+int run_svd(Context& c, SvdArgs& a, bool graded) {
 	ProfScope ps(c, "svd");
 	if (graded && c.svd_path == XTT_SVD_PATH_AUTO && svd_pc_fits(a.m, a.n)) {
 		size_t nq, nc, nqr, nsv;
@@ -1081,9 +1097,9 @@ void run_svd(Context& c, SvdArgs& a, bool graded) {
 		jacobi(c, sa, false);
 		svd_pc_finish(a, w, kept, c.stream);
 		c.count_launch(3);
-		return;
+		return -1;
 	}
-	jacobi(c, a, true);
+	return jacobi(c, a, true);
 }
 
 static int svd_into(Context& c, const double* X, int m, int n, int max_rank, double eps, double*& U, double*& S,
@@ -1095,8 +1111,8 @@ static int svd_into(Context& c, const double* X, int m, int n, int max_rank, dou
 	SvdArgs a;
 	a.X = X; a.ldx = n; a.m = m; a.n = n; a.max_rank = max_rank; a.eps = eps;
 	a.U = U; a.S = S; a.Vt = Vt; a.rank_out = c.d_ints + 1; a.status = c.d_status;
-	run_svd(c, a);
-	return c.read_int(1);
+	const int known = run_svd(c, a);
+	return known >= 0 ? known : c.read_int(1);
 }
 
 static void round_edge(Tensor& x, int from, int to, int64_t max_rank, double eps, std::vector<double>* spectra) {
