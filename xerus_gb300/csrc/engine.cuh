@@ -42,6 +42,8 @@ struct Context {
 	int contraction_terms = 0;
 	int tc_active = 0;
 	bool gram_qr = false;  // rank-revealing QRs by Cholesky QR where well-conditioned (GramQrScope)
+	// CUDA graphs of fixed launch sequences, by the shapes and buffers they were captured with
+	std::vector<std::pair<std::vector<long long>, struct ReplayGraph*>> graph_cache;
 	// batched ALS: the CUDA graph of the last batch launch (replayed while its
 	// signature holds), its pinned descriptor staging, and autotuned launch shapes
 	unsigned long long batch_key = 0;

@@ -53,6 +53,7 @@ Context::~Context() {
 	cudaSetDevice(device);
 	cudaStreamSynchronize(stream);
 	cudaStreamSynchronize(aux);
+	for (auto& e : graph_cache) delete e.second;
 	for (auto& s : slots)
 		if (s.p) cudaFree(s.p);
 	cudaFree(d_status);
@@ -503,7 +504,7 @@ bool exceeds_maximal_ranks(const Tensor& x) {
 // (so Q is orthonormal to ~1e-14); otherwise a flag is set and the caller runs the
 // pivoted Householder QR. Q and C differ from Householder's by an orthogonal n_w x n_w
 // factor (Q C is the same): round uses them only through Q C-invariant products.
-constexpr int kGqSlots = 5;  // scratch ids per concurrent factorisation
+constexpr int kGqSlots = 6;  // scratch ids per concurrent factorisation
 constexpr int kGqMaxCols = 128;
 constexpr int kGqNsSteps = 3;
 
@@ -636,37 +637,60 @@ static void gram_qr(Context& c, const QrArgs& a, int slot, int* flag) {
 	double* G = c.scratch<double>(id + 0, nn);
 	double* Ri = c.scratch<double>(id + 1, nn);
 	double* H = c.scratch<double>(id + 2, nn);
-	double* Qa = c.scratch<double>(id + 3, mn);
-	double* Qb = c.scratch<double>(id + 4, mn);
-	XTT_CUDA(cudaMemsetAsync(flag, 0, sizeof(int), c.stream));
-	gemm(c, gq_gemm(nw, nw, mw, a.A, sc, sr, lenA, a.A, sr, sc, lenA, G, nw, 1, nn));  // A_w^T A_w
-	const size_t smem = 2 * size_t(nw) * (nw + 1) * sizeof(float);
-	if (nw <= 64) {
-		k_gq_chol32<64><<<1, kGqRows * 32, smem, c.stream>>>(G, nw, Ri, flag);
-	} else {
+	double* Qa0 = c.scratch<double>(id + 3, mn);
+	double* Qb0 = c.scratch<double>(id + 4, mn);
+	if (nw > 64)
 		func_attr_once(k_gq_chol32<kGqMaxCols>, cudaFuncAttributeMaxDynamicSharedMemorySize,
 		               int(2 * kGqMaxCols * (kGqMaxCols + 1) * sizeof(float)));
-		k_gq_chol32<kGqMaxCols><<<1, kGqRows * 32, smem, c.stream>>>(G, nw, Ri, flag);
-	}
-	XTT_CUDA(cudaGetLastError());
-	c.count_launch();
-	gemm(c, gq_gemm(mw, nw, nw, a.A, sr, sc, lenA, Ri, nw, 1, nn, Qa, nw, 1, mn));  // Q_1 = A_w R^{-1}
-	// the output layouts: tr == 0: Q (m x n_w) ld n_w, C (n_w x n) ld n; tr == 1: Q (n_w x n)
-	// ld n (= Q_w^T), C (m x n_w) ld n_w (= C_w^T)
-	const long long qm = tr ? 1 : nw, qn = tr ? mw : 1;
-	for (int it = 0; it < kGqNsSteps; ++it) {
-		const bool last = it + 1 == kGqNsSteps;
-		gemm(c, gq_gemm(nw, nw, mw, Qa, 1, nw, mn, Qa, nw, 1, mn, G, nw, 1, nn));  // Q^T Q
-		k_gq_ns<<<(unsigned(nn) + 255) / 256, 256, 0, c.stream>>>(G, H, nw, last, flag, a.rank_out);
+	// the 13 launches in stream order, reading the factor from Ain
+	auto launches = [&](const double* Ain) {
+		double *Qa = Qa0, *Qb = Qb0;
+		XTT_CUDA(cudaMemsetAsync(flag, 0, sizeof(int), c.stream));
+		gemm(c, gq_gemm(nw, nw, mw, Ain, sc, sr, lenA, Ain, sr, sc, lenA, G, nw, 1, nn));  // A_w^T A_w
+		const size_t smem = 2 * size_t(nw) * (nw + 1) * sizeof(float);
+		if (nw <= 64) k_gq_chol32<64><<<1, kGqRows * 32, smem, c.stream>>>(G, nw, Ri, flag);
+		else k_gq_chol32<kGqMaxCols><<<1, kGqRows * 32, smem, c.stream>>>(G, nw, Ri, flag);
 		XTT_CUDA(cudaGetLastError());
 		c.count_launch();
-		if (last) gemm(c, gq_gemm(mw, nw, nw, Qa, nw, 1, mn, H, nw, 1, nn, a.Q, qm, qn, mn));
-		else gemm(c, gq_gemm(mw, nw, nw, Qa, nw, 1, mn, H, nw, 1, nn, Qb, nw, 1, mn));
-		std::swap(Qa, Qb);
+		gemm(c, gq_gemm(mw, nw, nw, Ain, sr, sc, lenA, Ri, nw, 1, nn, Qa, nw, 1, mn));  // Q_1 = A_w R^{-1}
+		// the output layouts: tr == 0: Q (m x n_w) ld n_w, C (n_w x n) ld n; tr == 1: Q (n_w x n)
+		// ld n (= Q_w^T), C (m x n_w) ld n_w (= C_w^T)
+		const long long qm = tr ? 1 : nw, qn = tr ? mw : 1;
+		for (int it = 0; it < kGqNsSteps; ++it) {
+			const bool last = it + 1 == kGqNsSteps;
+			gemm(c, gq_gemm(nw, nw, mw, Qa, 1, nw, mn, Qa, nw, 1, mn, G, nw, 1, nn));  // Q^T Q
+			k_gq_ns<<<(unsigned(nn) + 255) / 256, 256, 0, c.stream>>>(G, H, nw, last, flag, a.rank_out);
+			XTT_CUDA(cudaGetLastError());
+			c.count_launch();
+			if (last) gemm(c, gq_gemm(mw, nw, nw, Qa, nw, 1, mn, H, nw, 1, nn, a.Q, qm, qn, mn));
+			else gemm(c, gq_gemm(mw, nw, nw, Qa, nw, 1, mn, H, nw, 1, nn, Qb, nw, 1, mn));
+			std::swap(Qa, Qb);
+		}
+		// C_w = Q_w^T A_w, Q_w read back from a.Q
+		gemm(c, gq_gemm(nw, nw, mw, a.Q, tr ? mw : 1, tr ? 1 : nw, mn, Ain, sr, sc, lenA, a.C, tr ? 1 : nw,
+		                tr ? nw : 1, nn));
+	};
+	if (c.profiling) {  // per-launch timing: no graph
+		launches(a.A);
+		return;
 	}
-	// C_w = Q_w^T A_w, Q_w read back from a.Q
-	gemm(c, gq_gemm(nw, nw, mw, a.Q, tr ? mw : 1, tr ? 1 : nw, mn, a.A, sr, sc, lenA, a.C, tr ? 1 : nw, tr ? nw : 1,
-	                nn));
+	// replayed as one CUDA graph per shape and buffer set: the factor is first copied into a
+	// staging buffer the graph reads (the cores it factors live in different buffers)
+	double* As = c.scratch<double>(id + 5, size_t(lenA));
+	copy_d2d(c, As, a.A, size_t(lenA));
+	const std::vector<long long> key = {1, a.m, a.n, a.lda, a.transpose, slot, (long long)(uintptr_t)As,
+	                                    (long long)(uintptr_t)G, (long long)(uintptr_t)Ri, (long long)(uintptr_t)H,
+	                                    (long long)(uintptr_t)Qa0, (long long)(uintptr_t)Qb0,
+	                                    (long long)(uintptr_t)a.Q, (long long)(uintptr_t)a.C,
+	                                    (long long)(uintptr_t)a.rank_out, (long long)(uintptr_t)flag};
+	ReplayGraph* g = nullptr;
+	for (auto& e : c.graph_cache)
+		if (e.first == key) g = e.second;
+	if (!g) {
+		g = new ReplayGraph();
+		c.graph_cache.emplace_back(key, g);
+	}
+	g->run(c, [&] { launches(As); });
 }
 
 // The rank-revealing QR of transfer_core / round: Cholesky QR where the context asks for
