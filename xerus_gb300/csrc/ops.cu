@@ -1139,7 +1139,16 @@ static int svd_into(Context& c, const double* X, int m, int n, int max_rank, dou
 	return known >= 0 ? known : c.read_int(1);
 }
 
-static void round_edge(Tensor& x, int from, int to, int64_t max_rank, double eps, std::vector<double>* spectra) {
+__global__ void k_eye(double* I, int n) {
+	for (int e = blockIdx.x * blockDim.x + threadIdx.x; e < n * n; e += gridDim.x * blockDim.x)
+		I[e] = e / n == e % n ? 1.0 : 0.0;
+}
+
+// to_orth: core `to` has orthonormal columns (round's left-orthogonalised cores). Its QC is
+// then T = T I (Q_T = T, C_B = I, full rank: the reference's pivoted QR of such a matrix has
+// |R_kk| = 1 and keeps every column), and only F is factored.
+static void round_edge(Tensor& x, int from, int to, int64_t max_rank, double eps, std::vector<double>* spectra,
+                       bool to_orth) {
 	// TensorNetwork::round_edge (src/xerus/tensorNetwork.cpp:678-818) for from = core k+1, to = core k.
 	Context& c = *x.ctx;
 	const int64_t r = x.ranks[from], nF = x.n(from), rF = x.ranks[from + 1];
@@ -1161,15 +1170,21 @@ static void round_edge(Tensor& x, int from, int to, int64_t max_rank, double eps
 		// the two factorisations are independent: T's on the aux stream, F's on the main one
 		c.fork();
 		const int mT = int(rT * nT), nTc = int(r);
-		double* QT = c.scratch<double>(S_ROUND_QB, size_t(mT) * std::min(mT, nTc));
+		const bool skip_b = to_orth && mT >= nTc;
+		double* QT = skip_b ? x.core[to] : c.scratch<double>(S_ROUND_QB, size_t(mT) * std::min(mT, nTc));
 		double* CB = c.scratch<double>(S_ROUND_CB, size_t(std::min(mT, nTc)) * nTc);
 		wk = qr_work_doubles(mT, nTc);
 		QrArgs b;
 		b.A = x.core[to]; b.lda = nTc; b.m = mT; b.n = nTc; b.transpose = 0; b.pivot = 1;
 		b.work = wk ? c.scratch<double>(S_ROUND_X, wk) : nullptr;  // not S_QR_WORK: runs beside a
 		b.Q = QT; b.C = CB; b.rank_out = c.d_ints + 3;
-		const bool gb = c.gram_qr && gram_qr_fits(b), ga = c.gram_qr && gram_qr_fits(a);
-		{
+		const bool gb = !skip_b && c.gram_qr && gram_qr_fits(b), ga = c.gram_qr && gram_qr_fits(a);
+		if (skip_b) {
+			k_eye<<<unsigned((nTc * nTc + 255) / 256), 256, 0, c.stream>>>(CB, nTc);
+			XTT_CUDA(cudaGetLastError());
+			c.count_launch();
+		}
+		if (!skip_b) {
 			OnAux aux(c);
 			if (gb) {
 				ProfScope ps(c, "qr_gram", qr_work_bytes(b), qr_work_flops(b));
@@ -1206,7 +1221,7 @@ static void round_edge(Tensor& x, int from, int to, int64_t max_rank, double eps
 			again = true;
 		}
 		if (again) c.read_ints(2, 4);
-		const int ka = c.h_ints[2], kb = c.h_ints[3];
+		const int ka = c.h_ints[2], kb = skip_b ? nTc : c.h_ints[3];
 		double* X = c.scratch<double>(S_GEMM_B, size_t(ka) * kb);
 		Gemm<double> g;
 		g.M = ka; g.N = kb; g.K = int(r);
@@ -1275,7 +1290,8 @@ void round_tt(Tensor& x, const std::vector<int64_t>& max_ranks, double eps, std:
 	const int d = x.d;
 	GramQrScope gram(*x.ctx);
 	move_core(x, d - 1, false);
-	for (int i = 0; i + 1 < d; ++i) round_edge(x, d - 1 - i, d - 2 - i, max_ranks[d - 2 - i], eps, spectra);
+	// after move_core(d - 1) every core left of the one being truncated has orthonormal columns
+	for (int i = 0; i + 1 < d; ++i) round_edge(x, d - 1 - i, d - 2 - i, max_ranks[d - 2 - i], eps, spectra, true);
 	x.canonicalized = true;
 	x.core_position = 0;
 	if (init_canon) move_core(x, init_pos, false);
