@@ -1409,130 +1409,146 @@ __device__ __forceinline__ double warp_sum_d(double v) {
 	return v;
 }
 
-// RPT rows per lane (mw <= 32 RPT): instantiated for 1..4 so that no lane carries padding
-// rows through the FP64 chains (a warp-wide FP64 instruction occupies GB300's FP64 pipe
-// for ~19 cycles whether or not its lanes hold data).
-template <int kTwRpt>
+// RPT rows per lane (mw <= 32 RPT): the matrix in shared memory, lane l holding rows
+// l, l + 32, .. of every column; the column loops stay loops. A one-warp kernel runs each
+// instruction once, so straight-line (fully unrolled) code spends its time fetching
+// instructions: measured 50 us for a 48 x 6 move with ~6 cycles per issue waiting on the
+// instruction cache; looped, the body stays cached after the first column.
+template <int RPT>
 __global__ void __launch_bounds__(32) k_transfer_warp(TransferArgs t) {
+	__shared__ double sA[32 * kTwRptMax][kTwCols + 1];
 	__shared__ double sR[kTwCols][kTwCols];
+	__shared__ double sTau[kTwCols];
+	__shared__ double sSl[32][kTwMaxSlices + 1];
+	__shared__ double sStep[kTwMaxSlices];
 	const int lane = threadIdx.x;
 	const int mw = t.right ? t.r0 * t.nf : t.nf * t.r1, nw = t.right ? t.r1 : t.r0;
-	double a[kTwRpt][kTwCols];
 #pragma unroll
-	for (int u = 0; u < kTwRpt; ++u) {
+	for (int u = 0; u < RPT; ++u) {
 		const int row = lane + 32 * u;
-#pragma unroll
+#pragma unroll 1
 		for (int c = 0; c < kTwCols; ++c)
-			a[u][c] = (row < mw && c < nw) ? (t.right ? t.from[row * nw + c] : t.from[c * mw + row]) : 0.0;
+			sA[row][c] = (row < mw && c < nw) ? (t.right ? t.from[row * nw + c] : t.from[c * mw + row]) : 0.0;
 	}
 	if (t.G) {
-		// the ADF step on every slice i of core_from (rows (a, i), i = row mod n): the slice
-		// norms as n independent warp sums, their steps as n independent divisions
+		// the ADF step on every slice i of core_from (rows (a, i), i = row mod n): each lane's
+		// partial slice sums, lane i adds slice i's partials and divides (the n divisions run
+		// side by side in the warp's lanes)
 		const int n = t.nf;
-		double g[kTwRpt][kTwCols];
-		double sl[kTwMaxSlices];
+#pragma unroll 1
+		for (int i = 0; i < n; ++i) sSl[lane][i] = 0.0;
 #pragma unroll
-		for (int i = 0; i < kTwMaxSlices; ++i) sl[i] = 0.0;
-#pragma unroll
-		for (int u = 0; u < kTwRpt; ++u) {
+		for (int u = 0; u < RPT; ++u) {
 			const int row = lane + 32 * u;
-			double q = 0.0;
-#pragma unroll
-			for (int c = 0; c < kTwCols; ++c) {
-				g[u][c] = (row < mw && c < nw) ? t.G[row * nw + c] : 0.0;
-				q = fma(g[u][c], g[u][c], q);
+			if (row < mw) {
+				double q = 0.0;
+#pragma unroll 1
+				for (int c = 0; c < nw; ++c) q = fma(t.G[row * nw + c], t.G[row * nw + c], q);
+				sSl[lane][row % n] += q;
 			}
-			const int i = row < mw ? row % n : 0;
-#pragma unroll
-			for (int ii = 0; ii < kTwMaxSlices; ++ii)
-				if (ii == i) sl[ii] += q;
 		}
-		double step[kTwMaxSlices];
-#pragma unroll
-		for (int ii = 0; ii < kTwMaxSlices; ++ii) {
-			step[ii] = 0.0;
-			if (ii >= n) continue;
-			step[ii] = warp_sum_d(sl[ii]) / t.nrm[ii];
+		__syncwarp();
+		if (lane < n) {
+			double sum = 0.0;
+#pragma unroll 1
+			for (int l = 0; l < 32; ++l) sum += sSl[l][lane];
+			sStep[lane] = sum / t.nrm[lane];
 		}
+		__syncwarp();
 #pragma unroll
-		for (int u = 0; u < kTwRpt; ++u) {
+		for (int u = 0; u < RPT; ++u) {
 			const int row = lane + 32 * u;
-			const int i = row < mw ? row % n : 0;
-			double st = 0.0;
-#pragma unroll
-			for (int ii = 0; ii < kTwMaxSlices; ++ii)
-				if (ii == i) st = step[ii];
-#pragma unroll
-			for (int c = 0; c < kTwCols; ++c) a[u][c] = fma(st, g[u][c], a[u][c]);
+			if (row < mw) {
+				const double st = sStep[row % n];
+#pragma unroll 1
+				for (int c = 0; c < nw; ++c) sA[row][c] = fma(st, t.G[row * nw + c], sA[row][c]);
+			}
 		}
+		__syncwarp();
 	}
-	double tau[kTwCols];
+	// Householder QR (dlarfg conventions); rows >= mw are zero
+#pragma unroll 1
+	for (int j = 0; j < nw; ++j) {
+		double pu[RPT];
 #pragma unroll
-	for (int j = 0; j < kTwCols; ++j) {
-		tau[j] = 0.0;
-		if (j >= nw) continue;
-		// ||x||^2 below the diagonal; alpha = a(j, j) sits in lane j (rows j < 8 are in u = 0)
-		double pu[kTwRpt];
-#pragma unroll
-		for (int u = 0; u < kTwRpt; ++u) pu[u] = lane + 32 * u > j ? a[u][j] * a[u][j] : 0.0;
-		const double xn2 = warp_sum_d(tree_sum<kTwRpt>(pu));
-		const double alpha = __shfl_sync(0xffffffffu, a[0][j], j);
+		for (int u = 0; u < RPT; ++u) {
+			const int row = lane + 32 * u;
+			pu[u] = row > j ? sA[row][j] * sA[row][j] : 0.0;
+		}
+		const double xn2 = warp_sum_d(tree_sum<RPT>(pu));
+		const double alpha = sA[j][j];
 		double beta, tj, scal;
 		reflector_scalars(alpha, xn2, beta, tj, scal);
-		tau[j] = tj;
+		__syncwarp();
 #pragma unroll
-		for (int u = 0; u < kTwRpt; ++u)
-			if (lane + 32 * u > j) a[u][j] *= scal;
-		if (lane == j) a[0][j] = beta;
+		for (int u = 0; u < RPT; ++u) {
+			const int row = lane + 32 * u;
+			if (row > j) sA[row][j] *= scal;
+		}
+		if (lane == 0) {
+			sA[j][j] = beta;
+			sTau[j] = tj;
+		}
+		__syncwarp();
 		// trailing columns: a_c -= tau (a_jc + v^T a_c) v, v = [1; x scal]
+#pragma unroll 1
+		for (int c = j + 1; c < nw; ++c) {
+			double pv[RPT];
 #pragma unroll
-		for (int c = j + 1; c < kTwCols; ++c) {
-			if (c >= nw) continue;
-			double pv[kTwRpt];
+			for (int u = 0; u < RPT; ++u) {
+				const int row = lane + 32 * u;
+				pv[u] = row > j ? sA[row][j] * sA[row][c] : (row == j ? sA[j][c] : 0.0);
+			}
+			const double wc = tj * warp_sum_d(tree_sum<RPT>(pv));
 #pragma unroll
-			for (int u = 0; u < kTwRpt; ++u) pv[u] = lane + 32 * u > j ? a[u][j] * a[u][c] : 0.0;
-			if (lane == j) pv[0] = a[0][c];  // v_j = 1 (row j > j is false for u = 0, lane j)
-			const double wc = tj * warp_sum_d(tree_sum<kTwRpt>(pv));
-			if (lane == j) a[0][c] -= wc;
-#pragma unroll
-			for (int u = 0; u < kTwRpt; ++u)
-				if (lane + 32 * u > j) a[u][c] = fma(-wc, a[u][j], a[u][c]);
+			for (int u = 0; u < RPT; ++u) {
+				const int row = lane + 32 * u;
+				if (row > j) sA[row][c] = fma(-wc, sA[row][j], sA[row][c]);
+				else if (row == j) sA[j][c] -= wc;
+			}
+			__syncwarp();
 		}
 	}
-	// R (rows 0..nw-1 sit in lanes 0..nw-1, u = 0)
-	if (lane < nw) {
-#pragma unroll
-		for (int c = 0; c < kTwCols; ++c) sR[lane][c] = c >= lane ? a[0][c] : 0.0;
+	// R
+#pragma unroll 1
+	for (int e = lane; e < kTwCols * kTwCols; e += 32) {
+		const int i = e / kTwCols, c = e % kTwCols;
+		sR[i][c] = (i < nw && c < nw && c >= i) ? sA[i][c] : 0.0;
 	}
 	__syncwarp();
 	// Q in place of the reflectors (dorg2r, backward)
+#pragma unroll 1
+	for (int j = nw - 1; j >= 0; --j) {
+		const double tj = sTau[j];
+#pragma unroll 1
+		for (int c = j + 1; c < nw; ++c) {
+			double pv[RPT];
 #pragma unroll
-	for (int jr = 0; jr < kTwCols; ++jr) {
-		const int j = kTwCols - 1 - jr;
-		if (j >= nw) continue;
-		const double tj = tau[j];
+			for (int u = 0; u < RPT; ++u) {
+				const int row = lane + 32 * u;
+				pv[u] = row > j ? sA[row][j] * sA[row][c] : 0.0;
+			}
+			const double wc = tj * warp_sum_d(tree_sum<RPT>(pv));
 #pragma unroll
-		for (int c = j + 1; c < kTwCols; ++c) {
-			if (c >= nw) continue;
-			double pv[kTwRpt];
-#pragma unroll
-			for (int u = 0; u < kTwRpt; ++u) pv[u] = lane + 32 * u > j ? a[u][j] * a[u][c] : 0.0;
-			const double wc = tj * warp_sum_d(tree_sum<kTwRpt>(pv));
-#pragma unroll
-			for (int u = 0; u < kTwRpt; ++u)
-				if (lane + 32 * u > j) a[u][c] = fma(-wc, a[u][j], a[u][c]);
-			if (lane == j) a[0][c] = -wc;
+			for (int u = 0; u < RPT; ++u) {
+				const int row = lane + 32 * u;
+				if (row > j) sA[row][c] = fma(-wc, sA[row][j], sA[row][c]);
+				else if (row == j) sA[j][c] = -wc;
+			}
+			__syncwarp();
 		}
 #pragma unroll
-		for (int u = 0; u < kTwRpt; ++u) {
+		for (int u = 0; u < RPT; ++u) {
 			const int row = lane + 32 * u;
-			a[u][j] = row > j ? -tj * a[u][j] : (row == j ? 1.0 - tj : 0.0);
+			sA[row][j] = row > j ? -tj * sA[row][j] : (row == j ? 1.0 - tj : 0.0);
 		}
+		__syncwarp();
 	}
 	// the neighbour absorbs R (right: R * core_to; left: core_to * R^T), each lane reading
 	// whole columns (right) or rows (left) of core_to before writing them
 	if (t.right) {
 		const int n2 = t.nt * t.r2;
+#pragma unroll 1
 		for (int col = lane; col < n2; col += 32) {
 			double v[kTwCols];
 #pragma unroll
@@ -1548,6 +1564,7 @@ __global__ void __launch_bounds__(32) k_transfer_warp(TransferArgs t) {
 		}
 	} else {
 		const int m2 = t.rt * t.nt;
+#pragma unroll 1
 		for (int row = lane; row < m2; row += 32) {
 			double v[kTwCols];
 #pragma unroll
@@ -1564,15 +1581,14 @@ __global__ void __launch_bounds__(32) k_transfer_warp(TransferArgs t) {
 	}
 	// Q: right, core_from (mw x nw); left, Q^T as core_from (nw x mw)
 #pragma unroll
-	for (int u = 0; u < kTwRpt; ++u) {
+	for (int u = 0; u < RPT; ++u) {
 		const int row = lane + 32 * u;
 		if (row >= mw) continue;
-#pragma unroll
-		for (int c = 0; c < kTwCols; ++c)
-			if (c < nw) {
-				if (t.right) t.from[row * nw + c] = a[u][c];
-				else t.from[c * mw + row] = a[u][c];
-			}
+#pragma unroll 1
+		for (int c = 0; c < nw; ++c) {
+			if (t.right) t.from[row * nw + c] = sA[row][c];
+			else t.from[c * mw + row] = sA[row][c];
+		}
 	}
 }
 
