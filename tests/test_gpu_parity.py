@@ -296,6 +296,102 @@ def test_round_odd_shapes(ctx, svd_path):
     assert rel_err(x.entries(pos), o.tt_entries(xh, pos)) < 1e-10
 
 
+def _tt_with_bond_spectrum(sigma, seed):
+    """d=6, n=4 TT of ranks [4, 16, 64, 16, 4] whose middle bond (cores 2 | 3) has exactly the
+    singular values `sigma` (64): cores 0-2 left-orthogonal, core 3 = U diag(sigma) V^T
+    (U, V orthogonal), cores 4-5 right-orthogonal. round(32) factors that bond's 64 x 64
+    matrix: the product-refined SVD and the Cholesky QR of a core with condition
+    sigma_max / sigma_min."""
+    rng = np.random.default_rng(seed)
+    n, ranks = 4, [1, 4, 16, 64, 16, 4, 1]
+    cores = []
+    for k in range(3):
+        q, _ = np.linalg.qr(rng.standard_normal((ranks[k] * n, ranks[k + 1])))
+        cores.append(q.reshape(ranks[k], n, ranks[k + 1]))
+    q, _ = np.linalg.qr(rng.standard_normal((64, 64)))
+    u, _ = np.linalg.qr(rng.standard_normal((64, 64)))  # non-orthogonal rows: Gram condition sigma_max^2 / sigma_min^2
+    cores.append((u @ (np.asarray(sigma)[:, None] * q.T)).reshape(64, n, 16))
+    for k in range(4, 6):
+        q, _ = np.linalg.qr(rng.standard_normal((n * ranks[k + 1], ranks[k])))
+        cores.append(q.T.reshape(ranks[k], n, ranks[k + 1]))
+    return cores
+
+
+@pytest.mark.parametrize("spectrum", ["separated", "duplicate", "graded", "deficient"])
+def test_round_refinement_and_cholesky_qr_fallbacks(ctx, spectrum):
+    """The round's fast paths against the oracle's LAPACK round on one 64 x 64 bond:
+    separated singular values (product refinement, Cholesky QR); an exactly repeated pair
+    (the refinement's gap test declines, Jacobi sweeps run); a 1e-6 graded spectrum (the
+    FP32 start is too far off for the smallest singular vectors, so the refinement's last
+    corrections stay large and it declines; the Cholesky QR's gate fails, pivoted
+    Householder runs); eight exact zeros (both decline; the QC rank rule and the truncation
+    drop them). Ranks exact, spectra and entries 1e-10; the rank-revealing move_core of the
+    same tensor likewise."""
+    rng = np.random.default_rng(5)
+    sigma = np.sort(rng.uniform(0.5, 2.0, 64))[::-1]
+    if spectrum == "duplicate":
+        sigma[5] = sigma[4]
+    elif spectrum == "graded":
+        sigma = np.logspace(0, -6, 64)
+    elif spectrum == "deficient":
+        sigma[-8:] = 0.0
+    def profiled_round(sig):
+        t = xg.TTTensor.from_cores(_tt_with_bond_spectrum(sig, 11), ctx=ctx)
+        ctx.profile(True)
+        try:
+            out = np.array(t.round(32, spectra=True))
+            counts = {k: ctx.profile_get(k)[0] for k in ("svd_refine", "svd_sweeps", "qr_gram", "qr")}
+        finally:
+            ctx.profile(False)
+        return t, out, counts
+
+    cores = _tt_with_bond_spectrum(sigma, 11)
+    xh = o.TT([c.copy() for c in cores])
+    x, sp, counts = profiled_round(sigma)
+    # the path each case is meant to take
+    if spectrum == "separated":
+        assert counts["svd_refine"] == 1 and counts["svd_sweeps"] == 0
+    if spectrum in ("duplicate", "graded"):
+        assert counts["svd_refine"] == 1 and counts["svd_sweeps"] == 1
+    if spectrum == "graded":
+        # the right-to-left move_core factors the 64 x 64 core of condition 1e6: one Householder
+        # QR more than for the well-conditioned spectrum, after the same Cholesky QR attempts
+        def profiled_move(sig):
+            t = xg.TTTensor.from_cores(_tt_with_bond_spectrum(sig, 11), ctx=ctx)
+            t.move_core(5, False)
+            ctx.profile(True)
+            try:
+                t.move_core(0, False)
+                return {k: ctx.profile_get(k)[0] for k in ("qr_gram", "qr")}
+            finally:
+                ctx.profile(False)
+        base = profiled_move(np.sort(np.random.default_rng(5).uniform(0.5, 2.0, 64))[::-1])
+        mc = profiled_move(sigma)
+        assert mc["qr"] == base["qr"] + 1 and mc["qr_gram"] == base["qr_gram"] >= 1
+    spr = []
+    o.tt_round(xh, 32, o.EPSILON, spr)
+    spr = np.concatenate(spr)
+    assert x.ranks() == xh.ranks
+    assert sp.shape == spr.shape and np.max(np.abs(sp - spr) / spr) < 1e-10
+    pos = np.random.default_rng(3).integers(0, 4, size=(64, 6))
+    assert rel_err(x.entries(pos), o.tt_entries(xh, pos)) < 1e-10
+    # rank-revealing move_core, both directions. Exact zeros put R_kk at rounding level,
+    # where the reference's signed rule (|R_kk| < 16 eps R_00, kept whenever LAPACK's R_00
+    # is negative) depends on the gauge earlier factorisations left: there the rank must
+    # lie between the true and the representation rank, as for the other exactly
+    # deficient inputs; everywhere else it is exact
+    y = xg.TTTensor.from_cores(cores, ctx=ctx)
+    yh = o.TT([c.copy() for c in cores])
+    for p in (5, 0):
+        y.move_core(p, False)
+        o.move_core(yh, p, keep_rank=False)
+        if spectrum == "deficient":
+            assert all(56 <= a <= 64 for a in y.ranks()[2:3]) and y.ranks()[:2] + y.ranks()[3:] == [4, 16, 16, 4]
+        else:
+            assert y.ranks() == yh.ranks
+        assert rel_err(y.entries(pos), o.tt_entries(yh, pos)) < 1e-10
+
+
 def test_round_eps_and_max_ranks(ctx, golden):
     r = golden("round")
     e = tt_of(r, "eps_in", canonicalized=False)
