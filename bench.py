@@ -254,7 +254,7 @@ def bench_round_dot(xg, ctx, torch, stream, steps, cpu):
     nrm64, dot64 = x.frob_norm(), xg.dot(x0, y)
     forms = {}
     try:
-        for form in ("tf32x3", "tf32"):
+        for form in ("tf32x3", "bf16x3", "tf32"):
             ctx.set_contraction_precision(form)
             tf = {"move_core": [], "round": [], "dot": []}
             for i in range(steps + 1):
@@ -343,6 +343,10 @@ def bench_adf(xg, ctx, torch, stream, iters, peak, cpu):
     return out
 
 
+FP64_NOMINAL_GFLOPS = 1250.0  # GB300 dense FP64, nominal
+FP32_NOMINAL_GFLOPS = 152 * 128 * 2 * 2.07  # 152 SMs x 128 FP32 FMA per clock x 2.07 GHz
+
+
 def config4_params(count, seed=SEED):
     """Shapes of the config-4 batch, instance by instance: (d, n, shift, rhs rank, start
     rank) with d ~ U{4..16}, n ~ U{2..8}, shift ~ U[0.1, 1], rhs rank ~ U{2..8}, start
@@ -398,8 +402,21 @@ def bench_batch(xg, ctx, count, steps):
             en, its, rep = xg.als_batch(As, xs, bs, variant=v, numHalfSweeps=8)
             ms.append(rep["milliseconds"])
         t = statistics.mean(ms)
+        # algorithmic flops: per instance, its CG iterations times its mean 1-site local matvec,
+        # plus one operator-environment push (the same contraction) per micro-step
+        flops = 0.0
+        for prm, (_, rk), it in zip(config4_params(count), saved, its):
+            d, n = prm[0], prm[1]
+            mv = matvec_cost(rk, [1] + [2] * (d - 1) + [1], [n] * d, 8)
+            mean_mv = statistics.mean(mv[k][0] for k in range(d))
+            flops += float(it) * mean_mv + 8 * (d - 1) * mean_mv
+        gfs = flops / (t / 1e3) / 1e9
+        # the FP64 form against the FP64 peak; the mixed form's CG runs in FP32 on the CUDA cores
+        peak, pname = (FP64_NOMINAL_GFLOPS, "FP64") if name == "fp64" else (FP32_NOMINAL_GFLOPS, "FP32 CUDA-core")
         out[name] = {"ms": t, "instances_per_s": count / (t / 1e3), "launch": {k: rep[k] for k in ("threads", "ctas_per_sm", "ctas", "tile")},
-                     "cg_iterations": int(its.sum()), "energy_sum": float(en.sum())}
+                     "cg_iterations": int(its.sum()), "energy_sum": float(en.sum()),
+                     "algorithmic_gflop": flops / 1e9, "gflop_per_s": gfs, "peak_frac": gfs / peak,
+                     "peak": f"{peak:.0f} GFLOP/s {pname}, of nominal (MEASURED_PEAKS.json has neither figure)"}
     out["mixed_speedup_vs_fp64"] = out["fp64"]["ms"] / out["mixed"]["ms"]
     return out
 
