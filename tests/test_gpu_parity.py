@@ -131,6 +131,30 @@ def test_move_core_qr_and_rank_revealing(ctx, golden):
         assert all(a <= b for a, b in zip(y.ranks(), zz.ranks))
 
 
+def test_move_core_keep_rank_wide_cores(ctx):
+    """keepRank move_core over cores with 128 columns (512 x 128 moving right, its transpose
+    moving left): the cluster QR's reflectors and the blocked WY formation of Q. Entries
+    against the oracle, cores orthonormal to rounding, ranks kept, core norm preserved."""
+    rng = np.random.default_rng(21)
+    n, ranks = 8, [1, 8, 64, 128, 64, 8, 1]
+    cores = [rng.standard_normal((ranks[k], n, ranks[k + 1])) / np.sqrt(ranks[k] * n) for k in range(6)]
+    xh = o.TT([c.copy() for c in cores])
+    pos = np.random.default_rng(4).integers(0, n, size=(64, 6))
+    ref = o.tt_entries(xh, pos)
+    x = xg.TTTensor.from_cores(cores, ctx=ctx)
+    for p in (5, 0, 3):
+        x.move_core(p, True)
+        assert x.ranks() == ranks[1:-1] and x.corePosition == p
+        assert rel_err(x.entries(pos), ref) < 1e-10
+        cs = x.get_cores()
+        for k in range(p):
+            m = cs[k].reshape(-1, cs[k].shape[2])
+            assert np.allclose(m.T @ m, np.eye(m.shape[1]), atol=1e-12)
+        for k in range(p + 1, len(cs)):
+            m = cs[k].reshape(cs[k].shape[0], -1)
+            assert np.allclose(m @ m.T, np.eye(m.shape[0]), atol=1e-12)
+
+
 def test_move_core_cholesky_qr_cfg2(ctx, golden):
     """Rank-revealing move_core of the d=32, n=4, rank-64 tensor (its 256 x 64 cores take
     the Cholesky QR): ranks kept, entries and norm against the reference, cores

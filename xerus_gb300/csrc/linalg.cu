@@ -1165,6 +1165,17 @@ __global__ void __launch_bounds__(kQ1Threads, 1) k_qr_cl1(QrArgs a, Qc1Layout la
 	}
 	cl.sync();  // every CTA has read the last partials before they are rewritten or freed
 	if (!a.want_q) return;
+	if (a.V_out) {
+		// the reflectors for a blocked Q formation outside: rows of this CTA, unit diagonal
+		for (long long e = tid; e < (long long)nl * kq; e += kQ1Threads) {
+			const int il = int(e / kq), c = int(e % kq), gi = r0 + il;
+			a.V_out[(long long)gi * kq + c] = gi == c ? 1.0 : (gi > c ? w(il, c) : 0.0);
+		}
+		if (me == 0)
+			for (int c = tid; c < kq; c += kQ1Threads) a.tau_out[c] = tau[c];
+		cl.sync();
+		return;
+	}
 	if (lay.wy) {
 		// Q = [I; 0] - V T V_top^T with the UT transform T^{-1} = diag(1/tau) + striu(V^T V)
 		// (Joffrain, Low, Quintana-Orti, van de Geijn, Van Zee, "Accumulating Householder
@@ -1636,6 +1647,35 @@ static int qr_cluster_size(int mw, int nw, QcLayout& lay) {
 	lay.kq = std::min(mw, nw);
 	if (lay.total() * sizeof(double) > kDynSmemMax) return 0;
 	return P;
+}
+
+bool launch_qr_reflectors(const QrArgs& a, cudaStream_t s) {
+	const int mw = a.transpose ? a.n : a.m, nw = a.transpose ? a.m : a.n;
+	if (a.pivot || !a.want_q || !a.V_out || !a.tau_out) return false;
+	Qc1Layout l1;
+	const int P1 = qr_cl1_size(mw, nw, false, l1);  // no compact-WY buffers: Q is not formed here
+	if (P1 <= 1 || l1.kq <= 64) return false;
+	func_attr_once(k_qr_cl1, cudaFuncAttributeMaxDynamicSharedMemorySize, int(kDynSmemMax));
+	func_attr_once(k_qr_cl1, cudaFuncAttributeNonPortableClusterSizeAllowed, 1);
+	cudaLaunchConfig_t cfg = {};
+	cfg.gridDim = dim3(P1);
+	cfg.blockDim = dim3(kQ1Threads);
+	cfg.dynamicSmemBytes = l1.total() * sizeof(double);
+	cfg.stream = s;
+	cudaLaunchAttribute at[1];
+	at[0].id = cudaLaunchAttributeClusterDimension;
+	at[0].val.clusterDim.x = P1;
+	at[0].val.clusterDim.y = 1;
+	at[0].val.clusterDim.z = 1;
+	cfg.attrs = at;
+	cfg.numAttrs = 1;
+	int clusters = 0;
+	if (cudaOccupancyMaxActiveClusters(&clusters, k_qr_cl1, &cfg) != cudaSuccess || clusters <= 0) {
+		cudaGetLastError();
+		return false;
+	}
+	XTT_CUDA(cudaLaunchKernelEx(&cfg, k_qr_cl1, a, l1));
+	return true;
 }
 
 void launch_qr(const QrArgs& a, cudaStream_t s) {

@@ -24,6 +24,10 @@ struct QrArgs {
 	int want_q = 1;             // 0: only C (the triangular factor) is written, Q is not formed
 	int rank_rule = 1;          // 0 with pivot: keep all min(m, n) rows of R (pivoting only)
 	double rank_tol = 16 * 2.220446049250313e-16;  // the rank rule: first k with |R_kk| < rank_tol R_00
+	// reflector output instead of Q (launch_qr_reflectors): V (m_w x k_q row-major, unit lower
+	// trapezoidal: the dlarfg vectors of the factored m_w x n_w matrix) and tau (k_q)
+	double* V_out = nullptr;
+	double* tau_out = nullptr;
 };
 
 struct SvdArgs {
@@ -59,6 +63,10 @@ inline double qr_work_flops(const QrArgs& a) {
 
 // Launchers (stream-ordered, asynchronous).
 void launch_qr(const QrArgs& a, cudaStream_t s);
+// The one-barrier cluster QR writing C and the reflectors (a.V_out, a.tau_out) instead of Q,
+// for callers that form Q by blocked WY products; false (nothing launched) where that kernel
+// does not take the shape (or forms Q itself by compact WY, k_q <= 64).
+bool launch_qr_reflectors(const QrArgs& a, cudaStream_t s);
 
 // transfer_core with keepRank of a small core in one launch (QR / LQ of core `from`, Q in
 // place, the triangular factor absorbed into core `to`), for the shapes transfer_small_fits accepts.

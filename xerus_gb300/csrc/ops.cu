@@ -693,11 +693,107 @@ static void gram_qr(Context& c, const QrArgs& a, int slot, int* flag) {
 	g->run(c, [&] { launches(As); });
 }
 
+// ------------------------------------------------------------ blocked WY Q formation
+// For factorisations with more than 64 columns, the cluster QR's backward accumulation of
+// Q runs one reflector (one cluster barrier and a column-wide FP64 update) per column.
+// Instead it writes the reflectors, and Q = B_0 B_1 .. [I; 0] is formed here by blocks of
+// kQbBlock reflectors in compact WY form, B_b = I - V_b T_b V_b^T (dlarft's forward T:
+// T_ii = tau_i, T(0:i, i) = -tau_i T(0:i, 0:i) V_b(:, 0:i)^T v_i), applied backward as
+// three FP64 GEMMs per block over the whole GPU: Q(j0:, j0:) -= V_b (T_b (V_b^T Q(j0:, j0:))).
+// Columns left of j0 are unit vectors with zeros below row j0, which B_b leaves unchanged.
+constexpr int kQbBlock = 32;
+static_assert(S_GQ_FIRST + 2 * kGqSlots <= S_QB, "scratch ids of the Gram QR and the blocked Q overlap");
+
+// T_b of one block from its Gram G = V_b^T V_b (jb x jb) and tau: thread r owns row r.
+__global__ void k_wy_t(const double* __restrict__ G, const double* __restrict__ tau, double* __restrict__ T, int jb) {
+	__shared__ double sG[kQbBlock][kQbBlock + 1];
+	__shared__ double sT[kQbBlock][kQbBlock + 1];
+	const int r = threadIdx.x;
+	for (int e = r; e < jb * jb; e += blockDim.x) sG[e / jb][e % jb] = G[e];
+	__syncwarp();
+	if (r < jb) {
+		for (int i = 0; i < jb; ++i) {
+			double v = 0.0;
+			if (r == i) {
+				v = tau[i];
+			} else if (r < i) {
+				double acc = 0.0;
+				for (int t = r; t < i; ++t) acc = fma(sT[r][t], sG[t][i], acc);
+				v = -tau[i] * acc;
+			}
+			sT[r][i] = v;
+		}
+		for (int i = 0; i < jb; ++i) T[r * jb + i] = sT[r][i];
+	}
+}
+
+// Q_w = [I_kq; 0] (mw x kq) at Q with row / column strides.
+__global__ void k_eye_rect(double* Q, int mw, int kq, long long sr, long long sc) {
+	for (long long e = blockIdx.x * (long long)blockDim.x + threadIdx.x; e < (long long)mw * kq;
+	     e += (long long)gridDim.x * blockDim.x) {
+		const int i = int(e / kq), c = int(e % kq);
+		Q[i * sr + c * sc] = i == c ? 1.0 : 0.0;
+	}
+}
+
+// Unpivoted QR with Q (tall, k_q > 64) by the cluster kernel's reflectors and the blocked
+// Q formation above; false (nothing done) where the cluster kernel does not take it.
+static bool qr_blocked_q(Context& c, QrArgs a) {
+	const bool tr = a.transpose != 0;
+	const int mw = tr ? a.n : a.m, nw = tr ? a.m : a.n, kq = std::min(mw, nw);
+	if (a.pivot || !a.want_q || kq <= 64 || mw < nw) return false;
+	const size_t nv = size_t(mw) * kq, nb2 = size_t(kQbBlock) * kQbBlock, nwk = size_t(kQbBlock) * kq;
+	double* V = c.scratch<double>(S_QB, nv + kq + 2 * nb2 + 2 * nwk);
+	double *tau = V + nv, *G = tau + kq, *T = G + nb2, *W1 = T + nb2, *W2 = W1 + nwk;
+	a.V_out = V;
+	a.tau_out = tau;
+	if (!launch_qr_reflectors(a, c.stream)) return false;
+	c.count_launch();
+	Fp64ContractionScope fp64(c);
+	// Q_w[i][col] at a.Q[i sr + col sc]: tr == 0, Q (m x k) ld k; tr == 1, Q^T (k x n) ld n
+	const long long sr = tr ? 1 : kq, sc = tr ? mw : 1, lq = (long long)mw * kq;
+	k_eye_rect<<<grid_for(nv), 256, 0, c.stream>>>(a.Q, mw, kq, sr, sc);
+	XTT_CUDA(cudaGetLastError());
+	c.count_launch();
+	auto mk = [](int M, int N, int K, const double* A, long long sAm, long long sAk, long long lenA, const double* B,
+	             long long sBk, long long sBn, long long lenB, double* C, long long sCm, long long sCn, long long lenC,
+	             double alpha, double beta) {
+		Gemm<double> g;
+		g.M = M; g.N = N; g.K = K;
+		g.A = A; g.sAm = sAm; g.sAk = sAk;
+		g.B = B; g.sBk = sBk; g.sBn = sBn;
+		g.C = C; g.sCm = sCm; g.sCn = sCn;
+		g.alpha = alpha; g.beta = beta;
+		g.lens(lenA, lenB, lenC);
+		return g;
+	};
+	for (int j0 = ((kq - 1) / kQbBlock) * kQbBlock; j0 >= 0; j0 -= kQbBlock) {
+		const int jb = std::min(kQbBlock, kq - j0), mr = mw - j0, nc = kq - j0;
+		const double* Vb = V + (long long)j0 * kq + j0;  // mr x jb, ld kq
+		const long long lv = (long long)nv - (long long)j0 * kq - j0;
+		double* Qb = a.Q + j0 * sr + j0 * sc;
+		const long long lqb = lq - (j0 * sr + j0 * sc);
+		gemm(c, mk(jb, jb, mr, Vb, 1, kq, lv, Vb, kq, 1, lv, G, jb, 1, (long long)nb2, 1.0, 0.0));  // V_b^T V_b
+		k_wy_t<<<1, 32, 0, c.stream>>>(G, tau + j0, T, jb);
+		XTT_CUDA(cudaGetLastError());
+		c.count_launch();
+		gemm(c, mk(jb, nc, mr, Vb, 1, kq, lv, Qb, sr, sc, lqb, W1, nc, 1, (long long)nwk, 1.0, 0.0));  // V_b^T Q
+		gemm(c, mk(jb, nc, jb, T, jb, 1, (long long)nb2, W1, nc, 1, (long long)nwk, W2, nc, 1, (long long)nwk, 1.0,
+		           0.0));  // T_b W1
+		gemm(c, mk(mr, nc, jb, Vb, kq, 1, lv, W2, nc, 1, (long long)nwk, Qb, sr, sc, lqb, -1.0, 1.0));  // Q -= V_b W2
+	}
+	return true;
+}
+
 // The rank-revealing QR of transfer_core / round: Cholesky QR where the context asks for
 // it and the shape fits, the pivoted Householder QR otherwise or when its gate fails.
 // Returns the rank when the host knows it already (the Cholesky QR keeps all columns),
 // else -1: the rank is then in *a.rank_out (not synchronised).
 static int rank_revealing_qr(Context& c, QrArgs& a) {
+	if (!a.pivot) {
+		ProfScope ps(c, "qr", qr_work_bytes(a), qr_work_flops(a));
+		if (qr_blocked_q(c, a)) return std::min(a.m, a.n);
+	}
 	if (c.gram_qr && gram_qr_fits(a)) {
 		ProfScope ps(c, "qr_gram", qr_work_bytes(a), qr_work_flops(a));
 		int* flag = c.d_ints + 12;
