@@ -1654,7 +1654,7 @@ bool launch_qr_reflectors(const QrArgs& a, cudaStream_t s) {
 	if (a.pivot || !a.want_q || !a.V_out || !a.tau_out) return false;
 	Qc1Layout l1;
 	const int P1 = qr_cl1_size(mw, nw, false, l1);  // no compact-WY buffers: Q is not formed here
-	if (P1 <= 1 || l1.kq <= 64) return false;
+	if (P1 <= 1) return false;
 	func_attr_once(k_qr_cl1, cudaFuncAttributeMaxDynamicSharedMemorySize, int(kDynSmemMax));
 	func_attr_once(k_qr_cl1, cudaFuncAttributeNonPortableClusterSizeAllowed, 1);
 	cudaLaunchConfig_t cfg = {};

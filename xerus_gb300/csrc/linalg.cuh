@@ -65,7 +65,7 @@ inline double qr_work_flops(const QrArgs& a) {
 void launch_qr(const QrArgs& a, cudaStream_t s);
 // The one-barrier cluster QR writing C and the reflectors (a.V_out, a.tau_out) instead of Q,
 // for callers that form Q by blocked WY products; false (nothing launched) where that kernel
-// does not take the shape (or forms Q itself by compact WY, k_q <= 64).
+// does not take the shape.
 bool launch_qr_reflectors(const QrArgs& a, cudaStream_t s);
 
 // transfer_core with keepRank of a small core in one launch (QR / LQ of core `from`, Q in

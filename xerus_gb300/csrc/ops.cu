@@ -693,18 +693,22 @@ static void gram_qr(Context& c, const QrArgs& a, int slot, int* flag) {
 	g->run(c, [&] { launches(As); });
 }
 
-// ------------------------------------------------------------ blocked WY Q formation
-// For factorisations with more than 64 columns, the cluster QR's backward accumulation of
-// Q runs one reflector (one cluster barrier and a column-wide FP64 update) per column.
-// Instead it writes the reflectors, and Q = B_0 B_1 .. [I; 0] is formed here by blocks of
-// kQbBlock reflectors in compact WY form, B_b = I - V_b T_b V_b^T (dlarft's forward T:
-// T_ii = tau_i, T(0:i, i) = -tau_i T(0:i, 0:i) V_b(:, 0:i)^T v_i), applied backward as
-// three FP64 GEMMs per block over the whole GPU: Q(j0:, j0:) -= V_b (T_b (V_b^T Q(j0:, j0:))).
-// Columns left of j0 are unit vectors with zeros below row j0, which B_b leaves unchanged.
+// ------------------------------------------------------------ blocked Householder QR
+// For factorisations with more than 64 columns (the keepRank moves of rank-128 sweeps), the
+// cluster QR spreads each column step over 16 SMs only, and its trailing updates are FP64
+// work those SMs retire at ~2 FMAs per clock. Blocked instead (dgeqrf's scheme): panels of
+// kQbBlock columns are factored by the cluster kernel, which writes their reflectors V_p
+// and tau; the trailing columns are updated as three FP64 GEMMs over the whole GPU,
+// A_2 -= V_p T_p^T (V_p^T A_2), with T_p dlarft's forward factor (T_ii = tau_i,
+// T(0:i, i) = -tau_i T(0:i, 0:i) V_p(:, 0:i)^T v_i); and Q = B_0 B_1 .. [I; 0] with
+// B_p = I - V_p T_p V_p^T is formed backward the same way, Q(j0:, j0:) -= V_p (T_p (V_p^T
+// Q(j0:, j0:))) (columns left of j0 are unit vectors with zeros below row j0, which B_p
+// leaves unchanged). The reflectors and R are those of the unblocked factorisation up to
+// rounding (the same dlarfg vectors, in the same order).
 constexpr int kQbBlock = 32;
-static_assert(S_GQ_FIRST + 2 * kGqSlots <= S_QB, "scratch ids of the Gram QR and the blocked Q overlap");
+static_assert(S_GQ_FIRST + 2 * kGqSlots <= S_QB, "scratch ids of the Gram QR and the blocked QR overlap");
 
-// T_b of one block from its Gram G = V_b^T V_b (jb x jb) and tau: thread r owns row r.
+// T_p of one panel from its Gram G = V_p^T V_p (jb x jb) and tau: thread r owns row r.
 __global__ void k_wy_t(const double* __restrict__ G, const double* __restrict__ tau, double* __restrict__ T, int jb) {
 	__shared__ double sG[kQbBlock][kQbBlock + 1];
 	__shared__ double sT[kQbBlock][kQbBlock + 1];
@@ -727,6 +731,22 @@ __global__ void k_wy_t(const double* __restrict__ G, const double* __restrict__ 
 	}
 }
 
+// dst[i][c] (row / column strides) = src[i * ss + c * sc] for i < m, c < n.
+__global__ void k_copy2d(double* dst, long long dr, long long dc, const double* src, long long sr, long long sc, int m,
+                         int n) {
+	for (long long e = blockIdx.x * (long long)blockDim.x + threadIdx.x; e < (long long)m * n;
+	     e += (long long)gridDim.x * blockDim.x) {
+		const int i = int(e / n), c = int(e % n);
+		dst[i * dr + c * dc] = src[i * sr + c * sc];
+	}
+}
+
+__global__ void k_zero2d(double* dst, long long dr, long long dc, int m, int n) {
+	for (long long e = blockIdx.x * (long long)blockDim.x + threadIdx.x; e < (long long)m * n;
+	     e += (long long)gridDim.x * blockDim.x)
+		dst[(e / n) * dr + (e % n) * dc] = 0.0;
+}
+
 // Q_w = [I_kq; 0] (mw x kq) at Q with row / column strides.
 __global__ void k_eye_rect(double* Q, int mw, int kq, long long sr, long long sc) {
 	for (long long e = blockIdx.x * (long long)blockDim.x + threadIdx.x; e < (long long)mw * kq;
@@ -736,25 +756,29 @@ __global__ void k_eye_rect(double* Q, int mw, int kq, long long sr, long long sc
 	}
 }
 
-// Unpivoted QR with Q (tall, k_q > 64) by the cluster kernel's reflectors and the blocked
-// Q formation above; false (nothing done) where the cluster kernel does not take it.
-static bool qr_blocked_q(Context& c, QrArgs a) {
+// Unpivoted QR with Q (tall, k_q > 64) blocked as above; false (nothing done) where the
+// cluster kernel does not take a panel.
+static bool qr_blocked(Context& c, const QrArgs& a) {
 	const bool tr = a.transpose != 0;
 	const int mw = tr ? a.n : a.m, nw = tr ? a.m : a.n, kq = std::min(mw, nw);
-	if (a.pivot || !a.want_q || kq <= 64 || mw < nw) return false;
-	const size_t nv = size_t(mw) * kq, nb2 = size_t(kQbBlock) * kQbBlock, nwk = size_t(kQbBlock) * kq;
-	double* V = c.scratch<double>(S_QB, nv + kq + 2 * nb2 + 2 * nwk);
-	double *tau = V + nv, *G = tau + kq, *T = G + nb2, *W1 = T + nb2, *W2 = W1 + nwk;
-	a.V_out = V;
-	a.tau_out = tau;
-	if (!launch_qr_reflectors(a, c.stream)) return false;
-	c.count_launch();
+	if (a.pivot || !a.want_q || kq <= 64 || mw < nw || mw - (kq - 1) / kQbBlock * kQbBlock < 48) return false;
+	const int np = (kq + kQbBlock - 1) / kQbBlock;
+	if (kq - (np - 1) * kQbBlock < 8) return false;  // every panel needs 8 columns for the cluster kernel
+	const size_t nb2 = size_t(kQbBlock) * kQbBlock, nwk = size_t(kQbBlock) * nw, nA = size_t(mw) * nw;
+	// working copy of A_w, the panels' reflectors (mw x kQbBlock each, rows from j0), tau,
+	// T per panel, the panel's R, and the GEMM temporaries
+	double* Wk = c.scratch<double>(S_QB, nA + size_t(np) * mw * kQbBlock + kq + size_t(np) * nb2 + 2 * nb2 + 2 * nwk);
+	double* Vall = Wk + nA;
+	double* tau = Vall + size_t(np) * mw * kQbBlock;
+	double* Tall = tau + kq;
+	double *G = Tall + size_t(np) * nb2, *Rp = G + nb2, *W1 = Rp + nb2, *W2 = W1 + nwk;
 	Fp64ContractionScope fp64(c);
-	// Q_w[i][col] at a.Q[i sr + col sc]: tr == 0, Q (m x k) ld k; tr == 1, Q^T (k x n) ld n
-	const long long sr = tr ? 1 : kq, sc = tr ? mw : 1, lq = (long long)mw * kq;
-	k_eye_rect<<<grid_for(nv), 256, 0, c.stream>>>(a.Q, mw, kq, sr, sc);
+	const long long asr = tr ? 1 : a.lda, asc = tr ? a.lda : 1;  // A_w[i][j] = A[i asr + j asc]
+	k_copy2d<<<grid_for(nA), 256, 0, c.stream>>>(Wk, nw, 1, a.A, asr, asc, mw, nw);
 	XTT_CUDA(cudaGetLastError());
 	c.count_launch();
+	// R (kq x nw) into a.C: tr == 0, C (kq x n) ld n; tr == 1, C (m x kq) ld kq = R^T
+	const long long csr = tr ? 1 : nw, csc = tr ? kq : 1;
 	auto mk = [](int M, int N, int K, const double* A, long long sAm, long long sAk, long long lenA, const double* B,
 	             long long sBk, long long sBn, long long lenB, double* C, long long sCm, long long sCn, long long lenC,
 	             double alpha, double beta) {
@@ -767,20 +791,60 @@ static bool qr_blocked_q(Context& c, QrArgs a) {
 		g.lens(lenA, lenB, lenC);
 		return g;
 	};
-	for (int j0 = ((kq - 1) / kQbBlock) * kQbBlock; j0 >= 0; j0 -= kQbBlock) {
-		const int jb = std::min(kQbBlock, kq - j0), mr = mw - j0, nc = kq - j0;
-		const double* Vb = V + (long long)j0 * kq + j0;  // mr x jb, ld kq
-		const long long lv = (long long)nv - (long long)j0 * kq - j0;
-		double* Qb = a.Q + j0 * sr + j0 * sc;
-		const long long lqb = lq - (j0 * sr + j0 * sc);
-		gemm(c, mk(jb, jb, mr, Vb, 1, kq, lv, Vb, kq, 1, lv, G, jb, 1, (long long)nb2, 1.0, 0.0));  // V_b^T V_b
-		k_wy_t<<<1, 32, 0, c.stream>>>(G, tau + j0, T, jb);
+	const long long lw = (long long)nA;
+	for (int p = 0; p < np; ++p) {
+		const int j0 = p * kQbBlock, jb = std::min(kQbBlock, kq - j0), mp = mw - j0, n2 = nw - j0 - jb;
+		double* Vp = Vall + size_t(p) * mw * kQbBlock;  // mp x jb, ld jb
+		double* Tp = Tall + size_t(p) * nb2;
+		QrArgs ap;
+		ap.A = Wk + (long long)j0 * nw + j0; ap.lda = nw; ap.m = mp; ap.n = jb; ap.transpose = 0; ap.pivot = 0;
+		ap.want_q = 1; ap.C = Rp; ap.Q = nullptr; ap.rank_out = nullptr; ap.V_out = Vp; ap.tau_out = tau + j0;
+		ap.work = nullptr;
+		if (!launch_qr_reflectors(ap, c.stream)) {
+			XTT_REQUIRE(p == 0, "internal: blocked QR panel does not fit the cluster kernel");
+			return false;  // nothing done yet
+		}
+		c.count_launch();
+		// R_pp (jb x jb) and zeros left of it in rows j0.., into C
+		k_copy2d<<<grid_for(size_t(jb) * jb), 256, 0, c.stream>>>(a.C + j0 * csr + j0 * csc, csr, csc, Rp, jb, 1, jb, jb);
+		if (j0 > 0) k_zero2d<<<grid_for(size_t(jb) * j0), 256, 0, c.stream>>>(a.C + j0 * csr, csr, csc, jb, j0);
+		XTT_CUDA(cudaGetLastError());
+		c.count_launch(j0 > 0 ? 2 : 1);
+		const long long lv = (long long)mp * jb;
+		gemm(c, mk(jb, jb, mp, Vp, 1, jb, lv, Vp, jb, 1, lv, G, jb, 1, (long long)nb2, 1.0, 0.0));  // V_p^T V_p
+		k_wy_t<<<1, 32, 0, c.stream>>>(G, tau + j0, Tp, jb);
 		XTT_CUDA(cudaGetLastError());
 		c.count_launch();
-		gemm(c, mk(jb, nc, mr, Vb, 1, kq, lv, Qb, sr, sc, lqb, W1, nc, 1, (long long)nwk, 1.0, 0.0));  // V_b^T Q
-		gemm(c, mk(jb, nc, jb, T, jb, 1, (long long)nb2, W1, nc, 1, (long long)nwk, W2, nc, 1, (long long)nwk, 1.0,
-		           0.0));  // T_b W1
-		gemm(c, mk(mr, nc, jb, Vb, kq, 1, lv, W2, nc, 1, (long long)nwk, Qb, sr, sc, lqb, -1.0, 1.0));  // Q -= V_b W2
+		if (n2 > 0) {
+			double* A2 = Wk + (long long)j0 * nw + j0 + jb;  // mp x n2, ld nw
+			const long long la2 = lw - ((long long)j0 * nw + j0 + jb);
+			gemm(c, mk(jb, n2, mp, Vp, 1, jb, lv, A2, nw, 1, la2, W1, n2, 1, (long long)nwk, 1.0, 0.0));  // V^T A2
+			gemm(c, mk(jb, n2, jb, Tp, 1, jb, (long long)nb2, W1, n2, 1, (long long)nwk, W2, n2, 1, (long long)nwk, 1.0,
+			           0.0));  // T^T W1
+			gemm(c, mk(mp, n2, jb, Vp, jb, 1, lv, W2, n2, 1, (long long)nwk, A2, nw, 1, la2, -1.0, 1.0));  // A2 -= V W2
+			// R_12: the panel rows of the updated trailing columns
+			k_copy2d<<<grid_for(size_t(jb) * n2), 256, 0, c.stream>>>(a.C + j0 * csr + (j0 + jb) * csc, csr, csc, A2, nw,
+			                                                          1, jb, n2);
+			XTT_CUDA(cudaGetLastError());
+			c.count_launch();
+		}
+	}
+	// Q_w[i][col] at a.Q[i qsr + col qsc]: tr == 0, Q (m x k) ld k; tr == 1, Q^T (k x n) ld n
+	const long long qsr = tr ? 1 : kq, qsc = tr ? mw : 1, lq = (long long)mw * kq;
+	k_eye_rect<<<grid_for(size_t(mw) * kq), 256, 0, c.stream>>>(a.Q, mw, kq, qsr, qsc);
+	XTT_CUDA(cudaGetLastError());
+	c.count_launch();
+	for (int p = np - 1; p >= 0; --p) {
+		const int j0 = p * kQbBlock, jb = std::min(kQbBlock, kq - j0), mr = mw - j0, nc = kq - j0;
+		const double* Vp = Vall + size_t(p) * mw * kQbBlock;
+		const double* Tp = Tall + size_t(p) * nb2;
+		const long long lv = (long long)mr * jb;
+		double* Qb = a.Q + j0 * qsr + j0 * qsc;
+		const long long lqb = lq - (j0 * qsr + j0 * qsc);
+		gemm(c, mk(jb, nc, mr, Vp, 1, jb, lv, Qb, qsr, qsc, lqb, W1, nc, 1, (long long)nwk, 1.0, 0.0));  // V^T Q
+		gemm(c, mk(jb, nc, jb, Tp, jb, 1, (long long)nb2, W1, nc, 1, (long long)nwk, W2, nc, 1, (long long)nwk, 1.0,
+		           0.0));  // T W1
+		gemm(c, mk(mr, nc, jb, Vp, jb, 1, lv, W2, nc, 1, (long long)nwk, Qb, qsr, qsc, lqb, -1.0, 1.0));  // Q -= V W2
 	}
 	return true;
 }
@@ -792,7 +856,7 @@ static bool qr_blocked_q(Context& c, QrArgs a) {
 static int rank_revealing_qr(Context& c, QrArgs& a) {
 	if (!a.pivot) {
 		ProfScope ps(c, "qr", qr_work_bytes(a), qr_work_flops(a));
-		if (qr_blocked_q(c, a)) return std::min(a.m, a.n);
+		if (qr_blocked(c, a)) return std::min(a.m, a.n);
 	}
 	if (c.gram_qr && gram_qr_fits(a)) {
 		ProfScope ps(c, "qr_gram", qr_work_bytes(a), qr_work_flops(a));
