@@ -505,6 +505,7 @@ bool exceeds_maximal_ranks(const Tensor& x) {
 // pivoted Householder QR. Q and C differ from Householder's by an orthogonal n_w x n_w
 // factor (Q C is the same): round uses them only through Q C-invariant products.
 constexpr int kGqSlots = 6;  // scratch ids per concurrent factorisation
+constexpr size_t kGraphCacheMax = 64;  // captured launch sequences kept per context
 constexpr int kGqMaxCols = 128;
 constexpr int kGqNsSteps = 3;
 
@@ -687,6 +688,13 @@ static void gram_qr(Context& c, const QrArgs& a, int slot, int* flag) {
 	for (auto& e : c.graph_cache)
 		if (e.first == key) g = e.second;
 	if (!g) {
+		if (c.graph_cache.size() >= kGraphCacheMax) {  // bounded: the oldest entry goes, idle on both streams
+			XTT_CUDA(cudaStreamSynchronize(c.own));
+			XTT_CUDA(cudaStreamSynchronize(c.aux));
+			XTT_CUDA(cudaStreamSynchronize(c.stream));
+			delete c.graph_cache.front().second;
+			c.graph_cache.erase(c.graph_cache.begin());
+		}
 		g = new ReplayGraph();
 		c.graph_cache.emplace_back(key, g);
 	}
