@@ -520,7 +520,7 @@ struct AdfData {
 }  // namespace
 
 // update_x at core k followed by move_core(k + 1, keepRank) in ONE launch when the core
-// fits the one-warp factorisation (ranks <= 8, at most 128 rows): the step, the QR of the
+// fits the narrow-core factorisation (ranks <= 8, at most 128 rows): the step, the QR of the
 // updated core and the absorption of R into core k + 1. False if it does not fit.
 static bool update_and_move_right(Tensor& x, int k, const double* G, const double* nrm) {
 	if (!(x.canonicalized && x.core_position == k)) return false;
@@ -532,11 +532,11 @@ static bool update_and_move_right(Tensor& x, int k, const double* G, const doubl
 	t.right = 1;
 	t.G = G;
 	t.nrm = nrm;
-	if (!transfer_warp_fits(t)) return false;
+	if (!transfer_narrow_fits(t)) return false;
 	Context& c = *x.ctx;
 	{
 		ProfScope ps(c, "qr");
-		launch_transfer_warp(t, c.stream);
+		launch_transfer_narrow(t, c.stream);
 	}
 	c.count_launch();
 	x.core_position = k + 1;

@@ -1396,15 +1396,15 @@ __global__ void __launch_bounds__(kQrSmallThreads) k_transfer_small(TransferArgs
 }
 
 // transfer_core with keepRank for narrow cores (at most 8 columns, at most 128 rows) by
-// ONE warp with the matrix in registers: lane l holds rows l, l + 32, .. of every column.
-// The same Householder QR as blk_qr (dlarfg conventions, reflectors below the diagonal,
-// dorg2r's backward Q formation) and the same absorption of R into the neighbour, with
-// warp shuffles in place of block barriers. R goes through 8 x 8 doubles of shared memory.
-// Its use is the ADF sweep, where it also applies the core's gradient step first (one
-// launch instead of two). Measured on GB300: a warp issues FP64 instructions one at a
-// time (~64 cycles each, independent ones included), so a one-warp kernel is bound by its
-// FP64 instruction count; plain moves take the 4-warp block kernel where it fits.
-constexpr int kTwCols = 8, kTwRptMax = 4, kTwMaxSlices = 16;
+// one CTA of four warps, the matrix in shared memory: the same Householder QR as blk_qr
+// (dlarfg conventions, reflectors below the diagonal, dorg2r's backward Q formation) and
+// the same absorption of R into the neighbour. Its use is the ADF sweep, where it also
+// applies the core's gradient step first (one launch instead of two). Measured on GB300:
+// a warp issues its FP64 instructions one at a time (~64 cycles each, independent ones
+// included), so the trailing columns' dot products and updates of a column step, which
+// are independent, go to different warps (each SM sub-partition has its own FP64
+// issue); the column's norm and reflector scalars stay one chain.
+constexpr int kTwCols = 8, kTwRptMax = 4, kTwMaxSlices = 16, kTwWarps = 4;
 
 template <int R>
 __device__ __forceinline__ double tree_sum(const double* v) {
@@ -1420,147 +1420,153 @@ __device__ __forceinline__ double warp_sum_d(double v) {
 	return v;
 }
 
-// RPT rows per lane (mw <= 32 RPT): the matrix in shared memory, lane l holding rows
-// l, l + 32, .. of every column; the column loops stay loops. A one-warp kernel runs each
-// instruction once, so straight-line (fully unrolled) code spends its time fetching
-// instructions: measured 50 us for a 48 x 6 move with ~6 cycles per issue waiting on the
-// instruction cache; looped, the body stays cached after the first column.
+// RPT rows per lane (mw <= 32 RPT): in every warp lane l covers rows l, l + 32, .. of the
+// columns that warp owns; column loops stay loops (compact code for instructions that
+// run once or a few times).
 template <int RPT>
-__global__ void __launch_bounds__(32) k_transfer_warp(TransferArgs t) {
+__global__ void __launch_bounds__(32 * kTwWarps) k_transfer_narrow(TransferArgs t) {
 	__shared__ double sA[32 * kTwRptMax][kTwCols + 1];
+	__shared__ double sV[32 * kTwRptMax][kTwCols + 1];
 	__shared__ double sR[kTwCols][kTwCols];
 	__shared__ double sTau[kTwCols];
-	__shared__ double sSl[32][kTwMaxSlices + 1];
 	__shared__ double sStep[kTwMaxSlices];
-	const int lane = threadIdx.x;
+	const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5, nt = blockDim.x;
 	const int mw = t.right ? t.r0 * t.nf : t.nf * t.r1, nw = t.right ? t.r1 : t.r0;
-#pragma unroll
-	for (int u = 0; u < RPT; ++u) {
-		const int row = lane + 32 * u;
 #pragma unroll 1
-		for (int c = 0; c < kTwCols; ++c)
-			sA[row][c] = (row < mw && c < nw) ? (t.right ? t.from[row * nw + c] : t.from[c * mw + row]) : 0.0;
+	for (int e = tid; e < 32 * RPT * kTwCols; e += nt) {
+		const int row = e / kTwCols, c = e % kTwCols;
+		sA[row][c] = (row < mw && c < nw) ? (t.right ? t.from[row * nw + c] : t.from[c * mw + row]) : 0.0;
 	}
 	if (t.G) {
-		// the ADF step on every slice i of core_from (rows (a, i), i = row mod n): each lane's
-		// partial slice sums, lane i adds slice i's partials and divides (the n divisions run
-		// side by side in the warp's lanes)
+		// the ADF step on every slice i of core_from (rows (a, i), i = row mod n): thread i adds
+		// slice i's squares and divides (the n divisions side by side), then all threads update
 		const int n = t.nf;
-#pragma unroll 1
-		for (int i = 0; i < n; ++i) sSl[lane][i] = 0.0;
-#pragma unroll
-		for (int u = 0; u < RPT; ++u) {
-			const int row = lane + 32 * u;
-			if (row < mw) {
-				double q = 0.0;
-#pragma unroll 1
-				for (int c = 0; c < nw; ++c) q = fma(t.G[row * nw + c], t.G[row * nw + c], q);
-				sSl[lane][row % n] += q;
-			}
-		}
-		__syncwarp();
-		if (lane < n) {
+		__syncthreads();
+		if (tid < n) {
 			double sum = 0.0;
 #pragma unroll 1
-			for (int l = 0; l < 32; ++l) sum += sSl[l][lane];
-			sStep[lane] = sum / t.nrm[lane];
-		}
-		__syncwarp();
-#pragma unroll
-		for (int u = 0; u < RPT; ++u) {
-			const int row = lane + 32 * u;
-			if (row < mw) {
-				const double st = sStep[row % n];
+			for (int row = tid; row < mw; row += n)
 #pragma unroll 1
-				for (int c = 0; c < nw; ++c) sA[row][c] = fma(st, t.G[row * nw + c], sA[row][c]);
-			}
+				for (int c = 0; c < nw; ++c) sum = fma(t.G[row * nw + c], t.G[row * nw + c], sum);
+			sStep[tid] = sum / t.nrm[tid];
 		}
-		__syncwarp();
+		__syncthreads();
+#pragma unroll 1
+		for (int e = tid; e < mw * nw; e += nt) {
+			const int row = e / nw, c = e % nw;
+			sA[row][c] = fma(sStep[row % n], t.G[e], sA[row][c]);
+		}
 	}
-	// Householder QR (dlarfg conventions); rows >= mw are zero
+	__syncthreads();
+	// Householder QR, one barrier per column: every warp reads column j into registers,
+	// forms ||x||^2 and the reflector scalars itself (the same instructions on the same
+	// data in every warp: identical results, the FP64 chains of different warps overlap)
+	// and the dot products x^T a_c of the columns it owns, then updates those columns,
+	// a_c -= tau (a_jc + scal x^T a_c) [1; scal x]. Column j itself is written (scaled
+	// below the diagonal, beta on it) by warp 0 after the barrier, while the next column's
+	// work, which does not read it, runs. Rows >= mw are zero.
+	double scal_prev = 1.0, beta_prev = 0.0;
 #pragma unroll 1
 	for (int j = 0; j < nw; ++j) {
+		double x[RPT];
+#pragma unroll
+		for (int u = 0; u < RPT; ++u) {
+			const int row = lane + 32 * u;
+			x[u] = row > j ? sA[row][j] : 0.0;
+		}
 		double pu[RPT];
 #pragma unroll
-		for (int u = 0; u < RPT; ++u) {
-			const int row = lane + 32 * u;
-			pu[u] = row > j ? sA[row][j] * sA[row][j] : 0.0;
-		}
+		for (int u = 0; u < RPT; ++u) pu[u] = x[u] * x[u];
 		const double xn2 = warp_sum_d(tree_sum<RPT>(pu));
-		const double alpha = sA[j][j];
 		double beta, tj, scal;
-		reflector_scalars(alpha, xn2, beta, tj, scal);
-		__syncwarp();
+		reflector_scalars(sA[j][j], xn2, beta, tj, scal);
+		if (warp == 0 && j > 0) {  // column j - 1, nobody reads it any more
 #pragma unroll
-		for (int u = 0; u < RPT; ++u) {
-			const int row = lane + 32 * u;
-			if (row > j) sA[row][j] *= scal;
+			for (int u = 0; u < RPT; ++u) {
+				const int row = lane + 32 * u;
+				if (row > j - 1) sA[row][j - 1] *= scal_prev;
+			}
+			if (lane == 0) sA[j - 1][j - 1] = beta_prev;
 		}
-		if (lane == 0) {
-			sA[j][j] = beta;
-			sTau[j] = tj;
-		}
-		__syncwarp();
-		// trailing columns: a_c -= tau (a_jc + v^T a_c) v, v = [1; x scal]
 #pragma unroll 1
-		for (int c = j + 1; c < nw; ++c) {
+		for (int c = j + 1 + warp; c < nw; c += kTwWarps) {
 			double pv[RPT];
 #pragma unroll
-			for (int u = 0; u < RPT; ++u) {
-				const int row = lane + 32 * u;
-				pv[u] = row > j ? sA[row][j] * sA[row][c] : (row == j ? sA[j][c] : 0.0);
-			}
-			const double wc = tj * warp_sum_d(tree_sum<RPT>(pv));
+			for (int u = 0; u < RPT; ++u) pv[u] = x[u] * sA[lane + 32 * u][c];
+			const double ajc = sA[j][c];
+			const double wc = tj * fma(scal, warp_sum_d(tree_sum<RPT>(pv)), ajc);
+			const double ws = wc * scal;
 #pragma unroll
 			for (int u = 0; u < RPT; ++u) {
 				const int row = lane + 32 * u;
-				if (row > j) sA[row][c] = fma(-wc, sA[row][j], sA[row][c]);
-				else if (row == j) sA[j][c] -= wc;
+				if (row > j) sA[row][c] = fma(-ws, x[u], sA[row][c]);
 			}
-			__syncwarp();
+			if (lane == 0) sA[j][c] = ajc - wc;
 		}
+		if (tid == 0) sTau[j] = tj;
+		scal_prev = scal;
+		beta_prev = beta;
+		__syncthreads();
 	}
-	// R
-#pragma unroll 1
-	for (int e = lane; e < kTwCols * kTwCols; e += 32) {
+	if (warp == 0 && nw > 0) {
+		const int j = nw - 1;
+#pragma unroll
+		for (int u = 0; u < RPT; ++u) {
+			const int row = lane + 32 * u;
+			if (row > j) sA[row][j] *= scal_prev;
+		}
+		if (lane == 0) sA[j][j] = beta_prev;
+	}
+	__syncthreads();
+	// R, and the reflectors copied aside (the Q formation reads them there while it
+	// overwrites sA column by column)
+	for (int e = tid; e < kTwCols * kTwCols; e += nt) {
 		const int i = e / kTwCols, c = e % kTwCols;
 		sR[i][c] = (i < nw && c < nw && c >= i) ? sA[i][c] : 0.0;
 	}
-	__syncwarp();
-	// Q in place of the reflectors (dorg2r, backward)
+#pragma unroll 1
+	for (int e = tid; e < 32 * RPT * kTwCols; e += nt) sV[e / kTwCols][e % kTwCols] = sA[e / kTwCols][e % kTwCols];
+	__syncthreads();
+	// Q in place of the reflectors (dorg2r, backward), one barrier per step: every warp
+	// takes v_j from the copy, updates the trailing columns it owns; warp 0 rewrites
+	// column j, which no warp reads in this step
 #pragma unroll 1
 	for (int j = nw - 1; j >= 0; --j) {
 		const double tj = sTau[j];
+		double v[RPT];
+#pragma unroll
+		for (int u = 0; u < RPT; ++u) {
+			const int row = lane + 32 * u;
+			v[u] = row > j ? sV[row][j] : 0.0;
+		}
 #pragma unroll 1
-		for (int c = j + 1; c < nw; ++c) {
+		for (int c = j + 1 + warp; c < nw; c += kTwWarps) {
 			double pv[RPT];
 #pragma unroll
-			for (int u = 0; u < RPT; ++u) {
-				const int row = lane + 32 * u;
-				pv[u] = row > j ? sA[row][j] * sA[row][c] : 0.0;
-			}
+			for (int u = 0; u < RPT; ++u) pv[u] = v[u] * sA[lane + 32 * u][c];
 			const double wc = tj * warp_sum_d(tree_sum<RPT>(pv));
 #pragma unroll
 			for (int u = 0; u < RPT; ++u) {
 				const int row = lane + 32 * u;
-				if (row > j) sA[row][c] = fma(-wc, sA[row][j], sA[row][c]);
-				else if (row == j) sA[j][c] = -wc;
+				if (row > j) sA[row][c] = fma(-wc, v[u], sA[row][c]);
 			}
-			__syncwarp();
+			if (lane == 0) sA[j][c] = -wc;
 		}
+		if (warp == 0) {
 #pragma unroll
-		for (int u = 0; u < RPT; ++u) {
-			const int row = lane + 32 * u;
-			sA[row][j] = row > j ? -tj * sA[row][j] : (row == j ? 1.0 - tj : 0.0);
+			for (int u = 0; u < RPT; ++u) {
+				const int row = lane + 32 * u;
+				sA[row][j] = row > j ? -tj * v[u] : (row == j ? 1.0 - tj : 0.0);
+			}
 		}
-		__syncwarp();
+		__syncthreads();
 	}
-	// the neighbour absorbs R (right: R * core_to; left: core_to * R^T), each lane reading
+	// the neighbour absorbs R (right: R * core_to; left: core_to * R^T), each thread reading
 	// whole columns (right) or rows (left) of core_to before writing them
 	if (t.right) {
 		const int n2 = t.nt * t.r2;
 #pragma unroll 1
-		for (int col = lane; col < n2; col += 32) {
+		for (int col = tid; col < n2; col += nt) {
 			double v[kTwCols];
 #pragma unroll
 			for (int k = 0; k < kTwCols; ++k) v[k] = k < nw ? t.to[k * n2 + col] : 0.0;
@@ -1576,7 +1582,7 @@ __global__ void __launch_bounds__(32) k_transfer_warp(TransferArgs t) {
 	} else {
 		const int m2 = t.rt * t.nt;
 #pragma unroll 1
-		for (int row = lane; row < m2; row += 32) {
+		for (int row = tid; row < m2; row += nt) {
 			double v[kTwCols];
 #pragma unroll
 			for (int k = 0; k < kTwCols; ++k) v[k] = k < nw ? t.to[row * nw + k] : 0.0;
@@ -1591,31 +1597,27 @@ __global__ void __launch_bounds__(32) k_transfer_warp(TransferArgs t) {
 		}
 	}
 	// Q: right, core_from (mw x nw); left, Q^T as core_from (nw x mw)
-#pragma unroll
-	for (int u = 0; u < RPT; ++u) {
-		const int row = lane + 32 * u;
-		if (row >= mw) continue;
 #pragma unroll 1
-		for (int c = 0; c < nw; ++c) {
-			if (t.right) t.from[row * nw + c] = sA[row][c];
-			else t.from[c * mw + row] = sA[row][c];
-		}
+	for (int e = tid; e < mw * nw; e += nt) {
+		const int row = e / nw, c = e % nw;
+		if (t.right) t.from[row * nw + c] = sA[row][c];
+		else t.from[c * mw + row] = sA[row][c];
 	}
 }
 
-bool transfer_warp_fits(const TransferArgs& t) {
+bool transfer_narrow_fits(const TransferArgs& t) {
 	const int mw = t.right ? t.r0 * t.nf : t.nf * t.r1, nw = t.right ? t.r1 : t.r0;
 	if (t.G && (!t.right || t.nf > kTwMaxSlices)) return false;
 	return nw >= 1 && nw <= kTwCols && mw >= nw && mw <= 32 * kTwRptMax;
 }
 
-void launch_transfer_warp(const TransferArgs& t, cudaStream_t s) {
-	XTT_REQUIRE(transfer_warp_fits(t), "internal: transfer_core shapes do not fit the one-warp kernel");
+void launch_transfer_narrow(const TransferArgs& t, cudaStream_t s) {
+	XTT_REQUIRE(transfer_narrow_fits(t), "internal: transfer_core shapes do not fit the narrow-core kernel");
 	const int mw = t.right ? t.r0 * t.nf : t.nf * t.r1;
-	if (mw <= 32) k_transfer_warp<1><<<1, 32, 0, s>>>(t);
-	else if (mw <= 64) k_transfer_warp<2><<<1, 32, 0, s>>>(t);
-	else if (mw <= 96) k_transfer_warp<3><<<1, 32, 0, s>>>(t);
-	else k_transfer_warp<4><<<1, 32, 0, s>>>(t);
+	if (mw <= 32) k_transfer_narrow<1><<<1, 32 * kTwWarps, 0, s>>>(t);
+	else if (mw <= 64) k_transfer_narrow<2><<<1, 32 * kTwWarps, 0, s>>>(t);
+	else if (mw <= 96) k_transfer_narrow<3><<<1, 32 * kTwWarps, 0, s>>>(t);
+	else k_transfer_narrow<4><<<1, 32 * kTwWarps, 0, s>>>(t);
 	XTT_CUDA(cudaGetLastError());
 }
 

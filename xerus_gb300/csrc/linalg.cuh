@@ -83,9 +83,9 @@ struct TransferArgs {
 };
 bool transfer_small_fits(const TransferArgs& t);
 void launch_transfer_small(const TransferArgs& t, cudaStream_t s);
-// One warp, registers: cores with at most 8 columns (of the factored matrix) and 128 rows.
-bool transfer_warp_fits(const TransferArgs& t);
-void launch_transfer_warp(const TransferArgs& t, cudaStream_t s);
+// One CTA of four warps: cores with at most 8 columns (of the factored matrix) and 128 rows.
+bool transfer_narrow_fits(const TransferArgs& t);
+void launch_transfer_narrow(const TransferArgs& t, cudaStream_t s);
 size_t qr_work_doubles(int m, int n);        // global workspace needed (0 if shared memory suffices)
 void launch_svd(const SvdArgs& a, cudaStream_t s);
 size_t svd_work_doubles(int m, int n);

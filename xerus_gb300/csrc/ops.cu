@@ -889,14 +889,15 @@ void transfer_core(Tensor& x, int from, int to, bool rr) {
 		t.r0 = int(r0); t.nf = int(nf); t.r1 = int(r1);
 		t.right = to == from + 1;
 		t.rt = int(x.ranks[to]); t.nt = int(x.n(to)); t.r2 = int(x.ranks[to + 1]);
-		if (transfer_warp_fits(t) || transfer_small_fits(t)) {
+		if (transfer_narrow_fits(t) || transfer_small_fits(t)) {
 			QrArgs q;  // for the declared work only
 			q.m = t.right ? int(r0 * nf) : int(r0); q.n = t.right ? int(r1) : int(nf * r1); q.transpose = t.right ? 0 : 1;
 			ProfScope ps(c, "qr", qr_work_bytes(q), qr_work_flops(q));
-			// the 4-warp kernel where it fits: on GB300 one warp issues its FP64 instructions one
-			// at a time (~64 cycles each, no overlap within a warp), four warps overlap theirs
-			if (transfer_small_fits(t)) launch_transfer_small(t, c.stream);
-			else launch_transfer_warp(t, c.stream);
+			// the narrow-core kernel where it fits (measured 28 vs 39 us for 48 x 6), else the
+			// block one: on GB300 one warp issues its FP64 instructions one at a time (~64 cycles
+			// each, no overlap within a warp); both spread independent columns over four warps
+			if (transfer_narrow_fits(t)) launch_transfer_narrow(t, c.stream);
+			else launch_transfer_small(t, c.stream);
 			c.count_launch();
 			return;
 		}
