@@ -131,12 +131,15 @@ def test_move_core_qr_and_rank_revealing(ctx, golden):
         assert all(a <= b for a, b in zip(y.ranks(), zz.ranks))
 
 
-def test_move_core_keep_rank_wide_cores(ctx):
-    """keepRank move_core over cores with 128 columns (512 x 128 moving right, its transpose
-    moving left): the cluster QR's reflectors and the blocked WY formation of Q. Entries
-    against the oracle, cores orthonormal to rounding, ranks kept, core norm preserved."""
+@pytest.mark.parametrize("mid", [128, 72, 100])
+def test_move_core_keep_rank_wide_cores(ctx, mid):
+    """keepRank move_core over cores with more than 64 columns (512 x mid moving right, its
+    transpose moving left): the blocked Householder QR (32-column panels, the last one of
+    8 columns for mid = 72; mid = 100 leaves a 4-column panel, which the cluster kernel
+    does not take, so the unblocked factorisation runs). Entries against the oracle,
+    cores orthonormal to rounding, ranks kept."""
     rng = np.random.default_rng(21)
-    n, ranks = 8, [1, 8, 64, 128, 64, 8, 1]
+    n, ranks = 8, [1, 8, 64, mid, 64, 8, 1]
     cores = [rng.standard_normal((ranks[k], n, ranks[k + 1])) / np.sqrt(ranks[k] * n) for k in range(6)]
     xh = o.TT([c.copy() for c in cores])
     pos = np.random.default_rng(4).integers(0, n, size=(64, 6))
