@@ -110,7 +110,10 @@ int xtt_context_set_contraction_precision(xtt_context* ctx, int terms);
  * accumulation in tensor memory), FP64 row-major device matrices with leading
  * dimensions lda, ldb, ldc; terms = 3 splits each operand into two TF32 pieces
  * (FP32-level products), 6 into three BF16 pieces (FP32-level products on the
- * 16-bit MMA path), 1 is plain TF32. The building block of the precision forms
+ * 16-bit MMA path), 1 is plain TF32; terms = 2 runs the CUDA-core double-float
+ * tiles of the mixed local solves' residual updates instead (each FP64 operand as
+ * an FP32 pair, error-free FMA products, TwoSum accumulation: ~1e-15 of
+ * sum |a b|). The building block of the precision forms
  * (no reference counterpart: the reference multiplies in FP64 through BLAS,
  * src/xerus/blasLapackWrapper.cpp:96-147); exposed to check it against an FP64
  * product. Asynchronous on the context's stream. */

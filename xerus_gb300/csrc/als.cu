@@ -119,6 +119,138 @@ struct CoreTiles {
 	__device__ T tiles(const Gemm<T>& g, Grp& grp) { return gemm_tiles(g, grp.rank(), grp.size(), *sm); }
 };
 
+// Double-float tiles for the refinement's residual updates r -= ||r|| M d: FP64
+// operands split on load into an FP32 pair hi + lo (hi the leading 24 significand
+// bits, lo the next 29 rounded to 24: relative error ~2^-47), each product formed
+// error-free with an FMA (hi*hi + its rounding error + the two cross terms) and
+// summed by TwoSum into an FP32 pair, renormalised every fourth product: ~13 FP32
+// instructions per product, where GB300's FP64 pipe retires one DFMA in the time of
+// ~64 FFMAs. Sums of 384 products come out within ~1e-15 of sum |a b| (mean; FP64:
+// ~2e-16). The intrinsics keep
+// the compiler from contracting the error-free steps into FMAs.
+struct DfSmem {
+	float2 As[32][33];  // [k][m]: (hi, lo)
+	float2 Bs[32][33];  // [k][n]
+};
+
+__device__ __forceinline__ float2 df_split(double d) {
+	const unsigned long long u = (unsigned long long)__double_as_longlong(d);
+	const int e = int((u >> 52) & 0x7ffu) - 1023;
+	if (e >= -74 && e <= 127) {  // hi and the scale of lo are normal FP32 numbers
+		const unsigned sign = unsigned(u >> 32) & 0x80000000u;
+		const float hi = __uint_as_float(sign | (unsigned(e + 127) << 23) | unsigned((u >> 29) & 0x7fffffu));
+		const float scale = __uint_as_float(sign | (unsigned(e + 75) << 23));  // +-2^(e-52)
+		return make_float2(hi, __fmul_rn(__uint2float_rn(unsigned(u & 0x1fffffffu)), scale));
+	}
+	return make_float2(__double2float_rn(d), 0.f);  // zero, and magnitudes FP32 cannot split
+}
+
+__device__ __forceinline__ void df_fma(float2 a, float2 b, float& s, float& c) {
+	const float p = __fmul_rn(a.x, b.x);
+	float e = __fmaf_rn(a.x, b.x, -p);
+	e = __fmaf_rn(a.x, b.y, e);
+	e = __fmaf_rn(a.y, b.x, e);
+	const float t = __fadd_rn(s, p);
+	const float bp = __fsub_rn(t, s);
+	const float err = __fadd_rn(__fsub_rn(s, __fsub_rn(t, bp)), __fsub_rn(p, bp));
+	s = t;
+	c = __fadd_rn(c, __fadd_rn(err, e));
+}
+
+// s + c -> s + c with |c| <= ulp(s) / 2 (Fast2Sum); keeps the low part's own rounding small
+__device__ __forceinline__ void df_renorm(float& s, float& c) {
+	const float t = __fadd_rn(s, c);
+	c = __fsub_rn(c, __fsub_rn(t, s));
+	s = t;
+}
+
+// Output tile `tile` of g (32 x 32, 2 x 2 outputs per thread, as gemm_tile; no epilogue sum).
+__device__ void gemm_tile_df(const Gemm<double>& g, long long tile, DfSmem& sm) {
+	const int tid = threadIdx.x;
+	const long long tn = g.tiles_n(), tm = g.tiles_m();
+	const long long b = tile / (tm * tn);
+	const long long rem = tile - b * tm * tn;
+	const int m0 = int(rem / tn) * 32, n0 = int(rem % tn) * 32;
+	const double* A = g.A + b * g.sAb;
+	const double* B = g.B + b * g.sBb;
+	const int tx = tid & 15, ty = tid >> 4;
+	float s[2][2] = {{0.f, 0.f}, {0.f, 0.f}}, c[2][2] = {{0.f, 0.f}, {0.f, 0.f}};
+	const bool a_k_fast = (g.sAk == 1);
+	const bool b_n_fast = (g.sBn == 1) || (g.sBk != 1);
+	for (int k0 = 0; k0 < g.K; k0 += 32) {
+#pragma unroll
+		for (int t = 0; t < 4; ++t) {
+			const int e = tid + t * kGemmThreads;
+			const int hi = e >> 5, lo = e & 31;
+			{
+				const int mm = a_k_fast ? hi : lo, kk = a_k_fast ? lo : hi;
+				const int gm = m0 + mm, gk = k0 + kk;
+				sm.As[kk][mm] = df_split((gm < g.M && gk < g.K) ? A[g.offA(gm, gk)] : 0.0);
+			}
+			{
+				const int nn = b_n_fast ? lo : hi, kk = b_n_fast ? hi : lo;
+				const int gn = n0 + nn, gk = k0 + kk;
+				sm.Bs[kk][nn] = df_split((gn < g.N && gk < g.K) ? B[g.offB(gk, gn)] : 0.0);
+			}
+		}
+		__syncthreads();
+		const int kmax = min(32, g.K - k0);
+#pragma unroll 4
+		for (int kk = 0; kk < kmax; ++kk) {
+			const float2 a0 = sm.As[kk][ty], a1 = sm.As[kk][ty + 16];
+			const float2 b0 = sm.Bs[kk][tx], b1 = sm.Bs[kk][tx + 16];
+			df_fma(a0, b0, s[0][0], c[0][0]);
+			df_fma(a0, b1, s[0][1], c[0][1]);
+			df_fma(a1, b0, s[1][0], c[1][0]);
+			df_fma(a1, b1, s[1][1], c[1][1]);
+			if ((kk & 3) == 3) {  // every fourth product (accuracy ~1e-15 of sum |a b| at K = 384)
+				df_renorm(s[0][0], c[0][0]);
+				df_renorm(s[0][1], c[0][1]);
+				df_renorm(s[1][0], c[1][0]);
+				df_renorm(s[1][1], c[1][1]);
+			}
+		}
+		__syncthreads();
+	}
+	double* C = g.C + b * g.sCb;
+#pragma unroll
+	for (int i = 0; i < 2; ++i)
+#pragma unroll
+		for (int j = 0; j < 2; ++j) {
+			const int gm = m0 + ty + 16 * i, gn = n0 + tx + 16 * j;
+			if (gm < g.M && gn < g.N) {
+				const long long o = g.offC(gm, gn);
+				const double acc = double(s[i][j]) + double(c[i][j]);
+				C[o] = (g.beta == 0.0) ? g.alpha * acc : g.alpha * acc + g.beta * C[o];
+			}
+		}
+}
+
+struct DfTiles {
+	DfSmem* sm;
+	template <class Grp>
+	__device__ double tiles(const Gemm<double>& g, Grp& grp) {
+		const long long nt = g.tiles();
+		for (long long t = grp.rank(); t < nt; t += grp.size()) gemm_tile_df(g, t, *sm);
+		return 0.0;
+	}
+};
+
+__global__ void __launch_bounds__(kGemmThreads) k_gemm_df(Gemm<double> g) {
+	__shared__ DfSmem sm;
+	const long long nt = g.tiles();
+	for (long long t = blockIdx.x; t < nt; t += gridDim.x) gemm_tile_df(g, t, sm);
+}
+
+void gemm_df(Context& c, const Gemm<double>& g) {
+	check_gemm(g);
+	const long long nt = g.tiles();
+	if (nt == 0) return;
+	k_gemm_df<<<unsigned(std::min<long long>(nt, 4LL * c.num_sms)), kGemmThreads, 0, c.stream>>>(g);
+	XTT_CUDA(cudaGetLastError());
+	c.count_launch();
+}
+
 template <class T, class Grp, class E>
 __device__ bool matvec_dev(const MatvecPlan<T>& plan, const T* in, T* out, const T* dotv, E& eng, Grp& grp,
                            T& blk_dot) {
@@ -234,11 +366,18 @@ __global__ void __launch_bounds__(kGemmThreads) k_cg(CgParams<T> a, Grp grp, int
 	if (Grp::kCluster) grp.sync();
 }
 
-// Mixed precision: FP64 residual r = b - M x, FP32 CG for M d = r / ||r||, x += ||r|| d.
+// Mixed precision (iterative refinement): the residual r = b - M x is formed in FP64,
+// each correction M d = r / ||r|| is solved by CG in FP32, x += ||r|| d, and r is then
+// updated as r -= ||r|| M d with M d in double-float arithmetic (DfTiles). An update's
+// error is ~2^-47 ||M|| ||d|| ||r||: relative to the residual it corrects, not to ||b||,
+// so the updated residual follows the true one to FP64 level at a fraction of an FP64
+// operator application. When the updated residual meets the target while the updates
+// could have drifted by more than half the target (their residual norms summed, times
+// 2^-47, times an allowance of 1024 for ||M|| ||d||), the FP64 residual confirms it.
 struct MixedParams {
 	MatvecPlan<double> p64;
 	CgParams<float> inner;   // inner.b = rhs32, inner.x = d
-	double *x, *q64;
+	double *x, *q64, *r64;   // q64: operator products; r64: the residual
 	const double* b;
 	long long n;
 	double tol;
@@ -247,10 +386,29 @@ struct MixedParams {
 	int* sticky;             // set once FP32 corrections stalled; later solves skip them
 	int* status = nullptr;   // device status (the tensor-core engine's bounded waits)
 	float* part = nullptr;   // the tensor-core engine's split-K partials
+	int* arrivals = nullptr; // and its per-tile arrival counters (zeroed before the launch)
 };
 
-template <class Grp, class E64, class E32>
-__device__ void mixed_body(const MixedParams& a, E64& e64, E32& e32, Grp& grp, int* out_i, double* out_d) {
+// r = b - M x in FP64 (r64), returns ||r||^2 (identical in every CTA); false on a barrier timeout.
+template <class Grp, class E64>
+__device__ bool fp64_residual(const MixedParams& a, E64& e64, Grp& grp, double* sc, double& rr) {
+	const long long gt = grp.rank() * (long long)blockDim.x + threadIdx.x;
+	const long long gs = (long long)grp.size() * blockDim.x;
+	double dummy;
+	if (!matvec_dev(a.p64, a.x, a.q64, (const double*)nullptr, e64, grp, dummy) || !grp.sync()) return false;
+	double l = 0;
+	for (long long i = gt; i < a.n; i += gs) {
+		const double ri = a.b[i] - a.q64[i];
+		a.r64[i] = ri;
+		l += ri * ri;
+	}
+	bool ok = true;
+	rr = grp.total(block_sum(l, sc), ok);
+	return ok;
+}
+
+template <class Grp, class E64, class E32, class EDF>
+__device__ void mixed_body(const MixedParams& a, E64& e64, E32& e32, EDF& edf, Grp& grp, int* out_i, double* out_d) {
 	__shared__ double sc[32];
 	const long long gt = grp.rank() * (long long)blockDim.x + threadIdx.x;
 	const long long gs = (long long)grp.size() * blockDim.x;
@@ -258,43 +416,58 @@ __device__ void mixed_body(const MixedParams& a, E64& e64, E32& e32, Grp& grp, i
 	double bl = 0;
 	for (long long i = gt; i < a.n; i += gs) bl += a.b[i] * a.b[i];
 	const double bb = grp.total(block_sum(bl, sc), ok);
+	const double tol2 = a.tol * a.tol * bb;
+	// drift allowance of the double-float updates (see above): 2^-47 * 1024 = 2^-37
+	const double drift_limit = 0.5 * a.tol * sqrt(bb) * 137438953472.0;  // 2^37
 	int iters = 0, refs = 0;
-	double rel = 0, rr_prev = 0, nr_prev = 0;
+	double rel = 0, rr = 0, drift = 0;  // drift: sum of the residual norms updated in double-float
 	bool reached = false;
-	for (int ref = 0; ok && ref <= a.max_refine; ++ref) {
-		double dummy;
-		if (!matvec_dev(a.p64, a.x, a.q64, (const double*)nullptr, e64, grp, dummy)) break;
-		if (!grp.sync()) break;
-		double l = 0;
-		for (long long i = gt; i < a.n; i += gs) {
-			const double ri = a.b[i] - a.q64[i];
-			a.q64[i] = ri;
-			l += ri * ri;
-		}
-		const double rr = grp.total(block_sum(l, sc), ok);
-		if (!ok) break;
-		if (ref > 0 && !(rr < rr_prev)) {
-			// the FP32 correction did not help: take it back, the FP64 polish finishes
-			for (long long i = gt; i < a.n; i += gs) a.x[i] -= nr_prev * double(a.inner.x[i]);
-			rel = bb > 0 ? sqrt(rr_prev / bb) : 0.0;
-			break;
-		}
+	ok = ok && fp64_residual(a, e64, grp, sc, rr);
+	for (int ref = 0; ok; ++ref) {
 		rel = bb > 0 ? sqrt(rr / bb) : 0.0;
-		if (rr <= a.tol * a.tol * bb) {
-			reached = true;
-			break;
+		if (rr <= tol2) {
+			if (!(drift > drift_limit)) {
+				reached = true;
+				break;
+			}
+			// confirm against the FP64 residual; refinement goes on from it if it falls short
+			drift = 0;
+			if (!fp64_residual(a, e64, grp, sc, rr)) break;
+			rel = bb > 0 ? sqrt(rr / bb) : 0.0;
+			if (rr <= tol2) {
+				reached = true;
+				break;
+			}
 		}
-		if (ref == a.max_refine) break;
+		if (ref >= a.max_refine) break;
 		const double nr = sqrt(rr), inr = 1.0 / nr;
-		rr_prev = rr;
-		nr_prev = nr;
-		for (long long i = gt; i < a.n; i += gs) const_cast<float*>(a.inner.b)[i] = float(a.q64[i] * inr);
+		for (long long i = gt; i < a.n; i += gs) const_cast<float*>(a.inner.b)[i] = float(a.r64[i] * inr);
 		if (!grp.sync()) break;
 		const CgOut o = cg_body(a.inner, e32, grp);
 		iters += o.iterations;
-		for (long long i = gt; i < a.n; i += gs) a.x[i] += nr * double(a.inner.x[i]);
-		if (!grp.sync()) break;
+		for (long long i = gt; i < a.n; i += gs) {
+			const double di = double(a.inner.x[i]);
+			a.x[i] += nr * di;
+			a.q64[i] = di;
+		}
 		++refs;
+		double dummy;
+		if (!grp.sync() || !matvec_dev(a.p64, a.q64, a.q64, (const double*)nullptr, edf, grp, dummy) || !grp.sync()) break;
+		double l = 0;
+		for (long long i = gt; i < a.n; i += gs) {
+			const double ri = a.r64[i] - nr * a.q64[i];
+			a.r64[i] = ri;
+			l += ri * ri;
+		}
+		const double rn = grp.total(block_sum(l, sc), ok);
+		if (!ok) break;
+		if (!(rn < rr)) {
+			// the FP32 correction did not help: take it back, the FP64 polish finishes
+			for (long long i = gt; i < a.n; i += gs) a.x[i] -= nr * double(a.inner.x[i]);
+			break;
+		}
+		drift += nr;
+		rr = rn;
 	}
 	if (grp.rank() == 0 && threadIdx.x == 0) {
 		out_i[0] += iters;
@@ -307,7 +480,7 @@ __device__ void mixed_body(const MixedParams& a, E64& e64, E32& e32, Grp& grp, i
 }
 
 template <class Grp>
-__global__ void __launch_bounds__(kGemmThreads) k_cg_mixed(MixedParams a, Grp grp, int* out_i, double* out_d) {
+__global__ void __launch_bounds__(kGemmThreads, Grp::kCluster ? 1 : 2) k_cg_mixed(MixedParams a, Grp grp, int* out_i, double* out_d) {
 	if (a.sticky && __ldcg(a.sticky) != 0) {  // an earlier solve of this sweep showed FP32 does not help
 		if (blockIdx.x == 0 && threadIdx.x == 0) *a.flag = 1;
 		return;
@@ -315,11 +488,13 @@ __global__ void __launch_bounds__(kGemmThreads) k_cg_mixed(MixedParams a, Grp gr
 	__shared__ union U {
 		GemmSmem<double> d;
 		GemmSmem<float> f;
+		DfSmem df;
 		__device__ U() {}
 	} sm;
 	CoreTiles<double> e64{&sm.d};
 	CoreTiles<float> e32{&sm.f};
-	mixed_body(a, e64, e32, grp, out_i, out_d);
+	DfTiles edf{&sm.df};
+	mixed_body(a, e64, e32, edf, grp, out_i, out_d);
 	if (Grp::kCluster) grp.sync();
 }
 
@@ -331,10 +506,14 @@ __global__ void __launch_bounds__(kGemmThreads) k_cg_mixed_tc(MixedParams a, Gri
 		return;
 	}
 	extern __shared__ __align__(1024) unsigned char tc_dyn[];
-	__shared__ GemmSmem<double> sm64;
+	__shared__ union U {
+		GemmSmem<double> d;
+		DfSmem df;
+		__device__ U() {}
+	} sm64;
 	__shared__ __align__(8) uint64_t bars[2];
 	__shared__ uint32_t s_tmem;
-	__shared__ int s_ok, s_last;
+	__shared__ int s_ok, s_last, s_fix;
 	__shared__ float fred[32];
 	const int warp = threadIdx.x >> 5;
 	if (warp == 0) tc::tmem_alloc(&s_tmem, tc::kPN);
@@ -348,9 +527,10 @@ __global__ void __launch_bounds__(kGemmThreads) k_cg_mixed_tc(MixedParams a, Gri
 	tc::fence_before_sync();
 	__syncthreads();
 	tc::fence_after_sync();
-	tc::TcEngine e32{tc_dyn, bars, &s_ok, &s_last, fred, s_tmem, 0u, a.status, a.part};
-	CoreTiles<double> e64{&sm64};
-	mixed_body(a, e64, e32, grp, out_i, out_d);
+	tc::TcEngine e32{tc_dyn, bars, &s_ok, &s_last, fred, s_tmem, 0u, a.status, a.part, a.arrivals, &s_fix};
+	CoreTiles<double> e64{&sm64.d};
+	DfTiles edf{&sm64.df};
+	mixed_body(a, e64, e32, edf, grp, out_i, out_d);
 	__syncthreads();
 	// a wait gave up: wait (bounded) once more for the MMAs in flight before freeing TMEM
 	if (threadIdx.x == 0 && !s_ok && s_last >= 0) tc::mbar_wait(&bars[s_last & 1], uint32_t((s_last >> 1) & 1));
@@ -675,8 +855,9 @@ CgResult local_solve(Context& c, const LocalShape& s, const double* L, const dou
 		float* u3 = c.scratch<float>(S_ALS_FIRST + 30, matvec_tmp_elems(s, 2));
 		const MatvecPlan<float> p32 =
 		    make_matvec_plan<float>(s, f, f + nL, nA2 ? f + nL + nA1 : nullptr, f + nL + nA1 + nA2, u1, u2, u3);
-		bool persistent = true;  // the engine tabulates K offsets for at most 512 per stage
-		for (int i = 0; i < p32.ns; ++i) persistent = persistent && p32.g[i].K <= tc::kPMaxChunks * tc::kTileK;
+		bool persistent = true;  // the engine tabulates K offsets for at most 512 per stage, < 2^31 outputs
+		for (int i = 0; i < p32.ns; ++i)
+			persistent = persistent && p32.g[i].K <= tc::kPMaxChunks * tc::kTileK && tc::stage_fits(p32.g[i]);
 		if (persistent) {
 			// one cooperative launch: FP64 refinement, FP32 CG with tensor-core operator stages
 			MixedParams m;
@@ -694,6 +875,7 @@ CgResult local_solve(Context& c, const LocalShape& s, const double* L, const dou
 			m.inner.zero_guess = 1;
 			m.x = x;
 			m.q64 = c.scratch<double>(S_ALS_FIRST + 25, n);
+			m.r64 = c.scratch<double>(S_ALS_FIRST + 23, n);
 			m.b = b;
 			m.n = n;
 			m.tol = tol;
@@ -707,8 +889,14 @@ CgResult local_solve(Context& c, const LocalShape& s, const double* L, const dou
 			XTT_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, k_cg_mixed_tc, kGemmThreads, smem));
 			const int G = std::max(1, occ) * c.num_sms;
 			long long part_elems = 1;
-			for (int i = 0; i < p32.ns; ++i) part_elems = std::max(part_elems, tc::split_k_partials(p32.g[i], G));
+			int split_tiles = 1;
+			for (int i = 0; i < p32.ns; ++i) {
+				part_elems = std::max(part_elems, tc::split_k_partials(p32.g[i], G));
+				split_tiles = std::max(split_tiles, tc::split_k_tiles(p32.g[i], G));
+			}
 			m.part = c.scratch<float>(S_ALS_FIRST + 9, size_t(part_elems));
+			m.arrivals = c.scratch<int>(S_ALS_FIRST + 10, size_t(split_tiles));
+			XTT_CUDA(cudaMemsetAsync(m.arrivals, 0, sizeof(int) * size_t(split_tiles), c.stream));
 			GridGroup g{GridBarrier{c.d_barrier, c.d_barrier + 1, c.d_status}, c.scratch<double>(S_ALS_FIRST + 26, 2 * size_t(G)), 0};
 			void* args[] = {&m, &g, &oi, &od};
 			{
@@ -765,6 +953,7 @@ CgResult local_solve(Context& c, const LocalShape& s, const double* L, const dou
 		m.inner.zero_guess = 1;
 		m.x = x;
 		m.q64 = c.scratch<double>(S_ALS_FIRST + 25, n);
+		m.r64 = c.scratch<double>(S_ALS_FIRST + 23, n);
 		m.b = b;
 		m.n = n;
 		m.tol = tol;

@@ -178,14 +178,15 @@ int xtt_gemm_tc(xtt_context* ctx, int64_t m, int64_t n, int64_t k, const double*
 		ARG(ctx && A && B && C, "NULL argument");
 		ARG(m > 0 && n > 0 && k > 0 && m < (1 << 30) && n < (1 << 30) && k < (1 << 30), "illegal GEMM size");
 		ARG(lda >= k && ldb >= n && ldc >= n, "leading dimension smaller than the row");
-		ARG(terms == 1 || terms == 3 || terms == 6, "terms must be 1, 3 or 6");
+		ARG(terms == 1 || terms == 2 || terms == 3 || terms == 6, "terms must be 1, 2, 3 or 6");
 		xtt::Gemm<double> g;
 		g.M = int(m); g.N = int(n); g.K = int(k);
 		g.A = A; g.sAm = lda; g.sAk = 1;
 		g.B = B; g.sBk = ldb; g.sBn = 1;
 		g.C = C; g.sCm = ldc; g.sCn = 1;
 		g.lens((m - 1) * lda + k, (k - 1) * ldb + n, (m - 1) * ldc + n);
-		xtt::gemm_tc(*ctx->c, g, terms);
+		if (terms == 2) xtt::gemm_df(*ctx->c, g);
+		else xtt::gemm_tc(*ctx->c, g, terms);
 	});
 }
 
