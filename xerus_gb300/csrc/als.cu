@@ -177,23 +177,19 @@ __device__ void gemm_tile_df(const Gemm<double>& g, long long tile, DfSmem& sm) 
 	float s[2][2] = {{0.f, 0.f}, {0.f, 0.f}}, c[2][2] = {{0.f, 0.f}, {0.f, 0.f}};
 	const bool a_k_fast = (g.sAk == 1);
 	const bool b_n_fast = (g.sBn == 1) || (g.sBk != 1);
+	// the next K slab is fetched into registers while the current one is multiplied
+	GemmSlab<double> r;
+	gemm_slab_load(g, A, B, m0, n0, 0, a_k_fast, b_n_fast, r);
 	for (int k0 = 0; k0 < g.K; k0 += 32) {
 #pragma unroll
 		for (int t = 0; t < 4; ++t) {
-			const int e = tid + t * kGemmThreads;
-			const int hi = e >> 5, lo = e & 31;
-			{
-				const int mm = a_k_fast ? hi : lo, kk = a_k_fast ? lo : hi;
-				const int gm = m0 + mm, gk = k0 + kk;
-				sm.As[kk][mm] = df_split((gm < g.M && gk < g.K) ? A[g.offA(gm, gk)] : 0.0);
-			}
-			{
-				const int nn = b_n_fast ? lo : hi, kk = b_n_fast ? hi : lo;
-				const int gn = n0 + nn, gk = k0 + kk;
-				sm.Bs[kk][nn] = df_split((gn < g.N && gk < g.K) ? B[g.offB(gk, gn)] : 0.0);
-			}
+			int am, ak, bn, bk;
+			gemm_slab_index<double>(tid + t * kGemmThreads, a_k_fast, b_n_fast, am, ak, bn, bk);
+			sm.As[ak][am] = df_split(r.a[t]);
+			sm.Bs[bk][bn] = df_split(r.b[t]);
 		}
 		__syncthreads();
+		if (k0 + 32 < g.K) gemm_slab_load(g, A, B, m0, n0, k0 + 32, a_k_fast, b_n_fast, r);
 		const int kmax = min(32, g.K - k0);
 #pragma unroll 4
 		for (int kk = 0; kk < kmax; ++kk) {
@@ -354,7 +350,7 @@ __device__ CgOut cg_body(const CgParams<T>& a, E& sm, Grp& grp) {
 }
 
 template <class T, class Grp>
-__global__ void __launch_bounds__(kGemmThreads) k_cg(CgParams<T> a, Grp grp, int* out_i, double* out_d) {
+__global__ void __launch_bounds__(kGemmThreads, Grp::kCluster ? 1 : 2) k_cg(CgParams<T> a, Grp grp, int* out_i, double* out_d) {
 	if (a.gate && __ldcg(a.gate) == 0) return;  // uniform: every block reads the same flag
 	__shared__ GemmSmem<T> sm;
 	CoreTiles<T> eng{&sm};

@@ -81,8 +81,40 @@ struct GemmSmem {
 	T Bs[32][33];  // [k][n]
 };
 
+// The 32 x 32 operand slabs of K range [k0, k0 + 32): thread t holds elements
+// t + 256 j (j < 4) of each, fetched from global memory into registers; stored
+// into the shared-memory slabs by gemm_slab_store with the same index map.
+template <class T>
+struct GemmSlab {
+	T a[4], b[4];
+};
+
+template <class T>
+__device__ __forceinline__ void gemm_slab_index(int e, bool kfast_a, bool nfast_b, int& am, int& ak, int& bn, int& bk) {
+	const int hi = e >> 5, lo = e & 31;
+	am = kfast_a ? hi : lo;
+	ak = kfast_a ? lo : hi;
+	bn = nfast_b ? lo : hi;
+	bk = nfast_b ? hi : lo;
+}
+
+template <class T>
+__device__ __forceinline__ void gemm_slab_load(const Gemm<T>& g, const T* A, const T* B, int m0, int n0, int k0,
+                                               bool a_k_fast, bool b_n_fast, GemmSlab<T>& r) {
+#pragma unroll
+	for (int t = 0; t < 4; ++t) {
+		int am, ak, bn, bk;
+		gemm_slab_index<T>(threadIdx.x + t * kGemmThreads, a_k_fast, b_n_fast, am, ak, bn, bk);
+		const int gm = m0 + am, gka = k0 + ak, gn = n0 + bn, gkb = k0 + bk;
+		r.a[t] = (gm < g.M && gka < g.K) ? A[g.offA(gm, gka)] : T(0);
+		r.b[t] = (gn < g.N && gkb < g.K) ? B[g.offB(gkb, gn)] : T(0);
+	}
+}
+
 // Computes output tile `tile` of g with all 256 threads of the block. Returns,
-// in thread 0 only, sum over the tile of C .* D when g.D is set (else 0).
+// in thread 0 only, sum over the tile of C .* D when g.D is set (else 0). The next
+// K slab is fetched into registers while the current one is multiplied, so the
+// global (L2) latency of a slab overlaps the arithmetic of the one before.
 template <class T>
 __device__ T gemm_tile(const Gemm<T>& g, long long tile, GemmSmem<T>& sm) {
 	const int tid = threadIdx.x;
@@ -96,23 +128,18 @@ __device__ T gemm_tile(const Gemm<T>& g, long long tile, GemmSmem<T>& sm) {
 	T acc00 = 0, acc01 = 0, acc10 = 0, acc11 = 0;
 	const bool a_k_fast = (g.sAk == 1);
 	const bool b_n_fast = (g.sBn == 1) || (g.sBk != 1);
+	GemmSlab<T> r;
+	gemm_slab_load(g, A, B, m0, n0, 0, a_k_fast, b_n_fast, r);
 	for (int k0 = 0; k0 < g.K; k0 += 32) {
 #pragma unroll
 		for (int t = 0; t < 4; ++t) {
-			const int e = tid + t * kGemmThreads;
-			const int hi = e >> 5, lo = e & 31;
-			{
-				const int mm = a_k_fast ? hi : lo, kk = a_k_fast ? lo : hi;
-				const int gm = m0 + mm, gk = k0 + kk;
-				sm.As[kk][mm] = (gm < g.M && gk < g.K) ? A[g.offA(gm, gk)] : T(0);
-			}
-			{
-				const int nn = b_n_fast ? lo : hi, kk = b_n_fast ? hi : lo;
-				const int gn = n0 + nn, gk = k0 + kk;
-				sm.Bs[kk][nn] = (gn < g.N && gk < g.K) ? B[g.offB(gk, gn)] : T(0);
-			}
+			int am, ak, bn, bk;
+			gemm_slab_index<T>(tid + t * kGemmThreads, a_k_fast, b_n_fast, am, ak, bn, bk);
+			sm.As[ak][am] = r.a[t];
+			sm.Bs[bk][bn] = r.b[t];
 		}
 		__syncthreads();
+		if (k0 + 32 < g.K) gemm_slab_load(g, A, B, m0, n0, k0 + 32, a_k_fast, b_n_fast, r);
 		const int kmax = min(32, g.K - k0);
 		for (int kk = 0; kk < kmax; ++kk) {
 			const T a0 = sm.As[kk][ty], a1 = sm.As[kk][ty + 16];
