@@ -577,8 +577,22 @@ AdfResult adf(Tensor& x, const int64_t* positions, const double* values, long lo
 		ReplayGraph start_graph, sweep_graph;
 		const bool graphs = !c.profiling;
 		auto start = [&] {
-			move_core(x, 0, true);
-			for (int k = d - 1; k > 0; --k) D.backward(k);
+			// move_core(0): from a canonical position p the moves p -> 0 one step at a time,
+			// each backward stack B_k on the aux stream as soon as core k is right-orthogonal
+			// (at once for k > p), beside the next move
+			if (!x.canonicalized) {
+				move_core(x, 0, true);
+				for (int k = d - 1; k > 0; --k) D.backward(k);
+			} else {
+				const int p = int(x.core_position);
+				for (int k = d - 1; k > 0; --k) {
+					if (k <= p) move_core(x, k - 1, true);
+					c.fork();
+					OnAux on(c);
+					D.backward(k);
+				}
+				c.join();
+			}
 			D.res_grad(0, 0, x.core[0], D.G, 1.0);
 		};
 		auto sweep = [&] {
