@@ -439,7 +439,11 @@ __device__ void mixed_body(const MixedParams& a, E64& e64, E32& e32, EDF& edf, G
 		const double nr = sqrt(rr), inr = 1.0 / nr;
 		for (long long i = gt; i < a.n; i += gs) const_cast<float*>(a.inner.b)[i] = float(a.r64[i] * inr);
 		if (!grp.sync()) break;
-		const CgOut o = cg_body(a.inner, e32, grp);
+		// the correction solve need not reduce its residual below half of what the target
+		// still asks for (fewer FP32 iterations on the last correction)
+		CgParams<float> inner = a.inner;
+		inner.tol = fmin(0.5, fmax(a.inner.tol, 0.5 * a.tol * sqrt(bb) / nr));
+		const CgOut o = cg_body(inner, e32, grp);
 		iters += o.iterations;
 		for (long long i = gt; i < a.n; i += gs) {
 			const double di = double(a.inner.x[i]);

@@ -411,8 +411,11 @@ __global__ void __launch_bounds__(kCcThreads) k_cg_cluster_mixed(CcArgs a) {
 		for (int e = tid; e < n; e += kCcThreads) v.b[e] = float(r64[e] * inr);
 		__syncthreads();  // the FP32 CG below overwrites the region that held the FP64 iterate
 		double irel = 0;
-		iters += cc_cg<float>(s, me, P, b0, bwl, v.mv(s), v.pf, v.x, v.r, v.p, v.q, v.b, true, a.inner_tol,
-		                      a.max_iter, fslots, fbc, a.status, irel);
+		// the correction solve need not reduce its residual below half of what the target
+		// still asks for (fewer FP32 iterations on the last correction)
+		const double itol = fmin(0.5, fmax(double(a.inner_tol), 0.5 * a.tol * sqrt(bb) / nr));
+		iters += cc_cg<float>(s, me, P, b0, bwl, v.mv(s), v.pf, v.x, v.r, v.p, v.q, v.b, true, itol, a.max_iter,
+		                      fslots, fbc, a.status, irel);
 		for (int e = tid; e < n; e += kCcThreads) {
 			const int rho = e / bwl, b = e - rho * bwl;
 			double* xp = a.x + (size_t)rho * s.rb + b0 + b;
