@@ -68,8 +68,10 @@ def test_gemm_tc_strided_operands(ctx):
 
 
 @pytest.mark.parametrize("m,n,k", [(128, 64, 32), (300, 200, 100), (7, 5, 3), (1024, 128, 384), (64, 512, 1000),
-                                   (256, 130, 8)])
+                                   (256, 130, 8), (384, 128, 1024), (100, 60, 333)])
 def test_gemm_double_float_matches_fp64(ctx, m, n, k):
+    """K is split across CTAs (parts summed in order) where the tiles leave SMs idle:
+    (64, 512, 1000), (384, 128, 1024) and (100, 60, 333)."""
     g = torch.Generator(device="cpu").manual_seed(m * 131 + n * 17 + k)
     A = torch.randn(m, k, generator=g, dtype=torch.float64).cuda()
     B = torch.randn(k, n, generator=g, dtype=torch.float64).cuda()

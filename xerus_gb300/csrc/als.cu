@@ -164,8 +164,9 @@ __device__ __forceinline__ void df_renorm(float& s, float& c) {
 	s = t;
 }
 
-// Output tile `tile` of g (32 x 32, 2 x 2 outputs per thread, as gemm_tile; no epilogue sum).
-__device__ void gemm_tile_df(const Gemm<double>& g, long long tile, DfSmem& sm) {
+// Output tile `tile` of g (32 x 32, 2 x 2 outputs per thread, as gemm_tile; no epilogue
+// sum) over the K range [kb, ke) (ke <= 0: all of K).
+__device__ void gemm_tile_df(const Gemm<double>& g, long long tile, DfSmem& sm, int kb = 0, int ke = 0) {
 	const int tid = threadIdx.x;
 	const long long tn = g.tiles_n(), tm = g.tiles_m();
 	const long long b = tile / (tm * tn);
@@ -178,9 +179,12 @@ __device__ void gemm_tile_df(const Gemm<double>& g, long long tile, DfSmem& sm) 
 	const bool a_k_fast = (g.sAk == 1);
 	const bool b_n_fast = (g.sBn == 1) || (g.sBk != 1);
 	// the next K slab is fetched into registers while the current one is multiplied
+	const int kend = ke > 0 ? min(ke, g.K) : g.K;
+	Gemm<double> gk = g;  // K bounded to the range: the loads zero-fill beyond it
+	gk.K = kend;
 	GemmSlab<double> r;
-	gemm_slab_load(g, A, B, m0, n0, 0, a_k_fast, b_n_fast, r);
-	for (int k0 = 0; k0 < g.K; k0 += 32) {
+	gemm_slab_load(gk, A, B, m0, n0, kb, a_k_fast, b_n_fast, r);
+	for (int k0 = kb; k0 < kend; k0 += 32) {
 #pragma unroll
 		for (int t = 0; t < 4; ++t) {
 			int am, ak, bn, bk;
@@ -189,8 +193,8 @@ __device__ void gemm_tile_df(const Gemm<double>& g, long long tile, DfSmem& sm) 
 			sm.Bs[bk][bn] = df_split(r.b[t]);
 		}
 		__syncthreads();
-		if (k0 + 32 < g.K) gemm_slab_load(g, A, B, m0, n0, k0 + 32, a_k_fast, b_n_fast, r);
-		const int kmax = min(32, g.K - k0);
+		if (k0 + 32 < kend) gemm_slab_load(gk, A, B, m0, n0, k0 + 32, a_k_fast, b_n_fast, r);
+		const int kmax = min(32, kend - k0);
 #pragma unroll 4
 		for (int kk = 0; kk < kmax; ++kk) {
 			const float2 a0 = sm.As[kk][ty], a1 = sm.As[kk][ty + 16];
@@ -238,13 +242,59 @@ __global__ void __launch_bounds__(kGemmThreads) k_gemm_df(Gemm<double> g) {
 	for (long long t = blockIdx.x; t < nt; t += gridDim.x) gemm_tile_df(g, t, sm);
 }
 
+// Split K: CTA (tile, part) writes the part's products (alpha 1, beta 0) into C's layout at
+// part_base + part * span; k_gemm_df_sum adds the parts in order and applies alpha, beta.
+__global__ void __launch_bounds__(kGemmThreads) k_gemm_df_split(Gemm<double> g, int kchunk, double* part_base,
+                                                                 long long span) {
+	__shared__ DfSmem sm;
+	const long long nt = g.tiles();
+	const int part = int(blockIdx.x / nt);
+	Gemm<double> gp = g;
+	gp.C = part_base + part * span;
+	gp.alpha = 1.0;
+	gp.beta = 0.0;
+	gemm_tile_df(gp, blockIdx.x % nt, sm, part * kchunk, (part + 1) * kchunk);
+}
+
+__global__ void k_gemm_df_sum(Gemm<double> g, int S, const double* part_base, long long span) {
+	const long long mn = (long long)g.M * g.N, total = (long long)g.batch * mn;
+	for (long long e = blockIdx.x * (long long)blockDim.x + threadIdx.x; e < total;
+	     e += (long long)gridDim.x * blockDim.x) {
+		const long long b = e / mn, r = e - b * mn;
+		const int m = int(r / g.N), n = int(r - (long long)m * g.N);
+		const long long o = b * g.sCb + g.offC(m, n);
+		double acc = 0.0;
+		for (int s = 0; s < S; ++s) acc += part_base[s * span + o];
+		g.C[o] = g.beta == 0.0 ? g.alpha * acc : g.alpha * acc + g.beta * g.C[o];
+	}
+}
+
 void gemm_df(Context& c, const Gemm<double>& g) {
 	check_gemm(g);
 	const long long nt = g.tiles();
 	if (nt == 0) return;
-	k_gemm_df<<<unsigned(std::min<long long>(nt, 4LL * c.num_sms)), kGemmThreads, 0, c.stream>>>(g);
+	// split K when the tiles leave SMs idle: at least two 32-deep slabs per part
+	int S = 1;
+	if (nt < c.num_sms && g.K >= 128) {
+		S = int(std::min<long long>(8, (3 * c.num_sms / 2 + nt - 1) / nt));
+		S = std::max(1, std::min(S, g.K / 64));
+	}
+	if (S == 1) {
+		k_gemm_df<<<unsigned(std::min<long long>(nt, 4LL * c.num_sms)), kGemmThreads, 0, c.stream>>>(g);
+		XTT_CUDA(cudaGetLastError());
+		c.count_launch();
+		return;
+	}
+	const int kchunk = ((g.K + S - 1) / S + 31) / 32 * 32;
+	S = (g.K + kchunk - 1) / kchunk;
+	const long long span = g.max_off_C() + 1;
+	double* part = c.scratch<double>(S_ALS_FIRST + 12, size_t(S) * size_t(span));
+	k_gemm_df_split<<<unsigned(nt * S), kGemmThreads, 0, c.stream>>>(g, kchunk, part, span);
+	const long long total = (long long)g.batch * g.M * g.N;
+	k_gemm_df_sum<<<unsigned(std::min<long long>((total + 255) / 256, 8LL * c.num_sms)), 256, 0, c.stream>>>(g, S, part,
+	                                                                                                    span);
 	XTT_CUDA(cudaGetLastError());
-	c.count_launch();
+	c.count_launch(2);
 }
 
 template <class T, class Grp, class E>
@@ -1156,8 +1206,11 @@ struct AlsState {
 		s.K2 = S == 2 ? int(A.ranks[cur + 2]) : 1;
 		return s;
 	}
-	// the operator and rhs pushes are independent (separate scratch): rhs on the aux stream
+	// the operator and rhs pushes are independent (separate scratch): rhs on the aux stream;
+	// with `df` (the mixed form) their large GEMMs run in double-float tiles
+	bool df = false;
 	void push_left(int k) {
+		DfGemmScope dfs(c, df);
 		c.fork();
 		{
 			OnAux aux(c);
@@ -1177,6 +1230,7 @@ struct AlsState {
 		                           x.dims[kc] == x.dims[slot]),
 		            "index dimensions do not coincide (the two-site decreasing sweep contracts core k into the right "
 		            "environment of bond k+2, which needs equal neighbouring ranks)");
+		DfGemmScope dfs(c, df);
 		c.fork();
 		{
 			OnAux aux(c);
@@ -1345,6 +1399,9 @@ AlsReport als(const Tensor* Ap, Tensor& x, const Tensor& b, const AlsOptions& o)
 		for (int k = 1; k < d; ++k) rmax[k] = std::max(x.ranks[k], red[k - 1]);
 	}
 	AlsState s(c, A, x, bw, o, mode, norm_b);
+	// the mixed form's environments from double-float GEMMs (~1e-15 of sum |a b|): its local
+	// problems are solved to the FP64 target for these environments
+	s.df = o.precision != XTT_PRECISION_FP64;
 	// stacks: one buffer per family, a slot per bond 0..d
 	{
 		std::vector<size_t> oop(d + 2, 0), orh(d + 2, 0);

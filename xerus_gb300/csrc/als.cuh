@@ -249,10 +249,6 @@ bool cluster_local_solve(Context& c, const LocalShape& s, const double* L, const
                          const double* R, const double* b, double* x, double tol, int max_iter, int precision,
                          int* flag = nullptr, const int* gate = nullptr);
 
-// C = alpha A B + beta C with the double-float tile engine of the mixed solves'
-// residual updates (FP64 operands as FP32 pairs on the CUDA cores); one launch.
-void gemm_df(Context& c, const Gemm<double>& g);
-
 // y = M x once (FP64), host-launched chain.
 void local_matvec(Context& c, const LocalShape& s, const double* L, const double* A1, const double* A2,
                   const double* R, const double* x, double* y);

@@ -41,6 +41,9 @@ struct Context {
 	// `tc_active` is set, which those three entry points do for their duration.
 	int contraction_terms = 0;
 	int tc_active = 0;
+	// while set (DfGemmScope), FP64 GEMMs of at least kDfGemmMinFlops run in double-float
+	// tiles (FP32 pairs, ~1e-15 of sum |a b|): the environment pushes of the mixed sweeps
+	int df_gemm = 0;
 	bool gram_qr = false;  // rank-revealing QRs by Cholesky QR where well-conditioned (GramQrScope)
 	// CUDA graphs of fixed launch sequences, by the shapes and buffers they were captured with
 	std::vector<std::pair<std::vector<long long>, struct ReplayGraph*>> graph_cache;
@@ -237,6 +240,16 @@ bool gemm_tc_tma(Context& c, const Gemm<T>& g, int terms);
 
 // Stream-ordered helpers.
 void gemm(Context& c, const Gemm<double>& g);
+// C = alpha A B + beta C in double-float tiles (FP64 operands as FP32 pairs on the CUDA
+// cores, error-free products, TwoSum sums; K split across CTAs when the tiles leave SMs idle)
+void gemm_df(Context& c, const Gemm<double>& g);
+constexpr double kDfGemmMinFlops = 4e6;
+struct DfGemmScope {
+	Context& c;
+	int saved;
+	DfGemmScope(Context& cc, bool on) : c(cc), saved(cc.df_gemm) { c.df_gemm = on ? 1 : saved; }
+	~DfGemmScope() { c.df_gemm = saved; }
+};
 void gemm_f(Context& c, const Gemm<float>& g);
 void copy_d2d(Context& c, double* dst, const double* src, size_t count);
 void fill(Context& c, double* dst, double v, size_t count);
