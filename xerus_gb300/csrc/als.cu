@@ -417,9 +417,12 @@ __global__ void __launch_bounds__(kGemmThreads, Grp::kCluster ? 1 : 2) k_cg(CgPa
 // updated as r -= ||r|| M d with M d in double-float arithmetic (DfTiles). An update's
 // error is ~2^-47 ||M|| ||d|| ||r||: relative to the residual it corrects, not to ||b||,
 // so the updated residual follows the true one to FP64 level at a fraction of an FP64
-// operator application. When the updated residual meets the target while the updates
-// could have drifted by more than half the target (their residual norms summed, times
-// 2^-47, times an allowance of 1024 for ||M|| ||d||), the FP64 residual confirms it.
+// operator application. An update whose residual norm would take the summed norms of
+// the double-float updates past half the target's drift budget (times 2^-47, times an
+// allowance of 1024 for ||M|| ||d||) runs in FP64 instead, so from a poor start the
+// first, large correction is exact and the small ones that follow are cheap. Should
+// the updated residual meet the target while the double-float updates could have
+// drifted by more than that, the FP64 residual confirms it.
 struct MixedParams {
 	MatvecPlan<double> p64;
 	CgParams<float> inner;   // inner.b = rhs32, inner.x = d
@@ -501,8 +504,15 @@ __device__ void mixed_body(const MixedParams& a, E64& e64, E32& e32, EDF& edf, G
 			a.q64[i] = di;
 		}
 		++refs;
+		// a large correction (||r|| still a sizeable part of ||b||, as from a poor start) is
+		// applied with FP64 products, which add no drift; the others in double-float
+		const bool df = !(drift + nr > drift_limit);
 		double dummy;
-		if (!grp.sync() || !matvec_dev(a.p64, a.q64, a.q64, (const double*)nullptr, edf, grp, dummy) || !grp.sync()) break;
+		if (!grp.sync()) break;
+		if (!(df ? matvec_dev(a.p64, a.q64, a.q64, (const double*)nullptr, edf, grp, dummy)
+		         : matvec_dev(a.p64, a.q64, a.q64, (const double*)nullptr, e64, grp, dummy)) ||
+		    !grp.sync())
+			break;
 		double l = 0;
 		for (long long i = gt; i < a.n; i += gs) {
 			const double ri = a.r64[i] - nr * a.q64[i];
@@ -516,7 +526,7 @@ __device__ void mixed_body(const MixedParams& a, E64& e64, E32& e32, EDF& edf, G
 			for (long long i = gt; i < a.n; i += gs) a.x[i] -= nr * double(a.inner.x[i]);
 			break;
 		}
-		drift += nr;
+		if (df) drift += nr;
 		rr = rn;
 	}
 	if (grp.rank() == 0 && threadIdx.x == 0) {
