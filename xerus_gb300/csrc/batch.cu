@@ -390,7 +390,9 @@ struct BInstance {
 			}
 			const float bbf = block_sum(bl, sh.redf);
 			float rr = bbf;
-			const float tol2 = 1e-12f * bbf;  // FP32 inner tolerance 1e-6
+			// FP32 inner tolerance 1e-6, or half of the reduction the FP64 target still needs
+			const double itol = fmin(0.5, fmax(1e-6, 0.5 * a.tol * sqrt(bb) / nr));
+			const float tol2 = float(itol * itol) * bbf;
 			int it = 0;
 			while (rr > tol2 && it < maxit) {
 				apply(s, m32, qf);
