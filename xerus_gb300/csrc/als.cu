@@ -418,11 +418,11 @@ __global__ void __launch_bounds__(kGemmThreads, Grp::kCluster ? 1 : 2) k_cg(CgPa
 // error is ~2^-47 ||M|| ||d|| ||r||: relative to the residual it corrects, not to ||b||,
 // so the updated residual follows the true one to FP64 level at a fraction of an FP64
 // operator application. An update whose residual norm would take the summed norms of
-// the double-float updates past half the target's drift budget (times 2^-47, times an
-// allowance of 1024 for ||M|| ||d||) runs in FP64 instead, so from a poor start the
-// first, large correction is exact and the small ones that follow are cheap. Should
-// the updated residual meet the target while the double-float updates could have
-// drifted by more than that, the FP64 residual confirms it.
+// the double-float updates past the drift budget (their sum times 2^-47, times an
+// allowance of 1024 for ||M|| ||d||, at most half the target) runs with FP64 products
+// instead, so from a poor start the first, large correction is exact and the small
+// ones that follow are cheap; the updated residual then stays within half the target
+// of the true one, and meeting the target with it is meeting it.
 struct MixedParams {
 	MatvecPlan<double> p64;
 	CgParams<float> inner;   // inner.b = rhs32, inner.x = d
@@ -474,19 +474,9 @@ __device__ void mixed_body(const MixedParams& a, E64& e64, E32& e32, EDF& edf, G
 	ok = ok && fp64_residual(a, e64, grp, sc, rr);
 	for (int ref = 0; ok; ++ref) {
 		rel = bb > 0 ? sqrt(rr / bb) : 0.0;
-		if (rr <= tol2) {
-			if (!(drift > drift_limit)) {
-				reached = true;
-				break;
-			}
-			// confirm against the FP64 residual; refinement goes on from it if it falls short
-			drift = 0;
-			if (!fp64_residual(a, e64, grp, sc, rr)) break;
-			rel = bb > 0 ? sqrt(rr / bb) : 0.0;
-			if (rr <= tol2) {
-				reached = true;
-				break;
-			}
+		if (rr <= tol2) {  // drift <= drift_limit (the update rule below keeps it there)
+			reached = true;
+			break;
 		}
 		if (ref >= a.max_refine) break;
 		const double nr = sqrt(rr), inr = 1.0 / nr;
