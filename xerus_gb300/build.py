@@ -15,7 +15,8 @@ CSRC = os.path.join(HERE, "csrc")
 OUT = os.path.join(HERE, "_build")
 LIB = os.path.join(OUT, "libxtt.so")
 SOURCES = ["linalg.cu", "ops.cu", "als.cu", "cg_cluster.cu", "batch.cu", "adf.cu", "capi.cu", "noalloc.cu", "fileio.cu", "riemann.cu", "tc_gemm.cu", "tc_tma.cu"]
-HEADERS = ["common.cuh", "gemm.cuh", "linalg.cuh", "engine.cuh", "als.cuh", "local_op.cuh", "blk_qr.cuh", "tc.cuh", "tc_tiles.cuh"]
+HEADERS = ["common.cuh", "gemm.cuh", "linalg.cuh", "engine.cuh", "als.cuh", "local_op.cuh", "blk_qr.cuh", "tc.cuh", "tc_tiles.cuh",
+           "df.cuh"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 FLAGS = ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC", "--expt-relaxed-constexpr"]
 

@@ -16,6 +16,7 @@
 #include <cooperative_groups.h>
 
 #include "als.cuh"
+#include "df.cuh"
 #include "tc_tiles.cuh"
 
 namespace xtt {
@@ -119,50 +120,15 @@ struct CoreTiles {
 	__device__ T tiles(const Gemm<T>& g, Grp& grp) { return gemm_tiles(g, grp.rank(), grp.size(), *sm); }
 };
 
-// Double-float tiles for the refinement's residual updates r -= ||r|| M d: FP64
-// operands split on load into an FP32 pair hi + lo (hi the leading 24 significand
-// bits, lo the next 29 rounded to 24: relative error ~2^-47), each product formed
-// error-free with an FMA (hi*hi + its rounding error + the two cross terms) and
-// summed by TwoSum into an FP32 pair, renormalised every fourth product: ~13 FP32
-// instructions per product, where GB300's FP64 pipe retires one DFMA in the time of
-// ~64 FFMAs. Sums of 384 products come out within ~1e-15 of sum |a b| (mean; FP64:
-// ~2e-16). The intrinsics keep
-// the compiler from contracting the error-free steps into FMAs.
+// Double-float tiles (df.cuh) for the refinement's residual updates r -= ||r|| M d and
+// the mixed sweeps' environment pushes: FP64 operands split on load into FP32 pairs in
+// shared memory, ~13 FP32 instructions per product, where GB300's FP64 pipe retires one
+// DFMA in the time of ~64 FFMAs. Sums of 384 products come out within ~1e-15 of
+// sum |a b| (mean; FP64: ~2e-16).
 struct DfSmem {
 	float2 As[32][33];  // [k][m]: (hi, lo)
 	float2 Bs[32][33];  // [k][n]
 };
-
-__device__ __forceinline__ float2 df_split(double d) {
-	const unsigned long long u = (unsigned long long)__double_as_longlong(d);
-	const int e = int((u >> 52) & 0x7ffu) - 1023;
-	if (e >= -74 && e <= 127) {  // hi and the scale of lo are normal FP32 numbers
-		const unsigned sign = unsigned(u >> 32) & 0x80000000u;
-		const float hi = __uint_as_float(sign | (unsigned(e + 127) << 23) | unsigned((u >> 29) & 0x7fffffu));
-		const float scale = __uint_as_float(sign | (unsigned(e + 75) << 23));  // +-2^(e-52)
-		return make_float2(hi, __fmul_rn(__uint2float_rn(unsigned(u & 0x1fffffffu)), scale));
-	}
-	return make_float2(__double2float_rn(d), 0.f);  // zero, and magnitudes FP32 cannot split
-}
-
-__device__ __forceinline__ void df_fma(float2 a, float2 b, float& s, float& c) {
-	const float p = __fmul_rn(a.x, b.x);
-	float e = __fmaf_rn(a.x, b.x, -p);
-	e = __fmaf_rn(a.x, b.y, e);
-	e = __fmaf_rn(a.y, b.x, e);
-	const float t = __fadd_rn(s, p);
-	const float bp = __fsub_rn(t, s);
-	const float err = __fadd_rn(__fsub_rn(s, __fsub_rn(t, bp)), __fsub_rn(p, bp));
-	s = t;
-	c = __fadd_rn(c, __fadd_rn(err, e));
-}
-
-// s + c -> s + c with |c| <= ulp(s) / 2 (Fast2Sum); keeps the low part's own rounding small
-__device__ __forceinline__ void df_renorm(float& s, float& c) {
-	const float t = __fadd_rn(s, c);
-	c = __fsub_rn(c, __fsub_rn(t, s));
-	s = t;
-}
 
 // Output tile `tile` of g (32 x 32, 2 x 2 outputs per thread, as gemm_tile; no epilogue
 // sum) over the K range [kb, ke) (ke <= 0: all of K).

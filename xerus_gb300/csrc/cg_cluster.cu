@@ -307,7 +307,7 @@ struct CcView {
 };
 
 // FP64 form.
-__global__ void __launch_bounds__(kCcThreads) k_cg_cluster_f64(CcArgs a) {
+__global__ void __launch_bounds__(kCcThreads, 1) k_cg_cluster_f64(CcArgs a) {
 	if (a.gate && __ldcg(a.gate) == 0) return;  // uniform: every CTA reads the same flag
 	extern __shared__ __align__(16) unsigned char smem[];
 	cgx::cluster_group cl = cgx::this_cluster();
@@ -339,7 +339,7 @@ __global__ void __launch_bounds__(kCcThreads) k_cg_cluster_f64(CcArgs a) {
 }
 
 // Mixed form: FP32 CG corrections, FP64 residuals and iterate.
-__global__ void __launch_bounds__(kCcThreads) k_cg_cluster_mixed(CcArgs a) {
+__global__ void __launch_bounds__(kCcThreads, 1) k_cg_cluster_mixed(CcArgs a) {
 	if (a.sticky && __ldcg(a.sticky) != 0) {  // an earlier solve of this sweep showed FP32 does not help
 		if (blockIdx.x == 0 && threadIdx.x == 0) *a.flag = 1;
 		return;
