@@ -145,11 +145,9 @@ __device__ void gemm_tile_df(const Gemm<double>& g, long long tile, DfSmem& sm, 
 	const bool a_k_fast = (g.sAk == 1);
 	const bool b_n_fast = (g.sBn == 1) || (g.sBk != 1);
 	// the next K slab is fetched into registers while the current one is multiplied
-	const int kend = ke > 0 ? min(ke, g.K) : g.K;
-	Gemm<double> gk = g;  // K bounded to the range: the loads zero-fill beyond it
-	gk.K = kend;
+	const int kend = ke > 0 ? min(ke, g.K) : g.K;  // the loads zero-fill beyond it
 	GemmSlab<double> r;
-	gemm_slab_load(gk, A, B, m0, n0, kb, a_k_fast, b_n_fast, r);
+	gemm_slab_load(g, A, B, m0, n0, kb, kend, a_k_fast, b_n_fast, r);
 	for (int k0 = kb; k0 < kend; k0 += 32) {
 #pragma unroll
 		for (int t = 0; t < 4; ++t) {
@@ -159,7 +157,7 @@ __device__ void gemm_tile_df(const Gemm<double>& g, long long tile, DfSmem& sm, 
 			sm.Bs[bk][bn] = df_split(r.b[t]);
 		}
 		__syncthreads();
-		if (k0 + 32 < kend) gemm_slab_load(gk, A, B, m0, n0, k0 + 32, a_k_fast, b_n_fast, r);
+		if (k0 + 32 < kend) gemm_slab_load(g, A, B, m0, n0, k0 + 32, kend, a_k_fast, b_n_fast, r);
 		const int kmax = min(32, kend - k0);
 #pragma unroll 4
 		for (int kk = 0; kk < kmax; ++kk) {
@@ -281,7 +279,7 @@ __device__ bool matvec_dev(const MatvecPlan<T>& plan, const T* in, T* out, const
 }
 
 template <class T, class Grp, class E>
-__device__ CgOut cg_body(const CgParams<T>& a, E& sm, Grp& grp) {
+__device__ CgOut cg_body(const CgParams<T>& a, E& sm, Grp& grp, double tol = -1.0) {  // tol < 0: a.tol
 	__shared__ double sc[32];
 	CgOut out{0, 0, 0.0};
 	const long long gt = grp.rank() * (long long)blockDim.x + threadIdx.x;
@@ -318,7 +316,8 @@ __device__ CgOut cg_body(const CgParams<T>& a, E& sm, Grp& grp) {
 		for (long long i = gt; i < a.n; i += gs) a.x[i] = T(0);
 		return out;
 	}
-	const double tol2 = a.tol * a.tol * bb;
+	const double tl = tol < 0 ? a.tol : tol;
+	const double tol2 = tl * tl * bb;
 	int it = 0;
 	CgFloor floor_check;
 	while (rr > tol2 && it < a.max_iter) {
@@ -450,9 +449,8 @@ __device__ void mixed_body(const MixedParams& a, E64& e64, E32& e32, EDF& edf, G
 		if (!grp.sync()) break;
 		// the correction solve need not reduce its residual below half of what the target
 		// still asks for (fewer FP32 iterations on the last correction)
-		CgParams<float> inner = a.inner;
-		inner.tol = fmin(0.5, fmax(a.inner.tol, 0.5 * a.tol * sqrt(bb) / nr));
-		const CgOut o = cg_body(inner, e32, grp);
+		const double itol = fmin(0.5, fmax(a.inner.tol, 0.5 * a.tol * sqrt(bb) / nr));
+		const CgOut o = cg_body(a.inner, e32, grp, itol);
 		iters += o.iterations;
 		for (long long i = gt; i < a.n; i += gs) {
 			const double di = double(a.inner.x[i]);

@@ -98,16 +98,17 @@ __device__ __forceinline__ void gemm_slab_index(int e, bool kfast_a, bool nfast_
 	bk = nfast_b ? hi : lo;
 }
 
+// (zero beyond row M, column N and K index kend)
 template <class T>
 __device__ __forceinline__ void gemm_slab_load(const Gemm<T>& g, const T* A, const T* B, int m0, int n0, int k0,
-                                               bool a_k_fast, bool b_n_fast, GemmSlab<T>& r) {
+                                               int kend, bool a_k_fast, bool b_n_fast, GemmSlab<T>& r) {
 #pragma unroll
 	for (int t = 0; t < 4; ++t) {
 		int am, ak, bn, bk;
 		gemm_slab_index<T>(threadIdx.x + t * kGemmThreads, a_k_fast, b_n_fast, am, ak, bn, bk);
 		const int gm = m0 + am, gka = k0 + ak, gn = n0 + bn, gkb = k0 + bk;
-		r.a[t] = (gm < g.M && gka < g.K) ? A[g.offA(gm, gka)] : T(0);
-		r.b[t] = (gn < g.N && gkb < g.K) ? B[g.offB(gkb, gn)] : T(0);
+		r.a[t] = (gm < g.M && gka < kend) ? A[g.offA(gm, gka)] : T(0);
+		r.b[t] = (gn < g.N && gkb < kend) ? B[g.offB(gkb, gn)] : T(0);
 	}
 }
 
@@ -129,7 +130,7 @@ __device__ T gemm_tile(const Gemm<T>& g, long long tile, GemmSmem<T>& sm) {
 	const bool a_k_fast = (g.sAk == 1);
 	const bool b_n_fast = (g.sBn == 1) || (g.sBk != 1);
 	GemmSlab<T> r;
-	gemm_slab_load(g, A, B, m0, n0, 0, a_k_fast, b_n_fast, r);
+	gemm_slab_load(g, A, B, m0, n0, 0, g.K, a_k_fast, b_n_fast, r);
 	for (int k0 = 0; k0 < g.K; k0 += 32) {
 #pragma unroll
 		for (int t = 0; t < 4; ++t) {
@@ -139,7 +140,7 @@ __device__ T gemm_tile(const Gemm<T>& g, long long tile, GemmSmem<T>& sm) {
 			sm.Bs[bk][bn] = r.b[t];
 		}
 		__syncthreads();
-		if (k0 + 32 < g.K) gemm_slab_load(g, A, B, m0, n0, k0 + 32, a_k_fast, b_n_fast, r);
+		if (k0 + 32 < g.K) gemm_slab_load(g, A, B, m0, n0, k0 + 32, g.K, a_k_fast, b_n_fast, r);
 		const int kmax = min(32, g.K - k0);
 		for (int kk = 0; kk < kmax; ++kk) {
 			const T a0 = sm.As[kk][ty], a1 = sm.As[kk][ty + 16];
