@@ -783,7 +783,7 @@ def bench_tc_als(xg, ctx, torch, stream, peaks, rank=128, half_sweeps=2, reps=2)
     fl = 3.0 * mv * its
     tf32_peak = 0.5 * peaks.get("bf16_tflops", 1900.0)
     ach = fl / (ms / 1e3) / 1e12 if ms > 0 else 0.0
-    out["classes_ms"] = {k: ctx.profile_get(k)[1] for k in ("cg_tc", "cg_fp64", "gemm", "qr")}
+    out["classes_ms"] = {k: ctx.profile_get(k)[1] for k in ("cg_tc", "cg_fp64", "gemm", "gemm_df", "qr")}
     out["roofline_cg_tc"] = {"kernel": "k_cg_mixed_tc (persistent: tcgen05 kind::tf32 operator stages, FP64 refinement)",
                              "bound": "tensor", "launches": nl, "avg_launch_ms": ms / max(nl, 1),
                              "cg_iterations": its, "algorithmic_flops_per_launch": fl / max(nl, 1), "achieved": ach,

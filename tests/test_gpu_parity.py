@@ -503,8 +503,9 @@ def test_cg_paths_agree(ctx, golden, precision):
 
 def test_als_tensor_core_form_at_rank_64(ctx, golden):
     """Mixed precision at ranks >= 64 takes the tensor-core form by default (FP64
-    refinement of FP32 CG with split-TF32 tcgen05 operator stages): after two
-    half-sweeps from the same start it gives the FP64 form's energy and iterate."""
+    refinement of FP32 CG with split-TF32 tcgen05 operator stages, environment pushes
+    in double-float tiles): after two half-sweeps from the same start it gives the
+    FP64 form's energy and iterate."""
     z = golden("als")
     out = {}
     for prec in (xg.FP64, xg.MIXED):
@@ -518,9 +519,11 @@ def test_als_tensor_core_form_at_rank_64(ctx, golden):
         ctx.profile(True)
         e = v(A, x, b, 2)
         ctx.profile(False)
-        out[prec] = (e, x, xg.residual(A, x, b), ctx.profile_get("cg_tc")[0])
+        out[prec] = (e, x, xg.residual(A, x, b), ctx.profile_get("cg_tc")[0], ctx.profile_get("gemm_df")[0])
     assert max(x.ranks()) == 64
     assert out[xg.MIXED][3] > 0 and out[xg.FP64][3] == 0  # the tensor-core form ran (mixed only)
+    # the mixed form's environment pushes ran in double-float tiles; the FP64 form's did not
+    assert out[xg.MIXED][4] > 0 and out[xg.FP64][4] == 0
     assert abs(out[xg.MIXED][0] / out[xg.FP64][0] - 1) < 1e-10
     xm, xd = out[xg.MIXED][1], out[xg.FP64][1]
     assert (xm - xd).frob_norm() / xd.frob_norm() < 1e-8

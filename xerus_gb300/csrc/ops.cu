@@ -338,8 +338,9 @@ void gemm(Context& c, const Gemm<double>& g) {
 	}
 	check_gemm(g);
 	const double mn = double(g.batch) * g.M * g.N, mk = double(g.M) * g.K, kn = double(g.K) * g.N;
-	ProfScope ps(c, "gemm", 8.0 * (double(g.batch) * (mk + kn) + mn), 2.0 * mn * g.K);
-	if (c.df_gemm && !g.D && 2.0 * mn * g.K >= kDfGemmMinFlops) {
+	const bool df = c.df_gemm && !g.D && 2.0 * mn * g.K >= kDfGemmMinFlops;
+	ProfScope ps(c, df ? "gemm_df" : "gemm", 8.0 * (double(g.batch) * (mk + kn) + mn), 2.0 * mn * g.K);
+	if (df) {
 		gemm_df(c, g);
 		return;
 	}
