@@ -196,6 +196,7 @@ enum ScratchId : int {
 	S_SVD_PC_Q, S_SVD_PC_C, S_SVD_PC_UV, S_SVD_PC_QRW, S_GEMM_TC_WORK, S_SVD_PC_CT, S_SVD_PC_UT,
 	S_SVD_MX_W32, S_SVD_MX_W, S_SVD_MX_W2, S_SVD_MX_G, S_SVD_MX_B0, S_TMA_A, S_TMA_B, S_SVD_RF_U, S_SVD_RF_V,
 	S_SVD_RF_M, S_GQ_FIRST,  // 2 x kGqSlots ids from here: the Gram QR's buffers for two concurrent factorisations
+	S_RES_MEET = 60,         // the residual's two-core meeting products
 	S_QB = 61,               // the blocked Q formation's reflectors and products
 	S_ALS_FIRST = 64,
 	S_ADF_FIRST = 128,

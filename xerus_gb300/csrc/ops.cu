@@ -719,7 +719,8 @@ static void gram_qr(Context& c, const QrArgs& a, int slot, int* flag) {
 // leaves unchanged). The reflectors and R are those of the unblocked factorisation up to
 // rounding (the same dlarfg vectors, in the same order).
 constexpr int kQbBlock = 32;
-static_assert(S_GQ_FIRST + 2 * kGqSlots <= S_QB, "scratch ids of the Gram QR and the blocked QR overlap");
+static_assert(S_GQ_FIRST + 2 * kGqSlots <= S_RES_MEET && S_RES_MEET < S_QB,
+              "scratch ids of the Gram QR, the residual and the blocked QR overlap");
 
 // T_p of one panel from its Gram G = V_p^T V_p (jb x jb) and tau: thread r owns row r.
 __global__ void k_wy_t(const double* __restrict__ G, const double* __restrict__ tau, double* __restrict__ T, int jb) {
@@ -1655,9 +1656,12 @@ double residual(const Tensor* Ap, const Tensor& x, const Tensor& b) {
 	// als.cpp:301) without cancellation. The block
 	// cores Y_k of y = A x - b (TT sum, src/xerus/ttNetwork.cpp:796-856) are formed one at a time
 	// and orthogonalised from both ends at once: cores 0..mid-1 left to right on the context's
-	// stream (Householder QR, only the triangular factor R is carried), cores d-1..mid+1 right to
-	// left on the aux stream (LQ, only the factor L is carried). The two halves meet at core mid:
-	// ||y|| = ||R Y_mid L||. Neither the residual TT nor any orthogonal factor is stored.
+	// stream (Householder QR, only the triangular factor R is carried), cores d-1..mid+2 right to
+	// left on the aux stream (LQ, only the factor L is carried). The two halves meet over the two
+	// cores mid, mid+1 (mid = (d-2)/2, so the two chains are equally long and the widest
+	// factorisation, the one a single meeting core would leave to one side, is not needed):
+	// ||y|| = ||R Y_mid Y_mid+1 L||, three GEMMs. Neither the residual TT nor any orthogonal
+	// factor is stored.
 	XTT_REQUIRE(x.dims == b.dims && !x.op && !b.op && (!Ap || (Ap->dims == x.dims && Ap->op)),
 	            "x and b dimensions differ");
 	Context& c = *x.ctx;
@@ -1715,7 +1719,8 @@ double residual(const Tensor* Ap, const Tensor& x, const Tensor& b) {
 		launch_qr(a, c.stream);
 		c.count_launch();
 	};
-	const int mid = d / 2;
+	const int mid = d >= 2 ? (d - 2) / 2 : 0;
+	const int right_end = d >= 2 ? mid + 1 : mid;  // the right chain stops above this core
 	// right half on the aux stream: carry L (O1_k x rl), starting from [1]
 	int64_t rl = 1;
 	double* Lc = rb_.R;
@@ -1723,7 +1728,7 @@ double residual(const Tensor* Ap, const Tensor& x, const Tensor& b) {
 	{
 		OnAux on(c);
 		fill(c, Lc, 1.0, 1);
-		for (int k = d - 1; k > mid; --k) {
+		for (int k = d - 1; k > right_end; --k) {
 			const Dims dm = block(k, rb_);
 			Gemm<double> g;  // Z = Y_k ((O0 n) x O1) * L (O1 x rl)
 			g.M = dm.O0 * dm.n; g.N = int(rl); g.K = dm.O1;
@@ -1758,24 +1763,49 @@ double residual(const Tensor* Ap, const Tensor& x, const Tensor& b) {
 		rr = kq;
 	}
 	c.join();  // the meeting reads the right half's carry L
-	// meet at core mid: W = (R Y_mid) L, ||y|| = ||W||
 	const Dims dm = block(mid, lb);
-	Gemm<double> g1;  // Z = R (rr x O0) * Y (O0 x n O1)
+	Gemm<double> g1;  // Z = R (rr x O0) * Y_mid (O0 x n O1)
 	g1.M = int(rr); g1.N = dm.n * dm.O1; g1.K = dm.O0;
 	g1.A = lb.R; g1.sAm = dm.O0; g1.sAk = 1;
 	g1.B = lb.Y; g1.sBk = dm.n * dm.O1; g1.sBn = 1;
 	g1.C = lb.Z; g1.sCm = dm.n * dm.O1; g1.sCn = 1;
 	g1.lens((long long)cap_r, (long long)cap_core, (long long)2 * cap_core);
 	gemm(c, g1);
-	Gemm<double> g2;  // W = Z ((rr n) x O1) * L (O1 x rl)
-	g2.M = int(rr * dm.n); g2.N = int(rl); g2.K = dm.O1;
+	if (d == 1) {
+		// one core: W = Z L, ||y|| = ||W||
+		Gemm<double> g2;  // W = Z ((rr n) x O1) * L (O1 x rl)
+		g2.M = int(rr * dm.n); g2.N = int(rl); g2.K = dm.O1;
+		g2.A = lb.Z; g2.sAm = dm.O1; g2.sAk = 1;
+		g2.B = Lc; g2.sBk = rl; g2.sBn = 1;
+		g2.C = lb.ax; g2.sCm = rl; g2.sCn = 1;
+		g2.lens((long long)2 * cap_core, (long long)cap_r, (long long)cap_core);
+		XTT_REQUIRE(size_t(rr) * dm.n * rl <= cap_core, "internal: residual meeting block too small");
+		gemm(c, g2);
+		sumsq_async(c, lb.ax, size_t(rr) * dm.n * rl, 0);
+		return std::sqrt(read_dbl(c, 0)) / nb;
+	}
+	// two cores: W = ((R Y_mid) Y_mid+1) L, ||y|| = ||W|| (the right chain's buffers are free:
+	// the join above ordered its work before this)
+	const Dims dn = block(mid + 1, rb_);
+	XTT_REQUIRE(dn.O0 == dm.O1, "internal: residual meeting ranks differ");
+	const size_t rows2 = size_t(rr) * dm.n * dn.n;  // (a, i_mid, i_mid+1)
+	double* Z2 = c.scratch<double>(S_RES_MEET, rows2 * size_t(dn.O1 + rl));
+	double* W = Z2 + rows2 * dn.O1;
+	Gemm<double> g2;  // Z2 = Z ((rr n) x O1) * Y_mid+1 (O1 x n' O2)
+	g2.M = int(rr * dm.n); g2.N = dn.n * dn.O1; g2.K = dm.O1;
 	g2.A = lb.Z; g2.sAm = dm.O1; g2.sAk = 1;
-	g2.B = Lc; g2.sBk = rl; g2.sBn = 1;
-	g2.C = lb.ax; g2.sCm = rl; g2.sCn = 1;
-	g2.lens((long long)2 * cap_core, (long long)cap_r, (long long)cap_core);
-	XTT_REQUIRE(size_t(rr) * dm.n * rl <= cap_core, "internal: residual meeting block too small");
+	g2.B = rb_.Y; g2.sBk = dn.n * dn.O1; g2.sBn = 1;
+	g2.C = Z2; g2.sCm = dn.n * dn.O1; g2.sCn = 1;
+	g2.lens((long long)2 * cap_core, (long long)cap_core, (long long)(rows2 * dn.O1));
 	gemm(c, g2);
-	sumsq_async(c, lb.ax, size_t(rr) * dm.n * rl, 0);
+	Gemm<double> g3;  // W = Z2 ((rr n n') x O2) * L (O2 x rl)
+	g3.M = int(rows2); g3.N = int(rl); g3.K = dn.O1;
+	g3.A = Z2; g3.sAm = dn.O1; g3.sAk = 1;
+	g3.B = Lc; g3.sBk = rl; g3.sBn = 1;
+	g3.C = W; g3.sCm = rl; g3.sCn = 1;
+	g3.lens((long long)(rows2 * dn.O1), (long long)cap_r, (long long)(rows2 * rl));
+	gemm(c, g3);
+	sumsq_async(c, W, rows2 * size_t(rl), 0);
 	return std::sqrt(read_dbl(c, 0)) / nb;
 }
 
