@@ -1651,6 +1651,9 @@ void tt_add(Tensor& x, const Tensor& y, double f) {
 
 double residual(const Tensor& A, const Tensor& x, const Tensor& b) { return residual(&A, x, b); }
 
+// The residual's two-core meeting (below) where its GEMMs stay under this many flops.
+constexpr double kResMeetMaxFlops = 2e8;
+
 double residual(const Tensor* Ap, const Tensor& x, const Tensor& b) {
 	// ||A x - b|| / ||b|| (src/xerus/algorithms/als.cpp:258-261; A null: ||x - b|| / ||b||,
 	// als.cpp:301) without cancellation. The block
@@ -1660,8 +1663,9 @@ double residual(const Tensor* Ap, const Tensor& x, const Tensor& b) {
 	// left on the aux stream (LQ, only the factor L is carried). The two halves meet over the two
 	// cores mid, mid+1 (mid = (d-2)/2, so the two chains are equally long and the widest
 	// factorisation, the one a single meeting core would leave to one side, is not needed):
-	// ||y|| = ||R Y_mid Y_mid+1 L||, three GEMMs. Neither the residual TT nor any orthogonal
-	// factor is stored.
+	// ||y|| = ||R Y_mid Y_mid+1 L||, three GEMMs; where that product would cost more than
+	// kResMeetMaxFlops (large ranks), they meet over core d/2 alone: ||y|| = ||R Y_mid L||.
+	// Neither the residual TT nor any orthogonal factor is stored.
 	XTT_REQUIRE(x.dims == b.dims && !x.op && !b.op && (!Ap || (Ap->dims == x.dims && Ap->op)),
 	            "x and b dimensions differ");
 	Context& c = *x.ctx;
@@ -1719,8 +1723,20 @@ double residual(const Tensor* Ap, const Tensor& x, const Tensor& b) {
 		launch_qr(a, c.stream);
 		c.count_launch();
 	};
-	const int mid = d >= 2 ? (d - 2) / 2 : 0;
-	const int right_end = d >= 2 ? mid + 1 : mid;  // the right chain stops above this core
+	// the meeting: two cores when their product is cheap (the left carry's rows at mid follow
+	// rr <- min(rr n_k, O_k+1) along the chain)
+	auto bond = [&](int k) -> int64_t { return k == 0 || k == d ? 1 : opr(k) * x.ranks[k] + b.ranks[k]; };
+	bool two = false;
+	if (d >= 2) {
+		const int m2 = (d - 2) / 2;
+		int64_t rows = 1;
+		for (int k = 0; k < m2; ++k) rows = std::min<int64_t>(rows * x.dims[k], bond(k + 1));
+		const double flops = 2.0 * double(rows * x.dims[m2]) * double(bond(m2 + 1)) *
+		                     double(x.dims[m2 + 1] * bond(m2 + 2));
+		two = flops <= kResMeetMaxFlops;
+	}
+	const int mid = two ? (d - 2) / 2 : d / 2;
+	const int right_end = two ? mid + 1 : mid;  // the right chain stops above this core
 	// right half on the aux stream: carry L (O1_k x rl), starting from [1]
 	int64_t rl = 1;
 	double* Lc = rb_.R;
@@ -1771,7 +1787,7 @@ double residual(const Tensor* Ap, const Tensor& x, const Tensor& b) {
 	g1.C = lb.Z; g1.sCm = dm.n * dm.O1; g1.sCn = 1;
 	g1.lens((long long)cap_r, (long long)cap_core, (long long)2 * cap_core);
 	gemm(c, g1);
-	if (d == 1) {
+	if (!two) {
 		// one core: W = Z L, ||y|| = ||W||
 		Gemm<double> g2;  // W = Z ((rr n) x O1) * L (O1 x rl)
 		g2.M = int(rr * dm.n); g2.N = int(rl); g2.K = dm.O1;
