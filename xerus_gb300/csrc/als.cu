@@ -252,7 +252,8 @@ void gemm_df(Context& c, const Gemm<double>& g) {
 	const int kchunk = ((g.K + S - 1) / S + 31) / 32 * 32;
 	S = (g.K + kchunk - 1) / kchunk;
 	const long long span = g.max_off_C() + 1;
-	double* part = c.scratch<double>(S_ALS_FIRST + 12, size_t(S) * size_t(span));
+	// a buffer per stream: the sweeps' operator and rhs pushes run on the two streams at once
+	double* part = c.scratch<double>(c.stream == c.aux ? S_ALS_FIRST + 13 : S_ALS_FIRST + 12, size_t(S) * size_t(span));
 	k_gemm_df_split<<<unsigned(nt * S), kGemmThreads, 0, c.stream>>>(g, kchunk, part, span);
 	const long long total = (long long)g.batch * g.M * g.N;
 	k_gemm_df_sum<<<unsigned(std::min<long long>((total + 255) / 256, 8LL * c.num_sms)), 256, 0, c.stream>>>(g, S, part,
