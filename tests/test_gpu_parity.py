@@ -569,6 +569,25 @@ def test_als_mixed_precision_matches_fp64(ctx, golden):
     assert xg.residual(A, x, b) < 1e-10
 
 
+@pytest.mark.parametrize("d,n,rank,scale", [(1, 3, 1, 1.0), (2, 3, 2, 1.0), (3, 3, 2, 1.0), (4, 3, 2, 1.0),
+                                             (5, 3, 2, 1e-8), (8, 4, 8, 1e-8), (4, 8, 230, 1.0)])
+def test_residual_small_orders_and_meetings(ctx, d, n, rank, scale):
+    """The FP64 residual's two orthogonalisation chains meet over two cores, or over one
+    where the meeting's product would be large (the rank-230 case): orders 1 to 8
+    against the oracle, including residuals of ~1e-8 relative (b = A x + 1e-8 r),
+    where a cancellation would show."""
+    rng = np.random.default_rng(1000 * d + rank)
+    A = o.laplace_operator(d, n)
+    xr = [1] + [rank] * (d - 1) + [1]
+    x = o.TT([rng.standard_normal((xr[k], n, xr[k + 1])) / np.sqrt(n * xr[k]) for k in range(d)])
+    rr = [1] + [2] * (d - 1) + [1]
+    r = o.TT([rng.standard_normal((rr[k], n, rr[k + 1])) for k in range(d)])
+    b = r if scale == 1.0 else o.tt_add(o.op_apply(A, x), o.tt_scale(r, scale))
+    want = o.residual(A, x, b)
+    got = xg.residual(dev_op(ctx, A), dev_tt(ctx, x), dev_tt(ctx, b))
+    assert abs(got / want - 1) < (1e-9 if scale == 1.0 else 1e-5), (got, want)
+
+
 def test_dmrg_spd(ctx, golden):
     """The reference's decreasing half-sweep contracts core k (not k+1) into the
     right environment (als.cpp:371), so after the first half-sweep its result
