@@ -40,7 +40,9 @@ typedef enum xtt_status {
 
 typedef enum xtt_precision {
 	XTT_PRECISION_FP64 = 0,      /* plain form: FP64 everywhere */
-	XTT_PRECISION_MIXED = 1      /* local solves in FP32 with FP64 iterative refinement */
+	XTT_PRECISION_MIXED = 1      /* local solves in FP32 with FP64 iterative refinement (residual
+	                                updates and the sweeps' large environment pushes in
+	                                double-float, ~1e-15 relative) */
 } xtt_precision;
 
 typedef struct xtt_context xtt_context;
@@ -61,7 +63,8 @@ int xtt_context_kernel_launches(xtt_context* ctx, int64_t* count);
 /* Per-kernel-class timing with CUDA events on the context's stream (the analogue
  * of xerus's XERUS_PA_START/END accumulators, include/xerus/misc/performanceAnalysis.h:30-39).
  * enable = 1 starts (and clears) it, 0 stops it. Classes: "cg_fp64", "cg_mixed",
- * "gemm", "qr", "svd", "adf_res_grad", "adf_slicenorm", "adf_stack". */
+ * "cg_tc", "gemm", "gemm_df" (double-float GEMMs of the mixed sweeps), "gemm_tc", "qr",
+ * "qr_gram", "svd", "adf_res_grad", "adf_slicenorm", "adf_stack". */
 int xtt_context_profile(xtt_context* ctx, int enable);
 /* Launch count and total milliseconds of one class since profiling started (0 if none). */
 int xtt_context_profile_get(xtt_context* ctx, const char* name, int64_t* launches, double* milliseconds);
@@ -111,9 +114,9 @@ int xtt_context_set_contraction_precision(xtt_context* ctx, int terms);
  * dimensions lda, ldb, ldc; terms = 3 splits each operand into two TF32 pieces
  * (FP32-level products), 6 into three BF16 pieces (FP32-level products on the
  * 16-bit MMA path), 1 is plain TF32; terms = 2 runs the CUDA-core double-float
- * tiles of the mixed local solves' residual updates instead (each FP64 operand as
- * an FP32 pair, error-free FMA products, TwoSum accumulation: ~1e-15 of
- * sum |a b|). The building block of the precision forms
+ * tiles of the mixed local solves' residual updates and environment pushes instead
+ * (each FP64 operand as an FP32 pair, error-free FMA products, TwoSum accumulation:
+ * ~1e-15 of sum |a b|; K split across CTAs when the tiles leave SMs idle). The building block of the precision forms
  * (no reference counterpart: the reference multiplies in FP64 through BLAS,
  * src/xerus/blasLapackWrapper.cpp:96-147); exposed to check it against an FP64
  * product. Asynchronous on the context's stream. */
